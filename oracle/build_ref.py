@@ -1,0 +1,92 @@
+"""Builds the reference `c` backend programs used to pin the oracle.
+
+Test infrastructure, run only where the reference tree is present.  For each
+case below it
+  1. builds the OpenABL compiler from the reference sources (see
+     openabl_gb300/backend/Makefile),
+  2. runs `openabl -b c` on the reference example with the case's -P/-C
+     values, producing the reference's own main.c (src/backend/CBackend.cpp),
+  3. inserts one call `abl_ref_dump(&agents, agents_info);` after the
+     `dyn_array tmp;` line that opens every timestep
+     (src/backend/CPrinter.cpp:191-194) and compiles main.c with the
+     reference's build line (CBackend.cpp:21-27) plus `-Dsave=abl_ref_save`,
+     the reference's asset/c/libabl.c and oracle/ref_harness.c,
+  4. leaves the program in oracle/_ref/<case>/main (git-ignored).
+"""
+import os
+import subprocess
+import sys
+
+REF = os.environ.get("OPENABL_REF", "/root/reference")
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+OUT = os.path.join(HERE, "_ref")
+COMPILER = os.path.join(REPO, "_build", "compiler", "openabl")
+
+# name -> (example, -P params, -C config)
+CASES = {
+    "circle_4000": ("circle", {"num_agents": "4000", "rho": "0.1", "num_timesteps": "100"}, {}),
+    "circle3d_4000": ("circle3d", {"num_agents": "4000", "rho": "0.01", "num_timesteps": "50"}, {}),
+    "boids2d_4096": ("boids2d", {"num_agents": "4096", "agent_density": "3200.0",
+                                 "num_timesteps": "100"}, {}),
+    "game_of_life_64": ("game_of_life", {"num_agents": "4096", "alive_fraction": "0.5",
+                                         "num_timesteps": "100"}, {}),
+    "boids2d_4096_float": ("boids2d", {"num_agents": "4096", "agent_density": "3200.0",
+                                       "num_timesteps": "100"}, {"use_float": "true"}),
+}
+
+
+def build_compiler():
+    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "openabl_gb300", "backend"),
+                           "-j8", f"REF={REF}"])
+
+
+def build_case(name):
+    example, params, config = CASES[name]
+    d = os.path.join(OUT, name)
+    os.makedirs(d, exist_ok=True)
+    cmd = [COMPILER, "-A", os.path.join(REF, "asset"), "-i",
+           os.path.join(REF, "examples", example + ".abl"), "-o", d, "-b", "c"]
+    for k, v in params.items():
+        cmd += ["-P", f"{k}={v}"]
+    for k, v in config.items():
+        cmd += ["-C", f"{k}={v}"]
+    subprocess.check_call(cmd)
+    src = open(os.path.join(d, "main.c")).read()
+    marker = "dyn_array tmp;"
+    assert src.count(marker) == 1, "unexpected simulate loop shape"
+    src = src.replace(marker, marker + " abl_ref_dump(&agents, agents_info);")
+    src = src.replace('#include "libabl.h"',
+                      '#include "libabl.h"\nvoid abl_ref_dump(void *, const agent_info *);', 1)
+    with open(os.path.join(d, "main_dump.c"), "w") as f:
+        f.write(src)
+    use_float = config.get("use_float") == "true"
+    fl = ["-DLIBABL_USE_FLOAT=1"] if use_float else []
+    asset_c = os.path.join(REF, "asset", "c")
+    # Reference build line: gcc -O2 -std=c99 [-DLIBABL_USE_FLOAT=1] main.c libabl.c -lm -fopenmp
+    subprocess.check_call(["gcc", "-O2", "-std=c99", *fl, "-Dsave=abl_ref_save", "-I", asset_c,
+                           "-c", os.path.join(d, "main_dump.c"), "-o", os.path.join(d, "main.o"),
+                           "-fopenmp"])
+    subprocess.check_call(["gcc", "-O2", "-std=c99", *fl, "-I", asset_c, "-c",
+                           os.path.join(asset_c, "libabl.c"), "-o", os.path.join(d, "libabl.o")])
+    subprocess.check_call(["gcc", "-O2", "-std=c99", *fl, "-I", asset_c, "-c",
+                           os.path.join(HERE, "ref_harness.c"), "-o", os.path.join(d, "harness.o")])
+    subprocess.check_call(["gcc", os.path.join(d, "main.o"), os.path.join(d, "libabl.o"),
+                           os.path.join(d, "harness.o"), "-lm", "-fopenmp", "-o",
+                           os.path.join(d, "main")])
+    return os.path.join(d, "main")
+
+
+def main(argv):
+    if not os.path.isdir(REF):
+        print("reference tree not present; nothing to build")
+        return 0
+    build_compiler()
+    names = argv[1:] or list(CASES)
+    for n in names:
+        print("built", build_case(n))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv))
