@@ -1,0 +1,115 @@
+/* OpenABL CUDA runtime — C ABI (GB300, sm_103a).
+ *
+ * This is the device runtime behind the `-b cuda` backend.  The reference
+ * `c` backend keeps the agent population in host arrays and runs every step
+ * function in-process (src/backend/CPrinter.cpp:189-233; runtime
+ * asset/c/libabl.{h,c}).  With `-b cuda` the generated program keeps host
+ * initialisation and save() unchanged and hands the population to this
+ * runtime, which owns all device memory and one CUDA stream per context:
+ *
+ *   abl_create    -> allocation of the agent arrays (CPrinter.cpp:278-293,
+ *                    `struct agent_struct` with agents_X / agents_X_dbuf)
+ *   abl_upload    -> the state built by main() before `simulate`
+ *   abl_step/run  -> one / T iterations of the simulate loop
+ *                    (CPrinter.cpp:189-233: per step function, double buffer
+ *                    copy on first use, parallel loop, swap)
+ *   abl_download  -> the state read by save() after `simulate`
+ *                    (CPrinter.cpp:74-76, asset/c/libabl.c:215-231)
+ *   abl_reduce    -> the sequential-step reductions count()/sum()
+ *                    (builtins at src/main.cpp:65-130, lowered for FlameGPU
+ *                    at src/backend/FlameGPUBackend.cpp:204-225)
+ *   abl_last_exec_time -> getLastExecTime() (src/main.cpp:66)
+ *
+ * Conventions: every call returns 0 or a negative ABL_E_* code (text via
+ * abl_strerror); host buffers belong to the caller, device buffers to the
+ * context; one host thread per context; contexts on separate streams may run
+ * concurrently.  Agent state crosses the boundary as structure-of-arrays: one
+ * column per member, members in declaration order, each column holding n
+ * values of the member's type (bool = 1 byte, int = int32, float = double or
+ * float under use_float, float2/float3 = 2/3 consecutive floats).
+ */
+#ifndef OPENABL_CUDA_H
+#define OPENABL_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ABL_OK 0
+#define ABL_E_INVALID -1     /* bad argument */
+#define ABL_E_BUDGET -2      /* the HBM budget given to abl_create is exhausted */
+#define ABL_E_CUDA -3        /* a CUDA runtime call failed */
+#define ABL_E_TIMEOUT -4     /* a bounded device-side wait ran out */
+#define ABL_E_NONFINITE -5   /* an agent position is NaN or infinite */
+#define ABL_E_UNSUPPORTED -6 /* model feature not implemented by this runtime */
+#define ABL_E_CAPACITY -7    /* agent capacity exceeded by runtime additions */
+#define ABL_E_NOMODEL -8     /* unknown model name */
+
+/* Member value types (match asset/c/libabl.h:181-189 type_id). */
+#define ABL_T_BOOL 1
+#define ABL_T_INT 2
+#define ABL_T_FLOAT 3
+#define ABL_T_FLOAT2 5
+#define ABL_T_FLOAT3 6
+
+typedef struct abl_ctx abl_ctx;
+typedef struct abl_model_desc abl_model_desc;
+
+/* ---- model lookup (models compiled into this library by `-b cuda`) ---- */
+
+/* Returns the descriptor of a built-in model (e.g. "boids2d"), or NULL. */
+const abl_model_desc *abl_model_lookup(const char *name);
+/* Number of agent types / their names / members (for generic hosts). */
+int abl_model_num_agent_types(const abl_model_desc *m);
+const char *abl_model_agent_name(const abl_model_desc *m, int type_id);
+int abl_model_num_members(const abl_model_desc *m, int type_id);
+int abl_model_member(const abl_model_desc *m, int type_id, int member, const char **name,
+                     int *value_type);
+/* Size of the model's globals block (its `param`/constant declarations). */
+size_t abl_model_globals_size(const abl_model_desc *m);
+/* Writes the compile-time values of the globals (the constants printed by
+ * the code generator) into `out` (abl_model_globals_size bytes). */
+int abl_model_globals_default(const abl_model_desc *m, void *out);
+/* Offset and type of a named global inside the globals block. */
+int abl_model_global(const abl_model_desc *m, const char *name, size_t *offset, int *value_type);
+
+/* ---- context lifecycle ---- */
+
+/* Creates a context for `model` with the default globals.  `hbm_budget`
+ * bounds the device memory the context may allocate (0 = unbounded). */
+int abl_create(const abl_model_desc *model, size_t hbm_budget, abl_ctx **out);
+/* Replaces the globals block (must precede abl_upload). */
+int abl_set_globals(abl_ctx *ctx, const void *globals, size_t size);
+/* Uploads `n` agents of `type_id` from host SoA columns (see above). */
+int abl_upload(abl_ctx *ctx, int type_id, const void *const *cols, size_t n);
+/* Runs one / `timesteps` iterations of the simulate loop. */
+int abl_step(abl_ctx *ctx);
+int abl_run(abl_ctx *ctx, int timesteps);
+/* Number of live agents of a type. */
+int abl_count(abl_ctx *ctx, int type_id, size_t *n);
+/* Copies the agents of `type_id` into host SoA columns of capacity *n;
+ * sets *n to the number of agents. */
+int abl_download(abl_ctx *ctx, int type_id, void *const *cols, size_t *n);
+/* Sequential-step reductions: kind 0 = count(Type), 1 = sum(Type.member). */
+int abl_reduce(abl_ctx *ctx, int kind, int type_id, int member, void *out);
+/* Wall time of the last abl_step/abl_run call, in seconds (device events). */
+int abl_last_exec_time(abl_ctx *ctx, double *seconds);
+/* Device memory currently held by the context, in bytes. */
+int abl_memory_used(abl_ctx *ctx, size_t *bytes);
+/* Number of kernel launches issued by the last abl_step/abl_run call. */
+int abl_last_launch_count(abl_ctx *ctx, long *launches);
+/* Per-step-function kernel timing with device events (for profiling; eager
+ * timesteps only, so abl_run does not replay graphs while it is on). */
+int abl_set_profiling(abl_ctx *ctx, int enable);
+int abl_step_kernel_time(abl_ctx *ctx, int step, double *seconds, long *launches);
+int abl_destroy(abl_ctx *ctx);
+const char *abl_strerror(int code);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPENABL_CUDA_H */

@@ -1,9 +1,107 @@
+// `-b cuda`: writes <model>.cu (kernels, model descriptor and the host
+// main()), the device runtime, build.sh and run.sh into the output directory,
+// the same layout the `c` backend produces (src/backend/CBackend.cpp:29-45).
+//
+// Configuration (-C name=value):
+//   use_float=true   abl_float is float (as LIBABL_USE_FLOAT for `c`)
+//   cuda.model=NAME  identifier of the model inside the runtime (default "model")
 #include "CudaBackend.hpp"
+
+#include <cctype>
+#include <sstream>
+
+#include "CudaPrinter.hpp"
+#include "FileUtil.hpp"
+
+#ifndef ABL_CUDA_RUNTIME_DIR
+#define ABL_CUDA_RUNTIME_DIR ""
+#endif
+#ifndef ABL_CUDA_INCLUDE_DIR
+#define ABL_CUDA_INCLUDE_DIR ""
+#endif
 
 namespace OpenABL {
 
-void CudaBackend::generate(AST::Script &, const BackendContext &) {
-  throw BackendError("The cuda backend is not implemented yet");
+static const char *kRuntimeFiles[] = {
+  "abl_runtime.cu", "abl_host.cpp", "abl_host.h", "abl_model.h", "abl_device.cuh",
+  "abl_math.cuh", "abl_gen.cuh",
+};
+
+static std::string runtimeDir(const BackendContext &ctx) {
+  // The runtime ships as asset/cuda in an OpenABL tree; a build of this
+  // plugin outside such a tree points at its own copy.
+  std::string assetCuda = ctx.assetDir + "/cuda";
+  if (fileExists(assetCuda + "/abl_runtime.cu")) return assetCuda;
+  return ABL_CUDA_RUNTIME_DIR;
 }
 
+// The folded globals as the printers emit them (literals printed with the
+// stream's default six significant digits, src/backend/GenericPrinter.cpp:39-58),
+// so that hosts driving the runtime directly can reproduce a configuration.
+static std::string literalText(const AST::Expression &e) {
+  std::ostringstream s;
+  if (auto *f = dynamic_cast<const AST::FloatLiteral *>(&e)) {
+    s << f->value;
+  } else if (auto *i = dynamic_cast<const AST::IntLiteral *>(&e)) {
+    s << i->value;
+  } else if (auto *b = dynamic_cast<const AST::BoolLiteral *>(&e)) {
+    s << (b->value ? "true" : "false");
+  } else if (auto *c = dynamic_cast<const AST::CallExpression *>(&e)) {
+    s << "[";
+    for (size_t k = 0; k < c->args->size(); k++) {
+      s << (k ? ", " : "") << literalText(*(*c->args)[k]);
+    }
+    s << "]";
+  } else {
+    s << "null";
+  }
+  return s.str();
 }
+
+static std::string globalsManifest(const AST::Script &script, const std::string &model) {
+  std::ostringstream s;
+  s << "{\"model\": \"" << model << "\", \"globals\": {";
+  bool first = true;
+  for (const AST::ConstDeclaration *decl : script.consts) {
+    if (decl->isArray) continue;
+    s << (first ? "" : ", ") << "\"" << decl->var->name << "\": " << literalText(*decl->expr);
+    first = false;
+  }
+  s << "}}\n";
+  return s.str();
+}
+
+void CudaBackend::generate(AST::Script &script, const BackendContext &ctx) {
+  bool useFloat = ctx.config.getBool("use_float", false);
+  std::string model = "model";
+  auto it = ctx.config.config.find("cuda.model");
+  if (it != ctx.config.config.end()) model = it->second;
+  for (char ch : model) {
+    if (!(std::isalnum((unsigned char) ch) || ch == '_')) {
+      throw BackendError("cuda.model must be an identifier");
+    }
+  }
+
+  CudaPrinter printer(script, useFloat, model);
+  printer.print(script);
+  writeToFile(ctx.outputDir + "/" + model + ".cu", printer.extractStr());
+  writeToFile(ctx.outputDir + "/" + model + ".globals.json", globalsManifest(script, model));
+
+  std::string rt = runtimeDir(ctx);
+  for (const char *f : kRuntimeFiles) {
+    std::string src = rt + "/" + f;
+    if (!fileExists(src)) throw std::runtime_error("cuda runtime file missing: " + src);
+    copyFile(src, ctx.outputDir + "/" + f);
+  }
+  std::string header = fileExists(rt + "/openabl_cuda.h")
+      ? rt + "/openabl_cuda.h" : std::string(ABL_CUDA_INCLUDE_DIR) + "/openabl_cuda.h";
+  copyFile(header, ctx.outputDir + "/openabl_cuda.h");
+  writeToFile(ctx.outputDir + "/build.sh",
+              "nvcc -gencode arch=compute_103a,code=sm_103a -O3 -fmad=false -std=c++17 -diag-suppress 177 "
+              "-DABL_STANDALONE_MAIN -I. " + model + ".cu abl_runtime.cu abl_host.cpp -o main\n");
+  writeToFile(ctx.outputDir + "/run.sh", "./main\n");
+  makeFileExecutable(ctx.outputDir + "/build.sh");
+  makeFileExecutable(ctx.outputDir + "/run.sh");
+}
+
+}  // namespace OpenABL

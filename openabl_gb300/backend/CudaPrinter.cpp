@@ -1,1 +1,699 @@
-// placeholder
+#include "CudaPrinter.hpp"
+
+#include <functional>
+#include <map>
+#include <sstream>
+
+#include "ASTVisitor.hpp"
+#include "backend/Backend.hpp"
+
+namespace OpenABL {
+
+namespace {
+
+// Root variable of an assignment target (`x`, `x.m`, `x.m.c`, `x[i]`).
+const AST::VarExpression *targetRoot(const AST::Expression &e) {
+  if (auto *v = dynamic_cast<const AST::VarExpression *>(&e)) return v;
+  if (auto *m = dynamic_cast<const AST::MemberAccessExpression *>(&e)) return targetRoot(*m->expr);
+  if (auto *a = dynamic_cast<const AST::ArrayAccessExpression *>(&e)) return targetRoot(*a->arrayExpr);
+  return nullptr;
+}
+
+// Member of `var` named by an assignment target `var.m[...]`, or "" for the
+// whole variable.
+std::string targetMember(const AST::Expression &e) {
+  const AST::Expression *cur = &e;
+  std::string last;
+  while (true) {
+    if (auto *m = dynamic_cast<const AST::MemberAccessExpression *>(cur)) {
+      last = m->member;
+      cur = &*m->expr;
+    } else if (auto *a = dynamic_cast<const AST::ArrayAccessExpression *>(cur)) {
+      cur = &*a->arrayExpr;
+    } else {
+      return last;
+    }
+  }
+}
+
+bool isHostOnlyBuiltin(const std::string &name) {
+  return name == "random" || name == "randomInt" || name == "add" || name == "save"
+      || name == "removeCurrent" || name == "count" || name == "sum" || name == "log_csv"
+      || name == "getLastExecTime";
+}
+
+// Collects calls, loops and assignments below a node.
+struct Collector : public AST::Visitor {
+  std::vector<const AST::CallExpression *> calls;
+  std::vector<const AST::ForStatement *> nearLoops;
+  std::vector<const AST::AssignStatement *> assigns;
+  std::vector<const AST::AssignOpStatement *> assignOps;
+  std::vector<const AST::VarExpression *> varExprs;
+  std::vector<const AST::VarDeclarationStatement *> decls;
+  std::vector<const AST::ForStatement *> fors;
+  int breaks = 0, returns = 0;
+
+  void enter(AST::CallExpression &e) override { calls.push_back(&e); }
+  void enter(AST::ForStatement &s) override {
+    fors.push_back(&s);
+    if (s.isNear()) nearLoops.push_back(&s);
+  }
+  void enter(AST::AssignStatement &s) override { assigns.push_back(&s); }
+  void enter(AST::AssignOpStatement &s) override { assignOps.push_back(&s); }
+  void enter(AST::VarExpression &e) override { varExprs.push_back(&e); }
+  void enter(AST::VarDeclarationStatement &s) override { decls.push_back(&s); }
+  void enter(AST::BreakStatement &) override { breaks++; }
+  void enter(AST::ReturnStatement &) override { returns++; }
+};
+
+template <typename N>
+Collector collect(N &node) {
+  Collector c;
+  const_cast<typename std::remove_const<N>::type &>(node).accept(c);
+  return c;
+}
+
+// Whether the result of a near body can depend on the order in which
+// neighbours are visited.  Order-free bodies only accumulate integers into
+// variables declared outside the loop with +=, -=, |=, &=, ^= and never read
+// those variables otherwise; everything else is treated as order-dependent.
+bool nearBodyIsOrdered(const AST::ForStatement &loop) {
+  Collector c = collect(*loop.stmt);
+  if (c.breaks || c.returns) return true;
+  std::set<VarId> inner;
+  inner.insert(loop.var->id);
+  for (auto *d : c.decls) inner.insert(d->var->id);
+  for (auto *f : c.fors) inner.insert(f->var->id);
+  for (auto *call : c.calls) {
+    if (call->isBuiltin() && isHostOnlyBuiltin(call->name)) return true;
+    if (call->kind == AST::CallExpression::Kind::USER) return true;
+  }
+  for (auto *a : c.assigns) {
+    const AST::VarExpression *root = targetRoot(*a->left);
+    if (!root || !inner.count(root->var->id)) return true;
+  }
+  std::map<VarId, int> accTargets;
+  for (auto *a : c.assignOps) {
+    const AST::VarExpression *root = targetRoot(*a->left);
+    if (!root) return true;
+    if (inner.count(root->var->id)) continue;
+    auto *plain = dynamic_cast<const AST::VarExpression *>(&*a->left);
+    if (!plain) return true;
+    Type t = a->left->type;
+    bool okOp = a->op == AST::BinaryOp::ADD || a->op == AST::BinaryOp::SUB
+             || a->op == AST::BinaryOp::BITWISE_OR || a->op == AST::BinaryOp::BITWISE_AND
+             || a->op == AST::BinaryOp::BITWISE_XOR;
+    if (!okOp || !(t.isInt() || t.isBool())) return true;
+    accTargets[root->var->id]++;
+  }
+  std::map<VarId, int> uses;
+  for (auto *v : c.varExprs) uses[v->var->id]++;
+  for (auto &kv : accTargets) {
+    if (uses[kv.first] != kv.second) return true;  // read somewhere besides its own update
+  }
+  return false;
+}
+
+}  // namespace
+
+bool CudaPrinter::isGlobal(const AST::Var &var) const {
+  return script.scope.has(var.id) && script.scope.get(var.id).isGlobal;
+}
+
+int CudaPrinter::agentIndex(const AST::AgentDeclaration *decl) const {
+  for (size_t k = 0; k < script.agents.size(); k++) {
+    if (script.agents[k] == decl) return (int) k;
+  }
+  return -1;
+}
+
+std::string CudaPrinter::cType(Type t) {
+  switch (t.getTypeId()) {
+    case Type::BOOL: return "bool";
+    case Type::INT32: return "int";
+    case Type::FLOAT: return useFloat ? "float" : "double";
+    case Type::VEC2: return "float2";
+    case Type::VEC3: return "float3";
+    default:
+      throw BackendError("The cuda backend does not support agent members of this type");
+  }
+}
+
+static const char *ablTypeId(Type t) {
+  switch (t.getTypeId()) {
+    case Type::BOOL: return "ABL_T_BOOL";
+    case Type::INT32: return "ABL_T_INT";
+    case Type::FLOAT: return "ABL_T_FLOAT";
+    case Type::VEC2: return "ABL_T_FLOAT2";
+    case Type::VEC3: return "ABL_T_FLOAT3";
+    default: return "0";
+  }
+}
+
+void CudaPrinter::print(const AST::VarExpression &expr) {
+  if (isGlobal(*expr.var)) {
+    *this << "abl_G." << expr.var->name;
+    return;
+  }
+  CPrinter::print(expr);
+}
+
+void CudaPrinter::print(const AST::CallExpression &expr) {
+  if (expr.kind == AST::CallExpression::Kind::USER) {
+    *this << expr.calledSig.name << "(abl_G";
+    for (const AST::ExpressionPtr &arg : *expr.args) *this << ", " << *arg;
+    *this << ")";
+    return;
+  }
+  if (expr.isBuiltin() && isHostOnlyBuiltin(expr.name)) {
+    const std::string &n = expr.name;
+    if (n != "random" && n != "randomInt" && n != "add" && n != "save") {
+      throw BackendError("The cuda backend does not support " + n + "() yet");
+    }
+  }
+  CPrinter::print(expr);
+}
+
+// `Agent { m: e, ... }`: members are evaluated in the written order (as gcc
+// does for the reference's compound literal, CPrinter.cpp:87-90).
+void CudaPrinter::print(const AST::AgentCreationExpression &expr) {
+  *this << "([&]() { " << expr.name << " abl_a; ";
+  for (const AST::MemberInitEntryPtr &m : *expr.members) {
+    *this << "abl_a." << m->name << " = " << *m->expr << "; ";
+  }
+  *this << "return abl_a; }())";
+}
+
+void CudaPrinter::print(const AST::WhileStatement &stmt) {
+  if (nearLoopDepth >= 0) nearLoopDepth++;
+  CPrinter::print(stmt);
+  if (nearLoopDepth >= 0) nearLoopDepth--;
+}
+
+void CudaPrinter::print(const AST::BreakStatement &stmt) {
+  if (nearLoopDepth == 0) {
+    *this << "goto " << nearEndLabel << ";";
+    nearNeedsEnd = true;
+    return;
+  }
+  CPrinter::print(stmt);
+}
+
+// The near loop (reference: CPrinter.cpp:148-173).  Candidates come from the
+// runtime's grid; the reference's own radius test decides the rare
+// candidates that the float prefilter cannot.
+void CudaPrinter::print(const AST::ForStatement &stmt) {
+  if (!stmt.isNear()) {
+    if (nearLoopDepth >= 0) nearLoopDepth++;
+    CPrinter::print(stmt);
+    if (nearLoopDepth >= 0) nearLoopDepth--;
+    return;
+  }
+  if (nearLoopDepth >= 0) throw BackendError("Nested near loops are not supported");
+  const AST::Expression &agentExpr = stmt.getNearAgent();
+  const AST::Expression &radiusExpr = stmt.getNearRadius();
+  AST::AgentDeclaration *agentDecl = stmt.type->resolved.getAgentDecl();
+  AST::AgentMember *posMember = agentDecl->getPositionMember();
+  bool is3 = posMember->type->resolved == Type::VEC3;
+  const char *distFn = is3 ? "dist_float3" : "dist_float2";
+  int dim = is3 ? 3 : 2;
+  int id = ++nearCounter;
+  std::string sid = std::to_string(id);
+  std::string q = "abl_q" + sid, c = "abl_c" + sid, ex = "abl_exact" + sid;
+  std::string nxs = "abl_nx" + sid, slot = "abl_slot" + sid;
+
+  int posIdx = -1;
+  for (size_t k = 0; k < agentDecl->members->size(); k++) {
+    if (&*(*agentDecl->members)[k] == posMember) posIdx = (int) k;
+  }
+  std::string posCol = "((const " + cType(posMember->type->resolved) + " *) abl_NB.cols["
+                     + std::to_string(posIdx) + "])";
+
+  *this << "{" << indent << nl
+        << "const abl::near_query<" << dim << "> " << q << "(abl_NB, (double) " << agentExpr
+        << "->" << posMember->name << ".x, (double) " << agentExpr << "->" << posMember->name
+        << ".y, " << (is3 ? "(double) " : "0.0");
+  if (is3) *this << agentExpr << "->" << posMember->name << ".z";
+  *this << ");" << nl
+        << "abl::near_cursor<" << dim << "> " << c << "(abl_NB, " << q << ");" << nl
+        << "auto " << ex << " = [&](int abl_s) -> bool {" << indent << nl
+        << "const " << cType(posMember->type->resolved) << " abl_p = " << posCol << "[abl_s];"
+        << nl << "return !(" << distFn << "(abl_p, " << agentExpr << "->" << posMember->name
+        << ") > " << radiusExpr << ");" << outdent << nl << "};" << nl
+        << "while (" << c << ".fill(" << q << ", " << ex << ")) {" << indent << nl
+        << "for (int abl_k = 0; abl_k < " << c << ".cnt; ++abl_k) {" << indent << nl
+        << "const int " << slot << " = " << c << ".buf[abl_k];" << nl
+        << agentDecl->name << " " << nxs << ";";
+  // Load the members the loop reads (AnalysisVisitor collects them,
+  // src/AnalysisVisitor.cpp:1101-1105).
+  const AST::FunctionDeclaration *cur = steps.empty() ? nullptr : steps.back().decl;
+  for (size_t k = 0; k < agentDecl->members->size(); k++) {
+    const AST::AgentMember &m = *(*agentDecl->members)[k];
+    bool used = cur && cur->accessedMembers.count(m.name);
+    if (!used) continue;
+    *this << nl << nxs << "." << m.name << " = ((const " << cType(m.type->resolved)
+          << " *) abl_NB.cols[" << (int) k << "])[" << slot << "];";
+  }
+  *this << nl << agentDecl->name << "* " << *stmt.var << " = &" << nxs << ";" << nl;
+
+  std::string savedLabel = nearEndLabel;
+  bool savedNeeds = nearNeedsEnd;
+  nearEndLabel = "abl_near_end" + sid;
+  nearNeedsEnd = false;
+  nearLoopDepth = 0;
+  *this << *stmt.stmt;
+  nearLoopDepth = -1;
+  *this << outdent << nl << "}" << outdent << nl << "}" << outdent << nl << "}";
+  if (nearNeedsEnd) *this << nl << nearEndLabel << ": ;";
+  nearEndLabel = savedLabel;
+  nearNeedsEnd = savedNeeds;
+}
+
+void CudaPrinter::print(const AST::SimulateStatement &stmt) {
+  if (stmt.seqStepDecl) {
+    throw BackendError("The cuda backend does not support sequential step functions yet");
+  }
+  *this << "abl_simulate(" << *stmt.timestepsExpr << ");";
+}
+
+void CudaPrinter::print(const AST::FunctionDeclaration &decl) {
+  if (decl.isMain()) {
+    *this << "static int abl_main() {" << indent << *decl.stmts << nl << "return 0;"
+          << outdent << nl << "}";
+    return;
+  }
+  if (decl.isParallelStep()) {
+    printStepFunction(decl);
+    return;
+  }
+  if (decl.isSequentialStep()) {
+    throw BackendError("The cuda backend does not support sequential step functions yet");
+  }
+  printUserFunction(decl);
+}
+
+void CudaPrinter::printUserFunction(const AST::FunctionDeclaration &decl) {
+  // Functions that reach a host-only builtin (the sequential RNG of
+  // asset/c/libabl.c:8-39, add, save) run on the host only.
+  std::map<const AST::FunctionDeclaration *, bool> hostOnly;
+  std::function<bool(const AST::FunctionDeclaration *, int)> isHost =
+      [&](const AST::FunctionDeclaration *f, int depth) -> bool {
+    auto it = hostOnly.find(f);
+    if (it != hostOnly.end()) return it->second;
+    if (depth > 64) return true;
+    hostOnly[f] = false;
+    Collector c = collect(*const_cast<AST::FunctionDeclaration *>(f));
+    bool h = false;
+    for (auto *call : c.calls) {
+      if (call->isBuiltin() && isHostOnlyBuiltin(call->name)) h = true;
+      if (call->kind == AST::CallExpression::Kind::USER && call->calledFunc
+          && isHost(call->calledFunc, depth + 1)) h = true;
+    }
+    hostOnly[f] = h;
+    return h;
+  };
+  bool host = isHost(&decl, 0);
+  *this << (host ? "static inline " : "__host__ __device__ static inline ")
+        << *decl.returnType << " " << decl.sig.name << "(const abl_globals &abl_G";
+  if (!decl.params->empty()) *this << ", ";
+  printParams(decl);
+  *this << ") {" << indent << *decl.stmts << outdent << nl << "}";
+}
+
+void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
+  StepInfo info;
+  info.decl = &decl;
+  const AST::AgentDeclaration &agent = decl.stepAgent();
+  info.agentType = agentIndex(&agent);
+  Collector c = collect(*const_cast<AST::FunctionDeclaration *>(&decl));
+  for (auto *call : c.calls) {
+    if (call->isBuiltin() && (call->name == "add" || call->name == "removeCurrent")) {
+      throw BackendError("The cuda backend does not support runtime add/remove yet");
+    }
+    if (call->isBuiltin() && (call->name == "random" || call->name == "randomInt")) {
+      throw BackendError("The cuda backend does not support random() in step functions yet");
+    }
+  }
+  if (!c.nearLoops.empty()) {
+    const AST::ForStatement *loop = c.nearLoops[0];
+    info.nearLoop = loop;
+    const AST::AgentDeclaration *nearAgent = loop->type->resolved.getAgentDecl();
+    info.nearType = agentIndex(nearAgent);
+    info.ordered = nearBodyIsOrdered(*loop);
+    for (size_t k = 0; k < nearAgent->members->size(); k++) {
+      const AST::AgentMember &m = *(*nearAgent->members)[k];
+      if (decl.accessedMembers.count(m.name) || m.isPosition) info.nearMembers |= 1u << k;
+    }
+    // The radius must not depend on the agent: it sizes the grid search.
+    Collector rc = collect(*const_cast<AST::Expression *>(&loop->getNearRadius()));
+    for (auto *v : rc.varExprs) {
+      if (!isGlobal(*v->var)) {
+        throw BackendError("The cuda backend needs a near() radius that does not depend on "
+                           "the agent");
+      }
+    }
+  }
+  // Members of `out` written by the function: any assignment rooted at
+  // out.m may write it; a top-level `out.m = e` always does, provided `out`
+  // is never read and the function never returns early.
+  const AST::Param &param = decl.stepParam();
+  VarId outId = param.outVar->id;
+  auto memberBit = [&](const std::string &name) -> unsigned {
+    for (size_t k = 0; k < agent.members->size(); k++) {
+      if ((*agent.members)[k]->name == name) return 1u << k;
+    }
+    return 0;
+  };
+  unsigned all = agent.members->size() >= 32 ? ~0u : ((1u << agent.members->size()) - 1);
+  int outTargets = 0;
+  auto noteTarget = [&](const AST::Expression &left) {
+    const AST::VarExpression *root = targetRoot(left);
+    if (!root || root->var->id != outId) return;
+    outTargets++;
+    std::string m = targetMember(left);
+    info.outMaybe |= m.empty() ? all : memberBit(m);
+  };
+  for (auto *a : c.assigns) noteTarget(*a->left);
+  for (auto *a : c.assignOps) noteTarget(*a->left);
+  int outUses = 0;
+  for (auto *v : c.varExprs) outUses += v->var->id == outId;
+  if (c.returns == 0 && outUses == outTargets) {
+    for (const AST::StatementPtr &s : *decl.stmts) {
+      auto *a = dynamic_cast<const AST::AssignStatement *>(&*s);
+      if (!a) continue;
+      const AST::VarExpression *root = targetRoot(*a->left);
+      if (!root || root->var->id != outId) continue;
+      auto *ma = dynamic_cast<const AST::MemberAccessExpression *>(&*a->left);
+      if (dynamic_cast<const AST::VarExpression *>(&*a->left)) {
+        info.outAlways |= all;
+      } else if (ma && dynamic_cast<const AST::VarExpression *>(&*ma->expr)) {
+        info.outAlways |= memberBit(ma->member);
+      }
+    }
+  }
+  steps.push_back(info);
+
+  *this << "__device__ static void " << decl.name
+        << "(const abl_globals &abl_G, const abl_near_view &abl_NB, ";
+  printParams(decl);
+  *this << ") {" << indent << *decl.stmts << outdent << nl << "}" << nl;
+  printKernel(steps.back());
+}
+
+void CudaPrinter::printKernel(const StepInfo &info) {
+  const AST::FunctionDeclaration &decl = *info.decl;
+  const AST::AgentDeclaration &agent = decl.stepAgent();
+  const std::string &T = agent.name;
+  const std::string &name = decl.name;
+  *this << nl << "struct abl_kargs_" << name << " {" << indent << nl
+        << "abl_globals G;" << nl << "long n;" << nl << "const int *visit;" << nl
+        << "abl_cols_" << T << " in, out;" << nl << "abl_near_view NB;" << outdent << nl << "};"
+        << nl << "__global__ void __launch_bounds__(128) abl_kernel_" << name
+        << "(const __grid_constant__ abl_kargs_" << name << " A) {" << indent << nl
+        << "const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl
+        << "if (abl_t >= A.n) return;" << nl
+        << "const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;" << nl
+        << T << " abl_in, abl_out;";
+  for (size_t k = 0; k < agent.members->size(); k++) {
+    const std::string &m = (*agent.members)[k]->name;
+    *this << nl << "abl_in." << m << " = A.in." << m << "[abl_i];";
+  }
+  for (size_t k = 0; k < agent.members->size(); k++) {
+    const std::string &m = (*agent.members)[k]->name;
+    bool maybe = info.outMaybe & (1u << k), always = info.outAlways & (1u << k);
+    // The double buffer keeps whatever it held for members the step does not
+    // always write (the reference's agents_X_dbuf, CPrinter.cpp:210-228).
+    if (maybe && !always) *this << nl << "abl_out." << m << " = A.out." << m << "[abl_i];";
+  }
+  *this << nl << name << "(A.G, A.NB, &abl_in, &abl_out);";
+  for (size_t k = 0; k < agent.members->size(); k++) {
+    const std::string &m = (*agent.members)[k]->name;
+    if (info.outMaybe & (1u << k)) *this << nl << "A.out." << m << "[abl_i] = abl_out." << m << ";";
+  }
+  *this << outdent << nl << "}" << nl
+        << "static int abl_launch_" << name
+        << "(const abl_step_launch *L, cudaStream_t abl_stream) {" << indent << nl
+        << "abl_kargs_" << name << " A;" << nl
+        << "A.G = *(const abl_globals *) L->globals;" << nl
+        << "A.n = L->n;" << nl << "A.visit = L->visit_order;";
+  for (size_t k = 0; k < agent.members->size(); k++) {
+    const AST::AgentMember &m = *(*agent.members)[k];
+    std::string ty = cType(m.type->resolved);
+    *this << nl << "A.in." << m.name << " = (" << ty << " *) L->in_cols[" << (int) k << "];"
+          << nl << "A.out." << m.name << " = (" << ty << " *) L->out_cols[" << (int) k << "];";
+  }
+  *this << nl << "A.NB = L->near;" << nl
+        << "const int abl_block = L->block > 0 ? L->block : 128;" << nl
+        << "const long abl_grid = (A.n + abl_block - 1) / abl_block;" << nl
+        << "abl_kernel_" << name << "<<<abl_grid, abl_block, 0, abl_stream>>>(A);" << nl
+        << "return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;" << outdent << nl
+        << "}" << nl;
+  if (info.nearLoop) {
+    *this << "static double abl_radius_" << name << "(const void *abl_gp) {" << indent << nl
+          << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl
+          << "(void) abl_G;" << nl
+          << "return (double) (" << info.nearLoop->getNearRadius() << ");" << outdent << nl
+          << "}" << nl;
+  }
+}
+
+void CudaPrinter::printGlobals() {
+  *this << "struct abl_globals {" << indent;
+  for (AST::ConstDeclaration *decl : script.consts) {
+    if (decl->isArray) throw BackendError("The cuda backend does not support constant arrays yet");
+    *this << nl << *decl->type << " " << decl->var->name << ";";
+  }
+  *this << outdent << nl << "};" << nl
+        << "static const abl_globals abl_globals_default = {" << indent;
+  for (AST::ConstDeclaration *decl : script.consts) {
+    *this << nl;
+    if (decl->type->resolved.isVec()) {
+      auto *call = dynamic_cast<const AST::CallExpression *>(&*decl->expr);
+      if (!call) throw BackendError("Unexpected vector constant initializer");
+      *this << "{";
+      printCommaSeparated(*call->args, [&](const AST::ExpressionPtr &arg) { *this << *arg; });
+      *this << "},";
+    } else {
+      *this << *decl->expr << ",";
+    }
+  }
+  *this << outdent << nl << "};" << nl
+        << "static abl_globals abl_G = abl_globals_default;" << nl;
+}
+
+void CudaPrinter::printHostSimulate() {
+  // Hands the host-built population to the device runtime for the simulate
+  // loop and reads it back for the statements after it.
+  *this << "static void abl_check(int r, const char *what) {" << indent << nl
+        << "if (r != ABL_OK) {" << indent << nl
+        << "std::fprintf(stderr, \"%s failed: %s\\n\", what, abl_strerror(r));" << nl
+        << "std::exit(1);" << outdent << nl << "}" << outdent << nl << "}" << nl
+        << "static void abl_simulate(int abl_timesteps) {" << indent << nl
+        << "abl_ctx *ctx = nullptr;" << nl
+        << "abl_check(abl_create(&abl_desc, 0, &ctx), \"abl_create\");" << nl
+        << "abl_check(abl_set_globals(ctx, &abl_G, sizeof abl_G), \"abl_set_globals\");";
+  for (size_t ti = 0; ti < script.agents.size(); ti++) {
+    const AST::AgentDeclaration &a = *script.agents[ti];
+    const std::string &T = a.name;
+    *this << nl << "{" << indent << nl
+          << "size_t n = agents.agents_" << T << ".len;" << nl
+          << "const " << T << " *aos = (const " << T << " *) agents.agents_" << T << ".values;";
+    for (size_t k = 0; k < a.members->size(); k++) {
+      const AST::AgentMember &m = *(*a.members)[k];
+      std::string ty = cType(m.type->resolved);
+      *this << nl << ty << " *c" << k << " = (" << ty << " *) std::malloc(sizeof(" << ty
+            << ") * (n ? n : 1));" << nl << "for (size_t i = 0; i < n; i++) c" << k
+            << "[i] = aos[i]." << m.name << ";";
+    }
+    *this << nl << "const void *cols[] = {";
+    for (size_t k = 0; k < a.members->size(); k++) *this << (k ? ", " : "") << "c" << k;
+    *this << "};" << nl << "abl_check(abl_upload(ctx, " << (int) ti
+          << ", cols, n), \"abl_upload\");";
+    for (size_t k = 0; k < a.members->size(); k++) *this << nl << "std::free(c" << k << ");";
+    *this << outdent << nl << "}";
+  }
+  *this << nl << "abl_check(abl_run(ctx, abl_timesteps), \"abl_run\");";
+  for (size_t ti = 0; ti < script.agents.size(); ti++) {
+    const AST::AgentDeclaration &a = *script.agents[ti];
+    const std::string &T = a.name;
+    *this << nl << "{" << indent << nl << "size_t n = 0;" << nl
+          << "abl_check(abl_count(ctx, " << (int) ti << ", &n), \"abl_count\");";
+    for (size_t k = 0; k < a.members->size(); k++) {
+      const AST::AgentMember &m = *(*a.members)[k];
+      std::string ty = cType(m.type->resolved);
+      *this << nl << ty << " *c" << k << " = (" << ty << " *) std::malloc(sizeof(" << ty
+            << ") * (n ? n : 1));";
+    }
+    *this << nl << "void *cols[] = {";
+    for (size_t k = 0; k < a.members->size(); k++) *this << (k ? ", " : "") << "c" << k;
+    *this << "};" << nl << "size_t cap = n;" << nl
+          << "abl_check(abl_download(ctx, " << (int) ti << ", cols, &cap), \"abl_download\");"
+          << nl << "dyn_array_clean(&agents.agents_" << T << ");" << nl
+          << "agents.agents_" << T << " = dyn_array_create_fixed(sizeof(" << T << "), n);" << nl
+          << T << " *aos = (" << T << " *) agents.agents_" << T << ".values;" << nl
+          << "for (size_t i = 0; i < n; i++) {" << indent;
+    for (size_t k = 0; k < a.members->size(); k++) {
+      *this << nl << "aos[i]." << (*a.members)[k]->name << " = c" << k << "[i];";
+    }
+    *this << outdent << nl << "}";
+    for (size_t k = 0; k < a.members->size(); k++) *this << nl << "std::free(c" << k << ");";
+    *this << outdent << nl << "}";
+  }
+  *this << nl << "double abl_secs = 0;" << nl << "abl_last_exec_time(ctx, &abl_secs);" << nl
+        << "abl_destroy(ctx);" << outdent << nl << "}" << nl;
+}
+
+void CudaPrinter::printDescriptor() {
+  for (const AST::AgentDeclaration *a : script.agents) {
+    *this << "static const abl_member_desc abl_members_" << a->name << "[] = {" << indent;
+    for (const AST::AgentMemberPtr &m : *a->members) {
+      Type t = m->type->resolved;
+      int comps = t.isVec() ? (int) t.getVecLen() : 1;
+      std::string scalar = t.isBool() ? "1" : t.isInt() ? "4" : (useFloat ? "4" : "8");
+      *this << nl << "{\"" << m->name << "\", " << ablTypeId(t) << ", " << comps << ", " << scalar
+            << ", " << (m->isPosition ? 1 : 0) << "},";
+    }
+    *this << outdent << nl << "};" << nl;
+  }
+  *this << "static const abl_agent_desc abl_agents[] = {" << indent;
+  for (const AST::AgentDeclaration *a : script.agents) {
+    int posIdx = -1, dim = 0;
+    for (size_t k = 0; k < a->members->size(); k++) {
+      if ((*a->members)[k]->isPosition) {
+        posIdx = (int) k;
+        dim = (int) (*a->members)[k]->type->resolved.getVecLen();
+      }
+    }
+    *this << nl << "{\"" << a->name << "\", " << (int) a->members->size() << ", abl_members_"
+          << a->name << ", " << posIdx << ", " << dim << "},";
+  }
+  *this << outdent << nl << "};" << nl;
+  *this << "static const abl_global_desc abl_global_table[] = {" << indent;
+  for (AST::ConstDeclaration *decl : script.consts) {
+    *this << nl << "{\"" << decl->var->name << "\", " << ablTypeId(decl->type->resolved)
+          << ", offsetof(abl_globals, " << decl->var->name << ")},";
+  }
+  *this << nl << "{nullptr, 0, 0}" << outdent << nl << "};" << nl;
+
+  // Environment bounds and granularity (src/AnalysisVisitor.cpp:474-538).
+  AST::EnvironmentDeclaration *env = script.envDecl;
+  int envDim = env && env->hasEnvDimension() ? (int) env->getEnvDimension() : 0;
+  const AST::Expression *minE = nullptr, *maxE = nullptr, *granE = nullptr;
+  if (env) {
+    for (const AST::MemberInitEntryPtr &m : *env->members) {
+      if (m->name == "min") minE = &*m->expr;
+      if (m->name == "max") maxE = &*m->expr;
+      if (m->name == "granularity") granE = &*m->expr;
+    }
+  }
+  *this << "static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max) {"
+        << indent << nl << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl
+        << "(void) abl_G;";
+  if (envDim > 0) {
+    std::string vt = envDim == 2 ? "float2" : "float3";
+    *this << nl << vt << " abl_lo = ";
+    if (minE) *this << *minE;
+    else *this << vt << "_fill(0)";
+    *this << ";" << nl << vt << " abl_hi = ";
+    if (maxE) *this << *maxE;
+    else *this << vt << "_fill(0)";
+    *this << ";" << nl << "abl_min[0] = abl_lo.x; abl_min[1] = abl_lo.y; abl_min[2] = "
+          << (envDim == 3 ? "abl_lo.z" : "0") << ";" << nl
+          << "abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = "
+          << (envDim == 3 ? "abl_hi.z" : "0") << ";";
+  } else {
+    *this << nl << "for (int d = 0; d < 3; d++) abl_min[d] = abl_max[d] = 0;";
+  }
+  *this << outdent << nl << "}" << nl;
+  if (granE) {
+    *this << "static double abl_granularity(const void *abl_gp) {" << indent << nl
+          << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl << "(void) abl_G;"
+          << nl << "return (double) (" << *granE << ");" << outdent << nl << "}" << nl;
+  }
+
+  *this << "static const abl_step_desc abl_steps[] = {" << indent;
+  for (const StepInfo &s : steps) {
+    const std::string &n = s.decl->name;
+    *this << nl << "{\"" << n << "\", " << s.agentType << ", " << s.nearType << ", "
+          << (s.ordered ? 1 : 0) << ", " << (s.nearLoop ? "abl_radius_" + n : "nullptr") << ", "
+          << s.nearMembers << "u, " << s.outAlways << "u, abl_launch_" << n << "},";
+  }
+  if (steps.empty()) *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr},";
+  *this << outdent << nl << "};" << nl;
+  // The runtime runs the steps in simulate order (SimulateStatement::stepFuncDecls,
+  // CPrinter.cpp:196); abl_steps above is in declaration order.
+  *this << "static const abl_step_desc abl_steps_ordered[] = {" << indent;
+  if (script.simStmt) {
+    for (AST::FunctionDeclaration *f : script.simStmt->stepFuncDecls) {
+      for (size_t k = 0; k < steps.size(); k++) {
+        if (steps[k].decl == f) *this << nl << "abl_steps[" << (int) k << "],";
+      }
+    }
+  }
+  *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr}" << outdent << nl << "};" << nl;
+  int numSteps = 0;
+  if (script.simStmt) numSteps = (int) script.simStmt->stepFuncDecls.size();
+  *this << "extern const abl_model_desc abl_desc = {" << indent << nl
+        << "\"" << modelName << "\", " << (int) script.agents.size() << ", abl_agents, "
+        << numSteps << ", abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, "
+        << (int) script.consts.size() << ", abl_global_table, " << envDim
+        << ", abl_env_bounds, " << (granE ? "abl_granularity" : "nullptr") << ", "
+        << (useFloat ? 1 : 0) << outdent << nl << "};" << nl;
+}
+
+void CudaPrinter::print(const AST::Script &) {
+  *this << "// Generated by OpenABL -b cuda (model \"" << modelName << "\")." << nl
+        << "#include \"abl_gen.cuh\"" << nl << nl
+        << "namespace abl_model_" << modelName << " {" << nl << nl
+        << "typedef " << (useFloat ? "float" : "double") << " abl_float;" << nl
+        << "#include \"abl_math.cuh\"" << nl << nl;
+  for (AST::AgentDeclaration *decl : script.agents) *this << *decl << nl;
+  *this << "struct agent_struct {" << indent;
+  for (AST::AgentDeclaration *decl : script.agents) {
+    *this << nl << "dyn_array agents_" << decl->name << ";" << nl << "dyn_array agents_"
+          << decl->name << "_dbuf;";
+  }
+  *this << outdent << nl << "};" << nl << "static struct agent_struct agents;" << nl
+        << "static const agent_info agents_info[] = {" << indent << nl;
+  for (AST::AgentDeclaration *decl : script.agents) {
+    *this << "{ " << decl->name << "_info, offsetof(struct agent_struct, agents_" << decl->name
+          << "), \"" << decl->name << "\" }," << nl;
+  }
+  *this << "{ NULL, 0, NULL }" << outdent << nl << "};" << nl << nl;
+  printGlobals();
+  for (AST::AgentDeclaration *a : script.agents) {
+    *this << "struct abl_cols_" << a->name << " {" << indent;
+    for (const AST::AgentMemberPtr &m : *a->members) {
+      *this << nl << cType(m->type->resolved) << " *" << m->name << ";";
+    }
+    *this << outdent << nl << "};" << nl;
+  }
+  *this << nl;
+  const AST::FunctionDeclaration *mainDecl = nullptr;
+  for (AST::FunctionDeclaration *decl : script.funcs) {
+    if (decl->isMain()) {
+      mainDecl = decl;
+      continue;
+    }
+    *this << *decl << nl;
+  }
+  *this << nl;
+  printDescriptor();
+  if (mainDecl) {
+    printHostSimulate();
+    *this << *mainDecl << nl;
+  }
+  *this << nl << "}  // namespace abl_model_" << modelName << nl << nl
+        << "extern \"C\" const abl_model_desc *abl_model_desc_" << modelName << "(void) {"
+        << indent << nl << "return &abl_model_" << modelName << "::abl_desc;" << outdent << nl
+        << "}" << nl;
+  if (mainDecl) {
+    *this << nl << "#ifdef ABL_STANDALONE_MAIN" << nl
+          << "extern \"C\" const abl_model_desc *const abl_builtin_models[] = {" << nl
+          << "    &abl_model_" << modelName << "::abl_desc, nullptr};" << nl
+          << "int main() { return abl_model_" << modelName << "::abl_main(); }" << nl
+          << "#endif" << nl;
+  }
+}
+
+}  // namespace OpenABL

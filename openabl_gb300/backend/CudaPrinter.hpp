@@ -1,0 +1,78 @@
+// Printer of the `-b cuda` backend.
+//
+// Derives from the reference `c` backend's printer (src/backend/CPrinter.hpp)
+// so that every expression and statement is printed by the reference's own
+// rules -- operator forms, vector operation names, literal precision, casts --
+// and therefore evaluates with the same C semantics on the device.  It
+// overrides only what changes on the GPU:
+//   * globals are fields of a struct `G` handed to kernels and functions
+//     (instead of C globals);
+//   * a step function becomes a __device__ body plus a kernel over agents;
+//     its `near` loop walks the runtime's binned grid (abl_device.cuh) instead
+//     of every agent (CPrinter.cpp:148-173);
+//   * `simulate` hands the population to the device runtime
+//     (instead of CPrinter.cpp:189-233);
+//   * the generated file also carries the model descriptor of
+//     openabl_gb300/csrc/abl_model.h.
+#pragma once
+
+#include <set>
+#include <string>
+#include <vector>
+
+#include "CPrinter.hpp"
+
+namespace OpenABL {
+
+struct CudaPrinter : public CPrinter {
+  using CPrinter::print;
+
+  CudaPrinter(AST::Script &script, bool useFloat, const std::string &modelName)
+    : CPrinter(script, useFloat), script(script), useFloat(useFloat), modelName(modelName) {}
+
+  void print(const AST::VarExpression &) override;
+  void print(const AST::CallExpression &) override;
+  void print(const AST::AgentCreationExpression &) override;
+  void print(const AST::ForStatement &) override;
+  void print(const AST::WhileStatement &) override;
+  void print(const AST::BreakStatement &) override;
+  void print(const AST::SimulateStatement &) override;
+  void print(const AST::FunctionDeclaration &) override;
+  void print(const AST::Script &) override;
+
+private:
+  AST::Script &script;
+  bool useFloat;
+  std::string modelName;
+
+  // Near-loop printing state.
+  int nearCounter = 0;
+  int nearLoopDepth = -1;        // loop depth inside the current near body
+  bool nearNeedsEnd = false;     // a `break` left the current near body
+  std::string nearEndLabel;
+
+  // Per step function, filled while printing it.
+  struct StepInfo {
+    const AST::FunctionDeclaration *decl = nullptr;
+    int agentType = -1;
+    int nearType = -1;
+    bool ordered = true;
+    unsigned nearMembers = 0;
+    unsigned outMaybe = 0;
+    unsigned outAlways = 0;
+    const AST::ForStatement *nearLoop = nullptr;
+  };
+  std::vector<StepInfo> steps;
+
+  bool isGlobal(const AST::Var &var) const;
+  int agentIndex(const AST::AgentDeclaration *decl) const;
+  std::string cType(Type t);
+  void printGlobals();
+  void printStepFunction(const AST::FunctionDeclaration &decl);
+  void printKernel(const StepInfo &info);
+  void printDescriptor();
+  void printHostSimulate();
+  void printUserFunction(const AST::FunctionDeclaration &decl);
+};
+
+}  // namespace OpenABL

@@ -1,0 +1,187 @@
+// Device-side helpers shared by the runtime and generated step kernels.
+//
+// Neighbour iteration.  The reference `near` loop visits every agent of the
+// neighbour type in ascending index and skips those with
+// dist(nx.pos, in.pos) > radius (src/backend/CPrinter.cpp:148-173), where
+// dist is sqrtf of the double sum of squares (asset/c/libabl.h:156-168).
+// Here the neighbour type is binned into a uniform grid whose cells are at
+// least as wide as any near radius; an agent's candidates are the agents in
+// the cells within `range` of its own cell.
+//
+//  * Ordered mode (bodies whose result depends on the visiting order, e.g.
+//    floating-point accumulation): the runtime builds, per cell, the list of
+//    candidate slots in ascending agent id, so the body sees exactly the
+//    reference's sequence of in-radius neighbours.
+//  * Unordered mode (bodies that only do integer accumulation): candidates
+//    are walked cell row by cell row without sorting.
+//
+// The radius test is decided without FP64 arithmetic for almost every
+// candidate: the squared distance is computed in FP32 from float copies of
+// the positions and compared against [r^2 (1 - eps), r^2 (1 + eps)], where
+// eps bounds the error of that FP32 estimate relative to the reference's
+// double computation (given the largest coordinate magnitude A of the agents
+// involved).  Candidates inside that band fall back to the generated exact
+// test, which evaluates the reference expression itself.  Passing slots are
+// buffered per thread in ascending order and the loop body then runs over the
+// buffer, so the FP64 body work is not fragmented by the filter's branches.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "abl_model.h"
+
+#ifndef ABL_NEAR_CHUNK
+#define ABL_NEAR_CHUNK 32
+#endif
+
+namespace abl {
+
+// Cell coordinate of x along one axis; out-of-range positions are clamped
+// into the border cells (monotone, so neighbours within one cell width stay
+// within one cell index).
+__host__ __device__ inline int cell_coord(double x, double lo, double inv_cell, int n) {
+  double f = floor((x - lo) * inv_cell);
+  if (!(f > 0.0)) return 0;
+  if (f >= (double) (n - 1)) return n - 1;
+  return (int) f;
+}
+
+struct band {
+  float lo, hi;
+};
+
+// Prefilter band for radius r.  u = 2^-24.  For a pair whose reference test
+// is near the threshold, |dx| <= s ~ 1.1 r; float rounding of the two
+// positions (|x| <= A) and of the FP32 subtraction perturbs dx by at most
+// E = 2uA + u s per axis, hence d2 by dim * E (2 s + E); the FP32 squares and
+// sum and the reference's own rounding chain (double or float arithmetic, the
+// float rounding of d2 and sqrtf) add a few u relative.  eps doubles that sum.
+// When eps is not small (huge coordinates, zero or negative radius, non-finite
+// values) every candidate takes the exact test.
+__device__ inline band make_band(double radius, float amax, int dim) {
+  band b;
+  b.lo = -1.0f;
+  b.hi = __int_as_float(0x7f800000);  // +inf: nothing is decided by the filter
+  float r = (float) radius;
+  if (!(radius > 0.0) || !(r > 0.0f) || !(amax >= 0.0f) || !(amax < 1e30f)) return b;
+  const float u = 5.9604645e-8f;
+  float s = 1.1f * r;
+  float E = (2.0f * u * amax + u * s) * 1.01f;
+  s += E;
+  float mp = (float) dim * E * (2.0f * s + E);
+  float r2 = r * r;
+  float eps = 2.0f * (mp / r2 + 16.0f * u) + 4.0e-7f;
+  if (!(eps < 0.1f)) return b;
+  b.lo = r2 * (1.0f - eps);
+  b.hi = r2 * (1.0f + eps);
+  return b;
+}
+
+// Query side of a near loop: the agent's cell and float position.
+template <int DIM>
+struct near_query {
+  int c[3];
+  float pf[3];
+  band bd;
+
+  __device__ near_query(const abl_near_view &V, double x, double y, double z) {
+    const int dims[3] = {V.nx, V.ny, V.nz};
+    const double p[3] = {x, y, z};
+    for (int d = 0; d < 3; d++) {
+      c[d] = d < DIM ? cell_coord(p[d], V.lo[d], V.inv_cell, dims[d]) : 0;
+      pf[d] = d < DIM ? (float) p[d] : 0.0f;
+    }
+    bd = make_band(V.radius, *V.amax, DIM);
+  }
+};
+
+// Enumerates in-radius neighbour slots in chunks of at most ABL_NEAR_CHUNK.
+// `Exact` is a callable slot -> bool evaluating the reference's own test.
+template <int DIM>
+struct near_cursor {
+  const abl_near_view &V;
+  // ordered mode: position in the cell's neighbourhood list
+  int cur, end;
+  // unordered mode: current row of cells and slot range within it
+  int rz, ry;
+  int x0, x1;
+  int buf[ABL_NEAR_CHUNK];
+  int cnt;
+
+  __device__ near_cursor(const abl_near_view &v, const near_query<DIM> &q) : V(v), cnt(0) {
+    if (V.ordered) {
+      int cell = (q.c[2] * V.ny + q.c[1]) * V.nx + q.c[0];
+      cur = V.nb_off[cell];
+      end = V.nb_off[cell + 1];
+    } else {
+      rz = DIM == 3 ? max(q.c[2] - V.range, 0) : 0;
+      ry = max(q.c[1] - V.range, 0);
+      x0 = max(q.c[0] - V.range, 0);
+      x1 = min(q.c[0] + V.range, V.nx - 1);
+      cur = end = 0;
+      row_range(q);
+    }
+  }
+
+  // Loads the slot range of the current (rz, ry) row or moves past the grid.
+  __device__ void row_range(const near_query<DIM> &q) {
+    const int zmax = DIM == 3 ? min(q.c[2] + V.range, V.nz - 1) : 0;
+    const int ymax = min(q.c[1] + V.range, V.ny - 1);
+    while (rz <= zmax) {
+      if (ry <= ymax) {
+        int base = (rz * V.ny + ry) * V.nx;
+        cur = V.cell_start[base + x0];
+        end = V.cell_start[base + x1 + 1];
+        return;
+      }
+      rz++;
+      ry = max(q.c[1] - V.range, 0);
+    }
+    cur = end = 0;
+    rz = zmax + 1;
+  }
+
+  __device__ bool exhausted(const near_query<DIM> &q) const {
+    const int zmax = DIM == 3 ? min(q.c[2] + V.range, V.nz - 1) : 0;
+    return rz > zmax;
+  }
+
+  template <typename Exact>
+  __device__ bool fill(const near_query<DIM> &q, Exact &&exact) {
+    cnt = 0;
+    for (;;) {
+      while (cur < end && cnt < ABL_NEAR_CHUNK) {
+        int s = V.ordered ? __ldg(&V.nb_list[cur]) : cur;
+        cur++;
+        float d2 = 0.0f;
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+          float dd = __ldg(&V.posf[DIM * s + d]) - q.pf[d];
+          d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
+        }
+        bool take;
+        if (d2 < q.bd.lo) take = true;
+        else if (d2 > q.bd.hi) take = false;
+        else take = exact(s);
+        if (take) buf[cnt++] = s;
+      }
+      if (cnt == ABL_NEAR_CHUNK || V.ordered) break;
+      if (cur < end) break;
+      // unordered: advance to the next row of cells
+      if (exhausted(q)) break;
+      ry++;
+      row_range(q);
+      if (exhausted(q)) break;
+    }
+    return cnt > 0;
+  }
+};
+
+// Atomic max on non-negative floats (bit patterns order like the values).
+__device__ inline void atomic_max_nonneg(float *addr, float v) {
+  atomicMax(reinterpret_cast<int *>(addr), __float_as_int(v));
+}
+
+}  // namespace abl

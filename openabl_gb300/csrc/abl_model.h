@@ -1,0 +1,108 @@
+/* Contract between code emitted by the `-b cuda` backend and the runtime.
+ *
+ * A generated model file describes its agent types (from the AST's
+ * AgentDeclaration list, CPrinter.cpp:250-265 prints the same information as
+ * `type_info` tables), its globals (the folded `param`/constant
+ * declarations, CPrinter.cpp:305-307), its environment (EnvironmentDeclaration,
+ * src/AnalysisVisitor.cpp:474-538) and its step functions in simulate order
+ * (SimulateStatement::stepFuncDecls, CPrinter.cpp:196).  Each step function
+ * comes with a host launcher that runs its kernel on a stream.
+ */
+#ifndef ABL_MODEL_H
+#define ABL_MODEL_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#include "openabl_cuda.h"
+
+#define ABL_MAX_MEMBERS 16
+
+typedef struct {
+  const char *name;
+  int value_type;     /* ABL_T_* */
+  int components;     /* 1, 2 or 3 */
+  int scalar_bytes;   /* bytes of one component (1, 4 or 8) */
+  int is_position;
+} abl_member_desc;
+
+typedef struct {
+  const char *name;
+  int num_members;
+  const abl_member_desc *members;
+  int position_member; /* index of the `position` member, -1 if none */
+  int dim;             /* 2 or 3 when a position member exists */
+} abl_agent_desc;
+
+typedef struct {
+  const char *name;
+  int value_type;
+  size_t offset;
+} abl_global_desc;
+
+/* Binned view of the neighbour type, filled by the runtime for a step
+ * function that contains a `near` loop.  All pointers are device pointers;
+ * arrays indexed by "slot" are in (cell, agent id) order. */
+typedef struct {
+  int dim;
+  int ordered;              /* 1: per-cell neighbourhood lists in ascending id order */
+  int range;                /* cells searched on each side of the agent's cell */
+  int nx, ny, nz;           /* grid dimensions */
+  double lo[3];             /* grid origin */
+  double inv_cell;          /* 1 / cell size */
+  double radius;            /* value of the near() radius expression */
+  long n;                   /* agents of the neighbour type */
+  const int *cell_start;    /* ncells + 1 */
+  const int *order;         /* slot -> agent id */
+  const float *posf;        /* slot -> position rounded to float (dim per slot) */
+  const int *nb_off;        /* ordered mode: cell -> offset into nb_list (ncells + 1) */
+  const int *nb_list;       /* ordered mode: slots, ascending agent id per cell */
+  const float *amax;        /* max |coordinate| over neighbour and query agents */
+  const void *cols[ABL_MAX_MEMBERS]; /* slot-ordered copies of the members the loop reads */
+} abl_near_view;
+
+/* Everything a generated step launcher needs. */
+typedef struct {
+  long n;                            /* agents of the step's type */
+  void *in_cols[ABL_MAX_MEMBERS];    /* current buffer, per member */
+  void *out_cols[ABL_MAX_MEMBERS];   /* double buffer, per member */
+  const int *visit_order;            /* thread -> agent id (NULL: identity) */
+  const void *globals;               /* host copy of the globals block */
+  int *error;                        /* device error word */
+  abl_near_view near;                /* valid when the step has a near loop */
+  int block;                         /* threads per block chosen by the runtime */
+} abl_step_launch;
+
+typedef int (*abl_step_launch_fn)(const abl_step_launch *launch, cudaStream_t stream);
+typedef double (*abl_globals_fn)(const void *globals);
+typedef void (*abl_env_fn)(const void *globals, double *min3, double *max3);
+
+typedef struct {
+  const char *name;
+  int agent_type;              /* type of the step's `in -> out` parameter */
+  int near_type;               /* type iterated by the near loop, -1 if none */
+  int ordered;                 /* the near body depends on the visiting order */
+  abl_globals_fn radius;       /* value of the near radius expression */
+  uint32_t near_members;       /* bitmask of neighbour members read in the loop */
+  uint32_t out_written;        /* bitmask of members always written to `out` */
+  abl_step_launch_fn launch;
+} abl_step_desc;
+
+struct abl_model_desc {
+  const char *name;
+  int num_agent_types;
+  const abl_agent_desc *agents;
+  int num_steps;
+  const abl_step_desc *steps;   /* in simulate order */
+  size_t globals_size;
+  const void *globals_default;
+  int num_globals;
+  const abl_global_desc *globals;
+  int env_dim;                   /* 0 when there is no environment */
+  abl_env_fn env_bounds;
+  abl_globals_fn granularity;    /* cell size before the safety margin */
+  int uses_float;                /* built with use_float */
+};
+
+#endif /* ABL_MODEL_H */

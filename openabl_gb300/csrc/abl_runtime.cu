@@ -1,0 +1,1089 @@
+// OpenABL CUDA runtime: agent state, uniform-grid binning and the step loop.
+//
+// Per agent type the context keeps structure-of-arrays columns in two
+// buffers (the reference's agents_X / agents_X_dbuf pair,
+// src/backend/CPrinter.cpp:278-293).  A timestep runs the model's step
+// functions in simulate order (CPrinter.cpp:196-229); each one reads the
+// current buffer, writes the other, and the two are swapped afterwards.
+//
+// Before a step function whose body contains a `near` loop, the neighbour
+// type is binned (unless its positions have not changed since the last
+// binning):
+//   1. assign   cell index per agent, atomically counted per cell; the
+//               largest |coordinate| is reduced for the radius prefilter;
+//   2. scan     exclusive prefix sum of the cell counts -> cell_start;
+//   3. scatter  counting-sort placement: slot = cell_start[cell] + rank;
+//   4. gather   slot-ordered copies of the position (as float, for the
+//               prefilter) and of the members the near loops read;
+//   5. lists    (ordered bodies only) per cell, the slots of all agents in
+//               the surrounding cells sorted by agent id, so that the loop
+//               body sees neighbours in the reference's ascending index order.
+// Every buffer is sized from the agent count and the grid at upload time, so
+// a timestep needs no host synchronisation and is captured once into a CUDA
+// graph that abl_run replays.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "abl_device.cuh"
+#include "abl_model.h"
+
+namespace {
+
+constexpr int kScanBlock = 1024;
+constexpr int kListWarpsPerBlock = 8;
+constexpr int kListCap = 256;  // candidates staged in shared memory per warp
+
+#define ABL_CUDA_TRY(expr)                                                   \
+  do {                                                                       \
+    cudaError_t e_ = (expr);                                                 \
+    if (e_ != cudaSuccess) {                                                 \
+      std::fprintf(stderr, "openabl-cuda: %s failed: %s (%s:%d)\n", #expr,   \
+                   cudaGetErrorString(e_), __FILE__, __LINE__);              \
+      return ABL_E_CUDA;                                                     \
+    }                                                                        \
+  } while (0)
+
+#define ABL_TRY(expr)          \
+  do {                         \
+    int r_ = (expr);           \
+    if (r_ != ABL_OK) return r_; \
+  } while (0)
+
+// ------------------------------------------------------------------ scan
+
+// Inclusive scan of one block of kScanBlock ints (4 per thread, warp
+// shuffles), writing the block total to block_sums.
+__global__ void k_scan_blocks(const int *in, int *out, long m, int *block_sums) {
+  __shared__ int warp_tot[kScanBlock / 4 / 32];
+  long base = (long) blockIdx.x * kScanBlock;
+  int t = threadIdx.x;
+  int v[4];
+  int run = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    long i = base + 4 * t + k;
+    v[k] = i < m ? in[i] : 0;
+    run += v[k];
+  }
+  int lane = t & 31, w = t >> 5;
+  int incl = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int nw = blockDim.x / 32;
+    int x = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane < nw) warp_tot[lane] = x;
+  }
+  __syncthreads();
+  int prefix = (w > 0 ? warp_tot[w - 1] : 0) + incl - run;  // exclusive for this thread
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    long i = base + 4 * t + k;
+    prefix += v[k];
+    if (i < m) out[i] = prefix;  // inclusive
+  }
+  if (t == blockDim.x - 1) block_sums[blockIdx.x] = warp_tot[blockDim.x / 32 - 1];
+}
+
+// Turns per-block inclusive scans into a global exclusive scan with total.
+__global__ void k_scan_finish(const int *incl, int *out_excl, long m, const int *block_offsets) {
+  long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > m) return;
+  if (i == 0) {
+    out_excl[0] = 0;
+    return;
+  }
+  long j = i - 1;
+  out_excl[i] = incl[j] + block_offsets[j / kScanBlock];
+}
+
+// Scan plan for an exclusive scan of m ints.  Level l scans its input in
+// blocks (incl), collects the block totals (sums) and obtains the block
+// offsets (offs, nb + 1 entries) by scanning the totals one level up.
+struct ScanLevel {
+  long m = 0, nb = 0;
+  int *incl = nullptr, *sums = nullptr, *offs = nullptr;
+};
+struct ScanPlan {
+  std::vector<ScanLevel> levels;
+};
+
+// ------------------------------------------------------------ binning
+
+template <typename Real, int DIM>
+__global__ void k_bin_assign(const Real *pos, long n, int nx, int ny, int nz, double lo0,
+                             double lo1, double lo2, double inv_cell, int *cell_of,
+                             int *cell_count, int *local_rank, float *amax, int *error) {
+  long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  float m = 0.0f;
+  if (i < n) {
+    const double lo[3] = {lo0, lo1, lo2};
+    const int dims[3] = {nx, ny, nz};
+    int c[3] = {0, 0, 0};
+    bool finite = true;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      double x = (double) pos[DIM * i + d];
+      finite = finite && isfinite(x);
+      c[d] = abl::cell_coord(x, lo[d], inv_cell, dims[d]);
+      m = fmaxf(m, fabsf((float) x));
+    }
+    if (!finite) atomicExch(error, ABL_E_NONFINITE);
+    int cell = (c[2] * ny + c[1]) * nx + c[0];
+    cell_of[i] = cell;
+    local_rank[i] = atomicAdd(&cell_count[cell], 1);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0f) abl::atomic_max_nonneg(amax, m);
+}
+
+__global__ void k_bin_scatter(long n, const int *cell_of, const int *local_rank,
+                              const int *cell_start, int *order) {
+  long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  order[cell_start[cell_of[i]] + local_rank[i]] = (int) i;
+}
+
+// Largest |coordinate| of a type that is not binned (query side only).
+template <typename Real, int DIM>
+__global__ void k_amax(const Real *pos, long n, float *amax, int *error) {
+  long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  float m = 0.0f;
+  if (i < n) {
+    bool finite = true;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      double x = (double) pos[DIM * i + d];
+      finite = finite && isfinite(x);
+      m = fmaxf(m, fabsf((float) x));
+    }
+    if (!finite) atomicExch(error, ABL_E_NONFINITE);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0f) abl::atomic_max_nonneg(amax, m);
+}
+
+__global__ void k_max2(const float *a, const float *b, float *out) {
+  *out = fmaxf(*a, *b);
+}
+
+// Slot-ordered copies: float positions and the requested member columns.
+struct GatherArgs {
+  int nmem;
+  const void *src[ABL_MAX_MEMBERS];
+  void *dst[ABL_MAX_MEMBERS];
+  int bytes[ABL_MAX_MEMBERS];
+};
+
+template <typename Real, int DIM>
+__global__ void k_gather(long n, const int *order, const Real *pos, float *posf,
+                         const __grid_constant__ GatherArgs g) {
+  long s = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  long i = order[s];
+#pragma unroll
+  for (int d = 0; d < DIM; d++) posf[DIM * s + d] = (float) pos[DIM * i + d];
+  for (int k = 0; k < g.nmem; k++) {
+    int b = g.bytes[k];
+    if ((b & 7) == 0) {
+      const uint64_t *src = (const uint64_t *) g.src[k] + (b / 8) * i;
+      uint64_t *dst = (uint64_t *) g.dst[k] + (b / 8) * s;
+      for (int w = 0; w < b / 8; w++) dst[w] = src[w];
+    } else if ((b & 3) == 0) {
+      const uint32_t *src = (const uint32_t *) g.src[k] + (b / 4) * i;
+      uint32_t *dst = (uint32_t *) g.dst[k] + (b / 4) * s;
+      for (int w = 0; w < b / 4; w++) dst[w] = src[w];
+    } else {
+      const uint8_t *src = (const uint8_t *) g.src[k] + b * i;
+      uint8_t *dst = (uint8_t *) g.dst[k] + b * s;
+      for (int w = 0; w < b; w++) dst[w] = src[w];
+    }
+  }
+}
+
+// Per cell: number of candidates in the surrounding (2R+1)^DIM cells.
+template <int DIM>
+__global__ void k_nb_count(int nx, int ny, int nz, int R, const int *cell_start, int *nb_cnt,
+                           int skip_empty) {
+  long c = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  long ncells = (long) nx * ny * nz;
+  if (c >= ncells) return;
+  if (skip_empty && cell_start[c + 1] == cell_start[c]) {
+    nb_cnt[c] = 0;
+    return;
+  }
+  int cx = c % nx, cy = (c / nx) % ny, cz = c / ((long) nx * ny);
+  int x0 = max(cx - R, 0), x1 = min(cx + R, nx - 1);
+  int cnt = 0;
+  for (int z = (DIM == 3 ? max(cz - R, 0) : 0); z <= (DIM == 3 ? min(cz + R, nz - 1) : 0); z++) {
+    for (int y = max(cy - R, 0); y <= min(cy + R, ny - 1); y++) {
+      long base = ((long) z * ny + y) * nx;
+      cnt += cell_start[base + x1 + 1] - cell_start[base + x0];
+    }
+  }
+  nb_cnt[c] = cnt;
+}
+
+// Per cell (one warp each): the candidate slots sorted by agent id.  Up to
+// kListCap candidates are ranked in shared memory; larger neighbourhoods are
+// ranked straight from global memory (same result, slower).
+template <int DIM>
+__global__ void k_nb_build(int nx, int ny, int nz, int R, const int *cell_start,
+                           const int *order, const int *nb_off, int *nb_list) {
+  __shared__ int s_id[kListWarpsPerBlock][kListCap];
+  __shared__ int s_slot[kListWarpsPerBlock][kListCap];
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  long c = (long) blockIdx.x * kListWarpsPerBlock + w;
+  long ncells = (long) nx * ny * nz;
+  if (c >= ncells) return;
+  int base_out = nb_off[c];
+  int count = nb_off[c + 1] - base_out;
+  if (count == 0) return;
+  int cx = c % nx, cy = (c / nx) % ny, cz = c / ((long) nx * ny);
+  int x0 = max(cx - R, 0), x1 = min(cx + R, nx - 1);
+  int z0 = DIM == 3 ? max(cz - R, 0) : 0, z1 = DIM == 3 ? min(cz + R, nz - 1) : 0;
+  int y0 = max(cy - R, 0), y1 = min(cy + R, ny - 1);
+  if (count <= kListCap) {
+    int k = 0;
+    for (int z = z0; z <= z1; z++) {
+      for (int y = y0; y <= y1; y++) {
+        long rb = ((long) z * ny + y) * nx;
+        int s = cell_start[rb + x0], e = cell_start[rb + x1 + 1];
+        for (int j = lane; j < e - s; j += 32) {
+          s_id[w][k + j] = order[s + j];
+          s_slot[w][k + j] = s + j;
+        }
+        k += e - s;
+      }
+    }
+    __syncwarp();
+    for (int e = lane; e < count; e += 32) {
+      int id = s_id[w][e];
+      int r = 0;
+      for (int f = 0; f < count; f++) r += s_id[w][f] < id;
+      nb_list[base_out + r] = s_slot[w][e];
+    }
+    return;
+  }
+  // Large neighbourhood: element e is addressed by walking the rows.
+  for (int e = lane; e < count; e += 32) {
+    int se = -1, k = 0;
+    for (int z = z0; z <= z1 && se < 0; z++) {
+      for (int y = y0; y <= y1; y++) {
+        long rb = ((long) z * ny + y) * nx;
+        int s = cell_start[rb + x0], len = cell_start[rb + x1 + 1] - s;
+        if (e < k + len) {
+          se = s + (e - k);
+          break;
+        }
+        k += len;
+      }
+    }
+    int id = order[se];
+    int r = 0;
+    for (int z = z0; z <= z1; z++) {
+      for (int y = y0; y <= y1; y++) {
+        long rb = ((long) z * ny + y) * nx;
+        int s = cell_start[rb + x0], e2 = cell_start[rb + x1 + 1];
+        for (int j = s; j < e2; j++) r += order[j] < id;
+      }
+    }
+    nb_list[base_out + r] = se;
+  }
+}
+
+// --------------------------------------------------------------- state
+
+struct TypeState {
+  const abl_agent_desc *d = nullptr;
+  long n = 0;
+  bool uploaded = false;
+  void *cols[2][ABL_MAX_MEMBERS] = {};
+  int cur = 0;
+  float *amax = nullptr;  // this type's largest |coordinate| (device)
+
+  // binning (near types only)
+  bool is_near = false;
+  bool ordered = false;     // some near loop over this type needs id order
+  bool dirty = true;
+  int R = 1;
+  int nx = 1, ny = 1, nz = 1;
+  long ncells = 1;
+  double lo[3] = {0, 0, 0};
+  double inv_cell = 1.0;
+  uint32_t gather_mask = 0;
+  int *cell_count = nullptr, *cell_start = nullptr, *local_rank = nullptr, *cell_of = nullptr;
+  int *order = nullptr;
+  float *posf = nullptr;
+  void *gcols[ABL_MAX_MEMBERS] = {};
+  int *nb_cnt = nullptr, *nb_off = nullptr, *nb_list = nullptr;
+  ScanPlan cell_scan, nb_scan;
+  std::vector<void *> bin_allocs;  // freed when the type is re-uploaded
+};
+
+size_t member_bytes(const abl_member_desc &m) {
+  return (size_t) m.components * m.scalar_bytes;
+}
+
+}  // namespace
+
+struct abl_ctx {
+  const abl_model_desc *model = nullptr;
+  std::vector<unsigned char> globals;
+  cudaStream_t stream = nullptr;
+  std::vector<TypeState> types;
+  size_t budget = 0, used = 0;
+  std::vector<void *> allocations;
+  std::vector<size_t> sizes;
+  int *error = nullptr;
+  float *amax_pair = nullptr;  // per step: max of query and neighbour amax
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_exec = 0.0;
+  long launches = 0, last_launches = 0;
+  // Captured two-timestep graphs, keyed by the buffer parity and binning
+  // state they start from (kernel arguments depend on both).
+  struct Graph {
+    std::vector<int> key;
+    cudaGraphExec_t exec = nullptr;
+    long launches = 0;
+  };
+  std::vector<Graph> graphs;
+  bool prepared = false;
+  // Optional per-step-function kernel timing (eager timesteps only).
+  bool profile = false;
+  std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
+  std::vector<double> prof_seconds;
+  std::vector<long> prof_launches;
+};
+
+namespace {
+
+int dev_alloc(abl_ctx *ctx, void **p, size_t bytes, std::vector<void *> *owner = nullptr) {
+  if (bytes == 0) bytes = 16;
+  bytes = (bytes + 255) & ~(size_t) 255;
+  if (ctx->budget && ctx->used + bytes > ctx->budget) return ABL_E_BUDGET;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "openabl-cuda: cudaMalloc(%zu) failed: %s\n", bytes,
+                 cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? ABL_E_BUDGET : ABL_E_CUDA;
+  }
+  ctx->used += bytes;
+  ctx->allocations.push_back(*p);
+  ctx->sizes.push_back(bytes);
+  if (owner) owner->push_back(*p);
+  return ABL_OK;
+}
+
+void dev_free(abl_ctx *ctx, void *p) {
+  for (size_t k = 0; k < ctx->allocations.size(); k++) {
+    if (ctx->allocations[k] == p) {
+      cudaFree(p);
+      ctx->used -= ctx->sizes[k];
+      ctx->allocations.erase(ctx->allocations.begin() + k);
+      ctx->sizes.erase(ctx->sizes.begin() + k);
+      return;
+    }
+  }
+}
+
+template <typename T>
+int dev_alloc_t(abl_ctx *ctx, T **p, size_t count, std::vector<void *> *owner = nullptr) {
+  void *v = nullptr;
+  int r = dev_alloc(ctx, &v, count * sizeof(T), owner);
+  *p = (T *) v;
+  return r;
+}
+
+int scan_plan(abl_ctx *ctx, ScanPlan &p, long m, std::vector<void *> *owner) {
+  p.levels.clear();
+  long len = m;
+  for (;;) {
+    ScanLevel L;
+    L.m = len;
+    L.nb = std::max<long>(1, (len + kScanBlock - 1) / kScanBlock);
+    ABL_TRY(dev_alloc_t(ctx, &L.incl, std::max<long>(len, 1), owner));
+    ABL_TRY(dev_alloc_t(ctx, &L.sums, L.nb, owner));
+    ABL_TRY(dev_alloc_t(ctx, &L.offs, L.nb + 1, owner));
+    p.levels.push_back(L);
+    if (L.nb == 1) break;
+    len = L.nb;
+  }
+  return ABL_OK;
+}
+
+void scan_level(abl_ctx *ctx, const ScanPlan &p, size_t l, const int *in, int *out) {
+  const ScanLevel &L = p.levels[l];
+  cudaStream_t s = ctx->stream;
+  k_scan_blocks<<<L.nb, kScanBlock / 4, 0, s>>>(in, L.incl, L.m, L.sums);
+  ctx->launches++;
+  if (L.nb == 1) {
+    cudaMemsetAsync(L.offs, 0, sizeof(int), s);
+  } else {
+    scan_level(ctx, p, l + 1, L.sums, L.offs);
+  }
+  k_scan_finish<<<(L.m + 1 + 255) / 256, 256, 0, s>>>(L.incl, out, L.m, L.offs);
+  ctx->launches++;
+}
+
+// Exclusive scan of `in` (m ints) into `out` (m + 1 ints, out[m] = total).
+void scan_run(abl_ctx *ctx, const ScanPlan &p, const int *in, int *out) {
+  scan_level(ctx, p, 0, in, out);
+}
+
+
+inline long blocks_for(long n, int block) { return std::max<long>(1, (n + block - 1) / block); }
+
+const abl_member_desc &pos_member(const TypeState &t) {
+  return t.d->members[t.d->position_member];
+}
+
+bool pos_is_double(const TypeState &t) { return pos_member(t).scalar_bytes == 8; }
+
+// Largest near radius over the step functions that iterate type `ti`.
+double max_radius_for(const abl_ctx *ctx, int ti) {
+  double r = 0.0;
+  for (int k = 0; k < ctx->model->num_steps; k++) {
+    const abl_step_desc &sd = ctx->model->steps[k];
+    if (sd.near_type == ti && sd.radius) r = std::max(r, sd.radius(ctx->globals.data()));
+  }
+  return r;
+}
+
+void free_bins(abl_ctx *ctx, TypeState &t) {
+  for (void *p : t.bin_allocs) dev_free(ctx, p);
+  t.bin_allocs.clear();
+  t.cell_scan.levels.clear();
+  t.nb_scan.levels.clear();
+  t.cell_count = t.cell_start = t.local_rank = t.cell_of = t.order = nullptr;
+  t.nb_cnt = t.nb_off = t.nb_list = nullptr;
+  t.posf = nullptr;
+  for (auto &g : t.gcols) g = nullptr;
+}
+
+// Sizes the grid of every neighbour type from the environment and the
+// granularity (src/AnalysisVisitor.cpp:1378-1399: explicit, or the largest
+// constant near radius) and allocates the binning buffers.
+int prepare(abl_ctx *ctx) {
+  const abl_model_desc *m = ctx->model;
+  const void *G = ctx->globals.data();
+  double emin[3] = {0, 0, 0}, emax[3] = {0, 0, 0};
+  if (m->env_bounds) m->env_bounds(G, emin, emax);
+  for (int ti = 0; ti < m->num_agent_types; ti++) {
+    TypeState &t = ctx->types[ti];
+    free_bins(ctx, t);
+    t.is_near = false;
+    t.ordered = false;
+    t.gather_mask = 0;
+    for (int k = 0; k < m->num_steps; k++) {
+      const abl_step_desc &sd = m->steps[k];
+      if (sd.near_type != ti) continue;
+      t.is_near = true;
+      t.ordered = t.ordered || sd.ordered;
+      t.gather_mask |= sd.near_members;
+    }
+    if (!t.amax) ABL_TRY(dev_alloc_t(ctx, &t.amax, 1));
+    if (!t.is_near) continue;
+    if (t.d->position_member < 0) return ABL_E_UNSUPPORTED;
+    int dim = t.d->dim;
+    double gran = m->granularity ? m->granularity(G) : max_radius_for(ctx, ti);
+    double rmax = max_radius_for(ctx, ti);
+    if (!(gran > 0.0) || !std::isfinite(gran)) return ABL_E_INVALID;
+    // Cells slightly wider than the granularity: a pair that passes the
+    // float-rounded radius test lies within one cell width (see
+    // abl_device.cuh), with room for rounding in the cell computation.
+    double cell = gran * (1.0 + 1.0 / 1024.0);
+    t.R = std::max(1, (int) std::ceil(rmax * (1.0 + 1e-6) / cell));
+    t.inv_cell = 1.0 / cell;
+    int dims[3] = {1, 1, 1};
+    for (int d = 0; d < 3; d++) {
+      if (d < dim) {
+        double ext = emax[d] - emin[d];
+        if (!(ext >= 0.0) || !std::isfinite(ext)) return ABL_E_INVALID;
+        double k = std::floor(ext * t.inv_cell) + 1.0;
+        if (k > 1 << 24) return ABL_E_UNSUPPORTED;
+        dims[d] = (int) k;
+        t.lo[d] = emin[d];
+      } else {
+        t.lo[d] = 0.0;
+      }
+    }
+    t.nx = dims[0];
+    t.ny = dims[1];
+    t.nz = dims[2];
+    t.ncells = (long) t.nx * t.ny * t.nz;
+    if (t.ncells > (1L << 30)) return ABL_E_UNSUPPORTED;
+    long n = std::max<long>(t.n, 1);
+    auto *own = &t.bin_allocs;
+    ABL_TRY(dev_alloc_t(ctx, &t.cell_count, t.ncells, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.cell_start, t.ncells + 1, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.local_rank, n, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.cell_of, n, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.order, n, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.posf, n * dim, own));
+    ABL_TRY(scan_plan(ctx, t.cell_scan, t.ncells, own));
+    for (int k = 0; k < t.d->num_members; k++) {
+      if (t.gather_mask & (1u << k)) {
+        void *p = nullptr;
+        ABL_TRY(dev_alloc(ctx, &p, member_bytes(t.d->members[k]) * n, own));
+        t.gcols[k] = p;
+      }
+    }
+    if (t.ordered) {
+      long span = 2 * t.R + 1;
+      long per_agent = dim == 3 ? span * span * span : span * span;
+      ABL_TRY(dev_alloc_t(ctx, &t.nb_cnt, t.ncells, own));
+      ABL_TRY(dev_alloc_t(ctx, &t.nb_off, t.ncells + 1, own));
+      ABL_TRY(dev_alloc_t(ctx, &t.nb_list, per_agent * n, own));
+      ABL_TRY(scan_plan(ctx, t.nb_scan, t.ncells, own));
+    }
+    t.dirty = true;
+  }
+  if (!ctx->amax_pair) ABL_TRY(dev_alloc_t(ctx, &ctx->amax_pair, 1));
+  ctx->prepared = true;
+  return ABL_OK;
+}
+
+template <typename Real>
+void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
+  cudaStream_t s = ctx->stream;
+  const int B = 256;
+  long nb = blocks_for(t.n, B);
+  const Real *pos = (const Real *) t.cols[t.cur][t.d->position_member];
+  cudaMemsetAsync(t.cell_count, 0, sizeof(int) * t.ncells, s);
+  cudaMemsetAsync(t.amax, 0, sizeof(float), s);
+  if (dim == 2) {
+    k_bin_assign<Real, 2><<<nb, B, 0, s>>>(pos, t.n, t.nx, t.ny, t.nz, t.lo[0], t.lo[1], t.lo[2],
+                                           t.inv_cell, t.cell_of, t.cell_count, t.local_rank,
+                                           t.amax, ctx->error);
+  } else {
+    k_bin_assign<Real, 3><<<nb, B, 0, s>>>(pos, t.n, t.nx, t.ny, t.nz, t.lo[0], t.lo[1], t.lo[2],
+                                           t.inv_cell, t.cell_of, t.cell_count, t.local_rank,
+                                           t.amax, ctx->error);
+  }
+  ctx->launches++;
+  scan_run(ctx, t.cell_scan, t.cell_count, t.cell_start);
+  k_bin_scatter<<<nb, B, 0, s>>>(t.n, t.cell_of, t.local_rank, t.cell_start, t.order);
+  ctx->launches++;
+  GatherArgs g;
+  std::memset(&g, 0, sizeof g);
+  for (int k = 0; k < t.d->num_members; k++) {
+    if (!(t.gather_mask & (1u << k))) continue;
+    g.src[g.nmem] = t.cols[t.cur][k];
+    g.dst[g.nmem] = t.gcols[k];
+    g.bytes[g.nmem] = (int) member_bytes(t.d->members[k]);
+    g.nmem++;
+  }
+  if (dim == 2) {
+    k_gather<Real, 2><<<nb, B, 0, s>>>(t.n, t.order, pos, t.posf, g);
+  } else {
+    k_gather<Real, 3><<<nb, B, 0, s>>>(t.n, t.order, pos, t.posf, g);
+  }
+  ctx->launches++;
+  if (t.ordered) {
+    long cb = blocks_for(t.ncells, B);
+    int skip_empty = 0;  // lists for every cell: query agents may be of another type
+    if (dim == 2) {
+      k_nb_count<2><<<cb, B, 0, s>>>(t.nx, t.ny, t.nz, t.R, t.cell_start, t.nb_cnt, skip_empty);
+    } else {
+      k_nb_count<3><<<cb, B, 0, s>>>(t.nx, t.ny, t.nz, t.R, t.cell_start, t.nb_cnt, skip_empty);
+    }
+    ctx->launches++;
+    scan_run(ctx, t.nb_scan, t.nb_cnt, t.nb_off);
+    long lb = blocks_for(t.ncells, kListWarpsPerBlock);
+    if (dim == 2) {
+      k_nb_build<2><<<lb, 32 * kListWarpsPerBlock, 0, s>>>(t.nx, t.ny, t.nz, t.R, t.cell_start,
+                                                           t.order, t.nb_off, t.nb_list);
+    } else {
+      k_nb_build<3><<<lb, 32 * kListWarpsPerBlock, 0, s>>>(t.nx, t.ny, t.nz, t.R, t.cell_start,
+                                                           t.order, t.nb_off, t.nb_list);
+    }
+    ctx->launches++;
+  }
+}
+
+void bin_type(abl_ctx *ctx, TypeState &t) {
+  if (pos_is_double(t)) {
+    launch_bin<double>(ctx, t, t.d->dim);
+  } else {
+    launch_bin<float>(ctx, t, t.d->dim);
+  }
+  t.dirty = false;
+}
+
+void type_amax(abl_ctx *ctx, TypeState &t) {
+  cudaStream_t s = ctx->stream;
+  const int B = 256;
+  cudaMemsetAsync(t.amax, 0, sizeof(float), s);
+  long nb = blocks_for(t.n, B);
+  const void *pos = t.cols[t.cur][t.d->position_member];
+  bool dbl = pos_is_double(t);
+  if (t.d->dim == 2) {
+    if (dbl) k_amax<double, 2><<<nb, B, 0, s>>>((const double *) pos, t.n, t.amax, ctx->error);
+    else k_amax<float, 2><<<nb, B, 0, s>>>((const float *) pos, t.n, t.amax, ctx->error);
+  } else {
+    if (dbl) k_amax<double, 3><<<nb, B, 0, s>>>((const double *) pos, t.n, t.amax, ctx->error);
+    else k_amax<float, 3><<<nb, B, 0, s>>>((const float *) pos, t.n, t.amax, ctx->error);
+  }
+  ctx->launches++;
+}
+
+// One iteration of the simulate loop (src/backend/CPrinter.cpp:189-233).
+int step_once(abl_ctx *ctx) {
+  const abl_model_desc *m = ctx->model;
+  for (int k = 0; k < m->num_steps; k++) {
+    const abl_step_desc &sd = m->steps[k];
+    TypeState &t = ctx->types[sd.agent_type];
+    abl_step_launch L;
+    std::memset(&L, 0, sizeof L);
+    L.n = t.n;
+    L.globals = ctx->globals.data();
+    L.error = ctx->error;
+    L.block = 128;
+    for (int j = 0; j < t.d->num_members; j++) {
+      L.in_cols[j] = t.cols[t.cur][j];
+      L.out_cols[j] = t.cols[1 - t.cur][j];
+    }
+    if (sd.near_type >= 0) {
+      TypeState &nt = ctx->types[sd.near_type];
+      if (nt.dirty) bin_type(ctx, nt);
+      abl_near_view &V = L.near;
+      V.dim = nt.d->dim;
+      V.ordered = sd.ordered;
+      V.range = nt.R;
+      V.nx = nt.nx;
+      V.ny = nt.ny;
+      V.nz = nt.nz;
+      for (int d = 0; d < 3; d++) V.lo[d] = nt.lo[d];
+      V.inv_cell = nt.inv_cell;
+      V.radius = sd.radius(ctx->globals.data());
+      V.n = nt.n;
+      V.cell_start = nt.cell_start;
+      V.order = nt.order;
+      V.posf = nt.posf;
+      V.nb_off = nt.nb_off;
+      V.nb_list = nt.nb_list;
+      for (int j = 0; j < nt.d->num_members; j++) V.cols[j] = nt.gcols[j];
+      if (sd.agent_type == sd.near_type) {
+        V.amax = nt.amax;
+        L.visit_order = nt.order;
+      } else {
+        if (t.d->position_member >= 0 && t.n > 0) {
+          type_amax(ctx, t);
+          k_max2<<<1, 1, 0, ctx->stream>>>(t.amax, nt.amax, ctx->amax_pair);
+          ctx->launches++;
+          V.amax = ctx->amax_pair;
+        } else {
+          V.amax = nt.amax;
+        }
+      }
+    }
+    if (t.n > 0) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      cudaStreamIsCapturing(ctx->stream, &cs);
+      bool timed = ctx->profile && cs == cudaStreamCaptureStatusNone;
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      if (timed) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, ctx->stream);
+      }
+      ABL_TRY(sd.launch(&L, ctx->stream));
+      ctx->launches++;
+      if (timed) {
+        cudaEventRecord(e1, ctx->stream);
+        ctx->prof_pending[k].push_back({e0, e1});
+      }
+    }
+    t.cur = 1 - t.cur;  // swap agents_X and agents_X_dbuf
+    t.dirty = true;
+  }
+  return ABL_OK;
+}
+
+int check_error(abl_ctx *ctx) {
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  int h = 0;
+  ABL_CUDA_TRY(cudaMemcpy(&h, ctx->error, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h != 0) {
+    int zero = 0;
+    cudaMemcpy(ctx->error, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    return h;
+  }
+  return ABL_OK;
+}
+
+void drop_graph(abl_ctx *ctx) {
+  for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.exec);
+  ctx->graphs.clear();
+}
+
+std::vector<int> graph_key(const abl_ctx *ctx) {
+  std::vector<int> key;
+  for (const TypeState &t : ctx->types) {
+    key.push_back(t.cur);
+    key.push_back(t.dirty ? 1 : 0);
+  }
+  return key;
+}
+
+// Collects finished per-kernel timings.
+void collect_profile(abl_ctx *ctx) {
+  for (size_t k = 0; k < ctx->prof_pending.size(); k++) {
+    for (auto &ev : ctx->prof_pending[k]) {
+      float ms = 0.0f;
+      if (cudaEventElapsedTime(&ms, ev.first, ev.second) == cudaSuccess) {
+        ctx->prof_seconds[k] += ms / 1000.0;
+        ctx->prof_launches[k]++;
+      }
+      cudaEventDestroy(ev.first);
+      cudaEventDestroy(ev.second);
+    }
+    ctx->prof_pending[k].clear();
+  }
+}
+
+// Captures two timesteps (so that every double buffer returns to the same
+// parity) into a CUDA graph, or returns the one captured from this state.
+int capture_graph(abl_ctx *ctx, abl_ctx::Graph **out) {
+  std::vector<int> key = graph_key(ctx);
+  for (auto &g : ctx->graphs) {
+    if (g.key == key) {
+      *out = &g;
+      return ABL_OK;
+    }
+  }
+  abl_ctx::Graph G;
+  G.key = key;
+  cudaGraph_t g = nullptr;
+  long before = ctx->launches;
+  ABL_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int r = step_once(ctx);
+  if (r == ABL_OK) r = step_once(ctx);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (r != ABL_OK) {
+    if (g) cudaGraphDestroy(g);
+    return r;
+  }
+  ABL_CUDA_TRY(e);
+  e = cudaGraphInstantiate(&G.exec, g, 0);
+  cudaGraphDestroy(g);
+  ABL_CUDA_TRY(e);
+  G.launches = ctx->launches - before;
+  ctx->launches = before;
+  // Capturing does not run anything: restore the state the graph starts from.
+  for (size_t k = 0; k < ctx->types.size(); k++) {
+    ctx->types[k].cur = key[2 * k];
+    ctx->types[k].dirty = key[2 * k + 1] != 0;
+  }
+  ctx->graphs.push_back(G);
+  *out = &ctx->graphs.back();
+  return ABL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+extern const abl_model_desc *const abl_builtin_models[];
+
+const abl_model_desc *abl_model_lookup(const char *name) {
+  if (!name) return nullptr;
+  for (int k = 0; abl_builtin_models[k]; k++) {
+    if (std::strcmp(abl_builtin_models[k]->name, name) == 0) return abl_builtin_models[k];
+  }
+  return nullptr;
+}
+
+int abl_model_num_agent_types(const abl_model_desc *m) { return m ? m->num_agent_types : ABL_E_INVALID; }
+
+const char *abl_model_agent_name(const abl_model_desc *m, int type_id) {
+  if (!m || type_id < 0 || type_id >= m->num_agent_types) return nullptr;
+  return m->agents[type_id].name;
+}
+
+int abl_model_num_members(const abl_model_desc *m, int type_id) {
+  if (!m || type_id < 0 || type_id >= m->num_agent_types) return ABL_E_INVALID;
+  return m->agents[type_id].num_members;
+}
+
+int abl_model_member(const abl_model_desc *m, int type_id, int member, const char **name,
+                     int *value_type) {
+  if (!m || type_id < 0 || type_id >= m->num_agent_types) return ABL_E_INVALID;
+  const abl_agent_desc &a = m->agents[type_id];
+  if (member < 0 || member >= a.num_members) return ABL_E_INVALID;
+  if (name) *name = a.members[member].name;
+  if (value_type) *value_type = a.members[member].value_type;
+  return ABL_OK;
+}
+
+size_t abl_model_globals_size(const abl_model_desc *m) { return m ? m->globals_size : 0; }
+
+int abl_model_globals_default(const abl_model_desc *m, void *out) {
+  if (!m || !out) return ABL_E_INVALID;
+  std::memcpy(out, m->globals_default, m->globals_size);
+  return ABL_OK;
+}
+
+int abl_model_global(const abl_model_desc *m, const char *name, size_t *offset, int *value_type) {
+  if (!m || !name) return ABL_E_INVALID;
+  for (int k = 0; k < m->num_globals; k++) {
+    if (std::strcmp(m->globals[k].name, name) == 0) {
+      if (offset) *offset = m->globals[k].offset;
+      if (value_type) *value_type = m->globals[k].value_type;
+      return ABL_OK;
+    }
+  }
+  return ABL_E_INVALID;
+}
+
+int abl_create(const abl_model_desc *model, size_t hbm_budget, abl_ctx **out) {
+  if (!model || !out) return ABL_E_INVALID;
+  if (model->num_agent_types <= 0) return ABL_E_INVALID;
+  abl_ctx *ctx = new abl_ctx;
+  ctx->model = model;
+  ctx->budget = hbm_budget;
+  ctx->globals.assign((const unsigned char *) model->globals_default,
+                      (const unsigned char *) model->globals_default + model->globals_size);
+  ctx->types.resize(model->num_agent_types);
+  for (int k = 0; k < model->num_agent_types; k++) {
+    ctx->types[k].d = &model->agents[k];
+    if (model->agents[k].num_members > ABL_MAX_MEMBERS) {
+      delete ctx;
+      return ABL_E_UNSUPPORTED;
+    }
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "openabl-cuda: context setup failed: %s\n", cudaGetErrorString(e));
+    delete ctx;
+    return ABL_E_CUDA;
+  }
+  int r = dev_alloc_t(ctx, &ctx->error, 1);
+  if (r == ABL_OK) r = cudaMemsetAsync(ctx->error, 0, sizeof(int), ctx->stream) == cudaSuccess
+                           ? ABL_OK : ABL_E_CUDA;
+  if (r != ABL_OK) {
+    abl_destroy(ctx);
+    return r;
+  }
+  *out = ctx;
+  return ABL_OK;
+}
+
+int abl_set_globals(abl_ctx *ctx, const void *globals, size_t size) {
+  if (!ctx || !globals || size != ctx->model->globals_size) return ABL_E_INVALID;
+  std::memcpy(ctx->globals.data(), globals, size);
+  ctx->prepared = false;
+  drop_graph(ctx);
+  return ABL_OK;
+}
+
+int abl_upload(abl_ctx *ctx, int type_id, const void *const *cols, size_t n) {
+  if (!ctx || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
+  if (n > (size_t) INT32_MAX) return ABL_E_UNSUPPORTED;
+  TypeState &t = ctx->types[type_id];
+  if (n > 0 && !cols) return ABL_E_INVALID;
+  // (Re)allocate both buffers when the count changes.
+  bool resized_alloc = !t.uploaded || (long) n != t.n;
+  if (resized_alloc) {
+    for (int b = 0; b < 2; b++) {
+      for (int k = 0; k < t.d->num_members; k++) {
+        if (t.cols[b][k]) dev_free(ctx, t.cols[b][k]);
+        t.cols[b][k] = nullptr;
+        ABL_TRY(dev_alloc(ctx, &t.cols[b][k], member_bytes(t.d->members[k]) * std::max<size_t>(n, 1)));
+      }
+    }
+  }
+  bool resized = resized_alloc;
+  t.n = (long) n;
+  t.cur = 0;
+  for (int k = 0; k < t.d->num_members; k++) {
+    size_t bytes = member_bytes(t.d->members[k]) * n;
+    if (bytes == 0) continue;
+    if (!cols[k]) return ABL_E_INVALID;
+    ABL_CUDA_TRY(cudaMemcpyAsync(t.cols[0][k], cols[k], bytes, cudaMemcpyHostToDevice, ctx->stream));
+    // The double buffer starts as a copy (CPrinter.cpp:210-213).
+    ABL_CUDA_TRY(cudaMemcpyAsync(t.cols[1][k], t.cols[0][k], bytes, cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
+  }
+  t.uploaded = true;
+  t.dirty = true;
+  if (resized) {
+    ctx->prepared = false;
+    drop_graph(ctx);
+  }
+  return ABL_OK;
+}
+
+static int ensure_ready(abl_ctx *ctx) {
+  for (auto &t : ctx->types) {
+    if (!t.uploaded) {
+      // Types never uploaded have no agents.
+      for (int b = 0; b < 2; b++)
+        for (int k = 0; k < t.d->num_members; k++)
+          if (!t.cols[b][k]) ABL_TRY(dev_alloc(ctx, &t.cols[b][k], member_bytes(t.d->members[k])));
+      t.n = 0;
+      t.uploaded = true;
+    }
+  }
+  if (!ctx->prepared) ABL_TRY(prepare(ctx));
+  return ABL_OK;
+}
+
+int abl_run(abl_ctx *ctx, int timesteps) {
+  if (!ctx || timesteps < 0) return ABL_E_INVALID;
+  ABL_TRY(ensure_ready(ctx));
+  long launches0 = ctx->launches;
+  ABL_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
+  int done = 0;
+  // The first timestep runs eagerly (it also settles which binnings are
+  // current); the rest replays a two-timestep graph.
+  if (timesteps > 0) {
+    ABL_TRY(step_once(ctx));
+    done = 1;
+  }
+  if (timesteps - done >= 2 && !ctx->profile) {
+    abl_ctx::Graph *G = nullptr;
+    std::vector<int> key = graph_key(ctx);
+    ABL_TRY(capture_graph(ctx, &G));
+    for (; done + 2 <= timesteps; done += 2) {
+      ABL_CUDA_TRY(cudaGraphLaunch(G->exec, ctx->stream));
+      ctx->launches += G->launches;
+    }
+    // Two timesteps swap every buffer an even number of times; the binning
+    // state after them is the one after the captured sequence.
+    (void) key;
+  }
+  for (; done < timesteps; done++) ABL_TRY(step_once(ctx));
+  ABL_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
+  int r = check_error(ctx);
+  collect_profile(ctx);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->last_exec = ms / 1000.0;
+  ctx->last_launches = ctx->launches - launches0;
+  return r;
+}
+
+int abl_step(abl_ctx *ctx) { return abl_run(ctx, 1); }
+
+int abl_count(abl_ctx *ctx, int type_id, size_t *n) {
+  if (!ctx || !n || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
+  *n = (size_t) ctx->types[type_id].n;
+  return ABL_OK;
+}
+
+int abl_download(abl_ctx *ctx, int type_id, void *const *cols, size_t *n) {
+  if (!ctx || !n || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
+  TypeState &t = ctx->types[type_id];
+  size_t cnt = (size_t) t.n;
+  if (*n < cnt) {
+    *n = cnt;
+    return ABL_E_INVALID;
+  }
+  for (int k = 0; k < t.d->num_members; k++) {
+    size_t bytes = member_bytes(t.d->members[k]) * cnt;
+    if (bytes == 0) continue;
+    if (!cols || !cols[k]) return ABL_E_INVALID;
+    ABL_CUDA_TRY(cudaMemcpyAsync(cols[k], t.cols[t.cur][k], bytes, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  }
+  *n = cnt;
+  return check_error(ctx);
+}
+
+int abl_reduce(abl_ctx *ctx, int kind, int type_id, int member, void *out) {
+  (void) kind;
+  (void) member;
+  if (!ctx || !out || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
+  if (kind == 0) {
+    *(int *) out = (int) ctx->types[type_id].n;
+    return ABL_OK;
+  }
+  return ABL_E_UNSUPPORTED;
+}
+
+int abl_last_exec_time(abl_ctx *ctx, double *seconds) {
+  if (!ctx || !seconds) return ABL_E_INVALID;
+  *seconds = ctx->last_exec;
+  return ABL_OK;
+}
+
+int abl_memory_used(abl_ctx *ctx, size_t *bytes) {
+  if (!ctx || !bytes) return ABL_E_INVALID;
+  *bytes = ctx->used;
+  return ABL_OK;
+}
+
+int abl_last_launch_count(abl_ctx *ctx, long *launches) {
+  if (!ctx || !launches) return ABL_E_INVALID;
+  *launches = ctx->last_launches;
+  return ABL_OK;
+}
+
+int abl_set_profiling(abl_ctx *ctx, int enable) {
+  if (!ctx) return ABL_E_INVALID;
+  ctx->profile = enable != 0;
+  size_t ns = (size_t) ctx->model->num_steps;
+  ctx->prof_pending.assign(ns, {});
+  ctx->prof_seconds.assign(ns, 0.0);
+  ctx->prof_launches.assign(ns, 0);
+  return ABL_OK;
+}
+
+int abl_step_kernel_time(abl_ctx *ctx, int step, double *seconds, long *launches) {
+  if (!ctx || step < 0 || step >= (int) ctx->prof_seconds.size()) return ABL_E_INVALID;
+  if (seconds) *seconds = ctx->prof_seconds[step];
+  if (launches) *launches = ctx->prof_launches[step];
+  return ABL_OK;
+}
+
+int abl_destroy(abl_ctx *ctx) {
+  if (!ctx) return ABL_E_INVALID;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  drop_graph(ctx);
+  for (void *p : ctx->allocations) cudaFree(p);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return ABL_OK;
+}
+
+const char *abl_strerror(int code) {
+  switch (code) {
+    case ABL_OK: return "ok";
+    case ABL_E_INVALID: return "invalid argument";
+    case ABL_E_BUDGET: return "device memory budget exhausted";
+    case ABL_E_CUDA: return "CUDA runtime error";
+    case ABL_E_TIMEOUT: return "bounded device wait timed out";
+    case ABL_E_NONFINITE: return "agent position is NaN or infinite";
+    case ABL_E_UNSUPPORTED: return "unsupported model feature";
+    case ABL_E_CAPACITY: return "agent capacity exceeded";
+    case ABL_E_NOMODEL: return "unknown model";
+    default: return "unknown error";
+  }
+}
+
+}  // extern "C"

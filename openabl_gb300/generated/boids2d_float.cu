@@ -1,0 +1,324 @@
+// Generated by OpenABL -b cuda (model "boids2d_float").
+#include "abl_gen.cuh"
+
+namespace abl_model_boids2d_float {
+
+typedef float abl_float;
+#include "abl_math.cuh"
+
+typedef struct {
+    float2 pos;
+    float2 velocity;
+} Boid;
+static const type_info Boid_info[] = {
+    { TYPE_FLOAT2, offsetof(Boid, pos), "pos", true },
+    { TYPE_FLOAT2, offsetof(Boid, velocity), "velocity", false },
+    { TYPE_END, sizeof(Boid), NULL }
+};
+
+struct agent_struct {
+    dyn_array agents_Boid;
+    dyn_array agents_Boid_dbuf;
+};
+static struct agent_struct agents;
+static const agent_info agents_info[] = {
+    { Boid_info, offsetof(struct agent_struct, agents_Boid), "Boid" },
+    { NULL, 0, NULL }
+};
+
+struct abl_globals {
+    float PI;
+    float interaction_radius;
+    float separation_radius;
+    float agent_density;
+    float time_scale;
+    float global_scale;
+    float steer_scale;
+    float collision_scale;
+    float match_scale;
+    int num_agents;
+    int num_timesteps;
+    float min_pos;
+    float max_pos;
+};
+static const abl_globals abl_globals_default = {
+    3.14159,
+    0.05,
+    0.005,
+    500.0,
+    0.0005,
+    0.15,
+    0.65,
+    0.75,
+    1.25,
+    5000,
+    100,
+    0.0,
+    3.16228,
+};
+static abl_globals abl_G = abl_globals_default;
+struct abl_cols_Boid {
+    float2 *pos;
+    float2 *velocity;
+};
+
+static inline float2 random_1(const abl_globals &abl_G, float2 min, float2 max) {
+    return float2_create(random_float(min.x, max.x), random_float(min.y, max.y));
+}
+static inline float3 random_2(const abl_globals &abl_G, float3 min, float3 max) {
+    return float3_create(random_float(min.x, max.x), random_float(min.y, max.y), random_float(min.z, max.z));
+}
+static inline float random_3(const abl_globals &abl_G, float max) {
+    return random_float(0, max);
+}
+static inline float2 random_4(const abl_globals &abl_G, float2 max) {
+    return random_1(abl_G, float2_fill(0), max);
+}
+static inline float3 random_5(const abl_globals &abl_G, float3 max) {
+    return random_2(abl_G, float3_fill(0), max);
+}
+static inline int randomInt_1(const abl_globals &abl_G, int max) {
+    return random_int(0, max);
+}
+__host__ __device__ static inline float clamp(const abl_globals &abl_G, float pos, float min, float max) {
+    return ((pos < min) ? min : ((pos > max) ? max : pos));
+}
+__host__ __device__ static inline float2 clamp_1(const abl_globals &abl_G, float2 pos, float2 min, float2 max) {
+    return float2_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)));
+}
+__host__ __device__ static inline float3 clamp_2(const abl_globals &abl_G, float3 pos, float3 min, float3 max) {
+    return float3_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)), ((pos.z < min.z) ? min.z : ((pos.z > max.z) ? max.z : pos.z)));
+}
+__host__ __device__ static inline float clamp_3(const abl_globals &abl_G, float pos, float max) {
+    return clamp(abl_G, pos, 0, max);
+}
+__host__ __device__ static inline float2 clamp_4(const abl_globals &abl_G, float2 pos, float2 max) {
+    return clamp_1(abl_G, pos, float2_fill(0), max);
+}
+__host__ __device__ static inline float3 clamp_5(const abl_globals &abl_G, float3 pos, float3 max) {
+    return clamp_2(abl_G, pos, float3_fill(0), max);
+}
+__host__ __device__ static inline float wraparound(const abl_globals &abl_G, float pos, float max) {
+    return ((pos < 0) ? (max + pos) : ((pos >= max) ? (pos - max) : pos));
+}
+__host__ __device__ static inline float2 wraparound_1(const abl_globals &abl_G, float2 pos, float2 max) {
+    return float2_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)));
+}
+__host__ __device__ static inline float3 wraparound_2(const abl_globals &abl_G, float3 pos, float3 max) {
+    return float3_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)), ((pos.z < 0) ? (max.z + pos.z) : ((pos.z >= max.z) ? (pos.z - max.z) : pos.z)));
+}
+__host__ __device__ static inline bool is_inside(const abl_globals &abl_G, float2 pos, float2 max) {
+    return ((((pos.x >= 0) && (pos.y >= 0)) && (pos.x <= max.x)) && (pos.y <= max.y));
+}
+__host__ __device__ static inline float2 boundPosition(const abl_globals &abl_G, float2 pos) {
+    return float2_create(((pos.x < abl_G.min_pos) ? abl_G.max_pos : ((pos.x > abl_G.max_pos) ? abl_G.min_pos : pos.x)), ((pos.y < abl_G.min_pos) ? abl_G.max_pos : ((pos.y > abl_G.max_pos) ? abl_G.min_pos : pos.y)));
+}
+__device__ static void update_boid(const abl_globals &abl_G, const abl_near_view &abl_NB, Boid* in, Boid* out) {
+    float2 global_velocity = float2_create(0, 0);
+    float2 global_center = float2_create(0, 0);
+    float2 collision_center = float2_create(0, 0);
+    int interaction_count = 0;
+    int collision_count = 0;
+    {
+        const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
+        abl::near_cursor<2> abl_c1(abl_NB, abl_q1);
+        auto abl_exact1 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, in->pos) > abl_G.interaction_radius);
+        };
+        while (abl_c1.fill(abl_q1, abl_exact1)) {
+            for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
+                const int abl_slot1 = abl_c1.buf[abl_k];
+                Boid abl_nx1;
+                abl_nx1.pos = ((const float2 *) abl_NB.cols[0])[abl_slot1];
+                abl_nx1.velocity = ((const float2 *) abl_NB.cols[1])[abl_slot1];
+                Boid* nx = &abl_nx1;
+                {
+                    global_center = float2_add(global_center, nx->pos);
+                    global_velocity = float2_add(global_velocity, nx->velocity);
+                    interaction_count += 1;
+                    float separation = dist_float2(in->pos, nx->pos);
+                    if ((separation < abl_G.separation_radius)) {
+                        collision_center = float2_add(collision_center, nx->pos);
+                        collision_count += 1;
+                    }
+                }
+            }
+        }
+    }
+    float2 velocity_change = float2_create(0, 0);
+    float2 steer_velocity = float2_create(0, 0);
+    if ((interaction_count > 0)) {
+        global_center = float2_div_scalar(global_center, interaction_count);
+        steer_velocity = float2_mul_scalar(float2_sub(global_center, in->pos), abl_G.steer_scale);
+    }
+    velocity_change = float2_add(velocity_change, steer_velocity);
+    float2 match_velocity = float2_create(0, 0);
+    if ((interaction_count > 0)) {
+        global_velocity = float2_div_scalar(global_velocity, interaction_count);
+        match_velocity = float2_mul_scalar(global_velocity, abl_G.match_scale);
+    }
+    velocity_change = float2_add(velocity_change, match_velocity);
+    float2 avoid_velocity = float2_create(0, 0);
+    if ((collision_count > 0)) {
+        collision_center = float2_div_scalar(collision_center, collision_count);
+        avoid_velocity = float2_mul_scalar(float2_sub(in->pos, collision_center), abl_G.collision_scale);
+    }
+    velocity_change = float2_add(velocity_change, avoid_velocity);
+    float2 new_velocity = float2_add(in->velocity, float2_mul_scalar(velocity_change, abl_G.global_scale));
+    float new_velocity_scale = length_float2(new_velocity);
+    if ((new_velocity_scale > 1)) {
+        new_velocity = float2_div_scalar(new_velocity, new_velocity_scale);
+    }
+    float2 new_pos = float2_add(in->pos, float2_mul_scalar(new_velocity, abl_G.time_scale));
+    new_pos = boundPosition(abl_G, new_pos);
+    out->pos = new_pos;
+    out->velocity = new_velocity;
+}
+
+struct abl_kargs_update_boid {
+    abl_globals G;
+    long n;
+    const int *visit;
+    abl_cols_Boid in, out;
+    abl_near_view NB;
+};
+__global__ void __launch_bounds__(128) abl_kernel_update_boid(const __grid_constant__ abl_kargs_update_boid A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
+    Boid abl_in, abl_out;
+    abl_in.pos = A.in.pos[abl_i];
+    abl_in.velocity = A.in.velocity[abl_i];
+    update_boid(A.G, A.NB, &abl_in, &abl_out);
+    A.out.pos[abl_i] = abl_out.pos;
+    A.out.velocity[abl_i] = abl_out.velocity;
+}
+static int abl_launch_update_boid(const abl_step_launch *L, cudaStream_t abl_stream) {
+    abl_kargs_update_boid A;
+    A.G = *(const abl_globals *) L->globals;
+    A.n = L->n;
+    A.visit = L->visit_order;
+    A.in.pos = (float2 *) L->in_cols[0];
+    A.out.pos = (float2 *) L->out_cols[0];
+    A.in.velocity = (float2 *) L->in_cols[1];
+    A.out.velocity = (float2 *) L->out_cols[1];
+    A.NB = L->near;
+    const int abl_block = L->block > 0 ? L->block : 128;
+    const long abl_grid = (A.n + abl_block - 1) / abl_block;
+    abl_kernel_update_boid<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
+static double abl_radius_update_boid(const void *abl_gp) {
+    const abl_globals &abl_G = *(const abl_globals *) abl_gp;
+    (void) abl_G;
+    return (double) (abl_G.interaction_radius);
+}
+
+
+static const abl_member_desc abl_members_Boid[] = {
+    {"pos", ABL_T_FLOAT2, 2, 4, 1},
+    {"velocity", ABL_T_FLOAT2, 2, 4, 0},
+};
+static const abl_agent_desc abl_agents[] = {
+    {"Boid", 2, abl_members_Boid, 0, 2},
+};
+static const abl_global_desc abl_global_table[] = {
+    {"PI", ABL_T_FLOAT, offsetof(abl_globals, PI)},
+    {"interaction_radius", ABL_T_FLOAT, offsetof(abl_globals, interaction_radius)},
+    {"separation_radius", ABL_T_FLOAT, offsetof(abl_globals, separation_radius)},
+    {"agent_density", ABL_T_FLOAT, offsetof(abl_globals, agent_density)},
+    {"time_scale", ABL_T_FLOAT, offsetof(abl_globals, time_scale)},
+    {"global_scale", ABL_T_FLOAT, offsetof(abl_globals, global_scale)},
+    {"steer_scale", ABL_T_FLOAT, offsetof(abl_globals, steer_scale)},
+    {"collision_scale", ABL_T_FLOAT, offsetof(abl_globals, collision_scale)},
+    {"match_scale", ABL_T_FLOAT, offsetof(abl_globals, match_scale)},
+    {"num_agents", ABL_T_INT, offsetof(abl_globals, num_agents)},
+    {"num_timesteps", ABL_T_INT, offsetof(abl_globals, num_timesteps)},
+    {"min_pos", ABL_T_FLOAT, offsetof(abl_globals, min_pos)},
+    {"max_pos", ABL_T_FLOAT, offsetof(abl_globals, max_pos)},
+    {nullptr, 0, 0}
+};
+static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max) {
+    const abl_globals &abl_G = *(const abl_globals *) abl_gp;
+    (void) abl_G;
+    float2 abl_lo = float2_fill(abl_G.min_pos);
+    float2 abl_hi = float2_fill(abl_G.max_pos);
+    abl_min[0] = abl_lo.x; abl_min[1] = abl_lo.y; abl_min[2] = 0;
+    abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
+}
+static const abl_step_desc abl_steps[] = {
+    {"update_boid", 0, 0, 1, abl_radius_update_boid, 3u, 3u, abl_launch_update_boid},
+};
+static const abl_step_desc abl_steps_ordered[] = {
+    abl_steps[0],
+    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr}
+};
+extern const abl_model_desc abl_desc = {
+    "boids2d_float", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 13, abl_global_table, 2, abl_env_bounds, nullptr, 1
+};
+static void abl_check(int r, const char *what) {
+    if (r != ABL_OK) {
+        std::fprintf(stderr, "%s failed: %s\n", what, abl_strerror(r));
+        std::exit(1);
+    }
+}
+static void abl_simulate(int abl_timesteps) {
+    abl_ctx *ctx = nullptr;
+    abl_check(abl_create(&abl_desc, 0, &ctx), "abl_create");
+    abl_check(abl_set_globals(ctx, &abl_G, sizeof abl_G), "abl_set_globals");
+    {
+        size_t n = agents.agents_Boid.len;
+        const Boid *aos = (const Boid *) agents.agents_Boid.values;
+        float2 *c0 = (float2 *) std::malloc(sizeof(float2) * (n ? n : 1));
+        for (size_t i = 0; i < n; i++) c0[i] = aos[i].pos;
+        float2 *c1 = (float2 *) std::malloc(sizeof(float2) * (n ? n : 1));
+        for (size_t i = 0; i < n; i++) c1[i] = aos[i].velocity;
+        const void *cols[] = {c0, c1};
+        abl_check(abl_upload(ctx, 0, cols, n), "abl_upload");
+        std::free(c0);
+        std::free(c1);
+    }
+    abl_check(abl_run(ctx, abl_timesteps), "abl_run");
+    {
+        size_t n = 0;
+        abl_check(abl_count(ctx, 0, &n), "abl_count");
+        float2 *c0 = (float2 *) std::malloc(sizeof(float2) * (n ? n : 1));
+        float2 *c1 = (float2 *) std::malloc(sizeof(float2) * (n ? n : 1));
+        void *cols[] = {c0, c1};
+        size_t cap = n;
+        abl_check(abl_download(ctx, 0, cols, &cap), "abl_download");
+        dyn_array_clean(&agents.agents_Boid);
+        agents.agents_Boid = dyn_array_create_fixed(sizeof(Boid), n);
+        Boid *aos = (Boid *) agents.agents_Boid.values;
+        for (size_t i = 0; i < n; i++) {
+            aos[i].pos = c0[i];
+            aos[i].velocity = c1[i];
+        }
+        std::free(c0);
+        std::free(c1);
+    }
+    double abl_secs = 0;
+    abl_last_exec_time(ctx, &abl_secs);
+    abl_destroy(ctx);
+}
+static int abl_main() {
+    for (int i = 0, _var0 = abl_G.num_agents; i < _var0; ++i) {
+        *DYN_ARRAY_PLACE(&agents.agents_Boid, Boid) = ([&]() { Boid abl_a; abl_a.pos = random_1(abl_G, float2_fill(abl_G.min_pos), float2_fill(abl_G.max_pos)); abl_a.velocity = random_1(abl_G, float2_fill((-1)), float2_fill(1)); return abl_a; }());
+    }
+    abl_simulate(abl_G.num_timesteps);
+    save(&agents, agents_info, "boids.out", SAVE_JSON);
+    return 0;
+}
+
+}  // namespace abl_model_boids2d_float
+
+extern "C" const abl_model_desc *abl_model_desc_boids2d_float(void) {
+    return &abl_model_boids2d_float::abl_desc;
+}
+
+#ifdef ABL_STANDALONE_MAIN
+extern "C" const abl_model_desc *const abl_builtin_models[] = {
+    &abl_model_boids2d_float::abl_desc, nullptr};
+int main() { return abl_model_boids2d_float::abl_main(); }
+#endif

@@ -1,0 +1,95 @@
+"""Regenerates the model sources in this directory with `OpenABL -b cuda`.
+
+The code generator is a plugin of the OpenABL compiler, whose sources live in
+an OpenABL tree; it runs where such a tree is available (set OPENABL_REF):
+    python openabl_gb300/generated/regenerate.py
+For every model below it runs the compiler with `-b cuda -C cuda.model=NAME`
+and keeps NAME.cu; for every named configuration it records the folded
+globals that the compiler printed for those -P values (configs.json), so that
+hosts which drive the runtime directly can set up exactly that configuration.
+The build compiles the files kept here; it does not need the compiler.
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+REPO = os.path.dirname(PKG)
+REF = os.environ.get("OPENABL_REF", "/root/reference")
+COMPILER = os.path.join(REPO, "_build", "compiler", "openabl")
+
+# model name -> (example file, -C config)
+MODELS = {
+    "circle": ("circle.abl", {}),
+    "circle3d": ("circle3d.abl", {}),
+    "boids2d": ("boids2d.abl", {}),
+    "game_of_life": ("game_of_life.abl", {}),
+    "boids2d_float": ("boids2d.abl", {"use_float": "true"}),
+}
+
+# configuration name -> (model, -P params)
+CONFIGS = {
+    "circle_4000": ("circle", {"num_agents": "4000", "rho": "0.1", "num_timesteps": "100"}),
+    "circle3d_4000": ("circle3d", {"num_agents": "4000", "rho": "0.01", "num_timesteps": "50"}),
+    "boids2d_4096": ("boids2d", {"num_agents": "4096", "agent_density": "3200.0",
+                                 "num_timesteps": "100"}),
+    "boids2d_1m": ("boids2d", {"num_agents": "1048576", "agent_density": "3200.0",
+                               "num_timesteps": "100"}),
+    "boids2d_float_4096": ("boids2d_float", {"num_agents": "4096", "agent_density": "3200.0",
+                                             "num_timesteps": "100"}),
+    "boids2d_float_1m": ("boids2d_float", {"num_agents": "1048576", "agent_density": "3200.0",
+                                           "num_timesteps": "100"}),
+    "game_of_life_64": ("game_of_life", {"num_agents": "4096", "alive_fraction": "0.5",
+                                         "num_timesteps": "100"}),
+    "game_of_life_4096": ("game_of_life", {"num_agents": "16777216", "alive_fraction": "0.5",
+                                           "num_timesteps": "100"}),
+}
+
+
+def run_compiler(model, params):
+    example, config = MODELS[model]
+    out = tempfile.mkdtemp(prefix="abl_gen_")
+    cmd = [COMPILER, "-A", os.path.join(REF, "asset"), "-i",
+           os.path.join(REF, "examples", example), "-o", out, "-b", "cuda",
+           "-C", f"cuda.model={model}"]
+    for k, v in config.items():
+        cmd += ["-C", f"{k}={v}"]
+    for k, v in params.items():
+        cmd += ["-P", f"{k}={v}"]
+    subprocess.check_call(cmd)
+    return out
+
+
+def main():
+    subprocess.check_call(["make", "-s", "-C", os.path.join(PKG, "backend"), "-j8", f"REF={REF}"])
+    for model, (example, config) in MODELS.items():
+        out = run_compiler(model, {})
+        src = open(os.path.join(out, model + ".cu")).read()
+        with open(os.path.join(HERE, model + ".cu"), "w") as f:
+            f.write(src)
+        print("generated", model)
+    configs = {}
+    for name, (model, params) in CONFIGS.items():
+        out = run_compiler(model, params)
+        manifest = json.load(open(os.path.join(out, model + ".globals.json")))
+        configs[name] = {"model": model, "params": params, "globals": manifest["globals"]}
+    with open(os.path.join(HERE, "configs.json"), "w") as f:
+        json.dump(configs, f, indent=1)
+    with open(os.path.join(HERE, "registry.cpp"), "w") as f:
+        f.write("// Models compiled into libopenabl_cuda (written by regenerate.py).\n")
+        f.write('#include "abl_model.h"\n\nextern "C" {\n')
+        for model in MODELS:
+            f.write(f"const abl_model_desc *abl_model_desc_{model}(void);\n")
+        f.write("extern const abl_model_desc *const abl_builtin_models[];\n")
+        f.write("const abl_model_desc *const abl_builtin_models[] = {\n")
+        for model in MODELS:
+            f.write(f"    abl_model_desc_{model}(),\n")
+        f.write("    nullptr};\n}\n")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,18 @@
+// Models compiled into libopenabl_cuda (written by regenerate.py).
+#include "abl_model.h"
+
+extern "C" {
+const abl_model_desc *abl_model_desc_circle(void);
+const abl_model_desc *abl_model_desc_circle3d(void);
+const abl_model_desc *abl_model_desc_boids2d(void);
+const abl_model_desc *abl_model_desc_game_of_life(void);
+const abl_model_desc *abl_model_desc_boids2d_float(void);
+extern const abl_model_desc *const abl_builtin_models[];
+const abl_model_desc *const abl_builtin_models[] = {
+    abl_model_desc_circle(),
+    abl_model_desc_circle3d(),
+    abl_model_desc_boids2d(),
+    abl_model_desc_game_of_life(),
+    abl_model_desc_boids2d_float(),
+    nullptr};
+}

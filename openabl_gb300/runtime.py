@@ -1,0 +1,298 @@
+"""Python host for the OpenABL CUDA runtime, through its C ABI.
+
+The reference drives a simulation from a generated C program
+(src/backend/CPrinter.cpp:189-233).  This module offers the same steps to a
+Python caller -- build the population, run `simulate` for T timesteps, read it
+back -- by calling the C entry points of include/openabl_cuda.h with ctypes.
+No computation happens here: every step runs in libopenabl_cuda.so on the GPU,
+and a missing library or GPU is an error, never a fallback.
+
+Agent state is a dict member name -> numpy array (float2 members as (n, 2),
+float3 as (n, 3), float as (n,), int as int32, bool as uint8).
+"""
+import ctypes
+import json
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libopenabl_cuda.so")
+CONFIGS_PATH = os.path.join(PKG, "generated", "configs.json")
+
+ABL_T_BOOL, ABL_T_INT, ABL_T_FLOAT, ABL_T_FLOAT2, ABL_T_FLOAT3 = 1, 2, 3, 5, 6
+
+_lib = None
+
+
+class AblError(RuntimeError):
+    def __init__(self, code, what):
+        msg = _load().abl_strerror(code).decode() if _lib is not None else str(code)
+        super().__init__(f"{what}: {msg} ({code})")
+        self.code = code
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with "
+                               "`python -m openabl_gb300.build_lib`")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
+        L.abl_model_lookup.restype = vp
+        L.abl_model_lookup.argtypes = [ctypes.c_char_p]
+        L.abl_model_num_agent_types.argtypes = [vp]
+        L.abl_model_agent_name.restype = ctypes.c_char_p
+        L.abl_model_agent_name.argtypes = [vp, i]
+        L.abl_model_num_members.argtypes = [vp, i]
+        L.abl_model_member.argtypes = [vp, i, i, ctypes.POINTER(ctypes.c_char_p),
+                                       ctypes.POINTER(ctypes.c_int)]
+        L.abl_model_globals_size.restype = sz
+        L.abl_model_globals_size.argtypes = [vp]
+        L.abl_model_globals_default.argtypes = [vp, vp]
+        L.abl_model_global.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(sz),
+                                       ctypes.POINTER(ctypes.c_int)]
+        L.abl_create.argtypes = [vp, sz, ctypes.POINTER(vp)]
+        L.abl_set_globals.argtypes = [vp, vp, sz]
+        L.abl_upload.argtypes = [vp, i, ctypes.POINTER(vp), sz]
+        L.abl_step.argtypes = [vp]
+        L.abl_run.argtypes = [vp, i]
+        L.abl_count.argtypes = [vp, i, ctypes.POINTER(sz)]
+        L.abl_download.argtypes = [vp, i, ctypes.POINTER(vp), ctypes.POINTER(sz)]
+        L.abl_reduce.argtypes = [vp, i, i, i, vp]
+        L.abl_last_exec_time.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+        L.abl_memory_used.argtypes = [vp, ctypes.POINTER(sz)]
+        L.abl_last_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_long)]
+        L.abl_destroy.argtypes = [vp]
+        L.abl_strerror.restype = ctypes.c_char_p
+        L.abl_strerror.argtypes = [i]
+        _lib = L
+    return _lib
+
+
+def library():
+    return _load()
+
+
+def fp64_rates():
+    """Measured FP64 FMA / add / multiply instruction rates (per lane, per s)."""
+    L = _load()
+    d = ctypes.c_double
+    L.abl_diag_fp64_rates.argtypes = [ctypes.POINTER(d)] * 3
+    a, b, c = d(), d(), d()
+    _check(L.abl_diag_fp64_rates(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+           "abl_diag_fp64_rates")
+    return a.value, b.value, c.value
+
+
+def _check(code, what):
+    if code != 0:
+        raise AblError(code, what)
+
+
+def configs():
+    with open(CONFIGS_PATH) as f:
+        return json.load(f)
+
+
+class Model:
+    """A model compiled into the library by `-b cuda` (its descriptor)."""
+
+    def __init__(self, name):
+        L = _load()
+        self.name = name
+        self.ptr = L.abl_model_lookup(name.encode())
+        if not self.ptr:
+            raise KeyError(f"model {name!r} is not compiled into {LIB_PATH}")
+        self.agent_types = []
+        for t in range(L.abl_model_num_agent_types(self.ptr)):
+            members = []
+            for m in range(L.abl_model_num_members(self.ptr, t)):
+                nm, vt = ctypes.c_char_p(), ctypes.c_int()
+                _check(L.abl_model_member(self.ptr, t, m, ctypes.byref(nm), ctypes.byref(vt)),
+                       "abl_model_member")
+                members.append((nm.value.decode(), vt.value))
+            self.agent_types.append((L.abl_model_agent_name(self.ptr, t).decode(), members))
+        self.globals_size = L.abl_model_globals_size(self.ptr)
+
+    def type_id(self, name):
+        for k, (n, _) in enumerate(self.agent_types):
+            if n == name:
+                return k
+        raise KeyError(name)
+
+    def default_globals(self):
+        buf = (ctypes.c_ubyte * self.globals_size)()
+        _check(_load().abl_model_globals_default(self.ptr, buf), "abl_model_globals_default")
+        return Globals(self, buf)
+
+
+class Globals:
+    """The model's globals block, addressable by name."""
+
+    def __init__(self, model, buf):
+        self.model = model
+        self.buf = buf
+        self.float_bytes = 4 if model.name.endswith("_float") else 8
+
+    def _slot(self, name):
+        off, vt = ctypes.c_size_t(), ctypes.c_int()
+        _check(_load().abl_model_global(self.model.ptr, name.encode(), ctypes.byref(off),
+                                        ctypes.byref(vt)), f"unknown global {name!r}")
+        return off.value, vt.value
+
+    def set(self, name, value):
+        off, vt = self._slot(name)
+        base = ctypes.addressof(self.buf) + off
+        fdt = ctypes.c_float if self.float_bytes == 4 else ctypes.c_double
+        if vt == ABL_T_BOOL:
+            ctypes.c_bool.from_address(base).value = bool(value)
+        elif vt == ABL_T_INT:
+            ctypes.c_int.from_address(base).value = int(value)
+        elif vt == ABL_T_FLOAT:
+            fdt.from_address(base).value = float(value)
+        else:
+            comps = 2 if vt == ABL_T_FLOAT2 else 3
+            vals = list(value) if hasattr(value, "__len__") else [value] * comps
+            for k in range(comps):
+                fdt.from_address(base + k * ctypes.sizeof(fdt)).value = float(vals[k])
+
+    def get(self, name):
+        off, vt = self._slot(name)
+        base = ctypes.addressof(self.buf) + off
+        fdt = ctypes.c_float if self.float_bytes == 4 else ctypes.c_double
+        if vt == ABL_T_BOOL:
+            return ctypes.c_bool.from_address(base).value
+        if vt == ABL_T_INT:
+            return ctypes.c_int.from_address(base).value
+        if vt == ABL_T_FLOAT:
+            return fdt.from_address(base).value
+        comps = 2 if vt == ABL_T_FLOAT2 else 3
+        return [fdt.from_address(base + k * ctypes.sizeof(fdt)).value for k in range(comps)]
+
+    def update(self, values):
+        for k, v in values.items():
+            if isinstance(v, str):
+                v = json.loads(v) if v not in ("true", "false") else v == "true"
+            self.set(k, v)
+        return self
+
+
+def globals_for_config(config_name):
+    cfg = configs()[config_name]
+    model = Model(cfg["model"])
+    g = model.default_globals().update(cfg["globals"])
+    return model, g
+
+
+def member_dtype(vt, float_bytes):
+    fd = np.float32 if float_bytes == 4 else np.float64
+    return {ABL_T_BOOL: (np.uint8, ()), ABL_T_INT: (np.int32, ()), ABL_T_FLOAT: (fd, ()),
+            ABL_T_FLOAT2: (fd, (2,)), ABL_T_FLOAT3: (fd, (3,))}[vt]
+
+
+class Simulation:
+    """One runtime context: device-resident agents of one model."""
+
+    def __init__(self, model, globals_=None, hbm_budget=0):
+        L = _load()
+        self.model = model if isinstance(model, Model) else Model(model)
+        self.globals = globals_ if globals_ is not None else self.model.default_globals()
+        self.ctx = ctypes.c_void_p()
+        _check(L.abl_create(self.model.ptr, hbm_budget, ctypes.byref(self.ctx)), "abl_create")
+        _check(L.abl_set_globals(self.ctx, self.globals.buf, self.model.globals_size),
+               "abl_set_globals")
+
+    def close(self):
+        if self.ctx:
+            _load().abl_destroy(self.ctx)
+            self.ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _members(self, type_id):
+        return self.model.agent_types[type_id][1]
+
+    def upload(self, type_name, state):
+        tid = self.model.type_id(type_name)
+        members = self._members(tid)
+        n = None
+        keep, ptrs = [], []
+        for nm, vt in members:
+            dt, shape = member_dtype(vt, self.globals.float_bytes)
+            a = np.ascontiguousarray(state[nm], dtype=dt)
+            if n is None:
+                n = a.shape[0]
+            assert a.shape == (n,) + shape, (nm, a.shape)
+            keep.append(a)
+            ptrs.append(a.ctypes.data_as(ctypes.c_void_p))
+        arr = (ctypes.c_void_p * len(ptrs))(*[p.value for p in ptrs])
+        _check(_load().abl_upload(self.ctx, tid, arr, n), "abl_upload")
+
+    def run(self, timesteps):
+        _check(_load().abl_run(self.ctx, int(timesteps)), "abl_run")
+
+    def step(self):
+        _check(_load().abl_step(self.ctx), "abl_step")
+
+    def count(self, type_name):
+        n = ctypes.c_size_t()
+        _check(_load().abl_count(self.ctx, self.model.type_id(type_name), ctypes.byref(n)),
+               "abl_count")
+        return n.value
+
+    def download(self, type_name, out=None):
+        """Copies the agents of `type_name` to the host.  `out` may supply the
+        destination arrays (e.g. pinned buffers); they must be large enough."""
+        tid = self.model.type_id(type_name)
+        n = self.count(type_name)
+        ptrs = []
+        if out is None:
+            out = {}
+            for nm, vt in self._members(tid):
+                dt, shape = member_dtype(vt, self.globals.float_bytes)
+                out[nm] = np.empty((n,) + shape, dtype=dt)
+        for nm, vt in self._members(tid):
+            a = out[nm]
+            assert a.flags["C_CONTIGUOUS"] and a.shape[0] >= n
+            ptrs.append(a.ctypes.data)
+        arr = (ctypes.c_void_p * len(ptrs))(*ptrs)
+        cap = ctypes.c_size_t(n)
+        _check(_load().abl_download(self.ctx, tid, arr, ctypes.byref(cap)), "abl_download")
+        return out
+
+    def last_exec_time(self):
+        s = ctypes.c_double()
+        _check(_load().abl_last_exec_time(self.ctx, ctypes.byref(s)), "abl_last_exec_time")
+        return s.value
+
+    def memory_used(self):
+        b = ctypes.c_size_t()
+        _check(_load().abl_memory_used(self.ctx, ctypes.byref(b)), "abl_memory_used")
+        return b.value
+
+    def set_profiling(self, enable=True):
+        L = _load()
+        L.abl_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _check(L.abl_set_profiling(self.ctx, 1 if enable else 0), "abl_set_profiling")
+
+    def step_kernel_time(self, step=0):
+        """(total seconds, launches) of a step function's kernel while profiling."""
+        L = _load()
+        L.abl_step_kernel_time.argtypes = [ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_long)]
+        s, n = ctypes.c_double(), ctypes.c_long()
+        _check(L.abl_step_kernel_time(self.ctx, step, ctypes.byref(s), ctypes.byref(n)),
+               "abl_step_kernel_time")
+        return s.value, n.value
+
+    def last_launch_count(self):
+        c = ctypes.c_long()
+        _check(_load().abl_last_launch_count(self.ctx, ctypes.byref(c)), "abl_last_launch_count")
+        return c.value

@@ -1,0 +1,37 @@
+"""Seeded synthetic initial states for the benchmark configurations.
+
+They replace the examples' own main() initialisation (which draws from the
+reference's fixed-seed xorshift stream) with the distributions the
+benchmark configurations specify; the same arrays are loaded into the GPU
+path and into the CPU oracle.
+"""
+import numpy as np
+
+
+def boids2d(n, max_pos, seed=0, vmax=1.0):
+    """Positions uniform in [0, max_pos)^2; velocity directions uniform on the
+    circle with speed uniform in [0.5, 1] * vmax (the speed cap of
+    examples/boids2d.abl:98-101 is 1)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pos = rng.uniform(0.0, max_pos, size=(n, 2))
+    theta = rng.uniform(0.0, 2.0 * np.pi, size=n)
+    speed = rng.uniform(0.5, 1.0, size=n) * vmax
+    vel = np.stack([np.cos(theta) * speed, np.sin(theta) * speed], axis=1)
+    return {"pos": np.ascontiguousarray(pos), "velocity": np.ascontiguousarray(vel)}
+
+
+def circle(n, W, dim=2, seed=0):
+    """Positions uniform in [0, W)^dim."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return {"pos": np.ascontiguousarray(rng.uniform(0.0, W, size=(n, dim)))}
+
+
+def game_of_life(size, alive_fraction=0.5, seed=0):
+    """One cell agent at (x + 0.5, y + 0.5) per grid point, x-major as in
+    examples/game_of_life.abl:63-75; each alive with probability alive_fraction."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x, y = np.meshgrid(np.arange(size, dtype=np.float64), np.arange(size, dtype=np.float64),
+                       indexing="ij")
+    pos = np.stack([x.ravel() + 0.5, y.ravel() + 0.5], axis=1)
+    alive = (rng.uniform(size=size * size) < alive_fraction).astype(np.uint8)
+    return {"pos": np.ascontiguousarray(pos), "alive": alive}
