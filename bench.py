@@ -55,7 +55,7 @@ def cpu_reference_sample(state, consts, target_seconds, n_total):
     sample of agents, all host threads.  Returns (agent-steps/s, sample, cores)."""
     from oracle import oracle as O
     cores = os.cpu_count() or 1
-    count = 16
+    count = 512
     t0 = time.perf_counter()
     O.boids2d_step(state, consts, mode=0, nthreads=cores, first=0, count=count)
     dt = time.perf_counter() - t0

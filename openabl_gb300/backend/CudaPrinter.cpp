@@ -114,7 +114,102 @@ bool nearBodyIsOrdered(const AST::ForStatement &loop) {
   return false;
 }
 
+// Whether every variable in `e` is a global and every call a builtin or a
+// type constructor, i.e. `e` has one value for the whole near loop.
+bool isLoopInvariant(const AST::Script &script, const AST::Expression &e) {
+  Collector c = collect(*const_cast<AST::Expression *>(&e));
+  for (auto *v : c.varExprs) {
+    if (!script.scope.has(v->var->id) || !script.scope.get(v->var->id).isGlobal) return false;
+  }
+  for (auto *call : c.calls) {
+    if (call->kind == AST::CallExpression::Kind::USER) return false;
+    if (call->isBuiltin() && isHostOnlyBuiltin(call->name)) return false;
+  }
+  return true;
+}
+
+// `X.pos` for the given variable and position member.
+bool isPosOf(const AST::Expression &e, VarId var, const std::string &pos) {
+  auto *m = dynamic_cast<const AST::MemberAccessExpression *>(&e);
+  if (!m || m->member != pos) return false;
+  auto *v = dynamic_cast<const AST::VarExpression *>(&*m->expr);
+  return v && v->var->id == var;
+}
+
+struct ComparisonCollector : public AST::Visitor {
+  std::vector<const AST::BinaryOpExpression *> cmps;
+  void enter(AST::BinaryOpExpression &e) override {
+    switch (e.op) {
+      case AST::BinaryOp::SMALLER: case AST::BinaryOp::SMALLER_EQUALS:
+      case AST::BinaryOp::GREATER: case AST::BinaryOp::GREATER_EQUALS:
+      case AST::BinaryOp::EQUALS: case AST::BinaryOp::NOT_EQUALS:
+        cmps.push_back(&e);
+        break;
+      default:
+        break;
+    }
+  }
+};
+
+// Declarations `float d = dist(q.pos, nx.pos)` (or length(q.pos - nx.pos),
+// either order) inside a near body whose every use is a comparison with a
+// loop-invariant value.
+std::set<const AST::VarDeclarationStatement *> findLazyDistances(
+    const AST::Script &script, const AST::ForStatement &loop) {
+  std::set<const AST::VarDeclarationStatement *> out;
+  auto *q = dynamic_cast<const AST::VarExpression *>(&loop.getNearAgent());
+  if (!q) return out;
+  VarId qid = q->var->id, nid = loop.var->id;
+  const AST::AgentDeclaration *agent = loop.type->resolved.getAgentDecl();
+  std::string pos = agent->getPositionMember()->name;
+  Collector c = collect(*loop.stmt);
+  ComparisonCollector cc;
+  const_cast<AST::Statement &>(*loop.stmt).accept(cc);
+  for (auto *d : c.decls) {
+    if (!d->initializer || !d->type->resolved.isFloat()) continue;
+    auto *call = dynamic_cast<const AST::CallExpression *>(&*d->initializer);
+    if (!call || !call->isBuiltin()) continue;
+    const std::string &fn = call->calledSig.name;
+    const AST::Expression *a = nullptr, *b = nullptr;
+    if ((fn == "dist_float2" || fn == "dist_float3") && call->args->size() == 2) {
+      a = &*(*call->args)[0];
+      b = &*(*call->args)[1];
+    } else if ((fn == "length_float2" || fn == "length_float3") && call->args->size() == 1) {
+      auto *sub = dynamic_cast<const AST::BinaryOpExpression *>(&*(*call->args)[0]);
+      if (!sub || sub->op != AST::BinaryOp::SUB) continue;
+      a = &*sub->left;
+      b = &*sub->right;
+    } else {
+      continue;
+    }
+    bool pair = (isPosOf(*a, qid, pos) && isPosOf(*b, nid, pos))
+             || (isPosOf(*a, nid, pos) && isPosOf(*b, qid, pos));
+    if (!pair) continue;
+    VarId id = d->var->id;
+    int uses = 0, cmpUses = 0;
+    for (auto *v : c.varExprs) uses += v->var->id == id;
+    for (auto *cmp : cc.cmps) {
+      auto *l = dynamic_cast<const AST::VarExpression *>(&*cmp->left);
+      auto *r = dynamic_cast<const AST::VarExpression *>(&*cmp->right);
+      if (l && l->var->id == id && isLoopInvariant(script, *cmp->right)) cmpUses++;
+      else if (r && r->var->id == id && isLoopInvariant(script, *cmp->left)) cmpUses++;
+    }
+    if (uses > 0 && uses == cmpUses) out.insert(d);
+  }
+  return out;
+}
+
 }  // namespace
+
+void CudaPrinter::print(const AST::VarDeclarationStatement &stmt) {
+  if (lazyDecls.count(&stmt)) {
+    *this << "const auto " << *stmt.var << " = abl::make_lazy_dist(" << nearQuery
+          << ", abl_NB, " << nearSlot << ", [&]() -> abl_float { return " << *stmt.initializer
+          << "; });";
+    return;
+  }
+  CPrinter::print(stmt);
+}
 
 bool CudaPrinter::isGlobal(const AST::Var &var) const {
   return script.scope.has(var.id) && script.scope.get(var.id).isGlobal;
@@ -242,7 +337,7 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
         << ") > " << radiusExpr << ");" << outdent << nl << "};" << nl
         << "while (" << c << ".fill(" << q << ", " << ex << ")) {" << indent << nl
         << "for (int abl_k = 0; abl_k < " << c << ".cnt; ++abl_k) {" << indent << nl
-        << "const int " << slot << " = " << c << ".buf[abl_k];" << nl
+        << "const int " << slot << " = " << c << ".slot(abl_k);" << nl
         << agentDecl->name << " " << nxs << ";";
   // Load the members the loop reads (AnalysisVisitor collects them,
   // src/AnalysisVisitor.cpp:1101-1105).
@@ -258,11 +353,15 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
 
   std::string savedLabel = nearEndLabel;
   bool savedNeeds = nearNeedsEnd;
+  lazyDecls = findLazyDistances(script, stmt);
+  nearQuery = q;
+  nearSlot = slot;
   nearEndLabel = "abl_near_end" + sid;
   nearNeedsEnd = false;
   nearLoopDepth = 0;
   *this << *stmt.stmt;
   nearLoopDepth = -1;
+  lazyDecls.clear();
   *this << outdent << nl << "}" << outdent << nl << "}" << outdent << nl << "}";
   if (nearNeedsEnd) *this << nl << nearEndLabel << ": ;";
   nearEndLabel = savedLabel;

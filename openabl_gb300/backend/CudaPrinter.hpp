@@ -37,6 +37,7 @@ struct CudaPrinter : public CPrinter {
   void print(const AST::WhileStatement &) override;
   void print(const AST::BreakStatement &) override;
   void print(const AST::SimulateStatement &) override;
+  void print(const AST::VarDeclarationStatement &) override;
   void print(const AST::FunctionDeclaration &) override;
   void print(const AST::Script &) override;
 
@@ -50,6 +51,10 @@ private:
   int nearLoopDepth = -1;        // loop depth inside the current near body
   bool nearNeedsEnd = false;     // a `break` left the current near body
   std::string nearEndLabel;
+  // Distances in the current near body that are only compared with
+  // loop-invariant values (printed as abl::lazy_dist).
+  std::set<const AST::VarDeclarationStatement *> lazyDecls;
+  std::string nearQuery, nearSlot;
 
   // Per step function, filled while printing it.
   struct StepInfo {

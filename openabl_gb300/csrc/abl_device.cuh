@@ -35,6 +35,11 @@
 #ifndef ABL_NEAR_CHUNK
 #define ABL_NEAR_CHUNK 32
 #endif
+// Step kernels run with at most this many threads per block; each thread
+// owns one column of the block's shared chunk buffer.
+#ifndef ABL_STEP_BLOCK
+#define ABL_STEP_BLOCK 128
+#endif
 
 namespace abl {
 
@@ -60,12 +65,11 @@ struct band {
 // float rounding of d2 and sqrtf) add a few u relative.  eps doubles that sum.
 // When eps is not small (huge coordinates, zero or negative radius, non-finite
 // values) every candidate takes the exact test.
-__device__ inline band make_band(double radius, float amax, int dim) {
+__device__ inline band make_band(float r, float amax, int dim) {
   band b;
   b.lo = -1.0f;
   b.hi = __int_as_float(0x7f800000);  // +inf: nothing is decided by the filter
-  float r = (float) radius;
-  if (!(radius > 0.0) || !(r > 0.0f) || !(amax >= 0.0f) || !(amax < 1e30f)) return b;
+  if (!(r > 0.0f) || !(r < 1e15f) || !(amax >= 0.0f) || !(amax < 1e30f)) return b;
   const float u = 5.9604645e-8f;
   float s = 1.1f * r;
   float E = (2.0f * u * amax + u * s) * 1.01f;
@@ -79,12 +83,29 @@ __device__ inline band make_band(double radius, float amax, int dim) {
   return b;
 }
 
+// Band for a double threshold; the conversion to float is outward-safe
+// because eps covers more than one float rounding of r.
+__device__ inline band make_band(double radius, float amax, int dim) {
+  if (!(radius > 0.0)) {
+    band b;
+    b.lo = -1.0f;
+    b.hi = __int_as_float(0x7f800000);
+    return b;
+  }
+  return make_band((float) radius, amax, dim);
+}
+
 // Query side of a near loop: the agent's cell and float position.
 template <int DIM>
 struct near_query {
   int c[3];
   float pf[3];
   band bd;
+  float amax;
+  // Band of the last threshold a lazy distance was compared with.
+  mutable long long lazy_bits = 0;
+  mutable band lazy_band;
+  mutable bool lazy_valid = false;
 
   __device__ near_query(const abl_near_view &V, double x, double y, double z) {
     const int dims[3] = {V.nx, V.ny, V.nz};
@@ -93,7 +114,18 @@ struct near_query {
       c[d] = d < DIM ? cell_coord(p[d], V.lo[d], V.inv_cell, dims[d]) : 0;
       pf[d] = d < DIM ? (float) p[d] : 0.0f;
     }
-    bd = make_band(V.radius, *V.amax, DIM);
+    amax = *V.amax;
+    bd = make_band(V.radius, amax, DIM);
+  }
+
+  __device__ const band &band_for(double r) const {
+    long long bits = __double_as_longlong(r);
+    if (!lazy_valid || bits != lazy_bits) {
+      lazy_band = make_band(r, amax, DIM);
+      lazy_bits = bits;
+      lazy_valid = true;
+    }
+    return lazy_band;
   }
 };
 
@@ -107,10 +139,14 @@ struct near_cursor {
   // unordered mode: current row of cells and slot range within it
   int rz, ry;
   int x0, x1;
-  int buf[ABL_NEAR_CHUNK];
+  int *buf;  // this thread's column of the block's shared buffer (stride ABL_STEP_BLOCK)
   int cnt;
 
+  __device__ int slot(int k) const { return buf[k * ABL_STEP_BLOCK]; }
+
   __device__ near_cursor(const abl_near_view &v, const near_query<DIM> &q) : V(v), cnt(0) {
+    __shared__ int chunk[ABL_NEAR_CHUNK * ABL_STEP_BLOCK];
+    buf = chunk + threadIdx.x;
     if (V.ordered) {
       int cell = (q.c[2] * V.ny + q.c[1]) * V.nx + q.c[0];
       cur = V.nb_off[cell];
@@ -165,7 +201,7 @@ struct near_cursor {
         if (d2 < q.bd.lo) take = true;
         else if (d2 > q.bd.hi) take = false;
         else take = exact(s);
-        if (take) buf[cnt++] = s;
+        if (take) buf[ABL_STEP_BLOCK * cnt++] = s;
       }
       if (cnt == ABL_NEAR_CHUNK || V.ordered) break;
       if (cur < end) break;
@@ -178,6 +214,89 @@ struct near_cursor {
     return cnt > 0;
   }
 };
+
+// A distance between the query agent and the current neighbour that the
+// generated code only ever compares with loop-invariant values, e.g.
+//   float separation = dist(in.pos, nx.pos); if (separation < R) ...
+// A comparison is decided from the FP32 estimate whenever it lies outside the
+// error band of make_band(R); otherwise the reference expression (`exact`)
+// is evaluated.  Either way the result equals the reference's comparison.
+template <int DIM, typename Exact>
+struct lazy_dist {
+  const near_query<DIM> &q;
+  float d2f;
+  Exact exact;
+
+  __device__ lazy_dist(const near_query<DIM> &q_, const abl_near_view &V, int slot, Exact e)
+      : q(q_), exact(e) {
+    float d2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      float dd = __ldg(&V.posf[DIM * slot + d]) - q.pf[d];
+      d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
+    }
+    d2f = d2;
+  }
+
+  // -1: surely below R, +1: surely above R, 0: undecided.
+  __device__ int side(double R) const {
+    const band &b = q.band_for(R);
+    if (d2f < b.lo) return -1;
+    if (d2f > b.hi) return 1;
+    return 0;
+  }
+};
+
+template <int DIM, typename Exact>
+__device__ lazy_dist<DIM, Exact> make_lazy_dist(const near_query<DIM> &q, const abl_near_view &V,
+                                                int slot, Exact e) {
+  return lazy_dist<DIM, Exact>(q, V, slot, e);
+}
+
+
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator<(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s < 0 ? true : s > 0 ? false : a.exact() < r;
+}
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator<=(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s < 0 ? true : s > 0 ? false : a.exact() <= r;
+}
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator>(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s < 0 ? false : s > 0 ? true : a.exact() > r;
+}
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator>=(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s < 0 ? false : s > 0 ? true : a.exact() >= r;
+}
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator==(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s != 0 ? false : a.exact() == r;
+}
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator!=(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s != 0 ? true : a.exact() != r;
+}
+// R OP d  is  d OP' R.
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator<(R r, const lazy_dist<DIM, Exact> &a) { return a > r; }
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator<=(R r, const lazy_dist<DIM, Exact> &a) { return a >= r; }
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator>(R r, const lazy_dist<DIM, Exact> &a) { return a < r; }
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator>=(R r, const lazy_dist<DIM, Exact> &a) { return a <= r; }
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator==(R r, const lazy_dist<DIM, Exact> &a) { return a == r; }
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator!=(R r, const lazy_dist<DIM, Exact> &a) { return a != r; }
 
 // Atomic max on non-negative floats (bit patterns order like the values).
 __device__ inline void atomic_max_nonneg(float *addr, float v) {

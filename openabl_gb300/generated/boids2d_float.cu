@@ -128,7 +128,7 @@ __device__ static void update_boid(const abl_globals &abl_G, const abl_near_view
         };
         while (abl_c1.fill(abl_q1, abl_exact1)) {
             for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
-                const int abl_slot1 = abl_c1.buf[abl_k];
+                const int abl_slot1 = abl_c1.slot(abl_k);
                 Boid abl_nx1;
                 abl_nx1.pos = ((const float2 *) abl_NB.cols[0])[abl_slot1];
                 abl_nx1.velocity = ((const float2 *) abl_NB.cols[1])[abl_slot1];
@@ -137,7 +137,7 @@ __device__ static void update_boid(const abl_globals &abl_G, const abl_near_view
                     global_center = float2_add(global_center, nx->pos);
                     global_velocity = float2_add(global_velocity, nx->velocity);
                     interaction_count += 1;
-                    float separation = dist_float2(in->pos, nx->pos);
+                    const auto separation = abl::make_lazy_dist(abl_q1, abl_NB, abl_slot1, [&]() -> abl_float { return dist_float2(in->pos, nx->pos); });
                     if ((separation < abl_G.separation_radius)) {
                         collision_center = float2_add(collision_center, nx->pos);
                         collision_count += 1;

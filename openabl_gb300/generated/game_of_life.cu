@@ -109,7 +109,7 @@ __device__ static void step_move(const abl_globals &abl_G, const abl_near_view &
         };
         while (abl_c1.fill(abl_q1, abl_exact1)) {
             for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
-                const int abl_slot1 = abl_c1.buf[abl_k];
+                const int abl_slot1 = abl_c1.slot(abl_k);
                 Cell abl_nx1;
                 abl_nx1.alive = ((const bool *) abl_NB.cols[1])[abl_slot1];
                 Cell* nx = &abl_nx1;
