@@ -47,6 +47,7 @@ extern "C" {
 #define ABL_E_UNSUPPORTED -6 /* model feature not implemented by this runtime */
 #define ABL_E_CAPACITY -7    /* agent capacity exceeded by runtime additions */
 #define ABL_E_NOMODEL -8     /* unknown model name */
+#define ABL_E_SCRATCH -9     /* larger than abl_step_noalloc's fixed scratch area */
 
 /* Member value types (match asset/c/libabl.h:181-189 type_id). */
 #define ABL_T_BOOL 1
@@ -107,6 +108,34 @@ int abl_set_profiling(abl_ctx *ctx, int enable);
 int abl_step_kernel_time(abl_ctx *ctx, int step, double *seconds, long *launches);
 int abl_destroy(abl_ctx *ctx);
 const char *abl_strerror(int code);
+
+/* ---- allocation-free timestep ----
+ *
+ * No counterpart in the reference (whose `c` backend never touches a GPU).
+ * For callers that cannot allocate device memory while they run -- code
+ * embedded in another framework's memory pool or allocator, or loops that
+ * must not allocate once started: runs ONE timestep of a model with one
+ * agent type and one step function on device buffers the caller owns
+ * (SoA columns as above, device pointers): reads `in_cols`, writes
+ * `out_cols` (members the step does not always write keep the values
+ * already in `out_cols`, like the reference's double buffer).  `globals` is
+ * the model's globals block on the host; `stream` is a cudaStream_t (NULL for
+ * the default stream).  The call is synchronous.
+ *
+ * It calls no cudaMalloc/cudaFree: its temporaries live in one static device
+ * array of ABL_NOALLOC_SCRATCH_BYTES, which every GPU that loads this library
+ * holds until the process exits.  Limits: at most ABL_NOALLOC_MAX_AGENTS
+ * agents and ABL_NOALLOC_MAX_CELLS grid cells, and everything must fit the
+ * array; larger problems return ABL_E_SCRATCH without touching the GPU.  The
+ * first call on a device, with that device current, looks up the array's
+ * address (cudaGetSymbolAddress) and sets up host bookkeeping; make it
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+#define ABL_NOALLOC_MAX_AGENTS 131072
+#define ABL_NOALLOC_MAX_CELLS 131072
+#define ABL_NOALLOC_SCRATCH_BYTES (32u << 20)
+int abl_step_noalloc(const abl_model_desc *model, const void *globals, size_t globals_size,
+                     const void *const *in_cols, void *const *out_cols, size_t n, void *stream);
 
 #ifdef __cplusplus
 }

@@ -28,6 +28,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1082,8 +1083,206 @@ const char *abl_strerror(int code) {
     case ABL_E_UNSUPPORTED: return "unsupported model feature";
     case ABL_E_CAPACITY: return "agent capacity exceeded";
     case ABL_E_NOMODEL: return "unknown model";
+    case ABL_E_SCRATCH:
+      return "problem larger than the fixed scratch area of abl_step_noalloc "
+             "(see ABL_NOALLOC_MAX_AGENTS / ABL_NOALLOC_MAX_CELLS)";
     default: return "unknown error";
   }
 }
 
 }  // extern "C"
+
+// ------------------------------------------------- allocation-free timestep
+//
+// abl_step_noalloc runs one timestep of a single-type model on device buffers
+// the caller owns, for callers that cannot allocate device memory while they
+// run -- code that executes inside another framework's memory pool or
+// allocator, or that must not allocate once it has started (for example
+// between the steps of a real-time loop).  All temporary storage (grid
+// counts, the counting sort, gathered neighbour data, neighbourhood lists,
+// scan partials, the error word) lives in one fixed, file-scope device array.
+// Its address is looked up with cudaGetSymbolAddress once per device, on the
+// first call made with that device current; that first call also builds the
+// host-side bookkeeping, so it should be made before any stream capture.
+// Every call shares the array: calls that overlap on the GPU race with each
+// other and must be serialised by the caller.
+
+namespace {
+
+constexpr long kNoAllocMaxAgents = ABL_NOALLOC_MAX_AGENTS;
+constexpr long kNoAllocMaxCells = ABL_NOALLOC_MAX_CELLS;
+constexpr size_t kNoAllocScratchBytes = ABL_NOALLOC_SCRATCH_BYTES;
+constexpr int kNoAllocDevices = 64;
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char abl_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+struct NoAllocDevice {
+  bool ready = false;
+  unsigned char *scratch = nullptr;  // device address of abl_noalloc_scratch
+  abl_ctx *ctx = nullptr;            // reusable host bookkeeping
+};
+NoAllocDevice g_noalloc[kNoAllocDevices];
+std::mutex g_noalloc_mutex;
+
+struct Bump {
+  unsigned char *base;
+  size_t used, cap;
+  template <typename T>
+  T *take(size_t count) {
+    size_t bytes = (std::max<size_t>(count, 1) * sizeof(T) + 255) & ~(size_t) 255;
+    if (used + bytes > cap) return nullptr;
+    T *p = (T *) (base + used);
+    used += bytes;
+    return p;
+  }
+};
+
+bool scan_plan_static(ScanPlan &p, long m, Bump &b) {
+  p.levels.clear();
+  long len = m;
+  for (;;) {
+    if (p.levels.size() == p.levels.capacity()) return false;  // would allocate
+    ScanLevel L;
+    L.m = len;
+    L.nb = std::max<long>(1, (len + kScanBlock - 1) / kScanBlock);
+    L.incl = b.take<int>(len);
+    L.sums = b.take<int>(L.nb);
+    L.offs = b.take<int>(L.nb + 1);
+    if (!L.incl || !L.sums || !L.offs) return false;
+    p.levels.push_back(L);
+    if (L.nb == 1) return true;
+    len = L.nb;
+  }
+}
+
+}  // namespace
+
+extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals,
+                                size_t globals_size, const void *const *in_cols,
+                                void *const *out_cols, size_t n, void *stream) {
+  if (!model || !globals || !in_cols || !out_cols) return ABL_E_INVALID;
+  if (globals_size != model->globals_size) return ABL_E_INVALID;
+  if (model->num_agent_types != 1 || model->num_steps != 1) return ABL_E_UNSUPPORTED;
+  if ((long) n > kNoAllocMaxAgents) return ABL_E_SCRATCH;
+  const abl_agent_desc &ad = model->agents[0];
+  if (ad.num_members > ABL_MAX_MEMBERS) return ABL_E_UNSUPPORTED;
+  int dev = 0;
+  ABL_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocDevices) return ABL_E_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  NoAllocDevice &D = g_noalloc[dev];
+  if (!D.ready) {
+    // One-time set-up on this device (host bookkeeping and the device
+    // address of the static scratch array).
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, abl_noalloc_scratch);
+    if (e != cudaSuccess) {
+      std::fprintf(stderr, "openabl-cuda: cudaGetSymbolAddress(abl_noalloc_scratch) failed: %s\n",
+                   cudaGetErrorString(e));
+      return ABL_E_CUDA;
+    }
+    D.scratch = (unsigned char *) p;
+    D.ctx = new abl_ctx;
+    D.ctx->globals.reserve(16384);
+    D.ctx->types.resize(1);
+    D.ctx->types[0].cell_scan.levels.reserve(8);
+    D.ctx->types[0].nb_scan.levels.reserve(8);
+    D.ready = true;
+  }
+  if (model->globals_size > D.ctx->globals.capacity()) return ABL_E_SCRATCH;
+
+  abl_ctx &ctx = *D.ctx;
+  ctx.model = model;
+  ctx.stream = (cudaStream_t) stream;
+  ctx.globals.assign((const unsigned char *) globals, (const unsigned char *) globals + globals_size);
+  ctx.profile = false;
+  const void *G = ctx.globals.data();
+  TypeState &t = ctx.types[0];
+  t.d = &ad;
+  t.n = (long) n;
+  t.uploaded = true;
+  t.cur = 0;
+  for (int k = 0; k < ad.num_members; k++) {
+    t.cols[0][k] = const_cast<void *>(in_cols[k]);
+    t.cols[1][k] = out_cols[k];
+  }
+
+  Bump b{D.scratch, 0, kNoAllocScratchBytes};
+  ctx.error = b.take<int>(1);
+  t.amax = b.take<float>(1);
+
+  // Grid of the neighbour type, as prepare() sizes it.
+  const abl_step_desc &sd = model->steps[0];
+  t.is_near = sd.near_type == 0;
+  t.ordered = t.is_near && sd.ordered;
+  t.gather_mask = t.is_near ? sd.near_members : 0;
+  t.dirty = true;
+  if (t.is_near) {
+    if (ad.position_member < 0) return ABL_E_UNSUPPORTED;
+    int dim = ad.dim;
+    double emin[3] = {0, 0, 0}, emax[3] = {0, 0, 0};
+    if (model->env_bounds) model->env_bounds(G, emin, emax);
+    double rmax = sd.radius ? sd.radius(G) : 0.0;
+    double gran = model->granularity ? model->granularity(G) : rmax;
+    if (!(gran > 0.0) || !std::isfinite(gran)) return ABL_E_INVALID;
+    double cell = gran * (1.0 + 1.0 / 1024.0);
+    t.R = std::max(1, (int) std::ceil(rmax * (1.0 + 1e-6) / cell));
+    t.inv_cell = 1.0 / cell;
+    int dims[3] = {1, 1, 1};
+    for (int d = 0; d < 3; d++) {
+      t.lo[d] = d < dim ? emin[d] : 0.0;
+      if (d < dim) {
+        double ext = emax[d] - emin[d];
+        if (!(ext >= 0.0) || !std::isfinite(ext)) return ABL_E_INVALID;
+        double k = std::floor(ext * t.inv_cell) + 1.0;
+        if (k > (double) kNoAllocMaxCells) return ABL_E_SCRATCH;
+        dims[d] = (int) k;
+      }
+    }
+    t.nx = dims[0];
+    t.ny = dims[1];
+    t.nz = dims[2];
+    t.ncells = (long) t.nx * t.ny * t.nz;
+    if (t.ncells > kNoAllocMaxCells) return ABL_E_SCRATCH;
+    long nn = std::max<long>(t.n, 1);
+    t.cell_count = b.take<int>(t.ncells);
+    t.cell_start = b.take<int>(t.ncells + 1);
+    t.local_rank = b.take<int>(nn);
+    t.cell_of = b.take<int>(nn);
+    t.order = b.take<int>(nn);
+    t.posf = b.take<float>(nn * dim);
+    bool ok = t.cell_count && t.cell_start && t.local_rank && t.cell_of && t.order && t.posf
+              && scan_plan_static(t.cell_scan, t.ncells, b);
+    for (int k = 0; k < ad.num_members && ok; k++) {
+      t.gcols[k] = nullptr;
+      if (t.gather_mask & (1u << k)) {
+        t.gcols[k] = b.take<unsigned char>(member_bytes(ad.members[k]) * nn);
+        ok = t.gcols[k] != nullptr;
+      }
+    }
+    if (ok && t.ordered) {
+      long span = 2 * t.R + 1;
+      long per_agent = dim == 3 ? span * span * span : span * span;
+      t.nb_cnt = b.take<int>(t.ncells);
+      t.nb_off = b.take<int>(t.ncells + 1);
+      t.nb_list = b.take<int>(per_agent * nn);
+      ok = t.nb_cnt && t.nb_off && t.nb_list && scan_plan_static(t.nb_scan, t.ncells, b);
+    }
+    if (!ok) return ABL_E_SCRATCH;
+  }
+  ctx.prepared = true;
+
+  // The scratch keeps the previous call's contents: clear the words that
+  // must start at zero (the cell counters are cleared by the binning itself).
+  ABL_CUDA_TRY(cudaMemsetAsync(ctx.error, 0, sizeof(int), ctx.stream));
+  ABL_CUDA_TRY(cudaMemsetAsync(t.amax, 0, sizeof(float), ctx.stream));
+  if (t.n > 0) ABL_TRY(step_once(&ctx));
+  int h = 0;
+  ABL_CUDA_TRY(cudaMemcpyAsync(&h, ctx.error, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
+  return h;
+}
