@@ -94,8 +94,30 @@ int abl_count(abl_ctx *ctx, int type_id, size_t *n);
 /* Copies the agents of `type_id` into host SoA columns of capacity *n;
  * sets *n to the number of agents. */
 int abl_download(abl_ctx *ctx, int type_id, void *const *cols, size_t *n);
-/* Sequential-step reductions: kind 0 = count(Type), 1 = sum(Type.member). */
+/* Sequential-step reductions (src/main.cpp:104-130; FlameGPU lowering at
+ * src/backend/FlameGPUPrinter.cpp:204-225):
+ *   ABL_REDUCE_COUNT     count(Type)          -> int
+ *   ABL_REDUCE_SUM       sum(Type.member)     -> int for bool/int members (bools
+ *                        sum to int), else the member's type; float members
+ *                        are added in ascending agent order
+ *   ABL_REDUCE_COUNT_EQ  count(Type.member, v) -> int; *out holds v on entry
+ *                        (the member's type) and the count on return */
+#define ABL_REDUCE_COUNT 0
+#define ABL_REDUCE_SUM 1
+#define ABL_REDUCE_COUNT_EQ 2
 int abl_reduce(abl_ctx *ctx, int kind, int type_id, int member, void *out);
+/* Seed of the counter-based generator behind random() in step functions
+ * (Philox4x32-10 keyed by the seed; counter = agent index, step function,
+ * timestep, draw).  Default 0. */
+int abl_set_seed(abl_ctx *ctx, uint64_t seed);
+/* Device time of the most recent timestep, in seconds: getLastExecTime()
+ * inside a sequential step (src/backend/FlameGPUPrinter.cpp:246-249). */
+int abl_last_timestep_time(abl_ctx *ctx, double *seconds);
+/* Rows written by log_csv() in sequential steps ("%d"/"%f" comma-separated,
+ * one row per call, as src/backend/FlameGPUPrinter.cpp:226-245 formats them).
+ * abl_log_csv appends a row; abl_log_text copies the accumulated text. */
+int abl_log_csv(abl_ctx *ctx, const char *fmt, ...);
+int abl_log_text(abl_ctx *ctx, char *buf, size_t cap, size_t *len);
 /* Wall time of the last abl_step/abl_run call, in seconds (device events). */
 int abl_last_exec_time(abl_ctx *ctx, double *seconds);
 /* Device memory currently held by the context, in bytes. */

@@ -253,17 +253,77 @@ void CudaPrinter::print(const AST::VarExpression &expr) {
   CPrinter::print(expr);
 }
 
+int CudaPrinter::memberIndex(const AST::AgentDeclaration *agent,
+                             const AST::AgentMember *member) const {
+  for (size_t k = 0; k < agent->members->size(); k++) {
+    if (&*(*agent->members)[k] == member) return (int) k;
+  }
+  return -1;
+}
+
 void CudaPrinter::print(const AST::CallExpression &expr) {
   if (expr.kind == AST::CallExpression::Kind::USER) {
-    *this << expr.calledSig.name << "(abl_G";
+    *this << expr.calledSig.name << "(abl_G, abl_R";
     for (const AST::ExpressionPtr &arg : *expr.args) *this << ", " << *arg;
     *this << ")";
     return;
   }
-  if (expr.isBuiltin() && isHostOnlyBuiltin(expr.name)) {
+  if (expr.isBuiltin()) {
     const std::string &n = expr.name;
-    if (n != "random" && n != "randomInt" && n != "add" && n != "save") {
-      throw BackendError("The cuda backend does not support " + n + "() yet");
+    if (n == "random" || n == "randomInt") {
+      // Host: the reference's sequential stream; device: abl::rng.
+      *this << (n == "random" ? "abl_random(abl_R" : "abl_random_int(abl_R");
+      for (const AST::ExpressionPtr &arg : *expr.args) *this << ", " << *arg;
+      *this << ")";
+      return;
+    }
+    if (n == "removeCurrent") {
+      // FlameGPU lowers it to a flag as well (FlameGPUPrinter.cpp:171-173).
+      *this << "abl_K.remove()";
+      return;
+    }
+    if (n == "add" && fnKind == FnKind::STEP) {
+      const AST::AgentDeclaration *a = expr.calledSig.paramTypes[0].getAgentDecl();
+      *this << "abl_add_" << a->name << "(abl_K, " << expr.getArg(0) << ")";
+      return;
+    }
+    if (n == "count") {
+      Type t = expr.getArg(0).type;
+      const AST::AgentDeclaration *a = t.getAgentDecl();
+      if (expr.getNumArgs() == 2) {
+        const AST::AgentMember *m = t.getAgentMember();
+        *this << "abl_seq_count_eq(abl_C, " << agentIndex(a) << ", " << memberIndex(a, m)
+              << ", (" << cType(m->type->resolved) << ") " << expr.getArg(1) << ")";
+      } else {
+        *this << "abl_seq_count(abl_C, " << agentIndex(a) << ")";
+      }
+      return;
+    }
+    if (n == "sum") {
+      Type t = expr.getArg(0).type;
+      const AST::AgentDeclaration *a = t.getAgentDecl();
+      const AST::AgentMember *m = t.getAgentMember();
+      Type mt = m->type->resolved;
+      std::string rt = mt.isBool() ? "int" : cType(mt);
+      *this << "abl_seq_sum<" << rt << ">(abl_C, " << agentIndex(a) << ", " << memberIndex(a, m)
+            << ")";
+      return;
+    }
+    if (n == "getLastExecTime") {
+      *this << "abl_seq_exec_time(abl_C)";
+      return;
+    }
+    if (n == "log_csv") {
+      // "%d" / "%f" per argument, comma separated (FlameGPUPrinter.cpp:226-245).
+      std::string fmt;
+      for (size_t k = 0; k < expr.args->size(); k++) {
+        fmt += (k ? "," : "");
+        fmt += (*expr.args)[k]->type.isInt() ? "%d" : "%f";
+      }
+      *this << "abl_log_csv(abl_C, \"" << fmt << "\\n\"";
+      for (const AST::ExpressionPtr &arg : *expr.args) *this << ", " << *arg;
+      *this << ")";
+      return;
     }
   }
   CPrinter::print(expr);
@@ -369,26 +429,43 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
 }
 
 void CudaPrinter::print(const AST::SimulateStatement &stmt) {
-  if (stmt.seqStepDecl) {
-    throw BackendError("The cuda backend does not support sequential step functions yet");
-  }
   *this << "abl_simulate(" << *stmt.timestepsExpr << ");";
 }
 
 void CudaPrinter::print(const AST::FunctionDeclaration &decl) {
   if (decl.isMain()) {
+    fnKind = FnKind::HOST;
     *this << "static int abl_main() {" << indent << *decl.stmts << nl << "return 0;"
           << outdent << nl << "}";
     return;
   }
   if (decl.isParallelStep()) {
+    fnKind = FnKind::STEP;
     printStepFunction(decl);
+    fnKind = FnKind::HOST;
     return;
   }
   if (decl.isSequentialStep()) {
-    throw BackendError("The cuda backend does not support sequential step functions yet");
+    fnKind = FnKind::SEQ;
+    printSeqStep(decl);
+    fnKind = FnKind::HOST;
+    return;
   }
+  fnKind = FnKind::USER;
   printUserFunction(decl);
+  fnKind = FnKind::HOST;
+}
+
+// The sequential step runs on the host after every timestep; its builtins
+// (count, sum, log_csv, getLastExecTime) call the runtime's reductions.
+void CudaPrinter::printSeqStep(const AST::FunctionDeclaration &decl) {
+  seqStep = &decl;
+  *this << "static int abl_seq_" << decl.name
+        << "(abl_ctx *abl_C, const void *abl_gp) {" << indent << nl
+        << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl
+        << "abl::rng abl_R_host;" << nl << "abl::rng &abl_R = abl_R_host;" << nl
+        << "(void) abl_G; (void) abl_R;" << *decl.stmts << nl << "return ABL_OK;" << outdent
+        << nl << "}";
 }
 
 void CudaPrinter::printUserFunction(const AST::FunctionDeclaration &decl) {
@@ -404,7 +481,10 @@ void CudaPrinter::printUserFunction(const AST::FunctionDeclaration &decl) {
     Collector c = collect(*const_cast<AST::FunctionDeclaration *>(f));
     bool h = false;
     for (auto *call : c.calls) {
-      if (call->isBuiltin() && isHostOnlyBuiltin(call->name)) h = true;
+      // random()/randomInt() run on both sides (abl_random); the rest of the
+      // simulation builtins exist on the host only.
+      if (call->isBuiltin() && isHostOnlyBuiltin(call->name) && call->name != "random"
+          && call->name != "randomInt") h = true;
       if (call->kind == AST::CallExpression::Kind::USER && call->calledFunc
           && isHost(call->calledFunc, depth + 1)) h = true;
     }
@@ -413,7 +493,7 @@ void CudaPrinter::printUserFunction(const AST::FunctionDeclaration &decl) {
   };
   bool host = isHost(&decl, 0);
   *this << (host ? "static inline " : "__host__ __device__ static inline ")
-        << *decl.returnType << " " << decl.sig.name << "(const abl_globals &abl_G";
+        << *decl.returnType << " " << decl.sig.name << "(const abl_globals &abl_G, abl::rng &abl_R";
   if (!decl.params->empty()) *this << ", ";
   printParams(decl);
   *this << ") {" << indent << *decl.stmts << outdent << nl << "}";
@@ -426,13 +506,9 @@ void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
   info.agentType = agentIndex(&agent);
   Collector c = collect(*const_cast<AST::FunctionDeclaration *>(&decl));
   for (auto *call : c.calls) {
-    if (call->isBuiltin() && (call->name == "add" || call->name == "removeCurrent")) {
-      throw BackendError("The cuda backend does not support runtime add/remove yet");
-    }
-    if (call->isBuiltin() && (call->name == "random" || call->name == "randomInt")) {
-      throw BackendError("The cuda backend does not support random() in step functions yet");
-    }
+    if (call->isBuiltin() && call->name == "removeCurrent") info.usesRemove = true;
   }
+  if (decl.runtimeAddedAgent) info.addType = agentIndex(decl.runtimeAddedAgent);
   if (!c.nearLoops.empty()) {
     const AST::ForStatement *loop = c.nearLoops[0];
     info.nearLoop = loop;
@@ -493,9 +569,10 @@ void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
   steps.push_back(info);
 
   *this << "__device__ static void " << decl.name
-        << "(const abl_globals &abl_G, const abl_near_view &abl_NB, ";
+        << "(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, ";
   printParams(decl);
-  *this << ") {" << indent << *decl.stmts << outdent << nl << "}" << nl;
+  *this << ") {" << indent << nl << "abl::rng &abl_R = abl_K.R;" << nl
+        << "(void) abl_R; (void) abl_NB;" << *decl.stmts << outdent << nl << "}" << nl;
   printKernel(steps.back());
 }
 
@@ -504,31 +581,48 @@ void CudaPrinter::printKernel(const StepInfo &info) {
   const AST::AgentDeclaration &agent = decl.stepAgent();
   const std::string &T = agent.name;
   const std::string &name = decl.name;
+  bool copy = copyOut();
   *this << nl << "struct abl_kargs_" << name << " {" << indent << nl
         << "abl_globals G;" << nl << "long n;" << nl << "const int *visit;" << nl
-        << "abl_cols_" << T << " in, out;" << nl << "abl_near_view NB;" << outdent << nl << "};"
-        << nl << "__global__ void __launch_bounds__(128) abl_kernel_" << name
+        << "abl_cols_" << T << " in, out;" << nl << "abl_near_view NB;" << nl
+        << "uint8_t *removed;" << nl << "uint8_t *child_flag;" << nl
+        << "void *child_cols[ABL_MAX_MEMBERS];" << nl << "uint64_t seed;" << nl
+        << "long timestep;" << nl << "int step_index;" << outdent << nl << "};"
+        << nl << "__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_" << name
         << "(const __grid_constant__ abl_kargs_" << name << " A) {" << indent << nl
         << "const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl
         << "if (abl_t >= A.n) return;" << nl
         << "const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;" << nl
-        << T << " abl_in, abl_out;";
+        << "abl::step_ctx abl_K;" << nl
+        << "abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);"
+        << nl << "abl_K.self = abl_i;" << nl << "abl_K.removed = 0;" << nl << "abl_K.added = 0;"
+        << nl << "abl_K.child_cols = A.child_cols;" << nl << T << " abl_in, abl_out;";
   for (size_t k = 0; k < agent.members->size(); k++) {
     const std::string &m = (*agent.members)[k]->name;
     *this << nl << "abl_in." << m << " = A.in." << m << "[abl_i];";
   }
+  if (copy) {
+    // Models with runtime add/remove: `out` starts as a copy of `in`, as the
+    // MASON backend's prepareOutState does (MasonPrinter.cpp:480-486).
+    *this << nl << "abl_out = abl_in;";
+  } else {
+    for (size_t k = 0; k < agent.members->size(); k++) {
+      const std::string &m = (*agent.members)[k]->name;
+      bool maybe = info.outMaybe & (1u << k), always = info.outAlways & (1u << k);
+      // The double buffer keeps whatever it held for members the step does
+      // not always write (the reference's agents_X_dbuf, CPrinter.cpp:210-228).
+      if (maybe && !always) *this << nl << "abl_out." << m << " = A.out." << m << "[abl_i];";
+    }
+  }
+  *this << nl << name << "(A.G, A.NB, abl_K, &abl_in, &abl_out);";
   for (size_t k = 0; k < agent.members->size(); k++) {
     const std::string &m = (*agent.members)[k]->name;
-    bool maybe = info.outMaybe & (1u << k), always = info.outAlways & (1u << k);
-    // The double buffer keeps whatever it held for members the step does not
-    // always write (the reference's agents_X_dbuf, CPrinter.cpp:210-228).
-    if (maybe && !always) *this << nl << "abl_out." << m << " = A.out." << m << "[abl_i];";
+    if (copy || (info.outMaybe & (1u << k))) {
+      *this << nl << "A.out." << m << "[abl_i] = abl_out." << m << ";";
+    }
   }
-  *this << nl << name << "(A.G, A.NB, &abl_in, &abl_out);";
-  for (size_t k = 0; k < agent.members->size(); k++) {
-    const std::string &m = (*agent.members)[k]->name;
-    if (info.outMaybe & (1u << k)) *this << nl << "A.out." << m << "[abl_i] = abl_out." << m << ";";
-  }
+  if (info.usesRemove) *this << nl << "A.removed[abl_i] = (uint8_t) abl_K.removed;";
+  if (info.addType >= 0) *this << nl << "A.child_flag[abl_i] = (uint8_t) abl_K.added;";
   *this << outdent << nl << "}" << nl
         << "static int abl_launch_" << name
         << "(const abl_step_launch *L, cudaStream_t abl_stream) {" << indent << nl
@@ -541,8 +635,13 @@ void CudaPrinter::printKernel(const StepInfo &info) {
     *this << nl << "A.in." << m.name << " = (" << ty << " *) L->in_cols[" << (int) k << "];"
           << nl << "A.out." << m.name << " = (" << ty << " *) L->out_cols[" << (int) k << "];";
   }
-  *this << nl << "A.NB = L->near;" << nl
-        << "const int abl_block = L->block > 0 ? L->block : 128;" << nl
+  *this << nl << "A.NB = L->near;" << nl << "A.removed = L->removed;" << nl
+        << "A.child_flag = L->child_flag;" << nl
+        << "for (int k = 0; k < ABL_MAX_MEMBERS; k++) A.child_cols[k] = L->child_cols[k];" << nl
+        << "A.seed = L->seed;" << nl << "A.timestep = L->timestep;" << nl
+        << "A.step_index = L->step_index;" << nl
+        << "const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : "
+           "ABL_STEP_BLOCK;" << nl
         << "const long abl_grid = (A.n + abl_block - 1) / abl_block;" << nl
         << "abl_kernel_" << name << "<<<abl_grid, abl_block, 0, abl_stream>>>(A);" << nl
         << "return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;" << outdent << nl
@@ -550,7 +649,7 @@ void CudaPrinter::printKernel(const StepInfo &info) {
   if (info.nearLoop) {
     *this << "static double abl_radius_" << name << "(const void *abl_gp) {" << indent << nl
           << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl
-          << "(void) abl_G;" << nl
+          << "abl::rng abl_R;" << nl << "(void) abl_G; (void) abl_R;" << nl
           << "return (double) (" << info.nearLoop->getNearRadius() << ");" << outdent << nl
           << "}" << nl;
   }
@@ -638,7 +737,13 @@ void CudaPrinter::printHostSimulate() {
     for (size_t k = 0; k < a.members->size(); k++) *this << nl << "std::free(c" << k << ");";
     *this << outdent << nl << "}";
   }
-  *this << nl << "double abl_secs = 0;" << nl << "abl_last_exec_time(ctx, &abl_secs);" << nl
+  *this << nl << "size_t abl_log_len = 0;" << nl << "abl_log_text(ctx, nullptr, 0, &abl_log_len);"
+        << nl << "if (abl_log_len > 0) {" << indent << nl
+        << "char *abl_log = (char *) std::malloc(abl_log_len + 1);" << nl
+        << "abl_log_text(ctx, abl_log, abl_log_len + 1, nullptr);" << nl
+        << "FILE *abl_f = std::fopen(\"log.csv\", \"w\");" << nl
+        << "if (abl_f) { std::fputs(abl_log, abl_f); std::fclose(abl_f); }" << nl
+        << "std::free(abl_log);" << outdent << nl << "}" << nl
         << "abl_destroy(ctx);" << outdent << nl << "}" << nl;
 }
 
@@ -687,7 +792,7 @@ void CudaPrinter::printDescriptor() {
   }
   *this << "static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max) {"
         << indent << nl << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl
-        << "(void) abl_G;";
+        << "abl::rng abl_R;" << nl << "(void) abl_G; (void) abl_R;";
   if (envDim > 0) {
     std::string vt = envDim == 2 ? "float2" : "float3";
     *this << nl << vt << " abl_lo = ";
@@ -706,7 +811,8 @@ void CudaPrinter::printDescriptor() {
   *this << outdent << nl << "}" << nl;
   if (granE) {
     *this << "static double abl_granularity(const void *abl_gp) {" << indent << nl
-          << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl << "(void) abl_G;"
+          << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl
+          << "abl::rng abl_R;" << nl << "(void) abl_G; (void) abl_R;"
           << nl << "return (double) (" << *granE << ");" << outdent << nl << "}" << nl;
   }
 
@@ -715,9 +821,10 @@ void CudaPrinter::printDescriptor() {
     const std::string &n = s.decl->name;
     *this << nl << "{\"" << n << "\", " << s.agentType << ", " << s.nearType << ", "
           << (s.ordered ? 1 : 0) << ", " << (s.nearLoop ? "abl_radius_" + n : "nullptr") << ", "
-          << s.nearMembers << "u, " << s.outAlways << "u, abl_launch_" << n << "},";
+          << s.nearMembers << "u, " << s.outAlways << "u, abl_launch_" << n << ", "
+          << (s.usesRemove ? 1 : 0) << ", " << s.addType << ", " << (copyOut() ? 1 : 0) << "},";
   }
-  if (steps.empty()) *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr},";
+  if (steps.empty()) *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0},";
   *this << outdent << nl << "};" << nl;
   // The runtime runs the steps in simulate order (SimulateStatement::stepFuncDecls,
   // CPrinter.cpp:196); abl_steps above is in declaration order.
@@ -729,7 +836,8 @@ void CudaPrinter::printDescriptor() {
       }
     }
   }
-  *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr}" << outdent << nl << "};" << nl;
+  *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0}" << outdent << nl
+        << "};" << nl;
   int numSteps = 0;
   if (script.simStmt) numSteps = (int) script.simStmt->stepFuncDecls.size();
   *this << "extern const abl_model_desc abl_desc = {" << indent << nl
@@ -737,7 +845,9 @@ void CudaPrinter::printDescriptor() {
         << numSteps << ", abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, "
         << (int) script.consts.size() << ", abl_global_table, " << envDim
         << ", abl_env_bounds, " << (granE ? "abl_granularity" : "nullptr") << ", "
-        << (useFloat ? 1 : 0) << outdent << nl << "};" << nl;
+        << (useFloat ? 1 : 0) << ", "
+        << (seqStep ? "abl_seq_" + seqStep->name : std::string("nullptr")) << outdent << nl
+        << "};" << nl;
 }
 
 void CudaPrinter::print(const AST::Script &) {
@@ -760,12 +870,27 @@ void CudaPrinter::print(const AST::Script &) {
   }
   *this << "{ NULL, 0, NULL }" << outdent << nl << "};" << nl << nl;
   printGlobals();
+  *this << "static abl::rng abl_R;  // unused on the host: main() draws from the host stream" << nl;
   for (AST::AgentDeclaration *a : script.agents) {
     *this << "struct abl_cols_" << a->name << " {" << indent;
     for (const AST::AgentMemberPtr &m : *a->members) {
       *this << nl << cType(m->type->resolved) << " *" << m->name << ";";
     }
     *this << outdent << nl << "};" << nl;
+  }
+  // add() inside a step: the child is staged at its parent's index and
+  // appended to the population after the step (abl_runtime.cu).
+  if (script.usesRuntimeAddition) {
+    for (AST::AgentDeclaration *a : script.agents) {
+      *this << "__device__ static void abl_add_" << a->name << "(abl::step_ctx &K, const "
+            << a->name << " &c) {" << indent << nl << "K.added = 1;";
+      for (size_t k = 0; k < a->members->size(); k++) {
+        const AST::AgentMember &m = *(*a->members)[k];
+        *this << nl << "((" << cType(m.type->resolved) << " *) K.child_cols[" << (int) k
+              << "])[K.self] = c." << m.name << ";";
+      }
+      *this << outdent << nl << "}" << nl;
+    }
   }
   *this << nl;
   const AST::FunctionDeclaration *mainDecl = nullptr;

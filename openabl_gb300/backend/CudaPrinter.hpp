@@ -56,6 +56,11 @@ private:
   std::set<const AST::VarDeclarationStatement *> lazyDecls;
   std::string nearQuery, nearSlot;
 
+  // Kind of function being printed (decides how builtins are lowered).
+  enum class FnKind { HOST, STEP, USER, SEQ } fnKind = FnKind::HOST;
+  // `out` starts as a copy of `in` in models with runtime add/remove.
+  bool copyOut() const { return script.usesRuntimeRemoval || script.usesRuntimeAddition; }
+
   // Per step function, filled while printing it.
   struct StepInfo {
     const AST::FunctionDeclaration *decl = nullptr;
@@ -66,6 +71,8 @@ private:
     unsigned outMaybe = 0;
     unsigned outAlways = 0;
     const AST::ForStatement *nearLoop = nullptr;
+    bool usesRemove = false;
+    int addType = -1;
   };
   std::vector<StepInfo> steps;
 
@@ -78,6 +85,9 @@ private:
   void printDescriptor();
   void printHostSimulate();
   void printUserFunction(const AST::FunctionDeclaration &decl);
+  void printSeqStep(const AST::FunctionDeclaration &decl);
+  int memberIndex(const AST::AgentDeclaration *agent, const AST::AgentMember *member) const;
+  const AST::FunctionDeclaration *seqStep = nullptr;
 };
 
 }  // namespace OpenABL

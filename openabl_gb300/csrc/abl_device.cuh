@@ -298,6 +298,87 @@ __device__ inline bool operator==(R r, const lazy_dist<DIM, Exact> &a) { return 
 template <int DIM, typename Exact, typename R>
 __device__ inline bool operator!=(R r, const lazy_dist<DIM, Exact> &a) { return a != r; }
 
+// Counter-based random numbers for random() inside step functions.  The
+// reference draws from one sequential xorshift stream shared by all OpenMP
+// threads (asset/c/libabl.c:8-39), which has no parallel order; here every
+// draw is a pure function of (seed, agent index, step function, timestep,
+// draw number): Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC'11), counter (agent, step, timestep,
+// draw), key (seed low, seed high).  The CPU oracle implements the same.
+struct rng {
+  uint32_t k0, k1, c0, c1, c2, draw;
+
+  __host__ __device__ void init(uint64_t seed, uint32_t agent, uint32_t step, uint64_t timestep) {
+    k0 = (uint32_t) seed;
+    k1 = (uint32_t) (seed >> 32);
+    c0 = agent;
+    c1 = step;
+    c2 = (uint32_t) timestep;
+    draw = 0;
+  }
+
+  __host__ __device__ static void mulhilo(uint32_t a, uint32_t b, uint32_t &hi, uint32_t &lo) {
+    uint64_t p = (uint64_t) a * (uint64_t) b;
+    hi = (uint32_t) (p >> 32);
+    lo = (uint32_t) p;
+  }
+
+  __host__ __device__ void next4(uint32_t out[4]) {
+    uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = draw++;
+    uint32_t key0 = k0, key1 = k1;
+    for (int r = 0; r < 10; r++) {
+      if (r > 0) {
+        key0 += 0x9E3779B9u;
+        key1 += 0xBB67AE85u;
+      }
+      uint32_t hi0, lo0, hi1, lo1;
+      mulhilo(0xD2511F53u, x0, hi0, lo0);
+      mulhilo(0xCD9E8D57u, x2, hi1, lo1);
+      uint32_t y0 = hi1 ^ x1 ^ key0, y2 = hi0 ^ x3 ^ key1;
+      x0 = y0;
+      x1 = lo1;
+      x2 = y2;
+      x3 = lo0;
+    }
+    out[0] = x0;
+    out[1] = x1;
+    out[2] = x2;
+    out[3] = x3;
+  }
+
+  // Uniform in [0, 1) with 53 random bits.
+  __host__ __device__ double unit() {
+    uint32_t x[4];
+    next4(x);
+    uint64_t b = (((uint64_t) x[0] << 32) | x[1]) >> 11;
+    return (double) b * (1.0 / 9007199254740992.0);
+  }
+
+  template <typename F>
+  __host__ __device__ F uniform(F lo, F hi) {
+    F u = (F) unit();
+    return lo + u * (hi - lo);
+  }
+
+  __host__ __device__ int uniform_int(int lo, int hi) {
+    uint32_t x[4];
+    next4(x);
+    uint32_t n = (uint32_t) (hi - lo) + 1u;
+    return n == 0 ? (int) x[0] : lo + (int) (x[0] % n);
+  }
+};
+
+// Per-thread state of a step kernel: random numbers, removeCurrent() and add().
+struct step_ctx {
+  rng R;
+  long self;
+  int removed;
+  int added;
+  void *const *child_cols;
+
+  __device__ void remove() { removed = 1; }
+};
+
 // Atomic max on non-negative floats (bit patterns order like the values).
 __device__ inline void atomic_max_nonneg(float *addr, float v) {
   atomicMax(reinterpret_cast<int *>(addr), __float_as_int(v));

@@ -103,3 +103,22 @@ static inline abl_float abl_random_float(abl_float lo, abl_float hi) {
   if (sizeof(abl_float) == sizeof(float)) return (abl_float) random_float_f((float) lo, (float) hi);
   return (abl_float) random_float_d((double) lo, (double) hi);
 }
+
+// random() / randomInt(): the sequential host stream in main(), the
+// counter-based stream (abl::rng) inside step kernels.
+__host__ __device__ static inline abl_float abl_random(abl::rng &R, abl_float lo, abl_float hi) {
+#ifdef __CUDA_ARCH__
+  return R.uniform<abl_float>(lo, hi);
+#else
+  (void) R;
+  return abl_random_float(lo, hi);
+#endif
+}
+__host__ __device__ static inline int abl_random_int(abl::rng &R, int lo, int hi) {
+#ifdef __CUDA_ARCH__
+  return R.uniform_int(lo, hi);
+#else
+  (void) R;
+  return random_int(lo, hi);
+#endif
+}

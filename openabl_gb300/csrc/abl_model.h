@@ -72,6 +72,14 @@ typedef struct {
   int *error;                        /* device error word */
   abl_near_view near;                /* valid when the step has a near loop */
   int block;                         /* threads per block chosen by the runtime */
+  /* runtime removal / addition (steps that call removeCurrent() / add()) */
+  uint8_t *removed;                  /* per agent: 1 when the agent removed itself */
+  uint8_t *child_flag;               /* per agent: 1 when it created a child */
+  void *child_cols[ABL_MAX_MEMBERS]; /* members of the created child, by parent index */
+  /* counter-based random numbers for random() in step functions */
+  uint64_t seed;
+  long timestep;
+  int step_index;
 } abl_step_launch;
 
 typedef int (*abl_step_launch_fn)(const abl_step_launch *launch, cudaStream_t stream);
@@ -87,7 +95,13 @@ typedef struct {
   uint32_t near_members;       /* bitmask of neighbour members read in the loop */
   uint32_t out_written;        /* bitmask of members always written to `out` */
   abl_step_launch_fn launch;
+  int uses_remove;             /* the body may call removeCurrent() */
+  int add_type;                /* agent type created by add() in the body, -1 if none */
+  int out_copy;                /* `out` starts as a copy of `in` */
 } abl_step_desc;
+
+/* Host function run after every timestep: the `sequential step`. */
+typedef int (*abl_seq_step_fn)(abl_ctx *ctx, const void *globals);
 
 struct abl_model_desc {
   const char *name;
@@ -103,6 +117,7 @@ struct abl_model_desc {
   abl_env_fn env_bounds;
   abl_globals_fn granularity;    /* cell size before the safety margin */
   int uses_float;                /* built with use_float */
+  abl_seq_step_fn seq_step;      /* NULL when the simulation has none */
 };
 
 #endif /* ABL_MODEL_H */

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdarg>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -187,6 +188,60 @@ __global__ void k_max2(const float *a, const float *b, float *out) {
   *out = fmaxf(*a, *b);
 }
 
+// sum() of a bool (1 byte) or int (4 byte) column.
+__global__ void k_sum_int(const void *col, int bytes, long n, unsigned long long *out) {
+  long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  long long v = 0;
+  if (i < n) v = bytes == 1 ? (long long) ((const uint8_t *) col)[i] : ((const int *) col)[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v != 0) atomicAdd(out, (unsigned long long) v);
+}
+
+// sum() of floating-point members in ascending agent order (one thread).
+__global__ void k_sum_seq(const void *col, int scalar, int comps, long n, double *out) {
+  for (int c = 0; c < comps; c++) {
+    if (scalar == 4) {
+      float acc = 0.0f;
+      for (long i = 0; i < n; i++) acc = acc + ((const float *) col)[comps * i + c];
+      out[c] = acc;
+    } else {
+      double acc = 0.0;
+      for (long i = 0; i < n; i++) acc = acc + ((const double *) col)[comps * i + c];
+      out[c] = acc;
+    }
+  }
+}
+
+struct EqArgs {
+  unsigned char value[24];
+  int bytes, scalar, is_float;
+};
+
+// count(Type.member, value): element equality in the member's type.
+__global__ void k_count_eq(const void *col, long n, const __grid_constant__ EqArgs a,
+                           unsigned long long *out) {
+  long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  int eq = 0;
+  if (i < n) {
+    const unsigned char *e = (const unsigned char *) col + (long) a.bytes * i;
+    eq = 1;
+    if (a.is_float && a.scalar == 8) {
+      for (int c = 0; c < a.bytes / 8; c++)
+        eq &= ((const double *) e)[c] == ((const double *) a.value)[c];
+    } else if (a.is_float) {
+      for (int c = 0; c < a.bytes / 4; c++)
+        eq &= ((const float *) e)[c] == ((const float *) a.value)[c];
+    } else if (a.bytes == 1) {
+      eq = (e[0] != 0) == (a.value[0] != 0);
+    } else {
+      eq = *(const int *) e == *(const int *) a.value;
+    }
+  }
+  unsigned m = __ballot_sync(0xffffffffu, eq);
+  if ((threadIdx.x & 31) == 0 && m) atomicAdd(out, (unsigned long long) __popc(m));
+}
+
 // Slot-ordered copies: float positions and the requested member columns.
 struct GatherArgs {
   int nmem;
@@ -317,6 +372,8 @@ __global__ void k_nb_build(int nx, int ny, int nz, int R, const int *cell_start,
 struct TypeState {
   const abl_agent_desc *d = nullptr;
   long n = 0;
+  long cap = 0;            // agents the column buffers can hold
+  bool dynamic = false;    // some step function removes or adds agents of this type
   bool uploaded = false;
   void *cols[2][ABL_MAX_MEMBERS] = {};
   int cur = 0;
@@ -347,6 +404,17 @@ size_t member_bytes(const abl_member_desc &m) {
 
 }  // namespace
 
+// Per step function buffers for runtime removal and addition.
+struct StepState {
+  uint8_t *removed = nullptr;               // parent capacity
+  uint8_t *child_flag = nullptr;            // parent capacity
+  void *child_cols[ABL_MAX_MEMBERS] = {};   // added type's members, parent capacity
+  int *keep = nullptr, *keep_pos = nullptr; // parent capacity (+1)
+  int *child = nullptr, *child_pos = nullptr;
+  ScanPlan keep_scan, child_scan;
+  long parent_cap = 0;
+};
+
 struct abl_ctx {
   const abl_model_desc *model = nullptr;
   std::vector<unsigned char> globals;
@@ -369,6 +437,15 @@ struct abl_ctx {
   };
   std::vector<Graph> graphs;
   bool prepared = false;
+  std::vector<StepState> step_state;
+  std::vector<void *> step_allocs;
+  uint64_t seed = 0;
+  long timestep = 0;
+  cudaEvent_t ts0 = nullptr, ts1 = nullptr;
+  double last_timestep = 0.0;
+  std::string log;
+  int *d_pair = nullptr;   // two ints read back after compaction scans
+  double *d_red = nullptr; // reduction results
   // Optional per-step-function kernel timing (eager timesteps only).
   bool profile = false;
   std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
@@ -533,7 +610,7 @@ int prepare(abl_ctx *ctx) {
     t.nz = dims[2];
     t.ncells = (long) t.nx * t.ny * t.nz;
     if (t.ncells > (1L << 30)) return ABL_E_UNSUPPORTED;
-    long n = std::max<long>(t.n, 1);
+    long n = std::max<long>(std::max(t.n, t.cap), 1);
     auto *own = &t.bin_allocs;
     ABL_TRY(dev_alloc_t(ctx, &t.cell_count, t.ncells, own));
     ABL_TRY(dev_alloc_t(ctx, &t.cell_start, t.ncells + 1, own));
@@ -560,7 +637,181 @@ int prepare(abl_ctx *ctx) {
     t.dirty = true;
   }
   if (!ctx->amax_pair) ABL_TRY(dev_alloc_t(ctx, &ctx->amax_pair, 1));
+  if (!ctx->d_pair) ABL_TRY(dev_alloc_t(ctx, &ctx->d_pair, 2));
+  // Buffers of step functions that remove or add agents, sized by the
+  // capacity of the step's own type (one flag / one child per agent).
+  for (void *p : ctx->step_allocs) dev_free(ctx, p);
+  ctx->step_allocs.clear();
+  ctx->step_state.assign(m->num_steps, StepState());
+  for (int k = 0; k < m->num_steps; k++) {
+    const abl_step_desc &sd = m->steps[k];
+    if (!sd.uses_remove && sd.add_type < 0) continue;
+    StepState &st = ctx->step_state[k];
+    const TypeState &pt = ctx->types[sd.agent_type];
+    long pc = std::max<long>(std::max(pt.cap, pt.n), 1);
+    st.parent_cap = pc;
+    auto *own = &ctx->step_allocs;
+    ABL_TRY(dev_alloc_t(ctx, &st.removed, pc, own));
+    ABL_TRY(dev_alloc_t(ctx, &st.child_flag, pc, own));
+    ABL_TRY(dev_alloc_t(ctx, &st.keep, pc, own));
+    ABL_TRY(dev_alloc_t(ctx, &st.keep_pos, pc + 1, own));
+    ABL_TRY(dev_alloc_t(ctx, &st.child, pc, own));
+    ABL_TRY(dev_alloc_t(ctx, &st.child_pos, pc + 1, own));
+    ABL_TRY(scan_plan(ctx, st.keep_scan, pc, own));
+    ABL_TRY(scan_plan(ctx, st.child_scan, pc, own));
+    if (sd.add_type >= 0) {
+      const abl_agent_desc &ad = m->agents[sd.add_type];
+      for (int j = 0; j < ad.num_members; j++) {
+        void *p = nullptr;
+        ABL_TRY(dev_alloc(ctx, &p, member_bytes(ad.members[j]) * pc, own));
+        st.child_cols[j] = p;
+      }
+    }
+  }
   ctx->prepared = true;
+  return ABL_OK;
+}
+
+// ------------------------------------------------- removal and addition
+
+// keep[i] = 1 unless agent i removed itself; child[i] = 1 when it added one.
+__global__ void k_flags(long n, const uint8_t *removed, const uint8_t *child_flag, int *keep,
+                        int *child) {
+  long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  keep[i] = removed ? (removed[i] ? 0 : 1) : 1;
+  child[i] = child_flag ? (child_flag[i] ? 1 : 0) : 0;
+}
+
+__global__ void k_read_totals(const int *a, long na, const int *b, long nb, int *out) {
+  out[0] = a ? a[na] : 0;
+  out[1] = b ? b[nb] : 0;
+}
+
+struct MoveArgs {
+  int nmem;
+  const void *src[ABL_MAX_MEMBERS];
+  void *dst[ABL_MAX_MEMBERS];
+  int bytes[ABL_MAX_MEMBERS];
+};
+
+__device__ inline void copy_elem(const void *src, void *dst, long si, long di, int b) {
+  if ((b & 7) == 0) {
+    const uint64_t *s = (const uint64_t *) src + (b / 8) * si;
+    uint64_t *d = (uint64_t *) dst + (b / 8) * di;
+    for (int w = 0; w < b / 8; w++) d[w] = s[w];
+  } else if ((b & 3) == 0) {
+    const uint32_t *s = (const uint32_t *) src + (b / 4) * si;
+    uint32_t *d = (uint32_t *) dst + (b / 4) * di;
+    for (int w = 0; w < b / 4; w++) d[w] = s[w];
+  } else {
+    const uint8_t *s = (const uint8_t *) src + b * si;
+    uint8_t *d = (uint8_t *) dst + b * di;
+    for (int w = 0; w < b; w++) d[w] = s[w];
+  }
+}
+
+// Stable compaction: element i moves to base + pos[i] when flag[i] is set.
+__global__ void k_scatter_flagged(long n, const int *flag, const int *pos, long base,
+                                  const __grid_constant__ MoveArgs a) {
+  long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !flag[i]) return;
+  long di = base + pos[i];
+  for (int k = 0; k < a.nmem; k++) copy_elem(a.src[k], a.dst[k], i, di, a.bytes[k]);
+}
+
+// Grows a type's column buffers to hold `need` agents, keeping the first n
+// agents of both buffers.
+int grow_type(abl_ctx *ctx, TypeState &t, long need) {
+  long cap = std::max(need, 2 * std::max<long>(t.cap, 1));
+  for (int b = 0; b < 2; b++) {
+    for (int k = 0; k < t.d->num_members; k++) {
+      void *p = nullptr;
+      size_t mb = member_bytes(t.d->members[k]);
+      ABL_TRY(dev_alloc(ctx, &p, mb * cap));
+      if (t.n > 0) {
+        ABL_CUDA_TRY(cudaMemcpyAsync(p, t.cols[b][k], mb * t.n, cudaMemcpyDeviceToDevice,
+                                     ctx->stream));
+      }
+      ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+      dev_free(ctx, t.cols[b][k]);
+      t.cols[b][k] = p;
+    }
+  }
+  t.cap = cap;
+  return ABL_OK;
+}
+
+MoveArgs move_args(const abl_agent_desc &d, void *const *src, void *const *dst) {
+  MoveArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.nmem = d.num_members;
+  for (int k = 0; k < d.num_members; k++) {
+    a.src[k] = src[k];
+    a.dst[k] = dst[k];
+    a.bytes[k] = (int) member_bytes(d.members[k]);
+  }
+  return a;
+}
+
+// After a step function that removes or adds agents: stable compaction of
+// the survivors, then the children appended in parent order.  The step's
+// result is in the buffer it wrote (cols[1 - cur]).  Returns with `regrow`
+// set when a type had to grow (the binning buffers are then resized before
+// the next binning).
+int apply_population_changes(abl_ctx *ctx, int k, bool &regrow) {
+  const abl_step_desc &sd = ctx->model->steps[k];
+  StepState &st = ctx->step_state[k];
+  TypeState &t = ctx->types[sd.agent_type];
+  cudaStream_t s = ctx->stream;
+  const int B = 256;
+  long n = t.n;
+  long nb = blocks_for(n, B);
+  bool self_add = sd.add_type == sd.agent_type;
+  k_flags<<<nb, B, 0, s>>>(n, sd.uses_remove ? st.removed : nullptr,
+                           sd.add_type >= 0 ? st.child_flag : nullptr, st.keep, st.child);
+  ctx->launches++;
+  scan_run(ctx, st.keep_scan, st.keep, st.keep_pos);
+  scan_run(ctx, st.child_scan, st.child, st.child_pos);
+  k_read_totals<<<1, 1, 0, s>>>(st.keep_pos, n, st.child_pos, n, ctx->d_pair);
+  ctx->launches++;
+  int tot[2] = {0, 0};
+  ABL_CUDA_TRY(cudaMemcpyAsync(tot, ctx->d_pair, sizeof tot, cudaMemcpyDeviceToHost, s));
+  ABL_CUDA_TRY(cudaStreamSynchronize(s));
+  long survivors = tot[0], children = tot[1];
+  if (sd.uses_remove || self_add) {
+    long need = survivors + (self_add ? children : 0);
+    // `out` holds the step's result; compact it into the other buffer.
+    if (need > t.cap) {
+      ABL_TRY(grow_type(ctx, t, need));
+      regrow = true;
+    }
+    MoveArgs a = move_args(*t.d, t.cols[1 - t.cur], t.cols[t.cur]);
+    k_scatter_flagged<<<nb, B, 0, s>>>(n, st.keep, st.keep_pos, 0, a);
+    ctx->launches++;
+    if (self_add && children > 0) {
+      MoveArgs c = move_args(*t.d, st.child_cols, t.cols[t.cur]);
+      k_scatter_flagged<<<nb, B, 0, s>>>(n, st.child, st.child_pos, survivors, c);
+      ctx->launches++;
+    }
+    t.n = need;  // result now in cols[cur]
+  } else {
+    t.cur = 1 - t.cur;
+  }
+  if (sd.add_type >= 0 && !self_add && children > 0) {
+    TypeState &t2 = ctx->types[sd.add_type];
+    long need = t2.n + children;
+    if (need > t2.cap) {
+      ABL_TRY(grow_type(ctx, t2, need));
+      regrow = true;
+    }
+    MoveArgs c = move_args(*t2.d, st.child_cols, t2.cols[t2.cur]);
+    k_scatter_flagged<<<nb, B, 0, s>>>(n, st.child, st.child_pos, t2.n, c);
+    ctx->launches++;
+    t2.n = need;
+    t2.dirty = true;
+  }
+  t.dirty = true;
   return ABL_OK;
 }
 
@@ -651,6 +902,7 @@ void type_amax(abl_ctx *ctx, TypeState &t) {
 // One iteration of the simulate loop (src/backend/CPrinter.cpp:189-233).
 int step_once(abl_ctx *ctx) {
   const abl_model_desc *m = ctx->model;
+  if (m->seq_step) cudaEventRecord(ctx->ts0, ctx->stream);
   for (int k = 0; k < m->num_steps; k++) {
     const abl_step_desc &sd = m->steps[k];
     TypeState &t = ctx->types[sd.agent_type];
@@ -660,6 +912,16 @@ int step_once(abl_ctx *ctx) {
     L.globals = ctx->globals.data();
     L.error = ctx->error;
     L.block = 128;
+    L.seed = ctx->seed;
+    L.timestep = ctx->timestep;
+    L.step_index = k;
+    bool changes = sd.uses_remove || sd.add_type >= 0;
+    if (changes) {
+      StepState &st = ctx->step_state[k];
+      L.removed = st.removed;
+      L.child_flag = st.child_flag;
+      for (int j = 0; j < ABL_MAX_MEMBERS; j++) L.child_cols[j] = st.child_cols[j];
+    }
     for (int j = 0; j < t.d->num_members; j++) {
       L.in_cols[j] = t.cols[t.cur][j];
       L.out_cols[j] = t.cols[1 - t.cur][j];
@@ -715,10 +977,36 @@ int step_once(abl_ctx *ctx) {
         ctx->prof_pending[k].push_back({e0, e1});
       }
     }
-    t.cur = 1 - t.cur;  // swap agents_X and agents_X_dbuf
-    t.dirty = true;
+    if (changes) {
+      bool regrow = false;
+      ABL_TRY(apply_population_changes(ctx, k, regrow));
+      if (regrow) ABL_TRY(prepare(ctx));
+    } else {
+      t.cur = 1 - t.cur;  // swap agents_X and agents_X_dbuf
+      t.dirty = true;
+    }
+  }
+  ctx->timestep++;
+  if (m->seq_step) {
+    // The sequential step runs on the host after the parallel steps
+    // (src/AnalysisVisitor.cpp:695-704), with this timestep's device time.
+    cudaEventRecord(ctx->ts1, ctx->stream);
+    ABL_CUDA_TRY(cudaEventSynchronize(ctx->ts1));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ts0, ctx->ts1);
+    ctx->last_timestep = ms / 1000.0;
+    ABL_TRY(m->seq_step(ctx, ctx->globals.data()));
   }
   return ABL_OK;
+}
+
+bool graph_capturable(const abl_ctx *ctx) {
+  const abl_model_desc *m = ctx->model;
+  if (m->seq_step) return false;
+  for (int k = 0; k < m->num_steps; k++) {
+    if (m->steps[k].uses_remove || m->steps[k].add_type >= 0) return false;
+  }
+  return true;
 }
 
 int check_error(abl_ctx *ctx) {
@@ -866,6 +1154,11 @@ int abl_create(const abl_model_desc *model, size_t hbm_budget, abl_ctx **out) {
   ctx->globals.assign((const unsigned char *) model->globals_default,
                       (const unsigned char *) model->globals_default + model->globals_size);
   ctx->types.resize(model->num_agent_types);
+  for (int k = 0; k < model->num_steps; k++) {
+    const abl_step_desc &sd = model->steps[k];
+    if (sd.uses_remove) ctx->types[sd.agent_type].dynamic = true;
+    if (sd.add_type >= 0) ctx->types[sd.add_type].dynamic = true;
+  }
   for (int k = 0; k < model->num_agent_types; k++) {
     ctx->types[k].d = &model->agents[k];
     if (model->agents[k].num_members > ABL_MAX_MEMBERS) {
@@ -876,6 +1169,8 @@ int abl_create(const abl_model_desc *model, size_t hbm_budget, abl_ctx **out) {
   cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ts0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ts1);
   if (e != cudaSuccess) {
     std::fprintf(stderr, "openabl-cuda: context setup failed: %s\n", cudaGetErrorString(e));
     delete ctx;
@@ -905,16 +1200,20 @@ int abl_upload(abl_ctx *ctx, int type_id, const void *const *cols, size_t n) {
   if (n > (size_t) INT32_MAX) return ABL_E_UNSUPPORTED;
   TypeState &t = ctx->types[type_id];
   if (n > 0 && !cols) return ABL_E_INVALID;
-  // (Re)allocate both buffers when the count changes.
-  bool resized_alloc = !t.uploaded || (long) n != t.n;
+  // (Re)allocate both buffers when the count changes (types whose population
+  // changes at run time keep spare capacity and reallocate only to grow).
+  long want_cap = t.dynamic ? std::max<long>(2 * (long) n, 1024) : (long) n;
+  bool resized_alloc = !t.uploaded || (t.dynamic ? (long) n > t.cap : (long) n != t.n);
   if (resized_alloc) {
     for (int b = 0; b < 2; b++) {
       for (int k = 0; k < t.d->num_members; k++) {
         if (t.cols[b][k]) dev_free(ctx, t.cols[b][k]);
         t.cols[b][k] = nullptr;
-        ABL_TRY(dev_alloc(ctx, &t.cols[b][k], member_bytes(t.d->members[k]) * std::max<size_t>(n, 1)));
+        ABL_TRY(dev_alloc(ctx, &t.cols[b][k],
+                          member_bytes(t.d->members[k]) * std::max<long>(want_cap, 1)));
       }
     }
+    t.cap = want_cap;
   }
   bool resized = resized_alloc;
   t.n = (long) n;
@@ -941,10 +1240,13 @@ static int ensure_ready(abl_ctx *ctx) {
   for (auto &t : ctx->types) {
     if (!t.uploaded) {
       // Types never uploaded have no agents.
+      long cap = t.dynamic ? 1024 : 1;
       for (int b = 0; b < 2; b++)
         for (int k = 0; k < t.d->num_members; k++)
-          if (!t.cols[b][k]) ABL_TRY(dev_alloc(ctx, &t.cols[b][k], member_bytes(t.d->members[k])));
+          if (!t.cols[b][k])
+            ABL_TRY(dev_alloc(ctx, &t.cols[b][k], member_bytes(t.d->members[k]) * cap));
       t.n = 0;
+      t.cap = cap;
       t.uploaded = true;
     }
   }
@@ -964,7 +1266,7 @@ int abl_run(abl_ctx *ctx, int timesteps) {
     ABL_TRY(step_once(ctx));
     done = 1;
   }
-  if (timesteps - done >= 2 && !ctx->profile) {
+  if (timesteps - done >= 2 && !ctx->profile && graph_capturable(ctx)) {
     abl_ctx::Graph *G = nullptr;
     std::vector<int> key = graph_key(ctx);
     ABL_TRY(capture_graph(ctx, &G));
@@ -1015,14 +1317,96 @@ int abl_download(abl_ctx *ctx, int type_id, void *const *cols, size_t *n) {
 }
 
 int abl_reduce(abl_ctx *ctx, int kind, int type_id, int member, void *out) {
-  (void) kind;
-  (void) member;
   if (!ctx || !out || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
-  if (kind == 0) {
-    *(int *) out = (int) ctx->types[type_id].n;
+  TypeState &t = ctx->types[type_id];
+  if (kind == ABL_REDUCE_COUNT) {
+    *(int *) out = (int) t.n;
     return ABL_OK;
   }
-  return ABL_E_UNSUPPORTED;
+  if (member < 0 || member >= t.d->num_members) return ABL_E_INVALID;
+  const abl_member_desc &md = t.d->members[member];
+  const void *col = t.cols[t.cur][member];
+  cudaStream_t s = ctx->stream;
+  if (!ctx->d_pair) ABL_TRY(dev_alloc_t(ctx, &ctx->d_pair, 2));
+  if (!ctx->d_red) ABL_TRY(dev_alloc_t(ctx, &ctx->d_red, 4));
+  if (kind == ABL_REDUCE_SUM) {
+    if (md.value_type == ABL_T_BOOL || md.value_type == ABL_T_INT) {
+      ABL_CUDA_TRY(cudaMemsetAsync(ctx->d_red, 0, sizeof(double) * 4, s));
+      k_sum_int<<<blocks_for(t.n, 256), 256, 0, s>>>(col, md.scalar_bytes, t.n,
+                                                     (unsigned long long *) ctx->d_red);
+      long long v = 0;
+      ABL_CUDA_TRY(cudaMemcpyAsync(&v, ctx->d_red, sizeof v, cudaMemcpyDeviceToHost, s));
+      ABL_CUDA_TRY(cudaStreamSynchronize(s));
+      *(int *) out = (int) v;
+      return ABL_OK;
+    }
+    // Floating-point members: added in ascending agent order, one thread,
+    // so that the result does not depend on the launch configuration.
+    k_sum_seq<<<1, 1, 0, s>>>(col, md.scalar_bytes, md.components, t.n, ctx->d_red);
+    double v[3] = {0, 0, 0};
+    ABL_CUDA_TRY(cudaMemcpyAsync(v, ctx->d_red, sizeof v, cudaMemcpyDeviceToHost, s));
+    ABL_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int c = 0; c < md.components; c++) {
+      if (md.scalar_bytes == 4) ((float *) out)[c] = (float) v[c];
+      else ((double *) out)[c] = v[c];
+    }
+    return ABL_OK;
+  }
+  if (kind == ABL_REDUCE_COUNT_EQ) {
+    unsigned char value[24];
+    size_t vb = member_bytes(md);
+    std::memcpy(value, out, vb);
+    EqArgs a;
+    std::memcpy(a.value, value, vb);
+    a.bytes = (int) vb;
+    a.scalar = md.scalar_bytes;
+    a.is_float = md.value_type == ABL_T_FLOAT || md.value_type == ABL_T_FLOAT2
+                 || md.value_type == ABL_T_FLOAT3;
+    ABL_CUDA_TRY(cudaMemsetAsync(ctx->d_red, 0, sizeof(double) * 4, s));
+    k_count_eq<<<blocks_for(t.n, 256), 256, 0, s>>>(col, t.n, a,
+                                                    (unsigned long long *) ctx->d_red);
+    long long c = 0;
+    ABL_CUDA_TRY(cudaMemcpyAsync(&c, ctx->d_red, sizeof c, cudaMemcpyDeviceToHost, s));
+    ABL_CUDA_TRY(cudaStreamSynchronize(s));
+    *(int *) out = (int) c;
+    return ABL_OK;
+  }
+  return ABL_E_INVALID;
+}
+
+int abl_set_seed(abl_ctx *ctx, uint64_t seed) {
+  if (!ctx) return ABL_E_INVALID;
+  ctx->seed = seed;
+  return ABL_OK;
+}
+
+int abl_last_timestep_time(abl_ctx *ctx, double *seconds) {
+  if (!ctx || !seconds) return ABL_E_INVALID;
+  *seconds = ctx->last_timestep;
+  return ABL_OK;
+}
+
+int abl_log_csv(abl_ctx *ctx, const char *fmt, ...) {
+  if (!ctx || !fmt) return ABL_E_INVALID;
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  int len = std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (len < 0) return ABL_E_INVALID;
+  ctx->log.append(buf, std::min<size_t>((size_t) len, sizeof buf - 1));
+  return ABL_OK;
+}
+
+int abl_log_text(abl_ctx *ctx, char *buf, size_t cap, size_t *len) {
+  if (!ctx) return ABL_E_INVALID;
+  if (len) *len = ctx->log.size();
+  if (buf && cap) {
+    size_t c = std::min(cap - 1, ctx->log.size());
+    std::memcpy(buf, ctx->log.data(), c);
+    buf[c] = 0;
+  }
+  return ABL_OK;
 }
 
 int abl_last_exec_time(abl_ctx *ctx, double *seconds) {
@@ -1067,6 +1451,8 @@ int abl_destroy(abl_ctx *ctx) {
   for (void *p : ctx->allocations) cudaFree(p);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->ts0) cudaEventDestroy(ctx->ts0);
+  if (ctx->ts1) cudaEventDestroy(ctx->ts1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return ABL_OK;

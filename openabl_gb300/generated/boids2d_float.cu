@@ -57,63 +57,66 @@ static const abl_globals abl_globals_default = {
     3.16228,
 };
 static abl_globals abl_G = abl_globals_default;
+static abl::rng abl_R;  // unused on the host: main() draws from the host stream
 struct abl_cols_Boid {
     float2 *pos;
     float2 *velocity;
 };
 
-static inline float2 random_1(const abl_globals &abl_G, float2 min, float2 max) {
-    return float2_create(random_float(min.x, max.x), random_float(min.y, max.y));
+__host__ __device__ static inline float2 random_1(const abl_globals &abl_G, abl::rng &abl_R, float2 min, float2 max) {
+    return float2_create(abl_random(abl_R, min.x, max.x), abl_random(abl_R, min.y, max.y));
 }
-static inline float3 random_2(const abl_globals &abl_G, float3 min, float3 max) {
-    return float3_create(random_float(min.x, max.x), random_float(min.y, max.y), random_float(min.z, max.z));
+__host__ __device__ static inline float3 random_2(const abl_globals &abl_G, abl::rng &abl_R, float3 min, float3 max) {
+    return float3_create(abl_random(abl_R, min.x, max.x), abl_random(abl_R, min.y, max.y), abl_random(abl_R, min.z, max.z));
 }
-static inline float random_3(const abl_globals &abl_G, float max) {
-    return random_float(0, max);
+__host__ __device__ static inline float random_3(const abl_globals &abl_G, abl::rng &abl_R, float max) {
+    return abl_random(abl_R, 0, max);
 }
-static inline float2 random_4(const abl_globals &abl_G, float2 max) {
-    return random_1(abl_G, float2_fill(0), max);
+__host__ __device__ static inline float2 random_4(const abl_globals &abl_G, abl::rng &abl_R, float2 max) {
+    return random_1(abl_G, abl_R, float2_fill(0), max);
 }
-static inline float3 random_5(const abl_globals &abl_G, float3 max) {
-    return random_2(abl_G, float3_fill(0), max);
+__host__ __device__ static inline float3 random_5(const abl_globals &abl_G, abl::rng &abl_R, float3 max) {
+    return random_2(abl_G, abl_R, float3_fill(0), max);
 }
-static inline int randomInt_1(const abl_globals &abl_G, int max) {
-    return random_int(0, max);
+__host__ __device__ static inline int randomInt_1(const abl_globals &abl_G, abl::rng &abl_R, int max) {
+    return abl_random_int(abl_R, 0, max);
 }
-__host__ __device__ static inline float clamp(const abl_globals &abl_G, float pos, float min, float max) {
+__host__ __device__ static inline float clamp(const abl_globals &abl_G, abl::rng &abl_R, float pos, float min, float max) {
     return ((pos < min) ? min : ((pos > max) ? max : pos));
 }
-__host__ __device__ static inline float2 clamp_1(const abl_globals &abl_G, float2 pos, float2 min, float2 max) {
+__host__ __device__ static inline float2 clamp_1(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 min, float2 max) {
     return float2_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)));
 }
-__host__ __device__ static inline float3 clamp_2(const abl_globals &abl_G, float3 pos, float3 min, float3 max) {
+__host__ __device__ static inline float3 clamp_2(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 min, float3 max) {
     return float3_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)), ((pos.z < min.z) ? min.z : ((pos.z > max.z) ? max.z : pos.z)));
 }
-__host__ __device__ static inline float clamp_3(const abl_globals &abl_G, float pos, float max) {
-    return clamp(abl_G, pos, 0, max);
+__host__ __device__ static inline float clamp_3(const abl_globals &abl_G, abl::rng &abl_R, float pos, float max) {
+    return clamp(abl_G, abl_R, pos, 0, max);
 }
-__host__ __device__ static inline float2 clamp_4(const abl_globals &abl_G, float2 pos, float2 max) {
-    return clamp_1(abl_G, pos, float2_fill(0), max);
+__host__ __device__ static inline float2 clamp_4(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return clamp_1(abl_G, abl_R, pos, float2_fill(0), max);
 }
-__host__ __device__ static inline float3 clamp_5(const abl_globals &abl_G, float3 pos, float3 max) {
-    return clamp_2(abl_G, pos, float3_fill(0), max);
+__host__ __device__ static inline float3 clamp_5(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 max) {
+    return clamp_2(abl_G, abl_R, pos, float3_fill(0), max);
 }
-__host__ __device__ static inline float wraparound(const abl_globals &abl_G, float pos, float max) {
+__host__ __device__ static inline float wraparound(const abl_globals &abl_G, abl::rng &abl_R, float pos, float max) {
     return ((pos < 0) ? (max + pos) : ((pos >= max) ? (pos - max) : pos));
 }
-__host__ __device__ static inline float2 wraparound_1(const abl_globals &abl_G, float2 pos, float2 max) {
+__host__ __device__ static inline float2 wraparound_1(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
     return float2_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)));
 }
-__host__ __device__ static inline float3 wraparound_2(const abl_globals &abl_G, float3 pos, float3 max) {
+__host__ __device__ static inline float3 wraparound_2(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 max) {
     return float3_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)), ((pos.z < 0) ? (max.z + pos.z) : ((pos.z >= max.z) ? (pos.z - max.z) : pos.z)));
 }
-__host__ __device__ static inline bool is_inside(const abl_globals &abl_G, float2 pos, float2 max) {
+__host__ __device__ static inline bool is_inside(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
     return ((((pos.x >= 0) && (pos.y >= 0)) && (pos.x <= max.x)) && (pos.y <= max.y));
 }
-__host__ __device__ static inline float2 boundPosition(const abl_globals &abl_G, float2 pos) {
+__host__ __device__ static inline float2 boundPosition(const abl_globals &abl_G, abl::rng &abl_R, float2 pos) {
     return float2_create(((pos.x < abl_G.min_pos) ? abl_G.max_pos : ((pos.x > abl_G.max_pos) ? abl_G.min_pos : pos.x)), ((pos.y < abl_G.min_pos) ? abl_G.max_pos : ((pos.y > abl_G.max_pos) ? abl_G.min_pos : pos.y)));
 }
-__device__ static void update_boid(const abl_globals &abl_G, const abl_near_view &abl_NB, Boid* in, Boid* out) {
+__device__ static void update_boid(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Boid* in, Boid* out) {
+    abl::rng &abl_R = abl_K.R;
+    (void) abl_R; (void) abl_NB;
     float2 global_velocity = float2_create(0, 0);
     float2 global_center = float2_create(0, 0);
     float2 collision_center = float2_create(0, 0);
@@ -171,7 +174,7 @@ __device__ static void update_boid(const abl_globals &abl_G, const abl_near_view
         new_velocity = float2_div_scalar(new_velocity, new_velocity_scale);
     }
     float2 new_pos = float2_add(in->pos, float2_mul_scalar(new_velocity, abl_G.time_scale));
-    new_pos = boundPosition(abl_G, new_pos);
+    new_pos = boundPosition(abl_G, abl_R, new_pos);
     out->pos = new_pos;
     out->velocity = new_velocity;
 }
@@ -182,15 +185,27 @@ struct abl_kargs_update_boid {
     const int *visit;
     abl_cols_Boid in, out;
     abl_near_view NB;
+    uint8_t *removed;
+    uint8_t *child_flag;
+    void *child_cols[ABL_MAX_MEMBERS];
+    uint64_t seed;
+    long timestep;
+    int step_index;
 };
-__global__ void __launch_bounds__(128) abl_kernel_update_boid(const __grid_constant__ abl_kargs_update_boid A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_update_boid(const __grid_constant__ abl_kargs_update_boid A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = A.child_cols;
     Boid abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.velocity = A.in.velocity[abl_i];
-    update_boid(A.G, A.NB, &abl_in, &abl_out);
+    update_boid(A.G, A.NB, abl_K, &abl_in, &abl_out);
     A.out.pos[abl_i] = abl_out.pos;
     A.out.velocity[abl_i] = abl_out.velocity;
 }
@@ -204,14 +219,21 @@ static int abl_launch_update_boid(const abl_step_launch *L, cudaStream_t abl_str
     A.in.velocity = (float2 *) L->in_cols[1];
     A.out.velocity = (float2 *) L->out_cols[1];
     A.NB = L->near;
-    const int abl_block = L->block > 0 ? L->block : 128;
+    A.removed = L->removed;
+    A.child_flag = L->child_flag;
+    for (int k = 0; k < ABL_MAX_MEMBERS; k++) A.child_cols[k] = L->child_cols[k];
+    A.seed = L->seed;
+    A.timestep = L->timestep;
+    A.step_index = L->step_index;
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_update_boid<<<abl_grid, abl_block, 0, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_update_boid(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
-    (void) abl_G;
+    abl::rng abl_R;
+    (void) abl_G; (void) abl_R;
     return (double) (abl_G.interaction_radius);
 }
 
@@ -241,21 +263,22 @@ static const abl_global_desc abl_global_table[] = {
 };
 static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
-    (void) abl_G;
+    abl::rng abl_R;
+    (void) abl_G; (void) abl_R;
     float2 abl_lo = float2_fill(abl_G.min_pos);
     float2 abl_hi = float2_fill(abl_G.max_pos);
     abl_min[0] = abl_lo.x; abl_min[1] = abl_lo.y; abl_min[2] = 0;
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"update_boid", 0, 0, 1, abl_radius_update_boid, 3u, 3u, abl_launch_update_boid},
+    {"update_boid", 0, 0, 1, abl_radius_update_boid, 3u, 3u, abl_launch_update_boid, 0, -1, 0},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],
-    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr}
+    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0}
 };
 extern const abl_model_desc abl_desc = {
-    "boids2d_float", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 13, abl_global_table, 2, abl_env_bounds, nullptr, 1
+    "boids2d_float", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 13, abl_global_table, 2, abl_env_bounds, nullptr, 1, nullptr
 };
 static void abl_check(int r, const char *what) {
     if (r != ABL_OK) {
@@ -298,13 +321,20 @@ static void abl_simulate(int abl_timesteps) {
         std::free(c0);
         std::free(c1);
     }
-    double abl_secs = 0;
-    abl_last_exec_time(ctx, &abl_secs);
+    size_t abl_log_len = 0;
+    abl_log_text(ctx, nullptr, 0, &abl_log_len);
+    if (abl_log_len > 0) {
+        char *abl_log = (char *) std::malloc(abl_log_len + 1);
+        abl_log_text(ctx, abl_log, abl_log_len + 1, nullptr);
+        FILE *abl_f = std::fopen("log.csv", "w");
+        if (abl_f) { std::fputs(abl_log, abl_f); std::fclose(abl_f); }
+        std::free(abl_log);
+    }
     abl_destroy(ctx);
 }
 static int abl_main() {
     for (int i = 0, _var0 = abl_G.num_agents; i < _var0; ++i) {
-        *DYN_ARRAY_PLACE(&agents.agents_Boid, Boid) = ([&]() { Boid abl_a; abl_a.pos = random_1(abl_G, float2_fill(abl_G.min_pos), float2_fill(abl_G.max_pos)); abl_a.velocity = random_1(abl_G, float2_fill((-1)), float2_fill(1)); return abl_a; }());
+        *DYN_ARRAY_PLACE(&agents.agents_Boid, Boid) = ([&]() { Boid abl_a; abl_a.pos = random_1(abl_G, abl_R, float2_fill(abl_G.min_pos), float2_fill(abl_G.max_pos)); abl_a.velocity = random_1(abl_G, abl_R, float2_fill((-1)), float2_fill(1)); return abl_a; }());
     }
     abl_simulate(abl_G.num_timesteps);
     save(&agents, agents_info, "boids.out", SAVE_JSON);

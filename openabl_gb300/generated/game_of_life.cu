@@ -45,60 +45,63 @@ static const abl_globals abl_globals_default = {
     20,
 };
 static abl_globals abl_G = abl_globals_default;
+static abl::rng abl_R;  // unused on the host: main() draws from the host stream
 struct abl_cols_Cell {
     float2 *pos;
     bool *alive;
 };
 
-static inline float2 random_1(const abl_globals &abl_G, float2 min, float2 max) {
-    return float2_create(random_float(min.x, max.x), random_float(min.y, max.y));
+__host__ __device__ static inline float2 random_1(const abl_globals &abl_G, abl::rng &abl_R, float2 min, float2 max) {
+    return float2_create(abl_random(abl_R, min.x, max.x), abl_random(abl_R, min.y, max.y));
 }
-static inline float3 random_2(const abl_globals &abl_G, float3 min, float3 max) {
-    return float3_create(random_float(min.x, max.x), random_float(min.y, max.y), random_float(min.z, max.z));
+__host__ __device__ static inline float3 random_2(const abl_globals &abl_G, abl::rng &abl_R, float3 min, float3 max) {
+    return float3_create(abl_random(abl_R, min.x, max.x), abl_random(abl_R, min.y, max.y), abl_random(abl_R, min.z, max.z));
 }
-static inline double random_3(const abl_globals &abl_G, double max) {
-    return random_float(0, max);
+__host__ __device__ static inline double random_3(const abl_globals &abl_G, abl::rng &abl_R, double max) {
+    return abl_random(abl_R, 0, max);
 }
-static inline float2 random_4(const abl_globals &abl_G, float2 max) {
-    return random_1(abl_G, float2_fill(0), max);
+__host__ __device__ static inline float2 random_4(const abl_globals &abl_G, abl::rng &abl_R, float2 max) {
+    return random_1(abl_G, abl_R, float2_fill(0), max);
 }
-static inline float3 random_5(const abl_globals &abl_G, float3 max) {
-    return random_2(abl_G, float3_fill(0), max);
+__host__ __device__ static inline float3 random_5(const abl_globals &abl_G, abl::rng &abl_R, float3 max) {
+    return random_2(abl_G, abl_R, float3_fill(0), max);
 }
-static inline int randomInt_1(const abl_globals &abl_G, int max) {
-    return random_int(0, max);
+__host__ __device__ static inline int randomInt_1(const abl_globals &abl_G, abl::rng &abl_R, int max) {
+    return abl_random_int(abl_R, 0, max);
 }
-__host__ __device__ static inline double clamp(const abl_globals &abl_G, double pos, double min, double max) {
+__host__ __device__ static inline double clamp(const abl_globals &abl_G, abl::rng &abl_R, double pos, double min, double max) {
     return ((pos < min) ? min : ((pos > max) ? max : pos));
 }
-__host__ __device__ static inline float2 clamp_1(const abl_globals &abl_G, float2 pos, float2 min, float2 max) {
+__host__ __device__ static inline float2 clamp_1(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 min, float2 max) {
     return float2_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)));
 }
-__host__ __device__ static inline float3 clamp_2(const abl_globals &abl_G, float3 pos, float3 min, float3 max) {
+__host__ __device__ static inline float3 clamp_2(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 min, float3 max) {
     return float3_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)), ((pos.z < min.z) ? min.z : ((pos.z > max.z) ? max.z : pos.z)));
 }
-__host__ __device__ static inline double clamp_3(const abl_globals &abl_G, double pos, double max) {
-    return clamp(abl_G, pos, 0, max);
+__host__ __device__ static inline double clamp_3(const abl_globals &abl_G, abl::rng &abl_R, double pos, double max) {
+    return clamp(abl_G, abl_R, pos, 0, max);
 }
-__host__ __device__ static inline float2 clamp_4(const abl_globals &abl_G, float2 pos, float2 max) {
-    return clamp_1(abl_G, pos, float2_fill(0), max);
+__host__ __device__ static inline float2 clamp_4(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return clamp_1(abl_G, abl_R, pos, float2_fill(0), max);
 }
-__host__ __device__ static inline float3 clamp_5(const abl_globals &abl_G, float3 pos, float3 max) {
-    return clamp_2(abl_G, pos, float3_fill(0), max);
+__host__ __device__ static inline float3 clamp_5(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 max) {
+    return clamp_2(abl_G, abl_R, pos, float3_fill(0), max);
 }
-__host__ __device__ static inline double wraparound(const abl_globals &abl_G, double pos, double max) {
+__host__ __device__ static inline double wraparound(const abl_globals &abl_G, abl::rng &abl_R, double pos, double max) {
     return ((pos < 0) ? (max + pos) : ((pos >= max) ? (pos - max) : pos));
 }
-__host__ __device__ static inline float2 wraparound_1(const abl_globals &abl_G, float2 pos, float2 max) {
+__host__ __device__ static inline float2 wraparound_1(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
     return float2_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)));
 }
-__host__ __device__ static inline float3 wraparound_2(const abl_globals &abl_G, float3 pos, float3 max) {
+__host__ __device__ static inline float3 wraparound_2(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 max) {
     return float3_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)), ((pos.z < 0) ? (max.z + pos.z) : ((pos.z >= max.z) ? (pos.z - max.z) : pos.z)));
 }
-__host__ __device__ static inline bool is_inside(const abl_globals &abl_G, float2 pos, float2 max) {
+__host__ __device__ static inline bool is_inside(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
     return ((((pos.x >= 0) && (pos.y >= 0)) && (pos.x <= max.x)) && (pos.y <= max.y));
 }
-__device__ static void step_move(const abl_globals &abl_G, const abl_near_view &abl_NB, Cell* in, Cell* out) {
+__device__ static void step_move(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Cell* in, Cell* out) {
+    abl::rng &abl_R = abl_K.R;
+    (void) abl_R; (void) abl_NB;
     int living_neighbors = 0;
     {
         const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
@@ -134,16 +137,28 @@ struct abl_kargs_step_move {
     const int *visit;
     abl_cols_Cell in, out;
     abl_near_view NB;
+    uint8_t *removed;
+    uint8_t *child_flag;
+    void *child_cols[ABL_MAX_MEMBERS];
+    uint64_t seed;
+    long timestep;
+    int step_index;
 };
-__global__ void __launch_bounds__(128) abl_kernel_step_move(const __grid_constant__ abl_kargs_step_move A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_step_move(const __grid_constant__ abl_kargs_step_move A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = A.child_cols;
     Cell abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.alive = A.in.alive[abl_i];
     abl_out.alive = A.out.alive[abl_i];
-    step_move(A.G, A.NB, &abl_in, &abl_out);
+    step_move(A.G, A.NB, abl_K, &abl_in, &abl_out);
     A.out.pos[abl_i] = abl_out.pos;
     A.out.alive[abl_i] = abl_out.alive;
 }
@@ -157,22 +172,29 @@ static int abl_launch_step_move(const abl_step_launch *L, cudaStream_t abl_strea
     A.in.alive = (bool *) L->in_cols[1];
     A.out.alive = (bool *) L->out_cols[1];
     A.NB = L->near;
-    const int abl_block = L->block > 0 ? L->block : 128;
+    A.removed = L->removed;
+    A.child_flag = L->child_flag;
+    for (int k = 0; k < ABL_MAX_MEMBERS; k++) A.child_cols[k] = L->child_cols[k];
+    A.seed = L->seed;
+    A.timestep = L->timestep;
+    A.step_index = L->step_index;
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_step_move<<<abl_grid, abl_block, 0, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_step_move(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
-    (void) abl_G;
+    abl::rng abl_R;
+    (void) abl_G; (void) abl_R;
     return (double) (abl_G.radius);
 }
 
-static inline bool getInit(const abl_globals &abl_G, int x, int y) {
+__host__ __device__ static inline bool getInit(const abl_globals &abl_G, abl::rng &abl_R, int x, int y) {
     if (abl_G.debug) {
         return ((((x == 10) || (x == 11)) || (x == 12)) && (y == 10));
     } else {
-        return (random_float(0, 1) < abl_G.alive_fraction);
+        return (abl_random(abl_R, 0, 1) < abl_G.alive_fraction);
     }
 }
 
@@ -195,21 +217,22 @@ static const abl_global_desc abl_global_table[] = {
 };
 static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
-    (void) abl_G;
+    abl::rng abl_R;
+    (void) abl_G; (void) abl_R;
     float2 abl_lo = float2_fill(0);
     float2 abl_hi = float2_fill(abl_G.size);
     abl_min[0] = abl_lo.x; abl_min[1] = abl_lo.y; abl_min[2] = 0;
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"step_move", 0, 0, 0, abl_radius_step_move, 3u, 1u, abl_launch_step_move},
+    {"step_move", 0, 0, 0, abl_radius_step_move, 3u, 1u, abl_launch_step_move, 0, -1, 0},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],
-    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr}
+    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0}
 };
 extern const abl_model_desc abl_desc = {
-    "game_of_life", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 7, abl_global_table, 2, abl_env_bounds, nullptr, 0
+    "game_of_life", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 7, abl_global_table, 2, abl_env_bounds, nullptr, 0, nullptr
 };
 static void abl_check(int r, const char *what) {
     if (r != ABL_OK) {
@@ -252,14 +275,21 @@ static void abl_simulate(int abl_timesteps) {
         std::free(c0);
         std::free(c1);
     }
-    double abl_secs = 0;
-    abl_last_exec_time(ctx, &abl_secs);
+    size_t abl_log_len = 0;
+    abl_log_text(ctx, nullptr, 0, &abl_log_len);
+    if (abl_log_len > 0) {
+        char *abl_log = (char *) std::malloc(abl_log_len + 1);
+        abl_log_text(ctx, abl_log, abl_log_len + 1, nullptr);
+        FILE *abl_f = std::fopen("log.csv", "w");
+        if (abl_f) { std::fputs(abl_log, abl_f); std::fclose(abl_f); }
+        std::free(abl_log);
+    }
     abl_destroy(ctx);
 }
 static int abl_main() {
     for (int x = 0, _var0 = abl_G.size; x < _var0; ++x) {
         for (int y = 0, _var1 = abl_G.size; y < _var1; ++y) {
-            *DYN_ARRAY_PLACE(&agents.agents_Cell, Cell) = ([&]() { Cell abl_a; abl_a.pos = float2_create(((float) x + 0.5), ((float) y + 0.5)); abl_a.alive = getInit(abl_G, x, y); return abl_a; }());
+            *DYN_ARRAY_PLACE(&agents.agents_Cell, Cell) = ([&]() { Cell abl_a; abl_a.pos = float2_create(((float) x + 0.5), ((float) y + 0.5)); abl_a.alive = getInit(abl_G, abl_R, x, y); return abl_a; }());
         }
     }
     abl_simulate(abl_G.num_timesteps);

@@ -28,6 +28,7 @@ MODELS = {
     "boids2d": ("boids2d.abl", {}),
     "game_of_life": ("game_of_life.abl", {}),
     "boids2d_float": ("boids2d.abl", {"use_float": "true"}),
+    "predator_prey": ("predator_prey.abl", {}),
 }
 
 # configuration name -> (model, -P params)
@@ -46,6 +47,12 @@ CONFIGS = {
                                          "num_timesteps": "100"}),
     "game_of_life_4096": ("game_of_life", {"num_agents": "16777216", "alive_fraction": "0.5",
                                            "num_timesteps": "100"}),
+    # 800,000 prey and 200,000 predators (and 1,000,000 grass) at the file's
+    # density of 1600 agents per unit area.
+    "predator_prey_1m": ("predator_prey", {"num_agents": "2000000", "prey_fraction": "0.4",
+                                           "predator_fraction": "0.1", "num_timesteps": "500"}),
+    "predator_prey_small": ("predator_prey", {"num_agents": "20000", "prey_fraction": "0.4",
+                                              "predator_fraction": "0.1", "num_timesteps": "50"}),
 }
 
 

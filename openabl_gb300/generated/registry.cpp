@@ -7,6 +7,7 @@ const abl_model_desc *abl_model_desc_circle3d(void);
 const abl_model_desc *abl_model_desc_boids2d(void);
 const abl_model_desc *abl_model_desc_game_of_life(void);
 const abl_model_desc *abl_model_desc_boids2d_float(void);
+const abl_model_desc *abl_model_desc_predator_prey(void);
 extern const abl_model_desc *const abl_builtin_models[];
 const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_circle(),
@@ -14,5 +15,6 @@ const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_boids2d(),
     abl_model_desc_game_of_life(),
     abl_model_desc_boids2d_float(),
+    abl_model_desc_predator_prey(),
     nullptr};
 }

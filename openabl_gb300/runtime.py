@@ -276,6 +276,43 @@ class Simulation:
         _check(_load().abl_memory_used(self.ctx, ctypes.byref(b)), "abl_memory_used")
         return b.value
 
+    def set_seed(self, seed):
+        L = _load()
+        L.abl_set_seed.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        _check(L.abl_set_seed(self.ctx, int(seed)), "abl_set_seed")
+
+    def log_text(self):
+        """Rows written by log_csv() in the model's sequential step."""
+        L = _load()
+        L.abl_log_text.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
+                                   ctypes.POINTER(ctypes.c_size_t)]
+        n = ctypes.c_size_t()
+        _check(L.abl_log_text(self.ctx, None, 0, ctypes.byref(n)), "abl_log_text")
+        buf = ctypes.create_string_buffer(n.value + 1)
+        _check(L.abl_log_text(self.ctx, buf, n.value + 1, None), "abl_log_text")
+        return buf.value.decode()
+
+    def reduce(self, kind, type_name, member=None, value=None):
+        """count / sum / count-equal of the sequential-step builtins."""
+        L = _load()
+        tid = self.model.type_id(type_name)
+        midx = 0
+        vt = None
+        if member is not None:
+            names = [m for m, _ in self._members(tid)]
+            midx = names.index(member)
+            vt = self._members(tid)[midx][1]
+        buf = (ctypes.c_ubyte * 32)()
+        if value is not None:
+            dt, shape = member_dtype(vt, self.globals.float_bytes)
+            v = np.ascontiguousarray(np.array(value, dtype=dt).reshape(shape))
+            ctypes.memmove(buf, v.ctypes.data, v.nbytes)
+        _check(L.abl_reduce(self.ctx, kind, tid, midx, buf), "abl_reduce")
+        if kind in (0, 2) or vt in (ABL_T_BOOL, ABL_T_INT):
+            return ctypes.c_int.from_buffer(buf).value
+        dt, shape = member_dtype(vt, self.globals.float_bytes)
+        return np.frombuffer(bytes(buf), dtype=dt, count=int(np.prod(shape) or 1)).copy()
+
     def set_profiling(self, enable=True):
         L = _load()
         L.abl_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]

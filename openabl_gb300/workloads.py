@@ -35,3 +35,24 @@ def game_of_life(size, alive_fraction=0.5, seed=0):
     pos = np.stack([x.ravel() + 0.5, y.ravel() + 0.5], axis=1)
     alive = (rng.uniform(size=size * size) < alive_fraction).astype(np.uint8)
     return {"pos": np.ascontiguousarray(pos), "alive": alive}
+
+
+def predator_prey(n_pred, n_prey, n_grass, env_size, gain_pred=35, gain_prey=60, seed=0):
+    """Uniform positions in [0, env_size)^2 for all three types; animals get a
+    heading (sin phi, cos phi) with phi uniform in [0, 2 pi) and zero steer, as
+    examples/predator_prey.abl:87-90 and :316-333 initialise them, and life
+    GAIN_FROM_FOOD + an integer uniform in [0, 10]; grass starts available."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+
+    def animals(n, gain):
+        phi = rng.uniform(0.0, 2.0 * np.pi, size=n)
+        return {"pos": rng.uniform(0.0, env_size, size=(n, 2)),
+                "dir": np.stack([np.sin(phi), np.cos(phi)], axis=1),
+                "steer": np.zeros((n, 2)),
+                "life": (gain + rng.integers(0, 11, size=n)).astype(np.int32)}
+
+    grass = {"pos": rng.uniform(0.0, env_size, size=(n_grass, 2)),
+             "dead_cycles": np.zeros(n_grass, np.int32),
+             "avail": np.ones(n_grass, np.uint8)}
+    return {"Predator": animals(n_pred, gain_pred), "Prey": animals(n_prey, gain_prey),
+            "Grass": grass}
