@@ -69,6 +69,9 @@ const char *abl_model_agent_name(const abl_model_desc *m, int type_id);
 int abl_model_num_members(const abl_model_desc *m, int type_id);
 int abl_model_member(const abl_model_desc *m, int type_id, int member, const char **name,
                      int *value_type);
+/* Bytes of the model's float type: 8, or 4 when generated with use_float
+ * (LIBABL_USE_FLOAT, asset/c/libabl.h:59-63). */
+int abl_model_float_bytes(const abl_model_desc *m);
 /* Size of the model's globals block (its `param`/constant declarations). */
 size_t abl_model_globals_size(const abl_model_desc *m);
 /* Writes the compile-time values of the globals (the constants printed by
@@ -130,6 +133,36 @@ int abl_set_profiling(abl_ctx *ctx, int enable);
 int abl_step_kernel_time(abl_ctx *ctx, int step, double *seconds, long *launches);
 int abl_destroy(abl_ctx *ctx);
 const char *abl_strerror(int code);
+
+/* ---- ensembles ----
+ *
+ * Many replicas of one model -- different agent counts, parameter points
+ * (globals) and seeds -- run as one population over a segmented grid: each
+ * timestep is one launch per phase for all replicas, replayed from a CUDA
+ * graph.  Per replica the results equal those of a separate context.  Models
+ * with runtime add/remove or a sequential step are not supported. */
+typedef struct abl_ensemble abl_ensemble;
+/* `globals`: replicas x globals_size bytes (NULL: defaults); `seeds`: one
+ * random() seed per replica (NULL: 0). */
+int abl_ensemble_create(const abl_model_desc *model, int replicas, const void *globals,
+                        const uint64_t *seeds, size_t hbm_budget, abl_ensemble **out);
+/* All replicas of one agent type at once: counts[r] agents of replica r,
+ * columns concatenated replica after replica. */
+int abl_ensemble_upload(abl_ensemble *e, int type_id, const size_t *counts,
+                        const void *const *cols);
+int abl_ensemble_run(abl_ensemble *e, int timesteps);
+int abl_ensemble_download(abl_ensemble *e, int type_id, size_t *counts, void *const *cols);
+/* Launch configuration: threads per block of the step kernels (32..128),
+ * cell size as a multiple (>= 1) of the granularity, and whether threads visit
+ * agents in cell order (1) or index order (0).  Results do not depend on it. */
+int abl_ensemble_set_tuning(abl_ensemble *e, int block, double cell_factor, int visit_sorted);
+/* Times every configuration for `trial_timesteps` timesteps, restores the
+ * state after each trial and keeps the fastest. */
+int abl_ensemble_autotune(abl_ensemble *e, int trial_timesteps, int *block, double *cell_factor,
+                          int *visit_sorted);
+int abl_ensemble_last_exec_time(abl_ensemble *e, double *seconds);
+int abl_ensemble_last_launch_count(abl_ensemble *e, long *launches);
+int abl_ensemble_destroy(abl_ensemble *e);
 
 /* ---- allocation-free timestep ----
  *

@@ -508,6 +508,20 @@ void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
   for (auto *call : c.calls) {
     if (call->isBuiltin() && call->name == "removeCurrent") info.usesRemove = true;
   }
+  // Random numbers, drawn directly or through user functions.
+  std::set<const AST::FunctionDeclaration *> seen;
+  std::function<bool(const Collector &)> draws = [&](const Collector &cc) -> bool {
+    for (auto *call : cc.calls) {
+      if (call->isBuiltin() && (call->name == "random" || call->name == "randomInt")) return true;
+      if (call->kind == AST::CallExpression::Kind::USER && call->calledFunc
+          && seen.insert(call->calledFunc).second
+          && draws(collect(*const_cast<AST::FunctionDeclaration *>(call->calledFunc)))) {
+        return true;
+      }
+    }
+    return false;
+  };
+  info.usesRng = draws(c);
   if (decl.runtimeAddedAgent) info.addType = agentIndex(decl.runtimeAddedAgent);
   if (!c.nearLoops.empty()) {
     const AST::ForStatement *loop = c.nearLoops[0];
@@ -646,6 +660,59 @@ void CudaPrinter::printKernel(const StepInfo &info) {
         << "abl_kernel_" << name << "<<<abl_grid, abl_block, 0, abl_stream>>>(A);" << nl
         << "return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;" << outdent << nl
         << "}" << nl;
+  if (info.addType < 0 && !info.usesRemove) {
+    // Ensemble variant: every agent reads its replica's globals and grid.
+    // Random numbers are keyed by the replica's seed and the agent's index
+    // within its replica, so each replica draws what it would draw alone.
+    *this << "__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_" << name
+          << "(const __grid_constant__ abl_ens_launch A) {" << indent << nl
+          << "const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl
+          << "if (abl_t >= A.n) return;" << nl
+          << "const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;" << nl
+          << "const int abl_r = A.replica[abl_i];" << nl
+          << "const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];" << nl
+          << "abl::step_ctx abl_K;" << nl
+          << "abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), "
+             "(uint32_t) A.step_index, (uint64_t) A.timestep);"
+          << nl << "abl_K.self = abl_i;" << nl << "abl_K.removed = 0;" << nl
+          << "abl_K.added = 0;" << nl << "abl_K.child_cols = nullptr;" << nl
+          << T << " abl_in, abl_out;";
+    for (size_t k = 0; k < agent.members->size(); k++) {
+      const AST::AgentMember &m = *(*agent.members)[k];
+      std::string ty = cType(m.type->resolved);
+      *this << nl << "abl_in." << m.name << " = ((const " << ty << " *) A.in_cols[" << (int) k
+            << "])[abl_i];";
+    }
+    for (size_t k = 0; k < agent.members->size(); k++) {
+      const AST::AgentMember &m = *(*agent.members)[k];
+      std::string ty = cType(m.type->resolved);
+      bool maybe = info.outMaybe & (1u << k), always = info.outAlways & (1u << k);
+      if (copy) {
+        *this << nl << "abl_out." << m.name << " = abl_in." << m.name << ";";
+      } else if (maybe && !always) {
+        *this << nl << "abl_out." << m.name << " = ((const " << ty << " *) A.out_cols["
+              << (int) k << "])[abl_i];";
+      }
+    }
+    *this << nl << name << "(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);";
+    for (size_t k = 0; k < agent.members->size(); k++) {
+      const AST::AgentMember &m = *(*agent.members)[k];
+      std::string ty = cType(m.type->resolved);
+      if (copy || (info.outMaybe & (1u << k))) {
+        *this << nl << "((" << ty << " *) A.out_cols[" << (int) k << "])[abl_i] = abl_out."
+              << m.name << ";";
+      }
+    }
+    *this << outdent << nl << "}" << nl
+          << "static int abl_launch_ens_" << name
+          << "(const abl_ens_launch *L, cudaStream_t abl_stream) {" << indent << nl
+          << "const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : "
+             "ABL_STEP_BLOCK;" << nl
+          << "const long abl_grid = (L->n + abl_block - 1) / abl_block;" << nl
+          << "abl_kernel_ens_" << name << "<<<abl_grid, abl_block, 0, abl_stream>>>(*L);" << nl
+          << "return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;" << outdent << nl
+          << "}" << nl;
+  }
   if (info.nearLoop) {
     *this << "static double abl_radius_" << name << "(const void *abl_gp) {" << indent << nl
           << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl
@@ -822,9 +889,11 @@ void CudaPrinter::printDescriptor() {
     *this << nl << "{\"" << n << "\", " << s.agentType << ", " << s.nearType << ", "
           << (s.ordered ? 1 : 0) << ", " << (s.nearLoop ? "abl_radius_" + n : "nullptr") << ", "
           << s.nearMembers << "u, " << s.outAlways << "u, abl_launch_" << n << ", "
-          << (s.usesRemove ? 1 : 0) << ", " << s.addType << ", " << (copyOut() ? 1 : 0) << "},";
+          << (s.usesRemove ? 1 : 0) << ", " << s.addType << ", " << (copyOut() ? 1 : 0) << ", "
+          << (s.addType < 0 && !s.usesRemove ? "abl_launch_ens_" + n : std::string("nullptr"))
+          << ", " << (s.usesRng ? 1 : 0) << "},";
   }
-  if (steps.empty()) *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0},";
+  if (steps.empty()) *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0},";
   *this << outdent << nl << "};" << nl;
   // The runtime runs the steps in simulate order (SimulateStatement::stepFuncDecls,
   // CPrinter.cpp:196); abl_steps above is in declaration order.
@@ -836,8 +905,8 @@ void CudaPrinter::printDescriptor() {
       }
     }
   }
-  *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0}" << outdent << nl
-        << "};" << nl;
+  *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}" << outdent
+        << nl << "};" << nl;
   int numSteps = 0;
   if (script.simStmt) numSteps = (int) script.simStmt->stepFuncDecls.size();
   *this << "extern const abl_model_desc abl_desc = {" << indent << nl

@@ -73,6 +73,7 @@ private:
     const AST::ForStatement *nearLoop = nullptr;
     bool usesRemove = false;
     int addType = -1;
+    bool usesRng = false;
   };
   std::vector<StepInfo> steps;
 

@@ -83,6 +83,27 @@ typedef struct {
 } abl_step_launch;
 
 typedef int (*abl_step_launch_fn)(const abl_step_launch *launch, cudaStream_t stream);
+
+/* Ensemble launch: the agents of many replicas of one model in one launch.
+ * Agent i belongs to replica replica[i]; that replica's globals block is
+ * globals + replica[i] * globals_size and its binned neighbour view is
+ * views[replica[i]] (device arrays).  Column and slot indices are global. */
+typedef struct {
+  long n;                            /* agents of the step's type, all replicas */
+  void *in_cols[ABL_MAX_MEMBERS];
+  void *out_cols[ABL_MAX_MEMBERS];
+  const int *visit_order;
+  const int *replica;                /* agent -> replica */
+  const void *globals;               /* device: replicas x globals_size bytes */
+  const abl_near_view *views;        /* device: one view per replica */
+  const long *agent_base;            /* device: first agent of each replica */
+  const uint64_t *seeds;             /* device: random() seed per replica */
+  long timestep;
+  int step_index;
+  int block;
+} abl_ens_launch;
+
+typedef int (*abl_ens_launch_fn)(const abl_ens_launch *launch, cudaStream_t stream);
 typedef double (*abl_globals_fn)(const void *globals);
 typedef void (*abl_env_fn)(const void *globals, double *min3, double *max3);
 
@@ -98,6 +119,8 @@ typedef struct {
   int uses_remove;             /* the body may call removeCurrent() */
   int add_type;                /* agent type created by add() in the body, -1 if none */
   int out_copy;                /* `out` starts as a copy of `in` */
+  abl_ens_launch_fn launch_ens; /* ensemble variant (NULL: not supported) */
+  int uses_rng;                 /* the body draws random numbers */
 } abl_step_desc;
 
 /* Host function run after every timestep: the `sequential step`. */

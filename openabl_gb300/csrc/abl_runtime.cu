@@ -1004,7 +1004,10 @@ bool graph_capturable(const abl_ctx *ctx) {
   const abl_model_desc *m = ctx->model;
   if (m->seq_step) return false;
   for (int k = 0; k < m->num_steps; k++) {
-    if (m->steps[k].uses_remove || m->steps[k].add_type >= 0) return false;
+    // Population changes need host decisions; random() keys on the timestep,
+    // which a replayed graph would not advance.
+    if (m->steps[k].uses_remove || m->steps[k].add_type >= 0 || m->steps[k].uses_rng)
+      return false;
   }
   return true;
 }
@@ -1126,6 +1129,11 @@ int abl_model_member(const abl_model_desc *m, int type_id, int member, const cha
 }
 
 size_t abl_model_globals_size(const abl_model_desc *m) { return m ? m->globals_size : 0; }
+
+int abl_model_float_bytes(const abl_model_desc *m) {
+  if (!m) return ABL_E_INVALID;
+  return m->uses_float ? 4 : 8;
+}
 
 int abl_model_globals_default(const abl_model_desc *m, void *out) {
   if (!m || !out) return ABL_E_INVALID;
@@ -1672,3 +1680,783 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
   ABL_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
   return h;
 }
+
+// ------------------------------------------------------------- ensembles
+//
+// An ensemble runs many replicas of one model -- different agent counts,
+// different globals (parameter points), different random seeds -- as one
+// population.  Replica r's agents of a type occupy [base[r], base[r] +
+// count[r]) of shared columns; each replica has its own grid, and the grids
+// are laid end to end in one cell array (a segmented grid), so binning, the
+// prefix scans, the neighbourhood lists and every step function run as ONE
+// launch over all replicas.  Two timesteps are captured into a CUDA graph and
+// replayed.  Results are per replica what a separate context would compute:
+// step kernels read the replica's globals and grid view, slots and cell
+// starts are global, and random() is keyed by the replica's seed and the
+// agent's index within its replica.
+
+namespace {
+
+struct EnsGrid {
+  int nx, ny, nz, R;
+  double lo[3];
+  double inv_cell;
+  long cell_base;
+};
+
+template <typename Real, int DIM>
+__global__ void k_ens_bin_assign(const Real *pos, long n, const int *replica_of,
+                                 const EnsGrid *grids, int *cell_of, int *cell_count,
+                                 int *local_rank, float *amax, int *error) {
+  long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  float m = 0.0f;
+  if (i < n) {
+    const EnsGrid g = grids[replica_of[i]];
+    const int dims[3] = {g.nx, g.ny, g.nz};
+    int c[3] = {0, 0, 0};
+    bool finite = true;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      double x = (double) pos[DIM * i + d];
+      finite = finite && isfinite(x);
+      c[d] = abl::cell_coord(x, g.lo[d], g.inv_cell, dims[d]);
+      m = fmaxf(m, fabsf((float) x));
+    }
+    if (!finite) atomicExch(error, ABL_E_NONFINITE);
+    int cell = (int) (g.cell_base + ((long) c[2] * g.ny + c[1]) * g.nx + c[0]);
+    cell_of[i] = cell;
+    local_rank[i] = atomicAdd(&cell_count[cell], 1);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0f) abl::atomic_max_nonneg(amax, m);
+}
+
+// Neighbourhood of global cell c inside its replica's grid.
+struct EnsCellRange {
+  int x0, x1, y0, y1, z0, z1;
+  long base;
+  int nx, ny;
+};
+
+template <int DIM>
+__device__ inline EnsCellRange ens_cell_range(long c, const int *cell_replica,
+                                              const EnsGrid *grids) {
+  const EnsGrid g = grids[cell_replica[c]];
+  long local = c - g.cell_base;
+  int cx = local % g.nx, cy = (local / g.nx) % g.ny, cz = local / ((long) g.nx * g.ny);
+  EnsCellRange r;
+  r.x0 = max(cx - g.R, 0);
+  r.x1 = min(cx + g.R, g.nx - 1);
+  r.y0 = max(cy - g.R, 0);
+  r.y1 = min(cy + g.R, g.ny - 1);
+  r.z0 = DIM == 3 ? max(cz - g.R, 0) : 0;
+  r.z1 = DIM == 3 ? min(cz + g.R, g.nz - 1) : 0;
+  r.base = g.cell_base;
+  r.nx = g.nx;
+  r.ny = g.ny;
+  return r;
+}
+
+template <int DIM>
+__global__ void k_ens_nb_count(long ncells, const int *cell_replica, const EnsGrid *grids,
+                               const int *cell_start, int *nb_cnt) {
+  long c = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  if (cell_start[c + 1] == cell_start[c]) {
+    nb_cnt[c] = 0;  // replicas have no other agent types: only occupied cells query
+    return;
+  }
+  EnsCellRange r = ens_cell_range<DIM>(c, cell_replica, grids);
+  int cnt = 0;
+  for (int z = r.z0; z <= r.z1; z++) {
+    for (int y = r.y0; y <= r.y1; y++) {
+      long rb = r.base + ((long) z * r.ny + y) * r.nx;
+      cnt += cell_start[rb + r.x1 + 1] - cell_start[rb + r.x0];
+    }
+  }
+  nb_cnt[c] = cnt;
+}
+
+template <int DIM>
+__global__ void k_ens_nb_build(long ncells, const int *cell_replica, const EnsGrid *grids,
+                               const int *cell_start, const int *order, const int *nb_off,
+                               int *nb_list) {
+  __shared__ int s_id[kListWarpsPerBlock][kListCap];
+  __shared__ int s_slot[kListWarpsPerBlock][kListCap];
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  long c = (long) blockIdx.x * kListWarpsPerBlock + w;
+  if (c >= ncells) return;
+  int base_out = nb_off[c];
+  int count = nb_off[c + 1] - base_out;
+  if (count == 0) return;
+  EnsCellRange r = ens_cell_range<DIM>(c, cell_replica, grids);
+  if (count <= kListCap) {
+    int k = 0;
+    for (int z = r.z0; z <= r.z1; z++) {
+      for (int y = r.y0; y <= r.y1; y++) {
+        long rb = r.base + ((long) z * r.ny + y) * r.nx;
+        int s = cell_start[rb + r.x0], e = cell_start[rb + r.x1 + 1];
+        for (int j = lane; j < e - s; j += 32) {
+          s_id[w][k + j] = order[s + j];
+          s_slot[w][k + j] = s + j;
+        }
+        k += e - s;
+      }
+    }
+    __syncwarp();
+    for (int e = lane; e < count; e += 32) {
+      int id = s_id[w][e];
+      int rank = 0;
+      for (int f = 0; f < count; f++) rank += s_id[w][f] < id;
+      nb_list[base_out + rank] = s_slot[w][e];
+    }
+    return;
+  }
+  for (int e = lane; e < count; e += 32) {
+    int se = -1, k = 0;
+    for (int z = r.z0; z <= r.z1 && se < 0; z++) {
+      for (int y = r.y0; y <= r.y1; y++) {
+        long rb = r.base + ((long) z * r.ny + y) * r.nx;
+        int s = cell_start[rb + r.x0], len = cell_start[rb + r.x1 + 1] - s;
+        if (e < k + len) {
+          se = s + (e - k);
+          break;
+        }
+        k += len;
+      }
+    }
+    int id = order[se];
+    int rank = 0;
+    for (int z = r.z0; z <= r.z1; z++) {
+      for (int y = r.y0; y <= r.y1; y++) {
+        long rb = r.base + ((long) z * r.ny + y) * r.nx;
+        int s = cell_start[rb + r.x0], e2 = cell_start[rb + r.x1 + 1];
+        for (int j = s; j < e2; j++) rank += order[j] < id;
+      }
+    }
+    nb_list[base_out + rank] = se;
+  }
+}
+
+struct EnsType {
+  const abl_agent_desc *d = nullptr;
+  long n = 0;
+  std::vector<long> counts, base;
+  void *cols[2][ABL_MAX_MEMBERS] = {};
+  int cur = 0;
+  int *replica_of = nullptr;
+  long *d_base = nullptr;
+  bool uploaded = false;
+  // binning
+  bool is_near = false, ordered = false, dirty = true;
+  uint32_t gather_mask = 0;
+  std::vector<EnsGrid> grids;
+  EnsGrid *d_grids = nullptr;
+  long ncells = 0;
+  int *cell_replica = nullptr;
+  int *cell_count = nullptr, *cell_start = nullptr, *local_rank = nullptr, *cell_of = nullptr;
+  int *order = nullptr;
+  float *posf = nullptr, *amax = nullptr;
+  void *gcols[ABL_MAX_MEMBERS] = {};
+  int *nb_cnt = nullptr, *nb_off = nullptr, *nb_list = nullptr;
+  ScanPlan cell_scan, nb_scan;
+  std::vector<void *> allocs;
+};
+
+}  // namespace
+
+struct abl_ensemble {
+  abl_ctx base;  // stream, allocations, budget, scans
+  int replicas = 0;
+  std::vector<unsigned char> globals;  // replicas x globals_size
+  void *d_globals = nullptr;
+  uint64_t *d_seeds = nullptr;
+  std::vector<uint64_t> seeds;
+  std::vector<EnsType> types;
+  std::vector<abl_near_view *> d_views;  // per step with a near loop
+  std::vector<void *> view_allocs;
+  bool prepared = false;
+  int block = 128;
+  double cell_factor = 1.0;
+  int visit_sorted = 1;
+  std::vector<abl_ctx::Graph> graphs;
+  long timestep = 0;
+};
+
+namespace {
+
+void ens_free_bins(abl_ensemble *e, EnsType &t) {
+  for (void *p : t.allocs) dev_free(&e->base, p);
+  t.allocs.clear();
+  t.cell_scan.levels.clear();
+  t.nb_scan.levels.clear();
+  t.cell_count = t.cell_start = t.local_rank = t.cell_of = t.order = nullptr;
+  t.nb_cnt = t.nb_off = t.nb_list = t.cell_replica = nullptr;
+  t.posf = t.amax = nullptr;
+  t.d_grids = nullptr;
+  for (auto &g : t.gcols) g = nullptr;
+}
+
+void ens_drop_graphs(abl_ensemble *e) {
+  for (auto &g : e->graphs) cudaGraphExecDestroy(g.exec);
+  e->graphs.clear();
+}
+
+int ens_prepare(abl_ensemble *e) {
+  abl_ctx *ctx = &e->base;
+  const abl_model_desc *m = ctx->model;
+  ens_drop_graphs(e);
+  for (void *p : e->view_allocs) dev_free(ctx, p);
+  e->view_allocs.clear();
+  e->d_views.assign(m->num_steps, nullptr);
+  for (int ti = 0; ti < m->num_agent_types; ti++) {
+    EnsType &t = e->types[ti];
+    ens_free_bins(e, t);
+    t.is_near = false;
+    t.ordered = false;
+    t.gather_mask = 0;
+    for (int k = 0; k < m->num_steps; k++) {
+      const abl_step_desc &sd = m->steps[k];
+      if (sd.near_type != ti) continue;
+      t.is_near = true;
+      t.ordered = t.ordered || sd.ordered;
+      t.gather_mask |= sd.near_members;
+    }
+    auto *own = &t.allocs;
+    ABL_TRY(dev_alloc_t(ctx, &t.amax, 1, own));
+    if (!t.is_near) continue;
+    int dim = t.d->dim;
+    t.grids.assign(e->replicas, EnsGrid());
+    long cells = 0;
+    for (int r = 0; r < e->replicas; r++) {
+      const void *G = e->globals.data() + (size_t) r * m->globals_size;
+      double emin[3] = {0, 0, 0}, emax[3] = {0, 0, 0};
+      if (m->env_bounds) m->env_bounds(G, emin, emax);
+      double rmax = 0.0;
+      for (int k = 0; k < m->num_steps; k++) {
+        if (m->steps[k].near_type == ti && m->steps[k].radius)
+          rmax = std::max(rmax, m->steps[k].radius(G));
+      }
+      double gran = m->granularity ? m->granularity(G) : rmax;
+      if (!(gran > 0.0) || !std::isfinite(gran)) return ABL_E_INVALID;
+      double cell = gran * (1.0 + 1.0 / 1024.0) * std::max(1.0, e->cell_factor);
+      EnsGrid &g = t.grids[r];
+      g.R = std::max(1, (int) std::ceil(rmax * (1.0 + 1e-6) / cell));
+      g.inv_cell = 1.0 / cell;
+      int dims[3] = {1, 1, 1};
+      for (int d = 0; d < 3; d++) {
+        g.lo[d] = d < dim ? emin[d] : 0.0;
+        if (d < dim) {
+          double ext = emax[d] - emin[d];
+          if (!(ext >= 0.0) || !std::isfinite(ext)) return ABL_E_INVALID;
+          double k = std::floor(ext * g.inv_cell) + 1.0;
+          if (k > 1 << 24) return ABL_E_UNSUPPORTED;
+          dims[d] = (int) k;
+        }
+      }
+      g.nx = dims[0];
+      g.ny = dims[1];
+      g.nz = dims[2];
+      g.cell_base = cells;
+      cells += (long) g.nx * g.ny * g.nz;
+      if (cells > (1L << 30)) return ABL_E_UNSUPPORTED;
+    }
+    t.ncells = cells;
+    long n = std::max<long>(t.n, 1);
+    ABL_TRY(dev_alloc_t(ctx, &t.d_grids, e->replicas, own));
+    ABL_CUDA_TRY(cudaMemcpy(t.d_grids, t.grids.data(), sizeof(EnsGrid) * e->replicas,
+                            cudaMemcpyHostToDevice));
+    std::vector<int> cr(cells);
+    for (int r = 0; r < e->replicas; r++) {
+      long c0 = t.grids[r].cell_base;
+      long c1 = r + 1 < e->replicas ? t.grids[r + 1].cell_base : cells;
+      for (long c = c0; c < c1; c++) cr[c] = r;
+    }
+    ABL_TRY(dev_alloc_t(ctx, &t.cell_replica, std::max<long>(cells, 1), own));
+    ABL_CUDA_TRY(cudaMemcpy(t.cell_replica, cr.data(), sizeof(int) * cells,
+                            cudaMemcpyHostToDevice));
+    ABL_TRY(dev_alloc_t(ctx, &t.cell_count, cells, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.cell_start, cells + 1, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.local_rank, n, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.cell_of, n, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.order, n, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.posf, n * dim, own));
+    ABL_TRY(scan_plan(ctx, t.cell_scan, cells, own));
+    for (int k = 0; k < t.d->num_members; k++) {
+      if (t.gather_mask & (1u << k)) {
+        void *p = nullptr;
+        ABL_TRY(dev_alloc(ctx, &p, member_bytes(t.d->members[k]) * n, own));
+        t.gcols[k] = p;
+      }
+    }
+    if (t.ordered) {
+      int Rmax = 1;
+      for (auto &g : t.grids) Rmax = std::max(Rmax, g.R);
+      long span = 2 * Rmax + 1;
+      long per_agent = dim == 3 ? span * span * span : span * span;
+      ABL_TRY(dev_alloc_t(ctx, &t.nb_cnt, cells, own));
+      ABL_TRY(dev_alloc_t(ctx, &t.nb_off, cells + 1, own));
+      ABL_TRY(dev_alloc_t(ctx, &t.nb_list, per_agent * n, own));
+      ABL_TRY(scan_plan(ctx, t.nb_scan, cells, own));
+    }
+    t.dirty = true;
+  }
+  // Per replica neighbour views for every step function with a near loop.
+  for (int k = 0; k < m->num_steps; k++) {
+    const abl_step_desc &sd = m->steps[k];
+    if (sd.near_type < 0) continue;
+    EnsType &nt = e->types[sd.near_type];
+    std::vector<abl_near_view> views(e->replicas);
+    for (int r = 0; r < e->replicas; r++) {
+      const EnsGrid &g = nt.grids[r];
+      abl_near_view &V = views[r];
+      std::memset(&V, 0, sizeof V);
+      V.dim = nt.d->dim;
+      V.ordered = sd.ordered;
+      V.range = g.R;
+      V.nx = g.nx;
+      V.ny = g.ny;
+      V.nz = g.nz;
+      for (int d = 0; d < 3; d++) V.lo[d] = g.lo[d];
+      V.inv_cell = g.inv_cell;
+      V.radius = sd.radius(e->globals.data() + (size_t) r * m->globals_size);
+      V.n = nt.counts.empty() ? 0 : nt.counts[r];
+      V.cell_start = nt.cell_start + g.cell_base;
+      V.order = nt.order;
+      V.posf = nt.posf;
+      V.nb_off = nt.nb_off ? nt.nb_off + g.cell_base : nullptr;
+      V.nb_list = nt.nb_list;
+      V.amax = nt.amax;
+      for (int j = 0; j < nt.d->num_members; j++) V.cols[j] = nt.gcols[j];
+    }
+    abl_near_view *dv = nullptr;
+    ABL_TRY(dev_alloc_t(ctx, &dv, e->replicas, &e->view_allocs));
+    ABL_CUDA_TRY(cudaMemcpy(dv, views.data(), sizeof(abl_near_view) * e->replicas,
+                            cudaMemcpyHostToDevice));
+    e->d_views[k] = dv;
+  }
+  e->prepared = true;
+  return ABL_OK;
+}
+
+template <typename Real>
+void ens_launch_bin(abl_ensemble *e, EnsType &t) {
+  abl_ctx *ctx = &e->base;
+  cudaStream_t s = ctx->stream;
+  const int B = 256;
+  int dim = t.d->dim;
+  long nb = blocks_for(t.n, B);
+  const Real *pos = (const Real *) t.cols[t.cur][t.d->position_member];
+  cudaMemsetAsync(t.cell_count, 0, sizeof(int) * t.ncells, s);
+  cudaMemsetAsync(t.amax, 0, sizeof(float), s);
+  if (dim == 2) {
+    k_ens_bin_assign<Real, 2><<<nb, B, 0, s>>>(pos, t.n, t.replica_of, t.d_grids, t.cell_of,
+                                               t.cell_count, t.local_rank, t.amax, ctx->error);
+  } else {
+    k_ens_bin_assign<Real, 3><<<nb, B, 0, s>>>(pos, t.n, t.replica_of, t.d_grids, t.cell_of,
+                                               t.cell_count, t.local_rank, t.amax, ctx->error);
+  }
+  ctx->launches++;
+  scan_run(ctx, t.cell_scan, t.cell_count, t.cell_start);
+  k_bin_scatter<<<nb, B, 0, s>>>(t.n, t.cell_of, t.local_rank, t.cell_start, t.order);
+  ctx->launches++;
+  GatherArgs g;
+  std::memset(&g, 0, sizeof g);
+  for (int k = 0; k < t.d->num_members; k++) {
+    if (!(t.gather_mask & (1u << k))) continue;
+    g.src[g.nmem] = t.cols[t.cur][k];
+    g.dst[g.nmem] = t.gcols[k];
+    g.bytes[g.nmem] = (int) member_bytes(t.d->members[k]);
+    g.nmem++;
+  }
+  if (dim == 2) k_gather<Real, 2><<<nb, B, 0, s>>>(t.n, t.order, pos, t.posf, g);
+  else k_gather<Real, 3><<<nb, B, 0, s>>>(t.n, t.order, pos, t.posf, g);
+  ctx->launches++;
+  if (t.ordered) {
+    long cb = blocks_for(t.ncells, B);
+    if (dim == 2) k_ens_nb_count<2><<<cb, B, 0, s>>>(t.ncells, t.cell_replica, t.d_grids,
+                                                     t.cell_start, t.nb_cnt);
+    else k_ens_nb_count<3><<<cb, B, 0, s>>>(t.ncells, t.cell_replica, t.d_grids, t.cell_start,
+                                            t.nb_cnt);
+    ctx->launches++;
+    scan_run(ctx, t.nb_scan, t.nb_cnt, t.nb_off);
+    long lb = blocks_for(t.ncells, kListWarpsPerBlock);
+    if (dim == 2) k_ens_nb_build<2><<<lb, 32 * kListWarpsPerBlock, 0, s>>>(
+        t.ncells, t.cell_replica, t.d_grids, t.cell_start, t.order, t.nb_off, t.nb_list);
+    else k_ens_nb_build<3><<<lb, 32 * kListWarpsPerBlock, 0, s>>>(
+        t.ncells, t.cell_replica, t.d_grids, t.cell_start, t.order, t.nb_off, t.nb_list);
+    ctx->launches++;
+  }
+  t.dirty = false;
+}
+
+int ens_step_once(abl_ensemble *e) {
+  abl_ctx *ctx = &e->base;
+  const abl_model_desc *m = ctx->model;
+  for (int k = 0; k < m->num_steps; k++) {
+    const abl_step_desc &sd = m->steps[k];
+    EnsType &t = e->types[sd.agent_type];
+    if (sd.near_type >= 0) {
+      EnsType &nt = e->types[sd.near_type];
+      if (nt.dirty) {
+        if (nt.d->members[nt.d->position_member].scalar_bytes == 8)
+          ens_launch_bin<double>(e, nt);
+        else
+          ens_launch_bin<float>(e, nt);
+      }
+    }
+    abl_ens_launch L;
+    std::memset(&L, 0, sizeof L);
+    L.n = t.n;
+    for (int j = 0; j < t.d->num_members; j++) {
+      L.in_cols[j] = t.cols[t.cur][j];
+      L.out_cols[j] = t.cols[1 - t.cur][j];
+    }
+    L.visit_order = (e->visit_sorted && sd.near_type == sd.agent_type) ? t.order : nullptr;
+    L.replica = t.replica_of;
+    L.globals = e->d_globals;
+    L.views = sd.near_type >= 0 ? e->d_views[k] : nullptr;
+    L.agent_base = t.d_base;
+    L.seeds = e->d_seeds;
+    L.timestep = e->timestep;
+    L.step_index = k;
+    L.block = e->block;
+    if (t.n > 0) {
+      ABL_TRY(sd.launch_ens(&L, ctx->stream));
+      ctx->launches++;
+    }
+    t.cur = 1 - t.cur;
+    t.dirty = true;
+  }
+  e->timestep++;
+  return ABL_OK;
+}
+
+std::vector<int> ens_graph_key(const abl_ensemble *e) {
+  std::vector<int> key;
+  for (const EnsType &t : e->types) {
+    key.push_back(t.cur);
+    key.push_back(t.dirty ? 1 : 0);
+  }
+  return key;
+}
+
+int ens_capture(abl_ensemble *e, abl_ctx::Graph **out) {
+  std::vector<int> key = ens_graph_key(e);
+  for (auto &g : e->graphs) {
+    if (g.key == key) {
+      *out = &g;
+      return ABL_OK;
+    }
+  }
+  abl_ctx *ctx = &e->base;
+  abl_ctx::Graph G;
+  G.key = key;
+  long before = ctx->launches;
+  long ts = e->timestep;
+  cudaGraph_t g = nullptr;
+  ABL_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int r = ens_step_once(e);
+  if (r == ABL_OK) r = ens_step_once(e);
+  cudaError_t err = cudaStreamEndCapture(ctx->stream, &g);
+  if (r != ABL_OK) {
+    if (g) cudaGraphDestroy(g);
+    return r;
+  }
+  ABL_CUDA_TRY(err);
+  err = cudaGraphInstantiate(&G.exec, g, 0);
+  cudaGraphDestroy(g);
+  ABL_CUDA_TRY(err);
+  G.launches = ctx->launches - before;
+  ctx->launches = before;
+  e->timestep = ts;
+  for (size_t k = 0; k < e->types.size(); k++) {
+    e->types[k].cur = key[2 * k];
+    e->types[k].dirty = key[2 * k + 1] != 0;
+  }
+  e->graphs.push_back(G);
+  *out = &e->graphs.back();
+  return ABL_OK;
+}
+
+// Graph replay bakes the timestep into kernel arguments, and random() keys
+// on it: models that draw in step functions run eagerly.
+bool uses_rng(const abl_model_desc *m) {
+  for (int k = 0; k < m->num_steps; k++)
+    if (m->steps[k].uses_rng) return true;
+  return false;
+}
+
+}  // namespace
+
+extern "C" {
+
+int abl_ensemble_create(const abl_model_desc *model, int replicas, const void *globals,
+                        const uint64_t *seeds, size_t hbm_budget, abl_ensemble **out) {
+  if (!model || replicas <= 0 || !out) return ABL_E_INVALID;
+  if (model->seq_step) return ABL_E_UNSUPPORTED;
+  for (int k = 0; k < model->num_steps; k++) {
+    if (!model->steps[k].launch_ens) return ABL_E_UNSUPPORTED;
+  }
+  abl_ensemble *e = new abl_ensemble;
+  abl_ctx *ctx = &e->base;
+  ctx->model = model;
+  ctx->budget = hbm_budget;
+  e->replicas = replicas;
+  size_t gs = model->globals_size;
+  e->globals.resize(gs * replicas);
+  for (int r = 0; r < replicas; r++) {
+    std::memcpy(e->globals.data() + gs * r,
+                globals ? (const unsigned char *) globals + gs * r
+                        : (const unsigned char *) model->globals_default, gs);
+  }
+  e->seeds.assign(replicas, 0);
+  if (seeds) e->seeds.assign(seeds, seeds + replicas);
+  e->types.resize(model->num_agent_types);
+  for (int k = 0; k < model->num_agent_types; k++) {
+    e->types[k].d = &model->agents[k];
+    e->types[k].counts.assign(replicas, 0);
+    e->types[k].base.assign(replicas, 0);
+  }
+  cudaError_t err = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (err == cudaSuccess) err = cudaEventCreate(&ctx->ev0);
+  if (err == cudaSuccess) err = cudaEventCreate(&ctx->ev1);
+  if (err != cudaSuccess) {
+    delete e;
+    return ABL_E_CUDA;
+  }
+  int r = dev_alloc_t(ctx, &ctx->error, 1);
+  if (r == ABL_OK) r = dev_alloc(ctx, &e->d_globals, gs * replicas);
+  if (r == ABL_OK) r = dev_alloc_t(ctx, &e->d_seeds, replicas);
+  if (r == ABL_OK) {
+    cudaMemset(ctx->error, 0, sizeof(int));
+    cudaMemcpy(e->d_globals, e->globals.data(), gs * replicas, cudaMemcpyHostToDevice);
+    cudaMemcpy(e->d_seeds, e->seeds.data(), sizeof(uint64_t) * replicas, cudaMemcpyHostToDevice);
+  }
+  if (r != ABL_OK) {
+    abl_ensemble_destroy(e);
+    return r;
+  }
+  *out = e;
+  return ABL_OK;
+}
+
+int abl_ensemble_upload(abl_ensemble *e, int type_id, const size_t *counts,
+                        const void *const *cols) {
+  if (!e || !counts || type_id < 0 || type_id >= (int) e->types.size()) return ABL_E_INVALID;
+  abl_ctx *ctx = &e->base;
+  EnsType &t = e->types[type_id];
+  long total = 0;
+  for (int r = 0; r < e->replicas; r++) {
+    t.counts[r] = (long) counts[r];
+    t.base[r] = total;
+    total += (long) counts[r];
+  }
+  if (total > (long) INT32_MAX) return ABL_E_UNSUPPORTED;
+  for (int b = 0; b < 2; b++) {
+    for (int k = 0; k < t.d->num_members; k++) {
+      if (t.cols[b][k]) dev_free(ctx, t.cols[b][k]);
+      t.cols[b][k] = nullptr;
+      ABL_TRY(dev_alloc(ctx, &t.cols[b][k], member_bytes(t.d->members[k]) * std::max<long>(total, 1)));
+    }
+  }
+  if (t.replica_of) dev_free(ctx, t.replica_of);
+  if (t.d_base) dev_free(ctx, t.d_base);
+  ABL_TRY(dev_alloc_t(ctx, &t.replica_of, std::max<long>(total, 1)));
+  ABL_TRY(dev_alloc_t(ctx, &t.d_base, e->replicas));
+  std::vector<int> rep(total);
+  for (int r = 0; r < e->replicas; r++)
+    for (long i = 0; i < t.counts[r]; i++) rep[t.base[r] + i] = r;
+  ABL_CUDA_TRY(cudaMemcpy(t.replica_of, rep.data(), sizeof(int) * total, cudaMemcpyHostToDevice));
+  ABL_CUDA_TRY(cudaMemcpy(t.d_base, t.base.data(), sizeof(long) * e->replicas,
+                          cudaMemcpyHostToDevice));
+  t.n = total;
+  t.cur = 0;
+  for (int k = 0; k < t.d->num_members; k++) {
+    size_t bytes = member_bytes(t.d->members[k]) * total;
+    if (!bytes) continue;
+    if (!cols || !cols[k]) return ABL_E_INVALID;
+    ABL_CUDA_TRY(cudaMemcpy(t.cols[0][k], cols[k], bytes, cudaMemcpyHostToDevice));
+    ABL_CUDA_TRY(cudaMemcpy(t.cols[1][k], t.cols[0][k], bytes, cudaMemcpyDeviceToDevice));
+  }
+  t.uploaded = true;
+  t.dirty = true;
+  e->prepared = false;
+  e->timestep = 0;
+  return ABL_OK;
+}
+
+static int ens_ready(abl_ensemble *e) {
+  for (auto &t : e->types) {
+    if (!t.uploaded) {
+      std::vector<size_t> zero(e->replicas, 0);
+      ABL_TRY(abl_ensemble_upload(e, (int) (&t - &e->types[0]), zero.data(), nullptr));
+    }
+  }
+  if (!e->prepared) ABL_TRY(ens_prepare(e));
+  return ABL_OK;
+}
+
+int abl_ensemble_run(abl_ensemble *e, int timesteps) {
+  if (!e || timesteps < 0) return ABL_E_INVALID;
+  ABL_TRY(ens_ready(e));
+  abl_ctx *ctx = &e->base;
+  long l0 = ctx->launches;
+  ABL_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
+  int done = 0;
+  if (timesteps > 0) {
+    ABL_TRY(ens_step_once(e));
+    done = 1;
+  }
+  if (timesteps - done >= 2 && !uses_rng(ctx->model)) {
+    abl_ctx::Graph *G = nullptr;
+    ABL_TRY(ens_capture(e, &G));
+    for (; done + 2 <= timesteps; done += 2) {
+      ABL_CUDA_TRY(cudaGraphLaunch(G->exec, ctx->stream));
+      ctx->launches += G->launches;
+      e->timestep += 2;
+    }
+  }
+  for (; done < timesteps; done++) ABL_TRY(ens_step_once(e));
+  ABL_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
+  int r = check_error(ctx);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->last_exec = ms / 1000.0;
+  ctx->last_launches = ctx->launches - l0;
+  return r;
+}
+
+int abl_ensemble_download(abl_ensemble *e, int type_id, size_t *counts, void *const *cols) {
+  if (!e || type_id < 0 || type_id >= (int) e->types.size()) return ABL_E_INVALID;
+  EnsType &t = e->types[type_id];
+  if (counts)
+    for (int r = 0; r < e->replicas; r++) counts[r] = (size_t) t.counts[r];
+  if (!cols) return ABL_OK;
+  for (int k = 0; k < t.d->num_members; k++) {
+    size_t bytes = member_bytes(t.d->members[k]) * t.n;
+    if (!bytes) continue;
+    if (!cols[k]) return ABL_E_INVALID;
+    ABL_CUDA_TRY(cudaMemcpyAsync(cols[k], t.cols[t.cur][k], bytes, cudaMemcpyDeviceToHost,
+                                 e->base.stream));
+  }
+  return check_error(&e->base);
+}
+
+int abl_ensemble_set_tuning(abl_ensemble *e, int block, double cell_factor, int visit_sorted) {
+  if (!e || block <= 0 || block > ABL_STEP_BLOCK || block % 32 || !(cell_factor >= 1.0))
+    return ABL_E_INVALID;
+  e->block = block;
+  if (cell_factor != e->cell_factor) e->prepared = false;
+  e->cell_factor = cell_factor;
+  e->visit_sorted = visit_sorted ? 1 : 0;
+  ens_drop_graphs(e);
+  return ABL_OK;
+}
+
+// Tries every combination of block size, cell size factor and visiting order
+// for `trial_timesteps` timesteps (after one warm-up timestep) and keeps the
+// fastest.  The state and timestep counter are restored after each trial, so
+// tuning does not advance the simulation; every candidate computes identical
+// results.
+int abl_ensemble_autotune(abl_ensemble *e, int trial_timesteps, int *block, double *cell_factor,
+                          int *visit_sorted) {
+  if (!e || trial_timesteps <= 0) return ABL_E_INVALID;
+  ABL_TRY(ens_ready(e));
+  abl_ctx *ctx = &e->base;
+  // Snapshot of the current state.
+  std::vector<std::vector<void *>> snap(e->types.size());
+  std::vector<int> cur(e->types.size());
+  for (size_t ti = 0; ti < e->types.size(); ti++) {
+    EnsType &t = e->types[ti];
+    cur[ti] = t.cur;
+    for (int k = 0; k < t.d->num_members; k++) {
+      void *p = nullptr;
+      size_t bytes = member_bytes(t.d->members[k]) * std::max<long>(t.n, 1);
+      ABL_TRY(dev_alloc(ctx, &p, bytes));
+      ABL_CUDA_TRY(cudaMemcpyAsync(p, t.cols[t.cur][k], bytes, cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
+      snap[ti].push_back(p);
+    }
+  }
+  auto restore = [&]() -> int {
+    for (size_t ti = 0; ti < e->types.size(); ti++) {
+      EnsType &t = e->types[ti];
+      t.cur = cur[ti];
+      t.dirty = true;
+      for (int k = 0; k < t.d->num_members; k++) {
+        size_t bytes = member_bytes(t.d->members[k]) * std::max<long>(t.n, 1);
+        ABL_CUDA_TRY(cudaMemcpyAsync(t.cols[t.cur][k], snap[ti][k], bytes,
+                                     cudaMemcpyDeviceToDevice, ctx->stream));
+      }
+    }
+    return ABL_OK;
+  };
+  long ts0 = e->timestep;
+  const int blocks[] = {64, 128};
+  const double factors[] = {1.0, 1.5, 2.0};
+  const int visits[] = {1, 0};
+  double best = 1e30;
+  int bb = e->block, bv = e->visit_sorted;
+  double bf = e->cell_factor;
+  for (int b : blocks) {
+    for (double f : factors) {
+      for (int v : visits) {
+        ABL_TRY(abl_ensemble_set_tuning(e, b, f, v));
+        ABL_TRY(ens_ready(e));
+        ABL_TRY(restore());
+        e->timestep = ts0;
+        ABL_TRY(abl_ensemble_run(e, 1));
+        ABL_TRY(abl_ensemble_run(e, trial_timesteps));
+        double t = ctx->last_exec;
+        if (t < best) {
+          best = t;
+          bb = b;
+          bf = f;
+          bv = v;
+        }
+      }
+    }
+  }
+  ABL_TRY(abl_ensemble_set_tuning(e, bb, bf, bv));
+  ABL_TRY(ens_ready(e));
+  ABL_TRY(restore());
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  for (auto &v : snap)
+    for (void *p : v) dev_free(ctx, p);
+  e->timestep = ts0;
+  if (block) *block = bb;
+  if (cell_factor) *cell_factor = bf;
+  if (visit_sorted) *visit_sorted = bv;
+  return ABL_OK;
+}
+
+int abl_ensemble_last_exec_time(abl_ensemble *e, double *seconds) {
+  if (!e || !seconds) return ABL_E_INVALID;
+  *seconds = e->base.last_exec;
+  return ABL_OK;
+}
+
+int abl_ensemble_last_launch_count(abl_ensemble *e, long *launches) {
+  if (!e || !launches) return ABL_E_INVALID;
+  *launches = e->base.last_launches;
+  return ABL_OK;
+}
+
+int abl_ensemble_destroy(abl_ensemble *e) {
+  if (!e) return ABL_E_INVALID;
+  abl_ctx *ctx = &e->base;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ens_drop_graphs(e);
+  for (void *p : ctx->allocations) cudaFree(p);
+  ctx->allocations.clear();
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  ctx->stream = nullptr;
+  delete e;
+  return ABL_OK;
+}
+
+}  // extern "C"

@@ -180,6 +180,29 @@ static int abl_launch_move_point(const abl_step_launch *L, cudaStream_t abl_stre
     abl_kernel_move_point<<<abl_grid, abl_block, 0, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_move_point(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Point abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    move_point(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+}
+static int abl_launch_ens_move_point(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_move_point<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
 static double abl_radius_move_point(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
@@ -215,11 +238,11 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"move_point", 0, 0, 1, abl_radius_move_point, 1u, 1u, abl_launch_move_point, 0, -1, 0},
+    {"move_point", 0, 0, 1, abl_radius_move_point, 1u, 1u, abl_launch_move_point, 0, -1, 0, abl_launch_ens_move_point, 0},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],
-    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0}
+    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
 };
 extern const abl_model_desc abl_desc = {
     "circle", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 8, abl_global_table, 2, abl_env_bounds, nullptr, 0, nullptr

@@ -183,6 +183,32 @@ static int abl_launch_step_move(const abl_step_launch *L, cudaStream_t abl_strea
     abl_kernel_step_move<<<abl_grid, abl_block, 0, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_step_move(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Cell abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.alive = ((const bool *) A.in_cols[1])[abl_i];
+    abl_out.alive = ((const bool *) A.out_cols[1])[abl_i];
+    step_move(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+    ((bool *) A.out_cols[1])[abl_i] = abl_out.alive;
+}
+static int abl_launch_ens_step_move(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_step_move<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
 static double abl_radius_step_move(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
@@ -225,11 +251,11 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"step_move", 0, 0, 0, abl_radius_step_move, 3u, 1u, abl_launch_step_move, 0, -1, 0},
+    {"step_move", 0, 0, 0, abl_radius_step_move, 3u, 1u, abl_launch_step_move, 0, -1, 0, abl_launch_ens_step_move, 0},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],
-    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0}
+    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
 };
 extern const abl_model_desc abl_desc = {
     "game_of_life", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 7, abl_global_table, 2, abl_env_bounds, nullptr, 0, nullptr

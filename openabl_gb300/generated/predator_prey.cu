@@ -292,6 +292,39 @@ static int abl_launch_prey_avoid_pred(const abl_step_launch *L, cudaStream_t abl
     abl_kernel_prey_avoid_pred<<<abl_grid, abl_block, 0, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_avoid_pred(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Prey abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
+    abl_in.steer = ((const float2 *) A.in_cols[2])[abl_i];
+    abl_in.life = ((const int *) A.in_cols[3])[abl_i];
+    abl_out.pos = abl_in.pos;
+    abl_out.dir = abl_in.dir;
+    abl_out.steer = abl_in.steer;
+    abl_out.life = abl_in.life;
+    prey_avoid_pred(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+    ((float2 *) A.out_cols[1])[abl_i] = abl_out.dir;
+    ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
+    ((int *) A.out_cols[3])[abl_i] = abl_out.life;
+}
+static int abl_launch_ens_prey_avoid_pred(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_prey_avoid_pred<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
 static double abl_radius_prey_avoid_pred(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
@@ -399,6 +432,39 @@ static int abl_launch_prey_flock(const abl_step_launch *L, cudaStream_t abl_stre
     abl_kernel_prey_flock<<<abl_grid, abl_block, 0, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_flock(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Prey abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
+    abl_in.steer = ((const float2 *) A.in_cols[2])[abl_i];
+    abl_in.life = ((const int *) A.in_cols[3])[abl_i];
+    abl_out.pos = abl_in.pos;
+    abl_out.dir = abl_in.dir;
+    abl_out.steer = abl_in.steer;
+    abl_out.life = abl_in.life;
+    prey_flock(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+    ((float2 *) A.out_cols[1])[abl_i] = abl_out.dir;
+    ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
+    ((int *) A.out_cols[3])[abl_i] = abl_out.life;
+}
+static int abl_launch_ens_prey_flock(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_prey_flock<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
 static double abl_radius_prey_flock(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
@@ -480,6 +546,39 @@ static int abl_launch_prey_move(const abl_step_launch *L, cudaStream_t abl_strea
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_move<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_move(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Prey abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
+    abl_in.steer = ((const float2 *) A.in_cols[2])[abl_i];
+    abl_in.life = ((const int *) A.in_cols[3])[abl_i];
+    abl_out.pos = abl_in.pos;
+    abl_out.dir = abl_in.dir;
+    abl_out.steer = abl_in.steer;
+    abl_out.life = abl_in.life;
+    prey_move(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+    ((float2 *) A.out_cols[1])[abl_i] = abl_out.dir;
+    ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
+    ((int *) A.out_cols[3])[abl_i] = abl_out.life;
+}
+static int abl_launch_ens_prey_move(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_prey_move<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 
@@ -846,6 +945,39 @@ static int abl_launch_pred_follow_prey(const abl_step_launch *L, cudaStream_t ab
     abl_kernel_pred_follow_prey<<<abl_grid, abl_block, 0, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_follow_prey(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Predator abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
+    abl_in.steer = ((const float2 *) A.in_cols[2])[abl_i];
+    abl_in.life = ((const int *) A.in_cols[3])[abl_i];
+    abl_out.pos = abl_in.pos;
+    abl_out.dir = abl_in.dir;
+    abl_out.steer = abl_in.steer;
+    abl_out.life = abl_in.life;
+    pred_follow_prey(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+    ((float2 *) A.out_cols[1])[abl_i] = abl_out.dir;
+    ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
+    ((int *) A.out_cols[3])[abl_i] = abl_out.life;
+}
+static int abl_launch_ens_pred_follow_prey(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_pred_follow_prey<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
 static double abl_radius_pred_follow_prey(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
@@ -942,6 +1074,39 @@ static int abl_launch_pred_avoid(const abl_step_launch *L, cudaStream_t abl_stre
     abl_kernel_pred_avoid<<<abl_grid, abl_block, 0, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_avoid(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Predator abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
+    abl_in.steer = ((const float2 *) A.in_cols[2])[abl_i];
+    abl_in.life = ((const int *) A.in_cols[3])[abl_i];
+    abl_out.pos = abl_in.pos;
+    abl_out.dir = abl_in.dir;
+    abl_out.steer = abl_in.steer;
+    abl_out.life = abl_in.life;
+    pred_avoid(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+    ((float2 *) A.out_cols[1])[abl_i] = abl_out.dir;
+    ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
+    ((int *) A.out_cols[3])[abl_i] = abl_out.life;
+}
+static int abl_launch_ens_pred_avoid(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_pred_avoid<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
 static double abl_radius_pred_avoid(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
@@ -1025,6 +1190,39 @@ static int abl_launch_pred_move(const abl_step_launch *L, cudaStream_t abl_strea
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_move<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_move(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Predator abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
+    abl_in.steer = ((const float2 *) A.in_cols[2])[abl_i];
+    abl_in.life = ((const int *) A.in_cols[3])[abl_i];
+    abl_out.pos = abl_in.pos;
+    abl_out.dir = abl_in.dir;
+    abl_out.steer = abl_in.steer;
+    abl_out.life = abl_in.life;
+    pred_move(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+    ((float2 *) A.out_cols[1])[abl_i] = abl_out.dir;
+    ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
+    ((int *) A.out_cols[3])[abl_i] = abl_out.life;
+}
+static int abl_launch_ens_pred_move(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_pred_move<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 
@@ -1283,6 +1481,36 @@ static int abl_launch_grass_eaten(const abl_step_launch *L, cudaStream_t abl_str
     abl_kernel_grass_eaten<<<abl_grid, abl_block, 0, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_grass_eaten(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Grass abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.dead_cycles = ((const int *) A.in_cols[1])[abl_i];
+    abl_in.avail = ((const bool *) A.in_cols[2])[abl_i];
+    abl_out.pos = abl_in.pos;
+    abl_out.dead_cycles = abl_in.dead_cycles;
+    abl_out.avail = abl_in.avail;
+    grass_eaten(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+    ((int *) A.out_cols[1])[abl_i] = abl_out.dead_cycles;
+    ((bool *) A.out_cols[2])[abl_i] = abl_out.avail;
+}
+static int abl_launch_ens_grass_eaten(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_grass_eaten<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
 static double abl_radius_grass_eaten(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
@@ -1357,6 +1585,36 @@ static int abl_launch_grass_growth(const abl_step_launch *L, cudaStream_t abl_st
     abl_kernel_grass_growth<<<abl_grid, abl_block, 0, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_grass_growth(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Grass abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.dead_cycles = ((const int *) A.in_cols[1])[abl_i];
+    abl_in.avail = ((const bool *) A.in_cols[2])[abl_i];
+    abl_out.pos = abl_in.pos;
+    abl_out.dead_cycles = abl_in.dead_cycles;
+    abl_out.avail = abl_in.avail;
+    grass_growth(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+    ((int *) A.out_cols[1])[abl_i] = abl_out.dead_cycles;
+    ((bool *) A.out_cols[2])[abl_i] = abl_out.avail;
+}
+static int abl_launch_ens_grass_growth(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_grass_growth<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
 
 static int abl_seq_gather_stats(abl_ctx *abl_C, const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
@@ -1426,19 +1684,19 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"prey_avoid_pred", 1, 0, 1, abl_radius_prey_avoid_pred, 1u, 4u, abl_launch_prey_avoid_pred, 0, -1, 1},
-    {"prey_flock", 1, 1, 1, abl_radius_prey_flock, 1u, 4u, abl_launch_prey_flock, 0, -1, 1},
-    {"prey_move", 1, -1, 1, nullptr, 0u, 11u, abl_launch_prey_move, 0, -1, 1},
-    {"prey_eaten", 1, 0, 1, abl_radius_prey_eaten, 1u, 0u, abl_launch_prey_eaten, 1, -1, 1},
-    {"prey_eat_or_starve", 1, 2, 0, abl_radius_prey_eat_or_starve, 5u, 8u, abl_launch_prey_eat_or_starve, 1, -1, 1},
-    {"prey_reproduction", 1, -1, 1, nullptr, 0u, 0u, abl_launch_prey_reproduction, 0, 1, 1},
-    {"pred_follow_prey", 0, 1, 1, abl_radius_pred_follow_prey, 1u, 4u, abl_launch_pred_follow_prey, 0, -1, 1},
-    {"pred_avoid", 0, 0, 1, abl_radius_pred_avoid, 1u, 4u, abl_launch_pred_avoid, 0, -1, 1},
-    {"pred_move", 0, -1, 1, nullptr, 0u, 11u, abl_launch_pred_move, 0, -1, 1},
-    {"pred_eat_or_starve", 0, 1, 0, abl_radius_pred_eat_or_starve, 1u, 8u, abl_launch_pred_eat_or_starve, 1, -1, 1},
-    {"pred_reproduction", 0, -1, 1, nullptr, 0u, 0u, abl_launch_pred_reproduction, 0, 0, 1},
-    {"grass_eaten", 2, 1, 1, abl_radius_grass_eaten, 1u, 0u, abl_launch_grass_eaten, 0, -1, 1},
-    {"grass_growth", 2, -1, 1, nullptr, 0u, 0u, abl_launch_grass_growth, 0, -1, 1},
+    {"prey_avoid_pred", 1, 0, 1, abl_radius_prey_avoid_pred, 1u, 4u, abl_launch_prey_avoid_pred, 0, -1, 1, abl_launch_ens_prey_avoid_pred, 0},
+    {"prey_flock", 1, 1, 1, abl_radius_prey_flock, 1u, 4u, abl_launch_prey_flock, 0, -1, 1, abl_launch_ens_prey_flock, 0},
+    {"prey_move", 1, -1, 1, nullptr, 0u, 11u, abl_launch_prey_move, 0, -1, 1, abl_launch_ens_prey_move, 0},
+    {"prey_eaten", 1, 0, 1, abl_radius_prey_eaten, 1u, 0u, abl_launch_prey_eaten, 1, -1, 1, nullptr, 0},
+    {"prey_eat_or_starve", 1, 2, 0, abl_radius_prey_eat_or_starve, 5u, 8u, abl_launch_prey_eat_or_starve, 1, -1, 1, nullptr, 0},
+    {"prey_reproduction", 1, -1, 1, nullptr, 0u, 0u, abl_launch_prey_reproduction, 0, 1, 1, nullptr, 1},
+    {"pred_follow_prey", 0, 1, 1, abl_radius_pred_follow_prey, 1u, 4u, abl_launch_pred_follow_prey, 0, -1, 1, abl_launch_ens_pred_follow_prey, 0},
+    {"pred_avoid", 0, 0, 1, abl_radius_pred_avoid, 1u, 4u, abl_launch_pred_avoid, 0, -1, 1, abl_launch_ens_pred_avoid, 0},
+    {"pred_move", 0, -1, 1, nullptr, 0u, 11u, abl_launch_pred_move, 0, -1, 1, abl_launch_ens_pred_move, 0},
+    {"pred_eat_or_starve", 0, 1, 0, abl_radius_pred_eat_or_starve, 1u, 8u, abl_launch_pred_eat_or_starve, 1, -1, 1, nullptr, 0},
+    {"pred_reproduction", 0, -1, 1, nullptr, 0u, 0u, abl_launch_pred_reproduction, 0, 0, 1, nullptr, 1},
+    {"grass_eaten", 2, 1, 1, abl_radius_grass_eaten, 1u, 0u, abl_launch_grass_eaten, 0, -1, 1, abl_launch_ens_grass_eaten, 0},
+    {"grass_growth", 2, -1, 1, nullptr, 0u, 0u, abl_launch_grass_growth, 0, -1, 1, abl_launch_ens_grass_growth, 0},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[6],
@@ -1454,7 +1712,7 @@ static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[10],
     abl_steps[5],
     abl_steps[12],
-    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0}
+    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
 };
 extern const abl_model_desc abl_desc = {
     "predator_prey", 3, abl_agents, 13, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 20, abl_global_table, 2, abl_env_bounds, nullptr, 0, abl_seq_gather_stats

@@ -115,6 +115,8 @@ class Model:
                 members.append((nm.value.decode(), vt.value))
             self.agent_types.append((L.abl_model_agent_name(self.ptr, t).decode(), members))
         self.globals_size = L.abl_model_globals_size(self.ptr)
+        L.abl_model_float_bytes.argtypes = [ctypes.c_void_p]
+        self.float_bytes = L.abl_model_float_bytes(self.ptr)
 
     def type_id(self, name):
         for k, (n, _) in enumerate(self.agent_types):
@@ -134,7 +136,7 @@ class Globals:
     def __init__(self, model, buf):
         self.model = model
         self.buf = buf
-        self.float_bytes = 4 if model.name.endswith("_float") else 8
+        self.float_bytes = model.float_bytes
 
     def _slot(self, name):
         off, vt = ctypes.c_size_t(), ctypes.c_int()
@@ -333,3 +335,105 @@ class Simulation:
         c = ctypes.c_long()
         _check(_load().abl_last_launch_count(self.ctx, ctypes.byref(c)), "abl_last_launch_count")
         return c.value
+
+
+class Ensemble:
+    """Replicas of one model run together (abl_ensemble_* in the C ABI).
+
+    `globals_list` holds one Globals block per replica (its parameter point);
+    states are uploaded and downloaded as one list of per-replica dicts."""
+
+    def __init__(self, model, globals_list, seeds=None, hbm_budget=0):
+        L = _load()
+        vp = ctypes.c_void_p
+        L.abl_ensemble_create.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_size_t,
+                                          ctypes.POINTER(vp)]
+        L.abl_ensemble_upload.argtypes = [vp, ctypes.c_int, vp, ctypes.POINTER(vp)]
+        L.abl_ensemble_run.argtypes = [vp, ctypes.c_int]
+        L.abl_ensemble_download.argtypes = [vp, ctypes.c_int, vp, ctypes.POINTER(vp)]
+        L.abl_ensemble_set_tuning.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        L.abl_ensemble_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_double),
+                                            ctypes.POINTER(ctypes.c_int)]
+        L.abl_ensemble_last_exec_time.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+        L.abl_ensemble_last_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_long)]
+        L.abl_ensemble_destroy.argtypes = [vp]
+        self.model = model if isinstance(model, Model) else Model(model)
+        self.replicas = len(globals_list)
+        self.float_bytes = self.model.float_bytes
+        blob = b"".join(bytes(g.buf) for g in globals_list)
+        self._gbuf = ctypes.create_string_buffer(blob, len(blob))
+        sd = None
+        if seeds is not None:
+            self._seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+            sd = self._seeds.ctypes.data
+        self.e = ctypes.c_void_p()
+        _check(L.abl_ensemble_create(self.model.ptr, self.replicas, self._gbuf, sd, hbm_budget,
+                                     ctypes.byref(self.e)), "abl_ensemble_create")
+
+    def upload(self, type_name, states):
+        tid = self.model.type_id(type_name)
+        members = self.model.agent_types[tid][1]
+        counts = np.array([len(s[members[0][0]]) for s in states], np.uint64)
+        keep = []
+        for nm, vt in members:
+            dt, _ = member_dtype(vt, self.float_bytes)
+            keep.append(np.ascontiguousarray(np.concatenate([np.asarray(s[nm], dt)
+                                                             for s in states])))
+        arr = (ctypes.c_void_p * len(keep))(*[a.ctypes.data for a in keep])
+        _check(_load().abl_ensemble_upload(self.e, tid, counts.ctypes.data, arr),
+               "abl_ensemble_upload")
+
+    def run(self, timesteps):
+        _check(_load().abl_ensemble_run(self.e, int(timesteps)), "abl_ensemble_run")
+
+    def download(self, type_name):
+        tid = self.model.type_id(type_name)
+        members = self.model.agent_types[tid][1]
+        counts = np.zeros(self.replicas, np.uint64)
+        _check(_load().abl_ensemble_download(self.e, tid, counts.ctypes.data, None),
+               "abl_ensemble_download")
+        total = int(counts.sum())
+        cols = {}
+        for nm, vt in members:
+            dt, shape = member_dtype(vt, self.float_bytes)
+            cols[nm] = np.empty((total,) + shape, dt)
+        arr = (ctypes.c_void_p * len(members))(*[cols[nm].ctypes.data for nm, _ in members])
+        _check(_load().abl_ensemble_download(self.e, tid, None, arr), "abl_ensemble_download")
+        out, base = [], 0
+        for c in counts.astype(np.int64):
+            out.append({nm: cols[nm][base:base + c] for nm, _ in members})
+            base += c
+        return out
+
+    def set_tuning(self, block, cell_factor, visit_sorted):
+        _check(_load().abl_ensemble_set_tuning(self.e, block, cell_factor, visit_sorted),
+               "abl_ensemble_set_tuning")
+
+    def autotune(self, trial_timesteps=3):
+        b, f, v = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+        _check(_load().abl_ensemble_autotune(self.e, trial_timesteps, ctypes.byref(b),
+                                             ctypes.byref(f), ctypes.byref(v)),
+               "abl_ensemble_autotune")
+        return {"block": b.value, "cell_factor": f.value, "visit_sorted": v.value}
+
+    def last_exec_time(self):
+        s = ctypes.c_double()
+        _check(_load().abl_ensemble_last_exec_time(self.e, ctypes.byref(s)), "exec time")
+        return s.value
+
+    def last_launch_count(self):
+        c = ctypes.c_long()
+        _check(_load().abl_ensemble_last_launch_count(self.e, ctypes.byref(c)), "launches")
+        return c.value
+
+    def close(self):
+        if self.e:
+            _load().abl_ensemble_destroy(self.e)
+            self.e = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

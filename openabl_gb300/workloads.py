@@ -56,3 +56,34 @@ def predator_prey(n_pred, n_prey, n_grass, env_size, gain_pred=35, gain_prey=60,
              "avail": np.ones(n_grass, np.uint8)}
     return {"Predator": animals(n_pred, gain_pred), "Prey": animals(n_prey, gain_prey),
             "Grass": grass}
+
+
+def boids2d_ensemble(model, base_globals, replicas=256, n_min=1000, n_max=200000,
+                     weight_spread=0.2, seed=0, agent_density=3200.0):
+    """Parameter points for an ensemble of boids2d replicas: agent counts
+    log-uniform in [n_min, n_max]; steer_scale, match_scale and
+    collision_scale (the cohesion, alignment and separation weights of
+    examples/boids2d.abl:27-29) uniform within +-weight_spread of the file's
+    values; the domain side max_pos = sqrt(n / agent_density) printed to six
+    significant digits as the compiler folds it; one seed per replica.
+    Returns (globals list, states, seeds)."""
+    import math
+    rng = np.random.Generator(np.random.PCG64(seed))
+    counts = np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=replicas)).astype(np.int64)
+    globals_list, states = [], []
+    seeds = rng.integers(0, 2**63, size=replicas, dtype=np.uint64)
+    for r in range(replicas):
+        g = model.default_globals()
+        for name in ("interaction_radius", "separation_radius", "time_scale", "global_scale",
+                     "min_pos"):
+            g.set(name, base_globals.get(name))
+        for name in ("steer_scale", "match_scale", "collision_scale"):
+            g.set(name, base_globals.get(name) * (1.0 + rng.uniform(-weight_spread, weight_spread)))
+        n = int(counts[r])
+        max_pos = float("%g" % math.sqrt(n / agent_density))
+        g.set("num_agents", n)
+        g.set("agent_density", agent_density)
+        g.set("max_pos", max_pos)
+        globals_list.append(g)
+        states.append(boids2d(n, max_pos, seed=int(seeds[r] % (2**31))))
+    return globals_list, states, seeds

@@ -51,6 +51,19 @@ def test_graph_replay_matches_reference(case, agent):
     sim.close()
 
 
+def test_use_float_matches_reference_every_timestep():
+    """-C use_float=true: the reference `c` program built with
+    LIBABL_USE_FLOAT (float agents, double literals) against the generated
+    FP32 model, bit-exact after every timestep."""
+    meta, state = load_case("boids2d_4096_float")
+    sim = make_sim("boids2d_float_4096")
+    sim.upload("Boid", state)
+    for t in range(1, meta["timesteps"] + 1):
+        sim.step()
+        assert state_hash(meta, sim.download("Boid")) == meta["sha256"][t], f"timestep {t}"
+    sim.close()
+
+
 def boids_consts(g):
     return {k: g.get(k) for k in O.BOIDS2D_KEYS}
 
