@@ -36,10 +36,16 @@ FP64_FLOP_PER_AGENT_STEP = 560   # ~72 candidates x 5 + ~25 in-radius x 8 FP64 o
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the ensemble and precision measurements")
+    ap.add_argument("--ensemble-replicas", type=int, default=256)
+    ap.add_argument("--ensemble-steps", type=int, default=200)
+    ap.add_argument("--serve-jobs", type=int, default=48)
+    ap.add_argument("--serve-slots", type=int, default=8)
     return ap.parse_args()
 
 
@@ -80,7 +86,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                 "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.file,
                 stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
@@ -106,6 +112,121 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
                 "samples": len(rows)}
+
+
+def measure_ensemble(args, o, W, np):
+    """Form (2): boids2d replicas in FP32 with log-uniform agent counts in
+    [1e3, 2e5] and steer/match/collision weights within +-20% of the file's,
+    one seed each, run as one ensemble (segmented grid, graph replay,
+    autotuned launch configuration) against the same replicas run one after
+    another through the plain single-model path."""
+    model, base = o.globals_for_config("boids2d_float_4096")
+    gl, states, seeds = W.boids2d_ensemble(model, base, replicas=args.ensemble_replicas,
+                                           n_min=1000, n_max=200000, seed=0)
+    states = [{k: v.astype(np.float32) for k, v in s.items()} for s in states]
+    total = sum(len(s["pos"]) for s in states)
+    T = args.ensemble_steps
+    ens = o.Ensemble(model, gl, seeds=seeds)
+    ens.upload("Boid", states)
+    tuning = ens.autotune(3)
+    ens.run(3)
+    ens.upload("Boid", states)
+    ens.run(T)
+    ens_s = ens.last_exec_time()
+    launches = ens.last_launch_count()
+    ens.close()
+    base_s = 0.0
+    base_launches = 0
+    for g, st in zip(gl, states):
+        sim = o.Simulation(model, g)
+        sim.upload("Boid", st)
+        sim.run(2)
+        sim.upload("Boid", st)
+        sim.run(T)
+        base_s += sim.last_exec_time()
+        base_launches += sim.last_launch_count()
+        sim.close()
+    return {"workload": f"{args.ensemble_replicas} boids2d replicas FP32, agents log-uniform "
+                        f"1e3-2e5 (total {total}), weights +-20%, {T} timesteps",
+            "value": total * T / ens_s, "unit": "agent-steps/s", "seconds": ens_s,
+            "gpu_launches": launches, "tuning": tuning,
+            "baseline_value": total * T / base_s, "baseline_seconds": base_s,
+            "baseline_gpu_launches": base_launches,
+            "baseline": "same replicas one after another, each in its own context",
+            "speedup": base_s / ens_s}
+
+
+def measure_precision(args, o, W, np, steps=100):
+    """Form (1): the use_float model (all agent arithmetic in FP32, as
+    LIBABL_USE_FLOAT) against FP64 on the 1M boids2d workload."""
+    m64, g64 = o.globals_for_config(CONFIG)
+    m32, g32 = o.globals_for_config("boids2d_float_1m")
+    n = g64.get("num_agents")
+    st = W.boids2d(n, g64.get("max_pos"), seed=0)
+    a = o.Simulation(m64, g64)
+    a.upload("Boid", st)
+    a.run(steps)
+    t64 = a.last_exec_time()
+    r64 = a.download("Boid")
+    a.close()
+    b = o.Simulation(m32, g32)
+    b.upload("Boid", {k: v.astype(np.float32) for k, v in st.items()})
+    b.run(steps)
+    t32 = b.last_exec_time()
+    r32 = b.download("Boid")
+    b.close()
+    L = g64.get("max_pos")
+    dp = np.abs(r32["pos"].astype(np.float64) - r64["pos"]).max(axis=1) / L
+    # boundPosition moves an agent leaving the domain to the opposite side, so
+    # also measure the error up to that jump (minimum image).
+    d = np.abs(r32["pos"].astype(np.float64) - r64["pos"])
+    dpi = np.minimum(d, np.abs(L - d)).max(axis=1) / L
+    dv = np.abs(r32["velocity"].astype(np.float64) - r64["velocity"]).max(axis=1)
+    return {"workload": f"boids2d {n} agents, {steps} timesteps, FP32 (use_float) vs FP64",
+            "fp32_value": n * steps / t32, "fp64_value": n * steps / t64, "unit": "agent-steps/s",
+            "pos_rel_err_max": float(dp.max()), "pos_rel_err_median": float(np.median(dp)),
+            "pos_rel_err_p99": float(np.quantile(dp, 0.99)),
+            "vel_abs_err_median": float(np.median(dv)),
+            "frac_agents_rel_err_le_1e-5": float((dp <= 1e-5).mean()),
+            "pos_rel_err_min_image_max": float(dpi.max()),
+            "frac_agents_min_image_err_le_1e-5": float((dpi <= 1e-5).mean()),
+            "error_metric": "per agent max |pos32 - pos64| / max_pos"}
+
+
+def measure_serving(args, o, W, np):
+    """Form (5): a Poisson stream (200 jobs/s) of circle, circle3d, boids2d and
+    predator_prey simulations, agents log-uniform in [1e3, 1e6], timesteps
+    uniform in [50, 1000], FP32/FP64 50/50, admitted by an 80 GB device-memory
+    budget into `slots` concurrent workers.  Latency = completion - arrival."""
+    stream = W.serving_stream(jobs=args.serve_jobs, rate=200.0, seed=0)
+    prepared = [(t, W.served_job(m, n, prec, seed=k), steps, n, m, prec)
+                for k, (t, m, n, steps, prec, seed) in enumerate(stream)]
+    srv = o.Server(slots=args.serve_slots, hbm_budget=80 * 10**9)
+    ids = []
+    t0 = time.perf_counter()
+    for t_arr, (model, g, state), steps, n, m, prec in prepared:
+        delay = t0 + t_arr - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        ids.append((srv.submit(model, g, state, steps, seed=len(ids)), n, steps, m, prec))
+    for jid, *_ in ids:
+        srv.wait(jid, timeout=1800.0)
+    infos = [srv.info(jid) for jid, *_ in ids]
+    srv.close()
+    lat = np.array([i["done"] - i["submit"] for i in infos])
+    wait = np.array([i["admit"] - i["submit"] for i in infos])
+    first = min(i["submit"] for i in infos)
+    last = max(i["done"] for i in infos)
+    work = sum(n * steps for _, n, steps, _, _ in ids)
+    failed = sum(1 for i in infos if i["status"] != 2)
+    return {"workload": f"{len(ids)} jobs, Poisson 200/s, circle/circle3d/boids2d/predator_prey, "
+                        "agents log-uniform 1e3-1e6, timesteps U[50,1000], FP32/FP64 50/50, "
+                        f"80 GB budget, {args.serve_slots} slots",
+            "value": work / (last - first), "unit": "agent-steps/s",
+            "latency_p50_s": float(np.percentile(lat, 50)),
+            "latency_p99_s": float(np.percentile(lat, 99)),
+            "queue_wait_p50_s": float(np.percentile(wait, 50)),
+            "makespan_s": last - first, "jobs": len(ids), "failed": failed}
 
 
 def run_reference(args):
@@ -234,6 +355,12 @@ def run_ours(args):
     e2e_value = world * n * e2e_steps / e2e_wall
     h2d = sum(v.nbytes for v in pin.values())
 
+    forms = {}
+    if not args.no_forms:
+        forms["ensemble"] = measure_ensemble(args, o, W, np)
+        forms["precision"] = measure_precision(args, o, W, np)
+        forms["serving"] = measure_serving(args, o, W, np)
+
     cpu = None
     if rank == 0:
         from oracle import oracle as O
@@ -270,6 +397,7 @@ def run_ours(args):
         "clocks": clock_info,
         "cpu_baseline": cpu,
     }
+    line.update(forms)
     print(json.dumps(line))
     return 0
 

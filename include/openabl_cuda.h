@@ -164,6 +164,40 @@ int abl_ensemble_last_exec_time(abl_ensemble *e, double *seconds);
 int abl_ensemble_last_launch_count(abl_ensemble *e, long *launches);
 int abl_ensemble_destroy(abl_ensemble *e);
 
+/* ---- serving: continuous batching of simulation jobs ----
+ *
+ * No counterpart in the reference, whose programs run one simulation per
+ * process.  A server runs submitted simulation jobs concurrently: a job is
+ * admitted as soon as one of `slots` workers is free and its estimated
+ * device memory fits in what is left of `hbm_budget` (0: 90% of free
+ * memory); each running job has its own context and stream, so the work of
+ * all running jobs overlaps on the device, and queued jobs start as soon as
+ * running ones release their slot and memory.  State stays on the device for
+ * the whole job; results are kept in host memory until released. */
+typedef struct abl_server abl_server;
+typedef struct {
+  const abl_model_desc *model;
+  const void *globals;          /* NULL: the model's defaults */
+  uint64_t seed;                /* random() seed */
+  int timesteps;
+  const size_t *counts;         /* agents per type */
+  const void *const *const *cols; /* per type: host SoA columns (copied at submit) */
+} abl_job_desc;
+int abl_server_create(int slots, size_t hbm_budget, abl_server **out);
+int abl_server_submit(abl_server *s, const abl_job_desc *job, long *job_id);
+/* Blocks until the job has finished (ABL_E_TIMEOUT after timeout_s). */
+int abl_server_wait(abl_server *s, long job_id, double timeout_s);
+/* status: 0 queued, 1 running, 2 done, < 0 failed with that ABL_E_* code;
+ * times[4]: submit, admission and completion (seconds, steady clock) and the
+ * device time of its timesteps. */
+int abl_server_job_info(abl_server *s, long job_id, int *status, double *times);
+/* Final population of one agent type (like abl_download). */
+int abl_server_result(abl_server *s, long job_id, int type_id, void *const *cols, size_t *n);
+int abl_server_release(abl_server *s, long job_id);
+int abl_server_stats(abl_server *s, int *queued, int *running, size_t *bytes_in_use);
+/* Runs the queued jobs to completion, then stops the workers. */
+int abl_server_destroy(abl_server *s);
+
 /* ---- allocation-free timestep ----
  *
  * No counterpart in the reference (whose `c` backend never touches a GPU).

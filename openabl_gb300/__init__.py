@@ -6,5 +6,5 @@
     openabl_gb300/generated   `-b cuda` output for the example models
     openabl_gb300/runtime.py  Python host over the C ABI
 """
-from .runtime import (AblError, Ensemble, Globals, Model, Simulation, configs,  # noqa: F401
+from .runtime import (AblError, Ensemble, Globals, Model, Server, Simulation, configs,  # noqa: F401
                       globals_for_config, library)

@@ -36,7 +36,8 @@ def nvcc():
 
 def sources():
     srcs = [os.path.join(CSRC, "abl_runtime.cu"), os.path.join(CSRC, "abl_host.cpp"),
-            os.path.join(CSRC, "abl_diag.cu"), os.path.join(GEN, "registry.cpp")]
+            os.path.join(CSRC, "abl_diag.cu"), os.path.join(CSRC, "abl_serve.cpp"),
+            os.path.join(GEN, "registry.cpp")]
     srcs += sorted(os.path.join(GEN, f) for f in os.listdir(GEN) if f.endswith(".cu"))
     return srcs
 
@@ -52,7 +53,7 @@ def _compile(src):
     if (os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src)
             and os.path.getmtime(obj) >= _deps_mtime()):
         return obj
-    lang = ["-x", "cu"] if src.endswith((".cu", "registry.cpp")) else []
+    lang = ["-x", "cu"] if src.endswith((".cu", "registry.cpp")) else ["-Xcompiler", "-pthread"]
     cmd = [nvcc()] + NVCC_FLAGS + lang + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -67,7 +68,8 @@ def build(verbose=False):
         objs = list(ex.map(_compile, srcs))
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
         return LIB
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-ldl"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-ldl",
+                                                              "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

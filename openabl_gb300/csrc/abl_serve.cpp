@@ -1,0 +1,290 @@
+// Simulation-job server: continuous batching of whole simulations.
+//
+// Jobs (a model, its globals, a seed, an initial population and a number of
+// timesteps) are submitted from any thread and queue for admission.  A job is
+// admitted as soon as one of the server's slots is free AND its estimated
+// device memory fits in what is left of the server's HBM budget; an admitted
+// job runs in its own runtime context on its own CUDA stream, so the kernels
+// of all running jobs overlap on the device, and the next queued job starts
+// the moment a running one finishes and releases its slot and memory.  The
+// state stays resident on the device for the whole run; the final population
+// is copied back to host memory owned by the server until released.
+//
+// Each job keeps its submit, admission and completion times (steady clock)
+// and the device time of its timesteps, so callers can report latency
+// percentiles next to aggregate throughput.  A job computes exactly what the
+// same job computes alone: contexts share nothing but the device.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "abl_model.h"
+
+namespace {
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+size_t member_size(const abl_member_desc &m) { return (size_t) m.components * m.scalar_bytes; }
+
+struct Job {
+  long id = 0;
+  const abl_model_desc *model = nullptr;
+  std::vector<unsigned char> globals;
+  uint64_t seed = 0;
+  int timesteps = 0;
+  // population per type: counts and one host column per member
+  std::vector<size_t> counts;
+  std::vector<std::vector<std::vector<unsigned char>>> cols;
+  size_t reserve = 0;  // bytes of budget held while running
+  int status = 0;      // 0 queued, 1 running, 2 done, < 0 error code
+  double t_submit = 0, t_admit = 0, t_done = 0, exec_s = 0;
+};
+
+}  // namespace
+
+struct abl_server {
+  int device = 0;
+  size_t budget = 0, in_use = 0;
+  int slots = 0, running = 0;
+  bool stop = false;
+  long next_id = 1;
+  std::mutex mu;
+  std::condition_variable cv;       // queue, budget and stop changes
+  std::condition_variable done_cv;  // job completions
+  std::deque<std::shared_ptr<Job>> queue;
+  std::map<long, std::shared_ptr<Job>> jobs;
+  std::vector<std::thread> workers;
+};
+
+namespace {
+
+// Device memory a job needs: both buffers of every column, the binning
+// arrays (cell index, rank, slot order, float positions, gathered members,
+// neighbourhood lists of up to 27 slots per agent) and spare capacity for
+// types whose population changes, plus a fixed allowance for grid arrays.
+size_t estimate_bytes(const abl_model_desc *m, const std::vector<size_t> &counts) {
+  size_t total = 64u << 20;
+  for (int t = 0; t < m->num_agent_types; t++) {
+    size_t rec = 0;
+    for (int k = 0; k < m->agents[t].num_members; k++) rec += member_size(m->agents[t].members[k]);
+    bool dynamic = false;
+    for (int s = 0; s < m->num_steps; s++) {
+      if (m->steps[s].agent_type == t && m->steps[s].uses_remove) dynamic = true;
+      if (m->steps[s].add_type == t) dynamic = true;
+    }
+    size_t n = counts[t] * (dynamic ? 2 : 1) + (dynamic ? 1024 : 1);
+    size_t per = 2 * rec + 4 * 4 + 12 + rec + 27 * 4 + (dynamic ? 2 * rec + 24 : 0);
+    total += n * per;
+  }
+  return total;
+}
+
+void run_job(abl_server *S, const std::shared_ptr<Job> &job) {
+  abl_ctx *ctx = nullptr;
+  int r = abl_create(job->model, job->reserve, &ctx);
+  if (r == ABL_OK) r = abl_set_globals(ctx, job->globals.data(), job->globals.size());
+  if (r == ABL_OK) r = abl_set_seed(ctx, job->seed);
+  for (int t = 0; r == ABL_OK && t < job->model->num_agent_types; t++) {
+    std::vector<const void *> cols;
+    for (auto &c : job->cols[t]) cols.push_back(c.data());
+    r = abl_upload(ctx, t, cols.data(), job->counts[t]);
+  }
+  if (r == ABL_OK) r = abl_run(ctx, job->timesteps);
+  double exec = 0;
+  if (r == ABL_OK) abl_last_exec_time(ctx, &exec);
+  for (int t = 0; r == ABL_OK && t < job->model->num_agent_types; t++) {
+    size_t n = 0;
+    r = abl_count(ctx, t, &n);
+    if (r != ABL_OK) break;
+    std::vector<void *> cols;
+    for (int k = 0; k < job->model->agents[t].num_members; k++) {
+      job->cols[t][k].resize(std::max<size_t>(1, n * member_size(job->model->agents[t].members[k])));
+      cols.push_back(job->cols[t][k].data());
+    }
+    size_t cap = n;
+    r = abl_download(ctx, t, cols.data(), &cap);
+    job->counts[t] = n;
+  }
+  if (ctx) abl_destroy(ctx);
+  std::lock_guard<std::mutex> lock(S->mu);
+  job->exec_s = exec;
+  job->t_done = now_s();
+  job->status = r == ABL_OK ? 2 : r;
+  S->in_use -= job->reserve;
+  S->running--;
+  S->cv.notify_all();
+  S->done_cv.notify_all();
+}
+
+void worker(abl_server *S) {
+  cudaSetDevice(S->device);
+  for (;;) {
+    std::shared_ptr<Job> job;
+    {
+      std::unique_lock<std::mutex> lock(S->mu);
+      // Admit the oldest queued job once it fits in the remaining budget
+      // (jobs larger than the whole budget are rejected at submission).
+      S->cv.wait(lock, [&] {
+        return S->stop || (!S->queue.empty()
+                           && S->in_use + S->queue.front()->reserve <= S->budget);
+      });
+      if (S->stop && S->queue.empty()) return;
+      if (S->queue.empty()) continue;
+      job = S->queue.front();
+      S->queue.pop_front();
+      S->in_use += job->reserve;
+      S->running++;
+      job->status = 1;
+      job->t_admit = now_s();
+    }
+    run_job(S, job);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int abl_server_create(int slots, size_t hbm_budget, abl_server **out) {
+  if (slots <= 0 || !out) return ABL_E_INVALID;
+  abl_server *S = new abl_server;
+  cudaGetDevice(&S->device);
+  S->slots = slots;
+  if (hbm_budget == 0) {
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    hbm_budget = free_b / 10 * 9;
+  }
+  S->budget = hbm_budget;
+  for (int k = 0; k < slots; k++) S->workers.emplace_back(worker, S);
+  *out = S;
+  return ABL_OK;
+}
+
+int abl_server_submit(abl_server *S, const abl_job_desc *jd, long *job_id) {
+  if (!S || !jd || !jd->model || !jd->counts || jd->timesteps < 0) return ABL_E_INVALID;
+  const abl_model_desc *m = jd->model;
+  auto job = std::make_shared<Job>();
+  job->model = m;
+  const unsigned char *g = (const unsigned char *) (jd->globals ? jd->globals
+                                                                : m->globals_default);
+  job->globals.assign(g, g + m->globals_size);
+  job->seed = jd->seed;
+  job->timesteps = jd->timesteps;
+  job->counts.assign(jd->counts, jd->counts + m->num_agent_types);
+  job->cols.resize(m->num_agent_types);
+  for (int t = 0; t < m->num_agent_types; t++) {
+    for (int k = 0; k < m->agents[t].num_members; k++) {
+      size_t bytes = job->counts[t] * member_size(m->agents[t].members[k]);
+      const unsigned char *src = bytes ? (const unsigned char *) jd->cols[t][k] : nullptr;
+      job->cols[t].emplace_back(src, src + bytes);
+    }
+  }
+  job->reserve = estimate_bytes(m, job->counts);
+  std::lock_guard<std::mutex> lock(S->mu);
+  if (job->reserve > S->budget) return ABL_E_BUDGET;
+  job->id = S->next_id++;
+  job->t_submit = now_s();
+  S->jobs[job->id] = job;
+  S->queue.push_back(job);
+  S->cv.notify_all();
+  if (job_id) *job_id = job->id;
+  return ABL_OK;
+}
+
+int abl_server_wait(abl_server *S, long job_id, double timeout_s) {
+  if (!S) return ABL_E_INVALID;
+  std::unique_lock<std::mutex> lock(S->mu);
+  auto it = S->jobs.find(job_id);
+  if (it == S->jobs.end()) return ABL_E_INVALID;
+  auto job = it->second;
+  bool ok = S->done_cv.wait_for(lock, std::chrono::duration<double>(timeout_s),
+                                [&] { return job->status == 2 || job->status < 0; });
+  if (!ok) return ABL_E_TIMEOUT;
+  return job->status < 0 ? job->status : ABL_OK;
+}
+
+int abl_server_job_info(abl_server *S, long job_id, int *status, double *times) {
+  if (!S) return ABL_E_INVALID;
+  std::lock_guard<std::mutex> lock(S->mu);
+  auto it = S->jobs.find(job_id);
+  if (it == S->jobs.end()) return ABL_E_INVALID;
+  const Job &j = *it->second;
+  if (status) *status = j.status;
+  if (times) {
+    times[0] = j.t_submit;
+    times[1] = j.t_admit;
+    times[2] = j.t_done;
+    times[3] = j.exec_s;
+  }
+  return ABL_OK;
+}
+
+int abl_server_result(abl_server *S, long job_id, int type_id, void *const *cols, size_t *n) {
+  if (!S || !n) return ABL_E_INVALID;
+  std::shared_ptr<Job> job;
+  {
+    std::lock_guard<std::mutex> lock(S->mu);
+    auto it = S->jobs.find(job_id);
+    if (it == S->jobs.end()) return ABL_E_INVALID;
+    job = it->second;
+    if (job->status != 2) return job->status < 0 ? job->status : ABL_E_INVALID;
+  }
+  if (type_id < 0 || type_id >= job->model->num_agent_types) return ABL_E_INVALID;
+  size_t cnt = job->counts[type_id];
+  if (!cols || *n < cnt) {
+    *n = cnt;
+    return cols ? ABL_E_INVALID : ABL_OK;
+  }
+  for (int k = 0; k < job->model->agents[type_id].num_members; k++) {
+    size_t bytes = cnt * member_size(job->model->agents[type_id].members[k]);
+    if (bytes) std::memcpy(cols[k], job->cols[type_id][k].data(), bytes);
+  }
+  *n = cnt;
+  return ABL_OK;
+}
+
+int abl_server_release(abl_server *S, long job_id) {
+  if (!S) return ABL_E_INVALID;
+  std::lock_guard<std::mutex> lock(S->mu);
+  auto it = S->jobs.find(job_id);
+  if (it == S->jobs.end()) return ABL_E_INVALID;
+  if (it->second->status == 0 || it->second->status == 1) return ABL_E_INVALID;
+  S->jobs.erase(it);
+  return ABL_OK;
+}
+
+int abl_server_stats(abl_server *S, int *queued, int *running, size_t *bytes_in_use) {
+  if (!S) return ABL_E_INVALID;
+  std::lock_guard<std::mutex> lock(S->mu);
+  if (queued) *queued = (int) S->queue.size();
+  if (running) *running = S->running;
+  if (bytes_in_use) *bytes_in_use = S->in_use;
+  return ABL_OK;
+}
+
+int abl_server_destroy(abl_server *S) {
+  if (!S) return ABL_E_INVALID;
+  {
+    std::lock_guard<std::mutex> lock(S->mu);
+    S->stop = true;
+    S->cv.notify_all();
+  }
+  for (auto &w : S->workers) w.join();
+  delete S;
+  return ABL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,315 @@
+// Generated by OpenABL -b cuda (model "circle3d_float").
+#include "abl_gen.cuh"
+
+namespace abl_model_circle3d_float {
+
+typedef float abl_float;
+#include "abl_math.cuh"
+
+typedef struct {
+    float3 pos;
+} Point;
+static const type_info Point_info[] = {
+    { TYPE_FLOAT3, offsetof(Point, pos), "pos", true },
+    { TYPE_END, sizeof(Point), NULL }
+};
+
+struct agent_struct {
+    dyn_array agents_Point;
+    dyn_array agents_Point_dbuf;
+};
+static struct agent_struct agents;
+static const agent_info agents_info[] = {
+    { Point_info, offsetof(struct agent_struct, agents_Point), "Point" },
+    { NULL, 0, NULL }
+};
+
+struct abl_globals {
+    float PI;
+    int num_timesteps;
+    int num_agents;
+    float rho;
+    float k_rep;
+    float k_att;
+    float r;
+    float W;
+};
+static const abl_globals abl_globals_default = {
+    3.14159,
+    100,
+    1000,
+    0.05,
+    0.05,
+    0.01,
+    5.0,
+    27.1442,
+};
+static abl_globals abl_G = abl_globals_default;
+static abl::rng abl_R;  // unused on the host: main() draws from the host stream
+struct abl_cols_Point {
+    float3 *pos;
+};
+
+__host__ __device__ static inline float2 random_1(const abl_globals &abl_G, abl::rng &abl_R, float2 min, float2 max) {
+    return float2_create(abl_random(abl_R, min.x, max.x), abl_random(abl_R, min.y, max.y));
+}
+__host__ __device__ static inline float3 random_2(const abl_globals &abl_G, abl::rng &abl_R, float3 min, float3 max) {
+    return float3_create(abl_random(abl_R, min.x, max.x), abl_random(abl_R, min.y, max.y), abl_random(abl_R, min.z, max.z));
+}
+__host__ __device__ static inline float random_3(const abl_globals &abl_G, abl::rng &abl_R, float max) {
+    return abl_random(abl_R, 0, max);
+}
+__host__ __device__ static inline float2 random_4(const abl_globals &abl_G, abl::rng &abl_R, float2 max) {
+    return random_1(abl_G, abl_R, float2_fill(0), max);
+}
+__host__ __device__ static inline float3 random_5(const abl_globals &abl_G, abl::rng &abl_R, float3 max) {
+    return random_2(abl_G, abl_R, float3_fill(0), max);
+}
+__host__ __device__ static inline int randomInt_1(const abl_globals &abl_G, abl::rng &abl_R, int max) {
+    return abl_random_int(abl_R, 0, max);
+}
+__host__ __device__ static inline float clamp(const abl_globals &abl_G, abl::rng &abl_R, float pos, float min, float max) {
+    return ((pos < min) ? min : ((pos > max) ? max : pos));
+}
+__host__ __device__ static inline float2 clamp_1(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 min, float2 max) {
+    return float2_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)));
+}
+__host__ __device__ static inline float3 clamp_2(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 min, float3 max) {
+    return float3_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)), ((pos.z < min.z) ? min.z : ((pos.z > max.z) ? max.z : pos.z)));
+}
+__host__ __device__ static inline float clamp_3(const abl_globals &abl_G, abl::rng &abl_R, float pos, float max) {
+    return clamp(abl_G, abl_R, pos, 0, max);
+}
+__host__ __device__ static inline float2 clamp_4(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return clamp_1(abl_G, abl_R, pos, float2_fill(0), max);
+}
+__host__ __device__ static inline float3 clamp_5(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 max) {
+    return clamp_2(abl_G, abl_R, pos, float3_fill(0), max);
+}
+__host__ __device__ static inline float wraparound(const abl_globals &abl_G, abl::rng &abl_R, float pos, float max) {
+    return ((pos < 0) ? (max + pos) : ((pos >= max) ? (pos - max) : pos));
+}
+__host__ __device__ static inline float2 wraparound_1(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return float2_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)));
+}
+__host__ __device__ static inline float3 wraparound_2(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 max) {
+    return float3_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)), ((pos.z < 0) ? (max.z + pos.z) : ((pos.z >= max.z) ? (pos.z - max.z) : pos.z)));
+}
+__host__ __device__ static inline bool is_inside(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return ((((pos.x >= 0) && (pos.y >= 0)) && (pos.x <= max.x)) && (pos.y <= max.y));
+}
+__device__ static void move_point(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Point* in, Point* out) {
+    abl::rng &abl_R = abl_K.R;
+    (void) abl_R; (void) abl_NB;
+    float3 new_pos = in->pos;
+    {
+        const abl::near_query<3> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, (double) in->pos.z);
+        abl::near_cursor<3> abl_c1(abl_NB, abl_q1);
+        auto abl_exact1 = [&](int abl_s) -> bool {
+            const float3 abl_p = ((const float3 *) abl_NB.cols[0])[abl_s];
+            return !(dist_float3(abl_p, in->pos) > (2.0 * abl_G.r));
+        };
+        while (abl_c1.fill(abl_q1, abl_exact1)) {
+            for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
+                const int abl_slot1 = abl_c1.slot(abl_k);
+                Point abl_nx1;
+                abl_nx1.pos = ((const float3 *) abl_NB.cols[0])[abl_slot1];
+                Point* nx = &abl_nx1;
+                {
+                    float pos_dist = dist_float3(in->pos, nx->pos);
+                    if ((pos_dist == 0)) continue;
+                    float sep_dist = (pos_dist - abl_G.r);
+                    float3 force = float3_fill(0);
+                    if ((sep_dist > 0.0)) {
+                        force = float3_div_scalar(float3_mul_scalar(float3_sub(nx->pos, in->pos), (abl_G.k_att * ((2.0 * abl_G.r) - pos_dist))), pos_dist);
+                    } else {
+                        force = float3_mul_scalar(float3_sub(in->pos, nx->pos), abl_G.k_rep);
+                    }
+                    new_pos = float3_add(new_pos, force);
+                }
+            }
+        }
+    }
+    out->pos = clamp_2(abl_G, abl_R, new_pos, float3_fill(1), float3_fill((abl_G.W - 1.0)));
+}
+
+struct abl_kargs_move_point {
+    abl_globals G;
+    long n;
+    const int *visit;
+    abl_cols_Point in, out;
+    abl_near_view NB;
+    uint8_t *removed;
+    uint8_t *child_flag;
+    void *child_cols[ABL_MAX_MEMBERS];
+    uint64_t seed;
+    long timestep;
+    int step_index;
+};
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_move_point(const __grid_constant__ abl_kargs_move_point A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = A.child_cols;
+    Point abl_in, abl_out;
+    abl_in.pos = A.in.pos[abl_i];
+    move_point(A.G, A.NB, abl_K, &abl_in, &abl_out);
+    A.out.pos[abl_i] = abl_out.pos;
+}
+static int abl_launch_move_point(const abl_step_launch *L, cudaStream_t abl_stream) {
+    abl_kargs_move_point A;
+    A.G = *(const abl_globals *) L->globals;
+    A.n = L->n;
+    A.visit = L->visit_order;
+    A.in.pos = (float3 *) L->in_cols[0];
+    A.out.pos = (float3 *) L->out_cols[0];
+    A.NB = L->near;
+    A.removed = L->removed;
+    A.child_flag = L->child_flag;
+    for (int k = 0; k < ABL_MAX_MEMBERS; k++) A.child_cols[k] = L->child_cols[k];
+    A.seed = L->seed;
+    A.timestep = L->timestep;
+    A.step_index = L->step_index;
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (A.n + abl_block - 1) / abl_block;
+    abl_kernel_move_point<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
+__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_move_point(const __grid_constant__ abl_ens_launch A) {
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    Point abl_in, abl_out;
+    abl_in.pos = ((const float3 *) A.in_cols[0])[abl_i];
+    move_point(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float3 *) A.out_cols[0])[abl_i] = abl_out.pos;
+}
+static int abl_launch_ens_move_point(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_move_point<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
+static double abl_radius_move_point(const void *abl_gp) {
+    const abl_globals &abl_G = *(const abl_globals *) abl_gp;
+    abl::rng abl_R;
+    (void) abl_G; (void) abl_R;
+    return (double) ((2.0 * abl_G.r));
+}
+
+
+static const abl_member_desc abl_members_Point[] = {
+    {"pos", ABL_T_FLOAT3, 3, 4, 1},
+};
+static const abl_agent_desc abl_agents[] = {
+    {"Point", 1, abl_members_Point, 0, 3},
+};
+static const abl_global_desc abl_global_table[] = {
+    {"PI", ABL_T_FLOAT, offsetof(abl_globals, PI)},
+    {"num_timesteps", ABL_T_INT, offsetof(abl_globals, num_timesteps)},
+    {"num_agents", ABL_T_INT, offsetof(abl_globals, num_agents)},
+    {"rho", ABL_T_FLOAT, offsetof(abl_globals, rho)},
+    {"k_rep", ABL_T_FLOAT, offsetof(abl_globals, k_rep)},
+    {"k_att", ABL_T_FLOAT, offsetof(abl_globals, k_att)},
+    {"r", ABL_T_FLOAT, offsetof(abl_globals, r)},
+    {"W", ABL_T_FLOAT, offsetof(abl_globals, W)},
+    {nullptr, 0, 0}
+};
+static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max) {
+    const abl_globals &abl_G = *(const abl_globals *) abl_gp;
+    abl::rng abl_R;
+    (void) abl_G; (void) abl_R;
+    float3 abl_lo = float3_fill(0);
+    float3 abl_hi = float3_fill(abl_G.W);
+    abl_min[0] = abl_lo.x; abl_min[1] = abl_lo.y; abl_min[2] = abl_lo.z;
+    abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = abl_hi.z;
+}
+static const abl_step_desc abl_steps[] = {
+    {"move_point", 0, 0, 1, abl_radius_move_point, 1u, 1u, abl_launch_move_point, 0, -1, 0, abl_launch_ens_move_point, 0},
+};
+static const abl_step_desc abl_steps_ordered[] = {
+    abl_steps[0],
+    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
+};
+extern const abl_model_desc abl_desc = {
+    "circle3d_float", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 8, abl_global_table, 3, abl_env_bounds, nullptr, 1, nullptr
+};
+static void abl_check(int r, const char *what) {
+    if (r != ABL_OK) {
+        std::fprintf(stderr, "%s failed: %s\n", what, abl_strerror(r));
+        std::exit(1);
+    }
+}
+static void abl_simulate(int abl_timesteps) {
+    abl_ctx *ctx = nullptr;
+    abl_check(abl_create(&abl_desc, 0, &ctx), "abl_create");
+    abl_check(abl_set_globals(ctx, &abl_G, sizeof abl_G), "abl_set_globals");
+    {
+        size_t n = agents.agents_Point.len;
+        const Point *aos = (const Point *) agents.agents_Point.values;
+        float3 *c0 = (float3 *) std::malloc(sizeof(float3) * (n ? n : 1));
+        for (size_t i = 0; i < n; i++) c0[i] = aos[i].pos;
+        const void *cols[] = {c0};
+        abl_check(abl_upload(ctx, 0, cols, n), "abl_upload");
+        std::free(c0);
+    }
+    abl_check(abl_run(ctx, abl_timesteps), "abl_run");
+    {
+        size_t n = 0;
+        abl_check(abl_count(ctx, 0, &n), "abl_count");
+        float3 *c0 = (float3 *) std::malloc(sizeof(float3) * (n ? n : 1));
+        void *cols[] = {c0};
+        size_t cap = n;
+        abl_check(abl_download(ctx, 0, cols, &cap), "abl_download");
+        dyn_array_clean(&agents.agents_Point);
+        agents.agents_Point = dyn_array_create_fixed(sizeof(Point), n);
+        Point *aos = (Point *) agents.agents_Point.values;
+        for (size_t i = 0; i < n; i++) {
+            aos[i].pos = c0[i];
+        }
+        std::free(c0);
+    }
+    size_t abl_log_len = 0;
+    abl_log_text(ctx, nullptr, 0, &abl_log_len);
+    if (abl_log_len > 0) {
+        char *abl_log = (char *) std::malloc(abl_log_len + 1);
+        abl_log_text(ctx, abl_log, abl_log_len + 1, nullptr);
+        FILE *abl_f = std::fopen("log.csv", "w");
+        if (abl_f) { std::fputs(abl_log, abl_f); std::fclose(abl_f); }
+        std::free(abl_log);
+    }
+    abl_destroy(ctx);
+}
+static int abl_main() {
+    for (int i = 0, _var0 = abl_G.num_agents; i < _var0; ++i) {
+        *DYN_ARRAY_PLACE(&agents.agents_Point, Point) = ([&]() { Point abl_a; abl_a.pos = random_5(abl_G, abl_R, float3_create(27.1442, 27.1442, 27.1442)); return abl_a; }());
+    }
+    abl_simulate(abl_G.num_timesteps);
+    save(&agents, agents_info, "points.json", SAVE_JSON);
+    return 0;
+}
+
+}  // namespace abl_model_circle3d_float
+
+extern "C" const abl_model_desc *abl_model_desc_circle3d_float(void) {
+    return &abl_model_circle3d_float::abl_desc;
+}
+
+#ifdef ABL_STANDALONE_MAIN
+extern "C" const abl_model_desc *const abl_builtin_models[] = {
+    &abl_model_circle3d_float::abl_desc, nullptr};
+int main() { return abl_model_circle3d_float::abl_main(); }
+#endif

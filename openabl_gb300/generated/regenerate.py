@@ -29,6 +29,9 @@ MODELS = {
     "game_of_life": ("game_of_life.abl", {}),
     "boids2d_float": ("boids2d.abl", {"use_float": "true"}),
     "predator_prey": ("predator_prey.abl", {}),
+    "circle_float": ("circle.abl", {"use_float": "true"}),
+    "circle3d_float": ("circle3d.abl", {"use_float": "true"}),
+    "predator_prey_float": ("predator_prey.abl", {"use_float": "true"}),
 }
 
 # configuration name -> (model, -P params)

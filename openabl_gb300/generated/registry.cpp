@@ -8,6 +8,9 @@ const abl_model_desc *abl_model_desc_boids2d(void);
 const abl_model_desc *abl_model_desc_game_of_life(void);
 const abl_model_desc *abl_model_desc_boids2d_float(void);
 const abl_model_desc *abl_model_desc_predator_prey(void);
+const abl_model_desc *abl_model_desc_circle_float(void);
+const abl_model_desc *abl_model_desc_circle3d_float(void);
+const abl_model_desc *abl_model_desc_predator_prey_float(void);
 extern const abl_model_desc *const abl_builtin_models[];
 const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_circle(),
@@ -16,5 +19,8 @@ const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_game_of_life(),
     abl_model_desc_boids2d_float(),
     abl_model_desc_predator_prey(),
+    abl_model_desc_circle_float(),
+    abl_model_desc_circle3d_float(),
+    abl_model_desc_predator_prey_float(),
     nullptr};
 }

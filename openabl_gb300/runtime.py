@@ -437,3 +437,100 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+class _JobDesc(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_void_p), ("globals", ctypes.c_void_p),
+                ("seed", ctypes.c_uint64), ("timesteps", ctypes.c_int),
+                ("counts", ctypes.c_void_p), ("cols", ctypes.c_void_p)]
+
+
+class Server:
+    """Continuous-batching simulation server (abl_server_* in the C ABI)."""
+
+    def __init__(self, slots=8, hbm_budget=0):
+        L = _load()
+        vp = ctypes.c_void_p
+        L.abl_server_create.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(vp)]
+        L.abl_server_submit.argtypes = [vp, ctypes.POINTER(_JobDesc), ctypes.POINTER(ctypes.c_long)]
+        L.abl_server_wait.argtypes = [vp, ctypes.c_long, ctypes.c_double]
+        L.abl_server_job_info.argtypes = [vp, ctypes.c_long, ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_double)]
+        L.abl_server_result.argtypes = [vp, ctypes.c_long, ctypes.c_int, vp,
+                                        ctypes.POINTER(ctypes.c_size_t)]
+        L.abl_server_release.argtypes = [vp, ctypes.c_long]
+        L.abl_server_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int),
+                                       ctypes.POINTER(ctypes.c_int),
+                                       ctypes.POINTER(ctypes.c_size_t)]
+        L.abl_server_destroy.argtypes = [vp]
+        self.s = ctypes.c_void_p()
+        _check(L.abl_server_create(slots, hbm_budget, ctypes.byref(self.s)), "abl_server_create")
+        self.models = {}
+
+    def submit(self, model, globals_, state, timesteps, seed=0):
+        """`state`: {type name: {member: array}}; returns the job id."""
+        model = model if isinstance(model, Model) else Model(model)
+        self.models_for = getattr(self, "models_for", {})
+        keep = []
+        counts = np.zeros(len(model.agent_types), np.uint64)
+        per_type = []
+        for t, (tname, members) in enumerate(model.agent_types):
+            st = state.get(tname, {})
+            n = len(st[members[0][0]]) if st else 0
+            counts[t] = n
+            ptrs = []
+            for nm, vt in members:
+                dt, shape = member_dtype(vt, model.float_bytes)
+                a = np.ascontiguousarray(st[nm], dtype=dt) if n else np.zeros((1,) + shape, dt)
+                keep.append(a)
+                ptrs.append(a.ctypes.data)
+            arr = (ctypes.c_void_p * len(ptrs))(*ptrs)
+            keep.append(arr)
+            per_type.append(ctypes.cast(arr, ctypes.c_void_p).value)
+        tarr = (ctypes.c_void_p * len(per_type))(*per_type)
+        jd = _JobDesc(model.ptr, ctypes.addressof(globals_.buf), int(seed), int(timesteps),
+                      counts.ctypes.data, ctypes.cast(tarr, ctypes.c_void_p).value)
+        jid = ctypes.c_long()
+        _check(_load().abl_server_submit(self.s, ctypes.byref(jd), ctypes.byref(jid)),
+               "abl_server_submit")
+        self.models_for[jid.value] = model
+        return jid.value
+
+    def wait(self, job_id, timeout=600.0):
+        _check(_load().abl_server_wait(self.s, job_id, timeout), "abl_server_wait")
+
+    def info(self, job_id):
+        st = ctypes.c_int()
+        t = (ctypes.c_double * 4)()
+        _check(_load().abl_server_job_info(self.s, job_id, ctypes.byref(st), t), "job_info")
+        return {"status": st.value, "submit": t[0], "admit": t[1], "done": t[2],
+                "exec_s": t[3]}
+
+    def result(self, job_id):
+        model = self.models_for[job_id]
+        out = {}
+        for t, (tname, members) in enumerate(model.agent_types):
+            n = ctypes.c_size_t(0)
+            _check(_load().abl_server_result(self.s, job_id, t, None, ctypes.byref(n)), "result")
+            cols = {}
+            for nm, vt in members:
+                dt, shape = member_dtype(vt, model.float_bytes)
+                cols[nm] = np.empty((n.value,) + shape, dt)
+            arr = (ctypes.c_void_p * len(members))(*[cols[nm].ctypes.data for nm, _ in members])
+            _check(_load().abl_server_result(self.s, job_id, t, arr, ctypes.byref(n)), "result")
+            out[tname] = cols
+        return out
+
+    def release(self, job_id):
+        _check(_load().abl_server_release(self.s, job_id), "release")
+
+    def close(self):
+        if self.s:
+            _load().abl_server_destroy(self.s)
+            self.s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

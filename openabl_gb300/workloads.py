@@ -87,3 +87,75 @@ def boids2d_ensemble(model, base_globals, replicas=256, n_min=1000, n_max=200000
         globals_list.append(g)
         states.append(boids2d(n, max_pos, seed=int(seeds[r] % (2**31))))
     return globals_list, states, seeds
+
+
+def _g6(x):
+    """A folded constant as the compiler prints it: six significant digits."""
+    return float("%g" % x)
+
+
+def served_job(model_name, n, precision, seed):
+    """Globals and initial state for one served job of `n` agents.
+
+    The derived globals are the ones the compiler folds for
+    `-P num_agents=n` (in double, the `param float` densities dividing as
+    floats; results printed to six significant digits -- checked against the
+    compiler's own output in tests/test_library_cpu.py):
+      circle, circle3d   W = sqrt / cbrt(n / rho) with the file's rho = 0.05
+      boids2d            max_pos = sqrt(n / agent_density), agent_density = 3200.0
+      predator_prey      env_size = sqrt(n / 1600) * SPACE_MULT; prey and
+                         predator fractions 0.4 and 0.1.
+    """
+    import math
+    from . import runtime as R
+    name = model_name + ("_float" if precision == "fp32" else "")
+    model = R.Model(name)
+    g = model.default_globals()
+    fd = np.float32 if model.float_bytes == 4 else np.float64
+    if model_name in ("circle", "circle3d"):
+        w = _g6(math.sqrt(n / 0.05) if model_name == "circle" else (n / 0.05) ** (1.0 / 3.0))
+        g.set("num_agents", n)
+        g.set("W", w)
+        st = circle(n, w, dim=2 if model_name == "circle" else 3, seed=seed)
+        state = {"Point": {"pos": st["pos"].astype(fd)}}
+    elif model_name == "boids2d":
+        mp = _g6(math.sqrt(n / 3200.0))
+        g.set("num_agents", n)
+        g.set("agent_density", 3200.0)
+        g.set("max_pos", mp)
+        st = boids2d(n, mp, seed=seed)
+        state = {"Boid": {k: v.astype(fd) for k, v in st.items()}}
+    elif model_name == "predator_prey":
+        env = _g6(math.sqrt(n / 1600.0) * 1.0)
+        g.set("num_agents", n)
+        g.set("prey_fraction", 0.4)
+        g.set("predator_fraction", 0.1)
+        g.set("env_size", env)
+        n_pred, n_prey = int(0.1 * n), int(0.4 * n)
+        st = predator_prey(n_pred, n_prey, n - n_pred - n_prey, env, seed=seed)
+        state = {t: {k: (v.astype(fd) if v.dtype.kind == "f" else v) for k, v in d.items()}
+                 for t, d in st.items()}
+    else:
+        raise KeyError(model_name)
+    return model, g, state
+
+
+def serving_stream(jobs=100, rate=200.0, n_min=1000, n_max=1000000, steps_min=50,
+                   steps_max=1000, seed=0,
+                   models=("circle", "circle3d", "boids2d", "predator_prey")):
+    """A Poisson stream of jobs: (arrival time, model, agents, timesteps,
+    precision, seed), agents log-uniform in [n_min, n_max], timesteps uniform
+    in [steps_min, steps_max], FP32/FP64 with equal probability."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    out = []
+    for k in range(jobs):
+        t += rng.exponential(1.0 / rate)
+        m = models[int(rng.integers(0, len(models)))]
+        n = int(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        if m == "predator_prey":
+            n = max(n, 1600)
+        steps = int(rng.integers(steps_min, steps_max + 1))
+        prec = "fp32" if rng.uniform() < 0.5 else "fp64"
+        out.append((t, m, n, steps, prec, int(rng.integers(0, 2**31))))
+    return out

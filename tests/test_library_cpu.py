@@ -52,3 +52,17 @@ def test_config_globals_are_the_printed_constants():
     assert g.get("num_agents") == 1048576
     _, g = o.globals_for_config("circle_4000")
     assert g.get("W") == 200.0
+
+
+def test_served_job_globals_match_compiler_folding():
+    """The serving helper derives per-job globals the way the compiler folds
+    them; configs.json holds what the compiler printed for these -P values."""
+    import openabl_gb300 as o
+    from openabl_gb300 import workloads
+    cfg = o.configs()
+    for name, key in [("boids2d_1m", "max_pos"), ("boids2d_4096", "max_pos"),
+                      ("predator_prey_1m", "env_size"), ("predator_prey_small", "env_size")]:
+        c = cfg[name]
+        n = int(c["globals"]["num_agents"])
+        _, g, _ = workloads.served_job(c["model"].replace("_float", ""), n, "fp64", 0)
+        assert g.get(key) == float(c["globals"][key]), name
