@@ -164,6 +164,24 @@ __global__ void k_bin_scatter(long n, const int *cell_of, const int *local_rank,
   order[cell_start[cell_of[i]] + local_rank[i]] = (int) i;
 }
 
+// Sorts every cell's run of slots by agent id (one thread per cell,
+// insertion sort: runs are short).  Together with the counting-sort scatter
+// this gives the slot order sorted by (cell, agent id), deterministic.
+__global__ void k_cell_sort(long ncells, const int *cell_start, int *order) {
+  long c = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  int s = cell_start[c], e = cell_start[c + 1];
+  for (int i = s + 1; i < e; i++) {
+    int v = order[i];
+    int j = i - 1;
+    while (j >= s && order[j] > v) {
+      order[j + 1] = order[j];
+      j--;
+    }
+    order[j + 1] = v;
+  }
+}
+
 // Largest |coordinate| of a type that is not binned (query side only).
 template <typename Real, int DIM>
 __global__ void k_amax(const Real *pos, long n, float *amax, int *error) {
@@ -299,14 +317,29 @@ __global__ void k_nb_count(int nx, int ny, int nz, int R, const int *cell_start,
   nb_cnt[c] = cnt;
 }
 
-// Per cell (one warp each): the candidate slots sorted by agent id.  Up to
-// kListCap candidates are ranked in shared memory; larger neighbourhoods are
-// ranked straight from global memory (same result, slower).
+// Per cell (one warp each): the candidate slots of the surrounding cells in
+// ascending agent id.  Up to kListCap candidates are staged in shared memory
+// and ranked by counting smaller ids; in larger neighbourhoods an element's
+// place is its position in its own run (runs are id-sorted, k_cell_sort)
+// plus, for every other run, a binary search for the ids below its own.
+constexpr int kMaxRuns = 125;
+
+__device__ inline int lower_bound_ids(const int *a, int len, int id) {
+  int lo = 0, hi = len;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < id) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
 template <int DIM>
 __global__ void k_nb_build(int nx, int ny, int nz, int R, const int *cell_start,
                            const int *order, const int *nb_off, int *nb_list) {
   __shared__ int s_id[kListWarpsPerBlock][kListCap];
-  __shared__ int s_slot[kListWarpsPerBlock][kListCap];
+  __shared__ int s_run[kListWarpsPerBlock][kMaxRuns + 1];   // run begin within the list
+  __shared__ int s_slot0[kListWarpsPerBlock][kMaxRuns];     // first slot of each run
   int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   long c = (long) blockIdx.x * kListWarpsPerBlock + w;
   long ncells = (long) nx * ny * nz;
@@ -318,52 +351,56 @@ __global__ void k_nb_build(int nx, int ny, int nz, int R, const int *cell_start,
   int x0 = max(cx - R, 0), x1 = min(cx + R, nx - 1);
   int z0 = DIM == 3 ? max(cz - R, 0) : 0, z1 = DIM == 3 ? min(cz + R, nz - 1) : 0;
   int y0 = max(cy - R, 0), y1 = min(cy + R, ny - 1);
-  if (count <= kListCap) {
-    int k = 0;
-    for (int z = z0; z <= z1; z++) {
-      for (int y = y0; y <= y1; y++) {
-        long rb = ((long) z * ny + y) * nx;
-        int s = cell_start[rb + x0], e = cell_start[rb + x1 + 1];
-        for (int j = lane; j < e - s; j += 32) {
-          s_id[w][k + j] = order[s + j];
-          s_slot[w][k + j] = s + j;
+  // Runs in (z, y, x) order, each one cell.
+  int nruns = 0, k = 0;
+  for (int z = z0; z <= z1; z++) {
+    for (int y = y0; y <= y1; y++) {
+      long rb = ((long) z * ny + y) * nx;
+      for (int x = x0; x <= x1; x++) {
+        int s = cell_start[rb + x], e = cell_start[rb + x + 1];
+        if (lane == 0) {
+          s_run[w][nruns] = k;
+          s_slot0[w][nruns] = s;
+        }
+        if (count <= kListCap) {
+          for (int j = lane; j < e - s; j += 32) s_id[w][k + j] = order[s + j];
         }
         k += e - s;
+        nruns++;
       }
     }
-    __syncwarp();
+  }
+  if (lane == 0) s_run[w][nruns] = k;
+  __syncwarp();
+  if (count <= kListCap) {
+    // Small neighbourhoods: rank by counting smaller ids (independent
+    // shared-memory reads, no dependence on the runs being sorted).
     for (int e = lane; e < count; e += 32) {
+      int j = 0;
+      while (s_run[w][j + 1] <= e) j++;
+      int slot = s_slot0[w][j] + (e - s_run[w][j]);
       int id = s_id[w][e];
-      int r = 0;
-      for (int f = 0; f < count; f++) r += s_id[w][f] < id;
-      nb_list[base_out + r] = s_slot[w][e];
+      int rank = 0;
+      for (int f = 0; f < count; f++) rank += s_id[w][f] < id;
+      nb_list[base_out + rank] = slot;
     }
     return;
   }
-  // Large neighbourhood: element e is addressed by walking the rows.
+  // Large neighbourhoods: position in the own (sorted) run plus a binary
+  // search in every other run.
   for (int e = lane; e < count; e += 32) {
-    int se = -1, k = 0;
-    for (int z = z0; z <= z1 && se < 0; z++) {
-      for (int y = y0; y <= y1; y++) {
-        long rb = ((long) z * ny + y) * nx;
-        int s = cell_start[rb + x0], len = cell_start[rb + x1 + 1] - s;
-        if (e < k + len) {
-          se = s + (e - k);
-          break;
-        }
-        k += len;
-      }
+    int j = 0;
+    while (s_run[w][j + 1] <= e) j++;
+    int p = e - s_run[w][j];
+    int slot = s_slot0[w][j] + p;
+    int id = order[slot];
+    int rank = p;
+    for (int q = 0; q < nruns; q++) {
+      if (q == j) continue;
+      int len = s_run[w][q + 1] - s_run[w][q];
+      if (len > 0) rank += lower_bound_ids(order + s_slot0[w][q], len, id);
     }
-    int id = order[se];
-    int r = 0;
-    for (int z = z0; z <= z1; z++) {
-      for (int y = y0; y <= y1; y++) {
-        long rb = ((long) z * ny + y) * nx;
-        int s = cell_start[rb + x0], e2 = cell_start[rb + x1 + 1];
-        for (int j = s; j < e2; j++) r += order[j] < id;
-      }
-    }
-    nb_list[base_out + r] = se;
+    nb_list[base_out + rank] = slot;
   }
 }
 
@@ -629,6 +666,7 @@ int prepare(abl_ctx *ctx) {
     if (t.ordered) {
       long span = 2 * t.R + 1;
       long per_agent = dim == 3 ? span * span * span : span * span;
+      if (per_agent > kMaxRuns) return ABL_E_UNSUPPORTED;  // cells far finer than the radius
       ABL_TRY(dev_alloc_t(ctx, &t.nb_cnt, t.ncells, own));
       ABL_TRY(dev_alloc_t(ctx, &t.nb_off, t.ncells + 1, own));
       ABL_TRY(dev_alloc_t(ctx, &t.nb_list, per_agent * n, own));
@@ -835,6 +873,8 @@ void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
   ctx->launches++;
   scan_run(ctx, t.cell_scan, t.cell_count, t.cell_start);
   k_bin_scatter<<<nb, B, 0, s>>>(t.n, t.cell_of, t.local_rank, t.cell_start, t.order);
+  ctx->launches++;
+  k_cell_sort<<<blocks_for(t.ncells, B), B, 0, s>>>(t.ncells, t.cell_start, t.order);
   ctx->launches++;
   GatherArgs g;
   std::memset(&g, 0, sizeof g);
@@ -1661,6 +1701,7 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
     if (ok && t.ordered) {
       long span = 2 * t.R + 1;
       long per_agent = dim == 3 ? span * span * span : span * span;
+      if (per_agent > kMaxRuns) return ABL_E_UNSUPPORTED;
       t.nb_cnt = b.take<int>(t.ncells);
       t.nb_off = b.take<int>(t.ncells + 1);
       t.nb_list = b.take<int>(per_agent * nn);

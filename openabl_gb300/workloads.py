@@ -101,7 +101,9 @@ def served_job(model_name, n, precision, seed):
     `-P num_agents=n` (in double, the `param float` densities dividing as
     floats; results printed to six significant digits -- checked against the
     compiler's own output in tests/test_library_cpu.py):
-      circle, circle3d   W = sqrt / cbrt(n / rho) with the file's rho = 0.05
+      circle             W = sqrt(n / rho) with the file's rho = 0.05
+      circle3d           W = cbrt(n / rho) with rho = 0.01 (the file's 0.05 puts
+                         ~200 agents inside every interaction sphere)
       boids2d            max_pos = sqrt(n / agent_density), agent_density = 3200.0
       predator_prey      env_size = sqrt(n / 1600) * SPACE_MULT; prey and
                          predator fractions 0.4 and 0.1.
@@ -113,7 +115,9 @@ def served_job(model_name, n, precision, seed):
     g = model.default_globals()
     fd = np.float32 if model.float_bytes == 4 else np.float64
     if model_name in ("circle", "circle3d"):
-        w = _g6(math.sqrt(n / 0.05) if model_name == "circle" else (n / 0.05) ** (1.0 / 3.0))
+        rho = 0.05 if model_name == "circle" else 0.01
+        w = _g6(math.sqrt(n / rho) if model_name == "circle" else float(np.cbrt(n / rho)))
+        g.set("rho", rho)
         g.set("num_agents", n)
         g.set("W", w)
         st = circle(n, w, dim=2 if model_name == "circle" else 3, seed=seed)
