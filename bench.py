@@ -229,6 +229,70 @@ def measure_serving(args, o, W, np):
             "makespan_s": last - first, "jobs": len(ids), "failed": failed}
 
 
+def measure_other_workloads(args, o, W, np):
+    """The other hot-path configurations: circle 4,000 agents (the reference's
+    CPU-sized case), game_of_life 4096 x 4096 with 50% alive, and
+    predator_prey with 800,000 prey + 200,000 predators (+ 1,000,000 grass)
+    for 500 timesteps in FP64 and FP32."""
+    import sys as _sys
+    _sys.path.insert(0, os.path.join(REPO, "tests"))
+    out = {}
+    # circle, 4000 agents, 100 timesteps (reference init from the golden case)
+    from golden_io import load_case
+    meta, st = load_case("circle_4000")
+    model, g = o.globals_for_config("circle_4000")
+    sim = o.Simulation(model, g)
+    sim.upload("Point", st)
+    sim.run(3)
+    sim.upload("Point", st)
+    sim.run(100)
+    out["circle_4000"] = {"value": 4000 * 100 / sim.last_exec_time(), "unit": "agent-steps/s",
+                          "ms_per_step": sim.last_exec_time() * 10.0}
+    sim.close()
+    # game of life 4096^2, 50% live, 100 timesteps
+    model, g = o.globals_for_config("game_of_life_4096")
+    st = W.game_of_life(g.get("size"), 0.5, seed=0)
+    sim = o.Simulation(model, g)
+    sim.upload("Cell", st)
+    sim.run(3)
+    sim.upload("Cell", st)
+    sim.run(100)
+    n = len(st["alive"])
+    out["game_of_life_4096"] = {"value": n * 100 / sim.last_exec_time(), "unit": "agent-steps/s",
+                                "ms_per_step": sim.last_exec_time() * 10.0}
+    sim.close()
+    # predator_prey, 500 timesteps, FP64 and FP32
+    from pp_setup import case
+    cfg, st, consts = case("predator_prey_1m")
+    res = {}
+    for name in ("predator_prey", "predator_prey_float"):
+        model = o.Model(name)
+        g = model.default_globals().update(cfg["globals"])
+        sim = o.Simulation(model, g)
+        sim.set_seed(1)
+        fd = np.float32 if model.float_bytes == 4 else np.float64
+        for t, cols in st.items():
+            sim.upload(t, {k: (v.astype(fd) if v.dtype.kind == "f" else v)
+                           for k, v in cols.items()})
+        sim.run(500)
+        rows = [list(map(float, r.split(","))) for r in sim.log_text().strip().splitlines()]
+        agents = sum(r[0] + r[1] for r in rows) + 1e6 * len(rows)  # prey + predators + grass
+        res[name] = {"seconds": sim.last_exec_time(), "rows": rows}
+        out[name + "_1m"] = {"value": agents / sim.last_exec_time(), "unit": "agent-steps/s",
+                             "ms_per_step": sim.last_exec_time() * 2.0,
+                             "final_prey": rows[-1][0], "final_predators": rows[-1][1],
+                             "final_grass_available": rows[-1][2]}
+        sim.close()
+    a = np.array(res["predator_prey"]["rows"])[:, :3]
+    b = np.array(res["predator_prey_float"]["rows"])[:, :3]
+    rel = np.abs(a - b) / np.maximum(a, 1)
+    out["predator_prey_fp32_vs_fp64"] = {
+        "metric": "relative difference of the per-timestep counts (prey, predators, available "
+                  "grass) between the FP32 and FP64 runs",
+        "max_at_step_100": float(rel[:100].max()), "max_over_500": float(rel.max())}
+    return out
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -366,6 +430,7 @@ def run_ours(args):
         forms["ensemble"] = measure_ensemble(args, o, W, np)
         forms["precision"] = measure_precision(args, o, W, np)
         forms["serving"] = measure_serving(args, o, W, np)
+        forms["other_workloads"] = measure_other_workloads(args, o, W, np)
 
     cpu = None
     if rank == 0:

@@ -474,6 +474,11 @@ struct abl_ctx {
   };
   std::vector<Graph> graphs;
   bool prepared = false;
+  // One uniform grid per (neighbour type, cell size): every near loop bins
+  // its neighbour type with cells just wider than its own radius.
+  std::vector<TypeState> grids;
+  std::vector<int> grid_type;  // grid -> agent type
+  std::vector<int> step_grid;  // step function -> grid (-1: no near loop)
   std::vector<StepState> step_state;
   std::vector<void *> step_allocs;
   uint64_t seed = 0;
@@ -595,9 +600,11 @@ void free_bins(abl_ctx *ctx, TypeState &t) {
   for (auto &g : t.gcols) g = nullptr;
 }
 
-// Sizes the grid of every neighbour type from the environment and the
-// granularity (src/AnalysisVisitor.cpp:1378-1399: explicit, or the largest
-// constant near radius) and allocates the binning buffers.
+// Sizes one grid per (neighbour type, cell size) -- the cells of a near
+// loop's grid are just wider than the loop's radius, so each loop scans ~9
+// (2D) or ~27 (3D) cells' worth of its radius, whatever the environment
+// granularity (src/AnalysisVisitor.cpp:1378-1399, which only partitions
+// space and does not change results) -- and allocates the binning buffers.
 int prepare(abl_ctx *ctx) {
   const abl_model_desc *m = ctx->model;
   const void *G = ctx->globals.data();
@@ -605,74 +612,110 @@ int prepare(abl_ctx *ctx) {
   if (m->env_bounds) m->env_bounds(G, emin, emax);
   for (int ti = 0; ti < m->num_agent_types; ti++) {
     TypeState &t = ctx->types[ti];
-    free_bins(ctx, t);
-    t.is_near = false;
-    t.ordered = false;
-    t.gather_mask = 0;
-    for (int k = 0; k < m->num_steps; k++) {
-      const abl_step_desc &sd = m->steps[k];
-      if (sd.near_type != ti) continue;
-      t.is_near = true;
-      t.ordered = t.ordered || sd.ordered;
-      t.gather_mask |= sd.near_members;
-    }
     if (!t.amax) ABL_TRY(dev_alloc_t(ctx, &t.amax, 1));
-    if (!t.is_near) continue;
-    if (t.d->position_member < 0) return ABL_E_UNSUPPORTED;
-    int dim = t.d->dim;
-    double gran = m->granularity ? m->granularity(G) : max_radius_for(ctx, ti);
-    double rmax = max_radius_for(ctx, ti);
-    if (!(gran > 0.0) || !std::isfinite(gran)) return ABL_E_INVALID;
-    // Cells slightly wider than the granularity: a pair that passes the
+  }
+  for (TypeState &g : ctx->grids) free_bins(ctx, g);
+  ctx->grids.clear();
+  ctx->grid_type.clear();
+  ctx->step_grid.assign(m->num_steps, -1);
+  std::vector<double> grid_cell;
+  for (int k = 0; k < m->num_steps; k++) {
+    const abl_step_desc &sd = m->steps[k];
+    if (sd.near_type < 0) continue;
+    int ti = sd.near_type;
+    if (ctx->types[ti].d->position_member < 0) return ABL_E_UNSUPPORTED;
+    double r = sd.radius ? sd.radius(G) : 0.0;
+    if (!(r > 0.0) || !std::isfinite(r)) {
+      // A radius that is not a positive number: one cell per axis unit of the
+      // granularity (every candidate then takes the exact test).
+      r = m->granularity ? m->granularity(G) : max_radius_for(ctx, ti);
+    }
+    if (!(r > 0.0) || !std::isfinite(r)) return ABL_E_INVALID;
+    // Cells slightly wider than the radius: a pair that passes the
     // float-rounded radius test lies within one cell width (see
     // abl_device.cuh), with room for rounding in the cell computation.
-    double cell = gran * (1.0 + 1.0 / 1024.0);
-    t.R = std::max(1, (int) std::ceil(rmax * (1.0 + 1e-6) / cell));
-    t.inv_cell = 1.0 / cell;
+    double cell = r * (1.0 + 1.0 / 1024.0);
+    int gi = -1;
+    for (size_t q = 0; q < ctx->grids.size(); q++) {
+      if (ctx->grid_type[q] == ti && grid_cell[q] == cell) gi = (int) q;
+    }
+    if (gi < 0) {
+      gi = (int) ctx->grids.size();
+      ctx->grids.emplace_back();
+      ctx->grid_type.push_back(ti);
+      grid_cell.push_back(cell);
+      TypeState &g = ctx->grids.back();
+      g.d = ctx->types[ti].d;
+      g.is_near = true;
+    }
+    TypeState &g = ctx->grids[gi];
+    g.ordered = g.ordered || sd.ordered;
+    g.gather_mask |= sd.near_members;
+    ctx->step_grid[k] = gi;
+  }
+  for (size_t gi = 0; gi < ctx->grids.size(); gi++) {
+    TypeState &g = ctx->grids[gi];
+    const TypeState &t = ctx->types[ctx->grid_type[gi]];
+    int dim = g.d->dim;
+    double cell = grid_cell[gi];
+    // At most ~2 cells per agent: scans and list building cost per cell, and
+    // finer cells than that stop reducing the candidates worth visiting.
+    {
+      double max_cells = std::max(4096.0, 2.0 * (double) std::max(t.n, t.cap));
+      double vol = 1.0;
+      for (int d = 0; d < dim; d++) vol *= std::max(emax[d] - emin[d], cell);
+      double cells = vol / std::pow(cell, dim);
+      if (cells > max_cells && std::isfinite(vol)) cell = std::pow(vol / max_cells, 1.0 / dim);
+    }
+    g.inv_cell = 1.0 / cell;
+    g.R = 1;
     int dims[3] = {1, 1, 1};
     for (int d = 0; d < 3; d++) {
       if (d < dim) {
         double ext = emax[d] - emin[d];
         if (!(ext >= 0.0) || !std::isfinite(ext)) return ABL_E_INVALID;
-        double k = std::floor(ext * t.inv_cell) + 1.0;
+        double k = std::floor(ext * g.inv_cell) + 1.0;
         if (k > 1 << 24) return ABL_E_UNSUPPORTED;
         dims[d] = (int) k;
-        t.lo[d] = emin[d];
+        g.lo[d] = emin[d];
       } else {
-        t.lo[d] = 0.0;
+        g.lo[d] = 0.0;
       }
     }
-    t.nx = dims[0];
-    t.ny = dims[1];
-    t.nz = dims[2];
-    t.ncells = (long) t.nx * t.ny * t.nz;
-    if (t.ncells > (1L << 30)) return ABL_E_UNSUPPORTED;
+    g.nx = dims[0];
+    g.ny = dims[1];
+    g.nz = dims[2];
+    g.ncells = (long) g.nx * g.ny * g.nz;
+    if (g.ncells > (1L << 30)) return ABL_E_UNSUPPORTED;
+    g.n = t.n;
+    g.cap = t.cap;
     long n = std::max<long>(std::max(t.n, t.cap), 1);
-    auto *own = &t.bin_allocs;
-    ABL_TRY(dev_alloc_t(ctx, &t.cell_count, t.ncells, own));
-    ABL_TRY(dev_alloc_t(ctx, &t.cell_start, t.ncells + 1, own));
-    ABL_TRY(dev_alloc_t(ctx, &t.local_rank, n, own));
-    ABL_TRY(dev_alloc_t(ctx, &t.cell_of, n, own));
-    ABL_TRY(dev_alloc_t(ctx, &t.order, n, own));
-    ABL_TRY(dev_alloc_t(ctx, &t.posf, n * dim, own));
-    ABL_TRY(scan_plan(ctx, t.cell_scan, t.ncells, own));
-    for (int k = 0; k < t.d->num_members; k++) {
-      if (t.gather_mask & (1u << k)) {
+    auto *own = &g.bin_allocs;
+    ABL_TRY(dev_alloc_t(ctx, &g.amax, 1, own));
+    ABL_TRY(dev_alloc_t(ctx, &g.cell_count, g.ncells, own));
+    ABL_TRY(dev_alloc_t(ctx, &g.cell_start, g.ncells + 1, own));
+    ABL_TRY(dev_alloc_t(ctx, &g.local_rank, n, own));
+    ABL_TRY(dev_alloc_t(ctx, &g.cell_of, n, own));
+    ABL_TRY(dev_alloc_t(ctx, &g.order, n, own));
+    ABL_TRY(dev_alloc_t(ctx, &g.posf, n * dim, own));
+    ABL_TRY(scan_plan(ctx, g.cell_scan, g.ncells, own));
+    for (int k = 0; k < g.d->num_members; k++) {
+      if (g.gather_mask & (1u << k)) {
         void *p = nullptr;
-        ABL_TRY(dev_alloc(ctx, &p, member_bytes(t.d->members[k]) * n, own));
-        t.gcols[k] = p;
+        ABL_TRY(dev_alloc(ctx, &p, member_bytes(g.d->members[k]) * n, own));
+        g.gcols[k] = p;
       }
     }
-    if (t.ordered) {
-      long span = 2 * t.R + 1;
+    if (g.ordered) {
+      long span = 2 * g.R + 1;
       long per_agent = dim == 3 ? span * span * span : span * span;
-      if (per_agent > kMaxRuns) return ABL_E_UNSUPPORTED;  // cells far finer than the radius
-      ABL_TRY(dev_alloc_t(ctx, &t.nb_cnt, t.ncells, own));
-      ABL_TRY(dev_alloc_t(ctx, &t.nb_off, t.ncells + 1, own));
-      ABL_TRY(dev_alloc_t(ctx, &t.nb_list, per_agent * n, own));
-      ABL_TRY(scan_plan(ctx, t.nb_scan, t.ncells, own));
+      if (per_agent > kMaxRuns) return ABL_E_UNSUPPORTED;
+      ABL_TRY(dev_alloc_t(ctx, &g.nb_cnt, g.ncells, own));
+      ABL_TRY(dev_alloc_t(ctx, &g.nb_off, g.ncells + 1, own));
+      ABL_TRY(dev_alloc_t(ctx, &g.nb_list, per_agent * n, own));
+      ABL_TRY(scan_plan(ctx, g.nb_scan, g.ncells, own));
     }
-    t.dirty = true;
+    g.dirty = true;
   }
   if (!ctx->amax_pair) ABL_TRY(dev_alloc_t(ctx, &ctx->amax_pair, 1));
   if (!ctx->d_pair) ABL_TRY(dev_alloc_t(ctx, &ctx->d_pair, 2));
@@ -792,6 +835,8 @@ MoveArgs move_args(const abl_agent_desc &d, void *const *src, void *const *dst) 
   return a;
 }
 
+void mark_dirty(abl_ctx *ctx, int ti);
+
 // After a step function that removes or adds agents: stable compaction of
 // the survivors, then the children appended in parent order.  The step's
 // result is in the buffer it wrote (cols[1 - cur]).  Returns with `regrow`
@@ -847,9 +892,9 @@ int apply_population_changes(abl_ctx *ctx, int k, bool &regrow) {
     k_scatter_flagged<<<nb, B, 0, s>>>(n, st.child, st.child_pos, t2.n, c);
     ctx->launches++;
     t2.n = need;
-    t2.dirty = true;
+    mark_dirty(ctx, sd.add_type);
   }
-  t.dirty = true;
+  mark_dirty(ctx, sd.agent_type);
   return ABL_OK;
 }
 
@@ -922,6 +967,25 @@ void bin_type(abl_ctx *ctx, TypeState &t) {
   t.dirty = false;
 }
 
+// Bins the current population of a grid's agent type.
+void bin_grid(abl_ctx *ctx, int gi) {
+  TypeState &g = ctx->grids[gi];
+  const TypeState &t = ctx->types[ctx->grid_type[gi]];
+  for (int b = 0; b < 2; b++)
+    for (int k = 0; k < ABL_MAX_MEMBERS; k++) g.cols[b][k] = t.cols[b][k];
+  g.cur = t.cur;
+  g.n = t.n;
+  bin_type(ctx, g);
+}
+
+// The population of type ti changed: every grid of it must be rebuilt.
+void mark_dirty(abl_ctx *ctx, int ti) {
+  ctx->types[ti].dirty = true;
+  for (size_t gi = 0; gi < ctx->grids.size(); gi++) {
+    if (ctx->grid_type[gi] == ti) ctx->grids[gi].dirty = true;
+  }
+}
+
 void type_amax(abl_ctx *ctx, TypeState &t) {
   cudaStream_t s = ctx->stream;
   const int B = 256;
@@ -967,8 +1031,9 @@ int step_once(abl_ctx *ctx) {
       L.out_cols[j] = t.cols[1 - t.cur][j];
     }
     if (sd.near_type >= 0) {
-      TypeState &nt = ctx->types[sd.near_type];
-      if (nt.dirty) bin_type(ctx, nt);
+      int gi = ctx->step_grid[k];
+      if (ctx->grids[gi].dirty) bin_grid(ctx, gi);
+      TypeState &nt = ctx->grids[gi];
       abl_near_view &V = L.near;
       V.dim = nt.d->dim;
       V.ordered = sd.ordered;
@@ -1023,7 +1088,7 @@ int step_once(abl_ctx *ctx) {
       if (regrow) ABL_TRY(prepare(ctx));
     } else {
       t.cur = 1 - t.cur;  // swap agents_X and agents_X_dbuf
-      t.dirty = true;
+      mark_dirty(ctx, sd.agent_type);
     }
   }
   ctx->timestep++;
@@ -1075,6 +1140,7 @@ std::vector<int> graph_key(const abl_ctx *ctx) {
     key.push_back(t.cur);
     key.push_back(t.dirty ? 1 : 0);
   }
+  for (const TypeState &g : ctx->grids) key.push_back(g.dirty ? 1 : 0);
   return key;
 }
 
@@ -1126,6 +1192,9 @@ int capture_graph(abl_ctx *ctx, abl_ctx::Graph **out) {
   for (size_t k = 0; k < ctx->types.size(); k++) {
     ctx->types[k].cur = key[2 * k];
     ctx->types[k].dirty = key[2 * k + 1] != 0;
+  }
+  for (size_t q = 0; q < ctx->grids.size(); q++) {
+    ctx->grids[q].dirty = key[2 * ctx->types.size() + q] != 0;
   }
   ctx->graphs.push_back(G);
   *out = &ctx->graphs.back();
@@ -1276,7 +1345,7 @@ int abl_upload(abl_ctx *ctx, int type_id, const void *const *cols, size_t n) {
                                  ctx->stream));
   }
   t.uploaded = true;
-  t.dirty = true;
+  mark_dirty(ctx, type_id);
   if (resized) {
     ctx->prepared = false;
     drop_graph(ctx);
@@ -1625,6 +1694,11 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
     D.ctx->types.resize(1);
     D.ctx->types[0].cell_scan.levels.reserve(8);
     D.ctx->types[0].nb_scan.levels.reserve(8);
+    D.ctx->grids.resize(1);
+    D.ctx->grid_type.assign(1, 0);
+    D.ctx->step_grid.assign(1, -1);
+    D.ctx->grids[0].cell_scan.levels.reserve(8);
+    D.ctx->grids[0].nb_scan.levels.reserve(8);
     D.ready = true;
   }
   if (model->globals_size > D.ctx->globals.capacity()) return ABL_E_SCRATCH;
@@ -1648,64 +1722,74 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
   Bump b{D.scratch, 0, kNoAllocScratchBytes};
   ctx.error = b.take<int>(1);
   t.amax = b.take<float>(1);
+  ctx.grids[0].amax = b.take<float>(1);
 
-  // Grid of the neighbour type, as prepare() sizes it.
+  // Grid of the neighbour type, as prepare() sizes it (one grid, cells just
+  // wider than the near radius).
   const abl_step_desc &sd = model->steps[0];
-  t.is_near = sd.near_type == 0;
-  t.ordered = t.is_near && sd.ordered;
-  t.gather_mask = t.is_near ? sd.near_members : 0;
-  t.dirty = true;
-  if (t.is_near) {
+  ctx.step_grid[0] = sd.near_type == 0 ? 0 : -1;
+  ctx.grid_type[0] = 0;
+  TypeState &gb = ctx.grids[0];
+  gb.d = &ad;
+  gb.is_near = sd.near_type == 0;
+  gb.ordered = gb.is_near && sd.ordered;
+  gb.gather_mask = gb.is_near ? sd.near_members : 0;
+  gb.dirty = true;
+  gb.n = t.n;
+  gb.cap = t.n;
+  gb.cell_scan.levels.clear();
+  gb.nb_scan.levels.clear();
+  if (gb.is_near) {
     if (ad.position_member < 0) return ABL_E_UNSUPPORTED;
     int dim = ad.dim;
     double emin[3] = {0, 0, 0}, emax[3] = {0, 0, 0};
     if (model->env_bounds) model->env_bounds(G, emin, emax);
     double rmax = sd.radius ? sd.radius(G) : 0.0;
-    double gran = model->granularity ? model->granularity(G) : rmax;
-    if (!(gran > 0.0) || !std::isfinite(gran)) return ABL_E_INVALID;
-    double cell = gran * (1.0 + 1.0 / 1024.0);
-    t.R = std::max(1, (int) std::ceil(rmax * (1.0 + 1e-6) / cell));
-    t.inv_cell = 1.0 / cell;
+    if (!(rmax > 0.0) || !std::isfinite(rmax)) rmax = model->granularity ? model->granularity(G) : 0.0;
+    if (!(rmax > 0.0) || !std::isfinite(rmax)) return ABL_E_INVALID;
+    double cell = rmax * (1.0 + 1.0 / 1024.0);
+    gb.R = 1;
+    gb.inv_cell = 1.0 / cell;
     int dims[3] = {1, 1, 1};
     for (int d = 0; d < 3; d++) {
-      t.lo[d] = d < dim ? emin[d] : 0.0;
+      gb.lo[d] = d < dim ? emin[d] : 0.0;
       if (d < dim) {
         double ext = emax[d] - emin[d];
         if (!(ext >= 0.0) || !std::isfinite(ext)) return ABL_E_INVALID;
-        double k = std::floor(ext * t.inv_cell) + 1.0;
+        double k = std::floor(ext * gb.inv_cell) + 1.0;
         if (k > (double) kNoAllocMaxCells) return ABL_E_SCRATCH;
         dims[d] = (int) k;
       }
     }
-    t.nx = dims[0];
-    t.ny = dims[1];
-    t.nz = dims[2];
-    t.ncells = (long) t.nx * t.ny * t.nz;
-    if (t.ncells > kNoAllocMaxCells) return ABL_E_SCRATCH;
+    gb.nx = dims[0];
+    gb.ny = dims[1];
+    gb.nz = dims[2];
+    gb.ncells = (long) gb.nx * gb.ny * gb.nz;
+    if (gb.ncells > kNoAllocMaxCells) return ABL_E_SCRATCH;
     long nn = std::max<long>(t.n, 1);
-    t.cell_count = b.take<int>(t.ncells);
-    t.cell_start = b.take<int>(t.ncells + 1);
-    t.local_rank = b.take<int>(nn);
-    t.cell_of = b.take<int>(nn);
-    t.order = b.take<int>(nn);
-    t.posf = b.take<float>(nn * dim);
-    bool ok = t.cell_count && t.cell_start && t.local_rank && t.cell_of && t.order && t.posf
-              && scan_plan_static(t.cell_scan, t.ncells, b);
+    gb.cell_count = b.take<int>(gb.ncells);
+    gb.cell_start = b.take<int>(gb.ncells + 1);
+    gb.local_rank = b.take<int>(nn);
+    gb.cell_of = b.take<int>(nn);
+    gb.order = b.take<int>(nn);
+    gb.posf = b.take<float>(nn * dim);
+    bool ok = gb.cell_count && gb.cell_start && gb.local_rank && gb.cell_of && gb.order && gb.posf
+              && scan_plan_static(gb.cell_scan, gb.ncells, b);
     for (int k = 0; k < ad.num_members && ok; k++) {
-      t.gcols[k] = nullptr;
-      if (t.gather_mask & (1u << k)) {
-        t.gcols[k] = b.take<unsigned char>(member_bytes(ad.members[k]) * nn);
-        ok = t.gcols[k] != nullptr;
+      gb.gcols[k] = nullptr;
+      if (gb.gather_mask & (1u << k)) {
+        gb.gcols[k] = b.take<unsigned char>(member_bytes(ad.members[k]) * nn);
+        ok = gb.gcols[k] != nullptr;
       }
     }
-    if (ok && t.ordered) {
-      long span = 2 * t.R + 1;
+    if (ok && gb.ordered) {
+      long span = 2 * gb.R + 1;
       long per_agent = dim == 3 ? span * span * span : span * span;
       if (per_agent > kMaxRuns) return ABL_E_UNSUPPORTED;
-      t.nb_cnt = b.take<int>(t.ncells);
-      t.nb_off = b.take<int>(t.ncells + 1);
-      t.nb_list = b.take<int>(per_agent * nn);
-      ok = t.nb_cnt && t.nb_off && t.nb_list && scan_plan_static(t.nb_scan, t.ncells, b);
+      gb.nb_cnt = b.take<int>(gb.ncells);
+      gb.nb_off = b.take<int>(gb.ncells + 1);
+      gb.nb_list = b.take<int>(per_agent * nn);
+      ok = gb.nb_cnt && gb.nb_off && gb.nb_list && scan_plan_static(gb.nb_scan, gb.ncells, b);
     }
     if (!ok) return ABL_E_SCRATCH;
   }
