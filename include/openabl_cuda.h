@@ -131,6 +131,21 @@ int abl_last_launch_count(abl_ctx *ctx, long *launches);
  * timesteps only, so abl_run does not replay graphs while it is on). */
 int abl_set_profiling(abl_ctx *ctx, int enable);
 int abl_step_kernel_time(abl_ctx *ctx, int step, double *seconds, long *launches);
+/* Ordered near loops gather each block's neighbour lists in shared memory;
+ * with balancing on (the default) the block's agents are handed to its
+ * threads in order of neighbour count, so a warp's loops have similar
+ * lengths.  Results are identical either way. */
+int abl_set_balance(abl_ctx *ctx, int enable);
+/* How ordered near loops find their neighbours in ascending id: ABL_NEAR_AUTO
+ * (default) picks per step; RUNS sorts each agent's neighbours from the
+ * cells' own runs, ROWS (2D) merges three precomputed row lists, LISTS reads
+ * whole precomputed neighbourhood lists.  Results are identical in every
+ * mode; this is a tuning and testing control. */
+#define ABL_NEAR_AUTO 0
+#define ABL_NEAR_RUNS 1
+#define ABL_NEAR_ROWS 2
+#define ABL_NEAR_LISTS 3
+int abl_set_near_mode(abl_ctx *ctx, int mode);
 int abl_destroy(abl_ctx *ctx);
 const char *abl_strerror(int code);
 

@@ -384,13 +384,20 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   std::string posCol = "((const " + cType(posMember->type->resolved) + " *) abl_NB.cols["
                      + std::to_string(posIdx) + "])";
 
+  const bool presorted = fnKind == FnKind::STEP && !steps.empty() && steps.back().presorted;
+
   *this << "{" << indent << nl
         << "const abl::near_query<" << dim << "> " << q << "(abl_NB, (double) " << agentExpr
         << "->" << posMember->name << ".x, (double) " << agentExpr << "->" << posMember->name
         << ".y, " << (is3 ? "(double) " : "0.0");
   if (is3) *this << agentExpr << "->" << posMember->name << ".z";
-  *this << ");" << nl
-        << "abl::near_cursor<" << dim << "> " << c << "(abl_NB, " << q << ");" << nl
+  *this << ");" << nl;
+  if (presorted) {
+    *this << "abl::near_list_cursor<" << dim << "> " << c << "(abl_NB, " << q << ", abl_K);";
+  } else {
+    *this << "abl::near_cursor<" << dim << "> " << c << "(abl_NB, " << q << ");";
+  }
+  *this << nl
         << "auto " << ex << " = [&](int abl_s) -> bool {" << indent << nl
         << "const " << cType(posMember->type->resolved) << " abl_p = " << posCol << "[abl_s];"
         << nl << "return !(" << distFn << "(abl_p, " << agentExpr << "->" << posMember->name
@@ -541,6 +548,9 @@ void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
                            "the agent");
       }
     }
+    auto *center = dynamic_cast<const AST::VarExpression *>(&loop->getNearAgent());
+    info.presorted = info.ordered && c.nearLoops.size() == 1 && rc.calls.empty() && center
+                  && center->var->id == decl.stepParam().var->id;
   }
   // Members of `out` written by the function: any assignment rooted at
   // out.m may write it; a top-level `out.m = e` always does, provided `out`
@@ -590,6 +600,28 @@ void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
   printKernel(steps.back());
 }
 
+// Phase one of a presorted step kernel: this thread's agent (abl_i1, valid
+// when abl_has) gathers its sorted neighbour list and the block picks the
+// agent each thread runs (abl_j).  The radius test is the near loop's own.
+void CudaPrinter::printPresortPhase(const StepInfo &info, const std::string &view,
+                                    const std::string &pos) {
+  const AST::ForStatement &loop = *info.nearLoop;
+  AST::AgentDeclaration *nearAgent = loop.type->resolved.getAgentDecl();
+  AST::AgentMember *posMember = nearAgent->getPositionMember();
+  bool is3 = posMember->type->resolved == Type::VEC3;
+  int dim = is3 ? 3 : 2;
+  std::string pt = cType(posMember->type->resolved);
+  int posIdx = memberIndex(nearAgent, posMember);
+  *this << "const " << pt << " abl_p1 = abl_has ? " << pos << " : " << pt << "{};" << nl
+        << "const abl::near_query<" << dim << "> abl_q0(" << view
+        << ", (double) abl_p1.x, (double) abl_p1.y, " << (is3 ? "(double) abl_p1.z" : "0.0")
+        << ");" << nl << "auto abl_x0 = [&](int abl_s) -> bool {" << indent << nl
+        << "const " << pt << " abl_p = ((const " << pt << " *) " << view << ".cols[" << posIdx
+        << "])[abl_s];" << nl << "return !(" << (is3 ? "dist_float3" : "dist_float2")
+        << "(abl_p, abl_p1) > " << loop.getNearRadius() << ");" << outdent << nl << "};" << nl
+        << "abl_j = abl::presort_block<" << dim << ">(" << view << ", abl_has, abl_q0, abl_x0);";
+}
+
 void CudaPrinter::printKernel(const StepInfo &info) {
   const AST::FunctionDeclaration &decl = *info.decl;
   const AST::AgentDeclaration &agent = decl.stepAgent();
@@ -603,14 +635,28 @@ void CudaPrinter::printKernel(const StepInfo &info) {
         << "void *child_cols[ABL_MAX_MEMBERS];" << nl << "uint64_t seed;" << nl
         << "long timestep;" << nl << "int step_index;" << outdent << nl << "};"
         << nl << "__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_" << name
-        << "(const __grid_constant__ abl_kargs_" << name << " A) {" << indent << nl
-        << "const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl
-        << "if (abl_t >= A.n) return;" << nl
+        << "(const __grid_constant__ abl_kargs_" << name << " A) {" << indent << nl;
+  if (info.presorted) {
+    *this << "int abl_j;" << nl << "{" << indent << nl
+          << "const abl_globals &abl_G = A.G;" << nl
+          << "const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl
+          << "const bool abl_has = abl_t1 < A.n;" << nl
+          << "const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;"
+          << nl;
+    printPresortPhase(info, "A.NB", "A.in." + agent.getPositionMember()->name + "[abl_i1]");
+    *this << outdent << nl << "}" << nl
+          << "const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;" << nl;
+  } else {
+    *this << "const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl;
+  }
+  *this << "if (abl_t >= A.n) return;" << nl
         << "const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;" << nl
         << "abl::step_ctx abl_K;" << nl
         << "abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);"
         << nl << "abl_K.self = abl_i;" << nl << "abl_K.removed = 0;" << nl << "abl_K.added = 0;"
-        << nl << "abl_K.child_cols = A.child_cols;" << nl << T << " abl_in, abl_out;";
+        << nl << "abl_K.child_cols = A.child_cols;" << nl
+        << "abl_K.near_col = " << (info.presorted ? "abl_j" : "-1") << ";" << nl
+        << T << " abl_in, abl_out;";
   for (size_t k = 0; k < agent.members->size(); k++) {
     const std::string &m = (*agent.members)[k]->name;
     *this << nl << "abl_in." << m << " = A.in." << m << "[abl_i];";
@@ -657,7 +703,7 @@ void CudaPrinter::printKernel(const StepInfo &info) {
         << "const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : "
            "ABL_STEP_BLOCK;" << nl
         << "const long abl_grid = (A.n + abl_block - 1) / abl_block;" << nl
-        << "abl_kernel_" << name << "<<<abl_grid, abl_block, 0, abl_stream>>>(A);" << nl
+        << "abl_kernel_" << name << "<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);" << nl
         << "return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;" << outdent << nl
         << "}" << nl;
   if (info.addType < 0 && !info.usesRemove) {
@@ -665,9 +711,26 @@ void CudaPrinter::printKernel(const StepInfo &info) {
     // Random numbers are keyed by the replica's seed and the agent's index
     // within its replica, so each replica draws what it would draw alone.
     *this << "__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_" << name
-          << "(const __grid_constant__ abl_ens_launch A) {" << indent << nl
-          << "const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl
-          << "if (abl_t >= A.n) return;" << nl
+          << "(const __grid_constant__ abl_ens_launch A) {" << indent << nl;
+    if (info.presorted) {
+      int posIdx = memberIndex(&agent, agent.getPositionMember());
+      *this << "int abl_j;" << nl << "{" << indent << nl
+            << "const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl
+            << "const bool abl_has = abl_t1 < A.n;" << nl
+            << "const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] "
+               ": abl_t1) : 0;" << nl
+            << "const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;" << nl
+            << "const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];" << nl
+            << "const abl_near_view &abl_V1 = A.views[abl_r1];" << nl;
+      printPresortPhase(info, "abl_V1",
+                        "((const " + cType(agent.getPositionMember()->type->resolved)
+                            + " *) A.in_cols[" + std::to_string(posIdx) + "])[abl_i1]");
+      *this << outdent << nl << "}" << nl
+            << "const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;" << nl;
+    } else {
+      *this << "const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl;
+    }
+    *this << "if (abl_t >= A.n) return;" << nl
           << "const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;" << nl
           << "const int abl_r = A.replica[abl_i];" << nl
           << "const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];" << nl
@@ -676,6 +739,7 @@ void CudaPrinter::printKernel(const StepInfo &info) {
              "(uint32_t) A.step_index, (uint64_t) A.timestep);"
           << nl << "abl_K.self = abl_i;" << nl << "abl_K.removed = 0;" << nl
           << "abl_K.added = 0;" << nl << "abl_K.child_cols = nullptr;" << nl
+          << "abl_K.near_col = " << (info.presorted ? "abl_j" : "-1") << ";" << nl
           << T << " abl_in, abl_out;";
     for (size_t k = 0; k < agent.members->size(); k++) {
       const AST::AgentMember &m = *(*agent.members)[k];
@@ -709,7 +773,7 @@ void CudaPrinter::printKernel(const StepInfo &info) {
           << "const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : "
              "ABL_STEP_BLOCK;" << nl
           << "const long abl_grid = (L->n + abl_block - 1) / abl_block;" << nl
-          << "abl_kernel_ens_" << name << "<<<abl_grid, abl_block, 0, abl_stream>>>(*L);" << nl
+          << "abl_kernel_ens_" << name << "<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);" << nl
           << "return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;" << outdent << nl
           << "}" << nl;
   }
@@ -891,9 +955,9 @@ void CudaPrinter::printDescriptor() {
           << s.nearMembers << "u, " << s.outAlways << "u, abl_launch_" << n << ", "
           << (s.usesRemove ? 1 : 0) << ", " << s.addType << ", " << (copyOut() ? 1 : 0) << ", "
           << (s.addType < 0 && !s.usesRemove ? "abl_launch_ens_" + n : std::string("nullptr"))
-          << ", " << (s.usesRng ? 1 : 0) << "},";
+          << ", " << (s.usesRng ? 1 : 0) << ", " << (s.presorted ? 1 : 0) << "},";
   }
-  if (steps.empty()) *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0},";
+  if (steps.empty()) *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0, 0},";
   *this << outdent << nl << "};" << nl;
   // The runtime runs the steps in simulate order (SimulateStatement::stepFuncDecls,
   // CPrinter.cpp:196); abl_steps above is in declaration order.

@@ -74,6 +74,9 @@ private:
     bool usesRemove = false;
     int addType = -1;
     bool usesRng = false;
+    // The step's only near loop is ordered and iterates around the step's own
+    // agent: the kernel gathers and sorts neighbour lists per block.
+    bool presorted = false;
   };
   std::vector<StepInfo> steps;
 
@@ -83,6 +86,7 @@ private:
   void printGlobals();
   void printStepFunction(const AST::FunctionDeclaration &decl);
   void printKernel(const StepInfo &info);
+  void printPresortPhase(const StepInfo &info, const std::string &view, const std::string &pos);
   void printDescriptor();
   void printHostSimulate();
   void printUserFunction(const AST::FunctionDeclaration &decl);

@@ -14,6 +14,14 @@
 //    reference's sequence of in-radius neighbours.
 //  * Unordered mode (bodies that only do integer accumulation): candidates
 //    are walked cell row by cell row without sorting.
+//  * Presorted mode (ordered bodies of a step's single near loop around the
+//    step's own agent): before any step body runs, each thread of a block
+//    collects the in-radius neighbours of one of the block's agents and keeps
+//    them in shared memory sorted by agent id (at most a fixed number at a
+//    time; more are fetched again past the last one consumed).  Optionally
+//    the block then hands its agents to its threads in ascending order of
+//    neighbour count, so the lanes of a warp run loop bodies of nearly equal
+//    length.  No global neighbourhood lists are built.
 //
 // The radius test is decided without FP64 arithmetic for almost every
 // candidate: the squared distance is computed in FP32 from float copies of
@@ -215,89 +223,6 @@ struct near_cursor {
   }
 };
 
-// A distance between the query agent and the current neighbour that the
-// generated code only ever compares with loop-invariant values, e.g.
-//   float separation = dist(in.pos, nx.pos); if (separation < R) ...
-// A comparison is decided from the FP32 estimate whenever it lies outside the
-// error band of make_band(R); otherwise the reference expression (`exact`)
-// is evaluated.  Either way the result equals the reference's comparison.
-template <int DIM, typename Exact>
-struct lazy_dist {
-  const near_query<DIM> &q;
-  float d2f;
-  Exact exact;
-
-  __device__ lazy_dist(const near_query<DIM> &q_, const abl_near_view &V, int slot, Exact e)
-      : q(q_), exact(e) {
-    float d2 = 0.0f;
-#pragma unroll
-    for (int d = 0; d < DIM; d++) {
-      float dd = __ldg(&V.posf[DIM * slot + d]) - q.pf[d];
-      d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
-    }
-    d2f = d2;
-  }
-
-  // -1: surely below R, +1: surely above R, 0: undecided.
-  __device__ int side(double R) const {
-    const band &b = q.band_for(R);
-    if (d2f < b.lo) return -1;
-    if (d2f > b.hi) return 1;
-    return 0;
-  }
-};
-
-template <int DIM, typename Exact>
-__device__ lazy_dist<DIM, Exact> make_lazy_dist(const near_query<DIM> &q, const abl_near_view &V,
-                                                int slot, Exact e) {
-  return lazy_dist<DIM, Exact>(q, V, slot, e);
-}
-
-
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator<(const lazy_dist<DIM, Exact> &a, R r) {
-  int s = a.side((double) r);
-  return s < 0 ? true : s > 0 ? false : a.exact() < r;
-}
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator<=(const lazy_dist<DIM, Exact> &a, R r) {
-  int s = a.side((double) r);
-  return s < 0 ? true : s > 0 ? false : a.exact() <= r;
-}
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator>(const lazy_dist<DIM, Exact> &a, R r) {
-  int s = a.side((double) r);
-  return s < 0 ? false : s > 0 ? true : a.exact() > r;
-}
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator>=(const lazy_dist<DIM, Exact> &a, R r) {
-  int s = a.side((double) r);
-  return s < 0 ? false : s > 0 ? true : a.exact() >= r;
-}
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator==(const lazy_dist<DIM, Exact> &a, R r) {
-  int s = a.side((double) r);
-  return s != 0 ? false : a.exact() == r;
-}
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator!=(const lazy_dist<DIM, Exact> &a, R r) {
-  int s = a.side((double) r);
-  return s != 0 ? true : a.exact() != r;
-}
-// R OP d  is  d OP' R.
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator<(R r, const lazy_dist<DIM, Exact> &a) { return a > r; }
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator<=(R r, const lazy_dist<DIM, Exact> &a) { return a >= r; }
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator>(R r, const lazy_dist<DIM, Exact> &a) { return a < r; }
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator>=(R r, const lazy_dist<DIM, Exact> &a) { return a <= r; }
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator==(R r, const lazy_dist<DIM, Exact> &a) { return a == r; }
-template <int DIM, typename Exact, typename R>
-__device__ inline bool operator!=(R r, const lazy_dist<DIM, Exact> &a) { return a != r; }
-
 // Counter-based random numbers for random() inside step functions.  The
 // reference draws from one sequential xorshift stream shared by all OpenMP
 // threads (asset/c/libabl.c:8-39), which has no parallel order; here every
@@ -375,6 +300,7 @@ struct step_ctx {
   int removed;
   int added;
   void *const *child_cols;
+  int near_col;  // presorted mode: the block agent whose neighbour list this thread reads
 
   __device__ void remove() { removed = 1; }
 };
@@ -383,5 +309,394 @@ struct step_ctx {
 __device__ inline void atomic_max_nonneg(float *addr, float v) {
   atomicMax(reinterpret_cast<int *>(addr), __float_as_int(v));
 }
+
+// ---------------------------------------------------------------------------
+// Presorted mode.
+
+// Shared memory of a presorted step kernel (dynamic, presort_bytes() at
+// launch): per block agent c a column of `cap` neighbour slots and, in runs
+// mode (no neighbourhood lists), their ids; then per-agent bookkeeping.
+struct presort_shared {
+  int *slots;            // [cap][ABL_STEP_BLOCK]: slots, ascending neighbour id
+  int *ids;              // [cap][ABL_STEP_BLOCK]: runs mode, the slots' ids
+  int *total;            // in-radius neighbours past the column's lower bound
+  int *key;              // sort key: neighbour count, INT_MAX without agent
+  int *perm;             // thread -> block agent, ascending key
+  int *resume;           // lists: list index after the stored slots; rows: last stored id
+  unsigned char *fresh;  // column still holds the first `cap` neighbours
+  int cap;
+  int mode;  // kGather*
+};
+
+// Presorted gathering modes: whole neighbourhood lists, row lists merged on
+// the fly (2D), or the cells' own runs sorted per agent.
+enum { kGatherRuns = 0, kGatherRows = 1, kGatherLists = 2 };
+
+__host__ __device__ inline int gather_mode(const abl_near_view &V) {
+  return V.ordered ? kGatherLists : (V.rows && V.dim == 2) ? kGatherRows : kGatherRuns;
+}
+
+__host__ __device__ inline size_t presort_bytes(const abl_near_view &V) {
+  const size_t B = ABL_STEP_BLOCK;
+  const size_t cols = (size_t) V.cap * B * (gather_mode(V) == kGatherRuns ? 2 : 1);
+  return (cols + 4 * B) * sizeof(int) + B;
+}
+
+__device__ __forceinline__ presort_shared presort_smem(const abl_near_view &V) {
+  extern __shared__ int abl_presort_dyn[];
+  const int B = ABL_STEP_BLOCK;
+  presort_shared S;
+  S.cap = V.cap;
+  S.mode = gather_mode(V);
+  S.slots = abl_presort_dyn;
+  int *p = S.slots + S.cap * B;
+  S.ids = nullptr;
+  if (S.mode == kGatherRuns) {
+    S.ids = p;
+    p += S.cap * B;
+  }
+  S.total = p;
+  S.key = p + B;
+  S.perm = p + 2 * B;
+  S.resume = p + 3 * B;
+  S.fresh = (unsigned char *) (p + 4 * B);
+  return S;
+}
+
+// Runs mode: scans the candidate cells of query q and stores in column `col`
+// the ids (ascending) and slots of the first S.cap in-radius neighbours with
+// id > lower.  Returns how many in-radius neighbours have id > lower;
+// `stored` receives how many of them the column holds.
+template <int DIM, typename Exact>
+__device__ int gather_sorted(const presort_shared &S, const abl_near_view &V,
+                             const near_query<DIM> &q, Exact &exact, int col, int lower,
+                             int &stored) {
+  int *I = S.ids + col;
+  int *L = S.slots + col;
+  const int B = ABL_STEP_BLOCK, cap = S.cap;
+  int n = 0, total = 0;
+  const int zlo = DIM == 3 ? max(q.c[2] - V.range, 0) : 0;
+  const int zhi = DIM == 3 ? min(q.c[2] + V.range, V.nz - 1) : 0;
+  const int ylo = max(q.c[1] - V.range, 0), yhi = min(q.c[1] + V.range, V.ny - 1);
+  const int x0 = max(q.c[0] - V.range, 0), x1 = min(q.c[0] + V.range, V.nx - 1);
+  for (int z = zlo; z <= zhi; z++) {
+    for (int y = ylo; y <= yhi; y++) {
+      const int base = (z * V.ny + y) * V.nx;
+      const int s1 = __ldg(&V.cell_start[base + x1 + 1]);
+      for (int s = __ldg(&V.cell_start[base + x0]); s < s1; s++) {
+        float d2 = 0.0f;
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+          float dd = __ldg(&V.posf[DIM * s + d]) - q.pf[d];
+          d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
+        }
+        if (d2 > q.bd.hi) continue;
+        const int id = __ldg(&V.order[s]);
+        if (id <= lower) continue;
+        if (!(d2 < q.bd.lo) && !exact(s)) continue;
+        total++;
+        if (n == cap && id >= I[(cap - 1) * B]) continue;
+        int p = n < cap ? n : cap - 1;
+        while (p > 0) {
+          const int prev = I[(p - 1) * B];
+          if (prev < id) break;
+          I[p * B] = prev;
+          L[p * B] = L[(p - 1) * B];
+          p--;
+        }
+        I[p * B] = id;
+        L[p * B] = s;
+        if (n < cap) n++;
+      }
+    }
+  }
+  stored = n;
+  return total;
+}
+
+// List mode (the grid has per-cell neighbourhood lists in ascending id): from
+// list index `from` on, stores the slots of the first S.cap in-radius
+// neighbours in column `col` and counts all of them.  `next` receives the
+// list index just past the last stored slot.
+template <int DIM, typename Exact>
+__device__ int gather_list(const presort_shared &S, const abl_near_view &V,
+                           const near_query<DIM> &q, Exact &exact, int col, int from,
+                           int &stored, int &next) {
+  int *L = S.slots + col;
+  const int cap = S.cap;
+  const int cell = (q.c[2] * V.ny + q.c[1]) * V.nx + q.c[0];
+  const int end = __ldg(&V.nb_off[cell + 1]);
+  int n = 0, total = 0;
+  next = end;
+  for (int k = from; k < end; k++) {
+    const int s = __ldg(&V.nb_list[k]);
+    float d2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      float dd = __ldg(&V.posf[DIM * s + d]) - q.pf[d];
+      d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
+    }
+    if (d2 > q.bd.hi) continue;
+    if (!(d2 < q.bd.lo) && !exact(s)) continue;
+    total++;
+    if (n < cap) {
+      L[n * ABL_STEP_BLOCK] = s;
+      n++;
+      if (n == cap) next = k + 1;
+    }
+  }
+  stored = n;
+  return total;
+}
+
+// Rows mode (2D): the in-radius neighbours with id > lower, taken in
+// ascending id from a three-way merge of the row lists of the cells above,
+// at and below the query cell.  Stores the first S.cap slots in column `col`
+// and returns how many there are in all; `last` receives the id of the last
+// stored slot.
+template <int DIM, typename Exact>
+__device__ int gather_rows(const presort_shared &S, const abl_near_view &V,
+                           const near_query<DIM> &q, Exact &exact, int col, int lower,
+                           int &stored, int &last) {
+  int *L = S.slots + col;
+  const int cap = S.cap;
+  const int kNone = 0x7fffffff;
+  int pos[3], end[3], hid[3], hsl[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int y = q.c[1] + k - 1;
+    pos[k] = end[k] = 0;
+    if (y >= 0 && y < V.ny) {
+      const int u = y * V.nx + q.c[0];
+      pos[k] = __ldg(&V.row_off[u]);
+      end[k] = __ldg(&V.row_off[u + 1]);
+    }
+    hid[k] = kNone;
+    hsl[k] = 0;
+    if (pos[k] < end[k]) {
+      const int2 v = __ldg(&V.rows[pos[k]]);
+      hid[k] = v.x;
+      hsl[k] = v.y;
+    }
+  }
+  int n = 0, total = 0;
+  last = lower;
+  for (;;) {
+    const bool a01 = hid[0] < hid[1];
+    const int m01 = a01 ? hid[0] : hid[1];
+    const int k = hid[2] < m01 ? 2 : (a01 ? 0 : 1);
+    const int id = k == 2 ? hid[2] : m01;
+    if (id == kNone) break;
+    const int s = k == 0 ? hsl[0] : (k == 1 ? hsl[1] : hsl[2]);
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      if (j == k) {
+        const int e = ++pos[j];
+        hid[j] = kNone;
+        if (e < end[j]) {
+          const int2 v = __ldg(&V.rows[e]);
+          hid[j] = v.x;
+          hsl[j] = v.y;
+        }
+      }
+    }
+    if (id <= lower) continue;
+    float d2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      float dd = __ldg(&V.posf[DIM * s + d]) - q.pf[d];
+      d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
+    }
+    if (d2 > q.bd.hi) continue;
+    if (!(d2 < q.bd.lo) && !exact(s)) continue;
+    total++;
+    if (n < cap) {
+      L[n * ABL_STEP_BLOCK] = s;
+      n++;
+      last = id;
+    }
+  }
+  stored = n;
+  return total;
+}
+
+template <int DIM>
+__device__ __forceinline__ int list_begin(const abl_near_view &V, const near_query<DIM> &q) {
+  return __ldg(&V.nb_off[(q.c[2] * V.ny + q.c[1]) * V.nx + q.c[0]]);
+}
+
+// Phase one of a presorted step kernel; every thread of the block calls it.
+// Thread t gathers the neighbours of the block's agent t (has == false: no
+// agent).  With V.balance set the block then ranks its agents by neighbour
+// count; otherwise thread t keeps agent t.  Returns the block agent this
+// thread runs the step body for.
+template <int DIM, typename Exact>
+__device__ int presort_block(const abl_near_view &V, bool has, const near_query<DIM> &q,
+                             Exact &exact) {
+  const presort_shared S = presort_smem(V);
+  const int t = threadIdx.x;
+  int key = 0x7fffffff;
+  if (has) {
+    int stored = 0;
+    if (S.mode == kGatherLists) {
+      int next = 0;
+      key = gather_list(S, V, q, exact, t, list_begin(V, q), stored, next);
+      S.resume[t] = next;
+    } else if (S.mode == kGatherRows) {
+      int last = -1;
+      key = gather_rows(S, V, q, exact, t, -1, stored, last);
+      S.resume[t] = last;
+    } else {
+      key = gather_sorted(S, V, q, exact, t, -1, stored);
+    }
+    S.total[t] = key;
+  }
+  S.fresh[t] = 1;
+  if (!V.balance) return t;
+  S.key[t] = key;
+  __syncthreads();
+  int rank = 0;
+  const int nb = blockDim.x;
+  for (int j = 0; j < nb; j++) {
+    const int kj = S.key[j];
+    rank += (kj < key) || (kj == key && j < t);
+  }
+  S.perm[rank] = t;
+  __syncthreads();
+  return S.perm[t];
+}
+
+// Enumerates the in-radius neighbour slots of block agent `col` in ascending
+// id order, in chunks of at most S.cap, starting from the column that
+// presort_block left in shared memory.
+template <int DIM>
+struct near_list_cursor {
+  const abl_near_view &V;
+  const presort_shared S;
+  int col;
+  int cnt;
+  bool first, more;
+  int last;
+
+  __device__ near_list_cursor(const abl_near_view &v, const near_query<DIM> &, const step_ctx &K)
+      : V(v), S(presort_smem(v)), col(K.near_col), cnt(0), first(true), more(false), last(-1) {}
+
+  __device__ int slot(int k) const { return S.slots[k * ABL_STEP_BLOCK + col]; }
+
+  template <typename Exact>
+  __device__ bool fill(const near_query<DIM> &q, Exact &&exact) {
+    if (first && S.fresh[col]) {
+      first = false;
+      const int tot = S.total[col];
+      cnt = tot < S.cap ? tot : S.cap;
+      more = tot > S.cap;
+    } else if (first || more) {
+      // A second pass over the neighbours, or the ones past the stored ones.
+      int stored = 0, tot = 0;
+      if (S.mode == kGatherLists) {
+        const int from = first ? list_begin(V, q) : S.resume[col];
+        int next = 0;
+        tot = gather_list(S, V, q, exact, col, from, stored, next);
+        S.resume[col] = next;
+      } else if (S.mode == kGatherRows) {
+        int lastid = -1;
+        tot = gather_rows(S, V, q, exact, col, first ? -1 : S.resume[col], stored, lastid);
+        S.resume[col] = lastid;
+      } else {
+        tot = gather_sorted(S, V, q, exact, col, first ? -1 : last, stored);
+      }
+      first = false;
+      S.fresh[col] = 0;
+      cnt = stored;
+      more = tot > stored;
+    } else {
+      cnt = 0;
+    }
+    if (cnt > 0 && S.mode == kGatherRuns) last = S.ids[(cnt - 1) * ABL_STEP_BLOCK + col];
+    return cnt > 0;
+  }
+};
+
+// A distance between the query agent and the current neighbour that the
+// generated code only ever compares with loop-invariant values, e.g.
+//   float separation = dist(in.pos, nx.pos); if (separation < R) ...
+// A comparison is decided from the FP32 estimate whenever it lies outside the
+// error band of make_band(R); otherwise the reference expression (`exact`)
+// is evaluated.  Either way the result equals the reference's comparison.
+template <int DIM, typename Exact>
+struct lazy_dist {
+  const near_query<DIM> &q;
+  float d2f;
+  Exact exact;
+
+  __device__ lazy_dist(const near_query<DIM> &q_, const abl_near_view &V, int slot, Exact e)
+      : q(q_), exact(e) {
+    float d2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      float dd = __ldg(&V.posf[DIM * slot + d]) - q.pf[d];
+      d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
+    }
+    d2f = d2;
+  }
+
+  // -1: surely below R, +1: surely above R, 0: undecided.
+  __device__ int side(double R) const {
+    const band &b = q.band_for(R);
+    if (d2f < b.lo) return -1;
+    if (d2f > b.hi) return 1;
+    return 0;
+  }
+};
+
+template <int DIM, typename Exact>
+__device__ lazy_dist<DIM, Exact> make_lazy_dist(const near_query<DIM> &q, const abl_near_view &V,
+                                                int slot, Exact e) {
+  return lazy_dist<DIM, Exact>(q, V, slot, e);
+}
+
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator<(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s < 0 ? true : s > 0 ? false : a.exact() < r;
+}
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator<=(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s < 0 ? true : s > 0 ? false : a.exact() <= r;
+}
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator>(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s < 0 ? false : s > 0 ? true : a.exact() > r;
+}
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator>=(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s < 0 ? false : s > 0 ? true : a.exact() >= r;
+}
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator==(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s != 0 ? false : a.exact() == r;
+}
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator!=(const lazy_dist<DIM, Exact> &a, R r) {
+  int s = a.side((double) r);
+  return s != 0 ? true : a.exact() != r;
+}
+// R OP d  is  d OP' R.
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator<(R r, const lazy_dist<DIM, Exact> &a) { return a > r; }
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator<=(R r, const lazy_dist<DIM, Exact> &a) { return a >= r; }
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator>(R r, const lazy_dist<DIM, Exact> &a) { return a < r; }
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator>=(R r, const lazy_dist<DIM, Exact> &a) { return a <= r; }
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator==(R r, const lazy_dist<DIM, Exact> &a) { return a == r; }
+template <int DIM, typename Exact, typename R>
+__device__ inline bool operator!=(R r, const lazy_dist<DIM, Exact> &a) { return a != r; }
 
 }  // namespace abl

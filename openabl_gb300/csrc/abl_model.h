@@ -58,8 +58,12 @@ typedef struct {
   const float *posf;        /* slot -> position rounded to float (dim per slot) */
   const int *nb_off;        /* ordered mode: cell -> offset into nb_list (ncells + 1) */
   const int *nb_list;       /* ordered mode: slots, ascending agent id per cell */
+  const int *row_off;       /* row lists: cell -> offset into rows (ncells + 1) */
+  const int2 *rows;         /* row lists: (id, slot) of the cells c-1..c+1 along x, ascending id */
   const float *amax;        /* max |coordinate| over neighbour and query agents */
   const void *cols[ABL_MAX_MEMBERS]; /* slot-ordered copies of the members the loop reads */
+  int balance;              /* presorted mode: hand a block's agents to threads by neighbour count */
+  int cap;                  /* presorted mode: neighbours held per agent in shared memory */
 } abl_near_view;
 
 /* Everything a generated step launcher needs. */
@@ -72,6 +76,7 @@ typedef struct {
   int *error;                        /* device error word */
   abl_near_view near;                /* valid when the step has a near loop */
   int block;                         /* threads per block chosen by the runtime */
+  size_t smem;                       /* dynamic shared memory per block */
   /* runtime removal / addition (steps that call removeCurrent() / add()) */
   uint8_t *removed;                  /* per agent: 1 when the agent removed itself */
   uint8_t *child_flag;               /* per agent: 1 when it created a child */
@@ -101,6 +106,7 @@ typedef struct {
   long timestep;
   int step_index;
   int block;
+  size_t smem;                       /* dynamic shared memory per block */
 } abl_ens_launch;
 
 typedef int (*abl_ens_launch_fn)(const abl_ens_launch *launch, cudaStream_t stream);
@@ -121,6 +127,7 @@ typedef struct {
   int out_copy;                /* `out` starts as a copy of `in` */
   abl_ens_launch_fn launch_ens; /* ensemble variant (NULL: not supported) */
   int uses_rng;                 /* the body draws random numbers */
+  int presorted;                /* ordered near loop served from per-block sorted lists */
 } abl_step_desc;
 
 /* Host function run after every timestep: the `sequential step`. */

@@ -39,8 +39,6 @@
 namespace {
 
 constexpr int kScanBlock = 1024;
-constexpr int kListWarpsPerBlock = 8;
-constexpr int kListCap = 256;  // candidates staged in shared memory per warp
 
 #define ABL_CUDA_TRY(expr)                                                   \
   do {                                                                       \
@@ -295,36 +293,101 @@ __global__ void k_gather(long n, const int *order, const Real *pos, float *posf,
 }
 
 // Per cell: number of candidates in the surrounding (2R+1)^DIM cells.
-template <int DIM>
-__global__ void k_nb_count(int nx, int ny, int nz, int R, const int *cell_start, int *nb_cnt,
-                           int skip_empty) {
-  long c = (long) blockIdx.x * blockDim.x + threadIdx.x;
-  long ncells = (long) nx * ny * nz;
-  if (c >= ncells) return;
-  if (skip_empty && cell_start[c + 1] == cell_start[c]) {
-    nb_cnt[c] = 0;
-    return;
+// ------------------------------------------------- neighbourhood lists
+//
+// Ordered near loops read, per cell, the slots of every agent in the
+// surrounding (2R+1)^dim cells in ascending agent id.  The lists are built
+// one axis at a time: level 0 is the cells' own runs (id-sorted by
+// k_cell_sort); level a+1 merges, for every cell c, the level-a lists of the
+// cells c - R .. c + R along axis a.  An element's place in a merged list is
+// its index in its own source list plus, for every other source list, the
+// number of smaller ids there (a binary search), so every element is written
+// once per target list with no sorting pass.
+
+// Cell geometry of a single grid.
+struct GridGeom {
+  int nx, ny, nz, R;
+  __device__ void locate(long, long &base, int &gx, int &gy, int &gz, int &r) const {
+    base = 0;
+    gx = nx;
+    gy = ny;
+    gz = nz;
+    r = R;
   }
-  int cx = c % nx, cy = (c / nx) % ny, cz = c / ((long) nx * ny);
-  int x0 = max(cx - R, 0), x1 = min(cx + R, nx - 1);
-  int cnt = 0;
-  for (int z = (DIM == 3 ? max(cz - R, 0) : 0); z <= (DIM == 3 ? min(cz + R, nz - 1) : 0); z++) {
-    for (int y = max(cy - R, 0); y <= min(cy + R, ny - 1); y++) {
-      long base = ((long) z * ny + y) * nx;
-      cnt += cell_start[base + x1 + 1] - cell_start[base + x0];
-    }
-  }
-  nb_cnt[c] = cnt;
+};
+
+// Coordinates of a cell within its grid (32-bit: grids have < 2^30 cells).
+struct CellPos {
+  int x[3], n[3];
+  int stride[3];
+  int R;
+};
+
+template <typename G>
+__device__ inline CellPos cell_pos(const G &geo, long c) {
+  long base;
+  int nx, ny, nz, R;
+  geo.locate(c, base, nx, ny, nz, R);
+  CellPos p;
+  const int l = (int) (c - base);
+  const int nxy = nx * ny;
+  p.x[2] = l / nxy;
+  const int r = l - p.x[2] * nxy;
+  p.x[1] = r / nx;
+  p.x[0] = r - p.x[1] * nx;
+  p.n[0] = nx;
+  p.n[1] = ny;
+  p.n[2] = nz;
+  p.stride[0] = 1;
+  p.stride[1] = nx;
+  p.stride[2] = nxy;
+  p.R = R;
+  return p;
 }
 
-// Per cell (one warp each): the candidate slots of the surrounding cells in
-// ascending agent id.  Up to kListCap candidates are staged in shared memory
-// and ranked by counting smaller ids; in larger neighbourhoods an element's
-// place is its position in its own run (runs are id-sorted, k_cell_sort)
-// plus, for every other run, a binary search for the ids below its own.
-constexpr int kMaxRuns = 125;
+// Neighbour of cell c (at p) at offset d along AXIS, or -1 outside the grid.
+template <int AXIS>
+__device__ inline long axis_neighbour(const CellPos &p, long c, int d) {
+  const int k = p.x[AXIS] + d;
+  if (k < 0 || k >= p.n[AXIS]) return -1;
+  return c + (long) d * p.stride[AXIS];
+}
 
-__device__ inline int lower_bound_ids(const int *a, int len, int id) {
+template <typename G, int AXIS>
+__global__ void k_sep_count(long ncells, G geo, const int *src_off, int *dst_cnt) {
+  const long c = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const CellPos p = cell_pos(geo, c);
+  int cnt = 0;
+  for (int d = -p.R; d <= p.R; d++) {
+    const long u = axis_neighbour<AXIS>(p, c, d);
+    if (u >= 0) cnt += src_off[u + 1] - src_off[u];
+  }
+  dst_cnt[c] = cnt;
+}
+
+// Source lists of one level.  Level 0: the binned slots themselves (list of
+// cell u = slots off[u] .. off[u+1], ids order[slot]); later levels store
+// (id, slot) pairs.
+struct SepSrc {
+  const int *off;    // ncells + 1
+  const int *order;  // level 0
+  const int2 *pair;  // later levels
+};
+
+constexpr int kSepMaxSrc = 7;        // source lists per target: 2R + 1 for R <= 3
+constexpr int kSepWarps = 8;         // target cells (warps) per block of k_sep_merge_large
+constexpr int kSepThreads = 128;     // target cells (threads) per block of k_sep_merge
+constexpr int kSepStageInts = 1536;  // per warp of k_sep_merge: staged output ints
+constexpr int kSepSeqMax = 4096;     // longest list merged by one thread
+
+template <bool PAIR>
+__device__ __forceinline__ int2 sep_elem_t(const SepSrc &S, int e) {
+  if (PAIR) return __ldg(&S.pair[e]);
+  return make_int2(__ldg(&S.order[e]), e);
+}
+
+__device__ inline int lower_bound_shared(const int *a, int len, int id) {
   int lo = 0, hi = len;
   while (lo < hi) {
     int mid = (lo + hi) >> 1;
@@ -334,75 +397,154 @@ __device__ inline int lower_bound_ids(const int *a, int len, int id) {
   return lo;
 }
 
-template <int DIM>
-__global__ void k_nb_build(int nx, int ny, int nz, int R, const int *cell_start,
-                           const int *order, const int *nb_off, int *nb_list) {
-  __shared__ int s_id[kListWarpsPerBlock][kListCap];
-  __shared__ int s_run[kListWarpsPerBlock][kMaxRuns + 1];   // run begin within the list
-  __shared__ int s_slot0[kListWarpsPerBlock][kMaxRuns];     // first slot of each run
-  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  long c = (long) blockIdx.x * kListWarpsPerBlock + w;
-  long ncells = (long) nx * ny * nz;
-  if (c >= ncells) return;
-  int base_out = nb_off[c];
-  int count = nb_off[c + 1] - base_out;
-  if (count == 0) return;
-  int cx = c % nx, cy = (c / nx) % ny, cz = c / ((long) nx * ny);
-  int x0 = max(cx - R, 0), x1 = min(cx + R, nx - 1);
-  int z0 = DIM == 3 ? max(cz - R, 0) : 0, z1 = DIM == 3 ? min(cz + R, nz - 1) : 0;
-  int y0 = max(cy - R, 0), y1 = min(cy + R, ny - 1);
-  // Runs in (z, y, x) order, each one cell.
-  int nruns = 0, k = 0;
-  for (int z = z0; z <= z1; z++) {
-    for (int y = y0; y <= y1; y++) {
-      long rb = ((long) z * ny + y) * nx;
-      for (int x = x0; x <= x1; x++) {
-        int s = cell_start[rb + x], e = cell_start[rb + x + 1];
-        if (lane == 0) {
-          s_run[w][nruns] = k;
-          s_slot0[w][nruns] = s;
+__device__ __forceinline__ int2 sep_elem(const SepSrc &S, int e) {
+  return S.pair ? __ldg(&S.pair[e]) : make_int2(__ldg(&S.order[e]), e);
+}
+
+__device__ inline int lower_bound_src(const SepSrc &S, int b, int len, int id) {
+  int lo = 0, hi = len;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (sep_elem(S, b + mid).x < id) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Source lists of target cell t along AXIS: begin and length per offset
+// -R .. R (length 0 outside the grid).  Returns the total length.
+template <int AXIS>
+__device__ inline int sep_sources(const CellPos &P, long t, const SepSrc &S, int *b, int *n) {
+  int total = 0;
+#pragma unroll
+  for (int k = 0; k < kSepMaxSrc; k++) {
+    b[k] = 0;
+    n[k] = 0;
+    const int d = k - P.R;
+    if (d > P.R) continue;
+    const long u = axis_neighbour<AXIS>(P, t, d);
+    if (u < 0) continue;
+    b[k] = S.off[u];
+    n[k] = S.off[u + 1] - b[k];
+    total += n[k];
+  }
+  return total;
+}
+
+// One thread per target cell with R = 1 and at most kSepSeqMax elements:
+// a three-way merge of the id-sorted source lists.  The 32 cells of a warp
+// own one contiguous output range; when it fits, the outputs are staged in
+// shared memory and stored coalesced.  Other cells are left to
+// k_sep_merge_large (a warp whose range holds such a cell never stages).
+template <typename G, int AXIS, bool PAIR, bool STAGE>
+__global__ void __launch_bounds__(kSepThreads)
+k_sep_merge(long ncells, G geo, SepSrc S, const int *dst_off, int2 *dst_pair, int *dst_slot) {
+  __shared__ int stage[STAGE ? kSepThreads / 32 : 1][STAGE ? kSepStageInts : 1];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long t0 = (long) blockIdx.x * kSepThreads + 32 * w;
+  if (t0 >= ncells) return;
+  const long t = t0 + lane;
+  const long t1 = t0 + 32 < ncells ? t0 + 32 : ncells;
+  const long o0 = dst_off[t0];
+  const int per = dst_pair ? 2 : 1;
+  const bool staged = STAGE && (dst_off[t1] - o0) * per <= kSepStageInts;
+  int *st = stage[STAGE ? w : 0];
+  if (t < ncells) {
+    const CellPos P = cell_pos(geo, t);
+    const long out0 = dst_off[t];
+    const int total = (int) (dst_off[t + 1] - out0);
+    if (P.R == 1 && total > 0 && total <= kSepSeqMax) {
+      const int kNone = 0x7fffffff;
+      int pos[3], end[3], hid[3], hsl[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const long u = axis_neighbour<AXIS>(P, t, k - 1);
+        pos[k] = u >= 0 ? S.off[u] : 0;
+        end[k] = u >= 0 ? S.off[u + 1] : 0;
+        hid[k] = kNone;
+        hsl[k] = 0;
+        if (pos[k] < end[k]) {
+          const int2 v = sep_elem_t<PAIR>(S, pos[k]);
+          hid[k] = v.x;
+          hsl[k] = v.y;
         }
-        if (count <= kListCap) {
-          for (int j = lane; j < e - s; j += 32) s_id[w][k + j] = order[s + j];
+      }
+      int o = (int) (out0 - o0);
+      for (int q = 0; q < total; q++) {
+        const bool a01 = hid[0] < hid[1];
+        const int m01 = a01 ? hid[0] : hid[1];
+        const int k = hid[2] < m01 ? 2 : (a01 ? 0 : 1);
+        const int id = k == 2 ? hid[2] : m01;
+        const int sl = k == 0 ? hsl[0] : (k == 1 ? hsl[1] : hsl[2]);
+        if (staged) {
+          if (dst_pair) {
+            st[2 * (o + q)] = id;
+            st[2 * (o + q) + 1] = sl;
+          } else {
+            st[o + q] = sl;
+          }
+        } else if (dst_pair) {
+          dst_pair[out0 + q] = make_int2(id, sl);
+        } else {
+          dst_slot[out0 + q] = sl;
         }
-        k += e - s;
-        nruns++;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          if (j == k) {
+            const int e = ++pos[j];
+            hid[j] = kNone;
+            if (e < end[j]) {
+              const int2 v = sep_elem_t<PAIR>(S, e);
+              hid[j] = v.x;
+              hsl[j] = v.y;
+            }
+          }
+        }
       }
     }
   }
-  if (lane == 0) s_run[w][nruns] = k;
+  if (!staged) return;
   __syncwarp();
-  if (count <= kListCap) {
-    // Small neighbourhoods: rank by counting smaller ids (independent
-    // shared-memory reads, no dependence on the runs being sorted).
-    for (int e = lane; e < count; e += 32) {
-      int j = 0;
-      while (s_run[w][j + 1] <= e) j++;
-      int slot = s_slot0[w][j] + (e - s_run[w][j]);
-      int id = s_id[w][e];
-      int rank = 0;
-      for (int f = 0; f < count; f++) rank += s_id[w][f] < id;
-      nb_list[base_out + rank] = slot;
+  const int m = (int) (dst_off[t1] - o0) * per;
+  int *dst = dst_pair ? (int *) dst_pair : dst_slot;
+  for (int i = lane; i < m; i += 32) dst[per * o0 + i] = st[i];
+}
+
+// One warp per target cell that k_sep_merge leaves (R != 1 or more than
+// kSepStage source elements): an element's place is its index in its own
+// source list plus a binary search in every other source list.
+template <typename G, int AXIS>
+__global__ void __launch_bounds__(32 * kSepWarps)
+k_sep_merge_large(long ncells, G geo, SepSrc S, const int *dst_off, int2 *dst_pair,
+                  int *dst_slot) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long t = (long) blockIdx.x * kSepWarps + w;
+  if (t >= ncells) return;
+  const CellPos P = cell_pos(geo, t);
+  if (P.R == 1 && dst_off[t + 1] - dst_off[t] <= kSepSeqMax) return;
+  int b[kSepMaxSrc], n[kSepMaxSrc];
+  sep_sources<AXIS>(P, t, S, b, n);
+  const long out = dst_off[t];
+#pragma unroll
+  for (int k = 0; k < kSepMaxSrc; k++) {
+    for (int j = lane; j < n[k]; j += 32) {
+      const int2 v = sep_elem(S, b[k] + j);
+      int rank = j;
+#pragma unroll
+      for (int k2 = 0; k2 < kSepMaxSrc; k2++) {
+        if (k2 != k && n[k2] > 0) rank += lower_bound_src(S, b[k2], n[k2], v.x);
+      }
+      if (dst_pair) dst_pair[out + rank] = v;
+      else dst_slot[out + rank] = v.y;
     }
-    return;
-  }
-  // Large neighbourhoods: position in the own (sorted) run plus a binary
-  // search in every other run.
-  for (int e = lane; e < count; e += 32) {
-    int j = 0;
-    while (s_run[w][j + 1] <= e) j++;
-    int p = e - s_run[w][j];
-    int slot = s_slot0[w][j] + p;
-    int id = order[slot];
-    int rank = p;
-    for (int q = 0; q < nruns; q++) {
-      if (q == j) continue;
-      int len = s_run[w][q + 1] - s_run[w][q];
-      if (len > 0) rank += lower_bound_ids(order + s_slot0[w][q], len, id);
-    }
-    nb_list[base_out + rank] = slot;
   }
 }
+
+// Intermediate levels of the separable list build (dim - 1 of them).
+struct SepLevels {
+  int *off[2] = {nullptr, nullptr};
+  int2 *pair[2] = {nullptr, nullptr};
+};
 
 // --------------------------------------------------------------- state
 
@@ -418,7 +560,8 @@ struct TypeState {
 
   // binning (near types only)
   bool is_near = false;
-  bool ordered = false;     // some near loop over this type needs id order
+  bool ordered = false;     // whole neighbourhood lists (list depth 2)
+  bool rows = false;        // row lists (list depth 1)
   bool dirty = true;
   int R = 1;
   int nx = 1, ny = 1, nz = 1;
@@ -431,9 +574,31 @@ struct TypeState {
   float *posf = nullptr;
   void *gcols[ABL_MAX_MEMBERS] = {};
   int *nb_cnt = nullptr, *nb_off = nullptr, *nb_list = nullptr;
+  SepLevels sep;
   ScanPlan cell_scan, nb_scan;
   std::vector<void *> bin_allocs;  // freed when the type is re-uploaded
 };
+
+// Neighbour lists a near step's grid gets: 0 none (presorted loops sort
+// each agent's neighbours from the cells' runs), 1 row lists (2D presorted
+// loops merge the rows above, at and below on the fly), 2 whole
+// neighbourhood lists (every other ordered loop).  By default presorted loops
+// whose agents are the binned ones (threads visit agents cell by cell, so a
+// warp reads few lists in lockstep) use row lists in 2D and whole lists in
+// 3D; loops over another type sort the cells' runs per agent.  `mode`
+// (ABL_NEAR_*) forces one of them.
+int list_depth(const abl_step_desc &sd, const abl_agent_desc &d, int mode) {
+  if (!sd.ordered) return 0;
+  if (!sd.presorted) return 2;
+  switch (mode) {
+    case ABL_NEAR_RUNS: return 0;
+    case ABL_NEAR_ROWS: return d.dim == 2 ? 1 : 0;
+    case ABL_NEAR_LISTS: return 2;
+    default: break;
+  }
+  if (sd.agent_type != sd.near_type) return 0;
+  return d.dim == 2 ? 1 : 2;
+}
 
 size_t member_bytes(const abl_member_desc &m) {
   return (size_t) m.components * m.scalar_bytes;
@@ -490,6 +655,13 @@ struct abl_ctx {
   double *d_red = nullptr; // reduction results
   // Optional per-step-function kernel timing (eager timesteps only).
   bool profile = false;
+  // Presorted near steps: hand each block's agents to threads by neighbour
+  // count; neighbours held per agent in shared memory with and without
+  // neighbourhood lists (4 and 8 bytes each).
+  int balance = 1;
+  int list_cap = 32;
+  int runs_cap = 40;
+  int near_mode = ABL_NEAR_AUTO;
   std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
   std::vector<double> prof_seconds;
   std::vector<long> prof_launches;
@@ -596,6 +768,7 @@ void free_bins(abl_ctx *ctx, TypeState &t) {
   t.nb_scan.levels.clear();
   t.cell_count = t.cell_start = t.local_rank = t.cell_of = t.order = nullptr;
   t.nb_cnt = t.nb_off = t.nb_list = nullptr;
+  t.sep = SepLevels();
   t.posf = nullptr;
   for (auto &g : t.gcols) g = nullptr;
 }
@@ -649,7 +822,9 @@ int prepare(abl_ctx *ctx) {
       g.is_near = true;
     }
     TypeState &g = ctx->grids[gi];
-    g.ordered = g.ordered || sd.ordered;
+    const int depth = list_depth(sd, *g.d, ctx->near_mode);
+    g.ordered = g.ordered || depth == 2;
+    g.rows = g.rows || depth == 1;
     g.gather_mask |= sd.near_members;
     ctx->step_grid[k] = gi;
   }
@@ -706,14 +881,22 @@ int prepare(abl_ctx *ctx) {
         g.gcols[k] = p;
       }
     }
-    if (g.ordered) {
-      long span = 2 * g.R + 1;
-      long per_agent = dim == 3 ? span * span * span : span * span;
-      if (per_agent > kMaxRuns) return ABL_E_UNSUPPORTED;
+    if (g.ordered || g.rows) {
+      long span = 2 * g.R + 1, level = n;
+      const int inter = g.ordered ? dim - 1 : 1;  // levels kept as (id, slot) lists
+      for (int a = 0; a < inter; a++) {
+        level *= span;
+        ABL_TRY(dev_alloc_t(ctx, &g.sep.off[a], g.ncells + 1, own));
+        ABL_TRY(dev_alloc_t(ctx, &g.sep.pair[a], level, own));
+      }
+      // List offsets are 32-bit.
+      if (level * (g.ordered ? span : 1) > (long) INT32_MAX) return ABL_E_UNSUPPORTED;
       ABL_TRY(dev_alloc_t(ctx, &g.nb_cnt, g.ncells, own));
-      ABL_TRY(dev_alloc_t(ctx, &g.nb_off, g.ncells + 1, own));
-      ABL_TRY(dev_alloc_t(ctx, &g.nb_list, per_agent * n, own));
       ABL_TRY(scan_plan(ctx, g.nb_scan, g.ncells, own));
+      if (g.ordered) {
+        ABL_TRY(dev_alloc_t(ctx, &g.nb_off, g.ncells + 1, own));
+        ABL_TRY(dev_alloc_t(ctx, &g.nb_list, level * span, own));
+      }
     }
     g.dirty = true;
   }
@@ -837,6 +1020,7 @@ MoveArgs move_args(const abl_agent_desc &d, void *const *src, void *const *dst) 
 
 void mark_dirty(abl_ctx *ctx, int ti);
 
+
 // After a step function that removes or adds agents: stable compaction of
 // the survivors, then the children appended in parent order.  The step's
 // result is in the buffer it wrote (cols[1 - cur]).  Returns with `regrow`
@@ -898,6 +1082,48 @@ int apply_population_changes(abl_ctx *ctx, int k, bool &regrow) {
   return ABL_OK;
 }
 
+// Builds the first `levels` axes of a binned grid's lists: the row lists
+// (levels 1) or, with levels == dim, the whole neighbourhood lists (nb_off,
+// nb_list).
+template <typename G>
+void build_lists(abl_ctx *ctx, const G &geo, int dim, int levels, long ncells,
+                 const int *cell_start, const int *order, const SepLevels &L, int *cnt,
+                 const ScanPlan &scan, int *nb_off, int *nb_list) {
+  cudaStream_t s = ctx->stream;
+  const int B = 256;
+  SepSrc src{cell_start, order, nullptr};
+  const long cb = blocks_for(ncells, B), lb = blocks_for(ncells, kSepWarps);
+  for (int a = 0; a < levels; a++) {
+    const bool last = a == dim - 1;
+    int *off = last ? nb_off : L.off[a];
+    int2 *dp = last ? nullptr : L.pair[a];
+    int *ds = last ? nb_list : nullptr;
+    if (a == 0) k_sep_count<G, 0><<<cb, B, 0, s>>>(ncells, geo, src.off, cnt);
+    else if (a == 1) k_sep_count<G, 1><<<cb, B, 0, s>>>(ncells, geo, src.off, cnt);
+    else k_sep_count<G, 2><<<cb, B, 0, s>>>(ncells, geo, src.off, cnt);
+    ctx->launches++;
+    scan_run(ctx, scan, cnt, off);
+    // Intermediate levels stage their (id, slot) output in shared memory; the
+    // final level stores directly and leaves the shared memory to L1, which
+    // holds the three list heads each thread reads.
+    const long sb = blocks_for(ncells, kSepThreads);
+    if (a == 0) {
+      if (last) k_sep_merge<G, 0, false, false><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, dp, ds);
+      else k_sep_merge<G, 0, false, true><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, dp, ds);
+      k_sep_merge_large<G, 0><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, dp, ds);
+    } else if (a == 1) {
+      if (last) k_sep_merge<G, 1, true, false><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, dp, ds);
+      else k_sep_merge<G, 1, true, true><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, dp, ds);
+      k_sep_merge_large<G, 1><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, dp, ds);
+    } else {
+      k_sep_merge<G, 2, true, false><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, dp, ds);
+      k_sep_merge_large<G, 2><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, dp, ds);
+    }
+    ctx->launches += 2;
+    if (!last) src = SepSrc{L.off[a], nullptr, L.pair[a]};
+  }
+}
+
 template <typename Real>
 void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
   cudaStream_t s = ctx->stream;
@@ -936,25 +1162,10 @@ void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
     k_gather<Real, 3><<<nb, B, 0, s>>>(t.n, t.order, pos, t.posf, g);
   }
   ctx->launches++;
-  if (t.ordered) {
-    long cb = blocks_for(t.ncells, B);
-    int skip_empty = 0;  // lists for every cell: query agents may be of another type
-    if (dim == 2) {
-      k_nb_count<2><<<cb, B, 0, s>>>(t.nx, t.ny, t.nz, t.R, t.cell_start, t.nb_cnt, skip_empty);
-    } else {
-      k_nb_count<3><<<cb, B, 0, s>>>(t.nx, t.ny, t.nz, t.R, t.cell_start, t.nb_cnt, skip_empty);
-    }
-    ctx->launches++;
-    scan_run(ctx, t.nb_scan, t.nb_cnt, t.nb_off);
-    long lb = blocks_for(t.ncells, kListWarpsPerBlock);
-    if (dim == 2) {
-      k_nb_build<2><<<lb, 32 * kListWarpsPerBlock, 0, s>>>(t.nx, t.ny, t.nz, t.R, t.cell_start,
-                                                           t.order, t.nb_off, t.nb_list);
-    } else {
-      k_nb_build<3><<<lb, 32 * kListWarpsPerBlock, 0, s>>>(t.nx, t.ny, t.nz, t.R, t.cell_start,
-                                                           t.order, t.nb_off, t.nb_list);
-    }
-    ctx->launches++;
+  if (t.ordered || t.rows) {
+    GridGeom geo{t.nx, t.ny, t.nz, t.R};
+    build_lists(ctx, geo, dim, t.ordered ? dim : 1, t.ncells, t.cell_start, t.order, t.sep,
+                t.nb_cnt, t.nb_scan, t.nb_off, t.nb_list);
   }
 }
 
@@ -1035,8 +1246,11 @@ int step_once(abl_ctx *ctx) {
       if (ctx->grids[gi].dirty) bin_grid(ctx, gi);
       TypeState &nt = ctx->grids[gi];
       abl_near_view &V = L.near;
+      const int depth = list_depth(sd, *nt.d, ctx->near_mode);
       V.dim = nt.d->dim;
-      V.ordered = sd.ordered;
+      V.ordered = depth == 2;
+      V.rows = depth == 1 ? nt.sep.pair[0] : nullptr;
+      V.row_off = nt.sep.off[0];
       V.range = nt.R;
       V.nx = nt.nx;
       V.ny = nt.ny;
@@ -1051,6 +1265,9 @@ int step_once(abl_ctx *ctx) {
       V.nb_off = nt.nb_off;
       V.nb_list = nt.nb_list;
       for (int j = 0; j < nt.d->num_members; j++) V.cols[j] = nt.gcols[j];
+      V.balance = ctx->balance;
+      V.cap = V.ordered ? ctx->list_cap : ctx->runs_cap;
+      if (sd.presorted) L.smem = abl::presort_bytes(V);
       if (sd.agent_type == sd.near_type) {
         V.amax = nt.amax;
         L.visit_order = nt.order;
@@ -1554,6 +1771,21 @@ int abl_set_profiling(abl_ctx *ctx, int enable) {
   return ABL_OK;
 }
 
+int abl_set_near_mode(abl_ctx *ctx, int mode) {
+  if (!ctx || mode < ABL_NEAR_AUTO || mode > ABL_NEAR_LISTS) return ABL_E_INVALID;
+  ctx->near_mode = mode;
+  ctx->prepared = false;
+  drop_graph(ctx);
+  return ABL_OK;
+}
+
+int abl_set_balance(abl_ctx *ctx, int enable) {
+  if (!ctx) return ABL_E_INVALID;
+  ctx->balance = enable != 0;
+  drop_graph(ctx);
+  return ABL_OK;
+}
+
 int abl_step_kernel_time(abl_ctx *ctx, int step, double *seconds, long *launches) {
   if (!ctx || step < 0 || step >= (int) ctx->prof_seconds.size()) return ABL_E_INVALID;
   if (seconds) *seconds = ctx->prof_seconds[step];
@@ -1732,7 +1964,9 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
   TypeState &gb = ctx.grids[0];
   gb.d = &ad;
   gb.is_near = sd.near_type == 0;
-  gb.ordered = gb.is_near && sd.ordered;
+  const int depth = gb.is_near ? list_depth(sd, ad, ctx.near_mode) : 0;
+  gb.ordered = depth == 2;
+  gb.rows = depth == 1;
   gb.gather_mask = gb.is_near ? sd.near_members : 0;
   gb.dirty = true;
   gb.n = t.n;
@@ -1782,14 +2016,24 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
         ok = gb.gcols[k] != nullptr;
       }
     }
-    if (ok && gb.ordered) {
-      long span = 2 * gb.R + 1;
-      long per_agent = dim == 3 ? span * span * span : span * span;
-      if (per_agent > kMaxRuns) return ABL_E_UNSUPPORTED;
+    gb.sep = SepLevels();
+    gb.nb_off = gb.nb_list = nullptr;
+    if (ok && (gb.ordered || gb.rows)) {
+      long span = 2 * gb.R + 1, level = nn;
+      const int inter = gb.ordered ? dim - 1 : 1;
+      for (int a = 0; a < inter && ok; a++) {
+        level *= span;
+        gb.sep.off[a] = b.take<int>(gb.ncells + 1);
+        gb.sep.pair[a] = b.take<int2>(level);
+        ok = gb.sep.off[a] && gb.sep.pair[a];
+      }
       gb.nb_cnt = b.take<int>(gb.ncells);
-      gb.nb_off = b.take<int>(gb.ncells + 1);
-      gb.nb_list = b.take<int>(per_agent * nn);
-      ok = gb.nb_cnt && gb.nb_off && gb.nb_list && scan_plan_static(gb.nb_scan, gb.ncells, b);
+      ok = ok && gb.nb_cnt && scan_plan_static(gb.nb_scan, gb.ncells, b);
+      if (ok && gb.ordered) {
+        gb.nb_off = b.take<int>(gb.ncells + 1);
+        gb.nb_list = b.take<int>(level * span);
+        ok = gb.nb_off && gb.nb_list;
+      }
     }
     if (!ok) return ABL_E_SCRATCH;
   }
@@ -1857,112 +2101,19 @@ __global__ void k_ens_bin_assign(const Real *pos, long n, const int *replica_of,
   if ((threadIdx.x & 31) == 0 && m > 0.0f) abl::atomic_max_nonneg(amax, m);
 }
 
-// Neighbourhood of global cell c inside its replica's grid.
-struct EnsCellRange {
-  int x0, x1, y0, y1, z0, z1;
-  long base;
-  int nx, ny;
+// Cell geometry of a segmented grid: each replica's cells in its own block.
+struct EnsGeom {
+  const int *cell_replica;
+  const EnsGrid *grids;
+  __device__ void locate(long c, long &base, int &gx, int &gy, int &gz, int &r) const {
+    const EnsGrid &g = grids[cell_replica[c]];
+    base = g.cell_base;
+    gx = g.nx;
+    gy = g.ny;
+    gz = g.nz;
+    r = g.R;
+  }
 };
-
-template <int DIM>
-__device__ inline EnsCellRange ens_cell_range(long c, const int *cell_replica,
-                                              const EnsGrid *grids) {
-  const EnsGrid g = grids[cell_replica[c]];
-  long local = c - g.cell_base;
-  int cx = local % g.nx, cy = (local / g.nx) % g.ny, cz = local / ((long) g.nx * g.ny);
-  EnsCellRange r;
-  r.x0 = max(cx - g.R, 0);
-  r.x1 = min(cx + g.R, g.nx - 1);
-  r.y0 = max(cy - g.R, 0);
-  r.y1 = min(cy + g.R, g.ny - 1);
-  r.z0 = DIM == 3 ? max(cz - g.R, 0) : 0;
-  r.z1 = DIM == 3 ? min(cz + g.R, g.nz - 1) : 0;
-  r.base = g.cell_base;
-  r.nx = g.nx;
-  r.ny = g.ny;
-  return r;
-}
-
-template <int DIM>
-__global__ void k_ens_nb_count(long ncells, const int *cell_replica, const EnsGrid *grids,
-                               const int *cell_start, int *nb_cnt) {
-  long c = (long) blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
-  if (cell_start[c + 1] == cell_start[c]) {
-    nb_cnt[c] = 0;  // replicas have no other agent types: only occupied cells query
-    return;
-  }
-  EnsCellRange r = ens_cell_range<DIM>(c, cell_replica, grids);
-  int cnt = 0;
-  for (int z = r.z0; z <= r.z1; z++) {
-    for (int y = r.y0; y <= r.y1; y++) {
-      long rb = r.base + ((long) z * r.ny + y) * r.nx;
-      cnt += cell_start[rb + r.x1 + 1] - cell_start[rb + r.x0];
-    }
-  }
-  nb_cnt[c] = cnt;
-}
-
-template <int DIM>
-__global__ void k_ens_nb_build(long ncells, const int *cell_replica, const EnsGrid *grids,
-                               const int *cell_start, const int *order, const int *nb_off,
-                               int *nb_list) {
-  __shared__ int s_id[kListWarpsPerBlock][kListCap];
-  __shared__ int s_slot[kListWarpsPerBlock][kListCap];
-  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  long c = (long) blockIdx.x * kListWarpsPerBlock + w;
-  if (c >= ncells) return;
-  int base_out = nb_off[c];
-  int count = nb_off[c + 1] - base_out;
-  if (count == 0) return;
-  EnsCellRange r = ens_cell_range<DIM>(c, cell_replica, grids);
-  if (count <= kListCap) {
-    int k = 0;
-    for (int z = r.z0; z <= r.z1; z++) {
-      for (int y = r.y0; y <= r.y1; y++) {
-        long rb = r.base + ((long) z * r.ny + y) * r.nx;
-        int s = cell_start[rb + r.x0], e = cell_start[rb + r.x1 + 1];
-        for (int j = lane; j < e - s; j += 32) {
-          s_id[w][k + j] = order[s + j];
-          s_slot[w][k + j] = s + j;
-        }
-        k += e - s;
-      }
-    }
-    __syncwarp();
-    for (int e = lane; e < count; e += 32) {
-      int id = s_id[w][e];
-      int rank = 0;
-      for (int f = 0; f < count; f++) rank += s_id[w][f] < id;
-      nb_list[base_out + rank] = s_slot[w][e];
-    }
-    return;
-  }
-  for (int e = lane; e < count; e += 32) {
-    int se = -1, k = 0;
-    for (int z = r.z0; z <= r.z1 && se < 0; z++) {
-      for (int y = r.y0; y <= r.y1; y++) {
-        long rb = r.base + ((long) z * r.ny + y) * r.nx;
-        int s = cell_start[rb + r.x0], len = cell_start[rb + r.x1 + 1] - s;
-        if (e < k + len) {
-          se = s + (e - k);
-          break;
-        }
-        k += len;
-      }
-    }
-    int id = order[se];
-    int rank = 0;
-    for (int z = r.z0; z <= r.z1; z++) {
-      for (int y = r.y0; y <= r.y1; y++) {
-        long rb = r.base + ((long) z * r.ny + y) * r.nx;
-        int s = cell_start[rb + r.x0], e2 = cell_start[rb + r.x1 + 1];
-        for (int j = s; j < e2; j++) rank += order[j] < id;
-      }
-    }
-    nb_list[base_out + rank] = se;
-  }
-}
 
 struct EnsType {
   const abl_agent_desc *d = nullptr;
@@ -1974,7 +2125,7 @@ struct EnsType {
   long *d_base = nullptr;
   bool uploaded = false;
   // binning
-  bool is_near = false, ordered = false, dirty = true;
+  bool is_near = false, ordered = false, rows = false, dirty = true;
   uint32_t gather_mask = 0;
   std::vector<EnsGrid> grids;
   EnsGrid *d_grids = nullptr;
@@ -1985,6 +2136,7 @@ struct EnsType {
   float *posf = nullptr, *amax = nullptr;
   void *gcols[ABL_MAX_MEMBERS] = {};
   int *nb_cnt = nullptr, *nb_off = nullptr, *nb_list = nullptr;
+  SepLevels sep;
   ScanPlan cell_scan, nb_scan;
   std::vector<void *> allocs;
 };
@@ -2005,6 +2157,8 @@ struct abl_ensemble {
   int block = 128;
   double cell_factor = 1.0;
   int visit_sorted = 1;
+  int balance = 1;
+  std::vector<size_t> smem;  // per step: dynamic shared memory of its kernel
   std::vector<abl_ctx::Graph> graphs;
   long timestep = 0;
 };
@@ -2018,6 +2172,7 @@ void ens_free_bins(abl_ensemble *e, EnsType &t) {
   t.nb_scan.levels.clear();
   t.cell_count = t.cell_start = t.local_rank = t.cell_of = t.order = nullptr;
   t.nb_cnt = t.nb_off = t.nb_list = t.cell_replica = nullptr;
+  t.sep = SepLevels();
   t.posf = t.amax = nullptr;
   t.d_grids = nullptr;
   for (auto &g : t.gcols) g = nullptr;
@@ -2035,17 +2190,21 @@ int ens_prepare(abl_ensemble *e) {
   for (void *p : e->view_allocs) dev_free(ctx, p);
   e->view_allocs.clear();
   e->d_views.assign(m->num_steps, nullptr);
+  e->smem.assign(m->num_steps, 0);
   for (int ti = 0; ti < m->num_agent_types; ti++) {
     EnsType &t = e->types[ti];
     ens_free_bins(e, t);
     t.is_near = false;
     t.ordered = false;
+    t.rows = false;
     t.gather_mask = 0;
     for (int k = 0; k < m->num_steps; k++) {
       const abl_step_desc &sd = m->steps[k];
       if (sd.near_type != ti) continue;
       t.is_near = true;
-      t.ordered = t.ordered || sd.ordered;
+      const int depth = list_depth(sd, *t.d, ctx->near_mode);
+      t.ordered = t.ordered || depth == 2;
+      t.rows = t.rows || depth == 1;
       t.gather_mask |= sd.near_members;
     }
     auto *own = &t.allocs;
@@ -2068,6 +2227,7 @@ int ens_prepare(abl_ensemble *e) {
       double cell = gran * (1.0 + 1.0 / 1024.0) * std::max(1.0, e->cell_factor);
       EnsGrid &g = t.grids[r];
       g.R = std::max(1, (int) std::ceil(rmax * (1.0 + 1e-6) / cell));
+      if (2 * g.R + 1 > kSepMaxSrc) return ABL_E_UNSUPPORTED;
       g.inv_cell = 1.0 / cell;
       int dims[3] = {1, 1, 1};
       for (int d = 0; d < 3; d++) {
@@ -2115,15 +2275,23 @@ int ens_prepare(abl_ensemble *e) {
         t.gcols[k] = p;
       }
     }
-    if (t.ordered) {
+    if (t.ordered || t.rows) {
       int Rmax = 1;
       for (auto &g : t.grids) Rmax = std::max(Rmax, g.R);
-      long span = 2 * Rmax + 1;
-      long per_agent = dim == 3 ? span * span * span : span * span;
+      long span = 2 * Rmax + 1, level = n;
+      const int inter = t.ordered ? dim - 1 : 1;
+      for (int a = 0; a < inter; a++) {
+        level *= span;
+        ABL_TRY(dev_alloc_t(ctx, &t.sep.off[a], cells + 1, own));
+        ABL_TRY(dev_alloc_t(ctx, &t.sep.pair[a], level, own));
+      }
+      if (level * (t.ordered ? span : 1) > (long) INT32_MAX) return ABL_E_UNSUPPORTED;
       ABL_TRY(dev_alloc_t(ctx, &t.nb_cnt, cells, own));
-      ABL_TRY(dev_alloc_t(ctx, &t.nb_off, cells + 1, own));
-      ABL_TRY(dev_alloc_t(ctx, &t.nb_list, per_agent * n, own));
       ABL_TRY(scan_plan(ctx, t.nb_scan, cells, own));
+      if (t.ordered) {
+        ABL_TRY(dev_alloc_t(ctx, &t.nb_off, cells + 1, own));
+        ABL_TRY(dev_alloc_t(ctx, &t.nb_list, level * span, own));
+      }
     }
     t.dirty = true;
   }
@@ -2137,8 +2305,11 @@ int ens_prepare(abl_ensemble *e) {
       const EnsGrid &g = nt.grids[r];
       abl_near_view &V = views[r];
       std::memset(&V, 0, sizeof V);
+      const int depth = list_depth(sd, *nt.d, ctx->near_mode);
       V.dim = nt.d->dim;
-      V.ordered = sd.ordered;
+      V.ordered = depth == 2;
+      V.rows = depth == 1 ? nt.sep.pair[0] : nullptr;
+      V.row_off = nt.sep.off[0] ? nt.sep.off[0] + g.cell_base : nullptr;
       V.range = g.R;
       V.nx = g.nx;
       V.ny = g.ny;
@@ -2154,10 +2325,13 @@ int ens_prepare(abl_ensemble *e) {
       V.nb_list = nt.nb_list;
       V.amax = nt.amax;
       for (int j = 0; j < nt.d->num_members; j++) V.cols[j] = nt.gcols[j];
+      V.balance = e->balance;
+      V.cap = V.ordered ? ctx->list_cap : ctx->runs_cap;
     }
+    e->smem[k] = sd.presorted ? abl::presort_bytes(views[0]) : 0;
     abl_near_view *dv = nullptr;
-    ABL_TRY(dev_alloc_t(ctx, &dv, e->replicas, &e->view_allocs));
-    ABL_CUDA_TRY(cudaMemcpy(dv, views.data(), sizeof(abl_near_view) * e->replicas,
+    ABL_TRY(dev_alloc_t(ctx, &dv, views.size(), &e->view_allocs));
+    ABL_CUDA_TRY(cudaMemcpy(dv, views.data(), sizeof(abl_near_view) * views.size(),
                             cudaMemcpyHostToDevice));
     e->d_views[k] = dv;
   }
@@ -2186,6 +2360,8 @@ void ens_launch_bin(abl_ensemble *e, EnsType &t) {
   scan_run(ctx, t.cell_scan, t.cell_count, t.cell_start);
   k_bin_scatter<<<nb, B, 0, s>>>(t.n, t.cell_of, t.local_rank, t.cell_start, t.order);
   ctx->launches++;
+  k_cell_sort<<<blocks_for(t.ncells, B), B, 0, s>>>(t.ncells, t.cell_start, t.order);
+  ctx->launches++;
   GatherArgs g;
   std::memset(&g, 0, sizeof g);
   for (int k = 0; k < t.d->num_members; k++) {
@@ -2198,20 +2374,10 @@ void ens_launch_bin(abl_ensemble *e, EnsType &t) {
   if (dim == 2) k_gather<Real, 2><<<nb, B, 0, s>>>(t.n, t.order, pos, t.posf, g);
   else k_gather<Real, 3><<<nb, B, 0, s>>>(t.n, t.order, pos, t.posf, g);
   ctx->launches++;
-  if (t.ordered) {
-    long cb = blocks_for(t.ncells, B);
-    if (dim == 2) k_ens_nb_count<2><<<cb, B, 0, s>>>(t.ncells, t.cell_replica, t.d_grids,
-                                                     t.cell_start, t.nb_cnt);
-    else k_ens_nb_count<3><<<cb, B, 0, s>>>(t.ncells, t.cell_replica, t.d_grids, t.cell_start,
-                                            t.nb_cnt);
-    ctx->launches++;
-    scan_run(ctx, t.nb_scan, t.nb_cnt, t.nb_off);
-    long lb = blocks_for(t.ncells, kListWarpsPerBlock);
-    if (dim == 2) k_ens_nb_build<2><<<lb, 32 * kListWarpsPerBlock, 0, s>>>(
-        t.ncells, t.cell_replica, t.d_grids, t.cell_start, t.order, t.nb_off, t.nb_list);
-    else k_ens_nb_build<3><<<lb, 32 * kListWarpsPerBlock, 0, s>>>(
-        t.ncells, t.cell_replica, t.d_grids, t.cell_start, t.order, t.nb_off, t.nb_list);
-    ctx->launches++;
+  if (t.ordered || t.rows) {
+    EnsGeom geo{t.cell_replica, t.d_grids};
+    build_lists(ctx, geo, dim, t.ordered ? dim : 1, t.ncells, t.cell_start, t.order, t.sep,
+                t.nb_cnt, t.nb_scan, t.nb_off, t.nb_list);
   }
   t.dirty = false;
 }
@@ -2242,6 +2408,7 @@ int ens_step_once(abl_ensemble *e) {
     L.replica = t.replica_of;
     L.globals = e->d_globals;
     L.views = sd.near_type >= 0 ? e->d_views[k] : nullptr;
+    L.smem = e->smem[k];
     L.agent_base = t.d_base;
     L.seeds = e->d_seeds;
     L.timestep = e->timestep;

@@ -124,7 +124,7 @@ __device__ static void update_boid(const abl_globals &abl_G, const abl_near_view
     int collision_count = 0;
     {
         const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
-        abl::near_cursor<2> abl_c1(abl_NB, abl_q1);
+        abl::near_list_cursor<2> abl_c1(abl_NB, abl_q1, abl_K);
         auto abl_exact1 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, in->pos) > abl_G.interaction_radius);
@@ -193,7 +193,21 @@ struct abl_kargs_update_boid {
     int step_index;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_update_boid(const __grid_constant__ abl_kargs_update_boid A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const abl_globals &abl_G = A.G;
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
+        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.interaction_radius);
+        };
+        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
@@ -202,6 +216,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_update_boid(const _
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = abl_j;
     Boid abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.velocity = A.in.velocity[abl_i];
@@ -227,11 +242,27 @@ static int abl_launch_update_boid(const abl_step_launch *L, cudaStream_t abl_str
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_update_boid<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_update_boid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_update_boid(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
+        const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
+        const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
+        const abl_near_view &abl_V1 = A.views[abl_r1];
+        const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.interaction_radius);
+        };
+        abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
@@ -242,6 +273,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_update_boid(con
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = abl_j;
     Boid abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.velocity = ((const float2 *) A.in_cols[1])[abl_i];
@@ -252,7 +284,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_update_boid(con
 static int abl_launch_ens_update_boid(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_update_boid<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_update_boid<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_update_boid(const void *abl_gp) {
@@ -296,7 +328,7 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"update_boid", 0, 0, 1, abl_radius_update_boid, 3u, 3u, abl_launch_update_boid, 0, -1, 0, abl_launch_ens_update_boid, 0},
+    {"update_boid", 0, 0, 1, abl_radius_update_boid, 3u, 3u, abl_launch_update_boid, 0, -1, 0, abl_launch_ens_update_boid, 0, 1},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],

@@ -104,7 +104,7 @@ __device__ static void move_point(const abl_globals &abl_G, const abl_near_view 
     float2 new_pos = in->pos;
     {
         const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
-        abl::near_cursor<2> abl_c1(abl_NB, abl_q1);
+        abl::near_list_cursor<2> abl_c1(abl_NB, abl_q1, abl_K);
         auto abl_exact1 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, in->pos) > (2.0 * abl_G.r));
@@ -147,7 +147,21 @@ struct abl_kargs_move_point {
     int step_index;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_move_point(const __grid_constant__ abl_kargs_move_point A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const abl_globals &abl_G = A.G;
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
+        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > (2.0 * abl_G.r));
+        };
+        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
@@ -156,6 +170,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_move_point(const __
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = abl_j;
     Point abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     move_point(A.G, A.NB, abl_K, &abl_in, &abl_out);
@@ -177,11 +192,27 @@ static int abl_launch_move_point(const abl_step_launch *L, cudaStream_t abl_stre
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_move_point<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_move_point<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_move_point(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
+        const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
+        const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
+        const abl_near_view &abl_V1 = A.views[abl_r1];
+        const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > (2.0 * abl_G.r));
+        };
+        abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
@@ -192,6 +223,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_move_point(cons
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = abl_j;
     Point abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     move_point(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
@@ -200,7 +232,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_move_point(cons
 static int abl_launch_ens_move_point(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_move_point<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_move_point<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_move_point(const void *abl_gp) {
@@ -238,7 +270,7 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"move_point", 0, 0, 1, abl_radius_move_point, 1u, 1u, abl_launch_move_point, 0, -1, 0, abl_launch_ens_move_point, 0},
+    {"move_point", 0, 0, 1, abl_radius_move_point, 1u, 1u, abl_launch_move_point, 0, -1, 0, abl_launch_ens_move_point, 0, 1},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],

@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_step_move(const __g
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = -1;
     Cell abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.alive = A.in.alive[abl_i];
@@ -180,7 +181,7 @@ static int abl_launch_step_move(const abl_step_launch *L, cudaStream_t abl_strea
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_step_move<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_step_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_step_move(const __grid_constant__ abl_ens_launch A) {
@@ -195,6 +196,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_step_move(const
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = -1;
     Cell abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.alive = ((const bool *) A.in_cols[1])[abl_i];
@@ -206,7 +208,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_step_move(const
 static int abl_launch_ens_step_move(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_step_move<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_step_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_step_move(const void *abl_gp) {
@@ -251,7 +253,7 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"step_move", 0, 0, 0, abl_radius_step_move, 3u, 1u, abl_launch_step_move, 0, -1, 0, abl_launch_ens_step_move, 0},
+    {"step_move", 0, 0, 0, abl_radius_step_move, 3u, 1u, abl_launch_step_move, 0, -1, 0, abl_launch_ens_step_move, 0, 0},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],

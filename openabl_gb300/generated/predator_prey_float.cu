@@ -207,7 +207,7 @@ __device__ static void prey_avoid_pred(const abl_globals &abl_G, const abl_near_
     float2 avoid_velocity = float2_fill(0.0);
     {
         const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
-        abl::near_cursor<2> abl_c1(abl_NB, abl_q1);
+        abl::near_list_cursor<2> abl_c1(abl_NB, abl_q1, abl_K);
         auto abl_exact1 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, in->pos) > abl_G.PRED_PREY_INTERACTION_RADIUS);
@@ -246,7 +246,21 @@ struct abl_kargs_prey_avoid_pred {
     int step_index;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_avoid_pred(const __grid_constant__ abl_kargs_prey_avoid_pred A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const abl_globals &abl_G = A.G;
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
+        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.PRED_PREY_INTERACTION_RADIUS);
+        };
+        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
@@ -255,6 +269,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_avoid_pred(con
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = abl_j;
     Prey abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -289,11 +304,27 @@ static int abl_launch_prey_avoid_pred(const abl_step_launch *L, cudaStream_t abl
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_prey_avoid_pred<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_prey_avoid_pred<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_avoid_pred(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
+        const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
+        const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
+        const abl_near_view &abl_V1 = A.views[abl_r1];
+        const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.PRED_PREY_INTERACTION_RADIUS);
+        };
+        abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
@@ -304,6 +335,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_avoid_pred
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = abl_j;
     Prey abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
@@ -322,7 +354,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_avoid_pred
 static int abl_launch_ens_prey_avoid_pred(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_prey_avoid_pred<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_prey_avoid_pred<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_prey_avoid_pred(const void *abl_gp) {
@@ -341,7 +373,7 @@ __device__ static void prey_flock(const abl_globals &abl_G, const abl_near_view 
     int group_centre_count = 0;
     {
         const abl::near_query<2> abl_q2(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
-        abl::near_cursor<2> abl_c2(abl_NB, abl_q2);
+        abl::near_list_cursor<2> abl_c2(abl_NB, abl_q2, abl_K);
         auto abl_exact2 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, in->pos) > abl_G.PREY_GROUP_COHESION_RADIUS);
@@ -386,7 +418,21 @@ struct abl_kargs_prey_flock {
     int step_index;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_flock(const __grid_constant__ abl_kargs_prey_flock A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const abl_globals &abl_G = A.G;
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
+        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.PREY_GROUP_COHESION_RADIUS);
+        };
+        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
@@ -395,6 +441,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_flock(const __
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = abl_j;
     Prey abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -429,11 +476,27 @@ static int abl_launch_prey_flock(const abl_step_launch *L, cudaStream_t abl_stre
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_prey_flock<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_prey_flock<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_flock(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
+        const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
+        const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
+        const abl_near_view &abl_V1 = A.views[abl_r1];
+        const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.PREY_GROUP_COHESION_RADIUS);
+        };
+        abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
@@ -444,6 +507,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_flock(cons
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = abl_j;
     Prey abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
@@ -462,7 +526,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_flock(cons
 static int abl_launch_ens_prey_flock(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_prey_flock<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_prey_flock<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_prey_flock(const void *abl_gp) {
@@ -511,6 +575,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_move(const __g
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = -1;
     Prey abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -545,7 +610,7 @@ static int abl_launch_prey_move(const abl_step_launch *L, cudaStream_t abl_strea
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_prey_move<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_prey_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_move(const __grid_constant__ abl_ens_launch A) {
@@ -560,6 +625,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_move(const
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = -1;
     Prey abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
@@ -578,7 +644,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_move(const
 static int abl_launch_ens_prey_move(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_prey_move<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_prey_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 
@@ -589,7 +655,7 @@ __device__ static void prey_eaten(const abl_globals &abl_G, const abl_near_view 
     float closest_pred = abl_G.PRED_KILL_DISTANCE;
     {
         const abl::near_query<2> abl_q3(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
-        abl::near_cursor<2> abl_c3(abl_NB, abl_q3);
+        abl::near_list_cursor<2> abl_c3(abl_NB, abl_q3, abl_K);
         auto abl_exact3 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, in->pos) > abl_G.PRED_KILL_DISTANCE);
@@ -627,7 +693,21 @@ struct abl_kargs_prey_eaten {
     int step_index;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_eaten(const __grid_constant__ abl_kargs_prey_eaten A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const abl_globals &abl_G = A.G;
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
+        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.PRED_KILL_DISTANCE);
+        };
+        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
@@ -636,6 +716,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_eaten(const __
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = abl_j;
     Prey abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -671,7 +752,7 @@ static int abl_launch_prey_eaten(const abl_step_launch *L, cudaStream_t abl_stre
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_prey_eaten<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_prey_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_prey_eaten(const void *abl_gp) {
@@ -731,6 +812,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_eat_or_starve(
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = -1;
     Prey abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -766,7 +848,7 @@ static int abl_launch_prey_eat_or_starve(const abl_step_launch *L, cudaStream_t 
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_prey_eat_or_starve<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_prey_eat_or_starve<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_prey_eat_or_starve(const void *abl_gp) {
@@ -808,6 +890,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_reproduction(c
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = -1;
     Prey abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -843,7 +926,7 @@ static int abl_launch_prey_reproduction(const abl_step_launch *L, cudaStream_t a
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_prey_reproduction<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_prey_reproduction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 
@@ -857,7 +940,7 @@ __device__ static void pred_follow_prey(const abl_globals &abl_G, const abl_near
     bool can_see_prey = false;
     {
         const abl::near_query<2> abl_q5(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
-        abl::near_cursor<2> abl_c5(abl_NB, abl_q5);
+        abl::near_list_cursor<2> abl_c5(abl_NB, abl_q5, abl_K);
         auto abl_exact5 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, in->pos) > abl_G.PRED_PREY_INTERACTION_RADIUS);
@@ -899,7 +982,21 @@ struct abl_kargs_pred_follow_prey {
     int step_index;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_follow_prey(const __grid_constant__ abl_kargs_pred_follow_prey A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const abl_globals &abl_G = A.G;
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
+        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.PRED_PREY_INTERACTION_RADIUS);
+        };
+        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
@@ -908,6 +1005,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_follow_prey(co
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = abl_j;
     Predator abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -942,11 +1040,27 @@ static int abl_launch_pred_follow_prey(const abl_step_launch *L, cudaStream_t ab
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_pred_follow_prey<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_pred_follow_prey<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_follow_prey(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
+        const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
+        const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
+        const abl_near_view &abl_V1 = A.views[abl_r1];
+        const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.PRED_PREY_INTERACTION_RADIUS);
+        };
+        abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
@@ -957,6 +1071,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_follow_pre
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = abl_j;
     Predator abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
@@ -975,7 +1090,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_follow_pre
 static int abl_launch_ens_pred_follow_prey(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_pred_follow_prey<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_pred_follow_prey<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_pred_follow_prey(const void *abl_gp) {
@@ -991,7 +1106,7 @@ __device__ static void pred_avoid(const abl_globals &abl_G, const abl_near_view 
     float2 avoid_velocity = float2_create(0, 0);
     {
         const abl::near_query<2> abl_q6(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
-        abl::near_cursor<2> abl_c6(abl_NB, abl_q6);
+        abl::near_list_cursor<2> abl_c6(abl_NB, abl_q6, abl_K);
         auto abl_exact6 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, in->pos) > abl_G.SAME_SPECIES_AVOIDANCE_RADIUS);
@@ -1028,7 +1143,21 @@ struct abl_kargs_pred_avoid {
     int step_index;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_avoid(const __grid_constant__ abl_kargs_pred_avoid A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const abl_globals &abl_G = A.G;
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
+        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.SAME_SPECIES_AVOIDANCE_RADIUS);
+        };
+        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
@@ -1037,6 +1166,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_avoid(const __
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = abl_j;
     Predator abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -1071,11 +1201,27 @@ static int abl_launch_pred_avoid(const abl_step_launch *L, cudaStream_t abl_stre
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_pred_avoid<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_pred_avoid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_avoid(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
+        const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
+        const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
+        const abl_near_view &abl_V1 = A.views[abl_r1];
+        const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.SAME_SPECIES_AVOIDANCE_RADIUS);
+        };
+        abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
@@ -1086,6 +1232,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_avoid(cons
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = abl_j;
     Predator abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
@@ -1104,7 +1251,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_avoid(cons
 static int abl_launch_ens_pred_avoid(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_pred_avoid<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_pred_avoid<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_pred_avoid(const void *abl_gp) {
@@ -1155,6 +1302,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_move(const __g
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = -1;
     Predator abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -1189,7 +1337,7 @@ static int abl_launch_pred_move(const abl_step_launch *L, cudaStream_t abl_strea
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_pred_move<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_pred_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_move(const __grid_constant__ abl_ens_launch A) {
@@ -1204,6 +1352,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_move(const
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = -1;
     Predator abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.dir = ((const float2 *) A.in_cols[1])[abl_i];
@@ -1222,7 +1371,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_move(const
 static int abl_launch_ens_pred_move(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_pred_move<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_pred_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 
@@ -1275,6 +1424,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_eat_or_starve(
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = -1;
     Predator abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -1310,7 +1460,7 @@ static int abl_launch_pred_eat_or_starve(const abl_step_launch *L, cudaStream_t 
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_pred_eat_or_starve<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_pred_eat_or_starve<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_pred_eat_or_starve(const void *abl_gp) {
@@ -1352,6 +1502,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_reproduction(c
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = -1;
     Predator abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dir = A.in.dir[abl_i];
@@ -1387,7 +1538,7 @@ static int abl_launch_pred_reproduction(const abl_step_launch *L, cudaStream_t a
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_pred_reproduction<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_pred_reproduction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 
@@ -1398,7 +1549,7 @@ __device__ static void grass_eaten(const abl_globals &abl_G, const abl_near_view
     bool eaten = false;
     {
         const abl::near_query<2> abl_q8(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
-        abl::near_cursor<2> abl_c8(abl_NB, abl_q8);
+        abl::near_list_cursor<2> abl_c8(abl_NB, abl_q8, abl_K);
         auto abl_exact8 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, in->pos) > abl_G.GRASS_EAT_DISTANCE);
@@ -1439,7 +1590,21 @@ struct abl_kargs_grass_eaten {
     int step_index;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_grass_eaten(const __grid_constant__ abl_kargs_grass_eaten A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const abl_globals &abl_G = A.G;
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
+        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.GRASS_EAT_DISTANCE);
+        };
+        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
@@ -1448,6 +1613,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_grass_eaten(const _
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = abl_j;
     Grass abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dead_cycles = A.in.dead_cycles[abl_i];
@@ -1478,11 +1644,27 @@ static int abl_launch_grass_eaten(const abl_step_launch *L, cudaStream_t abl_str
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_grass_eaten<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_grass_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_grass_eaten(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    int abl_j;
+    {
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
+        const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
+        const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
+        const abl_near_view &abl_V1 = A.views[abl_r1];
+        const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.GRASS_EAT_DISTANCE);
+        };
+        abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
@@ -1493,6 +1675,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_grass_eaten(con
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = abl_j;
     Grass abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.dead_cycles = ((const int *) A.in_cols[1])[abl_i];
@@ -1508,7 +1691,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_grass_eaten(con
 static int abl_launch_ens_grass_eaten(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_grass_eaten<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_grass_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 static double abl_radius_grass_eaten(const void *abl_gp) {
@@ -1552,6 +1735,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_grass_growth(const 
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
+    abl_K.near_col = -1;
     Grass abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.dead_cycles = A.in.dead_cycles[abl_i];
@@ -1582,7 +1766,7 @@ static int abl_launch_grass_growth(const abl_step_launch *L, cudaStream_t abl_st
     A.step_index = L->step_index;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
-    abl_kernel_grass_growth<<<abl_grid, abl_block, 0, abl_stream>>>(A);
+    abl_kernel_grass_growth<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_grass_growth(const __grid_constant__ abl_ens_launch A) {
@@ -1597,6 +1781,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_grass_growth(co
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
+    abl_K.near_col = -1;
     Grass abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.dead_cycles = ((const int *) A.in_cols[1])[abl_i];
@@ -1612,7 +1797,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_grass_growth(co
 static int abl_launch_ens_grass_growth(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_grass_growth<<<abl_grid, abl_block, 0, abl_stream>>>(*L);
+    abl_kernel_ens_grass_growth<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 
@@ -1684,19 +1869,19 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"prey_avoid_pred", 1, 0, 1, abl_radius_prey_avoid_pred, 1u, 4u, abl_launch_prey_avoid_pred, 0, -1, 1, abl_launch_ens_prey_avoid_pred, 0},
-    {"prey_flock", 1, 1, 1, abl_radius_prey_flock, 1u, 4u, abl_launch_prey_flock, 0, -1, 1, abl_launch_ens_prey_flock, 0},
-    {"prey_move", 1, -1, 1, nullptr, 0u, 11u, abl_launch_prey_move, 0, -1, 1, abl_launch_ens_prey_move, 0},
-    {"prey_eaten", 1, 0, 1, abl_radius_prey_eaten, 1u, 0u, abl_launch_prey_eaten, 1, -1, 1, nullptr, 0},
-    {"prey_eat_or_starve", 1, 2, 0, abl_radius_prey_eat_or_starve, 5u, 8u, abl_launch_prey_eat_or_starve, 1, -1, 1, nullptr, 0},
-    {"prey_reproduction", 1, -1, 1, nullptr, 0u, 0u, abl_launch_prey_reproduction, 0, 1, 1, nullptr, 1},
-    {"pred_follow_prey", 0, 1, 1, abl_radius_pred_follow_prey, 1u, 4u, abl_launch_pred_follow_prey, 0, -1, 1, abl_launch_ens_pred_follow_prey, 0},
-    {"pred_avoid", 0, 0, 1, abl_radius_pred_avoid, 1u, 4u, abl_launch_pred_avoid, 0, -1, 1, abl_launch_ens_pred_avoid, 0},
-    {"pred_move", 0, -1, 1, nullptr, 0u, 11u, abl_launch_pred_move, 0, -1, 1, abl_launch_ens_pred_move, 0},
-    {"pred_eat_or_starve", 0, 1, 0, abl_radius_pred_eat_or_starve, 1u, 8u, abl_launch_pred_eat_or_starve, 1, -1, 1, nullptr, 0},
-    {"pred_reproduction", 0, -1, 1, nullptr, 0u, 0u, abl_launch_pred_reproduction, 0, 0, 1, nullptr, 1},
-    {"grass_eaten", 2, 1, 1, abl_radius_grass_eaten, 1u, 0u, abl_launch_grass_eaten, 0, -1, 1, abl_launch_ens_grass_eaten, 0},
-    {"grass_growth", 2, -1, 1, nullptr, 0u, 0u, abl_launch_grass_growth, 0, -1, 1, abl_launch_ens_grass_growth, 0},
+    {"prey_avoid_pred", 1, 0, 1, abl_radius_prey_avoid_pred, 1u, 4u, abl_launch_prey_avoid_pred, 0, -1, 1, abl_launch_ens_prey_avoid_pred, 0, 1},
+    {"prey_flock", 1, 1, 1, abl_radius_prey_flock, 1u, 4u, abl_launch_prey_flock, 0, -1, 1, abl_launch_ens_prey_flock, 0, 1},
+    {"prey_move", 1, -1, 1, nullptr, 0u, 11u, abl_launch_prey_move, 0, -1, 1, abl_launch_ens_prey_move, 0, 0},
+    {"prey_eaten", 1, 0, 1, abl_radius_prey_eaten, 1u, 0u, abl_launch_prey_eaten, 1, -1, 1, nullptr, 0, 1},
+    {"prey_eat_or_starve", 1, 2, 0, abl_radius_prey_eat_or_starve, 5u, 8u, abl_launch_prey_eat_or_starve, 1, -1, 1, nullptr, 0, 0},
+    {"prey_reproduction", 1, -1, 1, nullptr, 0u, 0u, abl_launch_prey_reproduction, 0, 1, 1, nullptr, 1, 0},
+    {"pred_follow_prey", 0, 1, 1, abl_radius_pred_follow_prey, 1u, 4u, abl_launch_pred_follow_prey, 0, -1, 1, abl_launch_ens_pred_follow_prey, 0, 1},
+    {"pred_avoid", 0, 0, 1, abl_radius_pred_avoid, 1u, 4u, abl_launch_pred_avoid, 0, -1, 1, abl_launch_ens_pred_avoid, 0, 1},
+    {"pred_move", 0, -1, 1, nullptr, 0u, 11u, abl_launch_pred_move, 0, -1, 1, abl_launch_ens_pred_move, 0, 0},
+    {"pred_eat_or_starve", 0, 1, 0, abl_radius_pred_eat_or_starve, 1u, 8u, abl_launch_pred_eat_or_starve, 1, -1, 1, nullptr, 0, 0},
+    {"pred_reproduction", 0, -1, 1, nullptr, 0u, 0u, abl_launch_pred_reproduction, 0, 0, 1, nullptr, 1, 0},
+    {"grass_eaten", 2, 1, 1, abl_radius_grass_eaten, 1u, 0u, abl_launch_grass_eaten, 0, -1, 1, abl_launch_ens_grass_eaten, 0, 1},
+    {"grass_growth", 2, -1, 1, nullptr, 0u, 0u, abl_launch_grass_growth, 0, -1, 1, abl_launch_ens_grass_growth, 0, 0},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[6],

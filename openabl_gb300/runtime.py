@@ -320,6 +320,20 @@ class Simulation:
         L.abl_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _check(L.abl_set_profiling(self.ctx, 1 if enable else 0), "abl_set_profiling")
 
+    NEAR_AUTO, NEAR_RUNS, NEAR_ROWS, NEAR_LISTS = 0, 1, 2, 3
+
+    def set_near_mode(self, mode):
+        """How ordered near loops gather neighbours (results are identical in every mode)."""
+        L = _load()
+        L.abl_set_near_mode.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _check(L.abl_set_near_mode(self.ctx, int(mode)), "abl_set_near_mode")
+
+    def set_balance(self, enable=True):
+        """Hand each block's agents to threads by neighbour count (ordered near loops)."""
+        L = _load()
+        L.abl_set_balance.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _check(L.abl_set_balance(self.ctx, 1 if enable else 0), "abl_set_balance")
+
     def step_kernel_time(self, step=0):
         """(total seconds, launches) of a step function's kernel while profiling."""
         L = _load()
