@@ -402,20 +402,31 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
         << "const " << cType(posMember->type->resolved) << " abl_p = " << posCol << "[abl_s];"
         << nl << "return !(" << distFn << "(abl_p, " << agentExpr << "->" << posMember->name
         << ") > " << radiusExpr << ");" << outdent << nl << "};" << nl
-        << "while (" << c << ".fill(" << q << ", " << ex << ")) {" << indent << nl
-        << "for (int abl_k = 0; abl_k < " << c << ".cnt; ++abl_k) {" << indent << nl
-        << "const int " << slot << " = " << c << ".slot(abl_k);" << nl
-        << agentDecl->name << " " << nxs << ";";
+        << "while (" << c << ".fill(" << q << ", " << ex << ")) {" << indent;
   // Load the members the loop reads (AnalysisVisitor collects them,
-  // src/AnalysisVisitor.cpp:1101-1105).
+  // src/AnalysisVisitor.cpp:1101-1105).  The next neighbour's members are
+  // loaded while the body runs on the current one.
   const AST::FunctionDeclaration *cur = steps.empty() ? nullptr : steps.back().decl;
-  for (size_t k = 0; k < agentDecl->members->size(); k++) {
-    const AST::AgentMember &m = *(*agentDecl->members)[k];
-    bool used = cur && cur->accessedMembers.count(m.name);
-    if (!used) continue;
-    *this << nl << nxs << "." << m.name << " = ((const " << cType(m.type->resolved)
-          << " *) abl_NB.cols[" << (int) k << "])[" << slot << "];";
-  }
+  std::string pslot = "abl_pslot" + sid, pnx = "abl_pnx" + sid;
+  auto loadMembers = [&](const std::string &var, const std::string &at) {
+    for (size_t k = 0; k < agentDecl->members->size(); k++) {
+      const AST::AgentMember &m = *(*agentDecl->members)[k];
+      bool used = cur && cur->accessedMembers.count(m.name);
+      if (!used) continue;
+      *this << nl << var << "." << m.name << " = ((const " << cType(m.type->resolved)
+            << " *) abl_NB.cols[" << (int) k << "])[" << at << "];";
+    }
+  };
+  *this << nl << "int " << pslot << " = " << c << ".slot(0);" << nl << agentDecl->name << " "
+        << pnx << ";";
+  loadMembers(pnx, pslot);
+  *this << nl << "for (int abl_k = 0; abl_k < " << c << ".cnt; ++abl_k) {" << indent << nl
+        << "const int " << slot << " = " << pslot << ";" << nl
+        << agentDecl->name << " " << nxs << " = " << pnx << ";" << nl
+        << "if (abl_k + 1 < " << c << ".cnt) {" << indent << nl
+        << pslot << " = " << c << ".slot(abl_k + 1);";
+  loadMembers(pnx, pslot);
+  *this << outdent << nl << "}";
   *this << nl << agentDecl->name << "* " << *stmt.var << " = &" << nxs << ";" << nl;
 
   std::string savedLabel = nearEndLabel;
@@ -634,7 +645,7 @@ void CudaPrinter::printKernel(const StepInfo &info) {
         << "uint8_t *removed;" << nl << "uint8_t *child_flag;" << nl
         << "void *child_cols[ABL_MAX_MEMBERS];" << nl << "uint64_t seed;" << nl
         << "long timestep;" << nl << "int step_index;" << outdent << nl << "};"
-        << nl << "__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_" << name
+        << nl << "__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_" << name
         << "(const __grid_constant__ abl_kargs_" << name << " A) {" << indent << nl;
   if (info.presorted) {
     *this << "int abl_j;" << nl << "{" << indent << nl
@@ -710,7 +721,7 @@ void CudaPrinter::printKernel(const StepInfo &info) {
     // Ensemble variant: every agent reads its replica's globals and grid.
     // Random numbers are keyed by the replica's seed and the agent's index
     // within its replica, so each replica draws what it would draw alone.
-    *this << "__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_" << name
+    *this << "__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_" << name
           << "(const __grid_constant__ abl_ens_launch A) {" << indent << nl;
     if (info.presorted) {
       int posIdx = memberIndex(&agent, agent.getPositionMember());

@@ -48,6 +48,11 @@
 #ifndef ABL_STEP_BLOCK
 #define ABL_STEP_BLOCK 128
 #endif
+// Resident step-kernel blocks per SM the register allocation must allow
+// (capping registers to fit more blocks spills the FP64 step bodies).
+#ifndef ABL_STEP_MIN_BLOCKS
+#define ABL_STEP_MIN_BLOCKS 1
+#endif
 
 namespace abl {
 
@@ -451,8 +456,9 @@ __device__ int gather_list(const presort_shared &S, const abl_near_view &V,
 
 // Rows mode (2D): the in-radius neighbours with id > lower, taken in
 // ascending id from a three-way merge of the row lists of the cells above,
-// at and below the query cell.  Stores the first S.cap slots in column `col`
-// and returns how many there are in all; `last` receives the id of the last
+// at and below the query cell.  Row list entries carry the float position
+// the prefilter needs.  Stores the first S.cap slots in column `col` and
+// returns how many there are in all; `last` receives the id of the last
 // stored slot.
 template <int DIM, typename Exact>
 __device__ int gather_rows(const presort_shared &S, const abl_near_view &V,
@@ -461,7 +467,8 @@ __device__ int gather_rows(const presort_shared &S, const abl_near_view &V,
   int *L = S.slots + col;
   const int cap = S.cap;
   const int kNone = 0x7fffffff;
-  int pos[3], end[3], hid[3], hsl[3];
+  int pos[3], end[3];
+  int4 h[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     const int y = q.c[1] + k - 1;
@@ -471,49 +478,33 @@ __device__ int gather_rows(const presort_shared &S, const abl_near_view &V,
       pos[k] = __ldg(&V.row_off[u]);
       end[k] = __ldg(&V.row_off[u + 1]);
     }
-    hid[k] = kNone;
-    hsl[k] = 0;
-    if (pos[k] < end[k]) {
-      const int2 v = __ldg(&V.rows[pos[k]]);
-      hid[k] = v.x;
-      hsl[k] = v.y;
-    }
+    h[k] = pos[k] < end[k] ? __ldg(&V.rows[pos[k]]) : make_int4(kNone, 0, 0, 0);
   }
   int n = 0, total = 0;
   last = lower;
   for (;;) {
-    const bool a01 = hid[0] < hid[1];
-    const int m01 = a01 ? hid[0] : hid[1];
-    const int k = hid[2] < m01 ? 2 : (a01 ? 0 : 1);
-    const int id = k == 2 ? hid[2] : m01;
-    if (id == kNone) break;
-    const int s = k == 0 ? hsl[0] : (k == 1 ? hsl[1] : hsl[2]);
+    const bool a01 = h[0].x < h[1].x;
+    const int m01 = a01 ? h[0].x : h[1].x;
+    const int k = h[2].x < m01 ? 2 : (a01 ? 0 : 1);
+    const int4 v = k == 0 ? h[0] : (k == 1 ? h[1] : h[2]);
+    if (v.x == kNone) break;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
       if (j == k) {
         const int e = ++pos[j];
-        hid[j] = kNone;
-        if (e < end[j]) {
-          const int2 v = __ldg(&V.rows[e]);
-          hid[j] = v.x;
-          hsl[j] = v.y;
-        }
+        h[j] = e < end[j] ? __ldg(&V.rows[e]) : make_int4(kNone, 0, 0, 0);
       }
     }
-    if (id <= lower) continue;
-    float d2 = 0.0f;
-#pragma unroll
-    for (int d = 0; d < DIM; d++) {
-      float dd = __ldg(&V.posf[DIM * s + d]) - q.pf[d];
-      d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
-    }
+    if (v.x <= lower) continue;
+    const float dx = __int_as_float(v.z) - q.pf[0], dy = __int_as_float(v.w) - q.pf[1];
+    const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
     if (d2 > q.bd.hi) continue;
-    if (!(d2 < q.bd.lo) && !exact(s)) continue;
+    if (!(d2 < q.bd.lo) && !exact(v.y)) continue;
     total++;
     if (n < cap) {
-      L[n * ABL_STEP_BLOCK] = s;
+      L[n * ABL_STEP_BLOCK] = v.y;
       n++;
-      last = id;
+      last = v.x;
     }
   }
   stored = n;

@@ -59,7 +59,8 @@ typedef struct {
   const int *nb_off;        /* ordered mode: cell -> offset into nb_list (ncells + 1) */
   const int *nb_list;       /* ordered mode: slots, ascending agent id per cell */
   const int *row_off;       /* row lists: cell -> offset into rows (ncells + 1) */
-  const int2 *rows;         /* row lists: (id, slot) of the cells c-1..c+1 along x, ascending id */
+  const int4 *rows;         /* row lists: (id, slot, float x, float y) of the cells c-1..c+1
+                               along x, ascending id */
   const float *amax;        /* max |coordinate| over neighbour and query agents */
   const void *cols[ABL_MAX_MEMBERS]; /* slot-ordered copies of the members the loop reads */
   int balance;              /* presorted mode: hand a block's agents to threads by neighbour count */

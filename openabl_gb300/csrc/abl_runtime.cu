@@ -367,38 +367,30 @@ __global__ void k_sep_count(long ncells, G geo, const int *src_off, int *dst_cnt
 }
 
 // Source lists of one level.  Level 0: the binned slots themselves (list of
-// cell u = slots off[u] .. off[u+1], ids order[slot]); later levels store
-// (id, slot) pairs.
+// cell u = slots off[u] .. off[u+1]); later levels store one element per
+// entry: (id, slot, float x, float y), the float position of the slot being
+// what the radius prefilter reads.
 struct SepSrc {
-  const int *off;    // ncells + 1
-  const int *order;  // level 0
-  const int2 *pair;  // later levels
+  const int *off;     // ncells + 1
+  const int *order;   // level 0: slot -> id
+  const float *posf;  // level 0: slot -> float position (dim per slot)
+  int dim;
+  const int4 *elem;   // later levels
 };
 
-constexpr int kSepMaxSrc = 7;        // source lists per target: 2R + 1 for R <= 3
-constexpr int kSepWarps = 8;         // target cells (warps) per block of k_sep_merge_large
-constexpr int kSepThreads = 128;     // target cells (threads) per block of k_sep_merge
-constexpr int kSepStageInts = 1536;  // per warp of k_sep_merge: staged output ints
-constexpr int kSepSeqMax = 4096;     // longest list merged by one thread
+constexpr int kSepMaxSrc = 7;    // source lists per target: 2R + 1 for R <= 3
+constexpr int kSepWarps = 8;     // target cells (warps) per block of k_sep_merge_large
+constexpr int kSepThreads = 128; // target cells (threads) per block of k_sep_merge
 
-template <bool PAIR>
-__device__ __forceinline__ int2 sep_elem_t(const SepSrc &S, int e) {
-  if (PAIR) return __ldg(&S.pair[e]);
-  return make_int2(__ldg(&S.order[e]), e);
+template <bool LEVEL0>
+__device__ __forceinline__ int4 sep_elem_t(const SepSrc &S, int e) {
+  if (!LEVEL0) return __ldg(&S.elem[e]);
+  return make_int4(__ldg(&S.order[e]), e, __float_as_int(__ldg(&S.posf[S.dim * e])),
+                   __float_as_int(__ldg(&S.posf[S.dim * e + 1])));
 }
 
-__device__ inline int lower_bound_shared(const int *a, int len, int id) {
-  int lo = 0, hi = len;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (a[mid] < id) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-__device__ __forceinline__ int2 sep_elem(const SepSrc &S, int e) {
-  return S.pair ? __ldg(&S.pair[e]) : make_int2(__ldg(&S.order[e]), e);
+__device__ __forceinline__ int4 sep_elem(const SepSrc &S, int e) {
+  return S.elem ? sep_elem_t<false>(S, e) : sep_elem_t<true>(S, e);
 }
 
 __device__ inline int lower_bound_src(const SepSrc &S, int b, int len, int id) {
@@ -431,110 +423,70 @@ __device__ inline int sep_sources(const CellPos &P, long t, const SepSrc &S, int
   return total;
 }
 
-// One thread per target cell with R = 1 and at most kSepSeqMax elements:
-// a three-way merge of the id-sorted source lists.  The 32 cells of a warp
-// own one contiguous output range; when it fits, the outputs are staged in
-// shared memory and stored coalesced.  Other cells are left to
-// k_sep_merge_large (a warp whose range holds such a cell never stages).
-template <typename G, int AXIS, bool PAIR, bool STAGE>
+// One thread per target cell with R = 1: a three-way merge of the id-sorted
+// source lists.  Writes elements (dst_elem) or, for the last level, slots
+// only (dst_slot).  Cells of grids with R > 1 are left to k_sep_merge_large.
+template <typename G, int AXIS, bool LEVEL0>
 __global__ void __launch_bounds__(kSepThreads)
-k_sep_merge(long ncells, G geo, SepSrc S, const int *dst_off, int2 *dst_pair, int *dst_slot) {
-  __shared__ int stage[STAGE ? kSepThreads / 32 : 1][STAGE ? kSepStageInts : 1];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long t0 = (long) blockIdx.x * kSepThreads + 32 * w;
-  if (t0 >= ncells) return;
-  const long t = t0 + lane;
-  const long t1 = t0 + 32 < ncells ? t0 + 32 : ncells;
-  const long o0 = dst_off[t0];
-  const int per = dst_pair ? 2 : 1;
-  const bool staged = STAGE && (dst_off[t1] - o0) * per <= kSepStageInts;
-  int *st = stage[STAGE ? w : 0];
-  if (t < ncells) {
-    const CellPos P = cell_pos(geo, t);
-    const long out0 = dst_off[t];
-    const int total = (int) (dst_off[t + 1] - out0);
-    if (P.R == 1 && total > 0 && total <= kSepSeqMax) {
-      const int kNone = 0x7fffffff;
-      int pos[3], end[3], hid[3], hsl[3];
+k_sep_merge(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_elem, int *dst_slot) {
+  const long t = (long) blockIdx.x * kSepThreads + threadIdx.x;
+  if (t >= ncells) return;
+  const CellPos P = cell_pos(geo, t);
+  const long out0 = dst_off[t];
+  const int total = (int) (dst_off[t + 1] - out0);
+  if (P.R != 1 || total == 0) return;
+  const int kNone = 0x7fffffff;
+  int pos[3], end[3];
+  int4 h[3];
 #pragma unroll
-      for (int k = 0; k < 3; k++) {
-        const long u = axis_neighbour<AXIS>(P, t, k - 1);
-        pos[k] = u >= 0 ? S.off[u] : 0;
-        end[k] = u >= 0 ? S.off[u + 1] : 0;
-        hid[k] = kNone;
-        hsl[k] = 0;
-        if (pos[k] < end[k]) {
-          const int2 v = sep_elem_t<PAIR>(S, pos[k]);
-          hid[k] = v.x;
-          hsl[k] = v.y;
-        }
-      }
-      int o = (int) (out0 - o0);
-      for (int q = 0; q < total; q++) {
-        const bool a01 = hid[0] < hid[1];
-        const int m01 = a01 ? hid[0] : hid[1];
-        const int k = hid[2] < m01 ? 2 : (a01 ? 0 : 1);
-        const int id = k == 2 ? hid[2] : m01;
-        const int sl = k == 0 ? hsl[0] : (k == 1 ? hsl[1] : hsl[2]);
-        if (staged) {
-          if (dst_pair) {
-            st[2 * (o + q)] = id;
-            st[2 * (o + q) + 1] = sl;
-          } else {
-            st[o + q] = sl;
-          }
-        } else if (dst_pair) {
-          dst_pair[out0 + q] = make_int2(id, sl);
-        } else {
-          dst_slot[out0 + q] = sl;
-        }
+  for (int k = 0; k < 3; k++) {
+    const long u = axis_neighbour<AXIS>(P, t, k - 1);
+    pos[k] = u >= 0 ? S.off[u] : 0;
+    end[k] = u >= 0 ? S.off[u + 1] : 0;
+    h[k] = pos[k] < end[k] ? sep_elem_t<LEVEL0>(S, pos[k]) : make_int4(kNone, 0, 0, 0);
+  }
+  for (int q = 0; q < total; q++) {
+    const bool a01 = h[0].x < h[1].x;
+    const int m01 = a01 ? h[0].x : h[1].x;
+    const int k = h[2].x < m01 ? 2 : (a01 ? 0 : 1);
+    const int4 v = k == 0 ? h[0] : (k == 1 ? h[1] : h[2]);
+    if (dst_elem) dst_elem[out0 + q] = v;
+    else dst_slot[out0 + q] = v.y;
 #pragma unroll
-        for (int j = 0; j < 3; j++) {
-          if (j == k) {
-            const int e = ++pos[j];
-            hid[j] = kNone;
-            if (e < end[j]) {
-              const int2 v = sep_elem_t<PAIR>(S, e);
-              hid[j] = v.x;
-              hsl[j] = v.y;
-            }
-          }
-        }
+    for (int j = 0; j < 3; j++) {
+      if (j == k) {
+        const int e = ++pos[j];
+        h[j] = e < end[j] ? sep_elem_t<LEVEL0>(S, e) : make_int4(kNone, 0, 0, 0);
       }
     }
   }
-  if (!staged) return;
-  __syncwarp();
-  const int m = (int) (dst_off[t1] - o0) * per;
-  int *dst = dst_pair ? (int *) dst_pair : dst_slot;
-  for (int i = lane; i < m; i += 32) dst[per * o0 + i] = st[i];
 }
 
-// One warp per target cell that k_sep_merge leaves (R != 1 or more than
-// kSepStage source elements): an element's place is its index in its own
-// source list plus a binary search in every other source list.
+// One warp per target cell of a grid with R > 1: an element's place is its
+// index in its own source list plus a binary search in every other source
+// list.
 template <typename G, int AXIS>
 __global__ void __launch_bounds__(32 * kSepWarps)
-k_sep_merge_large(long ncells, G geo, SepSrc S, const int *dst_off, int2 *dst_pair,
+k_sep_merge_large(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_elem,
                   int *dst_slot) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long t = (long) blockIdx.x * kSepWarps + w;
   if (t >= ncells) return;
   const CellPos P = cell_pos(geo, t);
-  if (P.R == 1 && dst_off[t + 1] - dst_off[t] <= kSepSeqMax) return;
+  if (P.R == 1) return;
   int b[kSepMaxSrc], n[kSepMaxSrc];
   sep_sources<AXIS>(P, t, S, b, n);
   const long out = dst_off[t];
 #pragma unroll
   for (int k = 0; k < kSepMaxSrc; k++) {
     for (int j = lane; j < n[k]; j += 32) {
-      const int2 v = sep_elem(S, b[k] + j);
+      const int4 v = sep_elem(S, b[k] + j);
       int rank = j;
 #pragma unroll
       for (int k2 = 0; k2 < kSepMaxSrc; k2++) {
         if (k2 != k && n[k2] > 0) rank += lower_bound_src(S, b[k2], n[k2], v.x);
       }
-      if (dst_pair) dst_pair[out + rank] = v;
+      if (dst_elem) dst_elem[out + rank] = v;
       else dst_slot[out + rank] = v.y;
     }
   }
@@ -543,7 +495,7 @@ k_sep_merge_large(long ncells, G geo, SepSrc S, const int *dst_off, int2 *dst_pa
 // Intermediate levels of the separable list build (dim - 1 of them).
 struct SepLevels {
   int *off[2] = {nullptr, nullptr};
-  int2 *pair[2] = {nullptr, nullptr};
+  int4 *elem[2] = {nullptr, nullptr};
 };
 
 // --------------------------------------------------------------- state
@@ -887,7 +839,7 @@ int prepare(abl_ctx *ctx) {
       for (int a = 0; a < inter; a++) {
         level *= span;
         ABL_TRY(dev_alloc_t(ctx, &g.sep.off[a], g.ncells + 1, own));
-        ABL_TRY(dev_alloc_t(ctx, &g.sep.pair[a], level, own));
+        ABL_TRY(dev_alloc_t(ctx, &g.sep.elem[a], level, own));
       }
       // List offsets are 32-bit.
       if (level * (g.ordered ? span : 1) > (long) INT32_MAX) return ABL_E_UNSUPPORTED;
@@ -1086,41 +1038,36 @@ int apply_population_changes(abl_ctx *ctx, int k, bool &regrow) {
 // (levels 1) or, with levels == dim, the whole neighbourhood lists (nb_off,
 // nb_list).
 template <typename G>
-void build_lists(abl_ctx *ctx, const G &geo, int dim, int levels, long ncells,
-                 const int *cell_start, const int *order, const SepLevels &L, int *cnt,
-                 const ScanPlan &scan, int *nb_off, int *nb_list) {
+void build_lists(abl_ctx *ctx, const G &geo, int dim, int levels, int Rmax, long ncells,
+                 const int *cell_start, const int *order, const float *posf,
+                 const SepLevels &L, int *cnt, const ScanPlan &scan, int *nb_off, int *nb_list) {
   cudaStream_t s = ctx->stream;
   const int B = 256;
-  SepSrc src{cell_start, order, nullptr};
+  SepSrc src{cell_start, order, posf, dim, nullptr};
   const long cb = blocks_for(ncells, B), lb = blocks_for(ncells, kSepWarps);
+  const long sb = blocks_for(ncells, kSepThreads);
   for (int a = 0; a < levels; a++) {
     const bool last = a == dim - 1;
     int *off = last ? nb_off : L.off[a];
-    int2 *dp = last ? nullptr : L.pair[a];
+    int4 *de = last ? nullptr : L.elem[a];
     int *ds = last ? nb_list : nullptr;
     if (a == 0) k_sep_count<G, 0><<<cb, B, 0, s>>>(ncells, geo, src.off, cnt);
     else if (a == 1) k_sep_count<G, 1><<<cb, B, 0, s>>>(ncells, geo, src.off, cnt);
     else k_sep_count<G, 2><<<cb, B, 0, s>>>(ncells, geo, src.off, cnt);
     ctx->launches++;
     scan_run(ctx, scan, cnt, off);
-    // Intermediate levels stage their (id, slot) output in shared memory; the
-    // final level stores directly and leaves the shared memory to L1, which
-    // holds the three list heads each thread reads.
-    const long sb = blocks_for(ncells, kSepThreads);
     if (a == 0) {
-      if (last) k_sep_merge<G, 0, false, false><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, dp, ds);
-      else k_sep_merge<G, 0, false, true><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, dp, ds);
-      k_sep_merge_large<G, 0><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, dp, ds);
+      k_sep_merge<G, 0, true><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, de, ds);
+      if (Rmax > 1) k_sep_merge_large<G, 0><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, de, ds);
     } else if (a == 1) {
-      if (last) k_sep_merge<G, 1, true, false><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, dp, ds);
-      else k_sep_merge<G, 1, true, true><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, dp, ds);
-      k_sep_merge_large<G, 1><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, dp, ds);
+      k_sep_merge<G, 1, false><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, de, ds);
+      if (Rmax > 1) k_sep_merge_large<G, 1><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, de, ds);
     } else {
-      k_sep_merge<G, 2, true, false><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, dp, ds);
-      k_sep_merge_large<G, 2><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, dp, ds);
+      k_sep_merge<G, 2, false><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, de, ds);
+      if (Rmax > 1) k_sep_merge_large<G, 2><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, de, ds);
     }
-    ctx->launches += 2;
-    if (!last) src = SepSrc{L.off[a], nullptr, L.pair[a]};
+    ctx->launches += Rmax > 1 ? 2 : 1;
+    if (!last) src = SepSrc{L.off[a], nullptr, nullptr, dim, L.elem[a]};
   }
 }
 
@@ -1164,8 +1111,8 @@ void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
   ctx->launches++;
   if (t.ordered || t.rows) {
     GridGeom geo{t.nx, t.ny, t.nz, t.R};
-    build_lists(ctx, geo, dim, t.ordered ? dim : 1, t.ncells, t.cell_start, t.order, t.sep,
-                t.nb_cnt, t.nb_scan, t.nb_off, t.nb_list);
+    build_lists(ctx, geo, dim, t.ordered ? dim : 1, t.R, t.ncells, t.cell_start, t.order,
+                t.posf, t.sep, t.nb_cnt, t.nb_scan, t.nb_off, t.nb_list);
   }
 }
 
@@ -1249,7 +1196,7 @@ int step_once(abl_ctx *ctx) {
       const int depth = list_depth(sd, *nt.d, ctx->near_mode);
       V.dim = nt.d->dim;
       V.ordered = depth == 2;
-      V.rows = depth == 1 ? nt.sep.pair[0] : nullptr;
+      V.rows = depth == 1 ? nt.sep.elem[0] : nullptr;
       V.row_off = nt.sep.off[0];
       V.range = nt.R;
       V.nx = nt.nx;
@@ -2024,8 +1971,8 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
       for (int a = 0; a < inter && ok; a++) {
         level *= span;
         gb.sep.off[a] = b.take<int>(gb.ncells + 1);
-        gb.sep.pair[a] = b.take<int2>(level);
-        ok = gb.sep.off[a] && gb.sep.pair[a];
+        gb.sep.elem[a] = b.take<int4>(level);
+        ok = gb.sep.off[a] && gb.sep.elem[a];
       }
       gb.nb_cnt = b.take<int>(gb.ncells);
       ok = ok && gb.nb_cnt && scan_plan_static(gb.nb_scan, gb.ncells, b);
@@ -2283,7 +2230,7 @@ int ens_prepare(abl_ensemble *e) {
       for (int a = 0; a < inter; a++) {
         level *= span;
         ABL_TRY(dev_alloc_t(ctx, &t.sep.off[a], cells + 1, own));
-        ABL_TRY(dev_alloc_t(ctx, &t.sep.pair[a], level, own));
+        ABL_TRY(dev_alloc_t(ctx, &t.sep.elem[a], level, own));
       }
       if (level * (t.ordered ? span : 1) > (long) INT32_MAX) return ABL_E_UNSUPPORTED;
       ABL_TRY(dev_alloc_t(ctx, &t.nb_cnt, cells, own));
@@ -2308,7 +2255,7 @@ int ens_prepare(abl_ensemble *e) {
       const int depth = list_depth(sd, *nt.d, ctx->near_mode);
       V.dim = nt.d->dim;
       V.ordered = depth == 2;
-      V.rows = depth == 1 ? nt.sep.pair[0] : nullptr;
+      V.rows = depth == 1 ? nt.sep.elem[0] : nullptr;
       V.row_off = nt.sep.off[0] ? nt.sep.off[0] + g.cell_base : nullptr;
       V.range = g.R;
       V.nx = g.nx;
@@ -2375,9 +2322,11 @@ void ens_launch_bin(abl_ensemble *e, EnsType &t) {
   else k_gather<Real, 3><<<nb, B, 0, s>>>(t.n, t.order, pos, t.posf, g);
   ctx->launches++;
   if (t.ordered || t.rows) {
+    int Rmax = 1;
+    for (auto &g : t.grids) Rmax = std::max(Rmax, g.R);
     EnsGeom geo{t.cell_replica, t.d_grids};
-    build_lists(ctx, geo, dim, t.ordered ? dim : 1, t.ncells, t.cell_start, t.order, t.sep,
-                t.nb_cnt, t.nb_scan, t.nb_off, t.nb_list);
+    build_lists(ctx, geo, dim, t.ordered ? dim : 1, Rmax, t.ncells, t.cell_start, t.order,
+                t.posf, t.sep, t.nb_cnt, t.nb_scan, t.nb_off, t.nb_list);
   }
   t.dirty = false;
 }

@@ -130,11 +130,18 @@ __device__ static void update_boid(const abl_globals &abl_G, const abl_near_view
             return !(dist_float2(abl_p, in->pos) > abl_G.interaction_radius);
         };
         while (abl_c1.fill(abl_q1, abl_exact1)) {
+            int abl_pslot1 = abl_c1.slot(0);
+            Boid abl_pnx1;
+            abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
+            abl_pnx1.velocity = ((const float2 *) abl_NB.cols[1])[abl_pslot1];
             for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
-                const int abl_slot1 = abl_c1.slot(abl_k);
-                Boid abl_nx1;
-                abl_nx1.pos = ((const float2 *) abl_NB.cols[0])[abl_slot1];
-                abl_nx1.velocity = ((const float2 *) abl_NB.cols[1])[abl_slot1];
+                const int abl_slot1 = abl_pslot1;
+                Boid abl_nx1 = abl_pnx1;
+                if (abl_k + 1 < abl_c1.cnt) {
+                    abl_pslot1 = abl_c1.slot(abl_k + 1);
+                    abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
+                    abl_pnx1.velocity = ((const float2 *) abl_NB.cols[1])[abl_pslot1];
+                }
                 Boid* nx = &abl_nx1;
                 {
                     global_center = float2_add(global_center, nx->pos);
@@ -192,7 +199,7 @@ struct abl_kargs_update_boid {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_update_boid(const __grid_constant__ abl_kargs_update_boid A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_update_boid(const __grid_constant__ abl_kargs_update_boid A) {
     int abl_j;
     {
         const abl_globals &abl_G = A.G;
@@ -245,7 +252,7 @@ static int abl_launch_update_boid(const abl_step_launch *L, cudaStream_t abl_str
     abl_kernel_update_boid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_update_boid(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_update_boid(const __grid_constant__ abl_ens_launch A) {
     int abl_j;
     {
         const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;

@@ -110,10 +110,16 @@ __device__ static void move_point(const abl_globals &abl_G, const abl_near_view 
             return !(dist_float3(abl_p, in->pos) > (2.0 * abl_G.r));
         };
         while (abl_c1.fill(abl_q1, abl_exact1)) {
+            int abl_pslot1 = abl_c1.slot(0);
+            Point abl_pnx1;
+            abl_pnx1.pos = ((const float3 *) abl_NB.cols[0])[abl_pslot1];
             for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
-                const int abl_slot1 = abl_c1.slot(abl_k);
-                Point abl_nx1;
-                abl_nx1.pos = ((const float3 *) abl_NB.cols[0])[abl_slot1];
+                const int abl_slot1 = abl_pslot1;
+                Point abl_nx1 = abl_pnx1;
+                if (abl_k + 1 < abl_c1.cnt) {
+                    abl_pslot1 = abl_c1.slot(abl_k + 1);
+                    abl_pnx1.pos = ((const float3 *) abl_NB.cols[0])[abl_pslot1];
+                }
                 Point* nx = &abl_nx1;
                 {
                     double pos_dist = dist_float3(in->pos, nx->pos);
@@ -146,7 +152,7 @@ struct abl_kargs_move_point {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_move_point(const __grid_constant__ abl_kargs_move_point A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_move_point(const __grid_constant__ abl_kargs_move_point A) {
     int abl_j;
     {
         const abl_globals &abl_G = A.G;
@@ -195,7 +201,7 @@ static int abl_launch_move_point(const abl_step_launch *L, cudaStream_t abl_stre
     abl_kernel_move_point<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_move_point(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_move_point(const __grid_constant__ abl_ens_launch A) {
     int abl_j;
     {
         const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;

@@ -111,10 +111,16 @@ __device__ static void step_move(const abl_globals &abl_G, const abl_near_view &
             return !(dist_float2(abl_p, in->pos) > abl_G.radius);
         };
         while (abl_c1.fill(abl_q1, abl_exact1)) {
+            int abl_pslot1 = abl_c1.slot(0);
+            Cell abl_pnx1;
+            abl_pnx1.alive = ((const bool *) abl_NB.cols[1])[abl_pslot1];
             for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
-                const int abl_slot1 = abl_c1.slot(abl_k);
-                Cell abl_nx1;
-                abl_nx1.alive = ((const bool *) abl_NB.cols[1])[abl_slot1];
+                const int abl_slot1 = abl_pslot1;
+                Cell abl_nx1 = abl_pnx1;
+                if (abl_k + 1 < abl_c1.cnt) {
+                    abl_pslot1 = abl_c1.slot(abl_k + 1);
+                    abl_pnx1.alive = ((const bool *) abl_NB.cols[1])[abl_pslot1];
+                }
                 Cell* nx = &abl_nx1;
                 {
                     living_neighbors += (nx->alive ? 1 : 0);
@@ -144,7 +150,7 @@ struct abl_kargs_step_move {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_step_move(const __grid_constant__ abl_kargs_step_move A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_step_move(const __grid_constant__ abl_kargs_step_move A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
@@ -184,7 +190,7 @@ static int abl_launch_step_move(const abl_step_launch *L, cudaStream_t abl_strea
     abl_kernel_step_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_step_move(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_step_move(const __grid_constant__ abl_ens_launch A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;

@@ -213,10 +213,16 @@ __device__ static void prey_avoid_pred(const abl_globals &abl_G, const abl_near_
             return !(dist_float2(abl_p, in->pos) > abl_G.PRED_PREY_INTERACTION_RADIUS);
         };
         while (abl_c1.fill(abl_q1, abl_exact1)) {
+            int abl_pslot1 = abl_c1.slot(0);
+            Predator abl_pnx1;
+            abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
             for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
-                const int abl_slot1 = abl_c1.slot(abl_k);
-                Predator abl_nx1;
-                abl_nx1.pos = ((const float2 *) abl_NB.cols[0])[abl_slot1];
+                const int abl_slot1 = abl_pslot1;
+                Predator abl_nx1 = abl_pnx1;
+                if (abl_k + 1 < abl_c1.cnt) {
+                    abl_pslot1 = abl_c1.slot(abl_k + 1);
+                    abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
+                }
                 Predator* pred = &abl_nx1;
                 {
                     double separation = length_float2(float2_sub(in->pos, pred->pos));
@@ -245,7 +251,7 @@ struct abl_kargs_prey_avoid_pred {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_avoid_pred(const __grid_constant__ abl_kargs_prey_avoid_pred A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_avoid_pred(const __grid_constant__ abl_kargs_prey_avoid_pred A) {
     int abl_j;
     {
         const abl_globals &abl_G = A.G;
@@ -307,7 +313,7 @@ static int abl_launch_prey_avoid_pred(const abl_step_launch *L, cudaStream_t abl
     abl_kernel_prey_avoid_pred<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_avoid_pred(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_prey_avoid_pred(const __grid_constant__ abl_ens_launch A) {
     int abl_j;
     {
         const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -379,10 +385,16 @@ __device__ static void prey_flock(const abl_globals &abl_G, const abl_near_view 
             return !(dist_float2(abl_p, in->pos) > abl_G.PREY_GROUP_COHESION_RADIUS);
         };
         while (abl_c2.fill(abl_q2, abl_exact2)) {
+            int abl_pslot2 = abl_c2.slot(0);
+            Prey abl_pnx2;
+            abl_pnx2.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot2];
             for (int abl_k = 0; abl_k < abl_c2.cnt; ++abl_k) {
-                const int abl_slot2 = abl_c2.slot(abl_k);
-                Prey abl_nx2;
-                abl_nx2.pos = ((const float2 *) abl_NB.cols[0])[abl_slot2];
+                const int abl_slot2 = abl_pslot2;
+                Prey abl_nx2 = abl_pnx2;
+                if (abl_k + 1 < abl_c2.cnt) {
+                    abl_pslot2 = abl_c2.slot(abl_k + 1);
+                    abl_pnx2.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot2];
+                }
                 Prey* prey = &abl_nx2;
                 {
                     double separation = length_float2(float2_sub(in->pos, prey->pos));
@@ -417,7 +429,7 @@ struct abl_kargs_prey_flock {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_flock(const __grid_constant__ abl_kargs_prey_flock A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_flock(const __grid_constant__ abl_kargs_prey_flock A) {
     int abl_j;
     {
         const abl_globals &abl_G = A.G;
@@ -479,7 +491,7 @@ static int abl_launch_prey_flock(const abl_step_launch *L, cudaStream_t abl_stre
     abl_kernel_prey_flock<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_flock(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_prey_flock(const __grid_constant__ abl_ens_launch A) {
     int abl_j;
     {
         const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -565,7 +577,7 @@ struct abl_kargs_prey_move {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_move(const __grid_constant__ abl_kargs_prey_move A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_move(const __grid_constant__ abl_kargs_prey_move A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
@@ -613,7 +625,7 @@ static int abl_launch_prey_move(const abl_step_launch *L, cudaStream_t abl_strea
     abl_kernel_prey_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_prey_move(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_prey_move(const __grid_constant__ abl_ens_launch A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
@@ -661,10 +673,16 @@ __device__ static void prey_eaten(const abl_globals &abl_G, const abl_near_view 
             return !(dist_float2(abl_p, in->pos) > abl_G.PRED_KILL_DISTANCE);
         };
         while (abl_c3.fill(abl_q3, abl_exact3)) {
+            int abl_pslot3 = abl_c3.slot(0);
+            Predator abl_pnx3;
+            abl_pnx3.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot3];
             for (int abl_k = 0; abl_k < abl_c3.cnt; ++abl_k) {
-                const int abl_slot3 = abl_c3.slot(abl_k);
-                Predator abl_nx3;
-                abl_nx3.pos = ((const float2 *) abl_NB.cols[0])[abl_slot3];
+                const int abl_slot3 = abl_pslot3;
+                Predator abl_nx3 = abl_pnx3;
+                if (abl_k + 1 < abl_c3.cnt) {
+                    abl_pslot3 = abl_c3.slot(abl_k + 1);
+                    abl_pnx3.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot3];
+                }
                 Predator* pred = &abl_nx3;
                 {
                     double distance = length_float2(float2_sub(pred->pos, in->pos));
@@ -692,7 +710,7 @@ struct abl_kargs_prey_eaten {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_eaten(const __grid_constant__ abl_kargs_prey_eaten A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_eaten(const __grid_constant__ abl_kargs_prey_eaten A) {
     int abl_j;
     {
         const abl_globals &abl_G = A.G;
@@ -774,10 +792,16 @@ __device__ static void prey_eat_or_starve(const abl_globals &abl_G, const abl_ne
             return !(dist_float2(abl_p, in->pos) > abl_G.GRASS_EAT_DISTANCE);
         };
         while (abl_c4.fill(abl_q4, abl_exact4)) {
+            int abl_pslot4 = abl_c4.slot(0);
+            Grass abl_pnx4;
+            abl_pnx4.avail = ((const bool *) abl_NB.cols[2])[abl_pslot4];
             for (int abl_k = 0; abl_k < abl_c4.cnt; ++abl_k) {
-                const int abl_slot4 = abl_c4.slot(abl_k);
-                Grass abl_nx4;
-                abl_nx4.avail = ((const bool *) abl_NB.cols[2])[abl_slot4];
+                const int abl_slot4 = abl_pslot4;
+                Grass abl_nx4 = abl_pnx4;
+                if (abl_k + 1 < abl_c4.cnt) {
+                    abl_pslot4 = abl_c4.slot(abl_k + 1);
+                    abl_pnx4.avail = ((const bool *) abl_NB.cols[2])[abl_pslot4];
+                }
                 Grass* grass = &abl_nx4;
                 {
                     if (grass->avail) life += abl_G.GAIN_FROM_FOOD_PREY;
@@ -802,7 +826,7 @@ struct abl_kargs_prey_eat_or_starve {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_eat_or_starve(const __grid_constant__ abl_kargs_prey_eat_or_starve A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_eat_or_starve(const __grid_constant__ abl_kargs_prey_eat_or_starve A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
@@ -880,7 +904,7 @@ struct abl_kargs_prey_reproduction {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_prey_reproduction(const __grid_constant__ abl_kargs_prey_reproduction A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_reproduction(const __grid_constant__ abl_kargs_prey_reproduction A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
@@ -946,10 +970,16 @@ __device__ static void pred_follow_prey(const abl_globals &abl_G, const abl_near
             return !(dist_float2(abl_p, in->pos) > abl_G.PRED_PREY_INTERACTION_RADIUS);
         };
         while (abl_c5.fill(abl_q5, abl_exact5)) {
+            int abl_pslot5 = abl_c5.slot(0);
+            Prey abl_pnx5;
+            abl_pnx5.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot5];
             for (int abl_k = 0; abl_k < abl_c5.cnt; ++abl_k) {
-                const int abl_slot5 = abl_c5.slot(abl_k);
-                Prey abl_nx5;
-                abl_nx5.pos = ((const float2 *) abl_NB.cols[0])[abl_slot5];
+                const int abl_slot5 = abl_pslot5;
+                Prey abl_nx5 = abl_pnx5;
+                if (abl_k + 1 < abl_c5.cnt) {
+                    abl_pslot5 = abl_c5.slot(abl_k + 1);
+                    abl_pnx5.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot5];
+                }
                 Prey* prey = &abl_nx5;
                 {
                     double separation = length_float2(float2_sub(in->pos, prey->pos));
@@ -981,7 +1011,7 @@ struct abl_kargs_pred_follow_prey {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_follow_prey(const __grid_constant__ abl_kargs_pred_follow_prey A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_follow_prey(const __grid_constant__ abl_kargs_pred_follow_prey A) {
     int abl_j;
     {
         const abl_globals &abl_G = A.G;
@@ -1043,7 +1073,7 @@ static int abl_launch_pred_follow_prey(const abl_step_launch *L, cudaStream_t ab
     abl_kernel_pred_follow_prey<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_follow_prey(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pred_follow_prey(const __grid_constant__ abl_ens_launch A) {
     int abl_j;
     {
         const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1112,10 +1142,16 @@ __device__ static void pred_avoid(const abl_globals &abl_G, const abl_near_view 
             return !(dist_float2(abl_p, in->pos) > abl_G.SAME_SPECIES_AVOIDANCE_RADIUS);
         };
         while (abl_c6.fill(abl_q6, abl_exact6)) {
+            int abl_pslot6 = abl_c6.slot(0);
+            Predator abl_pnx6;
+            abl_pnx6.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot6];
             for (int abl_k = 0; abl_k < abl_c6.cnt; ++abl_k) {
-                const int abl_slot6 = abl_c6.slot(abl_k);
-                Predator abl_nx6;
-                abl_nx6.pos = ((const float2 *) abl_NB.cols[0])[abl_slot6];
+                const int abl_slot6 = abl_pslot6;
+                Predator abl_nx6 = abl_pnx6;
+                if (abl_k + 1 < abl_c6.cnt) {
+                    abl_pslot6 = abl_c6.slot(abl_k + 1);
+                    abl_pnx6.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot6];
+                }
                 Predator* pred = &abl_nx6;
                 {
                     double separation = length_float2(float2_sub(in->pos, pred->pos));
@@ -1142,7 +1178,7 @@ struct abl_kargs_pred_avoid {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_avoid(const __grid_constant__ abl_kargs_pred_avoid A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_avoid(const __grid_constant__ abl_kargs_pred_avoid A) {
     int abl_j;
     {
         const abl_globals &abl_G = A.G;
@@ -1204,7 +1240,7 @@ static int abl_launch_pred_avoid(const abl_step_launch *L, cudaStream_t abl_stre
     abl_kernel_pred_avoid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_avoid(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pred_avoid(const __grid_constant__ abl_ens_launch A) {
     int abl_j;
     {
         const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1292,7 +1328,7 @@ struct abl_kargs_pred_move {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_move(const __grid_constant__ abl_kargs_pred_move A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_move(const __grid_constant__ abl_kargs_pred_move A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
@@ -1340,7 +1376,7 @@ static int abl_launch_pred_move(const abl_step_launch *L, cudaStream_t abl_strea
     abl_kernel_pred_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_pred_move(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pred_move(const __grid_constant__ abl_ens_launch A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
@@ -1387,9 +1423,14 @@ __device__ static void pred_eat_or_starve(const abl_globals &abl_G, const abl_ne
             return !(dist_float2(abl_p, in->pos) > abl_G.PRED_KILL_DISTANCE);
         };
         while (abl_c7.fill(abl_q7, abl_exact7)) {
+            int abl_pslot7 = abl_c7.slot(0);
+            Prey abl_pnx7;
             for (int abl_k = 0; abl_k < abl_c7.cnt; ++abl_k) {
-                const int abl_slot7 = abl_c7.slot(abl_k);
-                Prey abl_nx7;
+                const int abl_slot7 = abl_pslot7;
+                Prey abl_nx7 = abl_pnx7;
+                if (abl_k + 1 < abl_c7.cnt) {
+                    abl_pslot7 = abl_c7.slot(abl_k + 1);
+                }
                 Prey* prey = &abl_nx7;
                 {
                     pred_life += abl_G.GAIN_FROM_FOOD_PREDATOR;
@@ -1414,7 +1455,7 @@ struct abl_kargs_pred_eat_or_starve {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_eat_or_starve(const __grid_constant__ abl_kargs_pred_eat_or_starve A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_eat_or_starve(const __grid_constant__ abl_kargs_pred_eat_or_starve A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
@@ -1492,7 +1533,7 @@ struct abl_kargs_pred_reproduction {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_pred_reproduction(const __grid_constant__ abl_kargs_pred_reproduction A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_reproduction(const __grid_constant__ abl_kargs_pred_reproduction A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
@@ -1555,10 +1596,16 @@ __device__ static void grass_eaten(const abl_globals &abl_G, const abl_near_view
             return !(dist_float2(abl_p, in->pos) > abl_G.GRASS_EAT_DISTANCE);
         };
         while (abl_c8.fill(abl_q8, abl_exact8)) {
+            int abl_pslot8 = abl_c8.slot(0);
+            Prey abl_pnx8;
+            abl_pnx8.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot8];
             for (int abl_k = 0; abl_k < abl_c8.cnt; ++abl_k) {
-                const int abl_slot8 = abl_c8.slot(abl_k);
-                Prey abl_nx8;
-                abl_nx8.pos = ((const float2 *) abl_NB.cols[0])[abl_slot8];
+                const int abl_slot8 = abl_pslot8;
+                Prey abl_nx8 = abl_pnx8;
+                if (abl_k + 1 < abl_c8.cnt) {
+                    abl_pslot8 = abl_c8.slot(abl_k + 1);
+                    abl_pnx8.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot8];
+                }
                 Prey* prey = &abl_nx8;
                 {
                     double distance = length_float2(float2_sub(in->pos, prey->pos));
@@ -1589,7 +1636,7 @@ struct abl_kargs_grass_eaten {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_grass_eaten(const __grid_constant__ abl_kargs_grass_eaten A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_grass_eaten(const __grid_constant__ abl_kargs_grass_eaten A) {
     int abl_j;
     {
         const abl_globals &abl_G = A.G;
@@ -1647,7 +1694,7 @@ static int abl_launch_grass_eaten(const abl_step_launch *L, cudaStream_t abl_str
     abl_kernel_grass_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_grass_eaten(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_grass_eaten(const __grid_constant__ abl_ens_launch A) {
     int abl_j;
     {
         const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1725,7 +1772,7 @@ struct abl_kargs_grass_growth {
     long timestep;
     int step_index;
 };
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_grass_growth(const __grid_constant__ abl_kargs_grass_growth A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_grass_growth(const __grid_constant__ abl_kargs_grass_growth A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
@@ -1769,7 +1816,7 @@ static int abl_launch_grass_growth(const abl_step_launch *L, cudaStream_t abl_st
     abl_kernel_grass_growth<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK) abl_kernel_ens_grass_growth(const __grid_constant__ abl_ens_launch A) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_grass_growth(const __grid_constant__ abl_ens_launch A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
