@@ -386,12 +386,19 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
 
   const bool presorted = fnKind == FnKind::STEP && !steps.empty() && steps.back().presorted;
 
+  // The querying agent's index, when the loop is centred on the step's own
+  // agent: its cell then comes from the binning.
+  const AST::FunctionDeclaration *stepDecl =
+      fnKind == FnKind::STEP && !steps.empty() ? steps.back().decl : nullptr;
+  auto *centerVar = dynamic_cast<const AST::VarExpression *>(&agentExpr);
+  const bool centredOnSelf = stepDecl && centerVar
+                          && centerVar->var->id == stepDecl->stepParam().var->id;
   *this << "{" << indent << nl
         << "const abl::near_query<" << dim << "> " << q << "(abl_NB, (double) " << agentExpr
         << "->" << posMember->name << ".x, (double) " << agentExpr << "->" << posMember->name
         << ".y, " << (is3 ? "(double) " : "0.0");
   if (is3) *this << agentExpr << "->" << posMember->name << ".z";
-  *this << ");" << nl;
+  *this << (centredOnSelf ? ", abl_K.self" : "") << ");" << nl;
   if (presorted) {
     *this << "abl::near_list_cursor<" << dim << "> " << c << "(abl_NB, " << q << ", abl_K);";
   } else {
@@ -626,7 +633,8 @@ void CudaPrinter::printPresortPhase(const StepInfo &info, const std::string &vie
   *this << "const " << pt << " abl_p1 = abl_has ? " << pos << " : " << pt << "{};" << nl
         << "const abl::near_query<" << dim << "> abl_q0(" << view
         << ", (double) abl_p1.x, (double) abl_p1.y, " << (is3 ? "(double) abl_p1.z" : "0.0")
-        << ");" << nl << "auto abl_x0 = [&](int abl_s) -> bool {" << indent << nl
+        << ", abl_has ? abl_i1 : -1);" << nl
+        << "auto abl_x0 = [&](int abl_s) -> bool {" << indent << nl
         << "const " << pt << " abl_p = ((const " << pt << " *) " << view << ".cols[" << posIdx
         << "])[abl_s];" << nl << "return !(" << (is3 ? "dist_float3" : "dist_float2")
         << "(abl_p, abl_p1) > " << loop.getNearRadius() << ");" << outdent << nl << "};" << nl

@@ -120,13 +120,21 @@ struct near_query {
   mutable band lazy_band;
   mutable bool lazy_valid = false;
 
-  __device__ near_query(const abl_near_view &V, double x, double y, double z) {
+  // `self`: the querying agent's index when it belongs to the binned
+  // population (its cell is then the one binning gave it), else -1.
+  __device__ near_query(const abl_near_view &V, double x, double y, double z, long self = -1) {
     const int dims[3] = {V.nx, V.ny, V.nz};
     const double p[3] = {x, y, z};
-    for (int d = 0; d < 3; d++) {
-      c[d] = d < DIM ? cell_coord(p[d], V.lo[d], V.inv_cell, dims[d]) : 0;
-      pf[d] = d < DIM ? (float) p[d] : 0.0f;
+    if (self >= 0 && V.cell_of) {
+      const int l = (int) (__ldg(&V.cell_of[self]) - V.cell_base);
+      const int nxy = V.nx * V.ny;
+      c[2] = l / nxy;
+      c[1] = (l - c[2] * nxy) / V.nx;
+      c[0] = l - c[2] * nxy - c[1] * V.nx;
+    } else {
+      for (int d = 0; d < 3; d++) c[d] = d < DIM ? cell_coord(p[d], V.lo[d], V.inv_cell, dims[d]) : 0;
     }
+    for (int d = 0; d < 3; d++) pf[d] = d < DIM ? (float) p[d] : 0.0f;
     amax = *V.amax;
     bd = make_band(V.radius, amax, DIM);
   }

@@ -63,6 +63,8 @@ typedef struct {
                                along x, ascending id */
   const float *amax;        /* max |coordinate| over neighbour and query agents */
   const void *cols[ABL_MAX_MEMBERS]; /* slot-ordered copies of the members the loop reads */
+  const int *cell_of;       /* agent -> cell when the step's agents are the binned ones, else NULL */
+  long cell_base;           /* cell_of values are cell_base + cell index of this view */
   int balance;              /* presorted mode: hand a block's agents to threads by neighbour count */
   int cap;                  /* presorted mode: neighbours held per agent in shared memory */
 } abl_near_view;

@@ -1214,6 +1214,8 @@ int step_once(abl_ctx *ctx) {
       for (int j = 0; j < nt.d->num_members; j++) V.cols[j] = nt.gcols[j];
       V.balance = ctx->balance;
       V.cap = V.ordered ? ctx->list_cap : ctx->runs_cap;
+      V.cell_of = sd.agent_type == sd.near_type ? nt.cell_of : nullptr;
+      V.cell_base = 0;
       if (sd.presorted) L.smem = abl::presort_bytes(V);
       if (sd.agent_type == sd.near_type) {
         V.amax = nt.amax;
@@ -2274,6 +2276,8 @@ int ens_prepare(abl_ensemble *e) {
       for (int j = 0; j < nt.d->num_members; j++) V.cols[j] = nt.gcols[j];
       V.balance = e->balance;
       V.cap = V.ordered ? ctx->list_cap : ctx->runs_cap;
+      V.cell_of = sd.agent_type == sd.near_type ? nt.cell_of : nullptr;
+      V.cell_base = g.cell_base;
     }
     e->smem[k] = sd.presorted ? abl::presort_bytes(views[0]) : 0;
     abl_near_view *dv = nullptr;

@@ -103,7 +103,7 @@ __device__ static void move_point(const abl_globals &abl_G, const abl_near_view 
     (void) abl_R; (void) abl_NB;
     float3 new_pos = in->pos;
     {
-        const abl::near_query<3> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, (double) in->pos.z);
+        const abl::near_query<3> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, (double) in->pos.z, abl_K.self);
         abl::near_list_cursor<3> abl_c1(abl_NB, abl_q1, abl_K);
         auto abl_exact1 = [&](int abl_s) -> bool {
             const float3 abl_p = ((const float3 *) abl_NB.cols[0])[abl_s];
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
         const float3 abl_p1 = abl_has ? A.in.pos[abl_i1] : float3{};
-        const abl::near_query<3> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, (double) abl_p1.z);
+        const abl::near_query<3> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, (double) abl_p1.z, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float3 abl_p = ((const float3 *) A.NB.cols[0])[abl_s];
             return !(dist_float3(abl_p, abl_p1) > (2.0 * abl_G.r));
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
         const abl_near_view &abl_V1 = A.views[abl_r1];
         const float3 abl_p1 = abl_has ? ((const float3 *) A.in_cols[0])[abl_i1] : float3{};
-        const abl::near_query<3> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, (double) abl_p1.z);
+        const abl::near_query<3> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, (double) abl_p1.z, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float3 abl_p = ((const float3 *) abl_V1.cols[0])[abl_s];
             return !(dist_float3(abl_p, abl_p1) > (2.0 * abl_G.r));

@@ -104,7 +104,7 @@ __device__ static void step_move(const abl_globals &abl_G, const abl_near_view &
     (void) abl_R; (void) abl_NB;
     int living_neighbors = 0;
     {
-        const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
+        const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
         abl::near_cursor<2> abl_c1(abl_NB, abl_q1);
         auto abl_exact1 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];

@@ -206,7 +206,7 @@ __device__ static void prey_avoid_pred(const abl_globals &abl_G, const abl_near_
     (void) abl_R; (void) abl_NB;
     float2 avoid_velocity = float2_fill(0.0);
     {
-        const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
+        const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
         abl::near_list_cursor<2> abl_c1(abl_NB, abl_q1, abl_K);
         auto abl_exact1 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
         const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.PRED_PREY_INTERACTION_RADIUS);
@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
         const abl_near_view &abl_V1 = A.views[abl_r1];
         const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.PRED_PREY_INTERACTION_RADIUS);
@@ -378,7 +378,7 @@ __device__ static void prey_flock(const abl_globals &abl_G, const abl_near_view 
     float2 avoid_velocity = float2_fill(0.0);
     int group_centre_count = 0;
     {
-        const abl::near_query<2> abl_q2(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
+        const abl::near_query<2> abl_q2(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
         abl::near_list_cursor<2> abl_c2(abl_NB, abl_q2, abl_K);
         auto abl_exact2 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
         const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.PREY_GROUP_COHESION_RADIUS);
@@ -501,7 +501,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
         const abl_near_view &abl_V1 = A.views[abl_r1];
         const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.PREY_GROUP_COHESION_RADIUS);
@@ -666,7 +666,7 @@ __device__ static void prey_eaten(const abl_globals &abl_G, const abl_near_view 
     bool eaten = false;
     float closest_pred = abl_G.PRED_KILL_DISTANCE;
     {
-        const abl::near_query<2> abl_q3(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
+        const abl::near_query<2> abl_q3(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
         abl::near_list_cursor<2> abl_c3(abl_NB, abl_q3, abl_K);
         auto abl_exact3 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
@@ -718,7 +718,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
         const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.PRED_KILL_DISTANCE);
@@ -785,7 +785,7 @@ __device__ static void prey_eat_or_starve(const abl_globals &abl_G, const abl_ne
     (void) abl_R; (void) abl_NB;
     int life = in->life;
     {
-        const abl::near_query<2> abl_q4(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
+        const abl::near_query<2> abl_q4(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
         abl::near_cursor<2> abl_c4(abl_NB, abl_q4);
         auto abl_exact4 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
@@ -963,7 +963,7 @@ __device__ static void pred_follow_prey(const abl_globals &abl_G, const abl_near
     float closest_prey_distance = abl_G.PRED_PREY_INTERACTION_RADIUS;
     bool can_see_prey = false;
     {
-        const abl::near_query<2> abl_q5(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
+        const abl::near_query<2> abl_q5(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
         abl::near_list_cursor<2> abl_c5(abl_NB, abl_q5, abl_K);
         auto abl_exact5 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
@@ -1019,7 +1019,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
         const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.PRED_PREY_INTERACTION_RADIUS);
@@ -1083,7 +1083,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
         const abl_near_view &abl_V1 = A.views[abl_r1];
         const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.PRED_PREY_INTERACTION_RADIUS);
@@ -1135,7 +1135,7 @@ __device__ static void pred_avoid(const abl_globals &abl_G, const abl_near_view 
     (void) abl_R; (void) abl_NB;
     float2 avoid_velocity = float2_create(0, 0);
     {
-        const abl::near_query<2> abl_q6(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
+        const abl::near_query<2> abl_q6(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
         abl::near_list_cursor<2> abl_c6(abl_NB, abl_q6, abl_K);
         auto abl_exact6 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
@@ -1186,7 +1186,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
         const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.SAME_SPECIES_AVOIDANCE_RADIUS);
@@ -1250,7 +1250,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
         const abl_near_view &abl_V1 = A.views[abl_r1];
         const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.SAME_SPECIES_AVOIDANCE_RADIUS);
@@ -1416,7 +1416,7 @@ __device__ static void pred_eat_or_starve(const abl_globals &abl_G, const abl_ne
     (void) abl_R; (void) abl_NB;
     int pred_life = in->life;
     {
-        const abl::near_query<2> abl_q7(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
+        const abl::near_query<2> abl_q7(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
         abl::near_cursor<2> abl_c7(abl_NB, abl_q7);
         auto abl_exact7 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
@@ -1589,7 +1589,7 @@ __device__ static void grass_eaten(const abl_globals &abl_G, const abl_near_view
     float closest_prey = abl_G.GRASS_EAT_DISTANCE;
     bool eaten = false;
     {
-        const abl::near_query<2> abl_q8(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0);
+        const abl::near_query<2> abl_q8(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
         abl::near_list_cursor<2> abl_c8(abl_NB, abl_q8, abl_K);
         auto abl_exact8 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
@@ -1644,7 +1644,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
         const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.GRASS_EAT_DISTANCE);
@@ -1704,7 +1704,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
         const abl_near_view &abl_V1 = A.views[abl_r1];
         const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0);
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
         auto abl_x0 = [&](int abl_s) -> bool {
             const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
             return !(dist_float2(abl_p, abl_p1) > abl_G.GRASS_EAT_DISTANCE);
