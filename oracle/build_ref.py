@@ -12,6 +12,10 @@ case below it
      reference's build line (CBackend.cpp:21-27) plus `-Dsave=abl_ref_save`,
      the reference's asset/c/libabl.c and oracle/ref_harness.c,
   4. leaves the program in oracle/_ref/<case>/main (git-ignored).
+
+PROGRAMS are built unmodified (no dump hook, the example's default
+parameters) into oracle/_ref/prog_<model>/main: their save() output files
+are the reference results that the whole `-b cuda` program must reproduce.
 """
 import os
 import subprocess
@@ -33,6 +37,15 @@ CASES = {
                                          "num_timesteps": "100"}, {}),
     "boids2d_4096_float": ("boids2d", {"num_agents": "4096", "agent_density": "3200.0",
                                        "num_timesteps": "100"}, {"use_float": "true"}),
+}
+
+# model -> (example, -C config): whole reference programs at default parameters
+PROGRAMS = {
+    "circle": ("circle", {}),
+    "circle3d": ("circle3d", {}),
+    "boids2d": ("boids2d", {}),
+    "game_of_life": ("game_of_life", {}),
+    "boids2d_float": ("boids2d", {"use_float": "true"}),
 }
 
 
@@ -73,6 +86,24 @@ def build_case(name):
                            os.path.join(HERE, "ref_harness.c"), "-o", os.path.join(d, "harness.o")])
     subprocess.check_call(["gcc", os.path.join(d, "main.o"), os.path.join(d, "libabl.o"),
                            os.path.join(d, "harness.o"), "-lm", "-fopenmp", "-o",
+                           os.path.join(d, "main")])
+    return os.path.join(d, "main")
+
+
+def build_program(model):
+    """The reference compiler's unmodified `c` output for `model` at default
+    parameters, compiled with the build line of CBackend.cpp:21-27."""
+    example, config = PROGRAMS[model]
+    d = os.path.join(OUT, "prog_" + model)
+    os.makedirs(d, exist_ok=True)
+    cmd = [COMPILER, "-A", os.path.join(REF, "asset"), "-i",
+           os.path.join(REF, "examples", example + ".abl"), "-o", d, "-b", "c"]
+    for k, v in config.items():
+        cmd += ["-C", f"{k}={v}"]
+    subprocess.check_call(cmd)
+    fl = ["-DLIBABL_USE_FLOAT=1"] if config.get("use_float") == "true" else []
+    subprocess.check_call(["gcc", "-O2", "-std=c99", *fl, os.path.join(d, "main.c"),
+                           os.path.join(d, "libabl.c"), "-lm", "-fopenmp", "-o",
                            os.path.join(d, "main")])
     return os.path.join(d, "main")
 

@@ -9,6 +9,10 @@ runs it with the per-timestep dump hook, and writes
                     state at every timestep 0..T
   <case>_init.bin   the packed initial state (agent records, members in
                     declaration order, no padding)
+It also builds the unmodified reference programs of build_ref.PROGRAMS
+(default parameters), runs each in an empty directory and records the file
+its save() writes in
+  programs.json     per model: output file name, size and SHA-256
 The GPU and oracle tests compare against these files; nothing reads the
 reference tree at test time.
 """
@@ -84,6 +88,24 @@ def main():
         with open(os.path.join(HERE, name + ".json"), "w") as f:
             json.dump(meta, f, indent=1)
         print(name, len(states) - 1, "steps")
+    programs = {}
+    for model, (example, config) in build_ref.PROGRAMS.items():
+        exe = build_ref.build_program(model)
+        run_dir = os.path.join(os.path.dirname(exe), "run")
+        os.makedirs(run_dir, exist_ok=True)
+        for f in os.listdir(run_dir):
+            os.remove(os.path.join(run_dir, f))
+        env = dict(os.environ, OMP_NUM_THREADS=str(os.cpu_count()))
+        subprocess.check_call([exe], cwd=run_dir, env=env, stdout=subprocess.DEVNULL)
+        (out,) = os.listdir(run_dir)
+        data = open(os.path.join(run_dir, out), "rb").read()
+        programs[model] = {"example": example, "config": config, "file": out,
+                           "bytes": len(data), "sha256": hashlib.sha256(data).hexdigest(),
+                           "source": "reference c backend program at default parameters "
+                                     "(OpenABL -b c, gcc -O2 -std=c99 -fopenmp, x86-64)"}
+        print(model, out, len(data), "bytes")
+    with open(os.path.join(HERE, "programs.json"), "w") as f:
+        json.dump(programs, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,106 @@
+"""The OpenABL compiler with the `cuda` backend plugged in (CPU only).
+
+These tests need an OpenABL source tree (the compiler is built from it by
+openabl_gb300/backend/Makefile with the hand-written front end in place of
+the flex/bison output); they are skipped where none is present.
+
+- The reference's lint goldens (test.sh:34-52): `--lint-only` on every
+  test/*.abl that has a .exp file prints exactly the expected errors,
+  compared with `diff -b` as test.sh does.  This pins the hand-written
+  parser: every error message carries the line the bison parser would
+  have recorded.
+- The reference's example smoke test (test.sh:55-93) for `-b cuda`: every
+  example either generates code or is refused with exit code 2 (a
+  BackendError, which test.sh counts as a skip).
+- The model sources compiled into the library are what the generator
+  prints today (openabl_gb300/generated/regenerate.py writes them).
+"""
+import glob
+import json
+import os
+import shutil
+import subprocess
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = os.environ.get("OPENABL_REF", "/root/reference")
+COMPILER = os.path.join(REPO, "_build", "compiler", "openabl")
+GEN = os.path.join(REPO, "openabl_gb300", "generated")
+
+pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")),
+                                reason="no OpenABL source tree to build the compiler from")
+
+
+@pytest.fixture(scope="module")
+def compiler():
+    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "openabl_gb300", "backend"),
+                           "-j8", f"REF={REF}"], stdout=subprocess.DEVNULL)
+    return COMPILER
+
+
+def _lint_cases():
+    if not os.path.isdir(os.path.join(REF, "test")):
+        return []
+    return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(REF, "test", "*.abl"))
+                  if os.path.exists(f[:-4] + ".exp"))
+
+
+@pytest.mark.parametrize("case", _lint_cases())
+def test_lint_golden(compiler, case, tmp_path):
+    src = os.path.join(REF, "test", case + ".abl")
+    out = tmp_path / (case + ".out")
+    with open(out, "w") as f:
+        subprocess.run([compiler, "-A", os.path.join(REF, "asset"), "--lint-only", "-i", src],
+                       stderr=f, stdout=subprocess.DEVNULL)
+    r = subprocess.run(["diff", "-b", str(out), os.path.join(REF, "test", case + ".exp")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+
+
+def _examples():
+    return sorted(os.path.basename(f)[:-4]
+                  for f in glob.glob(os.path.join(REF, "examples", "*.abl")))
+
+
+@pytest.mark.parametrize("example", _examples())
+def test_example_generates_or_is_refused(compiler, example, tmp_path):
+    r = subprocess.run([compiler, "-A", os.path.join(REF, "asset"), "-i",
+                        os.path.join(REF, "examples", example + ".abl"), "-o", str(tmp_path),
+                        "-b", "cuda", "-C", f"cuda.model={example}"],
+                       capture_output=True, text=True)
+    assert r.returncode in (0, 2), r.stdout + r.stderr
+    if r.returncode == 0:
+        for f in (example + ".cu", example + ".globals.json", "build.sh", "run.sh",
+                  "abl_runtime.cu", "openabl_cuda.h"):
+            assert (tmp_path / f).exists(), f
+        json.load(open(tmp_path / (example + ".globals.json")))
+
+
+def test_unsupported_feature_exits_with_backend_error(compiler, tmp_path):
+    # keratinocyte declares constant arrays, which the cuda backend refuses.
+    r = subprocess.run([compiler, "-A", os.path.join(REF, "asset"), "-i",
+                        os.path.join(REF, "examples", "keratinocyte.abl"), "-o", str(tmp_path),
+                        "-b", "cuda"], capture_output=True, text=True)
+    assert r.returncode == 2
+
+
+def test_committed_model_sources_are_current(compiler):
+    sys.path.insert(0, GEN)
+    import regenerate
+    for model, (example, config) in regenerate.MODELS.items():
+        out = regenerate.run_compiler(model, {})
+        with open(os.path.join(out, model + ".cu")) as f:
+            now = f.read()
+        shutil.rmtree(out)
+        with open(os.path.join(GEN, model + ".cu")) as f:
+            committed = f.read()
+        assert now == committed, f"{model}.cu differs from the generator's output"
+    configs = json.load(open(os.path.join(GEN, "configs.json")))
+    for name, (model, params) in regenerate.CONFIGS.items():
+        out = regenerate.run_compiler(model, params)
+        with open(os.path.join(out, model + ".globals.json")) as f:
+            manifest = json.load(f)
+        shutil.rmtree(out)
+        assert configs[name]["globals"] == manifest["globals"], name
