@@ -1,6 +1,7 @@
 /* Diagnostics of the OpenABL CUDA runtime (no counterpart in the reference,
  * which has no GPU path of its own): instruction-rate probes used to state
- * the FP64 roofline of the neighbour kernels. */
+ * the FP64 roofline of the neighbour kernels, and a device-side check of the
+ * kernels' integer-divisor division. */
 #ifndef OPENABL_CUDA_DIAG_H
 #define OPENABL_CUDA_DIAG_H
 
@@ -8,11 +9,20 @@
 extern "C" {
 #endif
 
+#define ABL_DIAG_E_ARG -2
 #define ABL_DIAG_E_CUDA -3
 
 /* Measured FP64 fused-multiply-add, add and multiply instructions per second
  * (per lane) on the current device; any pointer may be NULL. */
 int abl_diag_fp64_rates(double *dfma_per_s, double *dadd_per_s, double *dmul_per_s);
+
+/* Checks the step kernels' division of a double by an int count (a two-term
+ * reciprocal table, abl::div_int in the runtime) against IEEE division on
+ * the device: per_n operands for every n from -3 to 1027 (both ends outside
+ * the table), over the whole double range.  Reports how many quotients were
+ * compared and how many differed in any bit (NaN equals NaN). */
+int abl_diag_check_int_division(unsigned long long seed, long per_n,
+                                unsigned long long *checked, unsigned long long *mismatches);
 
 #ifdef __cplusplus
 }

@@ -97,7 +97,8 @@ void CudaBackend::generate(AST::Script &script, const BackendContext &ctx) {
       ? rt + "/openabl_cuda.h" : std::string(ABL_CUDA_INCLUDE_DIR) + "/openabl_cuda.h";
   copyFile(header, ctx.outputDir + "/openabl_cuda.h");
   writeToFile(ctx.outputDir + "/build.sh",
-              "nvcc -gencode arch=compute_103a,code=sm_103a -O3 -fmad=false -std=c++17 -diag-suppress 177 "
+              "nvcc -gencode arch=compute_103a,code=sm_103a -O3 -fmad=false -Xcompiler -ffp-contract=off "
+              "-std=c++17 -diag-suppress 177 "
               "-DABL_STANDALONE_MAIN -I. " + model + ".cu abl_runtime.cu abl_host.cpp -o main\n");
   writeToFile(ctx.outputDir + "/run.sh", "./main\n");
   makeFileExecutable(ctx.outputDir + "/build.sh");

@@ -51,7 +51,7 @@ struct Collector : public AST::Visitor {
   std::vector<const AST::VarExpression *> varExprs;
   std::vector<const AST::VarDeclarationStatement *> decls;
   std::vector<const AST::ForStatement *> fors;
-  int breaks = 0, returns = 0;
+  int breaks = 0, returns = 0, continues = 0, whiles = 0;
 
   void enter(AST::CallExpression &e) override { calls.push_back(&e); }
   void enter(AST::ForStatement &s) override {
@@ -64,6 +64,8 @@ struct Collector : public AST::Visitor {
   void enter(AST::VarDeclarationStatement &s) override { decls.push_back(&s); }
   void enter(AST::BreakStatement &) override { breaks++; }
   void enter(AST::ReturnStatement &) override { returns++; }
+  void enter(AST::ContinueStatement &) override { continues++; }
+  void enter(AST::WhileStatement &) override { whiles++; }
 };
 
 template <typename N>
@@ -199,6 +201,95 @@ std::set<const AST::VarDeclarationStatement *> findLazyDistances(
   return out;
 }
 
+// Conditional accumulations that a near loop can run in a second pass.
+//
+// A top-level statement `if (C) B` (no else) of a near body qualifies when B
+// only updates variables declared before the loop ("its accumulators") that
+// nothing else in the body mentions, reads nothing but the neighbour, globals,
+// its own locals and accumulators, and variables the body never writes, and
+// has no calls other than pure builtins, no loops and no jumps; the body as a
+// whole has no break or return.  Then running B for the iterations where C
+// held, in the same ascending neighbour order but after the rest of the
+// body's iterations over the same chunk, performs every accumulator's updates
+// in the same order on the same values, so the results are identical.  The
+// gain: B's instructions issue once per neighbour where C held in some lane,
+// instead of once per neighbour where C held in any lane of the warp (e.g.
+// boids2d's collision sum, which every lane hits at its own agent).  Only
+// blocks that update floating-point accumulators are moved.
+std::vector<const AST::IfStatement *> findDeferredIfs(const AST::Script &script,
+                                                      const AST::FunctionDeclaration *step,
+                                                      const AST::ForStatement &loop) {
+  std::vector<const AST::IfStatement *> out;
+  auto *block = dynamic_cast<const AST::BlockStatement *>(&*loop.stmt);
+  if (!block || !step) return out;
+  Collector body = collect(*loop.stmt);
+  if (body.breaks || body.returns) return out;
+  std::set<VarId> inner;  // declared inside the body, or the loop variable
+  inner.insert(loop.var->id);
+  for (auto *d : body.decls) inner.insert(d->var->id);
+  for (auto *f : body.fors) inner.insert(f->var->id);
+  std::set<VarId> params;
+  for (const AST::ParamPtr &p : *step->params) params.insert(p->var->id);
+  if (step->isParallelStep()) params.insert(step->stepParam().outVar->id);
+  auto isGlobalVar = [&](VarId id) {
+    return script.scope.has(id) && script.scope.get(id).isGlobal;
+  };
+  std::map<VarId, int> bodyRefs;
+  for (auto *v : body.varExprs) bodyRefs[v->var->id]++;
+  std::set<VarId> bodyWritten;
+  for (auto *a : body.assigns) {
+    if (auto *r = targetRoot(*a->left)) bodyWritten.insert(r->var->id);
+  }
+  for (auto *a : body.assignOps) {
+    if (auto *r = targetRoot(*a->left)) bodyWritten.insert(r->var->id);
+  }
+  for (const AST::StatementPtr &st : *block->stmts) {
+    auto *ifs = dynamic_cast<const AST::IfStatement *>(&*st);
+    if (!ifs || ifs->elseStmt) continue;
+    Collector b = collect(*ifs->ifStmt);
+    if (b.breaks || b.returns || b.continues || b.whiles || !b.fors.empty()) continue;
+    bool ok = true, floatTarget = false;
+    for (auto *call : b.calls) {
+      if (call->kind == AST::CallExpression::Kind::USER) ok = false;
+      if (call->isBuiltin() && isHostOnlyBuiltin(call->name)) ok = false;
+    }
+    std::set<VarId> local, targets;
+    for (auto *d : b.decls) local.insert(d->var->id);
+    auto noteTarget = [&](const AST::Expression &left) {
+      const AST::VarExpression *r = targetRoot(left);
+      if (!r) {
+        ok = false;
+        return;
+      }
+      VarId id = r->var->id;
+      if (local.count(id)) return;
+      if (inner.count(id) || params.count(id) || isGlobalVar(id) || left.type.isAgent()) {
+        ok = false;
+        return;
+      }
+      targets.insert(id);
+      if (left.type.isFloat() || left.type.isVec()) floatTarget = true;
+    };
+    for (auto *a : b.assigns) noteTarget(*a->left);
+    for (auto *a : b.assignOps) noteTarget(*a->left);
+    if (!ok || targets.empty() || !floatTarget) continue;
+    std::map<VarId, int> refs;
+    for (auto *v : b.varExprs) refs[v->var->id]++;
+    for (auto &kv : refs) {
+      VarId id = kv.first;
+      if (targets.count(id)) {
+        if (bodyRefs[id] != kv.second) ok = false;  // mentioned elsewhere in the body
+      } else if (id == loop.var->id || local.count(id) || isGlobalVar(id)) {
+        // the neighbour, B's own locals, globals
+      } else if (inner.count(id) || bodyWritten.count(id)) {
+        ok = false;  // a per-iteration value of the rest of the body
+      }
+    }
+    if (ok) out.push_back(ifs);
+  }
+  return out;
+}
+
 }  // namespace
 
 void CudaPrinter::print(const AST::VarDeclarationStatement &stmt) {
@@ -261,7 +352,64 @@ int CudaPrinter::memberIndex(const AST::AgentDeclaration *agent,
   return -1;
 }
 
+// Whether evaluating `e` can draw random numbers: a random()/randomInt() call
+// in it, or a call of a user function that draws (directly or further down).
+bool CudaPrinter::mayDraw(const AST::Node &e) {
+  Collector c = collect(const_cast<AST::Node &>(e));
+  for (auto *call : c.calls) {
+    if (call->isBuiltin() && (call->name == "random" || call->name == "randomInt")) return true;
+    if (call->kind != AST::CallExpression::Kind::USER || !call->calledFunc) continue;
+    auto it = drawsMemo.find(call->calledFunc);
+    if (it == drawsMemo.end()) {
+      drawsMemo[call->calledFunc] = false;  // a recursive call draws nothing by itself
+      bool d = mayDraw(*call->calledFunc);
+      drawsMemo[call->calledFunc] = d;
+      if (d) return true;
+    } else if (it->second) {
+      return true;
+    }
+  }
+  return false;
+}
+
+// C leaves the evaluation order of function arguments unspecified, so a call
+// like float2_create(random_float(..), random_float(..)) -- the expansion of
+// random(float2 lo, float2 hi), asset/lib.abl -- draws its components in an
+// order the C compiler picks.  The reference programs built with gcc on
+// x86-64 evaluate arguments from last to first (the y component is drawn
+// before x); the generated code fixes that order whenever two or more
+// arguments can draw, so results do not depend on the host compiler or CPU.
+bool CudaPrinter::printSequencedCall(const AST::CallExpression &expr) {
+  const size_t n = expr.args->size();
+  if (n < 2) return false;
+  if (expr.isBuiltin() && (isHostOnlyBuiltin(expr.name) && expr.name != "random"
+                           && expr.name != "randomInt")) {
+    return false;
+  }
+  if (expr.isCtor() && !expr.type.isVec()) return false;
+  int drawing = 0;
+  for (const AST::ExpressionPtr &arg : *expr.args) drawing += mayDraw(*arg) ? 1 : 0;
+  if (drawing < 2) return false;
+  const std::string tmp = "abl_e" + std::to_string(++sequencedCounter) + "_";
+  *this << "([&]() { ";
+  for (size_t k = n; k-- > 0;) *this << "const auto " << tmp << k << " = " << *(*expr.args)[k] << "; ";
+  *this << "return ";
+  if (expr.isCtor()) {
+    *this << "float" << expr.type.getVecLen() << "_create(";
+  } else if (expr.kind == AST::CallExpression::Kind::USER) {
+    *this << expr.calledSig.name << "(abl_G, abl_R, ";
+  } else if (expr.name == "random" || expr.name == "randomInt") {
+    *this << (expr.name == "random" ? "abl_random(abl_R, " : "abl_random_int(abl_R, ");
+  } else {
+    *this << expr.calledSig.name << "(";
+  }
+  for (size_t k = 0; k < n; k++) *this << (k ? ", " : "") << tmp << k;
+  *this << "); }())";
+  return true;
+}
+
 void CudaPrinter::print(const AST::CallExpression &expr) {
+  if (printSequencedCall(expr)) return;
   if (expr.kind == AST::CallExpression::Kind::USER) {
     *this << expr.calledSig.name << "(abl_G, abl_R";
     for (const AST::ExpressionPtr &arg : *expr.args) *this << ", " << *arg;
@@ -337,6 +485,15 @@ void CudaPrinter::print(const AST::AgentCreationExpression &expr) {
     *this << "abl_a." << m->name << " = " << *m->expr << "; ";
   }
   *this << "return abl_a; }())";
+}
+
+void CudaPrinter::print(const AST::IfStatement &stmt) {
+  auto it = deferredMasks.find(&stmt);
+  if (it != deferredMasks.end()) {
+    *this << "if (" << *stmt.condExpr << ") " << it->second << " |= 1ull << abl_k;";
+    return;
+  }
+  CPrinter::print(stmt);
 }
 
 void CudaPrinter::print(const AST::WhileStatement &stmt) {
@@ -427,6 +584,15 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   *this << nl << "int " << pslot << " = " << c << ".slot(0);" << nl << agentDecl->name << " "
         << pnx << ";";
   loadMembers(pnx, pslot);
+  std::vector<const AST::IfStatement *> deferred;
+  if (fnKind == FnKind::STEP) deferred = findDeferredIfs(script, stepDecl, stmt);
+  std::map<const AST::IfStatement *, std::string> savedMasks = deferredMasks;
+  deferredMasks.clear();
+  for (size_t j = 0; j < deferred.size(); j++) {
+    std::string mask = "abl_dm" + sid + "_" + std::to_string(j);
+    deferredMasks[deferred[j]] = mask;
+    *this << nl << "unsigned long long " << mask << " = 0ull;";
+  }
   *this << nl << "for (int abl_k = 0; abl_k < " << c << ".cnt; ++abl_k) {" << indent << nl
         << "const int " << slot << " = " << pslot << ";" << nl
         << agentDecl->name << " " << nxs << " = " << pnx << ";" << nl
@@ -445,9 +611,22 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   nearNeedsEnd = false;
   nearLoopDepth = 0;
   *this << *stmt.stmt;
-  nearLoopDepth = -1;
   lazyDecls.clear();
-  *this << outdent << nl << "}" << outdent << nl << "}" << outdent << nl << "}";
+  *this << outdent << nl << "}";
+  // Second pass over the chunk: the deferred conditional blocks, each over
+  // the neighbours where its condition held, in ascending order.
+  for (size_t j = 0; j < deferred.size(); j++) {
+    const std::string &mask = deferredMasks[deferred[j]];
+    *this << nl << "for (unsigned long long abl_m = " << mask << "; abl_m; abl_m &= abl_m - 1ull) {"
+          << indent << nl << "const int " << slot << " = " << c
+          << ".slot(__ffsll((long long) abl_m) - 1);" << nl << agentDecl->name << " " << nxs << ";";
+    loadMembers(nxs, slot);
+    *this << nl << agentDecl->name << "* " << *stmt.var << " = &" << nxs << ";" << nl
+          << *deferred[j]->ifStmt << outdent << nl << "}";
+  }
+  deferredMasks = savedMasks;
+  nearLoopDepth = -1;
+  *this << outdent << nl << "}" << outdent << nl << "}";
   if (nearNeedsEnd) *this << nl << nearEndLabel << ": ;";
   nearEndLabel = savedLabel;
   nearNeedsEnd = savedNeeds;

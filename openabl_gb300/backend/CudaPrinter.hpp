@@ -16,6 +16,7 @@
 //     openabl_gb300/csrc/abl_model.h.
 #pragma once
 
+#include <map>
 #include <set>
 #include <string>
 #include <vector>
@@ -34,6 +35,7 @@ struct CudaPrinter : public CPrinter {
   void print(const AST::CallExpression &) override;
   void print(const AST::AgentCreationExpression &) override;
   void print(const AST::ForStatement &) override;
+  void print(const AST::IfStatement &) override;
   void print(const AST::WhileStatement &) override;
   void print(const AST::BreakStatement &) override;
   void print(const AST::SimulateStatement &) override;
@@ -55,6 +57,9 @@ private:
   // loop-invariant values (printed as abl::lazy_dist).
   std::set<const AST::VarDeclarationStatement *> lazyDecls;
   std::string nearQuery, nearSlot;
+  // Conditional blocks of the current near body run in a second pass over
+  // each chunk, and the per-chunk mask that records where their condition held.
+  std::map<const AST::IfStatement *, std::string> deferredMasks;
 
   // Kind of function being printed (decides how builtins are lowered).
   enum class FnKind { HOST, STEP, USER, SEQ } fnKind = FnKind::HOST;
@@ -92,6 +97,12 @@ private:
   void printUserFunction(const AST::FunctionDeclaration &decl);
   void printSeqStep(const AST::FunctionDeclaration &decl);
   int memberIndex(const AST::AgentDeclaration *agent, const AST::AgentMember *member) const;
+  // Calls whose arguments draw random numbers are printed with a fixed
+  // (last to first) argument evaluation order.
+  bool mayDraw(const AST::Node &e);
+  bool printSequencedCall(const AST::CallExpression &expr);
+  std::map<const AST::FunctionDeclaration *, bool> drawsMemo;
+  int sequencedCounter = 0;
   const AST::FunctionDeclaration *seqStep = nullptr;
 };
 

@@ -4,6 +4,7 @@
 // latency; the grid covers every SM several times.
 #include <cuda_runtime.h>
 
+#include "abl_device.cuh"
 #include "openabl_cuda_diag.h"
 
 namespace {
@@ -53,7 +54,61 @@ int time_op(double *ops_per_s) {
   return 0;
 }
 
+// Operands for the division check: random bit patterns over the whole
+// double range (guard cases included), sums of positions in [0, 40), signed
+// values, and exact multiples of n.
+__device__ double division_operand(uint64_t seed, long i, int n) {
+  uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t) (i + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  switch (i & 3) {
+    case 0: return __longlong_as_double((long long) z);
+    case 1: return (double) (z >> 11) * 0x1p-53 * 40.0;
+    case 2: return ((double) (z >> 11) * 0x1p-53 - 0.5) * 64.0;
+    default: return (double) (long) (z % 100000) * 0.001 * n;
+  }
+}
+
+__global__ void k_division_check(uint64_t seed, long per_n, unsigned long long *bad,
+                                 unsigned long long *checked) {
+  const long total = per_n * (abl::kRecipN + 7);
+  unsigned long long nbad = 0, nchk = 0;
+  for (long t = (long) blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long) gridDim.x * blockDim.x) {
+    const int n = (int) (t / per_n) - 3;  // n from -3 to kRecipN + 3: both guard sides
+    const double a = division_operand(seed, t, n);
+    const double q = abl::div_int(a, n);
+    const double r = __ddiv_rn(a, (double) n);
+    nchk++;
+    // Equal bits, or both NaN (the quotient of a NaN is a NaN either way).
+    if (__double_as_longlong(q) != __double_as_longlong(r) && !(q != q && r != r)) nbad++;
+  }
+  atomicAdd(bad, nbad);
+  atomicAdd(checked, nchk);
+}
+
 }  // namespace
+
+extern "C" int abl_diag_check_int_division(unsigned long long seed, long per_n,
+                                           unsigned long long *checked,
+                                           unsigned long long *mismatches) {
+  if (per_n <= 0 || !checked || !mismatches) return ABL_DIAG_E_ARG;
+  unsigned long long *d = nullptr;
+  if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return ABL_DIAG_E_CUDA;
+  cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_division_check<<<sms * 4, 256>>>(seed, per_n, d, d + 1);
+  unsigned long long h[2] = {0, 0};
+  cudaError_t err = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (err != cudaSuccess) return ABL_DIAG_E_CUDA;
+  *mismatches = h[0];
+  *checked = h[1];
+  return 0;
+}
 
 extern "C" int abl_diag_fp64_rates(double *dfma_per_s, double *dadd_per_s, double *dmul_per_s) {
   int r = 0;

@@ -42,6 +42,20 @@ __host__ __device__ static inline float2 float2_mul_scalar(float2 a, abl_float s
 __host__ __device__ static inline float2 float2_div_scalar(float2 a, abl_float s) {
   return float2_create(a.x / s, a.y / s);
 }
+// Division by an int (e.g. a neighbour count): the same value as converting
+// the int and dividing, computed on the device by abl::div_int in FP64.
+// A template on exactly `int`, so calls with a floating divisor keep the
+// overload above.
+__host__ __device__ static inline abl_float abl_div_count(abl_float a, int n) {
+#ifdef __CUDA_ARCH__
+  if (sizeof(abl_float) == sizeof(double)) return (abl_float) abl::div_int((double) a, n);
+#endif
+  return a / (abl_float) n;
+}
+template <typename I, typename std::enable_if<std::is_same<I, int>::value, int>::type = 0>
+__host__ __device__ static inline float2 float2_div_scalar(float2 a, I s) {
+  return float2_create(abl_div_count(a.x, s), abl_div_count(a.y, s));
+}
 __host__ __device__ static inline bool float2_equals(float2 a, float2 b) {
   return a.x == b.x && a.y == b.y;
 }
@@ -65,6 +79,10 @@ __host__ __device__ static inline float3 float3_mul_scalar(float3 a, abl_float s
 }
 __host__ __device__ static inline float3 float3_div_scalar(float3 a, abl_float s) {
   return float3_create(a.x / s, a.y / s, a.z / s);
+}
+template <typename I, typename std::enable_if<std::is_same<I, int>::value, int>::type = 0>
+__host__ __device__ static inline float3 float3_div_scalar(float3 a, I s) {
+  return float3_create(abl_div_count(a.x, s), abl_div_count(a.y, s), abl_div_count(a.z, s));
 }
 __host__ __device__ static inline bool float3_equals(float3 a, float3 b) {
   return a.x == b.x && a.y == b.y && a.z == b.z;

@@ -64,10 +64,10 @@ struct abl_cols_Boid {
 };
 
 __host__ __device__ static inline float2 random_1(const abl_globals &abl_G, abl::rng &abl_R, float2 min, float2 max) {
-    return float2_create(abl_random(abl_R, min.x, max.x), abl_random(abl_R, min.y, max.y));
+    return ([&]() { const auto abl_e1_1 = abl_random(abl_R, min.y, max.y); const auto abl_e1_0 = abl_random(abl_R, min.x, max.x); return float2_create(abl_e1_0, abl_e1_1); }());
 }
 __host__ __device__ static inline float3 random_2(const abl_globals &abl_G, abl::rng &abl_R, float3 min, float3 max) {
-    return float3_create(abl_random(abl_R, min.x, max.x), abl_random(abl_R, min.y, max.y), abl_random(abl_R, min.z, max.z));
+    return ([&]() { const auto abl_e2_2 = abl_random(abl_R, min.z, max.z); const auto abl_e2_1 = abl_random(abl_R, min.y, max.y); const auto abl_e2_0 = abl_random(abl_R, min.x, max.x); return float3_create(abl_e2_0, abl_e2_1, abl_e2_2); }());
 }
 __host__ __device__ static inline float random_3(const abl_globals &abl_G, abl::rng &abl_R, float max) {
     return abl_random(abl_R, 0, max);
@@ -134,6 +134,7 @@ __device__ static void update_boid(const abl_globals &abl_G, const abl_near_view
             Boid abl_pnx1;
             abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
             abl_pnx1.velocity = ((const float2 *) abl_NB.cols[1])[abl_pslot1];
+            unsigned long long abl_dm1_0 = 0ull;
             for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
                 const int abl_slot1 = abl_pslot1;
                 Boid abl_nx1 = abl_pnx1;
@@ -148,10 +149,18 @@ __device__ static void update_boid(const abl_globals &abl_G, const abl_near_view
                     global_velocity = float2_add(global_velocity, nx->velocity);
                     interaction_count += 1;
                     const auto separation = abl::make_lazy_dist(abl_q1, abl_NB, abl_slot1, [&]() -> abl_float { return dist_float2(in->pos, nx->pos); });
-                    if ((separation < abl_G.separation_radius)) {
-                        collision_center = float2_add(collision_center, nx->pos);
-                        collision_count += 1;
-                    }
+                    if ((separation < abl_G.separation_radius)) abl_dm1_0 |= 1ull << abl_k;
+                }
+            }
+            for (unsigned long long abl_m = abl_dm1_0; abl_m; abl_m &= abl_m - 1ull) {
+                const int abl_slot1 = abl_c1.slot(__ffsll((long long) abl_m) - 1);
+                Boid abl_nx1;
+                abl_nx1.pos = ((const float2 *) abl_NB.cols[0])[abl_slot1];
+                abl_nx1.velocity = ((const float2 *) abl_NB.cols[1])[abl_slot1];
+                Boid* nx = &abl_nx1;
+                {
+                    collision_center = float2_add(collision_center, nx->pos);
+                    collision_count += 1;
                 }
             }
         }

@@ -51,10 +51,10 @@ struct abl_cols_Point {
 };
 
 __host__ __device__ static inline float2 random_1(const abl_globals &abl_G, abl::rng &abl_R, float2 min, float2 max) {
-    return float2_create(abl_random(abl_R, min.x, max.x), abl_random(abl_R, min.y, max.y));
+    return ([&]() { const auto abl_e1_1 = abl_random(abl_R, min.y, max.y); const auto abl_e1_0 = abl_random(abl_R, min.x, max.x); return float2_create(abl_e1_0, abl_e1_1); }());
 }
 __host__ __device__ static inline float3 random_2(const abl_globals &abl_G, abl::rng &abl_R, float3 min, float3 max) {
-    return float3_create(abl_random(abl_R, min.x, max.x), abl_random(abl_R, min.y, max.y), abl_random(abl_R, min.z, max.z));
+    return ([&]() { const auto abl_e2_2 = abl_random(abl_R, min.z, max.z); const auto abl_e2_1 = abl_random(abl_R, min.y, max.y); const auto abl_e2_0 = abl_random(abl_R, min.x, max.x); return float3_create(abl_e2_0, abl_e2_1, abl_e2_2); }());
 }
 __host__ __device__ static inline float random_3(const abl_globals &abl_G, abl::rng &abl_R, float max) {
     return abl_random(abl_R, 0, max);

@@ -86,6 +86,19 @@ def fp64_rates():
     return a.value, b.value, c.value
 
 
+def check_int_division(seed=1, per_n=200000):
+    """Device check of the step kernels' division by an int count against
+    IEEE division: returns (quotients compared, quotients that differ)."""
+    L = _load()
+    u = ctypes.c_ulonglong
+    L.abl_diag_check_int_division.argtypes = [u, ctypes.c_long, ctypes.POINTER(u),
+                                              ctypes.POINTER(u)]
+    checked, bad = u(), u()
+    _check(L.abl_diag_check_int_division(seed, per_n, ctypes.byref(checked), ctypes.byref(bad)),
+           "abl_diag_check_int_division")
+    return checked.value, bad.value
+
+
 def _check(code, what):
     if code != 0:
         raise AblError(code, what)

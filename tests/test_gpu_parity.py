@@ -100,6 +100,15 @@ def test_game_of_life_4096_matches_oracle():
     sim.close()
 
 
+def test_integer_count_division_is_ieee_division():
+    """Step kernels divide by neighbour counts with a two-term reciprocal
+    table (abl::div_int); every quotient must equal IEEE a / n bit for bit,
+    here for 2e5 operands per n over n = -3..1027 (~2e8 quotients)."""
+    checked, bad = o.runtime.check_int_division(seed=7, per_n=200000)
+    assert checked == 200000 * 1031
+    assert bad == 0
+
+
 def test_budget_exhaustion_is_reported():
     model, g = o.globals_for_config("boids2d_4096")
     meta, state = load_case("boids2d_4096")

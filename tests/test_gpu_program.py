@@ -1,0 +1,59 @@
+"""Whole generated programs as a drop-in for the reference's.
+
+`OpenABL -b cuda` writes <model>.cu (openabl_gb300/generated/ holds the
+generator's output for each model): kernels plus the program's main(), which
+initialises the agents on the host from the reference's xorshift stream
+(asset/c/libabl.c:8-39), runs the simulate loop on the GPU through the C ABI
+and writes the result with save() (libabl.c:215-231).  Here each program is
+built with the backend's build.sh line (-DABL_STANDALONE_MAIN, -fmad=false)
+and run in an empty directory; the file its save() writes must equal, byte
+for byte, the file the reference `c` program writes at the same (default)
+parameters (tests/golden/programs.json, made by make_golden.py).
+"""
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(REPO, "openabl_gb300", "csrc")
+GEN = os.path.join(REPO, "openabl_gb300", "generated")
+INC = os.path.join(REPO, "include")
+PROGRAMS = json.load(open(os.path.join(REPO, "tests", "golden", "programs.json")))
+
+# The cuda backend's build.sh line (openabl_gb300/backend/CudaBackend.cpp).
+NVCC = [shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc", "-gencode",
+        "arch=compute_103a,code=sm_103a", "-O3", "-fmad=false", "-Xcompiler",
+        "-ffp-contract=off", "-std=c++17",
+        "-diag-suppress", "177", "-DABL_STANDALONE_MAIN", "-I", CSRC, "-I", INC]
+
+
+@pytest.fixture(scope="module")
+def runtime_objects(tmp_path_factory):
+    d = tmp_path_factory.mktemp("abl_program_runtime")
+    objs = []
+    for src in ("abl_runtime.cu", "abl_host.cpp"):
+        obj = str(d / (src + ".o"))
+        subprocess.check_call(NVCC + ["-c", os.path.join(CSRC, src), "-o", obj])
+        objs.append(obj)
+    return objs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("model", sorted(PROGRAMS))
+def test_generated_program_writes_the_reference_output(model, runtime_objects, tmp_path):
+    want = PROGRAMS[model]
+    obj = str(tmp_path / (model + ".o"))
+    exe = str(tmp_path / "main")
+    subprocess.check_call(NVCC + ["-c", os.path.join(GEN, model + ".cu"), "-o", obj])
+    subprocess.check_call(NVCC[:3] + [obj] + runtime_objects + ["-o", exe])
+    run_dir = tmp_path / "run"
+    run_dir.mkdir()
+    subprocess.run([exe], cwd=run_dir, check=True, stdout=subprocess.DEVNULL, timeout=300)
+    assert sorted(os.listdir(run_dir)) == [want["file"]]
+    data = (run_dir / want["file"]).read_bytes()
+    assert len(data) == want["bytes"]
+    assert hashlib.sha256(data).hexdigest() == want["sha256"]
