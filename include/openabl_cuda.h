@@ -138,13 +138,17 @@ int abl_step_kernel_time(abl_ctx *ctx, int step, double *seconds, long *launches
 int abl_set_balance(abl_ctx *ctx, int enable);
 /* How ordered near loops find their neighbours in ascending id: ABL_NEAR_AUTO
  * (default) picks per step; RUNS sorts each agent's neighbours from the
- * cells' own runs, ROWS (2D) merges three precomputed row lists, LISTS reads
- * whole precomputed neighbourhood lists.  Results are identical in every
- * mode; this is a tuning and testing control. */
+ * cells' own runs, ROWS (2D) merges three precomputed row lists per agent,
+ * LISTS reads whole precomputed neighbourhood lists, BLOCK (2D, loops around
+ * the step's own agents) has each thread block merge the row lists once per
+ * cell in shared memory (falling back to ROWS for a block whose lists do not
+ * fit).  Results are identical in every mode; this is a tuning and testing
+ * control. */
 #define ABL_NEAR_AUTO 0
 #define ABL_NEAR_RUNS 1
 #define ABL_NEAR_ROWS 2
 #define ABL_NEAR_LISTS 3
+#define ABL_NEAR_BLOCK 4
 int abl_set_near_mode(abl_ctx *ctx, int mode);
 int abl_destroy(abl_ctx *ctx);
 const char *abl_strerror(int code);

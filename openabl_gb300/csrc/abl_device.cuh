@@ -394,9 +394,14 @@ struct presort_shared {
   int *total;            // in-radius neighbours past the column's lower bound
   int *key;              // sort key: neighbour count, INT_MAX without agent
   int *perm;             // thread -> block agent, ascending key
-  int *resume;           // lists: list index after the stored slots; rows: last stored id
+  int *resume;           // lists: list index after the stored slots; rows: last stored id;
+                         // block lists: block-list index after the stored slots
+  int *bstart, *bend;    // block lists: the agent's cell list within `bl` (bstart -1:
+                         // the column was gathered per agent)
+  int *bl;               // block lists: [block_cap] slots, per cell in ascending id
   unsigned char *fresh;  // column still holds the first `cap` neighbours
   int cap;
+  int block_cap;
   int mode;  // kGather*
 };
 
@@ -408,10 +413,17 @@ __host__ __device__ inline int gather_mode(const abl_near_view &V) {
   return V.ordered ? kGatherLists : (V.rows && V.dim == 2) ? kGatherRows : kGatherRuns;
 }
 
+// Block lists reuse the column area while they are built: it must hold
+// 9 ints per thread plus the scan scratch.
+__host__ __device__ inline bool block_lists_fit(const abl_near_view &V) {
+  return gather_mode(V) == kGatherRows && V.block_cap > 0 && V.cap >= 11;
+}
+
 __host__ __device__ inline size_t presort_bytes(const abl_near_view &V) {
   const size_t B = ABL_STEP_BLOCK;
   const size_t cols = (size_t) V.cap * B * (gather_mode(V) == kGatherRuns ? 2 : 1);
-  return (cols + 4 * B) * sizeof(int) + B;
+  const size_t bl = block_lists_fit(V) ? (size_t) V.block_cap : 0;
+  return (cols + 6 * B + bl) * sizeof(int) + B;
 }
 
 __device__ __forceinline__ presort_shared presort_smem(const abl_near_view &V) {
@@ -431,7 +443,11 @@ __device__ __forceinline__ presort_shared presort_smem(const abl_near_view &V) {
   S.key = p + B;
   S.perm = p + 2 * B;
   S.resume = p + 3 * B;
-  S.fresh = (unsigned char *) (p + 4 * B);
+  S.bstart = p + 4 * B;
+  S.bend = p + 5 * B;
+  S.bl = p + 6 * B;
+  S.block_cap = block_lists_fit(V) ? V.block_cap : 0;
+  S.fresh = (unsigned char *) (S.bl + S.block_cap);
   return S;
 }
 
@@ -486,6 +502,58 @@ __device__ int gather_sorted(const presort_shared &S, const abl_near_view &V,
   return total;
 }
 
+// Filters the candidate slots slot_at(from) .. slot_at(end - 1), which are in
+// ascending id: the in-radius ones are counted and the first S.cap stored in
+// column `col`; `next` receives the index after the last stored candidate.
+// Four candidates are loaded at a time, so their (independent) slot and
+// position loads are in flight together.
+template <int DIM, typename Exact, typename SlotAt>
+__device__ __forceinline__ int filter_candidates(const presort_shared &S, const abl_near_view &V,
+                                                 const near_query<DIM> &q, Exact &exact,
+                                                 int col, int from, int end, SlotAt slot_at,
+                                                 int &stored, int &next) {
+  int *L = S.slots + col;
+  const int cap = S.cap;
+  int n = 0, total = 0;
+  next = end;
+  auto consider = [&](int s, float d2, int k) {
+    if (d2 > q.bd.hi) return;
+    if (!(d2 < q.bd.lo) && !exact(s)) return;
+    total++;
+    if (n < cap) {
+      L[n * ABL_STEP_BLOCK] = s;
+      n++;
+      if (n == cap) next = k + 1;
+    }
+  };
+  auto dist2 = [&](int s) {
+    float d2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      const float dd = __ldg(&V.posf[DIM * s + d]) - q.pf[d];
+      d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
+    }
+    return d2;
+  };
+  int k = from;
+  for (; k + 4 <= end; k += 4) {
+    int sl[4];
+    float d2[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) sl[u] = slot_at(k + u);
+#pragma unroll
+    for (int u = 0; u < 4; u++) d2[u] = dist2(sl[u]);
+#pragma unroll
+    for (int u = 0; u < 4; u++) consider(sl[u], d2[u], k + u);
+  }
+  for (; k < end; k++) {
+    const int s = slot_at(k);
+    consider(s, dist2(s), k);
+  }
+  stored = n;
+  return total;
+}
+
 // List mode (the grid has per-cell neighbourhood lists in ascending id): from
 // list index `from` on, stores the slots of the first S.cap in-radius
 // neighbours in column `col` and counts all of them.  `next` receives the
@@ -494,31 +562,11 @@ template <int DIM, typename Exact>
 __device__ int gather_list(const presort_shared &S, const abl_near_view &V,
                            const near_query<DIM> &q, Exact &exact, int col, int from,
                            int &stored, int &next) {
-  int *L = S.slots + col;
-  const int cap = S.cap;
   const int cell = (q.c[2] * V.ny + q.c[1]) * V.nx + q.c[0];
   const int end = __ldg(&V.nb_off[cell + 1]);
-  int n = 0, total = 0;
-  next = end;
-  for (int k = from; k < end; k++) {
-    const int s = __ldg(&V.nb_list[k]);
-    float d2 = 0.0f;
-#pragma unroll
-    for (int d = 0; d < DIM; d++) {
-      float dd = __ldg(&V.posf[DIM * s + d]) - q.pf[d];
-      d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
-    }
-    if (d2 > q.bd.hi) continue;
-    if (!(d2 < q.bd.lo) && !exact(s)) continue;
-    total++;
-    if (n < cap) {
-      L[n * ABL_STEP_BLOCK] = s;
-      n++;
-      if (n == cap) next = k + 1;
-    }
-  }
-  stored = n;
-  return total;
+  const int *list = V.nb_list;
+  return filter_candidates(S, V, q, exact, col, from, end,
+                           [list](int k) { return __ldg(&list[k]); }, stored, next);
 }
 
 // Rows mode (2D): the in-radius neighbours with id > lower, taken in
@@ -578,6 +626,180 @@ __device__ int gather_rows(const presort_shared &S, const abl_near_view &V,
   return total;
 }
 
+// Exclusive block-wide scans of two ints (every thread of the block calls
+// it; blockDim.x a multiple of 32).  `scr`: 160 ints of shared memory.
+__device__ inline void block_scan2(int a, int b, int *scr, int &ea, int &eb, int &ta, int &tb) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  int ia = a, ib = b;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int xa = __shfl_up_sync(0xffffffffu, ia, o), xb = __shfl_up_sync(0xffffffffu, ib, o);
+    if (lane >= o) {
+      ia += xa;
+      ib += xb;
+    }
+  }
+  if (lane == 31) {
+    scr[w] = ia;
+    scr[32 + w] = ib;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int va = lane < nw ? scr[lane] : 0, vb = lane < nw ? scr[32 + lane] : 0;
+    int sa = va, sb = vb;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int xa = __shfl_up_sync(0xffffffffu, sa, o), xb = __shfl_up_sync(0xffffffffu, sb, o);
+      if (lane >= o) {
+        sa += xa;
+        sb += xb;
+      }
+    }
+    scr[64 + lane] = sa - va;
+    scr[96 + lane] = sb - vb;
+    if (lane == 31) {
+      scr[128] = sa;
+      scr[129] = sb;
+    }
+  }
+  __syncthreads();
+  ea = ia - a + scr[64 + w];
+  eb = ib - b + scr[96 + w];
+  ta = scr[128];
+  tb = scr[129];
+}
+
+// Number of ids below `id` in the row list entries rows[b .. b+n).
+__device__ __forceinline__ int rows_lower_bound(const int4 *rows, int b, int n, int id) {
+  const int *ids = reinterpret_cast<const int *>(rows);
+  int lo = 0;
+  while (n > 0) {
+    const int half = n >> 1;
+    if (__ldg(&ids[4 * (b + lo + half)]) < id) {
+      lo += half + 1;
+      n -= half + 1;
+    } else {
+      n = half;
+    }
+  }
+  return lo;
+}
+
+// Block lists, filter: the in-radius slots of block list entries
+// bl[from .. end) in order; the first S.cap go to column `col`.  Returns how
+// many there are; `next` receives the entry index after the last stored one.
+template <int DIM, typename Exact>
+__device__ int filter_block_list(const presort_shared &S, const abl_near_view &V,
+                                 const near_query<DIM> &q, Exact &exact, int col, int from,
+                                 int end, int &stored, int &next) {
+  const int *bl = S.bl;
+  return filter_candidates(S, V, q, exact, col, from, end, [bl](int k) { return bl[k]; },
+                           stored, next);
+}
+
+// Block lists (2D row lists; thread t of a block runs the agent in slot
+// blockIdx.x * blockDim.x + t, so the block's agents fill a run of
+// consecutive cells, about blockDim.x / density of them).  Instead of every
+// agent merging the row lists of the rows below, at and above its cell, the
+// block builds each of its cells' merged list once, in shared memory: an
+// entry's place in its cell's list is its index in its own row list plus
+// the number of smaller ids in the other two (binary searches; the three
+// lists hold different agents).  Each thread then filters its cell's list.
+// Returns false, uniformly over the block, when the lists would not fit in
+// S.block_cap entries or the block's agents do not share one grid (an
+// ensemble block spanning two replicas); the caller then gathers per agent.
+template <int DIM, typename Exact>
+__device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bool has,
+                             const near_query<DIM> &q, Exact &exact, int &key) {
+  const int B = ABL_STEP_BLOCK, t = threadIdx.x, nb = blockDim.x;
+  // Scratch in the column area, which the filter below overwrites.
+  int *cellv = S.slots;
+  int *lrow = cellv + B;   // per leader thread: row list begin, 3 rows
+  int *llen = lrow + 3 * B;
+  int *lbase = llen + 3 * B;  // per leader ordinal: first entry of its cell's list
+  int *lthr = lbase + B;      // per leader ordinal: the leader thread
+  int *scr = lthr + B;        // 160 ints for the scans, then flags
+  const int cell = has ? q.c[1] * V.nx + q.c[0] : -1 - t;
+  cellv[t] = cell;
+  if (t == 0) {
+    const unsigned long long vp = (unsigned long long) &V;
+    scr[160] = (int) vp;
+    scr[161] = (int) (vp >> 32);
+    scr[162] = 0;
+  }
+  __syncthreads();
+  {
+    const unsigned long long vp = (unsigned long long) &V;
+    if (has && (scr[160] != (int) vp || scr[161] != (int) (vp >> 32))) scr[162] = 1;
+  }
+  const bool lead = has && (t == 0 || cellv[t - 1] != cell);
+  int len = 0;
+  if (lead) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int y = q.c[1] + k - 1;
+      int b = 0, n = 0;
+      if (y >= 0 && y < V.ny) {
+        const int u = y * V.nx + q.c[0];
+        b = __ldg(&V.row_off[u]);
+        n = __ldg(&V.row_off[u + 1]) - b;
+      }
+      lrow[3 * t + k] = b;
+      llen[3 * t + k] = n;
+      len += n;
+    }
+  }
+  int base, ord, total, nlead;
+  block_scan2(len, lead ? 1 : 0, scr, base, ord, total, nlead);
+  if (total > S.block_cap || scr[162]) {
+    __syncthreads();  // everyone has read the flag before the column is reused
+    return false;
+  }
+  if (lead) {
+    lbase[ord] = base;
+    lthr[ord] = t;
+  }
+  __syncthreads();
+  for (int j = t; j < total; j += nb) {
+    int lo = 0, hi = nlead - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (lbase[mid] <= j) lo = mid;
+      else hi = mid - 1;
+    }
+    const int lt = lthr[lo];
+    int i = j - lbase[lo], l = 0;
+    while (l < 2 && i >= llen[3 * lt + l]) {
+      i -= llen[3 * lt + l];
+      l++;
+    }
+    const int4 e = __ldg(&V.rows[lrow[3 * lt + l] + i]);
+    int p = lbase[lo] + i;
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+      if (m != l) p += rows_lower_bound(V.rows, lrow[3 * lt + m], llen[3 * lt + m], e.x);
+    }
+    S.bl[p] = e.y;
+  }
+  // This thread's cell list: its leader is the last leader at or before it.
+  const int mine = ord + (lead ? 0 : -1);
+  int from = 0, end = 0;
+  if (has) {
+    from = lbase[mine];
+    end = mine + 1 < nlead ? lbase[mine + 1] : total;
+  }
+  __syncthreads();  // lists complete; scratch no longer read
+  if (has) {
+    int stored = 0, next = 0;
+    key = filter_block_list(S, V, q, exact, t, from, end, stored, next);
+    S.total[t] = key;
+    S.resume[t] = next;
+    S.bstart[t] = from;
+    S.bend[t] = end;
+  }
+  return true;
+}
+
 template <int DIM>
 __device__ __forceinline__ int list_begin(const abl_near_view &V, const near_query<DIM> &q) {
   return __ldg(&V.nb_off[(q.c[2] * V.ny + q.c[1]) * V.nx + q.c[0]]);
@@ -594,7 +816,10 @@ __device__ int presort_block(const abl_near_view &V, bool has, const near_query<
   const presort_shared S = presort_smem(V);
   const int t = threadIdx.x;
   int key = 0x7fffffff;
-  if (has) {
+  if (S.block_cap > 0 && gather_block(S, V, has, q, exact, key)) {
+    // gathered from the block lists
+  } else if (has) {
+    if (S.block_cap > 0) S.bstart[t] = -1;
     int stored = 0;
     if (S.mode == kGatherLists) {
       int next = 0;
@@ -651,7 +876,12 @@ struct near_list_cursor {
     } else if (first || more) {
       // A second pass over the neighbours, or the ones past the stored ones.
       int stored = 0, tot = 0;
-      if (S.mode == kGatherLists) {
+      if (S.block_cap > 0 && S.bstart[col] >= 0) {
+        const int from = first ? S.bstart[col] : S.resume[col];
+        int next = 0;
+        tot = filter_block_list(S, V, q, exact, col, from, S.bend[col], stored, next);
+        S.resume[col] = next;
+      } else if (S.mode == kGatherLists) {
         const int from = first ? list_begin(V, q) : S.resume[col];
         int next = 0;
         tot = gather_list(S, V, q, exact, col, from, stored, next);

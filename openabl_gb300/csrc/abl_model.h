@@ -67,6 +67,8 @@ typedef struct {
   long cell_base;           /* cell_of values are cell_base + cell index of this view */
   int balance;              /* presorted mode: hand a block's agents to threads by neighbour count */
   int cap;                  /* presorted mode: neighbours held per agent in shared memory */
+  int block_cap;            /* row lists, agents visited in slot order: entries of the
+                               per-block neighbourhood lists in shared memory (0: off) */
 } abl_near_view;
 
 /* Everything a generated step launcher needs. */

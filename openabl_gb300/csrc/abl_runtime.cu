@@ -545,11 +545,19 @@ int list_depth(const abl_step_desc &sd, const abl_agent_desc &d, int mode) {
   switch (mode) {
     case ABL_NEAR_RUNS: return 0;
     case ABL_NEAR_ROWS: return d.dim == 2 ? 1 : 0;
+    case ABL_NEAR_BLOCK: return d.dim == 2 ? 1 : 0;
     case ABL_NEAR_LISTS: return 2;
     default: break;
   }
   if (sd.agent_type != sd.near_type) return 0;
   return d.dim == 2 ? 1 : 2;
+}
+
+// Block lists (abl_device.cuh, gather_block) serve 2D row-list loops whose
+// agents are the binned ones, unless the mode asks for per-agent rows.
+bool block_lists_wanted(const abl_step_desc &sd, int depth, int mode) {
+  return depth == 1 && sd.agent_type == sd.near_type
+      && (mode == ABL_NEAR_AUTO || mode == ABL_NEAR_BLOCK);
 }
 
 size_t member_bytes(const abl_member_desc &m) {
@@ -614,6 +622,8 @@ struct abl_ctx {
   int list_cap = 32;
   int runs_cap = 40;
   int near_mode = ABL_NEAR_AUTO;
+  // Entries of a thread block's shared-memory neighbourhood lists (ABL_NEAR_BLOCK).
+  int block_cap = 2048;
   std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
   std::vector<double> prof_seconds;
   std::vector<long> prof_launches;
@@ -1216,6 +1226,9 @@ int step_once(abl_ctx *ctx) {
       V.cap = V.ordered ? ctx->list_cap : ctx->runs_cap;
       V.cell_of = sd.agent_type == sd.near_type ? nt.cell_of : nullptr;
       V.cell_base = 0;
+      // Threads visit the binned agents in slot order, so a block's agents
+      // fill consecutive cells: block lists pay off.
+      V.block_cap = block_lists_wanted(sd, depth, ctx->near_mode) ? ctx->block_cap : 0;
       if (sd.presorted) L.smem = abl::presort_bytes(V);
       if (sd.agent_type == sd.near_type) {
         V.amax = nt.amax;
@@ -1721,7 +1734,7 @@ int abl_set_profiling(abl_ctx *ctx, int enable) {
 }
 
 int abl_set_near_mode(abl_ctx *ctx, int mode) {
-  if (!ctx || mode < ABL_NEAR_AUTO || mode > ABL_NEAR_LISTS) return ABL_E_INVALID;
+  if (!ctx || mode < ABL_NEAR_AUTO || mode > ABL_NEAR_BLOCK) return ABL_E_INVALID;
   ctx->near_mode = mode;
   ctx->prepared = false;
   drop_graph(ctx);
@@ -2278,6 +2291,8 @@ int ens_prepare(abl_ensemble *e) {
       V.cap = V.ordered ? ctx->list_cap : ctx->runs_cap;
       V.cell_of = sd.agent_type == sd.near_type ? nt.cell_of : nullptr;
       V.cell_base = g.cell_base;
+      V.block_cap = e->visit_sorted && block_lists_wanted(sd, depth, ctx->near_mode)
+                        ? ctx->block_cap : 0;
     }
     e->smem[k] = sd.presorted ? abl::presort_bytes(views[0]) : 0;
     abl_near_view *dv = nullptr;

@@ -11,6 +11,7 @@ The build compiles the files kept here; it does not need the compiler.
 """
 import json
 import os
+import shutil
 import subprocess
 import sys
 import tempfile
@@ -32,6 +33,8 @@ MODELS = {
     "circle_float": ("circle.abl", {"use_float": "true"}),
     "circle3d_float": ("circle3d.abl", {"use_float": "true"}),
     "predator_prey_float": ("predator_prey.abl", {"use_float": "true"}),
+    "boids3d": ("boids.abl", {}),
+    "sugarscape": ("sugarscape.abl", {}),
 }
 
 # configuration name -> (model, -P params)
@@ -56,6 +59,15 @@ CONFIGS = {
                                            "predator_fraction": "0.1", "num_timesteps": "500"}),
     "predator_prey_small": ("predator_prey", {"num_agents": "20000", "prey_fraction": "0.4",
                                               "predator_fraction": "0.1", "num_timesteps": "50"}),
+    # examples/boids.abl (3D) at its defaults: 5,000 agents, agent_density 1000.
+    "boids3d_5000": ("boids3d", {"num_timesteps": "100"}),
+    # 1,048,576 agents at 16 per unit volume: ~9 agents per interaction cell.
+    "boids3d_1m": ("boids3d", {"num_agents": "1048576", "agent_density": "16",
+                               "interaction_radius": "0.8", "separation_radius": "0.08",
+                               "num_timesteps": "100"}),
+    # examples/sugarscape.abl at its defaults: a 100 x 100 grid.
+    "sugarscape_10000": ("sugarscape", {"num_timesteps": "100"}),
+    "sugarscape_1m": ("sugarscape", {"num_agents": "1048576", "num_timesteps": "100"}),
 }
 
 
@@ -77,14 +89,18 @@ def main():
     subprocess.check_call(["make", "-s", "-C", os.path.join(PKG, "backend"), "-j8", f"REF={REF}"])
     for model, (example, config) in MODELS.items():
         out = run_compiler(model, {})
-        src = open(os.path.join(out, model + ".cu")).read()
+        with open(os.path.join(out, model + ".cu")) as f:
+            src = f.read()
+        shutil.rmtree(out)
         with open(os.path.join(HERE, model + ".cu"), "w") as f:
             f.write(src)
         print("generated", model)
     configs = {}
     for name, (model, params) in CONFIGS.items():
         out = run_compiler(model, params)
-        manifest = json.load(open(os.path.join(out, model + ".globals.json")))
+        with open(os.path.join(out, model + ".globals.json")) as f:
+            manifest = json.load(f)
+        shutil.rmtree(out)
         configs[name] = {"model": model, "params": params, "globals": manifest["globals"]}
     with open(os.path.join(HERE, "configs.json"), "w") as f:
         json.dump(configs, f, indent=1)

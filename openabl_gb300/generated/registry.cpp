@@ -11,6 +11,8 @@ const abl_model_desc *abl_model_desc_predator_prey(void);
 const abl_model_desc *abl_model_desc_circle_float(void);
 const abl_model_desc *abl_model_desc_circle3d_float(void);
 const abl_model_desc *abl_model_desc_predator_prey_float(void);
+const abl_model_desc *abl_model_desc_boids3d(void);
+const abl_model_desc *abl_model_desc_sugarscape(void);
 extern const abl_model_desc *const abl_builtin_models[];
 const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_circle(),
@@ -22,5 +24,7 @@ const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_circle_float(),
     abl_model_desc_circle3d_float(),
     abl_model_desc_predator_prey_float(),
+    abl_model_desc_boids3d(),
+    abl_model_desc_sugarscape(),
     nullptr};
 }

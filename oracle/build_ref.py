@@ -37,6 +37,8 @@ CASES = {
                                          "num_timesteps": "100"}, {}),
     "boids2d_4096_float": ("boids2d", {"num_agents": "4096", "agent_density": "3200.0",
                                        "num_timesteps": "100"}, {"use_float": "true"}),
+    "boids3d_5000": ("boids", {"num_timesteps": "100"}, {}),
+    "sugarscape_10000": ("sugarscape", {"num_timesteps": "100"}, {}),
 }
 
 # model -> (example, -C config): whole reference programs at default parameters
@@ -46,6 +48,7 @@ PROGRAMS = {
     "boids2d": ("boids2d", {}),
     "game_of_life": ("game_of_life", {}),
     "boids2d_float": ("boids2d", {"use_float": "true"}),
+    "boids3d": ("boids", {}),
 }
 
 

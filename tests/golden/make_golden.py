@@ -37,6 +37,10 @@ LAYOUTS = {
     "circle3d": [("pos", "<f8", (3,))],
     "boids2d": [("pos", "<f8", (2,)), ("velocity", "<f8", (2,))],
     "game_of_life": [("pos", "<f8", (2,)), ("alive", "u1", ())],
+    "boids": [("pos", "<f8", (3,)), ("velocity", "<f8", (3,))],
+    "sugarscape": [("pos", "<f8", (2,)), ("target_pos", "<f8", (2,)), ("agent_id", "<i4", ()),
+                   ("state", "<i4", ()), ("sugar_level", "<i4", ()), ("metabolism", "<i4", ()),
+                   ("env_sugar_level", "<i4", ()), ("max_env_sugar_level", "<i4", ())],
 }
 
 

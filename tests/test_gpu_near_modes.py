@@ -20,10 +20,12 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-MODES = [o.Simulation.NEAR_RUNS, o.Simulation.NEAR_ROWS, o.Simulation.NEAR_LISTS]
+MODES = [o.Simulation.NEAR_RUNS, o.Simulation.NEAR_ROWS, o.Simulation.NEAR_LISTS,
+         o.Simulation.NEAR_BLOCK]
 CASES = [("circle_4000", "circle_4000", "Point"), ("circle3d_4000", "circle3d_4000", "Point"),
          ("boids2d_4096", "boids2d_4096", "Boid"),
-         ("boids2d_4096_float", "boids2d_float_4096", "Boid")]
+         ("boids2d_4096_float", "boids2d_float_4096", "Boid"),
+         ("boids3d_5000", "boids3d_5000", "Boid"), ("sugarscape_10000", "sugarscape_10000", "Agent")]
 
 
 @pytest.mark.parametrize("balance", [0, 1])
@@ -55,6 +57,40 @@ def test_clustered_boids_match_oracle(mode):
              "velocity": rng.uniform(-1.0, 1.0, (n, 2))}
     sim = o.Simulation(model, g)
     sim.set_near_mode(mode)
+    sim.upload("Boid", state)
+    c = {k: g.get(k) for k in O.BOIDS2D_KEYS}
+    ref = state
+    for t in range(2):
+        sim.step()
+        ref = O.boids2d_step(ref, c, mode=1)
+        got = sim.download("Boid")
+        for k in ("pos", "velocity"):
+            assert np.array_equal(got[k], ref[k]), (t, k)
+    sim.close()
+
+
+@pytest.mark.parametrize("balance", [0, 1])
+@pytest.mark.parametrize("mode", [o.Simulation.NEAR_AUTO, o.Simulation.NEAR_BLOCK,
+                                  o.Simulation.NEAR_ROWS])
+def test_mixed_density_boids_match_oracle(mode, balance):
+    """Uneven density in one domain: a sparse background (~8 agents per
+    cell), a dense band (~60 per cell: most agents have more neighbours than
+    a thread keeps in shared memory, so the loop refills from the block's
+    lists) and a tight cluster (whose blocks' lists exceed the shared-memory
+    budget and are gathered per agent instead)."""
+    model, g = o.globals_for_config("boids2d_4096")
+    L = g.get("max_pos")
+    rng = np.random.default_rng(5)
+    sparse = rng.random((3000, 2)) * L
+    band = np.column_stack([rng.random(2500) * L, 0.30 + 0.05 * rng.random(2500)])
+    cluster = 0.8 + 0.04 * rng.random((1500, 2))
+    pos = np.concatenate([sparse, band, cluster])
+    perm = rng.permutation(len(pos))        # ids unrelated to position
+    state = {"pos": np.ascontiguousarray(pos[perm]),
+             "velocity": rng.uniform(-1.0, 1.0, (len(pos), 2))}
+    sim = o.Simulation(model, g)
+    sim.set_near_mode(mode)
+    sim.set_balance(balance)
     sim.upload("Boid", state)
     c = {k: g.get(k) for k in O.BOIDS2D_KEYS}
     ref = state

@@ -17,7 +17,7 @@ from openabl_gb300 import workloads
 pytestmark = pytest.mark.gpu
 
 GOLDEN = [("circle_4000", "Point"), ("circle3d_4000", "Point"), ("boids2d_4096", "Boid"),
-          ("game_of_life_64", "Cell")]
+          ("game_of_life_64", "Cell"), ("boids3d_5000", "Boid"), ("sugarscape_10000", "Agent")]
 
 
 def make_sim(config):
