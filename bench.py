@@ -31,6 +31,9 @@ CONFIG = "boids2d_1m"
 METRIC = "agent-steps/s (1M boids2d fp64)"
 BYTES_PER_AGENT_STEP = 80        # SoA pos+vel read + written, binning key/id written + read
 FP64_FLOP_PER_AGENT_STEP = 560   # ~72 candidates x 5 + ~25 in-radius x 8 FP64 ops
+# DRAM bytes of one update_boid launch on this workload (ncu capture, L2 cold
+# as in the timed steps, which flush L2 first).
+UPDATE_BOID_DRAM_BYTES = 237.95e6
 
 
 def parse():
@@ -231,9 +234,10 @@ def measure_serving(args, o, W, np):
 
 def measure_other_workloads(args, o, W, np):
     """The other hot-path configurations: circle 4,000 agents (the reference's
-    CPU-sized case), game_of_life 4096 x 4096 with 50% alive, and
-    predator_prey with 800,000 prey + 200,000 predators (+ 1,000,000 grass)
-    for 500 timesteps in FP64 and FP32."""
+    CPU-sized case), game_of_life 4096 x 4096 with 50% alive, boids (3D) with
+    1,048,576 agents, sugarscape on a 1024 x 1024 grid, and predator_prey
+    with 800,000 prey + 200,000 predators (+ 1,000,000 grass) for 500
+    timesteps in FP64 and FP32."""
     import sys as _sys
     _sys.path.insert(0, os.path.join(REPO, "tests"))
     out = {}
@@ -261,6 +265,24 @@ def measure_other_workloads(args, o, W, np):
     out["game_of_life_4096"] = {"value": n * 100 / sim.last_exec_time(), "unit": "agent-steps/s",
                                 "ms_per_step": sim.last_exec_time() * 10.0}
     sim.close()
+    # boids (3D), 1,048,576 agents (~9 per interaction cell), and sugarscape
+    # on a 1024 x 1024 grid, 100 timesteps each
+    for name, cfg, agent, make in (
+            ("boids3d_1m", "boids3d_1m", "Boid",
+             lambda g: W.boids3d(g.get("num_agents"), g.get("max_pos"), seed=0)),
+            ("sugarscape_1m", "sugarscape_1m", "Agent",
+             lambda g: W.sugarscape(g.get("grid_width"), g.get("occupiedFrac"), seed=0))):
+        model, g = o.globals_for_config(cfg)
+        st = make(g)
+        sim = o.Simulation(model, g)
+        sim.upload(agent, st)
+        sim.run(3)
+        sim.upload(agent, st)
+        sim.run(100)
+        n = len(st["pos"])
+        out[name] = {"value": n * 100 / sim.last_exec_time(), "unit": "agent-steps/s",
+                     "ms_per_step": sim.last_exec_time() * 10.0, "agents": n}
+        sim.close()
     # predator_prey, 500 timesteps, FP64 and FP32
     from pp_setup import case
     cfg, st, consts = case("predator_prey_1m")
@@ -457,7 +479,10 @@ def run_ours(args):
                 "d2h_bytes_per_step": h2d},
         "roofline": {"bound": "hbm", "kernel": "update_boid", "achieved": achieved_gbs,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
-                     "traffic": None, "bytes_per_agent": BYTES_PER_AGENT_STEP,
+                     "traffic": UPDATE_BOID_DRAM_BYTES,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one "
+                                       "launch (profiles/update_boid_boids2d_1m.md)",
+                     "bytes_per_agent": BYTES_PER_AGENT_STEP,
                      "kernel_ms": kernel_s * 1e3, "peak_source": "measured (MEASURED_PEAKS.json)"},
         "fp64": {"achieved_tflops": achieved_fp64, "peak_tflops": fp64_peak_tflops,
                  "frac": achieved_fp64 / fp64_peak_tflops,

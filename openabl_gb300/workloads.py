@@ -163,3 +163,49 @@ def serving_stream(jobs=100, rate=200.0, n_min=1000, n_max=1000000, steps_min=50
         prec = "fp32" if rng.uniform() < 0.5 else "fp64"
         out.append((t, m, n, steps, prec, int(rng.integers(0, 2**31))))
     return out
+
+
+def boids3d(n, max_pos, seed=0, vmax=1.0):
+    """examples/boids.abl in 3D: positions uniform in [0, max_pos)^3;
+    velocity directions uniform on the sphere with speed uniform in
+    [0.5, 1] * vmax."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pos = rng.uniform(0.0, max_pos, size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    vel = d * (rng.uniform(0.5, 1.0, size=n) * vmax)[:, None]
+    return {"pos": np.ascontiguousarray(pos), "velocity": np.ascontiguousarray(vel)}
+
+
+def sugarscape(grid_width, occupied_frac=0.1, seed=0, gmax=50, min_sugar=1, max_sugar=10):
+    """examples/sugarscape.abl: one agent per grid point at (x + 0.5, y + 0.5),
+    ids x-major (main() loops x, then y); occupied with probability
+    occupied_frac (state 1, sugar level uniform in [min_sugar, max_sugar],
+    metabolism 1), else unoccupied (state 0); the cell's capacity is
+    calc_max_env_sugar_level(x, y): two Gaussian hills of height gmax at
+    (0.25, 0.25) and (0.75, 0.75) * grid_width with variance
+    0.025 * grid_width^2, each term added to an int (truncation), distances
+    as libabl's dist (float-rounded square root); the sugar level starts
+    uniform in [0, capacity]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    w = grid_width
+    x, y = np.meshgrid(np.arange(w, dtype=np.float64), np.arange(w, dtype=np.float64),
+                       indexing="ij")
+    x, y = x.ravel(), y.ravel()
+    var = 0.025 * w * w
+    cap = np.zeros(w * w, dtype=np.int64)
+    for c in (0.25 * w, 0.75 * w):
+        d2 = (x - c) * (x - c) + (y - c) * (y - c)
+        d = np.sqrt(d2.astype(np.float32)).astype(np.float64)
+        cap = np.trunc(cap + gmax * np.exp(-d * d / (2 * var))).astype(np.int64)
+    occupied = rng.uniform(size=w * w) < occupied_frac
+    sugar = np.where(occupied, rng.integers(min_sugar, max_sugar + 1, size=w * w), 0)
+    env = rng.integers(0, cap + 1)
+    return {"pos": np.ascontiguousarray(np.stack([x + 0.5, y + 0.5], axis=1)),
+            "target_pos": np.zeros((w * w, 2)),
+            "agent_id": np.arange(w * w, dtype=np.int32),
+            "state": occupied.astype(np.int32),
+            "sugar_level": sugar.astype(np.int32),
+            "metabolism": occupied.astype(np.int32),
+            "env_sugar_level": env.astype(np.int32),
+            "max_env_sugar_level": cap.astype(np.int32)}
