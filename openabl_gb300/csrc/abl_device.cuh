@@ -669,13 +669,12 @@ __device__ inline void block_scan2(int a, int b, int *scr, int &ea, int &eb, int
   tb = scr[129];
 }
 
-// Number of ids below `id` in the row list entries rows[b .. b+n).
-__device__ __forceinline__ int rows_lower_bound(const int4 *rows, int b, int n, int id) {
-  const int *ids = reinterpret_cast<const int *>(rows);
+// Number of ids below `id` in ids[b .. b+n) (shared memory, ascending).
+__device__ __forceinline__ int ids_lower_bound(const int *ids, int b, int n, int id) {
   int lo = 0;
   while (n > 0) {
     const int half = n >> 1;
-    if (__ldg(&ids[4 * (b + lo + half)]) < id) {
+    if (ids[b + lo + half] < id) {
       lo += half + 1;
       n -= half + 1;
     } else {
@@ -699,15 +698,20 @@ __device__ int filter_block_list(const presort_shared &S, const abl_near_view &V
 
 // Block lists (2D row lists; thread t of a block runs the agent in slot
 // blockIdx.x * blockDim.x + t, so the block's agents fill a run of
-// consecutive cells, about blockDim.x / density of them).  Instead of every
-// agent merging the row lists of the rows below, at and above its cell, the
-// block builds each of its cells' merged list once, in shared memory: an
-// entry's place in its cell's list is its index in its own row list plus
-// the number of smaller ids in the other two (binary searches; the three
-// lists hold different agents).  Each thread then filters its cell's list.
-// Returns false, uniformly over the block, when the lists would not fit in
-// S.block_cap entries or the block's agents do not share one grid (an
-// ensemble block spanning two replicas); the caller then gathers per agent.
+// consecutive cells ca..cb, about blockDim.x / density of them).  Instead
+// of every agent merging the row lists of the rows below, at and above its
+// cell, the block builds each of its cells' merged list once, in shared
+// memory: an entry's place in its cell's list is its index in its own row
+// list plus the number of smaller ids in the other two (binary searches; the
+// three lists hold different agents).  The row lists the block reads are
+// those of cells ca-nx..cb-nx, ca..cb and ca+nx..cb+nx: three contiguous
+// ranges of V.rows, whose ids are first copied into shared memory with
+// coalesced loads, so the searches never wait on global memory.  Each thread
+// then filters its cell's list.  Returns false, uniformly over the block,
+// when the lists or the staged ids would not fit, the block's agents do not
+// share one grid (an ensemble block spanning two replicas) or are not in
+// cell order (threads not visiting slots in order); the caller then gathers
+// per agent.
 template <int DIM, typename Exact>
 __device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bool has,
                              const near_query<DIM> &q, Exact &exact, int &key) {
@@ -718,7 +722,9 @@ __device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bo
   int *llen = lrow + 3 * B;
   int *lbase = llen + 3 * B;  // per leader ordinal: first entry of its cell's list
   int *lthr = lbase + B;      // per leader ordinal: the leader thread
-  int *scr = lthr + B;        // 160 ints for the scans, then flags
+  int *scr = lthr + B;        // 0..129 scans, 160..162 view check, 168..177 staging
+  int *sid = scr + 192;       // staged row-list ids, to the end of the column area
+  const int scap = S.cap * B - (9 * B + 192);
   const int cell = has ? q.c[1] * V.nx + q.c[0] : -1 - t;
   cellv[t] = cell;
   if (t == 0) {
@@ -729,8 +735,12 @@ __device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bo
   }
   __syncthreads();
   {
+    // One grid for the whole block, and cells in visiting order (the
+    // staged ranges below hold the lists of cells cellv[0] .. the last one
+    // only if no thread's cell is below its predecessor's).
     const unsigned long long vp = (unsigned long long) &V;
     if (has && (scr[160] != (int) vp || scr[161] != (int) (vp >> 32))) scr[162] = 1;
+    if (has && t > 0 && cellv[t - 1] > cell) scr[162] = 1;
   }
   const bool lead = has && (t == 0 || cellv[t - 1] != cell);
   int len = 0;
@@ -751,13 +761,54 @@ __device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bo
   }
   int base, ord, total, nlead;
   block_scan2(len, lead ? 1 : 0, scr, base, ord, total, nlead);
-  if (total > S.block_cap || scr[162]) {
-    __syncthreads();  // everyone has read the flag before the column is reused
-    return false;
-  }
   if (lead) {
     lbase[ord] = base;
     lthr[ord] = t;
+  }
+  if (lead && ord == nlead - 1) {
+    // The last leader: stage ranges k = rows ca+(k-1)nx .. cb+(k-1)nx.
+    const int ca = cellv[0], cb = cell, ncells = V.nx * V.ny;
+    int staged = 0;
+    for (int k = 0; k < 3; k++) {
+      int lo = ca + (k - 1) * V.nx, hi = cb + (k - 1) * V.nx;
+      lo = lo < 0 ? 0 : lo;
+      hi = hi > ncells - 1 ? ncells - 1 : hi;
+      int e0 = 0, n = 0;
+      if (lo <= hi) {
+        e0 = __ldg(&V.row_off[lo]);
+        n = __ldg(&V.row_off[hi + 1]) - e0;
+      }
+      scr[168 + k] = e0;
+      scr[171 + k] = n;
+      scr[174 + k] = staged;
+      staged += n;
+    }
+    scr[177] = staged;
+  }
+  __syncthreads();
+  if (total > S.block_cap || scr[162] || (nlead > 0 && scr[177] > scap)) {
+    __syncthreads();  // everyone has read the flags before the column is reused
+    return false;
+  }
+  {
+    const int *ids = reinterpret_cast<const int *>(V.rows);
+    constexpr int kBatch = 8;
+    for (int k = 0; k < 3 && nlead > 0; k++) {
+      const int e0 = scr[168 + k], n = scr[171 + k], b = scr[174 + k];
+      for (int i0 = 0; i0 < n; i0 += kBatch * nb) {
+        int v[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; u++) {
+          const int i = i0 + u * nb + t;
+          if (i < n) v[u] = __ldg(&ids[4 * (e0 + i)]);
+        }
+#pragma unroll
+        for (int u = 0; u < kBatch; u++) {
+          const int i = i0 + u * nb + t;
+          if (i < n) sid[b + i] = v[u];
+        }
+      }
+    }
   }
   __syncthreads();
   for (int j = t; j < total; j += nb) {
@@ -773,13 +824,16 @@ __device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bo
       i -= llen[3 * lt + l];
       l++;
     }
-    const int4 e = __ldg(&V.rows[lrow[3 * lt + l] + i]);
+    // Staged position of list m of this leader: its row list lies in range m.
+    auto spos = [&](int m) { return scr[174 + m] + (lrow[3 * lt + m] - scr[168 + m]); };
+    const int id = sid[spos(l) + i];
+    const int slot = __ldg(reinterpret_cast<const int *>(V.rows) + 4 * (lrow[3 * lt + l] + i) + 1);
     int p = lbase[lo] + i;
 #pragma unroll
     for (int m = 0; m < 3; m++) {
-      if (m != l) p += rows_lower_bound(V.rows, lrow[3 * lt + m], llen[3 * lt + m], e.x);
+      if (m != l) p += ids_lower_bound(sid, spos(m), llen[3 * lt + m], id);
     }
-    S.bl[p] = e.y;
+    S.bl[p] = slot;
   }
   // This thread's cell list: its leader is the last leader at or before it.
   const int mine = ord + (lead ? 0 : -1);

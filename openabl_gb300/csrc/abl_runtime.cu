@@ -2608,7 +2608,9 @@ int abl_ensemble_set_tuning(abl_ensemble *e, int block, double cell_factor, int 
   if (!e || block <= 0 || block > ABL_STEP_BLOCK || block % 32 || !(cell_factor >= 1.0))
     return ABL_E_INVALID;
   e->block = block;
-  if (cell_factor != e->cell_factor) e->prepared = false;
+  // The views depend on both (cell sizes; block lists need slot-ordered visits).
+  if (cell_factor != e->cell_factor || (visit_sorted ? 1 : 0) != e->visit_sorted)
+    e->prepared = false;
   e->cell_factor = cell_factor;
   e->visit_sorted = visit_sorted ? 1 : 0;
   ens_drop_graphs(e);
