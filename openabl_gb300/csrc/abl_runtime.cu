@@ -593,11 +593,16 @@ struct abl_ctx {
   // Captured two-timestep graphs, keyed by the buffer parity and binning
   // state they start from (kernel arguments depend on both).
   struct Graph {
-    std::vector<int> key;
+    std::vector<int> key;      // state (parities, dirty flags) and timesteps captured
+    std::vector<int> end_key;  // state after the captured timesteps
+    int steps = 0;
     cudaGraphExec_t exec = nullptr;
     long launches = 0;
   };
   std::vector<Graph> graphs;
+  // An eager timestep has run since the graphs were dropped (allocations and
+  // binnings settled), so timesteps may be captured.
+  bool warm = false;
   bool prepared = false;
   // One uniform grid per (neighbour type, cell size): every near loop bins
   // its neighbour type with cells just wider than its own radius.
@@ -1311,6 +1316,7 @@ int check_error(abl_ctx *ctx) {
 void drop_graph(abl_ctx *ctx) {
   for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.exec);
   ctx->graphs.clear();
+  ctx->warm = false;
 }
 
 std::vector<int> graph_key(const abl_ctx *ctx) {
@@ -1339,24 +1345,45 @@ void collect_profile(abl_ctx *ctx) {
   }
 }
 
-// Captures two timesteps (so that every double buffer returns to the same
-// parity) into a CUDA graph, or returns the one captured from this state.
-int capture_graph(abl_ctx *ctx, abl_ctx::Graph **out) {
-  std::vector<int> key = graph_key(ctx);
-  for (auto &g : ctx->graphs) {
-    if (g.key == key) {
-      *out = &g;
-      return ABL_OK;
-    }
+void apply_key(abl_ctx *ctx, const std::vector<int> &key) {
+  for (size_t k = 0; k < ctx->types.size(); k++) {
+    ctx->types[k].cur = key[2 * k];
+    ctx->types[k].dirty = key[2 * k + 1] != 0;
   }
+  for (size_t q = 0; q < ctx->grids.size(); q++) {
+    ctx->grids[q].dirty = key[2 * ctx->types.size() + q] != 0;
+  }
+}
+
+// Captures `steps` timesteps into a CUDA graph, or returns the one captured
+// from this state.  The graph's buffers are those of the state it starts
+// from; after replaying it the context is in the graph's end state (the same
+// state again for two timesteps, where every double buffer swaps twice).
+abl_ctx::Graph *find_graph(abl_ctx *ctx, int steps) {
+  std::vector<int> key = graph_key(ctx);
+  key.push_back(steps);
+  for (auto &g : ctx->graphs) {
+    if (g.key == key) return &g;
+  }
+  return nullptr;
+}
+
+int capture_graph(abl_ctx *ctx, int steps, abl_ctx::Graph **out) {
+  if ((*out = find_graph(ctx, steps)) != nullptr) return ABL_OK;
+  std::vector<int> key = graph_key(ctx);
+  key.push_back(steps);
   abl_ctx::Graph G;
   G.key = key;
+  G.steps = steps;
   cudaGraph_t g = nullptr;
   long before = ctx->launches;
+  const long timestep = ctx->timestep;
   ABL_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  int r = step_once(ctx);
-  if (r == ABL_OK) r = step_once(ctx);
+  int r = ABL_OK;
+  for (int k = 0; k < steps && r == ABL_OK; k++) r = step_once(ctx);
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  G.end_key = graph_key(ctx);
+  ctx->timestep = timestep;
   if (r != ABL_OK) {
     if (g) cudaGraphDestroy(g);
     return r;
@@ -1368,13 +1395,7 @@ int capture_graph(abl_ctx *ctx, abl_ctx::Graph **out) {
   G.launches = ctx->launches - before;
   ctx->launches = before;
   // Capturing does not run anything: restore the state the graph starts from.
-  for (size_t k = 0; k < ctx->types.size(); k++) {
-    ctx->types[k].cur = key[2 * k];
-    ctx->types[k].dirty = key[2 * k + 1] != 0;
-  }
-  for (size_t q = 0; q < ctx->grids.size(); q++) {
-    ctx->grids[q].dirty = key[2 * ctx->types.size() + q] != 0;
-  }
+  apply_key(ctx, key);
   ctx->graphs.push_back(G);
   *out = &ctx->graphs.back();
   return ABL_OK;
@@ -1556,27 +1577,40 @@ int abl_run(abl_ctx *ctx, int timesteps) {
   long launches0 = ctx->launches;
   ABL_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
   int done = 0;
-  // The first timestep runs eagerly (it also settles which binnings are
-  // current); the rest replays a two-timestep graph.
-  if (timesteps > 0) {
+  const bool graphs = !ctx->profile && graph_capturable(ctx);
+  // After an upload or a change of settings the first timestep runs eagerly
+  // (it settles which binnings are current); then timesteps replay captured
+  // graphs: two at a time, and a one-timestep graph for an odd remainder
+  // (so that abl_step replays too).
+  if (timesteps > 0 && !(graphs && ctx->warm)) {
     ABL_TRY(step_once(ctx));
     done = 1;
+    ctx->warm = true;
   }
-  if (timesteps - done >= 2 && !ctx->profile && graph_capturable(ctx)) {
-    abl_ctx::Graph *G = nullptr;
-    std::vector<int> key = graph_key(ctx);
-    ABL_TRY(capture_graph(ctx, &G));
-    for (; done + 2 <= timesteps; done += 2) {
+  if (graphs) {
+    while (timesteps - done > 0) {
+      const int steps = timesteps - done >= 2 ? 2 : 1;
+      abl_ctx::Graph *G = find_graph(ctx, steps);
+      if (!G) {
+        // A single timestep is not worth a capture inside the timed region;
+        // its graph is captured after it (below).
+        if (steps == 1) break;
+        ABL_TRY(capture_graph(ctx, steps, &G));
+      }
       ABL_CUDA_TRY(cudaGraphLaunch(G->exec, ctx->stream));
       ctx->launches += G->launches;
+      apply_key(ctx, G->end_key);
+      ctx->timestep += steps;
+      done += steps;
     }
-    // Two timesteps swap every buffer an even number of times; the binning
-    // state after them is the one after the captured sequence.
-    (void) key;
   }
   for (; done < timesteps; done++) ABL_TRY(step_once(ctx));
   ABL_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
   int r = check_error(ctx);
+  if (r == ABL_OK && graphs && ctx->warm && !find_graph(ctx, 1)) {
+    abl_ctx::Graph *G = nullptr;
+    r = capture_graph(ctx, 1, &G);
+  }
   collect_profile(ctx);
   float ms = 0.0f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
