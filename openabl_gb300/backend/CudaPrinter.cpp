@@ -771,6 +771,29 @@ void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
   };
   for (auto *a : c.assigns) noteTarget(*a->left);
   for (auto *a : c.assignOps) noteTarget(*a->left);
+  // Members the body may set to anything but the agent's own value: every
+  // write except `out.m = in.m` (same member) counts.
+  VarId inId = param.var->id;
+  auto selfCopy = [&](const AST::AssignStatement &a) {
+    auto *l = dynamic_cast<const AST::MemberAccessExpression *>(&*a.left);
+    auto *r = dynamic_cast<const AST::MemberAccessExpression *>(&*a.right);
+    if (!l || !r || l->member != r->member) return false;
+    auto *lv = dynamic_cast<const AST::VarExpression *>(&*l->expr);
+    auto *rv = dynamic_cast<const AST::VarExpression *>(&*r->expr);
+    return lv && rv && lv->var->id == outId && rv->var->id == inId;
+  };
+  for (auto *a : c.assigns) {
+    const AST::VarExpression *root = targetRoot(*a->left);
+    if (!root || root->var->id != outId || selfCopy(*a)) continue;
+    std::string m = targetMember(*a->left);
+    info.outChanged |= m.empty() ? all : memberBit(m);
+  }
+  for (auto *a : c.assignOps) {
+    const AST::VarExpression *root = targetRoot(*a->left);
+    if (!root || root->var->id != outId) continue;
+    std::string m = targetMember(*a->left);
+    info.outChanged |= m.empty() ? all : memberBit(m);
+  }
   int outUses = 0;
   for (auto *v : c.varExprs) outUses += v->var->id == outId;
   if (c.returns == 0 && outUses == outTargets) {
@@ -1153,7 +1176,8 @@ void CudaPrinter::printDescriptor() {
           << s.nearMembers << "u, " << s.outAlways << "u, abl_launch_" << n << ", "
           << (s.usesRemove ? 1 : 0) << ", " << s.addType << ", " << (copyOut() ? 1 : 0) << ", "
           << (s.addType < 0 && !s.usesRemove ? "abl_launch_ens_" + n : std::string("nullptr"))
-          << ", " << (s.usesRng ? 1 : 0) << ", " << (s.presorted ? 1 : 0) << "},";
+          << ", " << (s.usesRng ? 1 : 0) << ", " << (s.presorted ? 1 : 0) << ", " << s.outChanged
+          << "u},";
   }
   if (steps.empty()) *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0, 0},";
   *this << outdent << nl << "};" << nl;

@@ -75,6 +75,7 @@ private:
     unsigned nearMembers = 0;
     unsigned outMaybe = 0;
     unsigned outAlways = 0;
+    unsigned outChanged = 0;   // members written with anything but `out.m = in.m`
     const AST::ForStatement *nearLoop = nullptr;
     bool usesRemove = false;
     int addType = -1;

@@ -133,6 +133,8 @@ typedef struct {
   abl_ens_launch_fn launch_ens; /* ensemble variant (NULL: not supported) */
   int uses_rng;                 /* the body draws random numbers */
   int presorted;                /* ordered near loop served from per-block sorted lists */
+  uint32_t out_changed;         /* bitmask of members the body may set to anything but the
+                                   agent's own `in` value (`out.m = in.m` does not count) */
 } abl_step_desc;
 
 /* Host function run after every timestep: the `sequential step`. */

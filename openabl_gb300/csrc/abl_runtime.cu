@@ -127,6 +127,25 @@ struct ScanPlan {
 
 // ------------------------------------------------------------ binning
 
+// Folds m (this thread's largest |coordinate|) into *amax: a block-wide
+// maximum first, then one atomic per block, skipped when it cannot raise the
+// current value.  A per-warp atomic on the one address serialised up to
+// 500 K atomics per binning of 16M agents at the L2.
+__device__ __forceinline__ void fold_amax(float m, float *amax) {
+  __shared__ float warp_max[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) warp_max[w] = m;
+  __syncthreads();
+  if (w == 0) {
+    m = lane < nw ? warp_max[lane] : 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && m > 0.0f && m > __ldcg(amax)) abl::atomic_max_nonneg(amax, m);
+  }
+}
+
 template <typename Real, int DIM>
 __global__ void k_bin_assign(const Real *pos, long n, int nx, int ny, int nz, double lo0,
                              double lo1, double lo2, double inv_cell, int *cell_of,
@@ -150,9 +169,7 @@ __global__ void k_bin_assign(const Real *pos, long n, int nx, int ny, int nz, do
     cell_of[i] = cell;
     local_rank[i] = atomicAdd(&cell_count[cell], 1);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0 && m > 0.0f) abl::atomic_max_nonneg(amax, m);
+  fold_amax(m, amax);
 }
 
 __global__ void k_bin_scatter(long n, const int *cell_of, const int *local_rank,
@@ -195,9 +212,7 @@ __global__ void k_amax(const Real *pos, long n, float *amax, int *error) {
     }
     if (!finite) atomicExch(error, ABL_E_NONFINITE);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0 && m > 0.0f) abl::atomic_max_nonneg(amax, m);
+  fold_amax(m, amax);
 }
 
 __global__ void k_max2(const float *a, const float *b, float *out) {
@@ -272,8 +287,10 @@ __global__ void k_gather(long n, const int *order, const Real *pos, float *posf,
   long s = (long) blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   long i = order[s];
+  if (posf) {
 #pragma unroll
-  for (int d = 0; d < DIM; d++) posf[DIM * s + d] = (float) pos[DIM * i + d];
+    for (int d = 0; d < DIM; d++) posf[DIM * s + d] = (float) pos[DIM * i + d];
+  }
   for (int k = 0; k < g.nmem; k++) {
     int b = g.bytes[k];
     if ((b & 7) == 0) {
@@ -515,6 +532,9 @@ struct TypeState {
   bool ordered = false;     // whole neighbourhood lists (list depth 2)
   bool rows = false;        // row lists (list depth 1)
   bool dirty = true;
+  // Only gathered non-position members changed (positions of this type are
+  // never written): the binning stands, the slot-ordered copies are stale.
+  bool regather = false;
   int R = 1;
   int nx = 1, ny = 1, nz = 1;
   long ncells = 1;
@@ -1086,6 +1106,34 @@ void build_lists(abl_ctx *ctx, const G &geo, int dim, int levels, int Rmax, long
   }
 }
 
+// Slot-ordered copies of the gathered members (and, with_pos, the float
+// positions); without with_pos the position member itself is skipped too.
+template <typename Real>
+void launch_gather(abl_ctx *ctx, TypeState &t, int dim, bool with_pos) {
+  cudaStream_t s = ctx->stream;
+  const int B = 256;
+  long nb = blocks_for(t.n, B);
+  const Real *pos = (const Real *) t.cols[t.cur][t.d->position_member];
+  GatherArgs g;
+  std::memset(&g, 0, sizeof g);
+  for (int k = 0; k < t.d->num_members; k++) {
+    if (!(t.gather_mask & (1u << k))) continue;
+    if (!with_pos && k == t.d->position_member) continue;
+    g.src[g.nmem] = t.cols[t.cur][k];
+    g.dst[g.nmem] = t.gcols[k];
+    g.bytes[g.nmem] = (int) member_bytes(t.d->members[k]);
+    g.nmem++;
+  }
+  if (!with_pos && g.nmem == 0) return;
+  float *posf = with_pos ? t.posf : nullptr;
+  if (dim == 2) {
+    k_gather<Real, 2><<<nb, B, 0, s>>>(t.n, t.order, pos, posf, g);
+  } else {
+    k_gather<Real, 3><<<nb, B, 0, s>>>(t.n, t.order, pos, posf, g);
+  }
+  ctx->launches++;
+}
+
 template <typename Real>
 void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
   cudaStream_t s = ctx->stream;
@@ -1109,21 +1157,7 @@ void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
   ctx->launches++;
   k_cell_sort<<<blocks_for(t.ncells, B), B, 0, s>>>(t.ncells, t.cell_start, t.order);
   ctx->launches++;
-  GatherArgs g;
-  std::memset(&g, 0, sizeof g);
-  for (int k = 0; k < t.d->num_members; k++) {
-    if (!(t.gather_mask & (1u << k))) continue;
-    g.src[g.nmem] = t.cols[t.cur][k];
-    g.dst[g.nmem] = t.gcols[k];
-    g.bytes[g.nmem] = (int) member_bytes(t.d->members[k]);
-    g.nmem++;
-  }
-  if (dim == 2) {
-    k_gather<Real, 2><<<nb, B, 0, s>>>(t.n, t.order, pos, t.posf, g);
-  } else {
-    k_gather<Real, 3><<<nb, B, 0, s>>>(t.n, t.order, pos, t.posf, g);
-  }
-  ctx->launches++;
+  launch_gather<Real>(ctx, t, dim, true);
   if (t.ordered || t.rows) {
     GridGeom geo{t.nx, t.ny, t.nz, t.R};
     build_lists(ctx, geo, dim, t.ordered ? dim : 1, t.R, t.ncells, t.cell_start, t.order,
@@ -1138,9 +1172,11 @@ void bin_type(abl_ctx *ctx, TypeState &t) {
     launch_bin<float>(ctx, t, t.d->dim);
   }
   t.dirty = false;
+  t.regather = false;
 }
 
-// Bins the current population of a grid's agent type.
+// Brings a grid up to date with its agent type: a full binning, or only the
+// slot-ordered copies of the gathered members when positions did not change.
 void bin_grid(abl_ctx *ctx, int gi) {
   TypeState &g = ctx->grids[gi];
   const TypeState &t = ctx->types[ctx->grid_type[gi]];
@@ -1148,7 +1184,13 @@ void bin_grid(abl_ctx *ctx, int gi) {
     for (int k = 0; k < ABL_MAX_MEMBERS; k++) g.cols[b][k] = t.cols[b][k];
   g.cur = t.cur;
   g.n = t.n;
-  bin_type(ctx, g);
+  if (g.dirty) {
+    bin_type(ctx, g);
+  } else if (g.regather) {
+    if (pos_is_double(g)) launch_gather<double>(ctx, g, g.d->dim, false);
+    else launch_gather<float>(ctx, g, g.d->dim, false);
+    g.regather = false;
+  }
 }
 
 // The population of type ti changed: every grid of it must be rebuilt.
@@ -1156,6 +1198,40 @@ void mark_dirty(abl_ctx *ctx, int ti) {
   ctx->types[ti].dirty = true;
   for (size_t gi = 0; gi < ctx->grids.size(); gi++) {
     if (ctx->grid_type[gi] == ti) ctx->grids[gi].dirty = true;
+  }
+}
+
+// Whether no step function ever moves agents of type ti: none may set its
+// position member to anything but the agent's own position (`out.pos =
+// in.pos` is allowed) and none removes or adds agents of it.  Both buffers
+// then hold the uploaded positions for good (CPrinter.cpp:210-213 copies the
+// double buffer once; members a step does not write keep their values).
+bool positions_static(const abl_model_desc *m, int ti) {
+  const abl_agent_desc &a = m->agents[ti];
+  if (a.position_member < 0) return false;
+  for (int k = 0; k < m->num_steps; k++) {
+    const abl_step_desc &sd = m->steps[k];
+    if (sd.add_type == ti) return false;
+    if (sd.agent_type != ti) continue;
+    if (sd.uses_remove || sd.add_type >= 0) return false;
+    if (sd.out_changed & (1u << a.position_member)) return false;
+  }
+  return true;
+}
+
+// A step function (without population changes) changed members `written`
+// of type ti.  Grids of a type whose positions never change keep their
+// binning and only re-gather (if they copy a changed member); every other
+// grid is rebuilt.
+void mark_written(abl_ctx *ctx, int ti, uint32_t written) {
+  if (!positions_static(ctx->model, ti)) {
+    mark_dirty(ctx, ti);
+    return;
+  }
+  ctx->types[ti].dirty = true;
+  for (size_t gi = 0; gi < ctx->grids.size(); gi++) {
+    TypeState &g = ctx->grids[gi];
+    if (ctx->grid_type[gi] == ti && (g.gather_mask & written)) g.regather = true;
   }
 }
 
@@ -1205,7 +1281,7 @@ int step_once(abl_ctx *ctx) {
     }
     if (sd.near_type >= 0) {
       int gi = ctx->step_grid[k];
-      if (ctx->grids[gi].dirty) bin_grid(ctx, gi);
+      if (ctx->grids[gi].dirty || ctx->grids[gi].regather) bin_grid(ctx, gi);
       TypeState &nt = ctx->grids[gi];
       abl_near_view &V = L.near;
       const int depth = list_depth(sd, *nt.d, ctx->near_mode);
@@ -1272,7 +1348,7 @@ int step_once(abl_ctx *ctx) {
       if (regrow) ABL_TRY(prepare(ctx));
     } else {
       t.cur = 1 - t.cur;  // swap agents_X and agents_X_dbuf
-      mark_dirty(ctx, sd.agent_type);
+      mark_written(ctx, sd.agent_type, sd.out_changed);
     }
   }
   ctx->timestep++;
@@ -1325,7 +1401,7 @@ std::vector<int> graph_key(const abl_ctx *ctx) {
     key.push_back(t.cur);
     key.push_back(t.dirty ? 1 : 0);
   }
-  for (const TypeState &g : ctx->grids) key.push_back(g.dirty ? 1 : 0);
+  for (const TypeState &g : ctx->grids) key.push_back((g.dirty ? 1 : 0) | (g.regather ? 2 : 0));
   return key;
 }
 
@@ -1351,7 +1427,8 @@ void apply_key(abl_ctx *ctx, const std::vector<int> &key) {
     ctx->types[k].dirty = key[2 * k + 1] != 0;
   }
   for (size_t q = 0; q < ctx->grids.size(); q++) {
-    ctx->grids[q].dirty = key[2 * ctx->types.size() + q] != 0;
+    ctx->grids[q].dirty = (key[2 * ctx->types.size() + q] & 1) != 0;
+    ctx->grids[q].regather = (key[2 * ctx->types.size() + q] & 2) != 0;
   }
 }
 
@@ -2092,9 +2169,7 @@ __global__ void k_ens_bin_assign(const Real *pos, long n, const int *replica_of,
     cell_of[i] = cell;
     local_rank[i] = atomicAdd(&cell_count[cell], 1);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0 && m > 0.0f) abl::atomic_max_nonneg(amax, m);
+  fold_amax(m, amax);
 }
 
 // Cell geometry of a segmented grid: each replica's cells in its own block.
