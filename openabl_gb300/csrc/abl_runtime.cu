@@ -102,6 +102,50 @@ __global__ void k_scan_blocks(const int *in, int *out, long m, int *block_sums) 
   if (t == blockDim.x - 1) block_sums[blockIdx.x] = warp_tot[blockDim.x / 32 - 1];
 }
 
+// Exclusive scan with total of at most kScanBlock ints in one block: out[0]
+// = 0, out[i + 1] = in[0] + ... + in[i].  Replaces the block pass, the
+// memset and the finishing pass of a one-block scan level.
+__global__ void k_scan_single(const int *in, int *out, long m) {
+  __shared__ int warp_tot[kScanBlock / 4 / 32];
+  int t = threadIdx.x;
+  int v[4];
+  int run = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    long i = 4 * t + k;
+    v[k] = i < m ? in[i] : 0;
+    run += v[k];
+  }
+  int lane = t & 31, w = t >> 5;
+  int incl = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int nw = blockDim.x / 32;
+    int x = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane < nw) warp_tot[lane] = x;
+  }
+  __syncthreads();
+  int prefix = (w > 0 ? warp_tot[w - 1] : 0) + incl - run;
+  if (t == 0) out[0] = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    long i = 4 * t + k;
+    prefix += v[k];
+    if (i < m) out[i + 1] = prefix;
+  }
+}
+
 // Turns per-block inclusive scans into a global exclusive scan with total.
 __global__ void k_scan_finish(const int *incl, int *out_excl, long m, const int *block_offsets) {
   long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -713,13 +757,14 @@ int scan_plan(abl_ctx *ctx, ScanPlan &p, long m, std::vector<void *> *owner) {
 void scan_level(abl_ctx *ctx, const ScanPlan &p, size_t l, const int *in, int *out) {
   const ScanLevel &L = p.levels[l];
   cudaStream_t s = ctx->stream;
+  if (L.nb == 1) {
+    k_scan_single<<<1, kScanBlock / 4, 0, s>>>(in, out, L.m);
+    ctx->launches++;
+    return;
+  }
   k_scan_blocks<<<L.nb, kScanBlock / 4, 0, s>>>(in, L.incl, L.m, L.sums);
   ctx->launches++;
-  if (L.nb == 1) {
-    cudaMemsetAsync(L.offs, 0, sizeof(int), s);
-  } else {
-    scan_level(ctx, p, l + 1, L.sums, L.offs);
-  }
+  scan_level(ctx, p, l + 1, L.sums, L.offs);
   k_scan_finish<<<(L.m + 1 + 255) / 256, 256, 0, s>>>(L.incl, out, L.m, L.offs);
   ctx->launches++;
 }
