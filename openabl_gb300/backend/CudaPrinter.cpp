@@ -153,11 +153,19 @@ struct ComparisonCollector : public AST::Visitor {
   }
 };
 
+// A conditional block of a near body run in a second pass over each chunk,
+// with the body's declarations it reads, recomputed there.
+struct DeferredIf {
+  const AST::IfStatement *ifs = nullptr;
+  std::vector<const AST::VarDeclarationStatement *> recompute;
+};
+
 // Declarations `float d = dist(q.pos, nx.pos)` (or length(q.pos - nx.pos),
 // either order) inside a near body whose every use is a comparison with a
 // loop-invariant value.
 std::set<const AST::VarDeclarationStatement *> findLazyDistances(
-    const AST::Script &script, const AST::ForStatement &loop) {
+    const AST::Script &script, const AST::ForStatement &loop,
+    const std::vector<const AST::Statement *> &excluded) {
   std::set<const AST::VarDeclarationStatement *> out;
   auto *q = dynamic_cast<const AST::VarExpression *>(&loop.getNearAgent());
   if (!q) return out;
@@ -189,12 +197,22 @@ std::set<const AST::VarDeclarationStatement *> findLazyDistances(
     if (!pair) continue;
     VarId id = d->var->id;
     int uses = 0, cmpUses = 0;
-    for (auto *v : c.varExprs) uses += v->var->id == id;
-    for (auto *cmp : cc.cmps) {
-      auto *l = dynamic_cast<const AST::VarExpression *>(&*cmp->left);
-      auto *r = dynamic_cast<const AST::VarExpression *>(&*cmp->right);
-      if (l && l->var->id == id && isLoopInvariant(script, *cmp->right)) cmpUses++;
-      else if (r && r->var->id == id && isLoopInvariant(script, *cmp->left)) cmpUses++;
+    auto count = [&](const Collector &cl, const ComparisonCollector &cmpc, int sign) {
+      for (auto *v : cl.varExprs) uses += sign * (v->var->id == id);
+      for (auto *cmp : cmpc.cmps) {
+        auto *l = dynamic_cast<const AST::VarExpression *>(&*cmp->left);
+        auto *r = dynamic_cast<const AST::VarExpression *>(&*cmp->right);
+        if (l && l->var->id == id && isLoopInvariant(script, *cmp->right)) cmpUses += sign;
+        else if (r && r->var->id == id && isLoopInvariant(script, *cmp->left)) cmpUses += sign;
+      }
+    };
+    count(c, cc, 1);
+    // Blocks run in the second pass recompute the value exactly; their uses
+    // do not count here.
+    for (const AST::Statement *e : excluded) {
+      ComparisonCollector ec;
+      const_cast<AST::Statement &>(*e).accept(ec);
+      count(collect(*const_cast<AST::Statement *>(e)), ec, -1);
     }
     if (uses > 0 && uses == cmpUses) out.insert(d);
   }
@@ -216,10 +234,10 @@ std::set<const AST::VarDeclarationStatement *> findLazyDistances(
 // instead of once per neighbour where C held in any lane of the warp (e.g.
 // boids2d's collision sum, which every lane hits at its own agent).  Only
 // blocks that update floating-point accumulators are moved.
-std::vector<const AST::IfStatement *> findDeferredIfs(const AST::Script &script,
-                                                      const AST::FunctionDeclaration *step,
-                                                      const AST::ForStatement &loop) {
-  std::vector<const AST::IfStatement *> out;
+std::vector<DeferredIf> findDeferredIfs(const AST::Script &script,
+                                        const AST::FunctionDeclaration *step,
+                                        const AST::ForStatement &loop) {
+  std::vector<DeferredIf> out;
   auto *block = dynamic_cast<const AST::BlockStatement *>(&*loop.stmt);
   if (!block || !step) return out;
   Collector body = collect(*loop.stmt);
@@ -242,6 +260,37 @@ std::vector<const AST::IfStatement *> findDeferredIfs(const AST::Script &script,
   }
   for (auto *a : body.assignOps) {
     if (auto *r = targetRoot(*a->left)) bodyWritten.insert(r->var->id);
+  }
+  // Top-level declarations of the body whose value the second pass can
+  // recompute: never assigned, initialised from the neighbour, globals,
+  // variables the body never writes and earlier such declarations only,
+  // through pure builtins.
+  std::map<VarId, const AST::VarDeclarationStatement *> recomputable;
+  std::map<VarId, std::set<VarId>> recomputeDeps;
+  for (const AST::StatementPtr &st : *block->stmts) {
+    auto *d = dynamic_cast<const AST::VarDeclarationStatement *>(&*st);
+    if (!d || !d->initializer || bodyWritten.count(d->var->id)) continue;
+    Collector ic = collect(*d->initializer);
+    bool pure = true;
+    std::set<VarId> deps;
+    for (auto *call : ic.calls) {
+      if (call->kind == AST::CallExpression::Kind::USER) pure = false;
+      if (call->isBuiltin() && isHostOnlyBuiltin(call->name)) pure = false;
+    }
+    for (auto *v : ic.varExprs) {
+      VarId id = v->var->id;
+      if (id == loop.var->id || isGlobalVar(id)) continue;
+      if (recomputable.count(id)) {
+        deps.insert(id);
+        deps.insert(recomputeDeps[id].begin(), recomputeDeps[id].end());
+        continue;
+      }
+      if (inner.count(id) || bodyWritten.count(id) || id == step->stepParam().outVar->id)
+        pure = false;
+    }
+    if (!pure) continue;
+    recomputable[d->var->id] = d;
+    recomputeDeps[d->var->id] = deps;
   }
   for (const AST::StatementPtr &st : *block->stmts) {
     auto *ifs = dynamic_cast<const AST::IfStatement *>(&*st);
@@ -275,17 +324,33 @@ std::vector<const AST::IfStatement *> findDeferredIfs(const AST::Script &script,
     if (!ok || targets.empty() || !floatTarget) continue;
     std::map<VarId, int> refs;
     for (auto *v : b.varExprs) refs[v->var->id]++;
+    std::set<VarId> need;
     for (auto &kv : refs) {
       VarId id = kv.first;
       if (targets.count(id)) {
         if (bodyRefs[id] != kv.second) ok = false;  // mentioned elsewhere in the body
       } else if (id == loop.var->id || local.count(id) || isGlobalVar(id)) {
         // the neighbour, B's own locals, globals
+      } else if (recomputable.count(id)) {
+        need.insert(id);  // a per-iteration value the second pass recomputes
+        need.insert(recomputeDeps[id].begin(), recomputeDeps[id].end());
       } else if (inner.count(id) || bodyWritten.count(id)) {
         ok = false;  // a per-iteration value of the rest of the body
       }
     }
-    if (ok) out.push_back(ifs);
+    if (!ok) continue;
+    DeferredIf di;
+    di.ifs = ifs;
+    // Recomputed declarations in body order; each must precede the if.
+    for (const AST::StatementPtr &st2 : *block->stmts) {
+      if (&*st2 == ifs) break;
+      auto *d = dynamic_cast<const AST::VarDeclarationStatement *>(&*st2);
+      if (d && need.count(d->var->id)) {
+        di.recompute.push_back(d);
+        need.erase(d->var->id);
+      }
+    }
+    if (need.empty()) out.push_back(di);
   }
   return out;
 }
@@ -293,7 +358,7 @@ std::vector<const AST::IfStatement *> findDeferredIfs(const AST::Script &script,
 }  // namespace
 
 void CudaPrinter::print(const AST::VarDeclarationStatement &stmt) {
-  if (lazyDecls.count(&stmt)) {
+  if (lazyDecls.count(&stmt) && !deferredPass) {
     *this << "const auto " << *stmt.var << " = abl::make_lazy_dist(" << nearQuery
           << ", abl_NB, " << nearSlot << ", [&]() -> abl_float { return " << *stmt.initializer
           << "; });";
@@ -584,13 +649,13 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   *this << nl << "int " << pslot << " = " << c << ".slot(0);" << nl << agentDecl->name << " "
         << pnx << ";";
   loadMembers(pnx, pslot);
-  std::vector<const AST::IfStatement *> deferred;
+  std::vector<DeferredIf> deferred;
   if (fnKind == FnKind::STEP) deferred = findDeferredIfs(script, stepDecl, stmt);
   std::map<const AST::IfStatement *, std::string> savedMasks = deferredMasks;
   deferredMasks.clear();
   for (size_t j = 0; j < deferred.size(); j++) {
     std::string mask = "abl_dm" + sid + "_" + std::to_string(j);
-    deferredMasks[deferred[j]] = mask;
+    deferredMasks[deferred[j].ifs] = mask;
     *this << nl << "unsigned long long " << mask << " = 0ull;";
   }
   *this << nl << "for (int abl_k = 0; abl_k < " << c << ".cnt; ++abl_k) {" << indent << nl
@@ -604,7 +669,9 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
 
   std::string savedLabel = nearEndLabel;
   bool savedNeeds = nearNeedsEnd;
-  lazyDecls = findLazyDistances(script, stmt);
+  std::vector<const AST::Statement *> deferredBodies;
+  for (const DeferredIf &d : deferred) deferredBodies.push_back(&*d.ifs->ifStmt);
+  lazyDecls = findLazyDistances(script, stmt, deferredBodies);
   nearQuery = q;
   nearSlot = slot;
   nearEndLabel = "abl_near_end" + sid;
@@ -615,15 +682,18 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   *this << outdent << nl << "}";
   // Second pass over the chunk: the deferred conditional blocks, each over
   // the neighbours where its condition held, in ascending order.
+  deferredPass = true;
   for (size_t j = 0; j < deferred.size(); j++) {
-    const std::string &mask = deferredMasks[deferred[j]];
+    const std::string &mask = deferredMasks[deferred[j].ifs];
     *this << nl << "for (unsigned long long abl_m = " << mask << "; abl_m; abl_m &= abl_m - 1ull) {"
           << indent << nl << "const int " << slot << " = " << c
           << ".slot(__ffsll((long long) abl_m) - 1);" << nl << agentDecl->name << " " << nxs << ";";
     loadMembers(nxs, slot);
-    *this << nl << agentDecl->name << "* " << *stmt.var << " = &" << nxs << ";" << nl
-          << *deferred[j]->ifStmt << outdent << nl << "}";
+    *this << nl << agentDecl->name << "* " << *stmt.var << " = &" << nxs << ";";
+    for (const AST::VarDeclarationStatement *d : deferred[j].recompute) *this << nl << *d;
+    *this << nl << *deferred[j].ifs->ifStmt << outdent << nl << "}";
   }
+  deferredPass = false;
   deferredMasks = savedMasks;
   nearLoopDepth = -1;
   *this << outdent << nl << "}" << outdent << nl << "}";

@@ -60,6 +60,8 @@ private:
   // Conditional blocks of the current near body run in a second pass over
   // each chunk, and the per-chunk mask that records where their condition held.
   std::map<const AST::IfStatement *, std::string> deferredMasks;
+  // Printing the second pass: declarations are printed with their exact value.
+  bool deferredPass = false;
 
   // Kind of function being printed (decides how builtins are lowered).
   enum class FnKind { HOST, STEP, USER, SEQ } fnKind = FnKind::HOST;

@@ -216,6 +216,7 @@ __device__ static void prey_avoid_pred(const abl_globals &abl_G, const abl_near_
             int abl_pslot1 = abl_c1.slot(0);
             Predator abl_pnx1;
             abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
+            unsigned long long abl_dm1_0 = 0ull;
             for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
                 const int abl_slot1 = abl_pslot1;
                 Predator abl_nx1 = abl_pnx1;
@@ -225,11 +226,19 @@ __device__ static void prey_avoid_pred(const abl_globals &abl_G, const abl_near_
                 }
                 Predator* pred = &abl_nx1;
                 {
-                    double separation = length_float2(float2_sub(in->pos, pred->pos));
-                    if ((separation < abl_G.PRED_PREY_INTERACTION_RADIUS)) {
-                        if ((separation > 0.0)) {
-                            avoid_velocity = float2_add(avoid_velocity, float2_mul_scalar(float2_sub(in->pos, pred->pos), (abl_G.PRED_PREY_INTERACTION_RADIUS / separation)));
-                        }
+                    const auto separation = abl::make_lazy_dist(abl_q1, abl_NB, abl_slot1, [&]() -> abl_float { return length_float2(float2_sub(in->pos, pred->pos)); });
+                    if ((separation < abl_G.PRED_PREY_INTERACTION_RADIUS)) abl_dm1_0 |= 1ull << abl_k;
+                }
+            }
+            for (unsigned long long abl_m = abl_dm1_0; abl_m; abl_m &= abl_m - 1ull) {
+                const int abl_slot1 = abl_c1.slot(__ffsll((long long) abl_m) - 1);
+                Predator abl_nx1;
+                abl_nx1.pos = ((const float2 *) abl_NB.cols[0])[abl_slot1];
+                Predator* pred = &abl_nx1;
+                double separation = length_float2(float2_sub(in->pos, pred->pos));
+                {
+                    if ((separation > 0.0)) {
+                        avoid_velocity = float2_add(avoid_velocity, float2_mul_scalar(float2_sub(in->pos, pred->pos), (abl_G.PRED_PREY_INTERACTION_RADIUS / separation)));
                     }
                 }
             }
@@ -388,6 +397,7 @@ __device__ static void prey_flock(const abl_globals &abl_G, const abl_near_view 
             int abl_pslot2 = abl_c2.slot(0);
             Prey abl_pnx2;
             abl_pnx2.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot2];
+            unsigned long long abl_dm2_0 = 0ull;
             for (int abl_k = 0; abl_k < abl_c2.cnt; ++abl_k) {
                 const int abl_slot2 = abl_pslot2;
                 Prey abl_nx2 = abl_pnx2;
@@ -397,13 +407,21 @@ __device__ static void prey_flock(const abl_globals &abl_G, const abl_near_view 
                 }
                 Prey* prey = &abl_nx2;
                 {
-                    double separation = length_float2(float2_sub(in->pos, prey->pos));
+                    const auto separation = abl::make_lazy_dist(abl_q2, abl_NB, abl_slot2, [&]() -> abl_float { return length_float2(float2_sub(in->pos, prey->pos)); });
                     group_center = float2_add(group_center, prey->pos);
                     group_centre_count += 1;
-                    if (((separation < abl_G.SAME_SPECIES_AVOIDANCE_RADIUS) && float2_not_equals(prey->pos, in->pos))) {
-                        if ((separation > 0.0)) {
-                            avoid_velocity = float2_add(avoid_velocity, float2_mul_scalar(float2_sub(in->pos, prey->pos), (abl_G.SAME_SPECIES_AVOIDANCE_RADIUS / separation)));
-                        }
+                    if (((separation < abl_G.SAME_SPECIES_AVOIDANCE_RADIUS) && float2_not_equals(prey->pos, in->pos))) abl_dm2_0 |= 1ull << abl_k;
+                }
+            }
+            for (unsigned long long abl_m = abl_dm2_0; abl_m; abl_m &= abl_m - 1ull) {
+                const int abl_slot2 = abl_c2.slot(__ffsll((long long) abl_m) - 1);
+                Prey abl_nx2;
+                abl_nx2.pos = ((const float2 *) abl_NB.cols[0])[abl_slot2];
+                Prey* prey = &abl_nx2;
+                double separation = length_float2(float2_sub(in->pos, prey->pos));
+                {
+                    if ((separation > 0.0)) {
+                        avoid_velocity = float2_add(avoid_velocity, float2_mul_scalar(float2_sub(in->pos, prey->pos), (abl_G.SAME_SPECIES_AVOIDANCE_RADIUS / separation)));
                     }
                 }
             }
@@ -1145,6 +1163,7 @@ __device__ static void pred_avoid(const abl_globals &abl_G, const abl_near_view 
             int abl_pslot6 = abl_c6.slot(0);
             Predator abl_pnx6;
             abl_pnx6.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot6];
+            unsigned long long abl_dm6_0 = 0ull;
             for (int abl_k = 0; abl_k < abl_c6.cnt; ++abl_k) {
                 const int abl_slot6 = abl_pslot6;
                 Predator abl_nx6 = abl_pnx6;
@@ -1154,10 +1173,18 @@ __device__ static void pred_avoid(const abl_globals &abl_G, const abl_near_view 
                 }
                 Predator* pred = &abl_nx6;
                 {
-                    double separation = length_float2(float2_sub(in->pos, pred->pos));
-                    if (((separation < abl_G.SAME_SPECIES_AVOIDANCE_RADIUS) && float2_not_equals(pred->pos, in->pos))) {
-                        if ((separation > 0.0)) avoid_velocity = float2_add(avoid_velocity, float2_mul_scalar(float2_sub(in->pos, pred->pos), (abl_G.SAME_SPECIES_AVOIDANCE_RADIUS / separation)));
-                    }
+                    const auto separation = abl::make_lazy_dist(abl_q6, abl_NB, abl_slot6, [&]() -> abl_float { return length_float2(float2_sub(in->pos, pred->pos)); });
+                    if (((separation < abl_G.SAME_SPECIES_AVOIDANCE_RADIUS) && float2_not_equals(pred->pos, in->pos))) abl_dm6_0 |= 1ull << abl_k;
+                }
+            }
+            for (unsigned long long abl_m = abl_dm6_0; abl_m; abl_m &= abl_m - 1ull) {
+                const int abl_slot6 = abl_c6.slot(__ffsll((long long) abl_m) - 1);
+                Predator abl_nx6;
+                abl_nx6.pos = ((const float2 *) abl_NB.cols[0])[abl_slot6];
+                Predator* pred = &abl_nx6;
+                double separation = length_float2(float2_sub(in->pos, pred->pos));
+                {
+                    if ((separation > 0.0)) avoid_velocity = float2_add(avoid_velocity, float2_mul_scalar(float2_sub(in->pos, pred->pos), (abl_G.SAME_SPECIES_AVOIDANCE_RADIUS / separation)));
                 }
             }
         }
