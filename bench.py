@@ -59,6 +59,24 @@ def dist_env():
     return world, rank, local
 
 
+def slowest_rank_seconds(total, world, device="cuda"):
+    """Time of the whole job: every rank times the same K timesteps of its
+    own replica; the job takes as long as its slowest rank."""
+    if world <= 1:
+        return total
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([total], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, agents, steps, seconds):
+    """Agent-steps per second of the whole job: each of `world` ranks
+    advances its own replica of `agents` agents by `steps` timesteps."""
+    return world * agents * steps / seconds
+
+
 def cpu_reference_sample(state, consts, target_seconds, n_total):
     """Brute-force reference step (every agent scans all agents) on a bounded
     sample of agents, all host threads.  Returns (agent-steps/s, sample, cores)."""
@@ -399,12 +417,8 @@ def run_ours(args):
         launches += sim.last_launch_count()
     barrier()
     clock_info = clocks.stop()
-    total = sum(times)
-    if world > 1:
-        t = torch.tensor([total], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total = float(t.item())
-    value = world * n * args.steps / total
+    total = slowest_rank_seconds(sum(times), world)
+    value = job_rate(world, n, args.steps, total)
 
     # graph replay of the same timesteps, back to back (no flush)
     sim.upload("Boid", state)
