@@ -89,6 +89,16 @@ int abl_create(const abl_model_desc *model, size_t hbm_budget, abl_ctx **out);
 int abl_set_globals(abl_ctx *ctx, const void *globals, size_t size);
 /* Uploads `n` agents of `type_id` from host SoA columns (see above). */
 int abl_upload(abl_ctx *ctx, int type_id, const void *const *cols, size_t n);
+/* Initialisation on the device instead of an upload (main()'s `add` loops
+ * run as kernels; the reference builds the population on the host,
+ * CPrinter.cpp:278-293, and has no counterpart).  abl_reserve sizes the
+ * type's buffers for `n` agents and stores the device address of each
+ * member's column in dev_cols[member]; the caller fills them (and
+ * synchronises its work with the device) before abl_commit, which makes the
+ * double buffer a copy, as abl_upload does, and marks the type's binning
+ * stale. */
+int abl_reserve(abl_ctx *ctx, int type_id, size_t n, void **dev_cols);
+int abl_commit(abl_ctx *ctx, int type_id);
 /* Runs one / `timesteps` iterations of the simulate loop. */
 int abl_step(abl_ctx *ctx);
 int abl_run(abl_ctx *ctx, int timesteps);

@@ -3,8 +3,9 @@
 // the same layout the `c` backend produces (src/backend/CBackend.cpp:29-45).
 //
 // Configuration (-C name=value):
-//   use_float=true   abl_float is float (as LIBABL_USE_FLOAT for `c`)
-//   cuda.model=NAME  identifier of the model inside the runtime (default "model")
+//   use_float=true         abl_float is float (as LIBABL_USE_FLOAT for `c`)
+//   cuda.model=NAME        identifier of the model inside the runtime (default "model")
+//   cuda.device_init=true  main()'s add() loops run as kernels (CudaPrinter::findDeviceInit)
 #include "CudaBackend.hpp"
 
 #include <cctype>
@@ -82,7 +83,7 @@ void CudaBackend::generate(AST::Script &script, const BackendContext &ctx) {
     }
   }
 
-  CudaPrinter printer(script, useFloat, model);
+  CudaPrinter printer(script, useFloat, model, ctx.config.getBool("cuda.device_init", false));
   printer.print(script);
   writeToFile(ctx.outputDir + "/" + model + ".cu", printer.extractStr());
   writeToFile(ctx.outputDir + "/" + model + ".globals.json", globalsManifest(script, model));

@@ -580,6 +580,14 @@ void CudaPrinter::print(const AST::BreakStatement &stmt) {
 // runtime's grid; the reference's own radius test decides the rare
 // candidates that the float prefilter cannot.
 void CudaPrinter::print(const AST::ForStatement &stmt) {
+  for (size_t k = 0; k < devInit.size(); k++) {
+    if (devInit[k].loop == &stmt && fnKind == FnKind::HOST) {
+      auto range = stmt.getRange();
+      *this << "abl_devinit_record(" << (int) k << ", " << range.first << ", " << range.second
+            << ");";
+      return;
+    }
+  }
   if (!stmt.isNear()) {
     if (nearLoopDepth >= 0) nearLoopDepth++;
     CPrinter::print(stmt);
@@ -742,30 +750,29 @@ void CudaPrinter::printSeqStep(const AST::FunctionDeclaration &decl) {
         << nl << "}";
 }
 
+// Functions that reach a host-only builtin (the sequential RNG of
+// asset/c/libabl.c:8-39, add, save) run on the host only.
+bool CudaPrinter::hostOnlyFunction(const AST::FunctionDeclaration *f, int depth) {
+  auto it = hostOnlyMemo.find(f);
+  if (it != hostOnlyMemo.end()) return it->second;
+  if (depth > 64) return true;
+  hostOnlyMemo[f] = false;
+  Collector c = collect(*const_cast<AST::FunctionDeclaration *>(f));
+  bool h = false;
+  for (auto *call : c.calls) {
+    // random()/randomInt() run on both sides (abl_random); the rest of the
+    // simulation builtins exist on the host only.
+    if (call->isBuiltin() && isHostOnlyBuiltin(call->name) && call->name != "random"
+        && call->name != "randomInt") h = true;
+    if (call->kind == AST::CallExpression::Kind::USER && call->calledFunc
+        && hostOnlyFunction(call->calledFunc, depth + 1)) h = true;
+  }
+  hostOnlyMemo[f] = h;
+  return h;
+}
+
 void CudaPrinter::printUserFunction(const AST::FunctionDeclaration &decl) {
-  // Functions that reach a host-only builtin (the sequential RNG of
-  // asset/c/libabl.c:8-39, add, save) run on the host only.
-  std::map<const AST::FunctionDeclaration *, bool> hostOnly;
-  std::function<bool(const AST::FunctionDeclaration *, int)> isHost =
-      [&](const AST::FunctionDeclaration *f, int depth) -> bool {
-    auto it = hostOnly.find(f);
-    if (it != hostOnly.end()) return it->second;
-    if (depth > 64) return true;
-    hostOnly[f] = false;
-    Collector c = collect(*const_cast<AST::FunctionDeclaration *>(f));
-    bool h = false;
-    for (auto *call : c.calls) {
-      // random()/randomInt() run on both sides (abl_random); the rest of the
-      // simulation builtins exist on the host only.
-      if (call->isBuiltin() && isHostOnlyBuiltin(call->name) && call->name != "random"
-          && call->name != "randomInt") h = true;
-      if (call->kind == AST::CallExpression::Kind::USER && call->calledFunc
-          && isHost(call->calledFunc, depth + 1)) h = true;
-    }
-    hostOnly[f] = h;
-    return h;
-  };
-  bool host = isHost(&decl, 0);
+  bool host = hostOnlyFunction(&decl, 0);
   *this << (host ? "static inline " : "__host__ __device__ static inline ")
         << *decl.returnType << " " << decl.sig.name << "(const abl_globals &abl_G, abl::rng &abl_R";
   if (!decl.params->empty()) *this << ", ";
@@ -1101,6 +1108,90 @@ void CudaPrinter::printGlobals() {
         << "static abl_globals abl_G = abl_globals_default;" << nl;
 }
 
+// -C cuda.device_init=true: main()'s loops `for (int i : a..b) add(T{...})`
+// run as kernels, one thread per iteration, instead of building the
+// population on the host.  Every add() of main() must be such a loop's only
+// statement, with member initialisers that read the loop variable and
+// globals and call builtins or device-capable user functions; random() draws
+// from the counter-based stream keyed by the iteration's index and the
+// loop's number (not the reference's sequential xorshift stream: host
+// initialisation stays the way to reproduce reference results).
+void CudaPrinter::findDeviceInit(const AST::FunctionDeclaration &mainDecl) {
+  int adds = 0;
+  Collector all = collect(*const_cast<AST::FunctionDeclaration *>(&mainDecl));
+  for (auto *call : all.calls) adds += call->isBuiltin() && call->name == "add";
+  for (const AST::StatementPtr &st : *mainDecl.stmts) {
+    auto *loop = dynamic_cast<const AST::ForStatement *>(&*st);
+    if (!loop || !loop->isRange()) continue;
+    const AST::Statement *body = &*loop->stmt;
+    if (auto *b = dynamic_cast<const AST::BlockStatement *>(body)) {
+      if (b->stmts->size() != 1) continue;
+      body = &*(*b->stmts)[0];
+    }
+    auto *es = dynamic_cast<const AST::ExpressionStatement *>(body);
+    if (!es) continue;
+    auto *call = dynamic_cast<const AST::CallExpression *>(&*es->expr);
+    if (!call || !call->isBuiltin() || call->name != "add") continue;
+    auto *create = dynamic_cast<const AST::AgentCreationExpression *>(&call->getArg(0));
+    if (!create) continue;
+    Collector c = collect(*const_cast<AST::AgentCreationExpression *>(create));
+    bool ok = true;
+    for (auto *v : c.varExprs) {
+      const VarId id = v->var->id;
+      const bool global = script.scope.has(id) && script.scope.get(id).isGlobal;
+      if (!global && id != loop->var->id) ok = false;
+    }
+    for (auto *cl : c.calls) {
+      if (cl->isBuiltin() && isHostOnlyBuiltin(cl->name) && cl->name != "random"
+          && cl->name != "randomInt") ok = false;
+      if (cl->kind == AST::CallExpression::Kind::USER
+          && (!cl->calledFunc || hostOnlyFunction(cl->calledFunc, 0))) ok = false;
+    }
+    if (!ok) continue;
+    DevInit d;
+    d.loop = loop;
+    d.create = create;
+    d.agentType = agentIndex(call->calledSig.paramTypes[0].getAgentDecl());
+    devInit.push_back(d);
+  }
+  if ((int) devInit.size() != adds) {
+    devInit.clear();
+    throw BackendError("cuda.device_init: every add() of main() must be the only statement of "
+                       "a `for (int i : a..b)` loop whose agent reads only the loop variable "
+                       "and globals");
+  }
+}
+
+void CudaPrinter::printDeviceInit() {
+  if (devInit.empty()) return;
+  *this << "// Device initialisation (-C cuda.device_init=true): main()'s add() loops." << nl
+        << "static const uint64_t abl_init_seed = 0x5eedull;" << nl
+        << "static long abl_dev_first[" << (int) devInit.size() << "], abl_dev_count["
+        << (int) devInit.size() << "];" << nl
+        << "static void abl_devinit_record(int k, long first, long last) {" << indent << nl
+        << "abl_dev_first[k] = first;" << nl << "abl_dev_count[k] = last > first ? last - first : 0;"
+        << outdent << nl << "}" << nl;
+  FnKind saved = fnKind;
+  fnKind = FnKind::USER;
+  for (size_t k = 0; k < devInit.size(); k++) {
+    const DevInit &d = devInit[k];
+    const AST::AgentDeclaration &a = *script.agents[d.agentType];
+    *this << "__global__ void abl_init_" << (int) k << "(const abl_globals abl_G, long abl_first, "
+          << "long abl_count, long abl_base, abl_cols_" << a.name << " abl_c) {" << indent << nl
+          << "const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl
+          << "if (abl_t >= abl_count) return;" << nl
+          << "const int " << *d.loop->var << " = (int) (abl_first + abl_t);" << nl
+          << "abl::rng abl_R;" << nl
+          << "abl_R.init(abl_init_seed, (uint32_t) abl_t, 0xffffff00u + " << (int) k << "u, 0);"
+          << nl << "const " << a.name << " abl_v = " << *d.create << ";";
+    for (const AST::AgentMemberPtr &m : *a.members) {
+      *this << nl << "abl_c." << m->name << "[abl_base + abl_t] = abl_v." << m->name << ";";
+    }
+    *this << outdent << nl << "}" << nl;
+  }
+  fnKind = saved;
+}
+
 void CudaPrinter::printHostSimulate() {
   // Hands the host-built population to the device runtime for the simulate
   // loop and reads it back for the statements after it.
@@ -1112,7 +1203,36 @@ void CudaPrinter::printHostSimulate() {
         << "abl_ctx *ctx = nullptr;" << nl
         << "abl_check(abl_create(&abl_desc, 0, &ctx), \"abl_create\");" << nl
         << "abl_check(abl_set_globals(ctx, &abl_G, sizeof abl_G), \"abl_set_globals\");";
-  for (size_t ti = 0; ti < script.agents.size(); ti++) {
+  for (size_t ti = 0; ti < script.agents.size() && !devInit.empty(); ti++) {
+    const AST::AgentDeclaration &a = *script.agents[ti];
+    const std::string &T = a.name;
+    *this << nl << "{" << indent << nl << "long n = 0;";
+    for (size_t k = 0; k < devInit.size(); k++) {
+      if (devInit[k].agentType == (int) ti) *this << nl << "n += abl_dev_count[" << (int) k << "];";
+    }
+    *this << nl << "void *cols[" << (int) a.members->size() << "];" << nl
+          << "abl_check(abl_reserve(ctx, " << (int) ti << ", (size_t) n, cols), \"abl_reserve\");"
+          << nl << "abl_cols_" << T << " c;";
+    for (size_t k = 0; k < a.members->size(); k++) {
+      const AST::AgentMember &m = *(*a.members)[k];
+      *this << nl << "c." << m.name << " = (" << cType(m.type->resolved) << " *) cols[" << (int) k
+            << "];";
+    }
+    *this << nl << "long base = 0;";
+    for (size_t k = 0; k < devInit.size(); k++) {
+      if (devInit[k].agentType != (int) ti) continue;
+      std::string K = std::to_string(k);
+      *this << nl << "if (abl_dev_count[" << K << "] > 0) {" << indent << nl << "abl_init_" << K
+            << "<<<(abl_dev_count[" << K << "] + 255) / 256, 256>>>(abl_G, abl_dev_first[" << K
+            << "], abl_dev_count[" << K << "], base, c);" << nl << "base += abl_dev_count[" << K
+            << "];" << outdent << nl << "}";
+    }
+    *this << nl << "abl_check(cudaDeviceSynchronize() == cudaSuccess ? ABL_OK : ABL_E_CUDA, "
+          << "\"device initialisation\");" << nl
+          << "abl_check(abl_commit(ctx, " << (int) ti << "), \"abl_commit\");" << outdent << nl
+          << "}";
+  }
+  for (size_t ti = 0; ti < script.agents.size() && devInit.empty(); ti++) {
     const AST::AgentDeclaration &a = *script.agents[ti];
     const std::string &T = a.name;
     *this << nl << "{" << indent << nl
@@ -1327,6 +1447,8 @@ void CudaPrinter::print(const AST::Script &) {
     *this << *decl << nl;
   }
   *this << nl;
+  if (deviceInit && mainDecl) findDeviceInit(*mainDecl);
+  printDeviceInit();
   printDescriptor();
   if (mainDecl) {
     printHostSimulate();

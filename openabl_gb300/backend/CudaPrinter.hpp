@@ -28,8 +28,10 @@ namespace OpenABL {
 struct CudaPrinter : public CPrinter {
   using CPrinter::print;
 
-  CudaPrinter(AST::Script &script, bool useFloat, const std::string &modelName)
-    : CPrinter(script, useFloat), script(script), useFloat(useFloat), modelName(modelName) {}
+  CudaPrinter(AST::Script &script, bool useFloat, const std::string &modelName,
+              bool deviceInit = false)
+    : CPrinter(script, useFloat), script(script), useFloat(useFloat), modelName(modelName),
+      deviceInit(deviceInit) {}
 
   void print(const AST::VarExpression &) override;
   void print(const AST::CallExpression &) override;
@@ -47,6 +49,19 @@ private:
   AST::Script &script;
   bool useFloat;
   std::string modelName;
+  bool deviceInit;
+
+  // Device initialisation: main()'s add() loops run as kernels.
+  struct DevInit {
+    const AST::ForStatement *loop = nullptr;
+    const AST::AgentCreationExpression *create = nullptr;
+    int agentType = -1;
+  };
+  std::vector<DevInit> devInit;
+  void findDeviceInit(const AST::FunctionDeclaration &mainDecl);
+  void printDeviceInit();
+  std::map<const AST::FunctionDeclaration *, bool> hostOnlyMemo;
+  bool hostOnlyFunction(const AST::FunctionDeclaration *f, int depth);
 
   // Near-loop printing state.
   int nearCounter = 0;

@@ -567,6 +567,7 @@ struct TypeState {
   long cap = 0;            // agents the column buffers can hold
   bool dynamic = false;    // some step function removes or adds agents of this type
   bool uploaded = false;
+  bool reserved_resize = false;  // abl_reserve resized the buffers; abl_commit re-prepares
   void *cols[2][ABL_MAX_MEMBERS] = {};
   int cur = 0;
   float *amax = nullptr;  // this type's largest |coordinate| (device)
@@ -1634,16 +1635,12 @@ int abl_set_globals(abl_ctx *ctx, const void *globals, size_t size) {
   return ABL_OK;
 }
 
-int abl_upload(abl_ctx *ctx, int type_id, const void *const *cols, size_t n) {
-  if (!ctx || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
-  if (n > (size_t) INT32_MAX) return ABL_E_UNSUPPORTED;
-  TypeState &t = ctx->types[type_id];
-  if (n > 0 && !cols) return ABL_E_INVALID;
-  // (Re)allocate both buffers when the count changes (types whose population
-  // changes at run time keep spare capacity and reallocate only to grow).
+// Sizes both buffers of a type for n agents (types whose population changes
+// at run time keep spare capacity and reallocate only to grow).
+static int size_type(abl_ctx *ctx, TypeState &t, size_t n, bool &resized) {
   long want_cap = t.dynamic ? std::max<long>(2 * (long) n, 1024) : (long) n;
-  bool resized_alloc = !t.uploaded || (t.dynamic ? (long) n > t.cap : (long) n != t.n);
-  if (resized_alloc) {
+  resized = !t.uploaded || (t.dynamic ? (long) n > t.cap : (long) n != t.n);
+  if (resized) {
     for (int b = 0; b < 2; b++) {
       for (int k = 0; k < t.d->num_members; k++) {
         if (t.cols[b][k]) dev_free(ctx, t.cols[b][k]);
@@ -1654,15 +1651,18 @@ int abl_upload(abl_ctx *ctx, int type_id, const void *const *cols, size_t n) {
     }
     t.cap = want_cap;
   }
-  bool resized = resized_alloc;
   t.n = (long) n;
   t.cur = 0;
+  return ABL_OK;
+}
+
+// The state in buffer 0 is the population: the double buffer starts as a
+// copy (CPrinter.cpp:210-213), every binning of the type is stale.
+static int finish_upload(abl_ctx *ctx, int type_id, bool resized) {
+  TypeState &t = ctx->types[type_id];
   for (int k = 0; k < t.d->num_members; k++) {
-    size_t bytes = member_bytes(t.d->members[k]) * n;
+    size_t bytes = member_bytes(t.d->members[k]) * (size_t) t.n;
     if (bytes == 0) continue;
-    if (!cols[k]) return ABL_E_INVALID;
-    ABL_CUDA_TRY(cudaMemcpyAsync(t.cols[0][k], cols[k], bytes, cudaMemcpyHostToDevice, ctx->stream));
-    // The double buffer starts as a copy (CPrinter.cpp:210-213).
     ABL_CUDA_TRY(cudaMemcpyAsync(t.cols[1][k], t.cols[0][k], bytes, cudaMemcpyDeviceToDevice,
                                  ctx->stream));
   }
@@ -1673,6 +1673,47 @@ int abl_upload(abl_ctx *ctx, int type_id, const void *const *cols, size_t n) {
     drop_graph(ctx);
   }
   return ABL_OK;
+}
+
+int abl_upload(abl_ctx *ctx, int type_id, const void *const *cols, size_t n) {
+  if (!ctx || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
+  if (n > (size_t) INT32_MAX) return ABL_E_UNSUPPORTED;
+  TypeState &t = ctx->types[type_id];
+  if (n > 0 && !cols) return ABL_E_INVALID;
+  if (n > 0) {
+    for (int k = 0; k < t.d->num_members; k++)
+      if (member_bytes(t.d->members[k]) > 0 && !cols[k]) return ABL_E_INVALID;
+  }
+  bool resized = false;
+  ABL_TRY(size_type(ctx, t, n, resized));
+  for (int k = 0; k < t.d->num_members; k++) {
+    size_t bytes = member_bytes(t.d->members[k]) * n;
+    if (bytes == 0) continue;
+    ABL_CUDA_TRY(cudaMemcpyAsync(t.cols[0][k], cols[k], bytes, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  return finish_upload(ctx, type_id, resized);
+}
+
+int abl_reserve(abl_ctx *ctx, int type_id, size_t n, void **dev_cols) {
+  if (!ctx || !dev_cols || type_id < 0 || type_id >= (int) ctx->types.size())
+    return ABL_E_INVALID;
+  if (n > (size_t) INT32_MAX) return ABL_E_UNSUPPORTED;
+  TypeState &t = ctx->types[type_id];
+  bool resized = false;
+  ABL_TRY(size_type(ctx, t, n, resized));
+  t.reserved_resize = t.reserved_resize || resized;
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // buffers free for the caller's writes
+  for (int k = 0; k < t.d->num_members; k++) dev_cols[k] = t.cols[0][k];
+  return ABL_OK;
+}
+
+int abl_commit(abl_ctx *ctx, int type_id) {
+  if (!ctx || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
+  TypeState &t = ctx->types[type_id];
+  if (t.n > 0 && !t.cols[0][0] && t.d->num_members > 0) return ABL_E_INVALID;
+  const bool resized = t.reserved_resize || !t.uploaded;
+  t.reserved_resize = false;
+  return finish_upload(ctx, type_id, resized);
 }
 
 static int ensure_ready(abl_ctx *ctx) {

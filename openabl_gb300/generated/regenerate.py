@@ -35,6 +35,8 @@ MODELS = {
     "predator_prey_float": ("predator_prey.abl", {"use_float": "true"}),
     "boids3d": ("boids.abl", {}),
     "sugarscape": ("sugarscape.abl", {}),
+    # main()'s add() loop as a kernel (-C cuda.device_init=true)
+    "boids2d_devinit": ("boids2d.abl", {"cuda.device_init": "true"}),
 }
 
 # configuration name -> (model, -P params)

@@ -13,6 +13,7 @@ const abl_model_desc *abl_model_desc_circle3d_float(void);
 const abl_model_desc *abl_model_desc_predator_prey_float(void);
 const abl_model_desc *abl_model_desc_boids3d(void);
 const abl_model_desc *abl_model_desc_sugarscape(void);
+const abl_model_desc *abl_model_desc_boids2d_devinit(void);
 extern const abl_model_desc *const abl_builtin_models[];
 const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_circle(),
@@ -26,5 +27,6 @@ const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_predator_prey_float(),
     abl_model_desc_boids3d(),
     abl_model_desc_sugarscape(),
+    abl_model_desc_boids2d_devinit(),
     nullptr};
 }

@@ -86,6 +86,22 @@ def test_unsupported_feature_exits_with_backend_error(compiler, tmp_path):
     assert r.returncode == 2
 
 
+@pytest.mark.parametrize("example,accepted", [("boids2d", True), ("predator_prey", True),
+                                              ("game_of_life", False), ("sugarscape", False)])
+def test_device_init_takes_independent_add_loops_only(compiler, example, accepted, tmp_path):
+    """-C cuda.device_init=true turns main()'s `for (int i : a..b) add(T{...})`
+    loops into kernels; a main() that builds agents any other way (nested
+    loops, a running counter) is refused with the plugin's exit code 2."""
+    r = subprocess.run([compiler, "-A", os.path.join(REF, "asset"), "-i",
+                        os.path.join(REF, "examples", example + ".abl"), "-o", str(tmp_path),
+                        "-b", "cuda", "-C", f"cuda.model={example}", "-C", "cuda.device_init=true"],
+                       capture_output=True, text=True)
+    assert r.returncode == (0 if accepted else 2), r.stdout + r.stderr
+    if accepted:
+        src = (tmp_path / (example + ".cu")).read_text()
+        assert "__global__ void abl_init_0(" in src and "abl_reserve(ctx" in src
+
+
 def test_committed_model_sources_are_current(compiler):
     sys.path.insert(0, GEN)
     import regenerate
