@@ -1656,13 +1656,27 @@ static int size_type(abl_ctx *ctx, TypeState &t, size_t n, bool &resized) {
   return ABL_OK;
 }
 
+// Whether the double buffer's copy of member k of type ti can ever be
+// read: not when every step function of the type always writes the member
+// (its `out` column is overwritten before the buffers swap), nor when no
+// step function runs on the type (the buffers never swap).
+static bool dbuf_read(const abl_model_desc *m, int ti, int k) {
+  for (int s = 0; s < m->num_steps; s++) {
+    const abl_step_desc &sd = m->steps[s];
+    if (sd.agent_type != ti) continue;
+    if (!(sd.out_written & (1u << k))) return true;
+  }
+  return false;
+}
+
 // The state in buffer 0 is the population: the double buffer starts as a
-// copy (CPrinter.cpp:210-213), every binning of the type is stale.
+// copy (CPrinter.cpp:210-213) where it can be read, every binning of the
+// type is stale.
 static int finish_upload(abl_ctx *ctx, int type_id, bool resized) {
   TypeState &t = ctx->types[type_id];
   for (int k = 0; k < t.d->num_members; k++) {
     size_t bytes = member_bytes(t.d->members[k]) * (size_t) t.n;
-    if (bytes == 0) continue;
+    if (bytes == 0 || !dbuf_read(ctx->model, type_id, k)) continue;
     ABL_CUDA_TRY(cudaMemcpyAsync(t.cols[1][k], t.cols[0][k], bytes, cudaMemcpyDeviceToDevice,
                                  ctx->stream));
   }
