@@ -160,6 +160,12 @@ int abl_set_balance(abl_ctx *ctx, int enable);
 #define ABL_NEAR_LISTS 3
 #define ABL_NEAR_BLOCK 4
 int abl_set_near_mode(abl_ctx *ctx, int mode);
+/* A near loop around the step's own agent, over a type whose positions no
+ * step function changes (nor adds or removes agents of), keeps each agent's
+ * in-radius neighbour list from one binning to the next: found once after an
+ * upload, read at every timestep (default on).  Results are identical either
+ * way. */
+int abl_set_near_cache(abl_ctx *ctx, int enable);
 int abl_destroy(abl_ctx *ctx);
 const char *abl_strerror(int code);
 

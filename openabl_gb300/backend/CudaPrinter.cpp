@@ -823,8 +823,12 @@ void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
       }
     }
     auto *center = dynamic_cast<const AST::VarExpression *>(&loop->getNearAgent());
-    info.presorted = info.ordered && c.nearLoops.size() == 1 && rc.calls.empty() && center
-                  && center->var->id == decl.stepParam().var->id;
+    const bool selfCentred = center && center->var->id == decl.stepParam().var->id;
+    info.presorted = info.ordered && c.nearLoops.size() == 1 && rc.calls.empty() && selfCentred;
+    // One near loop around the step's own agent, with a radius of plain
+    // arithmetic on globals (evaluated alike on host and device): its
+    // neighbours are a function of the population's positions alone.
+    info.nearCacheable = c.nearLoops.size() == 1 && selfCentred && rc.calls.empty();
   }
   // Members of `out` written by the function: any assignment rooted at
   // out.m may write it; a top-level `out.m = e` always does, provided `out`
@@ -1367,7 +1371,7 @@ void CudaPrinter::printDescriptor() {
           << (s.usesRemove ? 1 : 0) << ", " << s.addType << ", " << (copyOut() ? 1 : 0) << ", "
           << (s.addType < 0 && !s.usesRemove ? "abl_launch_ens_" + n : std::string("nullptr"))
           << ", " << (s.usesRng ? 1 : 0) << ", " << (s.presorted ? 1 : 0) << ", " << s.outChanged
-          << "u},";
+          << "u, " << (s.nearCacheable ? 1 : 0) << "},";
   }
   if (steps.empty()) *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0, 0},";
   *this << outdent << nl << "};" << nl;

@@ -93,6 +93,7 @@ private:
     unsigned outMaybe = 0;
     unsigned outAlways = 0;
     unsigned outChanged = 0;   // members written with anything but `out.m = in.m`
+    bool nearCacheable = false;  // one near loop, centred on the step's own agent
     const AST::ForStatement *nearLoop = nullptr;
     bool usesRemove = false;
     int addType = -1;

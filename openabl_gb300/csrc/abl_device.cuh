@@ -120,6 +120,7 @@ struct near_query {
   float pf[3];
   band bd;
   float amax;
+  long self;  // the querying agent's index in the step's population, or -1
   // Band of the last threshold a lazy distance was compared with.
   mutable long long lazy_bits = 0;
   mutable band lazy_band;
@@ -127,7 +128,8 @@ struct near_query {
 
   // `self`: the querying agent's index when it belongs to the binned
   // population (its cell is then the one binning gave it), else -1.
-  __device__ near_query(const abl_near_view &V, double x, double y, double z, long self = -1) {
+  __device__ near_query(const abl_near_view &V, double x, double y, double z, long self_ = -1)
+      : self(self_) {
     const int dims[3] = {V.nx, V.ny, V.nz};
     const double p[3] = {x, y, z};
     if (self >= 0 && V.cell_of) {
@@ -173,7 +175,13 @@ struct near_cursor {
   __device__ near_cursor(const abl_near_view &v, const near_query<DIM> &q) : V(v), cnt(0) {
     __shared__ int chunk[ABL_NEAR_CHUNK * ABL_STEP_BLOCK];
     buf = chunk + threadIdx.x;
-    if (V.ordered) {
+    if (V.ncache_off && q.self >= 0) {
+      // The agent's neighbour list kept across timesteps.
+      cur = __ldg(&V.ncache_off[q.self]);
+      end = __ldg(&V.ncache_off[q.self + 1]);
+      rz = ry = 0;
+      x0 = x1 = 0;
+    } else if (V.ordered) {
       int cell = (q.c[2] * V.ny + q.c[1]) * V.nx + q.c[0];
       cur = V.nb_off[cell];
       end = V.nb_off[cell + 1];
@@ -213,6 +221,10 @@ struct near_cursor {
   template <typename Exact>
   __device__ bool fill(const near_query<DIM> &q, Exact &&exact) {
     cnt = 0;
+    if (V.ncache_off && q.self >= 0) {
+      while (cur < end && cnt < ABL_NEAR_CHUNK) buf[ABL_STEP_BLOCK * cnt++] = __ldg(&V.ncache_slot[cur++]);
+      return cnt > 0;
+    }
     for (;;) {
       while (cur < end && cnt < ABL_NEAR_CHUNK) {
         int s = V.ordered ? __ldg(&V.nb_list[cur]) : cur;
@@ -410,6 +422,7 @@ struct presort_shared {
 enum { kGatherRuns = 0, kGatherRows = 1, kGatherLists = 2 };
 
 __host__ __device__ inline int gather_mode(const abl_near_view &V) {
+  if (V.ncache_off) return kGatherLists;  // lists kept across timesteps: slots only
   return V.ordered ? kGatherLists : (V.rows && V.dim == 2) ? kGatherRows : kGatherRuns;
 }
 
@@ -870,7 +883,17 @@ __device__ int presort_block(const abl_near_view &V, bool has, const near_query<
   const presort_shared S = presort_smem(V);
   const int t = threadIdx.x;
   int key = 0x7fffffff;
-  if (S.block_cap > 0 && gather_block(S, V, has, q, exact, key)) {
+  if (V.ncache_off) {
+    // The agent's neighbour list kept across timesteps (ascending id).
+    if (has) {
+      const int from = __ldg(&V.ncache_off[q.self]), end = __ldg(&V.ncache_off[q.self + 1]);
+      const int n = end - from < S.cap ? end - from : S.cap;
+      for (int j = 0; j < n; j++) S.slots[j * ABL_STEP_BLOCK + t] = __ldg(&V.ncache_slot[from + j]);
+      key = end - from;
+      S.total[t] = key;
+      S.resume[t] = from + n;
+    }
+  } else if (S.block_cap > 0 && gather_block(S, V, has, q, exact, key)) {
     // gathered from the block lists
   } else if (has) {
     if (S.block_cap > 0) S.bstart[t] = -1;
@@ -930,7 +953,15 @@ struct near_list_cursor {
     } else if (first || more) {
       // A second pass over the neighbours, or the ones past the stored ones.
       int stored = 0, tot = 0;
-      if (S.block_cap > 0 && S.bstart[col] >= 0) {
+      if (V.ncache_off) {
+        const int from = first ? __ldg(&V.ncache_off[q.self]) : S.resume[col];
+        const int end = __ldg(&V.ncache_off[q.self + 1]);
+        const int n = end - from < S.cap ? end - from : S.cap;
+        for (int j = 0; j < n; j++) S.slots[j * ABL_STEP_BLOCK + col] = __ldg(&V.ncache_slot[from + j]);
+        S.resume[col] = from + n;
+        stored = n;
+        tot = end - from;
+      } else if (S.block_cap > 0 && S.bstart[col] >= 0) {
         const int from = first ? S.bstart[col] : S.resume[col];
         int next = 0;
         tot = filter_block_list(S, V, q, exact, col, from, S.bend[col], stored, next);

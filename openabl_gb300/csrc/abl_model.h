@@ -69,6 +69,9 @@ typedef struct {
   int cap;                  /* presorted mode: neighbours held per agent in shared memory */
   int block_cap;            /* row lists, agents visited in slot order: entries of the
                                per-block neighbourhood lists in shared memory (0: off) */
+  const int *ncache_off;    /* neighbour lists kept across timesteps (NULL: none): query
+                               agent i's in-radius slots are ncache_slot[off[i] .. off[i+1]) */
+  const int *ncache_slot;   /* in ascending agent id for ordered loops */
 } abl_near_view;
 
 /* Everything a generated step launcher needs. */
@@ -135,6 +138,7 @@ typedef struct {
   int presorted;                /* ordered near loop served from per-block sorted lists */
   uint32_t out_changed;         /* bitmask of members the body may set to anything but the
                                    agent's own `in` value (`out.m = in.m` does not count) */
+  int near_cacheable;           /* one near loop, centred on the step's own agent */
 } abl_step_desc;
 
 /* Host function run after every timestep: the `sequential step`. */

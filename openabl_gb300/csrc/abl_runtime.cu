@@ -580,6 +580,7 @@ struct TypeState {
   // Only gathered non-position members changed (positions of this type are
   // never written): the binning stands, the slot-ordered copies are stale.
   bool regather = false;
+  long bin_id = 0;           // serial number of the last full binning
   int R = 1;
   int nx = 1, ny = 1, nz = 1;
   long ncells = 1;
@@ -640,6 +641,14 @@ struct StepState {
   int *child = nullptr, *child_pos = nullptr;
   ScanPlan keep_scan, child_scan;
   long parent_cap = 0;
+  // Neighbour lists kept across timesteps (static positions): per agent of
+  // the step's type its in-radius neighbour slots, ascending id for ordered
+  // loops.  Built for binning `nc_bin` of the step's grid (-1: none); nc_off
+  // null with nc_bin set means the lists did not fit for that binning.
+  int *nc_off = nullptr, *nc_slot = nullptr;
+  long nc_bin = -1;
+  double nc_radius = 0.0;
+  std::vector<void *> nc_allocs;
 };
 
 struct abl_ctx {
@@ -694,6 +703,8 @@ struct abl_ctx {
   int near_mode = ABL_NEAR_AUTO;
   // Entries of a thread block's shared-memory neighbourhood lists (ABL_NEAR_BLOCK).
   int block_cap = 2048;
+  bool near_cache = true;
+  long bin_serial = 0;
   std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
   std::vector<double> prof_seconds;
   std::vector<long> prof_launches;
@@ -939,6 +950,8 @@ int prepare(abl_ctx *ctx) {
   // capacity of the step's own type (one flag / one child per agent).
   for (void *p : ctx->step_allocs) dev_free(ctx, p);
   ctx->step_allocs.clear();
+  for (StepState &st : ctx->step_state)
+    for (void *p : st.nc_allocs) dev_free(ctx, p);
   ctx->step_state.assign(m->num_steps, StepState());
   for (int k = 0; k < m->num_steps; k++) {
     const abl_step_desc &sd = m->steps[k];
@@ -1212,6 +1225,7 @@ void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
 }
 
 void bin_type(abl_ctx *ctx, TypeState &t) {
+  t.bin_id = ++ctx->bin_serial;
   if (pos_is_double(t)) {
     launch_bin<double>(ctx, t, t.d->dim);
   } else {
@@ -1298,6 +1312,158 @@ void type_amax(abl_ctx *ctx, TypeState &t) {
   ctx->launches++;
 }
 
+void drop_graph(abl_ctx *ctx);
+
+// ------------------------------------------------- kept neighbour lists
+//
+// When no step function moves agents of a type (and none adds or removes
+// them), the set of agents within a constant radius of each agent is the
+// same at every timestep.  A near loop around the step's own agent then
+// reads its neighbours from a list per agent, found once per binning: the
+// candidates are the (2R+1)^DIM cells around the agent's cell, as for the
+// step kernels' own search, and the test is the reference's own near test.
+
+__device__ __forceinline__ double nc_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float nc_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double nc_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float nc_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float nc_float(double a) { return __double2float_rn(a); }
+__device__ __forceinline__ float nc_float(float a) { return a; }
+
+// Whether agent j is a neighbour of agent i: !(dist(j.pos, i.pos) > radius),
+// dist = sqrtf((float) (vx*vx + vy*vy [+ vz*vz])) in the position's type
+// (asset/c/libabl.h:156-167; the near test of src/backend/CPrinter.cpp:160-170).  The
+// radius is the step's radius expression in that type, widened to double.
+template <typename Real, int DIM>
+__device__ __forceinline__ bool nc_within(const Real *pos, long i, long j, double radius) {
+  Real s = 0;
+#pragma unroll
+  for (int d = 0; d < DIM; d++) {
+    const Real v = pos[DIM * j + d] - pos[DIM * i + d];
+    s = d == 0 ? nc_mul(v, v) : nc_add(s, nc_mul(v, v));
+  }
+  const float f = __fsqrt_rn(nc_float(s));
+  return !((double) f > radius);
+}
+
+// Pass 1 (slots == nullptr): count[i] = agent i's neighbours.  Pass 2: its
+// neighbours' slots from slots[off[i]], in the cells' order; with `sorted`
+// then in ascending agent id (the order the reference visits them in).
+template <typename Real, int DIM>
+__global__ void k_nc_lists(const Real *pos, long n, const int *cell_of, const int *cell_start,
+                           const int *order, int nx, int ny, int nz, int R, double radius,
+                           int *count, const int *off, int *slots, bool sorted) {
+  const long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int l = cell_of[i];
+  const int nxy = nx * ny;
+  const int c2 = l / nxy, c1 = (l - c2 * nxy) / nx, c0 = l - c2 * nxy - c1 * nx;
+  const int z0 = DIM == 3 ? max(c2 - R, 0) : 0, z1 = DIM == 3 ? min(c2 + R, nz - 1) : 0;
+  const int y0 = max(c1 - R, 0), y1 = min(c1 + R, ny - 1);
+  const int x0 = max(c0 - R, 0), x1 = min(c0 + R, nx - 1);
+  int k = 0;
+  int *out = slots ? slots + off[i] : nullptr;
+  for (int z = z0; z <= z1; z++) {
+    for (int y = y0; y <= y1; y++) {
+      const int base = (z * ny + y) * nx;
+      const int e = cell_start[base + x1 + 1];
+      for (int s = cell_start[base + x0]; s < e; s++) {
+        if (!nc_within<Real, DIM>(pos, i, order[s], radius)) continue;
+        if (out) out[k] = s;
+        k++;
+      }
+    }
+  }
+  if (!out) {
+    count[i] = k;
+    return;
+  }
+  if (!sorted) return;
+  for (int a = 1; a < k; a++) {
+    const int v = out[a], key = order[v];
+    int b = a - 1;
+    while (b >= 0 && order[out[b]] > key) {
+      out[b + 1] = out[b];
+      b--;
+    }
+    out[b + 1] = v;
+  }
+}
+
+template <typename Real>
+void launch_nc_lists(abl_ctx *ctx, const TypeState &g, double radius, int *count, const int *off,
+                     int *slots, bool sorted) {
+  const int B = 128;
+  const Real *pos = (const Real *) g.cols[g.cur][g.d->position_member];
+  const long nb = blocks_for(g.n, B);
+  if (g.d->dim == 2) {
+    k_nc_lists<Real, 2><<<nb, B, 0, ctx->stream>>>(pos, g.n, g.cell_of, g.cell_start, g.order,
+                                                   g.nx, g.ny, g.nz, g.R, radius, count, off,
+                                                   slots, sorted);
+  } else {
+    k_nc_lists<Real, 3><<<nb, B, 0, ctx->stream>>>(pos, g.n, g.cell_of, g.cell_start, g.order,
+                                                   g.nx, g.ny, g.nz, g.R, radius, count, off,
+                                                   slots, sorted);
+  }
+  ctx->launches++;
+}
+
+// Whether step k keeps its neighbour lists.
+bool near_cache_wanted(const abl_ctx *ctx, const abl_step_desc &sd) {
+  return ctx->near_cache && sd.near_cacheable && sd.agent_type == sd.near_type
+      && positions_static(ctx->model, sd.agent_type);
+}
+
+// Brings step k's kept lists up to date with grid g (just binned) and
+// returns whether they can be read.  Building needs a host read of the total,
+// so a stream capture only reads lists that are already current.
+int near_cache_ready(abl_ctx *ctx, int k, const TypeState &g, double radius, bool sorted,
+                     bool &ready) {
+  ready = false;
+  StepState &st = ctx->step_state[k];
+  if (st.nc_bin == g.bin_id && st.nc_radius == radius) {
+    ready = st.nc_off != nullptr;
+    return ABL_OK;
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(ctx->stream, &cs);
+  if (cs != cudaStreamCaptureStatusNone) return ABL_OK;
+  // Graphs captured earlier may read the lists about to be replaced.
+  drop_graph(ctx);
+  for (void *p : st.nc_allocs) dev_free(ctx, p);
+  st.nc_allocs.clear();
+  st.nc_off = st.nc_slot = nullptr;
+  st.nc_bin = g.bin_id;
+  st.nc_radius = radius;
+  if (g.n <= 0) return ABL_OK;
+  auto *own = &st.nc_allocs;
+  int *count = nullptr;
+  ScanPlan plan;
+  if (dev_alloc_t(ctx, &count, g.n, own) != ABL_OK || dev_alloc_t(ctx, &st.nc_off, g.n + 1, own) != ABL_OK
+      || scan_plan(ctx, plan, g.n, own) != ABL_OK) {
+    st.nc_off = nullptr;
+    return ABL_OK;  // no room: the step searches the grid
+  }
+  const bool dbl = pos_is_double(g);
+  if (dbl) launch_nc_lists<double>(ctx, g, radius, count, nullptr, nullptr, sorted);
+  else launch_nc_lists<float>(ctx, g, radius, count, nullptr, nullptr, sorted);
+  scan_run(ctx, plan, count, st.nc_off);
+  int total = 0;
+  ABL_CUDA_TRY(cudaMemcpyAsync(&total, st.nc_off + g.n, sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  // Lists far longer than a handful of cells' worth are not worth keeping.
+  if (total < 0 || (long) total > 64 * g.n + 4096
+      || dev_alloc_t(ctx, &st.nc_slot, std::max(total, 1), own) != ABL_OK) {
+    st.nc_off = st.nc_slot = nullptr;
+    return ABL_OK;
+  }
+  if (dbl) launch_nc_lists<double>(ctx, g, radius, nullptr, st.nc_off, st.nc_slot, sorted);
+  else launch_nc_lists<float>(ctx, g, radius, nullptr, st.nc_off, st.nc_slot, sorted);
+  ready = true;
+  return ABL_OK;
+}
+
 // One iteration of the simulate loop (src/backend/CPrinter.cpp:189-233).
 int step_once(abl_ctx *ctx) {
   const abl_model_desc *m = ctx->model;
@@ -1356,10 +1522,19 @@ int step_once(abl_ctx *ctx) {
       // Threads visit the binned agents in slot order, so a block's agents
       // fill consecutive cells: block lists pay off.
       V.block_cap = block_lists_wanted(sd, depth, ctx->near_mode) ? ctx->block_cap : 0;
+      bool cached = false;
+      if (near_cache_wanted(ctx, sd))
+        ABL_TRY(near_cache_ready(ctx, k, nt, V.radius, sd.ordered != 0, cached));
+      if (cached) {
+        // Kept lists: agents in index order, no block lists.
+        V.ncache_off = ctx->step_state[k].nc_off;
+        V.ncache_slot = ctx->step_state[k].nc_slot;
+        V.block_cap = 0;
+      }
       if (sd.presorted) L.smem = abl::presort_bytes(V);
       if (sd.agent_type == sd.near_type) {
         V.amax = nt.amax;
-        L.visit_order = nt.order;
+        L.visit_order = cached ? nullptr : nt.order;
       } else {
         if (t.d->position_member >= 0 && t.n > 0) {
           type_amax(ctx, t);
@@ -1682,6 +1857,12 @@ static int finish_upload(abl_ctx *ctx, int type_id, bool resized) {
   }
   t.uploaded = true;
   mark_dirty(ctx, type_id);
+  // Graphs reading kept neighbour lists of this type would read stale ones.
+  for (int k = 0; k < ctx->model->num_steps && !resized; k++) {
+    if (ctx->model->steps[k].near_type == type_id && k < (int) ctx->step_state.size()
+        && ctx->step_state[k].nc_off)
+      drop_graph(ctx);
+  }
   if (resized) {
     ctx->prepared = false;
     drop_graph(ctx);
@@ -1952,6 +2133,13 @@ int abl_set_near_mode(abl_ctx *ctx, int mode) {
   return ABL_OK;
 }
 
+int abl_set_near_cache(abl_ctx *ctx, int enable) {
+  if (!ctx) return ABL_E_INVALID;
+  ctx->near_cache = enable != 0;
+  drop_graph(ctx);
+  return ABL_OK;
+}
+
 int abl_set_balance(abl_ctx *ctx, int enable) {
   if (!ctx) return ABL_E_INVALID;
   ctx->balance = enable != 0;
@@ -2113,6 +2301,7 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
   ctx.stream = (cudaStream_t) stream;
   ctx.globals.assign((const unsigned char *) globals, (const unsigned char *) globals + globals_size);
   ctx.profile = false;
+  ctx.near_cache = false;  // kept lists would need an allocation per binning
   const void *G = ctx.globals.data();
   TypeState &t = ctx.types[0];
   t.d = &ad;

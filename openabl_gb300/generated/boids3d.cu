@@ -344,7 +344,7 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = abl_hi.z;
 }
 static const abl_step_desc abl_steps[] = {
-    {"update_boid", 0, 0, 1, abl_radius_update_boid, 3u, 3u, abl_launch_update_boid, 0, -1, 0, abl_launch_ens_update_boid, 0, 1, 3u},
+    {"update_boid", 0, 0, 1, abl_radius_update_boid, 3u, 3u, abl_launch_update_boid, 0, -1, 0, abl_launch_ens_update_boid, 0, 1, 3u, 1},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],

@@ -276,7 +276,7 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = abl_hi.z;
 }
 static const abl_step_desc abl_steps[] = {
-    {"move_point", 0, 0, 1, abl_radius_move_point, 1u, 1u, abl_launch_move_point, 0, -1, 0, abl_launch_ens_move_point, 0, 1, 1u},
+    {"move_point", 0, 0, 1, abl_radius_move_point, 1u, 1u, abl_launch_move_point, 0, -1, 0, abl_launch_ens_move_point, 0, 1, 1u, 1},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],

@@ -259,7 +259,7 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"step_move", 0, 0, 0, abl_radius_step_move, 3u, 1u, abl_launch_step_move, 0, -1, 0, abl_launch_ens_step_move, 0, 0, 2u},
+    {"step_move", 0, 0, 0, abl_radius_step_move, 3u, 1u, abl_launch_step_move, 0, -1, 0, abl_launch_ens_step_move, 0, 0, 2u, 1},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],

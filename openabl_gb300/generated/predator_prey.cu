@@ -1943,19 +1943,19 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"prey_avoid_pred", 1, 0, 1, abl_radius_prey_avoid_pred, 1u, 4u, abl_launch_prey_avoid_pred, 0, -1, 1, abl_launch_ens_prey_avoid_pred, 0, 1, 4u},
-    {"prey_flock", 1, 1, 1, abl_radius_prey_flock, 1u, 4u, abl_launch_prey_flock, 0, -1, 1, abl_launch_ens_prey_flock, 0, 1, 4u},
-    {"prey_move", 1, -1, 1, nullptr, 0u, 11u, abl_launch_prey_move, 0, -1, 1, abl_launch_ens_prey_move, 0, 0, 11u},
-    {"prey_eaten", 1, 0, 1, abl_radius_prey_eaten, 1u, 0u, abl_launch_prey_eaten, 1, -1, 1, nullptr, 0, 1, 0u},
-    {"prey_eat_or_starve", 1, 2, 0, abl_radius_prey_eat_or_starve, 5u, 8u, abl_launch_prey_eat_or_starve, 1, -1, 1, nullptr, 0, 0, 8u},
-    {"prey_reproduction", 1, -1, 1, nullptr, 0u, 0u, abl_launch_prey_reproduction, 0, 1, 1, nullptr, 1, 0, 8u},
-    {"pred_follow_prey", 0, 1, 1, abl_radius_pred_follow_prey, 1u, 4u, abl_launch_pred_follow_prey, 0, -1, 1, abl_launch_ens_pred_follow_prey, 0, 1, 4u},
-    {"pred_avoid", 0, 0, 1, abl_radius_pred_avoid, 1u, 4u, abl_launch_pred_avoid, 0, -1, 1, abl_launch_ens_pred_avoid, 0, 1, 4u},
-    {"pred_move", 0, -1, 1, nullptr, 0u, 11u, abl_launch_pred_move, 0, -1, 1, abl_launch_ens_pred_move, 0, 0, 11u},
-    {"pred_eat_or_starve", 0, 1, 0, abl_radius_pred_eat_or_starve, 1u, 8u, abl_launch_pred_eat_or_starve, 1, -1, 1, nullptr, 0, 0, 8u},
-    {"pred_reproduction", 0, -1, 1, nullptr, 0u, 0u, abl_launch_pred_reproduction, 0, 0, 1, nullptr, 1, 0, 8u},
-    {"grass_eaten", 2, 1, 1, abl_radius_grass_eaten, 1u, 0u, abl_launch_grass_eaten, 0, -1, 1, abl_launch_ens_grass_eaten, 0, 1, 6u},
-    {"grass_growth", 2, -1, 1, nullptr, 0u, 0u, abl_launch_grass_growth, 0, -1, 1, abl_launch_ens_grass_growth, 0, 0, 6u},
+    {"prey_avoid_pred", 1, 0, 1, abl_radius_prey_avoid_pred, 1u, 4u, abl_launch_prey_avoid_pred, 0, -1, 1, abl_launch_ens_prey_avoid_pred, 0, 1, 4u, 1},
+    {"prey_flock", 1, 1, 1, abl_radius_prey_flock, 1u, 4u, abl_launch_prey_flock, 0, -1, 1, abl_launch_ens_prey_flock, 0, 1, 4u, 1},
+    {"prey_move", 1, -1, 1, nullptr, 0u, 11u, abl_launch_prey_move, 0, -1, 1, abl_launch_ens_prey_move, 0, 0, 11u, 0},
+    {"prey_eaten", 1, 0, 1, abl_radius_prey_eaten, 1u, 0u, abl_launch_prey_eaten, 1, -1, 1, nullptr, 0, 1, 0u, 1},
+    {"prey_eat_or_starve", 1, 2, 0, abl_radius_prey_eat_or_starve, 5u, 8u, abl_launch_prey_eat_or_starve, 1, -1, 1, nullptr, 0, 0, 8u, 1},
+    {"prey_reproduction", 1, -1, 1, nullptr, 0u, 0u, abl_launch_prey_reproduction, 0, 1, 1, nullptr, 1, 0, 8u, 0},
+    {"pred_follow_prey", 0, 1, 1, abl_radius_pred_follow_prey, 1u, 4u, abl_launch_pred_follow_prey, 0, -1, 1, abl_launch_ens_pred_follow_prey, 0, 1, 4u, 1},
+    {"pred_avoid", 0, 0, 1, abl_radius_pred_avoid, 1u, 4u, abl_launch_pred_avoid, 0, -1, 1, abl_launch_ens_pred_avoid, 0, 1, 4u, 1},
+    {"pred_move", 0, -1, 1, nullptr, 0u, 11u, abl_launch_pred_move, 0, -1, 1, abl_launch_ens_pred_move, 0, 0, 11u, 0},
+    {"pred_eat_or_starve", 0, 1, 0, abl_radius_pred_eat_or_starve, 1u, 8u, abl_launch_pred_eat_or_starve, 1, -1, 1, nullptr, 0, 0, 8u, 1},
+    {"pred_reproduction", 0, -1, 1, nullptr, 0u, 0u, abl_launch_pred_reproduction, 0, 0, 1, nullptr, 1, 0, 8u, 0},
+    {"grass_eaten", 2, 1, 1, abl_radius_grass_eaten, 1u, 0u, abl_launch_grass_eaten, 0, -1, 1, abl_launch_ens_grass_eaten, 0, 1, 6u, 1},
+    {"grass_growth", 2, -1, 1, nullptr, 0u, 0u, abl_launch_grass_growth, 0, -1, 1, abl_launch_ens_grass_growth, 0, 0, 6u, 0},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[6],

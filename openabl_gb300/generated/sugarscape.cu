@@ -927,10 +927,10 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"metabolise_and_growback", 0, -1, 1, nullptr, 0u, 64u, abl_launch_metabolise_and_growback, 0, -1, 0, abl_launch_ens_metabolise_and_growback, 0, 0, 124u},
-    {"movement_request", 0, 0, 1, abl_radius_movement_request, 73u, 0u, abl_launch_movement_request, 0, -1, 0, abl_launch_ens_movement_request, 0, 1, 10u},
-    {"movement_response", 0, 0, 1, abl_radius_movement_response, 63u, 0u, abl_launch_movement_response, 0, -1, 0, abl_launch_ens_movement_response, 0, 1, 60u},
-    {"movement_transaction", 0, 0, 1, abl_radius_movement_transaction, 13u, 0u, abl_launch_movement_transaction, 0, -1, 0, abl_launch_ens_movement_transaction, 0, 1, 60u},
+    {"metabolise_and_growback", 0, -1, 1, nullptr, 0u, 64u, abl_launch_metabolise_and_growback, 0, -1, 0, abl_launch_ens_metabolise_and_growback, 0, 0, 124u, 0},
+    {"movement_request", 0, 0, 1, abl_radius_movement_request, 73u, 0u, abl_launch_movement_request, 0, -1, 0, abl_launch_ens_movement_request, 0, 1, 10u, 1},
+    {"movement_response", 0, 0, 1, abl_radius_movement_response, 63u, 0u, abl_launch_movement_response, 0, -1, 0, abl_launch_ens_movement_response, 0, 1, 60u, 1},
+    {"movement_transaction", 0, 0, 1, abl_radius_movement_transaction, 13u, 0u, abl_launch_movement_transaction, 0, -1, 0, abl_launch_ens_movement_transaction, 0, 1, 60u, 1},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],

@@ -341,6 +341,13 @@ class Simulation:
         L.abl_set_near_mode.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _check(L.abl_set_near_mode(self.ctx, int(mode)), "abl_set_near_mode")
 
+    def set_near_cache(self, enable=True):
+        """Keep each agent's neighbour list across timesteps where positions
+        never change (abl_set_near_cache); results are identical either way."""
+        L = _load()
+        L.abl_set_near_cache.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _check(L.abl_set_near_cache(self.ctx, 1 if enable else 0), "abl_set_near_cache")
+
     def set_balance(self, enable=True):
         """Hand each block's agents to threads by neighbour count (ordered near loops)."""
         L = _load()
