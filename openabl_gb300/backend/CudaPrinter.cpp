@@ -935,7 +935,8 @@ void CudaPrinter::printKernel(const StepInfo &info) {
         << "abl_cols_" << T << " in, out;" << nl << "abl_near_view NB;" << nl
         << "uint8_t *removed;" << nl << "uint8_t *child_flag;" << nl
         << "void *child_cols[ABL_MAX_MEMBERS];" << nl << "uint64_t seed;" << nl
-        << "long timestep;" << nl << "int step_index;" << outdent << nl << "};"
+        << "long timestep;" << nl << "int step_index;" << nl << "uint32_t skip_store;" << outdent
+        << nl << "};"
         << nl << "__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_" << name
         << "(const __grid_constant__ abl_kargs_" << name << " A) {" << indent << nl;
   if (info.presorted) {
@@ -980,7 +981,11 @@ void CudaPrinter::printKernel(const StepInfo &info) {
   for (size_t k = 0; k < agent.members->size(); k++) {
     const std::string &m = (*agent.members)[k]->name;
     if (copy || (info.outMaybe & (1u << k))) {
-      *this << nl << "A.out." << m << "[abl_i] = abl_out." << m << ";";
+      // A member the step only copies from `in` (out.m = in.m) is stored
+      // unless the runtime knows the double buffer holds the same value.
+      const bool selfCopyOnly = !copy && !(info.outChanged & (1u << k));
+      *this << nl << (selfCopyOnly ? "if (!(A.skip_store & " + std::to_string(1u << k) + "u)) " : "")
+            << "A.out." << m << "[abl_i] = abl_out." << m << ";";
     }
   }
   if (info.usesRemove) *this << nl << "A.removed[abl_i] = (uint8_t) abl_K.removed;";
@@ -1001,7 +1006,7 @@ void CudaPrinter::printKernel(const StepInfo &info) {
         << "A.child_flag = L->child_flag;" << nl
         << "for (int k = 0; k < ABL_MAX_MEMBERS; k++) A.child_cols[k] = L->child_cols[k];" << nl
         << "A.seed = L->seed;" << nl << "A.timestep = L->timestep;" << nl
-        << "A.step_index = L->step_index;" << nl
+        << "A.step_index = L->step_index;" << nl << "A.skip_store = L->skip_store;" << nl
         << "const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : "
            "ABL_STEP_BLOCK;" << nl
         << "const long abl_grid = (A.n + abl_block - 1) / abl_block;" << nl

@@ -113,6 +113,13 @@ __device__ inline band make_band(double radius, float amax, int dim) {
   return make_band((float) radius, amax, dim);
 }
 
+// Entry k of the kept neighbour lists (abl_near_view::ncache_list) of agent
+// `self`: the neighbour's agent index.
+__device__ __forceinline__ int kept_entry(const abl_near_view &V, long self, int k) {
+  return V.ncache_narrow ? (int) self + (int) __ldg(&((const short *) V.ncache_list)[k])
+                         : __ldg(&((const int *) V.ncache_list)[k]);
+}
+
 // Query side of a near loop: the agent's cell and float position.
 template <int DIM>
 struct near_query {
@@ -132,7 +139,9 @@ struct near_query {
       : self(self_) {
     const int dims[3] = {V.nx, V.ny, V.nz};
     const double p[3] = {x, y, z};
-    if (self >= 0 && V.cell_of) {
+    if (self >= 0 && V.ncache_off) {
+      c[0] = c[1] = c[2] = 0;  // kept lists: no cell search
+    } else if (self >= 0 && V.cell_of) {
       const int l = (int) (__ldg(&V.cell_of[self]) - V.cell_base);
       const int nxy = V.nx * V.ny;
       c[2] = l / nxy;
@@ -222,7 +231,7 @@ struct near_cursor {
   __device__ bool fill(const near_query<DIM> &q, Exact &&exact) {
     cnt = 0;
     if (V.ncache_off && q.self >= 0) {
-      while (cur < end && cnt < ABL_NEAR_CHUNK) buf[ABL_STEP_BLOCK * cnt++] = __ldg(&V.ncache_slot[cur++]);
+      while (cur < end && cnt < ABL_NEAR_CHUNK) buf[ABL_STEP_BLOCK * cnt++] = kept_entry(V, q.self, cur++);
       return cnt > 0;
     }
     for (;;) {
@@ -888,7 +897,7 @@ __device__ int presort_block(const abl_near_view &V, bool has, const near_query<
     if (has) {
       const int from = __ldg(&V.ncache_off[q.self]), end = __ldg(&V.ncache_off[q.self + 1]);
       const int n = end - from < S.cap ? end - from : S.cap;
-      for (int j = 0; j < n; j++) S.slots[j * ABL_STEP_BLOCK + t] = __ldg(&V.ncache_slot[from + j]);
+      for (int j = 0; j < n; j++) S.slots[j * ABL_STEP_BLOCK + t] = kept_entry(V, q.self, from + j);
       key = end - from;
       S.total[t] = key;
       S.resume[t] = from + n;
@@ -957,7 +966,7 @@ struct near_list_cursor {
         const int from = first ? __ldg(&V.ncache_off[q.self]) : S.resume[col];
         const int end = __ldg(&V.ncache_off[q.self + 1]);
         const int n = end - from < S.cap ? end - from : S.cap;
-        for (int j = 0; j < n; j++) S.slots[j * ABL_STEP_BLOCK + col] = __ldg(&V.ncache_slot[from + j]);
+        for (int j = 0; j < n; j++) S.slots[j * ABL_STEP_BLOCK + col] = kept_entry(V, q.self, from + j);
         S.resume[col] = from + n;
         stored = n;
         tot = end - from;

@@ -70,8 +70,12 @@ typedef struct {
   int block_cap;            /* row lists, agents visited in slot order: entries of the
                                per-block neighbourhood lists in shared memory (0: off) */
   const int *ncache_off;    /* neighbour lists kept across timesteps (NULL: none): query
-                               agent i's in-radius slots are ncache_slot[off[i] .. off[i+1]) */
-  const int *ncache_slot;   /* in ascending agent id for ordered loops */
+                               agent i's in-radius neighbours are entries off[i] .. off[i+1]
+                               of ncache_list, in ascending index for ordered loops; `cols`
+                               and `posf` are then indexed by agent, not by slot */
+  const void *ncache_list;  /* int32 agent indices, or with ncache_narrow int16 offsets
+                               from the query agent's index */
+  int ncache_narrow;
 } abl_near_view;
 
 /* Everything a generated step launcher needs. */
@@ -93,6 +97,9 @@ typedef struct {
   uint64_t seed;
   long timestep;
   int step_index;
+  /* members the kernel need not store: the step only ever copies them from
+     `in`, and the double buffer already holds the same values */
+  uint32_t skip_store;
 } abl_step_launch;
 
 typedef int (*abl_step_launch_fn)(const abl_step_launch *launch, cudaStream_t stream);

@@ -642,10 +642,14 @@ struct StepState {
   ScanPlan keep_scan, child_scan;
   long parent_cap = 0;
   // Neighbour lists kept across timesteps (static positions): per agent of
-  // the step's type its in-radius neighbour slots, ascending id for ordered
-  // loops.  Built for binning `nc_bin` of the step's grid (-1: none); nc_off
-  // null with nc_bin set means the lists did not fit for that binning.
-  int *nc_off = nullptr, *nc_slot = nullptr;
+  // the step's type the indices of its in-radius neighbours, ascending (int16
+  // offsets from the agent's own index when they all fit), and the agents'
+  // float positions by index.  Built for binning `nc_bin` of the step's grid
+  // (-1: none); nc_off null with nc_bin set means they did not fit.
+  int *nc_off = nullptr;
+  void *nc_list = nullptr;
+  bool nc_narrow = false;
+  float *nc_posf = nullptr;
   long nc_bin = -1;
   double nc_radius = 0.0;
   std::vector<void *> nc_allocs;
@@ -705,6 +709,9 @@ struct abl_ctx {
   int block_cap = 2048;
   bool near_cache = true;
   long bin_serial = 0;
+  // Step kernels skip stores of members that never change (both buffers
+  // hold them since the upload).
+  bool skip_stores = true;
   std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
   std::vector<double> prof_seconds;
   std::vector<long> prof_launches;
@@ -1279,6 +1286,24 @@ bool positions_static(const abl_model_desc *m, int ti) {
   return true;
 }
 
+// Members of type ti that keep their uploaded values for good: no step
+// function writes them except as `out.m = in.m`, and no step adds or removes
+// agents of the type.  Once both buffers hold them (the upload copies them),
+// step kernels need not store them.
+uint32_t invariant_members(const abl_model_desc *m, int ti) {
+  const abl_agent_desc &a = m->agents[ti];
+  uint32_t changed = 0;
+  for (int k = 0; k < m->num_steps; k++) {
+    const abl_step_desc &sd = m->steps[k];
+    if (sd.add_type == ti) return 0;
+    if (sd.agent_type != ti) continue;
+    if (sd.uses_remove || sd.add_type >= 0) return 0;
+    changed |= sd.out_changed;
+  }
+  const uint32_t all = a.num_members >= 32 ? ~0u : (1u << a.num_members) - 1;
+  return all & ~changed;
+}
+
 // A step function (without population changes) changed members `written`
 // of type ti.  Grids of a type whose positions never change keep their
 // binning and only re-gather (if they copy a changed member); every other
@@ -1346,13 +1371,14 @@ __device__ __forceinline__ bool nc_within(const Real *pos, long i, long j, doubl
   return !((double) f > radius);
 }
 
-// Pass 1 (slots == nullptr): count[i] = agent i's neighbours.  Pass 2: its
-// neighbours' slots from slots[off[i]], in the cells' order; with `sorted`
-// then in ascending agent id (the order the reference visits them in).
+// Pass 1 (list == nullptr): count[i] = agent i's neighbours.  Pass 2: their
+// agent indices from list[off[i]], ascending (the order the reference visits
+// them in), the largest |neighbour - i| folded into *span, and agent i's
+// float position (as the grid's slot-ordered copy rounds it) into posf.
 template <typename Real, int DIM>
 __global__ void k_nc_lists(const Real *pos, long n, const int *cell_of, const int *cell_start,
                            const int *order, int nx, int ny, int nz, int R, double radius,
-                           int *count, const int *off, int *slots, bool sorted) {
+                           int *count, const int *off, int *list, int *span, float *posf) {
   const long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int l = cell_of[i];
@@ -1362,14 +1388,15 @@ __global__ void k_nc_lists(const Real *pos, long n, const int *cell_of, const in
   const int y0 = max(c1 - R, 0), y1 = min(c1 + R, ny - 1);
   const int x0 = max(c0 - R, 0), x1 = min(c0 + R, nx - 1);
   int k = 0;
-  int *out = slots ? slots + off[i] : nullptr;
+  int *out = list ? list + off[i] : nullptr;
   for (int z = z0; z <= z1; z++) {
     for (int y = y0; y <= y1; y++) {
       const int base = (z * ny + y) * nx;
       const int e = cell_start[base + x1 + 1];
       for (int s = cell_start[base + x0]; s < e; s++) {
-        if (!nc_within<Real, DIM>(pos, i, order[s], radius)) continue;
-        if (out) out[k] = s;
+        const int j = order[s];
+        if (!nc_within<Real, DIM>(pos, i, j, radius)) continue;
+        if (out) out[k] = j;
         k++;
       }
     }
@@ -1378,32 +1405,43 @@ __global__ void k_nc_lists(const Real *pos, long n, const int *cell_of, const in
     count[i] = k;
     return;
   }
-  if (!sorted) return;
-  for (int a = 1; a < k; a++) {
-    const int v = out[a], key = order[v];
+  int far = 0;
+  for (int a = 0; a < k; a++) {
+    const int v = out[a];
+    far = max(far, abs(v - (int) i));
     int b = a - 1;
-    while (b >= 0 && order[out[b]] > key) {
+    while (b >= 0 && out[b] > v) {
       out[b + 1] = out[b];
       b--;
     }
     out[b + 1] = v;
   }
+  atomicMax(span, far);
+#pragma unroll
+  for (int d = 0; d < DIM; d++) posf[DIM * i + d] = (float) pos[DIM * i + d];
+}
+
+// The int16 form of the lists: entry - owning agent's index.
+__global__ void k_nc_narrow(long n, const int *off, const int *list, short *narrow) {
+  const long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = off[i]; k < off[i + 1]; k++) narrow[k] = (short) (list[k] - (int) i);
 }
 
 template <typename Real>
 void launch_nc_lists(abl_ctx *ctx, const TypeState &g, double radius, int *count, const int *off,
-                     int *slots, bool sorted) {
+                     int *list, int *span, float *posf) {
   const int B = 128;
   const Real *pos = (const Real *) g.cols[g.cur][g.d->position_member];
   const long nb = blocks_for(g.n, B);
   if (g.d->dim == 2) {
     k_nc_lists<Real, 2><<<nb, B, 0, ctx->stream>>>(pos, g.n, g.cell_of, g.cell_start, g.order,
                                                    g.nx, g.ny, g.nz, g.R, radius, count, off,
-                                                   slots, sorted);
+                                                   list, span, posf);
   } else {
     k_nc_lists<Real, 3><<<nb, B, 0, ctx->stream>>>(pos, g.n, g.cell_of, g.cell_start, g.order,
                                                    g.nx, g.ny, g.nz, g.R, radius, count, off,
-                                                   slots, sorted);
+                                                   list, span, posf);
   }
   ctx->launches++;
 }
@@ -1414,39 +1452,53 @@ bool near_cache_wanted(const abl_ctx *ctx, const abl_step_desc &sd) {
       && positions_static(ctx->model, sd.agent_type);
 }
 
-// Brings step k's kept lists up to date with grid g (just binned) and
-// returns whether they can be read.  Building needs a host read of the total,
-// so a stream capture only reads lists that are already current.
-int near_cache_ready(abl_ctx *ctx, int k, const TypeState &g, double radius, bool sorted,
-                     bool &ready) {
+void nc_release(abl_ctx *ctx, StepState &st, void *p) {
+  dev_free(ctx, p);
+  st.nc_allocs.erase(std::remove(st.nc_allocs.begin(), st.nc_allocs.end(), p),
+                     st.nc_allocs.end());
+}
+
+// Brings step k's kept lists up to date with grid g and returns whether they
+// can be read.  Building needs host reads (the total, the index span), so a
+// stream capture only reads lists that are already current.
+int near_cache_ready(abl_ctx *ctx, int k, const TypeState &g, double radius, bool &ready) {
   ready = false;
   StepState &st = ctx->step_state[k];
-  if (st.nc_bin == g.bin_id && st.nc_radius == radius) {
+  if (!g.dirty && st.nc_bin == g.bin_id && st.nc_radius == radius) {
     ready = st.nc_off != nullptr;
     return ABL_OK;
   }
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(ctx->stream, &cs);
-  if (cs != cudaStreamCaptureStatusNone) return ABL_OK;
+  if (cs != cudaStreamCaptureStatusNone || g.dirty) return ABL_OK;
   // Graphs captured earlier may read the lists about to be replaced.
   drop_graph(ctx);
   for (void *p : st.nc_allocs) dev_free(ctx, p);
   st.nc_allocs.clear();
-  st.nc_off = st.nc_slot = nullptr;
+  st.nc_off = nullptr;
+  st.nc_list = nullptr;
+  st.nc_posf = nullptr;
   st.nc_bin = g.bin_id;
   st.nc_radius = radius;
   if (g.n <= 0) return ABL_OK;
   auto *own = &st.nc_allocs;
-  int *count = nullptr;
+  int *count = nullptr, *span = nullptr, *list = nullptr;
   ScanPlan plan;
-  if (dev_alloc_t(ctx, &count, g.n, own) != ABL_OK || dev_alloc_t(ctx, &st.nc_off, g.n + 1, own) != ABL_OK
-      || scan_plan(ctx, plan, g.n, own) != ABL_OK) {
+  auto give_up = [&]() {
+    for (void *p : st.nc_allocs) dev_free(ctx, p);
+    st.nc_allocs.clear();
     st.nc_off = nullptr;
     return ABL_OK;  // no room: the step searches the grid
-  }
+  };
+  if (dev_alloc_t(ctx, &count, g.n, own) != ABL_OK
+      || dev_alloc_t(ctx, &st.nc_off, g.n + 1, own) != ABL_OK
+      || dev_alloc_t(ctx, &span, 1, own) != ABL_OK
+      || dev_alloc_t(ctx, &st.nc_posf, g.n * g.d->dim, own) != ABL_OK
+      || scan_plan(ctx, plan, g.n, own) != ABL_OK)
+    return give_up();
   const bool dbl = pos_is_double(g);
-  if (dbl) launch_nc_lists<double>(ctx, g, radius, count, nullptr, nullptr, sorted);
-  else launch_nc_lists<float>(ctx, g, radius, count, nullptr, nullptr, sorted);
+  if (dbl) launch_nc_lists<double>(ctx, g, radius, count, nullptr, nullptr, nullptr, nullptr);
+  else launch_nc_lists<float>(ctx, g, radius, count, nullptr, nullptr, nullptr, nullptr);
   scan_run(ctx, plan, count, st.nc_off);
   int total = 0;
   ABL_CUDA_TRY(cudaMemcpyAsync(&total, st.nc_off + g.n, sizeof(int), cudaMemcpyDeviceToHost,
@@ -1454,12 +1506,26 @@ int near_cache_ready(abl_ctx *ctx, int k, const TypeState &g, double radius, boo
   ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   // Lists far longer than a handful of cells' worth are not worth keeping.
   if (total < 0 || (long) total > 64 * g.n + 4096
-      || dev_alloc_t(ctx, &st.nc_slot, std::max(total, 1), own) != ABL_OK) {
-    st.nc_off = st.nc_slot = nullptr;
-    return ABL_OK;
+      || dev_alloc_t(ctx, &list, std::max(total, 1), own) != ABL_OK)
+    return give_up();
+  ABL_CUDA_TRY(cudaMemsetAsync(span, 0, sizeof(int), ctx->stream));
+  if (dbl) launch_nc_lists<double>(ctx, g, radius, nullptr, st.nc_off, list, span, st.nc_posf);
+  else launch_nc_lists<float>(ctx, g, radius, nullptr, st.nc_off, list, span, st.nc_posf);
+  int far = 0;
+  ABL_CUDA_TRY(cudaMemcpyAsync(&far, span, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  st.nc_list = list;
+  st.nc_narrow = false;
+  short *narrow = nullptr;
+  if (far <= 32767 && dev_alloc_t(ctx, &narrow, std::max(total, 1), own) == ABL_OK) {
+    k_nc_narrow<<<blocks_for(g.n, 256), 256, 0, ctx->stream>>>(g.n, st.nc_off, list, narrow);
+    ctx->launches++;
+    ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    nc_release(ctx, st, list);
+    st.nc_list = narrow;
+    st.nc_narrow = true;
   }
-  if (dbl) launch_nc_lists<double>(ctx, g, radius, nullptr, st.nc_off, st.nc_slot, sorted);
-  else launch_nc_lists<float>(ctx, g, radius, nullptr, st.nc_off, st.nc_slot, sorted);
+  nc_release(ctx, st, count);
   ready = true;
   return ABL_OK;
 }
@@ -1480,6 +1546,7 @@ int step_once(abl_ctx *ctx) {
     L.seed = ctx->seed;
     L.timestep = ctx->timestep;
     L.step_index = k;
+    L.skip_store = ctx->skip_stores ? invariant_members(m, sd.agent_type) : 0;
     bool changes = sd.uses_remove || sd.add_type >= 0;
     if (changes) {
       StepState &st = ctx->step_state[k];
@@ -1493,8 +1560,14 @@ int step_once(abl_ctx *ctx) {
     }
     if (sd.near_type >= 0) {
       int gi = ctx->step_grid[k];
-      if (ctx->grids[gi].dirty || ctx->grids[gi].regather) bin_grid(ctx, gi);
       TypeState &nt = ctx->grids[gi];
+      // Kept lists read the step's own columns: a grid that only needs its
+      // slot-ordered copies refreshed is left as it is.
+      bool cached = false;
+      if (nt.dirty) bin_grid(ctx, gi);
+      if (near_cache_wanted(ctx, sd))
+        ABL_TRY(near_cache_ready(ctx, k, nt, sd.radius(ctx->globals.data()), cached));
+      if (!cached && nt.regather) bin_grid(ctx, gi);
       abl_near_view &V = L.near;
       const int depth = list_depth(sd, *nt.d, ctx->near_mode);
       V.dim = nt.d->dim;
@@ -1522,13 +1595,15 @@ int step_once(abl_ctx *ctx) {
       // Threads visit the binned agents in slot order, so a block's agents
       // fill consecutive cells: block lists pay off.
       V.block_cap = block_lists_wanted(sd, depth, ctx->near_mode) ? ctx->block_cap : 0;
-      bool cached = false;
-      if (near_cache_wanted(ctx, sd))
-        ABL_TRY(near_cache_ready(ctx, k, nt, V.radius, sd.ordered != 0, cached));
       if (cached) {
-        // Kept lists: agents in index order, no block lists.
-        V.ncache_off = ctx->step_state[k].nc_off;
-        V.ncache_slot = ctx->step_state[k].nc_slot;
+        // Kept lists: agents in index order, neighbours read by index from
+        // the step's own columns, no block lists.
+        const StepState &st = ctx->step_state[k];
+        V.ncache_off = st.nc_off;
+        V.ncache_list = st.nc_list;
+        V.ncache_narrow = st.nc_narrow ? 1 : 0;
+        V.posf = st.nc_posf;
+        for (int j = 0; j < t.d->num_members; j++) V.cols[j] = t.cols[t.cur][j];
         V.block_cap = 0;
       }
       if (sd.presorted) L.smem = abl::presort_bytes(V);
@@ -1836,6 +1911,7 @@ static int size_type(abl_ctx *ctx, TypeState &t, size_t n, bool &resized) {
 // (its `out` column is overwritten before the buffers swap), nor when no
 // step function runs on the type (the buffers never swap).
 static bool dbuf_read(const abl_model_desc *m, int ti, int k) {
+  if (invariant_members(m, ti) & (1u << k)) return true;  // kernels skip their stores
   for (int s = 0; s < m->num_steps; s++) {
     const abl_step_desc &sd = m->steps[s];
     if (sd.agent_type != ti) continue;
@@ -2302,6 +2378,7 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
   ctx.globals.assign((const unsigned char *) globals, (const unsigned char *) globals + globals_size);
   ctx.profile = false;
   ctx.near_cache = false;  // kept lists would need an allocation per binning
+  ctx.skip_stores = false; // the caller's output buffers hold nothing yet
   const void *G = ctx.globals.data();
   TypeState &t = ctx.types[0];
   t.d = &ad;

@@ -207,6 +207,7 @@ struct abl_kargs_update_boid {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_update_boid(const __grid_constant__ abl_kargs_update_boid A) {
     int abl_j;
@@ -256,6 +257,7 @@ static int abl_launch_update_boid(const abl_step_launch *L, cudaStream_t abl_str
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_update_boid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);

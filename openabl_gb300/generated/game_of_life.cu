@@ -149,6 +149,7 @@ struct abl_kargs_step_move {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_step_move(const __grid_constant__ abl_kargs_step_move A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -166,7 +167,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     abl_in.alive = A.in.alive[abl_i];
     abl_out.alive = A.out.alive[abl_i];
     step_move(A.G, A.NB, abl_K, &abl_in, &abl_out);
-    A.out.pos[abl_i] = abl_out.pos;
+    if (!(A.skip_store & 1u)) A.out.pos[abl_i] = abl_out.pos;
     A.out.alive[abl_i] = abl_out.alive;
 }
 static int abl_launch_step_move(const abl_step_launch *L, cudaStream_t abl_stream) {
@@ -185,6 +186,7 @@ static int abl_launch_step_move(const abl_step_launch *L, cudaStream_t abl_strea
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_step_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);

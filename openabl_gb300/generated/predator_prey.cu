@@ -259,6 +259,7 @@ struct abl_kargs_prey_avoid_pred {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_avoid_pred(const __grid_constant__ abl_kargs_prey_avoid_pred A) {
     int abl_j;
@@ -317,6 +318,7 @@ static int abl_launch_prey_avoid_pred(const abl_step_launch *L, cudaStream_t abl
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_avoid_pred<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -446,6 +448,7 @@ struct abl_kargs_prey_flock {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_flock(const __grid_constant__ abl_kargs_prey_flock A) {
     int abl_j;
@@ -504,6 +507,7 @@ static int abl_launch_prey_flock(const abl_step_launch *L, cudaStream_t abl_stre
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_flock<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -594,6 +598,7 @@ struct abl_kargs_prey_move {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_move(const __grid_constant__ abl_kargs_prey_move A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -638,6 +643,7 @@ static int abl_launch_prey_move(const abl_step_launch *L, cudaStream_t abl_strea
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -727,6 +733,7 @@ struct abl_kargs_prey_eaten {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_eaten(const __grid_constant__ abl_kargs_prey_eaten A) {
     int abl_j;
@@ -786,6 +793,7 @@ static int abl_launch_prey_eaten(const abl_step_launch *L, cudaStream_t abl_stre
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -843,6 +851,7 @@ struct abl_kargs_prey_eat_or_starve {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_eat_or_starve(const __grid_constant__ abl_kargs_prey_eat_or_starve A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -888,6 +897,7 @@ static int abl_launch_prey_eat_or_starve(const abl_step_launch *L, cudaStream_t 
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_eat_or_starve<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -921,6 +931,7 @@ struct abl_kargs_prey_reproduction {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_reproduction(const __grid_constant__ abl_kargs_prey_reproduction A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -966,6 +977,7 @@ static int abl_launch_prey_reproduction(const abl_step_launch *L, cudaStream_t a
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_reproduction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1028,6 +1040,7 @@ struct abl_kargs_pred_follow_prey {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_follow_prey(const __grid_constant__ abl_kargs_pred_follow_prey A) {
     int abl_j;
@@ -1086,6 +1099,7 @@ static int abl_launch_pred_follow_prey(const abl_step_launch *L, cudaStream_t ab
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_follow_prey<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1204,6 +1218,7 @@ struct abl_kargs_pred_avoid {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_avoid(const __grid_constant__ abl_kargs_pred_avoid A) {
     int abl_j;
@@ -1262,6 +1277,7 @@ static int abl_launch_pred_avoid(const abl_step_launch *L, cudaStream_t abl_stre
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_avoid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1354,6 +1370,7 @@ struct abl_kargs_pred_move {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_move(const __grid_constant__ abl_kargs_pred_move A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1398,6 +1415,7 @@ static int abl_launch_pred_move(const abl_step_launch *L, cudaStream_t abl_strea
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1481,6 +1499,7 @@ struct abl_kargs_pred_eat_or_starve {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_eat_or_starve(const __grid_constant__ abl_kargs_pred_eat_or_starve A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1526,6 +1545,7 @@ static int abl_launch_pred_eat_or_starve(const abl_step_launch *L, cudaStream_t 
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_eat_or_starve<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1559,6 +1579,7 @@ struct abl_kargs_pred_reproduction {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_reproduction(const __grid_constant__ abl_kargs_pred_reproduction A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1604,6 +1625,7 @@ static int abl_launch_pred_reproduction(const abl_step_launch *L, cudaStream_t a
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_reproduction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1662,6 +1684,7 @@ struct abl_kargs_grass_eaten {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_grass_eaten(const __grid_constant__ abl_kargs_grass_eaten A) {
     int abl_j;
@@ -1716,6 +1739,7 @@ static int abl_launch_grass_eaten(const abl_step_launch *L, cudaStream_t abl_str
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_grass_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1798,6 +1822,7 @@ struct abl_kargs_grass_growth {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_grass_growth(const __grid_constant__ abl_kargs_grass_growth A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1838,6 +1863,7 @@ static int abl_launch_grass_growth(const abl_step_launch *L, cudaStream_t abl_st
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_grass_growth<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);

@@ -173,6 +173,7 @@ struct abl_kargs_metabolise_and_growback {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_metabolise_and_growback(const __grid_constant__ abl_kargs_metabolise_and_growback A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -233,6 +234,7 @@ static int abl_launch_metabolise_and_growback(const abl_step_launch *L, cudaStre
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_metabolise_and_growback<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -338,6 +340,7 @@ struct abl_kargs_movement_request {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_movement_request(const __grid_constant__ abl_kargs_movement_request A) {
     int abl_j;
@@ -407,6 +410,7 @@ static int abl_launch_movement_request(const abl_step_launch *L, cudaStream_t ab
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_movement_request<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -539,6 +543,7 @@ struct abl_kargs_movement_response {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_movement_response(const __grid_constant__ abl_kargs_movement_response A) {
     int abl_j;
@@ -612,6 +617,7 @@ static int abl_launch_movement_response(const abl_step_launch *L, cudaStream_t a
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_movement_response<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -734,6 +740,7 @@ struct abl_kargs_movement_transaction {
     uint64_t seed;
     long timestep;
     int step_index;
+    uint32_t skip_store;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_movement_transaction(const __grid_constant__ abl_kargs_movement_transaction A) {
     int abl_j;
@@ -807,6 +814,7 @@ static int abl_launch_movement_transaction(const abl_step_launch *L, cudaStream_
     A.seed = L->seed;
     A.timestep = L->timestep;
     A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_movement_transaction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
