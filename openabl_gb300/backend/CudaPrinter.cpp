@@ -1096,7 +1096,14 @@ void CudaPrinter::printKernel(const StepInfo &info) {
 void CudaPrinter::printGlobals() {
   *this << "struct abl_globals {" << indent;
   for (AST::ConstDeclaration *decl : script.consts) {
-    if (decl->isArray) throw BackendError("The cuda backend does not support constant arrays yet");
+    if (decl->isArray) {
+      // A constant array (`int A[] = {...}`) becomes a fixed-size field,
+      // initialised like the reference's C array (GenericCPrinter.cpp:77-80).
+      auto *init = dynamic_cast<const AST::ArrayInitExpression *>(&*decl->expr);
+      if (!init) throw BackendError("Unexpected constant array initializer");
+      *this << nl << *decl->type << " " << decl->var->name << "[" << init->exprs->size() << "];";
+      continue;
+    }
     *this << nl << *decl->type << " " << decl->var->name << ";";
   }
   *this << outdent << nl << "};" << nl
@@ -1324,9 +1331,12 @@ void CudaPrinter::printDescriptor() {
   }
   *this << outdent << nl << "};" << nl;
   *this << "static const abl_global_desc abl_global_table[] = {" << indent;
+  int scalarConsts = 0;
   for (AST::ConstDeclaration *decl : script.consts) {
+    if (decl->isArray) continue;  // constant arrays are not set by name
     *this << nl << "{\"" << decl->var->name << "\", " << ablTypeId(decl->type->resolved)
           << ", offsetof(abl_globals, " << decl->var->name << ")},";
+    scalarConsts++;
   }
   *this << nl << "{nullptr, 0, 0}" << outdent << nl << "};" << nl;
 
@@ -1397,7 +1407,7 @@ void CudaPrinter::printDescriptor() {
   *this << "extern const abl_model_desc abl_desc = {" << indent << nl
         << "\"" << modelName << "\", " << (int) script.agents.size() << ", abl_agents, "
         << numSteps << ", abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, "
-        << (int) script.consts.size() << ", abl_global_table, " << envDim
+        << scalarConsts << ", abl_global_table, " << envDim
         << ", abl_env_bounds, " << (granE ? "abl_granularity" : "nullptr") << ", "
         << (useFloat ? 1 : 0) << ", "
         << (seqStep ? "abl_seq_" + seqStep->name : std::string("nullptr")) << outdent << nl

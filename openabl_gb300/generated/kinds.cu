@@ -1,0 +1,380 @@
+// Generated by OpenABL -b cuda (model "kinds").
+#include "abl_gen.cuh"
+
+namespace abl_model_kinds {
+
+typedef double abl_float;
+#include "abl_math.cuh"
+
+typedef struct {
+    float2 pos;
+    int kind;
+    double score;
+} Cell;
+static const type_info Cell_info[] = {
+    { TYPE_FLOAT2, offsetof(Cell, pos), "pos", true },
+    { TYPE_INT, offsetof(Cell, kind), "kind", false },
+    { TYPE_FLOAT, offsetof(Cell, score), "score", false },
+    { TYPE_END, sizeof(Cell), NULL }
+};
+
+struct agent_struct {
+    dyn_array agents_Cell;
+    dyn_array agents_Cell_dbuf;
+};
+static struct agent_struct agents;
+static const agent_info agents_info[] = {
+    { Cell_info, offsetof(struct agent_struct, agents_Cell), "Cell" },
+    { NULL, 0, NULL }
+};
+
+struct abl_globals {
+    double PI;
+    int num_timesteps;
+    int num_agents;
+    double W;
+    double reach;
+    float WEIGHT[3];
+    int NEXT_KIND[3];
+};
+static const abl_globals abl_globals_default = {
+    3.14159,
+    30,
+    3000,
+    60.0,
+    2.5,
+    { 0.5, (-1.25), 2.0 },
+    { 1, 2, 0 },
+};
+static abl_globals abl_G = abl_globals_default;
+static abl::rng abl_R;  // unused on the host: main() draws from the host stream
+struct abl_cols_Cell {
+    float2 *pos;
+    int *kind;
+    double *score;
+};
+
+__host__ __device__ static inline float2 random_1(const abl_globals &abl_G, abl::rng &abl_R, float2 min, float2 max) {
+    return ([&]() { const auto abl_e1_1 = abl_random(abl_R, min.y, max.y); const auto abl_e1_0 = abl_random(abl_R, min.x, max.x); return float2_create(abl_e1_0, abl_e1_1); }());
+}
+__host__ __device__ static inline float3 random_2(const abl_globals &abl_G, abl::rng &abl_R, float3 min, float3 max) {
+    return ([&]() { const auto abl_e2_2 = abl_random(abl_R, min.z, max.z); const auto abl_e2_1 = abl_random(abl_R, min.y, max.y); const auto abl_e2_0 = abl_random(abl_R, min.x, max.x); return float3_create(abl_e2_0, abl_e2_1, abl_e2_2); }());
+}
+__host__ __device__ static inline double random_3(const abl_globals &abl_G, abl::rng &abl_R, double max) {
+    return abl_random(abl_R, 0, max);
+}
+__host__ __device__ static inline float2 random_4(const abl_globals &abl_G, abl::rng &abl_R, float2 max) {
+    return random_1(abl_G, abl_R, float2_fill(0), max);
+}
+__host__ __device__ static inline float3 random_5(const abl_globals &abl_G, abl::rng &abl_R, float3 max) {
+    return random_2(abl_G, abl_R, float3_fill(0), max);
+}
+__host__ __device__ static inline int randomInt_1(const abl_globals &abl_G, abl::rng &abl_R, int max) {
+    return abl_random_int(abl_R, 0, max);
+}
+__host__ __device__ static inline double clamp(const abl_globals &abl_G, abl::rng &abl_R, double pos, double min, double max) {
+    return ((pos < min) ? min : ((pos > max) ? max : pos));
+}
+__host__ __device__ static inline float2 clamp_1(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 min, float2 max) {
+    return float2_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)));
+}
+__host__ __device__ static inline float3 clamp_2(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 min, float3 max) {
+    return float3_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)), ((pos.z < min.z) ? min.z : ((pos.z > max.z) ? max.z : pos.z)));
+}
+__host__ __device__ static inline double clamp_3(const abl_globals &abl_G, abl::rng &abl_R, double pos, double max) {
+    return clamp(abl_G, abl_R, pos, 0, max);
+}
+__host__ __device__ static inline float2 clamp_4(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return clamp_1(abl_G, abl_R, pos, float2_fill(0), max);
+}
+__host__ __device__ static inline float3 clamp_5(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 max) {
+    return clamp_2(abl_G, abl_R, pos, float3_fill(0), max);
+}
+__host__ __device__ static inline double wraparound(const abl_globals &abl_G, abl::rng &abl_R, double pos, double max) {
+    return ((pos < 0) ? (max + pos) : ((pos >= max) ? (pos - max) : pos));
+}
+__host__ __device__ static inline float2 wraparound_1(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return float2_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)));
+}
+__host__ __device__ static inline float3 wraparound_2(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 max) {
+    return float3_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)), ((pos.z < 0) ? (max.z + pos.z) : ((pos.z >= max.z) ? (pos.z - max.z) : pos.z)));
+}
+__host__ __device__ static inline bool is_inside(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return ((((pos.x >= 0) && (pos.y >= 0)) && (pos.x <= max.x)) && (pos.y <= max.y));
+}
+__device__ static void mix(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Cell* in, Cell* out) {
+    abl::rng &abl_R = abl_K.R;
+    (void) abl_R; (void) abl_NB;
+    double total = 0.0;
+    int seen = 0;
+    {
+        const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
+        abl::near_list_cursor<2> abl_c1(abl_NB, abl_q1, abl_K);
+        auto abl_exact1 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, in->pos) > abl_G.reach);
+        };
+        while (abl_c1.fill(abl_q1, abl_exact1)) {
+            int abl_pslot1 = abl_c1.slot(0);
+            Cell abl_pnx1;
+            abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
+            abl_pnx1.kind = ((const int *) abl_NB.cols[1])[abl_pslot1];
+            for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
+                const int abl_slot1 = abl_pslot1;
+                Cell abl_nx1 = abl_pnx1;
+                if (abl_k + 1 < abl_c1.cnt) {
+                    abl_pslot1 = abl_c1.slot(abl_k + 1);
+                    abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
+                    abl_pnx1.kind = ((const int *) abl_NB.cols[1])[abl_pslot1];
+                }
+                Cell* nx = &abl_nx1;
+                {
+                    total += (abl_G.WEIGHT[nx->kind] * dist_float2(in->pos, nx->pos));
+                    seen += 1;
+                }
+            }
+        }
+    }
+    out->score = ((in->score * 0.5) + (total / (float) seen));
+    if ((total > 3)) {
+        out->kind = abl_G.NEXT_KIND[in->kind];
+    }
+}
+
+struct abl_kargs_mix {
+    abl_globals G;
+    long n;
+    const int *visit;
+    abl_cols_Cell in, out;
+    abl_near_view NB;
+    uint8_t *removed;
+    uint8_t *child_flag;
+    void *child_cols[ABL_MAX_MEMBERS];
+    uint64_t seed;
+    long timestep;
+    int step_index;
+    uint32_t skip_store;
+};
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_mix(const __grid_constant__ abl_kargs_mix A) {
+    int abl_j;
+    {
+        const abl_globals &abl_G = A.G;
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
+        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.reach);
+        };
+        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = A.child_cols;
+    abl_K.near_col = abl_j;
+    Cell abl_in, abl_out;
+    abl_in.pos = A.in.pos[abl_i];
+    abl_in.kind = A.in.kind[abl_i];
+    abl_in.score = A.in.score[abl_i];
+    abl_out.kind = A.out.kind[abl_i];
+    mix(A.G, A.NB, abl_K, &abl_in, &abl_out);
+    A.out.kind[abl_i] = abl_out.kind;
+    A.out.score[abl_i] = abl_out.score;
+}
+static int abl_launch_mix(const abl_step_launch *L, cudaStream_t abl_stream) {
+    abl_kargs_mix A;
+    A.G = *(const abl_globals *) L->globals;
+    A.n = L->n;
+    A.visit = L->visit_order;
+    A.in.pos = (float2 *) L->in_cols[0];
+    A.out.pos = (float2 *) L->out_cols[0];
+    A.in.kind = (int *) L->in_cols[1];
+    A.out.kind = (int *) L->out_cols[1];
+    A.in.score = (double *) L->in_cols[2];
+    A.out.score = (double *) L->out_cols[2];
+    A.NB = L->near;
+    A.removed = L->removed;
+    A.child_flag = L->child_flag;
+    for (int k = 0; k < ABL_MAX_MEMBERS; k++) A.child_cols[k] = L->child_cols[k];
+    A.seed = L->seed;
+    A.timestep = L->timestep;
+    A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (A.n + abl_block - 1) / abl_block;
+    abl_kernel_mix<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_mix(const __grid_constant__ abl_ens_launch A) {
+    int abl_j;
+    {
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
+        const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
+        const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
+        const abl_near_view &abl_V1 = A.views[abl_r1];
+        const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.reach);
+        };
+        abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    abl_K.near_col = abl_j;
+    Cell abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.kind = ((const int *) A.in_cols[1])[abl_i];
+    abl_in.score = ((const double *) A.in_cols[2])[abl_i];
+    abl_out.kind = ((const int *) A.out_cols[1])[abl_i];
+    mix(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((int *) A.out_cols[1])[abl_i] = abl_out.kind;
+    ((double *) A.out_cols[2])[abl_i] = abl_out.score;
+}
+static int abl_launch_ens_mix(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_mix<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
+static double abl_radius_mix(const void *abl_gp) {
+    const abl_globals &abl_G = *(const abl_globals *) abl_gp;
+    abl::rng abl_R;
+    (void) abl_G; (void) abl_R;
+    return (double) (abl_G.reach);
+}
+
+
+static const abl_member_desc abl_members_Cell[] = {
+    {"pos", ABL_T_FLOAT2, 2, 8, 1},
+    {"kind", ABL_T_INT, 1, 4, 0},
+    {"score", ABL_T_FLOAT, 1, 8, 0},
+};
+static const abl_agent_desc abl_agents[] = {
+    {"Cell", 3, abl_members_Cell, 0, 2},
+};
+static const abl_global_desc abl_global_table[] = {
+    {"PI", ABL_T_FLOAT, offsetof(abl_globals, PI)},
+    {"num_timesteps", ABL_T_INT, offsetof(abl_globals, num_timesteps)},
+    {"num_agents", ABL_T_INT, offsetof(abl_globals, num_agents)},
+    {"W", ABL_T_FLOAT, offsetof(abl_globals, W)},
+    {"reach", ABL_T_FLOAT, offsetof(abl_globals, reach)},
+    {nullptr, 0, 0}
+};
+static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max) {
+    const abl_globals &abl_G = *(const abl_globals *) abl_gp;
+    abl::rng abl_R;
+    (void) abl_G; (void) abl_R;
+    float2 abl_lo = float2_fill(0);
+    float2 abl_hi = float2_fill(abl_G.W);
+    abl_min[0] = abl_lo.x; abl_min[1] = abl_lo.y; abl_min[2] = 0;
+    abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
+}
+static const abl_step_desc abl_steps[] = {
+    {"mix", 0, 0, 1, abl_radius_mix, 3u, 4u, abl_launch_mix, 0, -1, 0, abl_launch_ens_mix, 0, 1, 6u, 1},
+};
+static const abl_step_desc abl_steps_ordered[] = {
+    abl_steps[0],
+    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
+};
+extern const abl_model_desc abl_desc = {
+    "kinds", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 5, abl_global_table, 2, abl_env_bounds, nullptr, 0, nullptr
+};
+static void abl_check(int r, const char *what) {
+    if (r != ABL_OK) {
+        std::fprintf(stderr, "%s failed: %s\n", what, abl_strerror(r));
+        std::exit(1);
+    }
+}
+static void abl_simulate(int abl_timesteps) {
+    abl_ctx *ctx = nullptr;
+    abl_check(abl_create(&abl_desc, 0, &ctx), "abl_create");
+    abl_check(abl_set_globals(ctx, &abl_G, sizeof abl_G), "abl_set_globals");
+    {
+        size_t n = agents.agents_Cell.len;
+        const Cell *aos = (const Cell *) agents.agents_Cell.values;
+        float2 *c0 = (float2 *) std::malloc(sizeof(float2) * (n ? n : 1));
+        for (size_t i = 0; i < n; i++) c0[i] = aos[i].pos;
+        int *c1 = (int *) std::malloc(sizeof(int) * (n ? n : 1));
+        for (size_t i = 0; i < n; i++) c1[i] = aos[i].kind;
+        double *c2 = (double *) std::malloc(sizeof(double) * (n ? n : 1));
+        for (size_t i = 0; i < n; i++) c2[i] = aos[i].score;
+        const void *cols[] = {c0, c1, c2};
+        abl_check(abl_upload(ctx, 0, cols, n), "abl_upload");
+        std::free(c0);
+        std::free(c1);
+        std::free(c2);
+    }
+    abl_check(abl_run(ctx, abl_timesteps), "abl_run");
+    {
+        size_t n = 0;
+        abl_check(abl_count(ctx, 0, &n), "abl_count");
+        float2 *c0 = (float2 *) std::malloc(sizeof(float2) * (n ? n : 1));
+        int *c1 = (int *) std::malloc(sizeof(int) * (n ? n : 1));
+        double *c2 = (double *) std::malloc(sizeof(double) * (n ? n : 1));
+        void *cols[] = {c0, c1, c2};
+        size_t cap = n;
+        abl_check(abl_download(ctx, 0, cols, &cap), "abl_download");
+        dyn_array_clean(&agents.agents_Cell);
+        agents.agents_Cell = dyn_array_create_fixed(sizeof(Cell), n);
+        Cell *aos = (Cell *) agents.agents_Cell.values;
+        for (size_t i = 0; i < n; i++) {
+            aos[i].pos = c0[i];
+            aos[i].kind = c1[i];
+            aos[i].score = c2[i];
+        }
+        std::free(c0);
+        std::free(c1);
+        std::free(c2);
+    }
+    size_t abl_log_len = 0;
+    abl_log_text(ctx, nullptr, 0, &abl_log_len);
+    if (abl_log_len > 0) {
+        char *abl_log = (char *) std::malloc(abl_log_len + 1);
+        abl_log_text(ctx, abl_log, abl_log_len + 1, nullptr);
+        FILE *abl_f = std::fopen("log.csv", "w");
+        if (abl_f) { std::fputs(abl_log, abl_f); std::fclose(abl_f); }
+        std::free(abl_log);
+    }
+    abl_destroy(ctx);
+}
+static int abl_main() {
+    for (int i = 0, _var0 = abl_G.num_agents; i < _var0; ++i) {
+        *DYN_ARRAY_PLACE(&agents.agents_Cell, Cell) = ([&]() { Cell abl_a; abl_a.pos = random_4(abl_G, abl_R, float2_fill(abl_G.W)); abl_a.kind = abl_random_int(abl_R, 0, 2); abl_a.score = 0.0; return abl_a; }());
+    }
+    abl_simulate(abl_G.num_timesteps);
+    save(&agents, agents_info, "cells.json", SAVE_JSON);
+    return 0;
+}
+
+}  // namespace abl_model_kinds
+
+extern "C" const abl_model_desc *abl_model_desc_kinds(void) {
+    return &abl_model_kinds::abl_desc;
+}
+
+#ifdef ABL_STANDALONE_MAIN
+extern "C" const abl_model_desc *const abl_builtin_models[] = {
+    &abl_model_kinds::abl_desc, nullptr};
+int main() { return abl_model_kinds::abl_main(); }
+#endif

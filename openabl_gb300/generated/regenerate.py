@@ -37,6 +37,8 @@ MODELS = {
     "sugarscape": ("sugarscape.abl", {}),
     # main()'s add() loop as a kernel (-C cuda.device_init=true)
     "boids2d_devinit": ("boids2d.abl", {"cuda.device_init": "true"}),
+    # a model of this repository's tests: constant arrays
+    "kinds": ("tests/models/kinds.abl", {}),
 }
 
 # configuration name -> (model, -P params)
@@ -76,8 +78,8 @@ CONFIGS = {
 def run_compiler(model, params):
     example, config = MODELS[model]
     out = tempfile.mkdtemp(prefix="abl_gen_")
-    cmd = [COMPILER, "-A", os.path.join(REF, "asset"), "-i",
-           os.path.join(REF, "examples", example), "-o", out, "-b", "cuda",
+    src = os.path.join(REPO, example) if "/" in example else os.path.join(REF, "examples", example)
+    cmd = [COMPILER, "-A", os.path.join(REF, "asset"), "-i", src, "-o", out, "-b", "cuda",
            "-C", f"cuda.model={model}"]
     for k, v in config.items():
         cmd += ["-C", f"{k}={v}"]

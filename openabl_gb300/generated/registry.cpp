@@ -14,6 +14,7 @@ const abl_model_desc *abl_model_desc_predator_prey_float(void);
 const abl_model_desc *abl_model_desc_boids3d(void);
 const abl_model_desc *abl_model_desc_sugarscape(void);
 const abl_model_desc *abl_model_desc_boids2d_devinit(void);
+const abl_model_desc *abl_model_desc_kinds(void);
 extern const abl_model_desc *const abl_builtin_models[];
 const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_circle(),
@@ -28,5 +29,6 @@ const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_boids3d(),
     abl_model_desc_sugarscape(),
     abl_model_desc_boids2d_devinit(),
+    abl_model_desc_kinds(),
     nullptr};
 }

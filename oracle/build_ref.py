@@ -49,7 +49,17 @@ PROGRAMS = {
     "game_of_life": ("game_of_life", {}),
     "boids2d_float": ("boids2d", {"use_float": "true"}),
     "boids3d": ("boids", {}),
+    # a model of this repository's tests (constant arrays, a member written
+    # on one branch only)
+    "kinds": ("tests/models/kinds", {}),
 }
+
+
+def model_path(example):
+    """An example of the reference tree, or a model path within this repository."""
+    if "/" in example:
+        return os.path.join(REPO, example + ".abl")
+    return os.path.join(REF, "examples", example + ".abl")
 
 
 def build_compiler():
@@ -99,8 +109,8 @@ def build_program(model):
     example, config = PROGRAMS[model]
     d = os.path.join(OUT, "prog_" + model)
     os.makedirs(d, exist_ok=True)
-    cmd = [COMPILER, "-A", os.path.join(REF, "asset"), "-i",
-           os.path.join(REF, "examples", example + ".abl"), "-o", d, "-b", "c"]
+    cmd = [COMPILER, "-A", os.path.join(REF, "asset"), "-i", model_path(example), "-o", d,
+           "-b", "c"]
     for k, v in config.items():
         cmd += ["-C", f"{k}={v}"]
     subprocess.check_call(cmd)

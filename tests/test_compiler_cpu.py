@@ -79,7 +79,8 @@ def test_example_generates_or_is_refused(compiler, example, tmp_path):
 
 
 def test_unsupported_feature_exits_with_backend_error(compiler, tmp_path):
-    # keratinocyte declares constant arrays, which the cuda backend refuses.
+    # keratinocyte's near() radius is a variable of the step function, which the
+    # cuda backend refuses (a grid's cell size must not depend on the agent).
     r = subprocess.run([compiler, "-A", os.path.join(REF, "asset"), "-i",
                         os.path.join(REF, "examples", "keratinocyte.abl"), "-o", str(tmp_path),
                         "-b", "cuda"], capture_output=True, text=True)
