@@ -814,8 +814,26 @@ void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
       const AST::AgentMember &m = *(*nearAgent->members)[k];
       if (decl.accessedMembers.count(m.name) || m.isPosition) info.nearMembers |= 1u << k;
     }
-    // The radius must not depend on the agent: it sizes the grid search.
-    Collector rc = collect(*const_cast<AST::Expression *>(&loop->getNearRadius()));
+    // The radius must not depend on the agent: it sizes the grid search.  A
+    // step-local variable holding a value of globals (`float radius = 125;`
+    // in keratinocyte.abl) stands for its initialiser.
+    if (auto *rv = dynamic_cast<const AST::VarExpression *>(&loop->getNearRadius())) {
+      if (!isGlobal(*rv->var)) {
+        for (const AST::StatementPtr &st : *decl.stmts) {
+          auto *d = dynamic_cast<const AST::VarDeclarationStatement *>(&*st);
+          if (d && d->var->id == rv->var->id && d->initializer) info.radiusLocal = d;
+        }
+        auto assigned = [&](const AST::Expression &left) {
+          const AST::VarExpression *root = targetRoot(left);
+          return root && root->var->id == rv->var->id;
+        };
+        for (auto *a : c.assigns) if (assigned(*a->left)) info.radiusLocal = nullptr;
+        for (auto *a : c.assignOps) if (assigned(*a->left)) info.radiusLocal = nullptr;
+      }
+    }
+    Collector rc = collect(info.radiusLocal
+                               ? *const_cast<AST::Expression *>(&*info.radiusLocal->initializer)
+                               : *const_cast<AST::Expression *>(&loop->getNearRadius()));
     for (auto *v : rc.varExprs) {
       if (!isGlobal(*v->var)) {
         throw BackendError("The cuda backend needs a near() radius that does not depend on "
@@ -920,8 +938,21 @@ void CudaPrinter::printPresortPhase(const StepInfo &info, const std::string &vie
         << "auto abl_x0 = [&](int abl_s) -> bool {" << indent << nl
         << "const " << pt << " abl_p = ((const " << pt << " *) " << view << ".cols[" << posIdx
         << "])[abl_s];" << nl << "return !(" << (is3 ? "dist_float3" : "dist_float2")
-        << "(abl_p, abl_p1) > " << loop.getNearRadius() << ");" << outdent << nl << "};" << nl
+        << "(abl_p, abl_p1) > ";
+  printNearRadius(info);
+  *this << ");" << outdent << nl << "};" << nl
         << "abl_j = abl::presort_block<" << dim << ">(" << view << ", abl_has, abl_q0, abl_x0);";
+}
+
+// The near radius outside the step body (phase one of a presorted kernel,
+// the host's radius function): a step-local radius variable is replaced by
+// its initialiser converted to the variable's type.
+void CudaPrinter::printNearRadius(const StepInfo &info) {
+  if (info.radiusLocal) {
+    *this << "((" << *info.radiusLocal->type << ") (" << *info.radiusLocal->initializer << "))";
+  } else {
+    *this << info.nearLoop->getNearRadius();
+  }
 }
 
 void CudaPrinter::printKernel(const StepInfo &info) {
@@ -1088,7 +1119,9 @@ void CudaPrinter::printKernel(const StepInfo &info) {
     *this << "static double abl_radius_" << name << "(const void *abl_gp) {" << indent << nl
           << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl
           << "abl::rng abl_R;" << nl << "(void) abl_G; (void) abl_R;" << nl
-          << "return (double) (" << info.nearLoop->getNearRadius() << ");" << outdent << nl
+          << "return (double) (";
+    printNearRadius(info);
+    *this << ");" << outdent << nl
           << "}" << nl;
   }
 }

@@ -95,6 +95,9 @@ private:
     unsigned outChanged = 0;   // members written with anything but `out.m = in.m`
     bool nearCacheable = false;  // one near loop, centred on the step's own agent
     const AST::ForStatement *nearLoop = nullptr;
+    // The near radius names a step-local variable declared at the top of the
+    // step with an initialiser of globals and never assigned: its value.
+    const AST::VarDeclarationStatement *radiusLocal = nullptr;
     bool usesRemove = false;
     int addType = -1;
     bool usesRng = false;
@@ -110,6 +113,7 @@ private:
   void printGlobals();
   void printStepFunction(const AST::FunctionDeclaration &decl);
   void printKernel(const StepInfo &info);
+  void printNearRadius(const StepInfo &info);
   void printPresortPhase(const StepInfo &info, const std::string &view, const std::string &pos);
   void printDescriptor();
   void printHostSimulate();

@@ -15,6 +15,9 @@ const abl_model_desc *abl_model_desc_boids3d(void);
 const abl_model_desc *abl_model_desc_sugarscape(void);
 const abl_model_desc *abl_model_desc_boids2d_devinit(void);
 const abl_model_desc *abl_model_desc_kinds(void);
+const abl_model_desc *abl_model_desc_ants(void);
+const abl_model_desc *abl_model_desc_boids2d_flockers(void);
+const abl_model_desc *abl_model_desc_keratinocyte(void);
 extern const abl_model_desc *const abl_builtin_models[];
 const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_circle(),
@@ -30,5 +33,8 @@ const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_sugarscape(),
     abl_model_desc_boids2d_devinit(),
     abl_model_desc_kinds(),
+    abl_model_desc_ants(),
+    abl_model_desc_boids2d_flockers(),
+    abl_model_desc_keratinocyte(),
     nullptr};
 }

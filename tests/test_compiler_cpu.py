@@ -79,12 +79,13 @@ def test_example_generates_or_is_refused(compiler, example, tmp_path):
 
 
 def test_unsupported_feature_exits_with_backend_error(compiler, tmp_path):
-    # keratinocyte's near() radius is a variable of the step function, which the
-    # cuda backend refuses (a grid's cell size must not depend on the agent).
+    # A near() radius read from the agent: no single cell size serves the
+    # loop, so the cuda backend refuses the model (exit 2, main.cpp:270-274).
     r = subprocess.run([compiler, "-A", os.path.join(REF, "asset"), "-i",
-                        os.path.join(REF, "examples", "keratinocyte.abl"), "-o", str(tmp_path),
-                        "-b", "cuda"], capture_output=True, text=True)
+                        os.path.join(REPO, "tests", "models", "agent_radius.abl"), "-o",
+                        str(tmp_path), "-b", "cuda"], capture_output=True, text=True)
     assert r.returncode == 2
+    assert "radius" in r.stdout + r.stderr
 
 
 @pytest.mark.parametrize("example,accepted", [("boids2d", True), ("predator_prey", True),
