@@ -647,11 +647,17 @@ struct StepState {
   // float positions by index.  Built for binning `nc_bin` of the step's grid
   // (-1: none); nc_off null with nc_bin set means they did not fit.
   int *nc_off = nullptr;
-  void *nc_list = nullptr;
+  void *nc_list = nullptr;  // nc_wide or nc_short
   bool nc_narrow = false;
   float *nc_posf = nullptr;
   long nc_bin = -1;
   double nc_radius = 0.0;
+  // Buffers kept from one build to the next (a rebuild after an upload
+  // reuses them, so graphs captured earlier stay valid).
+  int *nc_count = nullptr, *nc_span = nullptr, *nc_wide = nullptr;
+  short *nc_short = nullptr;
+  ScanPlan nc_scan;
+  long nc_n = 0, nc_wide_cap = 0, nc_short_cap = 0;
   std::vector<void *> nc_allocs;
 };
 
@@ -829,6 +835,8 @@ void free_bins(abl_ctx *ctx, TypeState &t) {
 // (2D) or ~27 (3D) cells' worth of its radius, whatever the environment
 // granularity (src/AnalysisVisitor.cpp:1378-1399, which only partitions
 // space and does not change results) -- and allocates the binning buffers.
+void nc_free_all(abl_ctx *ctx, StepState &st);
+
 int prepare(abl_ctx *ctx) {
   const abl_model_desc *m = ctx->model;
   const void *G = ctx->globals.data();
@@ -957,8 +965,7 @@ int prepare(abl_ctx *ctx) {
   // capacity of the step's own type (one flag / one child per agent).
   for (void *p : ctx->step_allocs) dev_free(ctx, p);
   ctx->step_allocs.clear();
-  for (StepState &st : ctx->step_state)
-    for (void *p : st.nc_allocs) dev_free(ctx, p);
+  for (StepState &st : ctx->step_state) nc_free_all(ctx, st);
   ctx->step_state.assign(m->num_steps, StepState());
   for (int k = 0; k < m->num_steps; k++) {
     const abl_step_desc &sd = m->steps[k];
@@ -1375,12 +1382,20 @@ __device__ __forceinline__ bool nc_within(const Real *pos, long i, long j, doubl
 // agent indices from list[off[i]], ascending (the order the reference visits
 // them in), the largest |neighbour - i| folded into *span, and agent i's
 // float position (as the grid's slot-ordered copy rounds it) into posf.
+// Candidates are prefiltered as the step kernels do: the FP32 distance of the
+// float copies (`slot_posf`, slot order) outside the error band of the radius
+// decides; inside it the reference test does.
 template <typename Real, int DIM>
 __global__ void k_nc_lists(const Real *pos, long n, const int *cell_of, const int *cell_start,
-                           const int *order, int nx, int ny, int nz, int R, double radius,
+                           const int *order, const float *slot_posf, const float *amax,
+                           int nx, int ny, int nz, int R, double radius,
                            int *count, const int *off, int *list, int *span, float *posf) {
   const long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const abl::band bd = abl::make_band(radius, *amax, DIM);
+  float pf[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; d++) pf[d] = (float) pos[DIM * i + d];
   const int l = cell_of[i];
   const int nxy = nx * ny;
   const int c2 = l / nxy, c1 = (l - c2 * nxy) / nx, c0 = l - c2 * nxy - c1 * nx;
@@ -1394,8 +1409,15 @@ __global__ void k_nc_lists(const Real *pos, long n, const int *cell_of, const in
       const int base = (z * ny + y) * nx;
       const int e = cell_start[base + x1 + 1];
       for (int s = cell_start[base + x0]; s < e; s++) {
+        float d2 = 0.0f;
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+          const float dd = slot_posf[DIM * s + d] - pf[d];
+          d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
+        }
+        if (d2 > bd.hi) continue;
         const int j = order[s];
-        if (!nc_within<Real, DIM>(pos, i, j, radius)) continue;
+        if (!(d2 < bd.lo) && !nc_within<Real, DIM>(pos, i, j, radius)) continue;
         if (out) out[k] = j;
         k++;
       }
@@ -1436,12 +1458,12 @@ void launch_nc_lists(abl_ctx *ctx, const TypeState &g, double radius, int *count
   const long nb = blocks_for(g.n, B);
   if (g.d->dim == 2) {
     k_nc_lists<Real, 2><<<nb, B, 0, ctx->stream>>>(pos, g.n, g.cell_of, g.cell_start, g.order,
-                                                   g.nx, g.ny, g.nz, g.R, radius, count, off,
-                                                   list, span, posf);
+                                                   g.posf, g.amax, g.nx, g.ny, g.nz, g.R,
+                                                   radius, count, off, list, span, posf);
   } else {
     k_nc_lists<Real, 3><<<nb, B, 0, ctx->stream>>>(pos, g.n, g.cell_of, g.cell_start, g.order,
-                                                   g.nx, g.ny, g.nz, g.R, radius, count, off,
-                                                   list, span, posf);
+                                                   g.posf, g.amax, g.nx, g.ny, g.nz, g.R,
+                                                   radius, count, off, list, span, posf);
   }
   ctx->launches++;
 }
@@ -1458,74 +1480,100 @@ void nc_release(abl_ctx *ctx, StepState &st, void *p) {
                      st.nc_allocs.end());
 }
 
+void nc_free_all(abl_ctx *ctx, StepState &st) {
+  for (void *p : st.nc_allocs) dev_free(ctx, p);
+  st.nc_allocs.clear();
+  st.nc_scan.levels.clear();
+  st.nc_off = st.nc_count = st.nc_span = st.nc_wide = nullptr;
+  st.nc_short = nullptr;
+  st.nc_posf = nullptr;
+  st.nc_list = nullptr;
+  st.nc_n = st.nc_wide_cap = st.nc_short_cap = 0;
+}
+
 // Brings step k's kept lists up to date with grid g and returns whether they
 // can be read.  Building needs host reads (the total, the index span), so a
-// stream capture only reads lists that are already current.
+// stream capture only reads lists that are already current.  A rebuild
+// reuses the buffers it fits in; graphs captured before are dropped when the
+// buffers the step kernels read move, or when the lists are given up.
 int near_cache_ready(abl_ctx *ctx, int k, const TypeState &g, double radius, bool &ready) {
   ready = false;
   StepState &st = ctx->step_state[k];
   if (!g.dirty && st.nc_bin == g.bin_id && st.nc_radius == radius) {
-    ready = st.nc_off != nullptr;
+    ready = st.nc_list != nullptr;
     return ABL_OK;
   }
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(ctx->stream, &cs);
   if (cs != cudaStreamCaptureStatusNone || g.dirty) return ABL_OK;
-  // Graphs captured earlier may read the lists about to be replaced.
-  drop_graph(ctx);
-  for (void *p : st.nc_allocs) dev_free(ctx, p);
-  st.nc_allocs.clear();
-  st.nc_off = nullptr;
-  st.nc_list = nullptr;
-  st.nc_posf = nullptr;
   st.nc_bin = g.bin_id;
   st.nc_radius = radius;
-  if (g.n <= 0) return ABL_OK;
-  auto *own = &st.nc_allocs;
-  int *count = nullptr, *span = nullptr, *list = nullptr;
-  ScanPlan plan;
+  const void *prev_list = st.nc_list;
+  st.nc_list = nullptr;
   auto give_up = [&]() {
-    for (void *p : st.nc_allocs) dev_free(ctx, p);
-    st.nc_allocs.clear();
-    st.nc_off = nullptr;
-    return ABL_OK;  // no room: the step searches the grid
+    nc_free_all(ctx, st);
+    drop_graph(ctx);
+    return ABL_OK;  // no room, or lists too long: the step searches the grid
   };
-  if (dev_alloc_t(ctx, &count, g.n, own) != ABL_OK
-      || dev_alloc_t(ctx, &st.nc_off, g.n + 1, own) != ABL_OK
-      || dev_alloc_t(ctx, &span, 1, own) != ABL_OK
-      || dev_alloc_t(ctx, &st.nc_posf, g.n * g.d->dim, own) != ABL_OK
-      || scan_plan(ctx, plan, g.n, own) != ABL_OK)
-    return give_up();
+  if (g.n <= 0) return give_up();
+  auto *own = &st.nc_allocs;
+  bool moved = false;
+  if (st.nc_n != g.n) {
+    nc_free_all(ctx, st);
+    moved = true;
+    if (dev_alloc_t(ctx, &st.nc_count, g.n, own) != ABL_OK
+        || dev_alloc_t(ctx, &st.nc_off, g.n + 1, own) != ABL_OK
+        || dev_alloc_t(ctx, &st.nc_span, 1, own) != ABL_OK
+        || dev_alloc_t(ctx, &st.nc_posf, g.n * g.d->dim, own) != ABL_OK
+        || scan_plan(ctx, st.nc_scan, g.n, own) != ABL_OK)
+      return give_up();
+    st.nc_n = g.n;
+  }
   const bool dbl = pos_is_double(g);
-  if (dbl) launch_nc_lists<double>(ctx, g, radius, count, nullptr, nullptr, nullptr, nullptr);
-  else launch_nc_lists<float>(ctx, g, radius, count, nullptr, nullptr, nullptr, nullptr);
-  scan_run(ctx, plan, count, st.nc_off);
+  if (dbl) launch_nc_lists<double>(ctx, g, radius, st.nc_count, nullptr, nullptr, nullptr, nullptr);
+  else launch_nc_lists<float>(ctx, g, radius, st.nc_count, nullptr, nullptr, nullptr, nullptr);
+  scan_run(ctx, st.nc_scan, st.nc_count, st.nc_off);
   int total = 0;
   ABL_CUDA_TRY(cudaMemcpyAsync(&total, st.nc_off + g.n, sizeof(int), cudaMemcpyDeviceToHost,
                                ctx->stream));
   ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   // Lists far longer than a handful of cells' worth are not worth keeping.
-  if (total < 0 || (long) total > 64 * g.n + 4096
-      || dev_alloc_t(ctx, &list, std::max(total, 1), own) != ABL_OK)
-    return give_up();
-  ABL_CUDA_TRY(cudaMemsetAsync(span, 0, sizeof(int), ctx->stream));
-  if (dbl) launch_nc_lists<double>(ctx, g, radius, nullptr, st.nc_off, list, span, st.nc_posf);
-  else launch_nc_lists<float>(ctx, g, radius, nullptr, st.nc_off, list, span, st.nc_posf);
-  int far = 0;
-  ABL_CUDA_TRY(cudaMemcpyAsync(&far, span, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  st.nc_list = list;
-  st.nc_narrow = false;
-  short *narrow = nullptr;
-  if (far <= 32767 && dev_alloc_t(ctx, &narrow, std::max(total, 1), own) == ABL_OK) {
-    k_nc_narrow<<<blocks_for(g.n, 256), 256, 0, ctx->stream>>>(g.n, st.nc_off, list, narrow);
-    ctx->launches++;
-    ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    nc_release(ctx, st, list);
-    st.nc_list = narrow;
-    st.nc_narrow = true;
+  if (total < 0 || (long) total > 64 * g.n + 4096) return give_up();
+  if (st.nc_wide_cap < std::max(total, 1)) {
+    if (st.nc_wide) nc_release(ctx, st, st.nc_wide);
+    st.nc_wide = nullptr;
+    st.nc_wide_cap = 0;
+    if (dev_alloc_t(ctx, &st.nc_wide, std::max(total, 1), own) != ABL_OK) return give_up();
+    st.nc_wide_cap = std::max(total, 1);
   }
-  nc_release(ctx, st, count);
+  ABL_CUDA_TRY(cudaMemsetAsync(st.nc_span, 0, sizeof(int), ctx->stream));
+  if (dbl) launch_nc_lists<double>(ctx, g, radius, nullptr, st.nc_off, st.nc_wide, st.nc_span,
+                                   st.nc_posf);
+  else launch_nc_lists<float>(ctx, g, radius, nullptr, st.nc_off, st.nc_wide, st.nc_span,
+                              st.nc_posf);
+  int far = 0;
+  ABL_CUDA_TRY(cudaMemcpyAsync(&far, st.nc_span, sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  st.nc_list = st.nc_wide;
+  st.nc_narrow = false;
+  if (far <= 32767) {
+    if (st.nc_short_cap < std::max(total, 1)) {
+      if (st.nc_short) nc_release(ctx, st, st.nc_short);
+      st.nc_short = nullptr;
+      st.nc_short_cap = 0;
+      if (dev_alloc_t(ctx, &st.nc_short, std::max(total, 1), own) == ABL_OK)
+        st.nc_short_cap = std::max(total, 1);
+    }
+    if (st.nc_short) {
+      k_nc_narrow<<<blocks_for(g.n, 256), 256, 0, ctx->stream>>>(g.n, st.nc_off, st.nc_wide,
+                                                                   st.nc_short);
+      ctx->launches++;
+      st.nc_list = st.nc_short;
+      st.nc_narrow = true;
+    }
+  }
+  if (moved || st.nc_list != prev_list) drop_graph(ctx);
   ready = true;
   return ABL_OK;
 }
@@ -1933,11 +1981,12 @@ static int finish_upload(abl_ctx *ctx, int type_id, bool resized) {
   }
   t.uploaded = true;
   mark_dirty(ctx, type_id);
-  // Graphs reading kept neighbour lists of this type would read stale ones.
+  // Kept neighbour lists of this type are rebuilt (in place) by an eager
+  // timestep before graphs that read them replay again.
   for (int k = 0; k < ctx->model->num_steps && !resized; k++) {
     if (ctx->model->steps[k].near_type == type_id && k < (int) ctx->step_state.size()
-        && ctx->step_state[k].nc_off)
-      drop_graph(ctx);
+        && ctx->step_state[k].nc_list)
+      ctx->warm = false;
   }
   if (resized) {
     ctx->prepared = false;
