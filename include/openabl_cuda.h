@@ -166,6 +166,14 @@ int abl_set_near_mode(abl_ctx *ctx, int mode);
  * upload, read at every timestep (default on).  Results are identical either
  * way. */
 int abl_set_near_cache(abl_ctx *ctx, int enable);
+/* Sequential random numbers: random() inside step functions continues the
+ * reference's single xorshift128+ stream (asset/c/libabl.c:8-39) from
+ * `state`, in the order the reference program draws on one thread: step
+ * functions in order, agents in index order.  Steps that draw run one agent
+ * per launch, so this is a parity mode, not a fast one.  NULL turns it off
+ * (counter-based streams).  abl_get_serial_random reads the state back. */
+int abl_set_serial_random(abl_ctx *ctx, const uint64_t *state);
+int abl_get_serial_random(abl_ctx *ctx, uint64_t *state);
 int abl_destroy(abl_ctx *ctx);
 const char *abl_strerror(int code);
 

@@ -966,8 +966,8 @@ void CudaPrinter::printKernel(const StepInfo &info) {
         << "abl_cols_" << T << " in, out;" << nl << "abl_near_view NB;" << nl
         << "uint8_t *removed;" << nl << "uint8_t *child_flag;" << nl
         << "void *child_cols[ABL_MAX_MEMBERS];" << nl << "uint64_t seed;" << nl
-        << "long timestep;" << nl << "int step_index;" << nl << "uint32_t skip_store;" << outdent
-        << nl << "};"
+        << "long timestep;" << nl << "int step_index;" << nl << "uint32_t skip_store;" << nl
+        << "unsigned long long *serial_rng;" << outdent << nl << "};"
         << nl << "__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_" << name
         << "(const __grid_constant__ abl_kargs_" << name << " A) {" << indent << nl;
   if (info.presorted) {
@@ -987,6 +987,7 @@ void CudaPrinter::printKernel(const StepInfo &info) {
         << "const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;" << nl
         << "abl::step_ctx abl_K;" << nl
         << "abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);"
+        << nl << "abl_K.R.xs = A.serial_rng;"
         << nl << "abl_K.self = abl_i;" << nl << "abl_K.removed = 0;" << nl << "abl_K.added = 0;"
         << nl << "abl_K.child_cols = A.child_cols;" << nl
         << "abl_K.near_col = " << (info.presorted ? "abl_j" : "-1") << ";" << nl
@@ -1038,6 +1039,7 @@ void CudaPrinter::printKernel(const StepInfo &info) {
         << "for (int k = 0; k < ABL_MAX_MEMBERS; k++) A.child_cols[k] = L->child_cols[k];" << nl
         << "A.seed = L->seed;" << nl << "A.timestep = L->timestep;" << nl
         << "A.step_index = L->step_index;" << nl << "A.skip_store = L->skip_store;" << nl
+        << "A.serial_rng = L->serial_rng;" << nl
         << "const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : "
            "ABL_STEP_BLOCK;" << nl
         << "const long abl_grid = (A.n + abl_block - 1) / abl_block;" << nl
@@ -1301,7 +1303,16 @@ void CudaPrinter::printHostSimulate() {
     for (size_t k = 0; k < a.members->size(); k++) *this << nl << "std::free(c" << k << ");";
     *this << outdent << nl << "}";
   }
+  // -DABL_SERIAL_RANDOM: random() in steps continues the host's xorshift
+  // stream in agent order, as the reference program does on one thread.
+  *this << nl << "#ifdef ABL_SERIAL_RANDOM" << nl << "uint64_t abl_xs[2];" << nl
+        << "abl_host_rng_get(abl_xs);" << nl
+        << "abl_check(abl_set_serial_random(ctx, abl_xs), \"abl_set_serial_random\");" << nl
+        << "#endif";
   *this << nl << "abl_check(abl_run(ctx, abl_timesteps), \"abl_run\");";
+  *this << nl << "#ifdef ABL_SERIAL_RANDOM" << nl
+        << "abl_check(abl_get_serial_random(ctx, abl_xs), \"abl_get_serial_random\");" << nl
+        << "abl_host_rng_set(abl_xs);" << nl << "#endif";
   for (size_t ti = 0; ti < script.agents.size(); ti++) {
     const AST::AgentDeclaration &a = *script.agents[ti];
     const std::string &T = a.name;

@@ -325,6 +325,10 @@ __device__ __forceinline__ double div_int(double a, int n) {
 // draw), key (seed low, seed high).  The CPU oracle implements the same.
 struct rng {
   uint32_t k0, k1, c0, c1, c2, draw;
+  // Sequential mode (abl_set_serial_random): the reference's single
+  // xorshift128+ stream (asset/c/libabl.c:8-39), shared by the agents one
+  // thread steps in agent order.  nullptr: the counter-based stream.
+  unsigned long long *xs;
 
   __host__ __device__ void init(uint64_t seed, uint32_t agent, uint32_t step, uint64_t timestep) {
     k0 = (uint32_t) seed;
@@ -333,6 +337,17 @@ struct rng {
     c1 = step;
     c2 = (uint32_t) timestep;
     draw = 0;
+    xs = nullptr;
+  }
+
+  // xorshift128+ (Vigna): the step the reference's xorshift128plus() takes.
+  __host__ __device__ uint64_t serial_next() {
+    uint64_t a = xs[0];
+    const uint64_t b = xs[1];
+    xs[0] = b;
+    a ^= a << 23;
+    xs[1] = a ^ b ^ (a >> 17) ^ (b >> 26);
+    return xs[1] + b;
   }
 
   __host__ __device__ static void mulhilo(uint32_t a, uint32_t b, uint32_t &hi, uint32_t &lo) {
@@ -374,11 +389,27 @@ struct rng {
 
   template <typename F>
   __host__ __device__ F uniform(F lo, F hi) {
+    if (xs) {
+      // random_float: min + (F) x / (F) (UINT64_MAX / (max - min)).
+      const uint64_t x = serial_next();
+      return lo + (F) x / (F) ((F) UINT64_MAX / (hi - lo));
+    }
     F u = (F) unit();
     return lo + u * (hi - lo);
   }
 
   __host__ __device__ int uniform_int(int lo, int hi) {
+    if (xs) {
+      // random_int, with its power-of-two shortcut that omits `lo`.
+      const unsigned n = (unsigned) (hi - lo + 1);
+      if ((n & (n - 1)) == 0) return (int) (serial_next() & (n - 1));
+      const unsigned lim = 0xffffffffu - 0xffffffffu % n;
+      unsigned v;
+      do {
+        v = (unsigned) serial_next();
+      } while (v >= lim);
+      return lo + (int) (v % n);
+    }
     uint32_t x[4];
     next4(x);
     uint32_t n = (uint32_t) (hi - lo) + 1u;

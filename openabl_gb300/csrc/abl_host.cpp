@@ -44,6 +44,16 @@ void abl_host_rng_reset(void) {
   rng_state[1] = 0xbeefdeadull;
 }
 
+void abl_host_rng_get(uint64_t state[2]) {
+  state[0] = rng_state[0];
+  state[1] = rng_state[1];
+}
+
+void abl_host_rng_set(const uint64_t state[2]) {
+  rng_state[0] = state[0];
+  rng_state[1] = state[1];
+}
+
 static uint64_t rng_next(void) {
   uint64_t s1 = rng_state[0];
   const uint64_t s0 = rng_state[1];

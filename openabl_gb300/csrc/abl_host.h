@@ -43,6 +43,9 @@ double random_float_d(double min, double max);
 float random_float_f(float min, float max);
 int random_int(int min, int max);
 void abl_host_rng_reset(void);
+/* The xorshift128+ state, to hand the stream to the device and back. */
+void abl_host_rng_get(uint64_t state[2]);
+void abl_host_rng_set(const uint64_t state[2]);
 
 typedef enum {
   TYPE_END,

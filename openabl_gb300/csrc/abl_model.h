@@ -100,6 +100,8 @@ typedef struct {
   /* members the kernel need not store: the step only ever copies them from
      `in`, and the double buffer already holds the same values */
   uint32_t skip_store;
+  /* sequential random numbers: the xorshift128+ state (device), or NULL */
+  unsigned long long *serial_rng;
 } abl_step_launch;
 
 typedef int (*abl_step_launch_fn)(const abl_step_launch *launch, cudaStream_t stream);

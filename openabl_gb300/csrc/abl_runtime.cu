@@ -718,6 +718,11 @@ struct abl_ctx {
   // Step kernels skip stores of members that never change (both buffers
   // hold them since the upload).
   bool skip_stores = true;
+  // Sequential random numbers (abl_set_serial_random): the xorshift128+
+  // state on the device, and agent indices 0..n-1 for one-agent launches.
+  unsigned long long *serial_rng = nullptr;
+  int *serial_iota = nullptr;
+  long serial_iota_n = 0;
   std::vector<std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
   std::vector<double> prof_seconds;
   std::vector<long> prof_launches;
@@ -1346,6 +1351,11 @@ void type_amax(abl_ctx *ctx, TypeState &t) {
 
 void drop_graph(abl_ctx *ctx);
 
+__global__ void k_iota(int *a, long n) {
+  const long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = (int) i;
+}
+
 // ------------------------------------------------- kept neighbour lists
 //
 // When no step function moves agents of a type (and none adds or removes
@@ -1595,6 +1605,21 @@ int step_once(abl_ctx *ctx) {
     L.timestep = ctx->timestep;
     L.step_index = k;
     L.skip_store = ctx->skip_stores ? invariant_members(m, sd.agent_type) : 0;
+    // Steps that draw random numbers in sequential mode: one agent per
+    // launch, in index order.
+    const bool serial = ctx->serial_rng && sd.uses_rng && t.n > 0;
+    if (serial) {
+      L.serial_rng = ctx->serial_rng;
+      if (ctx->serial_iota_n < t.n) {
+        if (ctx->serial_iota) dev_free(ctx, ctx->serial_iota);
+        ctx->serial_iota = nullptr;
+        ctx->serial_iota_n = 0;
+        ABL_TRY(dev_alloc_t(ctx, &ctx->serial_iota, t.n));
+        k_iota<<<blocks_for(t.n, 256), 256, 0, ctx->stream>>>(ctx->serial_iota, t.n);
+        ctx->launches++;
+        ctx->serial_iota_n = t.n;
+      }
+    }
     bool changes = sd.uses_remove || sd.add_type >= 0;
     if (changes) {
       StepState &st = ctx->step_state[k];
@@ -1679,8 +1704,22 @@ int step_once(abl_ctx *ctx) {
         cudaEventCreate(&e1);
         cudaEventRecord(e0, ctx->stream);
       }
-      ABL_TRY(sd.launch(&L, ctx->stream));
-      ctx->launches++;
+      if (serial) {
+        abl_step_launch L1 = L;
+        L1.n = 1;
+        L1.block = 1;
+        L1.near.block_cap = 0;
+        L1.near.balance = 0;
+        if (sd.presorted && sd.near_type >= 0) L1.smem = abl::presort_bytes(L1.near);
+        for (long i = 0; i < t.n; i++) {
+          L1.visit_order = ctx->serial_iota + i;
+          ABL_TRY(sd.launch(&L1, ctx->stream));
+          ctx->launches++;
+        }
+      } else {
+        ABL_TRY(sd.launch(&L, ctx->stream));
+        ctx->launches++;
+      }
       if (timed) {
         cudaEventRecord(e1, ctx->stream);
         ctx->prof_pending[k].push_back({e0, e1});
@@ -2262,6 +2301,29 @@ int abl_set_near_cache(abl_ctx *ctx, int enable) {
   if (!ctx) return ABL_E_INVALID;
   ctx->near_cache = enable != 0;
   drop_graph(ctx);
+  return ABL_OK;
+}
+
+int abl_set_serial_random(abl_ctx *ctx, const uint64_t *state) {
+  if (!ctx) return ABL_E_INVALID;
+  drop_graph(ctx);
+  if (!state) {
+    if (ctx->serial_rng) dev_free(ctx, ctx->serial_rng);
+    ctx->serial_rng = nullptr;
+    return ABL_OK;
+  }
+  if (!ctx->serial_rng) ABL_TRY(dev_alloc_t(ctx, &ctx->serial_rng, 2));
+  ABL_CUDA_TRY(cudaMemcpyAsync(ctx->serial_rng, state, 2 * sizeof(uint64_t),
+                               cudaMemcpyHostToDevice, ctx->stream));
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return ABL_OK;
+}
+
+int abl_get_serial_random(abl_ctx *ctx, uint64_t *state) {
+  if (!ctx || !state || !ctx->serial_rng) return ABL_E_INVALID;
+  ABL_CUDA_TRY(cudaMemcpyAsync(state, ctx->serial_rng, 2 * sizeof(uint64_t),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return ABL_OK;
 }
 

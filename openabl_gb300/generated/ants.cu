@@ -246,6 +246,7 @@ struct abl_kargs_ant_deposit {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ant_deposit(const __grid_constant__ abl_kargs_ant_deposit A) {
     int abl_j;
@@ -267,6 +268,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -311,6 +313,7 @@ static int abl_launch_ant_deposit(const abl_step_launch *L, cudaStream_t abl_str
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_ant_deposit<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -427,6 +430,7 @@ struct abl_kargs_pheromone_deposit {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pheromone_deposit(const __grid_constant__ abl_kargs_pheromone_deposit A) {
     int abl_j;
@@ -448,6 +452,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -480,6 +485,7 @@ static int abl_launch_pheromone_deposit(const abl_step_launch *L, cudaStream_t a
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pheromone_deposit<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -624,6 +630,7 @@ struct abl_kargs_ant_act {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ant_act(const __grid_constant__ abl_kargs_ant_act A) {
     int abl_j;
@@ -645,6 +652,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -692,6 +700,7 @@ static int abl_launch_ant_act(const abl_step_launch *L, cudaStream_t abl_stream)
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_ant_act<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -866,7 +875,16 @@ static void abl_simulate(int abl_timesteps) {
         std::free(c1);
         std::free(c2);
     }
+    #ifdef ABL_SERIAL_RANDOM
+    uint64_t abl_xs[2];
+    abl_host_rng_get(abl_xs);
+    abl_check(abl_set_serial_random(ctx, abl_xs), "abl_set_serial_random");
+    #endif
     abl_check(abl_run(ctx, abl_timesteps), "abl_run");
+    #ifdef ABL_SERIAL_RANDOM
+    abl_check(abl_get_serial_random(ctx, abl_xs), "abl_get_serial_random");
+    abl_host_rng_set(abl_xs);
+    #endif
     {
         size_t n = 0;
         abl_check(abl_count(ctx, 0, &n), "abl_count");

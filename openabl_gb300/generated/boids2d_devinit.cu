@@ -208,6 +208,7 @@ struct abl_kargs_update_boid {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_update_boid(const __grid_constant__ abl_kargs_update_boid A) {
     int abl_j;
@@ -229,6 +230,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -258,6 +260,7 @@ static int abl_launch_update_boid(const abl_step_launch *L, cudaStream_t abl_str
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_update_boid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -398,7 +401,16 @@ static void abl_simulate(int abl_timesteps) {
         abl_check(cudaDeviceSynchronize() == cudaSuccess ? ABL_OK : ABL_E_CUDA, "device initialisation");
         abl_check(abl_commit(ctx, 0), "abl_commit");
     }
+    #ifdef ABL_SERIAL_RANDOM
+    uint64_t abl_xs[2];
+    abl_host_rng_get(abl_xs);
+    abl_check(abl_set_serial_random(ctx, abl_xs), "abl_set_serial_random");
+    #endif
     abl_check(abl_run(ctx, abl_timesteps), "abl_run");
+    #ifdef ABL_SERIAL_RANDOM
+    abl_check(abl_get_serial_random(ctx, abl_xs), "abl_get_serial_random");
+    abl_host_rng_set(abl_xs);
+    #endif
     {
         size_t n = 0;
         abl_check(abl_count(ctx, 0, &n), "abl_count");

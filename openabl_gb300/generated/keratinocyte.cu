@@ -286,6 +286,7 @@ struct abl_kargs_cycle {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_cycle(const __grid_constant__ abl_kargs_cycle A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -293,6 +294,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -368,6 +370,7 @@ static int abl_launch_cycle(const abl_step_launch *L, cudaStream_t abl_stream) {
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_cycle<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -467,6 +470,7 @@ struct abl_kargs_differentiate {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_differentiate(const __grid_constant__ abl_kargs_differentiate A) {
     int abl_j;
@@ -488,6 +492,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -562,6 +567,7 @@ static int abl_launch_differentiate(const abl_step_launch *L, cudaStream_t abl_s
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_differentiate<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -706,6 +712,7 @@ struct abl_kargs_death_signal {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_death_signal(const __grid_constant__ abl_kargs_death_signal A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -713,6 +720,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -787,6 +795,7 @@ static int abl_launch_death_signal(const abl_step_launch *L, cudaStream_t abl_st
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_death_signal<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -951,6 +960,7 @@ struct abl_kargs_migrate {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_migrate(const __grid_constant__ abl_kargs_migrate A) {
     int abl_j;
@@ -972,6 +982,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1046,6 +1057,7 @@ static int abl_launch_migrate(const abl_step_launch *L, cudaStream_t abl_stream)
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_migrate<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1226,6 +1238,7 @@ struct abl_kargs_resolve_forces {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_resolve_forces(const __grid_constant__ abl_kargs_resolve_forces A) {
     int abl_j;
@@ -1247,6 +1260,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1321,6 +1335,7 @@ static int abl_launch_resolve_forces(const abl_step_launch *L, cudaStream_t abl_
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_resolve_forces<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1546,7 +1561,16 @@ static void abl_simulate(int abl_timesteps) {
         std::free(c11);
         std::free(c12);
     }
+    #ifdef ABL_SERIAL_RANDOM
+    uint64_t abl_xs[2];
+    abl_host_rng_get(abl_xs);
+    abl_check(abl_set_serial_random(ctx, abl_xs), "abl_set_serial_random");
+    #endif
     abl_check(abl_run(ctx, abl_timesteps), "abl_run");
+    #ifdef ABL_SERIAL_RANDOM
+    abl_check(abl_get_serial_random(ctx, abl_xs), "abl_get_serial_random");
+    abl_host_rng_set(abl_xs);
+    #endif
     {
         size_t n = 0;
         abl_check(abl_count(ctx, 0, &n), "abl_count");

@@ -260,6 +260,7 @@ struct abl_kargs_prey_avoid_pred {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_avoid_pred(const __grid_constant__ abl_kargs_prey_avoid_pred A) {
     int abl_j;
@@ -281,6 +282,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -319,6 +321,7 @@ static int abl_launch_prey_avoid_pred(const abl_step_launch *L, cudaStream_t abl
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_avoid_pred<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -449,6 +452,7 @@ struct abl_kargs_prey_flock {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_flock(const __grid_constant__ abl_kargs_prey_flock A) {
     int abl_j;
@@ -470,6 +474,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -508,6 +513,7 @@ static int abl_launch_prey_flock(const abl_step_launch *L, cudaStream_t abl_stre
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_flock<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -599,6 +605,7 @@ struct abl_kargs_prey_move {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_move(const __grid_constant__ abl_kargs_prey_move A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -606,6 +613,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -644,6 +652,7 @@ static int abl_launch_prey_move(const abl_step_launch *L, cudaStream_t abl_strea
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -734,6 +743,7 @@ struct abl_kargs_prey_eaten {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_eaten(const __grid_constant__ abl_kargs_prey_eaten A) {
     int abl_j;
@@ -755,6 +765,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -794,6 +805,7 @@ static int abl_launch_prey_eaten(const abl_step_launch *L, cudaStream_t abl_stre
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -852,6 +864,7 @@ struct abl_kargs_prey_eat_or_starve {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_eat_or_starve(const __grid_constant__ abl_kargs_prey_eat_or_starve A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -859,6 +872,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -898,6 +912,7 @@ static int abl_launch_prey_eat_or_starve(const abl_step_launch *L, cudaStream_t 
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_eat_or_starve<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -932,6 +947,7 @@ struct abl_kargs_prey_reproduction {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_prey_reproduction(const __grid_constant__ abl_kargs_prey_reproduction A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -939,6 +955,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -978,6 +995,7 @@ static int abl_launch_prey_reproduction(const abl_step_launch *L, cudaStream_t a
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_prey_reproduction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1041,6 +1059,7 @@ struct abl_kargs_pred_follow_prey {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_follow_prey(const __grid_constant__ abl_kargs_pred_follow_prey A) {
     int abl_j;
@@ -1062,6 +1081,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1100,6 +1120,7 @@ static int abl_launch_pred_follow_prey(const abl_step_launch *L, cudaStream_t ab
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_follow_prey<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1219,6 +1240,7 @@ struct abl_kargs_pred_avoid {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_avoid(const __grid_constant__ abl_kargs_pred_avoid A) {
     int abl_j;
@@ -1240,6 +1262,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1278,6 +1301,7 @@ static int abl_launch_pred_avoid(const abl_step_launch *L, cudaStream_t abl_stre
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_avoid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1371,6 +1395,7 @@ struct abl_kargs_pred_move {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_move(const __grid_constant__ abl_kargs_pred_move A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1378,6 +1403,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1416,6 +1442,7 @@ static int abl_launch_pred_move(const abl_step_launch *L, cudaStream_t abl_strea
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1500,6 +1527,7 @@ struct abl_kargs_pred_eat_or_starve {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_eat_or_starve(const __grid_constant__ abl_kargs_pred_eat_or_starve A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1507,6 +1535,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1546,6 +1575,7 @@ static int abl_launch_pred_eat_or_starve(const abl_step_launch *L, cudaStream_t 
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_eat_or_starve<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1580,6 +1610,7 @@ struct abl_kargs_pred_reproduction {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_pred_reproduction(const __grid_constant__ abl_kargs_pred_reproduction A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1587,6 +1618,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1626,6 +1658,7 @@ static int abl_launch_pred_reproduction(const abl_step_launch *L, cudaStream_t a
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_pred_reproduction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1685,6 +1718,7 @@ struct abl_kargs_grass_eaten {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_grass_eaten(const __grid_constant__ abl_kargs_grass_eaten A) {
     int abl_j;
@@ -1706,6 +1740,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1740,6 +1775,7 @@ static int abl_launch_grass_eaten(const abl_step_launch *L, cudaStream_t abl_str
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_grass_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -1823,6 +1859,7 @@ struct abl_kargs_grass_growth {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_grass_growth(const __grid_constant__ abl_kargs_grass_growth A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1830,6 +1867,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1864,6 +1902,7 @@ static int abl_launch_grass_growth(const abl_step_launch *L, cudaStream_t abl_st
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_grass_growth<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -2063,7 +2102,16 @@ static void abl_simulate(int abl_timesteps) {
         std::free(c1);
         std::free(c2);
     }
+    #ifdef ABL_SERIAL_RANDOM
+    uint64_t abl_xs[2];
+    abl_host_rng_get(abl_xs);
+    abl_check(abl_set_serial_random(ctx, abl_xs), "abl_set_serial_random");
+    #endif
     abl_check(abl_run(ctx, abl_timesteps), "abl_run");
+    #ifdef ABL_SERIAL_RANDOM
+    abl_check(abl_get_serial_random(ctx, abl_xs), "abl_get_serial_random");
+    abl_host_rng_set(abl_xs);
+    #endif
     {
         size_t n = 0;
         abl_check(abl_count(ctx, 0, &n), "abl_count");

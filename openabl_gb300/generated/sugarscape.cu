@@ -174,6 +174,7 @@ struct abl_kargs_metabolise_and_growback {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_metabolise_and_growback(const __grid_constant__ abl_kargs_metabolise_and_growback A) {
     const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -181,6 +182,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -235,6 +237,7 @@ static int abl_launch_metabolise_and_growback(const abl_step_launch *L, cudaStre
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_metabolise_and_growback<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -341,6 +344,7 @@ struct abl_kargs_movement_request {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_movement_request(const __grid_constant__ abl_kargs_movement_request A) {
     int abl_j;
@@ -362,6 +366,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -411,6 +416,7 @@ static int abl_launch_movement_request(const abl_step_launch *L, cudaStream_t ab
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_movement_request<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -544,6 +550,7 @@ struct abl_kargs_movement_response {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_movement_response(const __grid_constant__ abl_kargs_movement_response A) {
     int abl_j;
@@ -565,6 +572,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -618,6 +626,7 @@ static int abl_launch_movement_response(const abl_step_launch *L, cudaStream_t a
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_movement_response<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -741,6 +750,7 @@ struct abl_kargs_movement_transaction {
     long timestep;
     int step_index;
     uint32_t skip_store;
+    unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_movement_transaction(const __grid_constant__ abl_kargs_movement_transaction A) {
     int abl_j;
@@ -762,6 +772,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
     abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -815,6 +826,7 @@ static int abl_launch_movement_transaction(const abl_step_launch *L, cudaStream_
     A.timestep = L->timestep;
     A.step_index = L->step_index;
     A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (A.n + abl_block - 1) / abl_block;
     abl_kernel_movement_transaction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
@@ -990,7 +1002,16 @@ static void abl_simulate(int abl_timesteps) {
         std::free(c6);
         std::free(c7);
     }
+    #ifdef ABL_SERIAL_RANDOM
+    uint64_t abl_xs[2];
+    abl_host_rng_get(abl_xs);
+    abl_check(abl_set_serial_random(ctx, abl_xs), "abl_set_serial_random");
+    #endif
     abl_check(abl_run(ctx, abl_timesteps), "abl_run");
+    #ifdef ABL_SERIAL_RANDOM
+    abl_check(abl_get_serial_random(ctx, abl_xs), "abl_get_serial_random");
+    abl_host_rng_set(abl_xs);
+    #endif
     {
         size_t n = 0;
         abl_check(abl_count(ctx, 0, &n), "abl_count");

@@ -52,7 +52,14 @@ PROGRAMS = {
     # a model of this repository's tests (constant arrays, a member written
     # on one branch only)
     "kinds": ("tests/models/kinds", {}),
+    # random() inside the step: run on one OpenMP thread, so its draws come
+    # from the xorshift stream in agent order (SERIAL_RANDOM)
+    "boids2d_flockers": ("boids2d_flockers", {}),
 }
+
+# Programs whose reference run uses one thread and whose cuda build continues
+# the host stream in steps (-DABL_SERIAL_RANDOM).
+SERIAL_RANDOM = {"boids2d_flockers"}
 
 
 def model_path(example):

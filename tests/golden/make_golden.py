@@ -99,14 +99,18 @@ def main():
         os.makedirs(run_dir, exist_ok=True)
         for f in os.listdir(run_dir):
             os.remove(os.path.join(run_dir, f))
-        env = dict(os.environ, OMP_NUM_THREADS=str(os.cpu_count()))
+        serial = model in build_ref.SERIAL_RANDOM
+        threads = 1 if serial else os.cpu_count()
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads))
         subprocess.check_call([exe], cwd=run_dir, env=env, stdout=subprocess.DEVNULL)
         (out,) = os.listdir(run_dir)
         data = open(os.path.join(run_dir, out), "rb").read()
         programs[model] = {"example": example, "config": config, "file": out,
                            "bytes": len(data), "sha256": hashlib.sha256(data).hexdigest(),
+                           "serial_random": serial,
                            "source": "reference c backend program at default parameters "
-                                     "(OpenABL -b c, gcc -O2 -std=c99 -fopenmp, x86-64)"}
+                                     "(OpenABL -b c, gcc -O2 -std=c99 -fopenmp, x86-64, "
+                                     f"OMP_NUM_THREADS={'1' if serial else 'all cores'})"}
         print(model, out, len(data), "bytes")
     with open(os.path.join(HERE, "programs.json"), "w") as f:
         json.dump(programs, f, indent=1)

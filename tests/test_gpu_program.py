@@ -48,7 +48,10 @@ def test_generated_program_writes_the_reference_output(model, runtime_objects, t
     want = PROGRAMS[model]
     obj = str(tmp_path / (model + ".o"))
     exe = str(tmp_path / "main")
-    subprocess.check_call(NVCC + ["-c", os.path.join(GEN, model + ".cu"), "-o", obj])
+    # Programs drawing random numbers in steps were recorded on one thread;
+    # -DABL_SERIAL_RANDOM continues the host stream in the same order.
+    serial = ["-DABL_SERIAL_RANDOM"] if want.get("serial_random") else []
+    subprocess.check_call(NVCC + serial + ["-c", os.path.join(GEN, model + ".cu"), "-o", obj])
     subprocess.check_call(NVCC[:3] + [obj] + runtime_objects + ["-o", exe])
     run_dir = tmp_path / "run"
     run_dir.mkdir()
