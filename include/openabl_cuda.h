@@ -48,6 +48,7 @@ extern "C" {
 #define ABL_E_CAPACITY -7    /* agent capacity exceeded by runtime additions */
 #define ABL_E_NOMODEL -8     /* unknown model name */
 #define ABL_E_SCRATCH -9     /* larger than abl_step_noalloc's fixed scratch area */
+#define ABL_E_IO -10         /* a state file could not be written, read or matched */
 
 /* Member value types (match asset/c/libabl.h:181-189 type_id). */
 #define ABL_T_BOOL 1
@@ -174,6 +175,17 @@ int abl_set_near_cache(abl_ctx *ctx, int enable);
  * (counter-based streams).  abl_get_serial_random reads the state back. */
 int abl_set_serial_random(abl_ctx *ctx, const uint64_t *state);
 int abl_get_serial_random(abl_ctx *ctx, uint64_t *state);
+/* Checkpoint and resume (the reference has no resume, and its save() prints
+ * %f, which loses bits): abl_save_state writes the whole simulation state to
+ * a binary file -- globals, timestep, random-number seed and sequential
+ * state, and per agent type both buffers of every member (step functions
+ * that do not write a member leave the double buffer's older value visible,
+ * as the reference's agents_X_dbuf does).  abl_load_state restores it into a
+ * context of the same model; the resumed run then equals the uninterrupted
+ * one bit for bit.  ABL_E_IO: the file cannot be written or read, or holds
+ * another model's state. */
+int abl_save_state(abl_ctx *ctx, const char *path);
+int abl_load_state(abl_ctx *ctx, const char *path);
 int abl_destroy(abl_ctx *ctx);
 const char *abl_strerror(int code);
 

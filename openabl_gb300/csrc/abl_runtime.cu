@@ -2168,6 +2168,130 @@ int abl_download(abl_ctx *ctx, int type_id, void *const *cols, size_t *n) {
   return check_error(ctx);
 }
 
+// ------------------------------------------------- checkpoint and resume
+//
+// File layout (host byte order): "ABLSTAT1", the model's name (64 bytes),
+// the number of agent types, timestep, seed, whether the sequential random
+// stream is on and its state, the globals block; then per type its agent
+// count and, per member, its bytes per agent followed by the current
+// buffer's and the double buffer's first n agents.
+
+namespace {
+
+const char kStateMagic[8] = {'A', 'B', 'L', 'S', 'T', 'A', 'T', '1'};
+
+struct StateHeader {
+  char magic[8];
+  char model[64];
+  int32_t types;
+  int32_t serial_on;
+  int64_t timestep;
+  uint64_t seed;
+  uint64_t serial_state[2];
+  uint64_t globals_size;
+};
+
+struct FileCloser {
+  FILE *f;
+  ~FileCloser() {
+    if (f) std::fclose(f);
+  }
+};
+
+}  // namespace
+
+int abl_save_state(abl_ctx *ctx, const char *path) {
+  if (!ctx || !path) return ABL_E_INVALID;
+  ABL_TRY(ensure_ready(ctx));
+  StateHeader h;
+  std::memset(&h, 0, sizeof h);
+  std::memcpy(h.magic, kStateMagic, 8);
+  std::snprintf(h.model, sizeof h.model, "%s", ctx->model->name);
+  h.types = (int32_t) ctx->types.size();
+  h.timestep = ctx->timestep;
+  h.seed = ctx->seed;
+  h.serial_on = ctx->serial_rng ? 1 : 0;
+  if (ctx->serial_rng) ABL_TRY(abl_get_serial_random(ctx, h.serial_state));
+  h.globals_size = ctx->globals.size();
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  FileCloser fc{std::fopen(path, "wb")};
+  if (!fc.f) return ABL_E_IO;
+  bool ok = std::fwrite(&h, sizeof h, 1, fc.f) == 1
+         && std::fwrite(ctx->globals.data(), 1, ctx->globals.size(), fc.f) == ctx->globals.size();
+  std::vector<unsigned char> buf;
+  for (const TypeState &t : ctx->types) {
+    const int64_t n = t.n;
+    const int32_t members = t.d->num_members;
+    ok = ok && std::fwrite(&n, sizeof n, 1, fc.f) == 1
+            && std::fwrite(&members, sizeof members, 1, fc.f) == 1;
+    for (int k = 0; k < t.d->num_members && ok; k++) {
+      const uint64_t b = member_bytes(t.d->members[k]);
+      ok = std::fwrite(&b, sizeof b, 1, fc.f) == 1;
+      const size_t bytes = b * (size_t) n;
+      buf.resize(std::max<size_t>(bytes, 1));
+      for (int which = 0; which < 2 && ok && bytes > 0; which++) {
+        const void *src = t.cols[which == 0 ? t.cur : 1 - t.cur][k];
+        ABL_CUDA_TRY(cudaMemcpy(buf.data(), src, bytes, cudaMemcpyDeviceToHost));
+        ok = std::fwrite(buf.data(), 1, bytes, fc.f) == bytes;
+      }
+    }
+  }
+  ok = ok && std::fflush(fc.f) == 0;
+  return ok ? check_error(ctx) : ABL_E_IO;
+}
+
+int abl_load_state(abl_ctx *ctx, const char *path) {
+  if (!ctx || !path) return ABL_E_INVALID;
+  FileCloser fc{std::fopen(path, "rb")};
+  if (!fc.f) return ABL_E_IO;
+  StateHeader h;
+  if (std::fread(&h, sizeof h, 1, fc.f) != 1 || std::memcmp(h.magic, kStateMagic, 8) != 0)
+    return ABL_E_IO;
+  h.model[sizeof h.model - 1] = 0;
+  if (std::strcmp(h.model, ctx->model->name) != 0 || h.types != (int32_t) ctx->types.size()
+      || h.globals_size != ctx->globals.size())
+    return ABL_E_IO;
+  std::vector<unsigned char> globals(h.globals_size);
+  if (std::fread(globals.data(), 1, globals.size(), fc.f) != globals.size()) return ABL_E_IO;
+  ABL_TRY(abl_set_globals(ctx, globals.data(), globals.size()));
+  for (int ti = 0; ti < (int) ctx->types.size(); ti++) {
+    const abl_agent_desc &d = ctx->model->agents[ti];
+    int64_t n = 0;
+    int32_t members = 0;
+    if (std::fread(&n, sizeof n, 1, fc.f) != 1 || std::fread(&members, sizeof members, 1, fc.f) != 1
+        || members != d.num_members || n < 0 || n > INT32_MAX)
+      return ABL_E_IO;
+    std::vector<std::vector<unsigned char>> cur(members), dbuf(members);
+    std::vector<const void *> cols(members);
+    for (int k = 0; k < members; k++) {
+      uint64_t b = 0;
+      if (std::fread(&b, sizeof b, 1, fc.f) != 1 || b != member_bytes(d.members[k]))
+        return ABL_E_IO;
+      const size_t bytes = b * (size_t) n;
+      cur[k].resize(std::max<size_t>(bytes, 1));
+      dbuf[k].resize(std::max<size_t>(bytes, 1));
+      if (bytes > 0 && (std::fread(cur[k].data(), 1, bytes, fc.f) != bytes
+                        || std::fread(dbuf[k].data(), 1, bytes, fc.f) != bytes))
+        return ABL_E_IO;
+      cols[k] = cur[k].data();
+    }
+    ABL_TRY(abl_upload(ctx, ti, cols.data(), (size_t) n));
+    TypeState &t = ctx->types[ti];
+    for (int k = 0; k < members; k++) {
+      const size_t bytes = member_bytes(d.members[k]) * (size_t) n;
+      if (bytes == 0) continue;
+      ABL_CUDA_TRY(cudaMemcpyAsync(t.cols[1 - t.cur][k], dbuf[k].data(), bytes,
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    }
+    ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  }
+  ctx->timestep = h.timestep;
+  ctx->seed = h.seed;
+  ABL_TRY(abl_set_serial_random(ctx, h.serial_on ? h.serial_state : nullptr));
+  drop_graph(ctx);
+  return ABL_OK;
+}
+
 int abl_reduce(abl_ctx *ctx, int kind, int type_id, int member, void *out) {
   if (!ctx || !out || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
   TypeState &t = ctx->types[type_id];
@@ -2366,6 +2490,7 @@ const char *abl_strerror(int code) {
     case ABL_E_UNSUPPORTED: return "unsupported model feature";
     case ABL_E_CAPACITY: return "agent capacity exceeded";
     case ABL_E_NOMODEL: return "unknown model";
+    case ABL_E_IO: return "state file could not be written, read or matched to the model";
     case ABL_E_SCRATCH:
       return "problem larger than the fixed scratch area of abl_step_noalloc "
              "(see ABL_NOALLOC_MAX_AGENTS / ABL_NOALLOC_MAX_CELLS)";

@@ -291,6 +291,31 @@ class Simulation:
         _check(_load().abl_memory_used(self.ctx, ctypes.byref(b)), "abl_memory_used")
         return b.value
 
+    def set_serial_random(self, state):
+        """random() in steps continues the xorshift128+ stream `state` (two
+        uint64) in agent order, as the reference does on one thread; None
+        returns to the counter-based streams (abl_set_serial_random)."""
+        L = _load()
+        L.abl_set_serial_random.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        if state is None:
+            _check(L.abl_set_serial_random(self.ctx, None), "abl_set_serial_random")
+            return
+        arr = (ctypes.c_uint64 * 2)(*[int(v) for v in state])
+        _check(L.abl_set_serial_random(self.ctx, ctypes.cast(arr, ctypes.c_void_p)),
+               "abl_set_serial_random")
+
+    def save_state(self, path):
+        """Checkpoint: the whole state, both buffers, bit for bit (abl_save_state)."""
+        L = _load()
+        L.abl_save_state.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        _check(L.abl_save_state(self.ctx, os.fsencode(str(path))), "abl_save_state")
+
+    def load_state(self, path):
+        """Resume from a checkpoint of the same model (abl_load_state)."""
+        L = _load()
+        L.abl_load_state.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        _check(L.abl_load_state(self.ctx, os.fsencode(str(path))), "abl_load_state")
+
     def set_seed(self, seed):
         L = _load()
         L.abl_set_seed.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
