@@ -6,6 +6,7 @@
 //   use_float=true         abl_float is float (as LIBABL_USE_FLOAT for `c`)
 //   cuda.model=NAME        identifier of the model inside the runtime (default "model")
 //   cuda.device_init=true  main()'s add() loops run as kernels (CudaPrinter::findDeviceInit)
+//   cuda.seed=N            key of the counter-based random() stream in steps (default 0)
 #include "CudaBackend.hpp"
 
 #include <cctype>
@@ -83,7 +84,8 @@ void CudaBackend::generate(AST::Script &script, const BackendContext &ctx) {
     }
   }
 
-  CudaPrinter printer(script, useFloat, model, ctx.config.getBool("cuda.device_init", false));
+  CudaPrinter printer(script, useFloat, model, ctx.config.getBool("cuda.device_init", false),
+                      ctx.config.getInt("cuda.seed", 0));
   printer.print(script);
   writeToFile(ctx.outputDir + "/" + model + ".cu", printer.extractStr());
   writeToFile(ctx.outputDir + "/" + model + ".globals.json", globalsManifest(script, model));

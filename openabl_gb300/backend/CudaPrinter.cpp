@@ -1252,8 +1252,12 @@ void CudaPrinter::printHostSimulate() {
         << "std::exit(1);" << outdent << nl << "}" << outdent << nl << "}" << nl
         << "static void abl_simulate(int abl_timesteps) {" << indent << nl
         << "abl_ctx *ctx = nullptr;" << nl
-        << "abl_check(abl_create(&abl_desc, 0, &ctx), \"abl_create\");" << nl
-        << "abl_check(abl_set_globals(ctx, &abl_G, sizeof abl_G), \"abl_set_globals\");";
+        << "abl_check(abl_create(&abl_desc, 0, &ctx), \"abl_create\");" << nl;
+  if (seed) {
+    *this << "abl_check(abl_set_seed(ctx, " << std::to_string((unsigned long) seed)
+          << "ull), \"abl_set_seed\");" << nl;
+  }
+  *this << "abl_check(abl_set_globals(ctx, &abl_G, sizeof abl_G), \"abl_set_globals\");";
   for (size_t ti = 0; ti < script.agents.size() && !devInit.empty(); ti++) {
     const AST::AgentDeclaration &a = *script.agents[ti];
     const std::string &T = a.name;

@@ -29,9 +29,9 @@ struct CudaPrinter : public CPrinter {
   using CPrinter::print;
 
   CudaPrinter(AST::Script &script, bool useFloat, const std::string &modelName,
-              bool deviceInit = false)
+              bool deviceInit = false, long seed = 0)
     : CPrinter(script, useFloat), script(script), useFloat(useFloat), modelName(modelName),
-      deviceInit(deviceInit) {}
+      deviceInit(deviceInit), seed(seed) {}
 
   void print(const AST::VarExpression &) override;
   void print(const AST::CallExpression &) override;
@@ -50,6 +50,7 @@ private:
   bool useFloat;
   std::string modelName;
   bool deviceInit;
+  long seed;  // -C cuda.seed: key of random() in steps (abl_set_seed)
 
   // Device initialisation: main()'s add() loops run as kernels.
   struct DevInit {

@@ -33,6 +33,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "abl_device.cuh"
 #include "abl_model.h"
 
@@ -729,6 +731,14 @@ struct abl_ctx {
 };
 
 namespace {
+
+// A named range on the host timeline (NVTX): binning, list builds, each step
+// function's launch, compaction, uploads, downloads and reductions show up
+// as phases in profilers.  Without a tool attached it costs a call.
+struct Phase {
+  explicit Phase(const char *name) { nvtxRangePushA(name); }
+  ~Phase() { nvtxRangePop(); }
+};
 
 int dev_alloc(abl_ctx *ctx, void **p, size_t bytes, std::vector<void *> *owner = nullptr) {
   if (bytes == 0) bytes = 16;
@@ -1637,10 +1647,18 @@ int step_once(abl_ctx *ctx) {
       // Kept lists read the step's own columns: a grid that only needs its
       // slot-ordered copies refreshed is left as it is.
       bool cached = false;
-      if (nt.dirty) bin_grid(ctx, gi);
-      if (near_cache_wanted(ctx, sd))
+      if (nt.dirty) {
+        Phase ph("bin");
+        bin_grid(ctx, gi);
+      }
+      if (near_cache_wanted(ctx, sd)) {
+        Phase ph("kept lists");
         ABL_TRY(near_cache_ready(ctx, k, nt, sd.radius(ctx->globals.data()), cached));
-      if (!cached && nt.regather) bin_grid(ctx, gi);
+      }
+      if (!cached && nt.regather) {
+        Phase ph("gather");
+        bin_grid(ctx, gi);
+      }
       abl_near_view &V = L.near;
       const int depth = list_depth(sd, *nt.d, ctx->near_mode);
       V.dim = nt.d->dim;
@@ -1695,6 +1713,7 @@ int step_once(abl_ctx *ctx) {
       }
     }
     if (t.n > 0) {
+      Phase ph(sd.name);
       cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
       cudaStreamIsCapturing(ctx->stream, &cs);
       bool timed = ctx->profile && cs == cudaStreamCaptureStatusNone;
@@ -1726,6 +1745,7 @@ int step_once(abl_ctx *ctx) {
       }
     }
     if (changes) {
+      Phase ph("compact");
       bool regrow = false;
       ABL_TRY(apply_population_changes(ctx, k, regrow));
       if (regrow) ABL_TRY(prepare(ctx));
@@ -2036,6 +2056,7 @@ static int finish_upload(abl_ctx *ctx, int type_id, bool resized) {
 
 int abl_upload(abl_ctx *ctx, int type_id, const void *const *cols, size_t n) {
   if (!ctx || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
+  Phase ph("upload");
   if (n > (size_t) INT32_MAX) return ABL_E_UNSUPPORTED;
   TypeState &t = ctx->types[type_id];
   if (n > 0 && !cols) return ABL_E_INVALID;
@@ -2151,6 +2172,7 @@ int abl_count(abl_ctx *ctx, int type_id, size_t *n) {
 
 int abl_download(abl_ctx *ctx, int type_id, void *const *cols, size_t *n) {
   if (!ctx || !n || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
+  Phase ph("download");
   TypeState &t = ctx->types[type_id];
   size_t cnt = (size_t) t.n;
   if (*n < cnt) {
@@ -2294,6 +2316,7 @@ int abl_load_state(abl_ctx *ctx, const char *path) {
 
 int abl_reduce(abl_ctx *ctx, int kind, int type_id, int member, void *out) {
   if (!ctx || !out || type_id < 0 || type_id >= (int) ctx->types.size()) return ABL_E_INVALID;
+  Phase ph("reduce");
   TypeState &t = ctx->types[type_id];
   if (kind == ABL_REDUCE_COUNT) {
     *(int *) out = (int) t.n;

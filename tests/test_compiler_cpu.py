@@ -122,3 +122,14 @@ def test_committed_model_sources_are_current(compiler):
             manifest = json.load(f)
         shutil.rmtree(out)
         assert configs[name]["globals"] == manifest["globals"], name
+
+
+def test_seed_option_keys_random_in_steps(compiler, tmp_path):
+    """-C cuda.seed=N: the generated program keys random() in steps by N."""
+    r = subprocess.run([compiler, "-A", os.path.join(REF, "asset"), "-i",
+                        os.path.join(REF, "examples", "boids2d_flockers.abl"), "-o", str(tmp_path),
+                        "-b", "cuda", "-C", "cuda.model=flockers", "-C", "cuda.seed=42"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    src = (tmp_path / "flockers.cu").read_text()
+    assert 'abl_check(abl_set_seed(ctx, 42ull), "abl_set_seed");' in src
