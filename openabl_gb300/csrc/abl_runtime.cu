@@ -1113,15 +1113,36 @@ int apply_population_changes(abl_ctx *ctx, int k, bool &regrow) {
   k_flags<<<nb, B, 0, s>>>(n, sd.uses_remove ? st.removed : nullptr,
                            sd.add_type >= 0 ? st.child_flag : nullptr, st.keep, st.child);
   ctx->launches++;
-  scan_run(ctx, st.keep_scan, st.keep, st.keep_pos);
-  scan_run(ctx, st.child_scan, st.child, st.child_pos);
-  k_read_totals<<<1, 1, 0, s>>>(st.keep_pos, n, st.child_pos, n, ctx->d_pair);
+  // Only the scans a step needs: survivors when it removes, children when
+  // it adds.
+  const bool scan_keep = sd.uses_remove, scan_child = sd.add_type >= 0;
+  if (scan_keep) scan_run(ctx, st.keep_scan, st.keep, st.keep_pos);
+  if (scan_child) scan_run(ctx, st.child_scan, st.child, st.child_pos);
+  k_read_totals<<<1, 1, 0, s>>>(scan_keep ? st.keep_pos : nullptr, n,
+                                scan_child ? st.child_pos : nullptr, n, ctx->d_pair);
   ctx->launches++;
   int tot[2] = {0, 0};
   ABL_CUDA_TRY(cudaMemcpyAsync(tot, ctx->d_pair, sizeof tot, cudaMemcpyDeviceToHost, s));
   ABL_CUDA_TRY(cudaStreamSynchronize(s));
-  long survivors = tot[0], children = tot[1];
-  if (sd.uses_remove || self_add) {
+  long survivors = scan_keep ? tot[0] : n, children = scan_child ? tot[1] : 0;
+  if (!sd.uses_remove && self_add) {
+    // Nobody left: `out` becomes the current buffer as it is, and the
+    // children follow its n agents.  (The double buffer's content does not
+    // matter here: with runtime add/remove, step kernels start `out` as a
+    // copy of `in`.)
+    t.cur = 1 - t.cur;
+    if (children > 0) {
+      long need = n + children;
+      if (need > t.cap) {
+        ABL_TRY(grow_type(ctx, t, need));
+        regrow = true;
+      }
+      MoveArgs c = move_args(*t.d, st.child_cols, t.cols[t.cur]);
+      k_scatter_flagged<<<nb, B, 0, s>>>(n, st.child, st.child_pos, n, c);
+      ctx->launches++;
+      t.n = need;
+    }
+  } else if (sd.uses_remove) {
     long need = survivors + (self_add ? children : 0);
     // `out` holds the step's result; compact it into the other buffer.
     if (need > t.cap) {
