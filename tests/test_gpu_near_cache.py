@@ -97,3 +97,22 @@ def test_lists_too_long_to_keep():
              "alive": (rng.random(n) < 0.5).astype(np.uint8)}
     kept, searched = run_pair("game_of_life_64", "Cell", [state], 3)
     assert_same(kept, searched)
+
+
+def test_lists_beyond_the_budget_are_not_kept():
+    """With an HBM budget that holds the simulation but not the lists, the
+    lists are given up (no error) and the step searches the grid."""
+    model, g = o.globals_for_config("game_of_life_64")
+    state = workloads.game_of_life(64, 0.5, seed=9)
+    a = o.Simulation(model, g)
+    a.set_near_cache(0)
+    a.upload("Cell", state)
+    a.run(5)
+    used = a.memory_used()
+    want = a.download("Cell")
+    a.close()
+    b = o.Simulation(model, g, hbm_budget=used + 4096)
+    b.upload("Cell", state)
+    b.run(5)
+    assert_same(b.download("Cell"), want)
+    b.close()
