@@ -442,7 +442,7 @@ struct SepSrc {
 };
 
 constexpr int kSepMaxSrc = 7;    // source lists per target: 2R + 1 for R <= 3
-constexpr int kSepWarps = 8;     // target cells (warps) per block of k_sep_merge_large
+constexpr int kSepWarps = 8;     // target cells (warps) per block of the warp merge kernels
 constexpr int kSepThreads = 128; // target cells (threads) per block of k_sep_merge
 
 template <bool LEVEL0>
@@ -486,28 +486,17 @@ __device__ inline int sep_sources(const CellPos &P, long t, const SepSrc &S, int
   return total;
 }
 
-// One thread per target cell with R = 1: a three-way merge of the id-sorted
-// source lists.  Writes elements (dst_elem) or, for the last level, slots
-// only (dst_slot).  Cells of grids with R > 1 are left to k_sep_merge_large.
-template <typename G, int AXIS, bool LEVEL0>
-__global__ void __launch_bounds__(kSepThreads)
-k_sep_merge(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_elem, int *dst_slot) {
-  const long t = (long) blockIdx.x * kSepThreads + threadIdx.x;
-  if (t >= ncells) return;
-  const CellPos P = cell_pos(geo, t);
-  const long out0 = dst_off[t];
-  const int total = (int) (dst_off[t + 1] - out0);
-  if (P.R != 1 || total == 0) return;
+// A three-way merge of the id-sorted source lists pos[k] .. end[k], by one
+// thread.  Writes elements (dst_elem) or, for the last level, slots only
+// (dst_slot).
+template <bool LEVEL0>
+__device__ void seq_merge3(const SepSrc &S, int *pos, const int *end, int total, long out0,
+                           int4 *dst_elem, int *dst_slot) {
   const int kNone = 0x7fffffff;
-  int pos[3], end[3];
   int4 h[3];
 #pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const long u = axis_neighbour<AXIS>(P, t, k - 1);
-    pos[k] = u >= 0 ? S.off[u] : 0;
-    end[k] = u >= 0 ? S.off[u + 1] : 0;
+  for (int k = 0; k < 3; k++)
     h[k] = pos[k] < end[k] ? sep_elem_t<LEVEL0>(S, pos[k]) : make_int4(kNone, 0, 0, 0);
-  }
   for (int q = 0; q < total; q++) {
     const bool a01 = h[0].x < h[1].x;
     const int m01 = a01 ? h[0].x : h[1].x;
@@ -521,6 +510,98 @@ k_sep_merge(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_elem, in
         const int e = ++pos[j];
         h[j] = e < end[j] ? sep_elem_t<LEVEL0>(S, e) : make_int4(kNone, 0, 0, 0);
       }
+    }
+  }
+}
+
+// One thread per target cell with R = 1 (short lists: level 0).
+template <typename G, int AXIS, bool LEVEL0>
+__global__ void __launch_bounds__(kSepThreads)
+k_sep_merge(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_elem, int *dst_slot) {
+  const long t = (long) blockIdx.x * kSepThreads + threadIdx.x;
+  if (t >= ncells) return;
+  const CellPos P = cell_pos(geo, t);
+  const long out0 = dst_off[t];
+  const int total = (int) (dst_off[t + 1] - out0);
+  if (P.R != 1 || total == 0) return;
+  int pos[3], end[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const long u = axis_neighbour<AXIS>(P, t, k - 1);
+    pos[k] = u >= 0 ? S.off[u] : 0;
+    end[k] = u >= 0 ? S.off[u + 1] : 0;
+  }
+  seq_merge3<LEVEL0>(S, pos, end, total, out0, dst_elem, dst_slot);
+}
+
+constexpr int kSepStage = 512;  // source ids a warp of k_sep_merge_warp stages
+
+// One warp per target cell with R = 1.  The ids of the three source lists
+// are staged in shared memory with coalesced loads; an element's place is
+// its index in its own list plus the number of smaller ids in the other two
+// (binary searches in shared memory; the lists hold different agents).  So
+// the loads are independent instead of a chain of one per merged element.
+// Cells whose sources exceed the staging area are merged by one lane.
+// Cells of grids with R > 1 are left to k_sep_merge_large.
+template <typename G, int AXIS, bool LEVEL0>
+__global__ void __launch_bounds__(32 * kSepWarps)
+k_sep_merge_warp(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_elem,
+                 int *dst_slot) {
+  __shared__ int ids[kSepWarps][kSepStage];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long t = (long) blockIdx.x * kSepWarps + w;
+  if (t >= ncells) return;  // uniform over the warp, as is every exit below
+  const CellPos P = cell_pos(geo, t);
+  const long out0 = dst_off[t];
+  const int total = (int) (dst_off[t + 1] - out0);
+  if (P.R != 1 || total == 0) return;
+  int b[3], n[3], st[3];
+  int staged = 0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const long u = axis_neighbour<AXIS>(P, t, k - 1);
+    b[k] = u >= 0 ? S.off[u] : 0;
+    n[k] = u >= 0 ? S.off[u + 1] - b[k] : 0;
+    st[k] = staged;
+    staged += n[k];
+  }
+  if (staged > kSepStage) {
+    if (lane == 0) {
+      int pos[3] = {b[0], b[1], b[2]}, end[3] = {b[0] + n[0], b[1] + n[1], b[2] + n[2]};
+      seq_merge3<LEVEL0>(S, pos, end, total, out0, dst_elem, dst_slot);
+    }
+    return;
+  }
+  int *my = ids[w];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    for (int j = lane; j < n[k]; j += 32)
+      my[st[k] + j] = LEVEL0 ? __ldg(&S.order[b[k] + j]) : __ldg(&S.elem[b[k] + j].x);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    for (int j = lane; j < n[k]; j += 32) {
+      const int4 v = sep_elem_t<LEVEL0>(S, b[k] + j);
+      int rank = j;
+#pragma unroll
+      for (int k2 = 0; k2 < 3; k2++) {
+        if (k2 == k) continue;
+        int lo = 0, len = n[k2];
+        const int *a = my + st[k2];
+        while (len > 0) {
+          const int half = len >> 1;
+          if (a[lo + half] < v.x) {
+            lo += half + 1;
+            len -= half + 1;
+          } else {
+            len = half;
+          }
+        }
+        rank += lo;
+      }
+      if (dst_elem) dst_elem[out0 + rank] = v;
+      else dst_slot[out0 + rank] = v.y;
     }
   }
 }
@@ -1189,7 +1270,6 @@ void build_lists(abl_ctx *ctx, const G &geo, int dim, int levels, int Rmax, long
   const int B = 256;
   SepSrc src{cell_start, order, posf, dim, nullptr};
   const long cb = blocks_for(ncells, B), lb = blocks_for(ncells, kSepWarps);
-  const long sb = blocks_for(ncells, kSepThreads);
   for (int a = 0; a < levels; a++) {
     const bool last = a == dim - 1;
     int *off = last ? nb_off : L.off[a];
@@ -1201,13 +1281,16 @@ void build_lists(abl_ctx *ctx, const G &geo, int dim, int levels, int Rmax, long
     ctx->launches++;
     scan_run(ctx, scan, cnt, off);
     if (a == 0) {
-      k_sep_merge<G, 0, true><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, de, ds);
+      // Level 0 merges a few agents per cell: one thread per cell.  The
+      // later levels' lists are 3 and 9 times longer: one warp per cell.
+      k_sep_merge<G, 0, true><<<blocks_for(ncells, kSepThreads), kSepThreads, 0, s>>>(
+          ncells, geo, src, off, de, ds);
       if (Rmax > 1) k_sep_merge_large<G, 0><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, de, ds);
     } else if (a == 1) {
-      k_sep_merge<G, 1, false><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, de, ds);
+      k_sep_merge_warp<G, 1, false><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, de, ds);
       if (Rmax > 1) k_sep_merge_large<G, 1><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, de, ds);
     } else {
-      k_sep_merge<G, 2, false><<<sb, kSepThreads, 0, s>>>(ncells, geo, src, off, de, ds);
+      k_sep_merge_warp<G, 2, false><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, de, ds);
       if (Rmax > 1) k_sep_merge_large<G, 2><<<lb, 32 * kSepWarps, 0, s>>>(ncells, geo, src, off, de, ds);
     }
     ctx->launches += Rmax > 1 ? 2 : 1;
