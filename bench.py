@@ -34,6 +34,10 @@ FP64_FLOP_PER_AGENT_STEP = 560   # ~72 candidates x 5 + ~25 in-radius x 8 FP64 o
 # DRAM bytes of one update_boid launch on this workload (ncu capture, L2 cold
 # as in the timed steps, which flush L2 first).
 UPDATE_BOID_DRAM_BYTES = 239.36e6
+# game_of_life 4096^2 step kernel with kept neighbour lists: algorithmic bytes
+# per cell and timestep, and ncu's DRAM bytes for one launch
+GOL_BYTES_PER_CELL = 41
+GOL_DRAM_BYTES_4096 = 671.98e6
 
 
 def parse():
@@ -282,6 +286,24 @@ def measure_other_workloads(args, o, W, np):
     n = len(st["alive"])
     out["game_of_life_4096"] = {"value": n * 100 / sim.last_exec_time(), "unit": "agent-steps/s",
                                 "ms_per_step": sim.last_exec_time() * 10.0}
+    # its step kernel against HBM: per cell 40 B read (position 16, alive and
+    # the double buffer's alive 2, list offset 4, nine int16 list entries 18)
+    # and 1 B written; neighbours' alive bytes come from L1/L2
+    sim.set_profiling(True)
+    sim.run(20)
+    ksec, klaunch = sim.step_kernel_time(0)
+    sim.set_profiling(False)
+    kernel_s = ksec / max(1, klaunch)
+    peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(REPO, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    gbs = GOL_BYTES_PER_CELL * n / kernel_s / 1e9
+    out["game_of_life_4096"]["roofline"] = {
+        "bound": "hbm", "kernel": "step_move", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+        "frac": gbs / hbm_peak, "kernel_ms": kernel_s * 1e3, "bytes_per_agent": GOL_BYTES_PER_CELL,
+        "traffic": GOL_DRAM_BYTES_4096,
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
+                          "(profiles/step_move_game_of_life_4096.md)"}
     sim.close()
     # boids (3D), 1,048,576 agents (~9 per interaction cell), and sugarscape
     # on a 1024 x 1024 grid, 100 timesteps each
