@@ -192,7 +192,25 @@ __device__ __forceinline__ void fold_amax(float m, float *amax) {
   }
 }
 
-template <typename Real, int DIM>
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+__device__ __forceinline__ bool finite_bits(float x) {
+  return ((__float_as_int(x) >> 23) & 0xff) != 0xff;
+}
+
+// Cell coordinate in FP32 arithmetic (bin_in_fp32 decides when it may be
+// used): monotone in x, clamped into the border cells like cell_coord.
+__device__ __forceinline__ int cell_coord_f32(float x, float lo, float inv, int n) {
+  const float f = floorf(__fmul_rn(__fsub_rn(x, lo), inv));
+  if (!(f > 0.0f)) return 0;
+  if (f >= (float) (n - 1)) return n - 1;
+  return (int) f;
+}
+
+// F32: cell coordinates from the float-rounded position in FP32 (this GPU's
+// FP64 pipe is narrow; the conversions to float are needed for amax anyway).
+template <typename Real, int DIM, bool F32>
 __global__ void k_bin_assign(const Real *pos, long n, int nx, int ny, int nz, double lo0,
                              double lo1, double lo2, double inv_cell, int *cell_of,
                              int *cell_count, int *local_rank, float *amax, int *error) {
@@ -205,10 +223,15 @@ __global__ void k_bin_assign(const Real *pos, long n, int nx, int ny, int nz, do
     bool finite = true;
 #pragma unroll
     for (int d = 0; d < DIM; d++) {
-      double x = (double) pos[DIM * i + d];
-      finite = finite && isfinite(x);
-      c[d] = abl::cell_coord(x, lo[d], inv_cell, dims[d]);
-      m = fmaxf(m, fabsf((float) x));
+      const Real xr = pos[DIM * i + d];
+      finite = finite && finite_bits(xr);
+      const float xf = (float) xr;
+      if (F32) {
+        c[d] = cell_coord_f32(xf, (float) lo[d], (float) inv_cell, dims[d]);
+      } else {
+        c[d] = abl::cell_coord((double) xr, lo[d], inv_cell, dims[d]);
+      }
+      m = fmaxf(m, fabsf(xf));
     }
     if (!finite) atomicExch(error, ABL_E_NONFINITE);
     int cell = (c[2] * ny + c[1]) * nx + c[0];
@@ -1326,6 +1349,26 @@ void launch_gather(abl_ctx *ctx, TypeState &t, int dim, bool with_pos) {
   ctx->launches++;
 }
 
+// Whether a grid may compute cell coordinates in FP32 (k_bin_assign).  The
+// grid's cells are wider than its radius by 2^-10, so two agents within the
+// radius (as the reference's float-rounded test decides it, at most 2^-22
+// beyond) have exact cell coordinates less than 1 - 9.7e-4 apart, and their
+// cells differ by at most one whenever each computed coordinate is within
+// 4.8e-4 of the exact one.  FP32 rounds x, lo and 1/w (relative u = 2^-24
+// each), the difference and the product: for a point inside the grid the
+// error is at most (|x| + |lo|) inv u + 3 n u <= (2 |lo| inv + 4 n) u, with
+// n the cells along the axis.  Points outside clamp into border cells, which
+// keeps them in order.  FP32 is used when that bound is below 2.4e-4, half
+// the allowance; queries that compute their cell in FP64 stay consistent.
+bool bin_in_fp32(const TypeState &t, int dim) {
+  const int dims[3] = {t.nx, t.ny, t.nz};
+  for (int d = 0; d < dim; d++) {
+    const double bound = (2.0 * std::fabs(t.lo[d]) * t.inv_cell + 4.0 * dims[d]) * 5.9604644775390625e-8;
+    if (!(bound <= 2.4e-4)) return false;
+  }
+  return true;
+}
+
 template <typename Real>
 void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
   cudaStream_t s = ctx->stream;
@@ -1334,15 +1377,16 @@ void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
   const Real *pos = (const Real *) t.cols[t.cur][t.d->position_member];
   cudaMemsetAsync(t.cell_count, 0, sizeof(int) * t.ncells, s);
   cudaMemsetAsync(t.amax, 0, sizeof(float), s);
-  if (dim == 2) {
-    k_bin_assign<Real, 2><<<nb, B, 0, s>>>(pos, t.n, t.nx, t.ny, t.nz, t.lo[0], t.lo[1], t.lo[2],
-                                           t.inv_cell, t.cell_of, t.cell_count, t.local_rank,
-                                           t.amax, ctx->error);
-  } else {
-    k_bin_assign<Real, 3><<<nb, B, 0, s>>>(pos, t.n, t.nx, t.ny, t.nz, t.lo[0], t.lo[1], t.lo[2],
-                                           t.inv_cell, t.cell_of, t.cell_count, t.local_rank,
-                                           t.amax, ctx->error);
-  }
+  const bool f32 = bin_in_fp32(t, dim);
+#define ABL_BIN_ASSIGN(D, F)                                                                   \
+  k_bin_assign<Real, D, F><<<nb, B, 0, s>>>(pos, t.n, t.nx, t.ny, t.nz, t.lo[0], t.lo[1],    \
+                                            t.lo[2], t.inv_cell, t.cell_of, t.cell_count,     \
+                                            t.local_rank, t.amax, ctx->error)
+  if (dim == 2 && f32) ABL_BIN_ASSIGN(2, true);
+  else if (dim == 2) ABL_BIN_ASSIGN(2, false);
+  else if (f32) ABL_BIN_ASSIGN(3, true);
+  else ABL_BIN_ASSIGN(3, false);
+#undef ABL_BIN_ASSIGN
   ctx->launches++;
   scan_run(ctx, t.cell_scan, t.cell_count, t.cell_start);
   k_bin_scatter<<<nb, B, 0, s>>>(t.n, t.cell_of, t.local_rank, t.cell_start, t.order);
