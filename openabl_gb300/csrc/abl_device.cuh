@@ -71,6 +71,20 @@ __host__ __device__ inline int cell_coord(double x, double lo, double inv_cell, 
   return (int) f;
 }
 
+// The same in FP32 arithmetic, for grids whose size and offset keep its
+// rounding error far inside the cells' 2^-10 margin (the runtime decides,
+// bin_in_fp32): monotone in x, clamped into the border cells.
+__host__ __device__ inline int cell_coord_f32(float x, float lo, float inv_cell, int n) {
+#ifdef __CUDA_ARCH__
+  const float f = floorf(__fmul_rn(__fsub_rn(x, lo), inv_cell));
+#else
+  const float f = floorf((x - lo) * inv_cell);
+#endif
+  if (!(f > 0.0f)) return 0;
+  if (f >= (float) (n - 1)) return n - 1;
+  return (int) f;
+}
+
 struct band {
   float lo, hi;
 };
@@ -148,7 +162,11 @@ struct near_query {
       c[1] = (l - c[2] * nxy) / V.nx;
       c[0] = l - c[2] * nxy - c[1] * V.nx;
     } else {
-      for (int d = 0; d < 3; d++) c[d] = d < DIM ? cell_coord(p[d], V.lo[d], V.inv_cell, dims[d]) : 0;
+      for (int d = 0; d < 3; d++) {
+        if (d >= DIM) c[d] = 0;
+        else if (V.cell_f32) c[d] = cell_coord_f32((float) p[d], (float) V.lo[d], (float) V.inv_cell, dims[d]);
+        else c[d] = cell_coord(p[d], V.lo[d], V.inv_cell, dims[d]);
+      }
     }
     for (int d = 0; d < 3; d++) pf[d] = d < DIM ? (float) p[d] : 0.0f;
     amax = *V.amax;

@@ -76,6 +76,7 @@ typedef struct {
   const void *ncache_list;  /* int32 agent indices, or with ncache_narrow int16 offsets
                                from the query agent's index */
   int ncache_narrow;
+  int cell_f32;             /* query cells may be computed in FP32 (as the binning does) */
 } abl_near_view;
 
 /* Everything a generated step launcher needs. */

@@ -199,15 +199,6 @@ __device__ __forceinline__ bool finite_bits(float x) {
   return ((__float_as_int(x) >> 23) & 0xff) != 0xff;
 }
 
-// Cell coordinate in FP32 arithmetic (bin_in_fp32 decides when it may be
-// used): monotone in x, clamped into the border cells like cell_coord.
-__device__ __forceinline__ int cell_coord_f32(float x, float lo, float inv, int n) {
-  const float f = floorf(__fmul_rn(__fsub_rn(x, lo), inv));
-  if (!(f > 0.0f)) return 0;
-  if (f >= (float) (n - 1)) return n - 1;
-  return (int) f;
-}
-
 // F32: cell coordinates from the float-rounded position in FP32 (this GPU's
 // FP64 pipe is narrow; the conversions to float are needed for amax anyway).
 template <typename Real, int DIM, bool F32>
@@ -227,7 +218,7 @@ __global__ void k_bin_assign(const Real *pos, long n, int nx, int ny, int nz, do
       finite = finite && finite_bits(xr);
       const float xf = (float) xr;
       if (F32) {
-        c[d] = cell_coord_f32(xf, (float) lo[d], (float) inv_cell, dims[d]);
+        c[d] = abl::cell_coord_f32(xf, (float) lo[d], (float) inv_cell, dims[d]);
       } else {
         c[d] = abl::cell_coord((double) xr, lo[d], inv_cell, dims[d]);
       }
@@ -1831,6 +1822,7 @@ int step_once(abl_ctx *ctx) {
       V.cap = V.ordered ? ctx->list_cap : ctx->runs_cap;
       V.cell_of = sd.agent_type == sd.near_type ? nt.cell_of : nullptr;
       V.cell_base = 0;
+      V.cell_f32 = bin_in_fp32(nt, nt.d->dim) ? 1 : 0;
       // Threads visit the binned agents in slot order, so a block's agents
       // fill consecutive cells: block lists pay off.
       V.block_cap = block_lists_wanted(sd, depth, ctx->near_mode) ? ctx->block_cap : 0;
