@@ -339,6 +339,11 @@ struct GatherArgs {
   const void *src[ABL_MAX_MEMBERS];
   void *dst[ABL_MAX_MEMBERS];
   int bytes[ABL_MAX_MEMBERS];
+  // Up to four members of 16 bytes each (float2 of doubles, e.g. boids2d's
+  // pos and velocity): all loads issued before the stores.  pos16 is the
+  // position's place among them (-1: not gathered, or 3D).
+  int all16;
+  int pos16;
 };
 
 template <typename Real, int DIM>
@@ -347,6 +352,27 @@ __global__ void k_gather(long n, const int *order, const Real *pos, float *posf,
   long s = (long) blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   long i = order[s];
+  if (g.all16) {
+    uint4 v[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (k < g.nmem) v[k] = __ldg((const uint4 *) g.src[k] + i);
+    if (posf && g.pos16 >= 0 && DIM == 2) {
+      uint4 p = v[0];
+#pragma unroll
+      for (int k = 1; k < 4; k++)
+        if (k == g.pos16) p = v[k];
+      posf[2 * s] = (float) __hiloint2double((int) p.y, (int) p.x);
+      posf[2 * s + 1] = (float) __hiloint2double((int) p.w, (int) p.z);
+    } else if (posf) {
+#pragma unroll
+      for (int d = 0; d < DIM; d++) posf[DIM * s + d] = (float) pos[DIM * i + d];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (k < g.nmem) ((uint4 *) g.dst[k])[s] = v[k];
+    return;
+  }
   if (posf) {
 #pragma unroll
     for (int d = 0; d < DIM; d++) posf[DIM * s + d] = (float) pos[DIM * i + d];
@@ -1322,14 +1348,20 @@ void launch_gather(abl_ctx *ctx, TypeState &t, int dim, bool with_pos) {
   const Real *pos = (const Real *) t.cols[t.cur][t.d->position_member];
   GatherArgs g;
   std::memset(&g, 0, sizeof g);
+  g.pos16 = -1;
   for (int k = 0; k < t.d->num_members; k++) {
     if (!(t.gather_mask & (1u << k))) continue;
     if (!with_pos && k == t.d->position_member) continue;
+    if (k == t.d->position_member) g.pos16 = g.nmem;
     g.src[g.nmem] = t.cols[t.cur][k];
     g.dst[g.nmem] = t.gcols[k];
     g.bytes[g.nmem] = (int) member_bytes(t.d->members[k]);
     g.nmem++;
   }
+  g.all16 = g.nmem > 0 && g.nmem <= 4;
+  for (int k = 0; k < g.nmem; k++) g.all16 = g.all16 && g.bytes[k] == 16;
+  // The position taken from its gathered copy only for double 2D positions.
+  if (!(dim == 2 && sizeof(Real) == 8)) g.pos16 = -1;
   if (!with_pos && g.nmem == 0) return;
   float *posf = with_pos ? t.posf : nullptr;
   if (dim == 2) {
