@@ -574,6 +574,53 @@ k_sep_merge(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_elem, in
   seq_merge3<LEVEL0>(S, pos, end, total, out0, dst_elem, dst_slot);
 }
 
+// Level 0 of a single grid (R = 1), one thread per source slot: the three
+// runs merged into cell t's list are the runs of cells t-1, t and t+1, so the
+// slot's element goes to the lists of its own cell and of its x-neighbours.
+// Its place in each is its index in its own run plus the number of smaller
+// ids in the other two runs (binary searches over the short, id-sorted runs).
+// The loads are independent, where a thread merging a cell's list waits on
+// one load per element.  Writes the same lists as k_sep_merge<G, 0, true>.
+template <typename G>
+__global__ void k_sep_rows_by_slot(long n, G geo, const int *cell_start, const int *order,
+                                   const float *posf, int dim, const int *cell_of,
+                                   const int *dst_off, int4 *dst_elem) {
+  const long e = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int id = __ldg(&order[e]);
+  const int c = __ldg(&cell_of[id]);
+  const CellPos P = cell_pos(geo, c);
+  const int own = (int) e - __ldg(&cell_start[c]);
+  const int4 v = make_int4(id, (int) e, __float_as_int(__ldg(&posf[dim * e])),
+                           __float_as_int(__ldg(&posf[dim * e + 1])));
+  const int x = P.x[0], nx = P.n[0];
+#pragma unroll
+  for (int d = -1; d <= 1; d++) {
+    const int xt = x + d;
+    if (xt < 0 || xt >= nx) continue;
+    const int t = c + d;
+    int rank = own;
+#pragma unroll
+    for (int k = -1; k <= 1; k++) {
+      const int xu = xt + k;
+      if (xu < 0 || xu >= nx || t + k == c) continue;
+      const int b = __ldg(&cell_start[t + k]);
+      int len = __ldg(&cell_start[t + k + 1]) - b, lo = 0;
+      while (len > 0) {
+        const int half = len >> 1;
+        if (__ldg(&order[b + lo + half]) < id) {
+          lo += half + 1;
+          len -= half + 1;
+        } else {
+          len = half;
+        }
+      }
+      rank += lo;
+    }
+    dst_elem[__ldg(&dst_off[t]) + rank] = v;
+  }
+}
+
 constexpr int kSepStage = 512;  // source ids a warp of k_sep_merge_warp stages
 
 // One warp per target cell with R = 1.  The ids of the three source lists
@@ -1305,7 +1352,8 @@ int apply_population_changes(abl_ctx *ctx, int k, bool &regrow) {
 template <typename G>
 void build_lists(abl_ctx *ctx, const G &geo, int dim, int levels, int Rmax, long ncells,
                  const int *cell_start, const int *order, const float *posf,
-                 const SepLevels &L, int *cnt, const ScanPlan &scan, int *nb_off, int *nb_list) {
+                 const SepLevels &L, int *cnt, const ScanPlan &scan, int *nb_off, int *nb_list,
+                 long nslots = 0, const int *cell_of = nullptr) {
   cudaStream_t s = ctx->stream;
   const int B = 256;
   SepSrc src{cell_start, order, posf, dim, nullptr};
@@ -1320,7 +1368,11 @@ void build_lists(abl_ctx *ctx, const G &geo, int dim, int levels, int Rmax, long
     else k_sep_count<G, 2><<<cb, B, 0, s>>>(ncells, geo, src.off, cnt);
     ctx->launches++;
     scan_run(ctx, scan, cnt, off);
-    if (a == 0) {
+    if (a == 0 && cell_of && de && Rmax == 1) {
+      // A single grid's row lists: one thread per slot.
+      k_sep_rows_by_slot<G><<<blocks_for(nslots, B), B, 0, s>>>(nslots, geo, cell_start, order,
+                                                               posf, dim, cell_of, off, de);
+    } else if (a == 0) {
       // Level 0 merges a few agents per cell: one thread per cell.  The
       // later levels' lists are 3 and 9 times longer: one warp per cell.
       k_sep_merge<G, 0, true><<<blocks_for(ncells, kSepThreads), kSepThreads, 0, s>>>(
@@ -1420,7 +1472,7 @@ void launch_bin(abl_ctx *ctx, TypeState &t, int dim) {
   if (t.ordered || t.rows) {
     GridGeom geo{t.nx, t.ny, t.nz, t.R};
     build_lists(ctx, geo, dim, t.ordered ? dim : 1, t.R, t.ncells, t.cell_start, t.order,
-                t.posf, t.sep, t.nb_cnt, t.nb_scan, t.nb_off, t.nb_list);
+                t.posf, t.sep, t.nb_cnt, t.nb_scan, t.nb_off, t.nb_list, t.n, t.cell_of);
   }
 }
 
