@@ -160,6 +160,28 @@ __global__ void k_scan_finish(const int *incl, int *out_excl, long m, const int 
   out_excl[i] = incl[j] + block_offsets[j / kScanBlock];
 }
 
+// Last pass of a scan whose block totals fit one block: thread j of a CTA
+// of 256 (all in one scan block, as kScanBlock is a multiple of 256) writes
+// out_excl[j + 1] = incl[j] + the totals of the scan blocks before its own,
+// which the CTA adds up itself instead of a separate kernel scanning them.
+__global__ void k_scan_finish_sums(const int *incl, int *out_excl, long m, const int *sums) {
+  __shared__ int part[8];
+  const long j0 = (long) blockIdx.x * blockDim.x;
+  const int sb = (int) (j0 / kScanBlock);
+  int acc = 0;
+  for (int k = threadIdx.x; k < sb; k += blockDim.x) acc += sums[k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  int off = 0;
+#pragma unroll
+  for (int w = 0; w < 8; w++) off += part[w];
+  const long j = j0 + threadIdx.x;
+  if (j == 0) out_excl[0] = 0;
+  if (j < m) out_excl[j + 1] = incl[j] + off;
+}
+
 // Scan plan for an exclusive scan of m ints.  Level l scans its input in
 // blocks (incl), collects the block totals (sums) and obtains the block
 // offsets (offs, nb + 1 entries) by scanning the totals one level up.
@@ -246,6 +268,28 @@ __global__ void k_cell_sort(long ncells, const int *cell_start, int *order) {
   long c = (long) blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   int s = cell_start[c], e = cell_start[c + 1];
+  constexpr int K = 16;
+  if (e - s <= K) {
+    // Short runs (nearly all): loaded together into registers, sorted by an
+    // odd-even transposition network, stored back.
+    const int len = e - s;
+    int v[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = k < len ? order[s + k] : 0x7fffffff;
+#pragma unroll
+    for (int p = 0; p < K; p++) {
+#pragma unroll
+      for (int k = p & 1; k + 1 < K; k += 2) {
+        const int a = min(v[k], v[k + 1]), b = max(v[k], v[k + 1]);
+        v[k] = a;
+        v[k + 1] = b;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (k < len) order[s + k] = v[k];
+    return;
+  }
   for (int i = s + 1; i < e; i++) {
     int v = order[i];
     int j = i - 1;
@@ -972,6 +1016,11 @@ void scan_level(abl_ctx *ctx, const ScanPlan &p, size_t l, const int *in, int *o
   }
   k_scan_blocks<<<L.nb, kScanBlock / 4, 0, s>>>(in, L.incl, L.m, L.sums);
   ctx->launches++;
+  if (L.nb <= kScanBlock) {
+    k_scan_finish_sums<<<(L.m + 255) / 256, 256, 0, s>>>(L.incl, out, L.m, L.sums);
+    ctx->launches++;
+    return;
+  }
   scan_level(ctx, p, l + 1, L.sums, L.offs);
   k_scan_finish<<<(L.m + 1 + 255) / 256, 256, 0, s>>>(L.incl, out, L.m, L.offs);
   ctx->launches++;
