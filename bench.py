@@ -33,7 +33,7 @@ BYTES_PER_AGENT_STEP = 80        # SoA pos+vel read + written, binning key/id wr
 FP64_FLOP_PER_AGENT_STEP = 560   # ~72 candidates x 5 + ~25 in-radius x 8 FP64 ops
 # DRAM bytes of one update_boid launch on this workload (ncu capture, L2 cold
 # as in the timed steps, which flush L2 first).
-UPDATE_BOID_DRAM_BYTES = 239.36e6
+UPDATE_BOID_DRAM_BYTES = 240.00e6
 # game_of_life 4096^2 step kernel with kept neighbour lists: algorithmic bytes
 # per cell and timestep, and ncu's DRAM bytes for one launch
 GOL_BYTES_PER_CELL = 41
