@@ -133,3 +133,25 @@ def test_seed_option_keys_random_in_steps(compiler, tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     src = (tmp_path / "flockers.cu").read_text()
     assert 'abl_check(abl_set_seed(ctx, 42ull), "abl_set_seed");' in src
+
+
+def test_constant_arrays_and_local_radius(compiler, tmp_path):
+    """Constant arrays become fixed-size fields of the globals block with the
+    reference's initialisers; a near() radius held in a step-local variable of
+    globals (keratinocyte's `float radius = 125;`) stands for its value."""
+    r = subprocess.run([compiler, "-A", os.path.join(REF, "asset"), "-i",
+                        os.path.join(REPO, "tests", "models", "kinds.abl"), "-o",
+                        str(tmp_path / "kinds"), "-b", "cuda", "-C", "cuda.model=kinds"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    src = (tmp_path / "kinds" / "kinds.cu").read_text()
+    assert "float WEIGHT[3];" in src and "int NEXT_KIND[3];" in src
+    assert "abl_G.WEIGHT[nx->kind]" in src
+    r = subprocess.run([compiler, "-A", os.path.join(REF, "asset"), "-i",
+                        os.path.join(REF, "examples", "keratinocyte.abl"), "-o",
+                        str(tmp_path / "ker"), "-b", "cuda", "-C", "cuda.model=keratinocyte"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    src = (tmp_path / "ker" / "keratinocyte.cu").read_text()
+    # the host's radius function and the presorted phase use the initialiser
+    assert "return (double) (((double) (125.0)));" in src
