@@ -885,6 +885,7 @@ struct abl_ctx {
   std::vector<size_t> sizes;
   int *error = nullptr;
   float *amax_pair = nullptr;  // per step: max of query and neighbour amax
+  int *error_host = nullptr;   // pinned copy of `error` read by check_error
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_exec = 0.0;
   long launches = 0, last_launches = 0;
@@ -2054,6 +2055,20 @@ bool graph_capturable(const abl_ctx *ctx) {
 }
 
 int check_error(abl_ctx *ctx) {
+  if (ctx->error_host) {
+    // One round trip: the error word follows the stream's work into pinned
+    // memory, then a single synchronisation.
+    ABL_CUDA_TRY(cudaMemcpyAsync(ctx->error_host, ctx->error, sizeof(int),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    const int e = *ctx->error_host;
+    if (e != 0) {
+      cudaMemsetAsync(ctx->error, 0, sizeof(int), ctx->stream);
+      cudaStreamSynchronize(ctx->stream);
+      return e;
+    }
+    return ABL_OK;
+  }
   ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   int h = 0;
   ABL_CUDA_TRY(cudaMemcpy(&h, ctx->error, sizeof(int), cudaMemcpyDeviceToHost));
@@ -2241,6 +2256,7 @@ int abl_create(const abl_model_desc *model, size_t hbm_budget, abl_ctx **out) {
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ts0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ts1);
+  if (e == cudaSuccess) e = cudaHostAlloc(&ctx->error_host, sizeof(int), cudaHostAllocDefault);
   if (e != cudaSuccess) {
     std::fprintf(stderr, "openabl-cuda: context setup failed: %s\n", cudaGetErrorString(e));
     delete ctx;
@@ -2766,6 +2782,7 @@ int abl_destroy(abl_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   drop_graph(ctx);
   for (void *p : ctx->allocations) cudaFree(p);
+  if (ctx->error_host) cudaFreeHost(ctx->error_host);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->ts0) cudaEventDestroy(ctx->ts0);
