@@ -155,3 +155,34 @@ def test_constant_arrays_and_local_radius(compiler, tmp_path):
     src = (tmp_path / "ker" / "keratinocyte.cu").read_text()
     # the host's radius function and the presorted phase use the initialiser
     assert "return (double) (((double) (125.0)));" in src
+
+
+def step_descriptor(model, step):
+    """The fields of a generated step descriptor (abl_step_desc), by name."""
+    src = open(os.path.join(REPO, "openabl_gb300", "generated", model + ".cu")).read()
+    line = next(l for l in src.splitlines() if l.strip().startswith('{"%s",' % step))
+    f = [x.strip() for x in line.strip().strip("{},").split(",")]
+    names = ["name", "agent_type", "near_type", "ordered", "radius", "near_members",
+             "out_written", "launch", "uses_remove", "add_type", "out_copy", "launch_ens",
+             "uses_rng", "presorted", "out_changed", "near_cacheable"]
+    return dict(zip(names, f))
+
+
+@pytest.mark.parametrize("model,step,changed,cacheable", [
+    # out.pos = in.pos is not a change: game_of_life's positions never move
+    ("game_of_life", "step_move", "2u", "1"),
+    ("boids2d", "update_boid", "3u", "1"),
+    # sugarscape's agents sit on the grid; the step writes state and target
+    ("sugarscape", "movement_request", "10u", "1"),
+    ("kinds", "mix", "6u", "1"),
+    # no near loop
+    ("predator_prey", "prey_move", "11u", "0"),
+])
+def test_step_descriptors(model, step, changed, cacheable):
+    """The analysis behind static positions and kept neighbour lists: which
+    members a step may change, and whether its near loop is centred on its own
+    agent with a radius of globals."""
+    d = step_descriptor(model, step)
+    if changed is not None:
+        assert d["out_changed"] == changed
+    assert d["near_cacheable"] == cacheable
