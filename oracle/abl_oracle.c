@@ -119,6 +119,18 @@ ORACLE_API void oracle_init_boids2d(long n, double min_pos, double max_pos, doub
   }
 }
 
+/* examples/boids.abl:112-120 (3D): pos = random(float3(min_pos), float3(max_pos)),
+ * velocity = random(float3(-1), float3(1)). */
+ORACLE_API void oracle_init_boids3d(long n, double min_pos, double max_pos, double *pos,
+                                    double *vel) {
+  double plo[3] = {min_pos, min_pos, min_pos}, phi[3] = {max_pos, max_pos, max_pos};
+  double vlo[3] = {-1, -1, -1}, vhi[3] = {1, 1, 1};
+  for (long i = 0; i < n; i++) {
+    draw_vec(pos + 3 * i, 3, plo, phi);
+    draw_vec(vel + 3 * i, 3, vlo, vhi);
+  }
+}
+
 /* examples/game_of_life.abl:63-75 with debug = false:
  * pos = float2(x + 0.5, y + 0.5) (x cast to C float first, as the reference
  * prints `(float) x`), alive = random(0, 1) < alive_fraction. */
@@ -325,94 +337,95 @@ ORACLE_API int oracle_circle_step(int dim, long n, const double *pos_in, double 
   return 0;
 }
 
-/* ------------------------------------------------------------ boids2d */
-/* examples/boids2d.abl:43-108 as printed by the reference (see the module
+/* ------------------------------------------------------------ boids */
+/* examples/boids2d.abl:43-108 (DIM 2) and examples/boids.abl:43-110 (DIM 3,
+ * the same rules on float3) as printed by the reference (see the module
  * comment for the arithmetic rules).  Parameters are the printed constants:
  * p[0..9] = interaction_radius, separation_radius, time_scale, global_scale,
- * steer_scale, collision_scale, match_scale, min_pos, max_pos, (unused). */
-ORACLE_API int oracle_boids2d_step(long n, const double *pos_in, const double *vel_in,
-                                   double *pos_out, double *vel_out, const double *p,
-                                   int mode, int nthreads, long first, long count) {
+ * steer_scale, collision_scale, match_scale, min_pos, max_pos, (unused).
+ * Component-wise statements keep the reference's order of operations; length
+ * and dist sum the squares x, y, z left to right (libabl.h:156-167). */
+static int boids_step(int dim, long n, const double *pos_in, const double *vel_in,
+                      double *pos_out, double *vel_out, const double *p, int mode, int nthreads,
+                      long first, long count) {
   const double interaction_radius = p[0], separation_radius = p[1], time_scale = p[2],
                global_scale = p[3], steer_scale = p[4], collision_scale = p[5],
                match_scale = p[6], min_pos = p[7], max_pos = p[8];
   grid_t g;
-  double emin[2] = {min_pos, min_pos}, emax[2] = {max_pos, max_pos};
-  if (mode == 1) grid_build(&g, 2, n, pos_in, emin, emax, interaction_radius);
+  double emin[3] = {min_pos, min_pos, min_pos}, emax[3] = {max_pos, max_pos, max_pos};
+  if (mode == 1) grid_build(&g, dim, n, pos_in, emin, emax, interaction_radius);
 #pragma omp parallel num_threads(threads_or_default(nthreads))
   {
     long *buf = NULL, cap = 0;
 #pragma omp for schedule(dynamic, 64)
     for (long i = first; i < first + count; i++) {
-      const double *ip = pos_in + 2 * i;
-      const double *iv = vel_in + 2 * i;
-      double gv[2] = {0, 0}, gc[2] = {0, 0}, cc[2] = {0, 0};
+      const double *ip = pos_in + dim * i;
+      const double *iv = vel_in + dim * i;
+      double gv[3] = {0, 0, 0}, gc[3] = {0, 0, 0}, cc[3] = {0, 0, 0};
       int interaction_count = 0, collision_count = 0;
       FOR_EACH_CANDIDATE(j, i, n, mode, &g, buf, cap, {
-        const double *jp = pos_in + 2 * j;
-        const double *jv = vel_in + 2 * j;
-        if (dist2(jp, ip) > interaction_radius) continue;
-        gc[0] = gc[0] + jp[0];
-        gc[1] = gc[1] + jp[1];
-        gv[0] = gv[0] + jv[0];
-        gv[1] = gv[1] + jv[1];
+        const double *jp = pos_in + dim * j;
+        const double *jv = vel_in + dim * j;
+        if (distd(dim, jp, ip) > interaction_radius) continue;
+        for (int d = 0; d < dim; d++) gc[d] = gc[d] + jp[d];
+        for (int d = 0; d < dim; d++) gv[d] = gv[d] + jv[d];
         interaction_count += 1;
-        double separation = dist2(ip, jp);
+        double separation = distd(dim, ip, jp);
         if (separation < separation_radius) {
-          cc[0] = cc[0] + jp[0];
-          cc[1] = cc[1] + jp[1];
+          for (int d = 0; d < dim; d++) cc[d] = cc[d] + jp[d];
           collision_count += 1;
         }
       });
-      double vc[2] = {0, 0};
-      double steer[2] = {0, 0};
+      double vc[3] = {0, 0, 0};
+      double steer[3] = {0, 0, 0};
       if (interaction_count > 0) {
-        gc[0] = gc[0] / interaction_count;
-        gc[1] = gc[1] / interaction_count;
-        steer[0] = (gc[0] - ip[0]) * steer_scale;
-        steer[1] = (gc[1] - ip[1]) * steer_scale;
+        for (int d = 0; d < dim; d++) gc[d] = gc[d] / interaction_count;
+        for (int d = 0; d < dim; d++) steer[d] = (gc[d] - ip[d]) * steer_scale;
       }
-      vc[0] = vc[0] + steer[0];
-      vc[1] = vc[1] + steer[1];
-      double match[2] = {0, 0};
+      for (int d = 0; d < dim; d++) vc[d] = vc[d] + steer[d];
+      double match[3] = {0, 0, 0};
       if (interaction_count > 0) {
-        gv[0] = gv[0] / interaction_count;
-        gv[1] = gv[1] / interaction_count;
-        match[0] = gv[0] * match_scale;
-        match[1] = gv[1] * match_scale;
+        for (int d = 0; d < dim; d++) gv[d] = gv[d] / interaction_count;
+        for (int d = 0; d < dim; d++) match[d] = gv[d] * match_scale;
       }
-      vc[0] = vc[0] + match[0];
-      vc[1] = vc[1] + match[1];
-      double avoid[2] = {0, 0};
+      for (int d = 0; d < dim; d++) vc[d] = vc[d] + match[d];
+      double avoid[3] = {0, 0, 0};
       if (collision_count > 0) {
-        cc[0] = cc[0] / collision_count;
-        cc[1] = cc[1] / collision_count;
-        avoid[0] = (ip[0] - cc[0]) * collision_scale;
-        avoid[1] = (ip[1] - cc[1]) * collision_scale;
+        for (int d = 0; d < dim; d++) cc[d] = cc[d] / collision_count;
+        for (int d = 0; d < dim; d++) avoid[d] = (ip[d] - cc[d]) * collision_scale;
       }
-      vc[0] = vc[0] + avoid[0];
-      vc[1] = vc[1] + avoid[1];
-      double nv[2] = {iv[0] + vc[0] * global_scale, iv[1] + vc[1] * global_scale};
-      double scale = (double) sqrtf((float) (nv[0] * nv[0] + nv[1] * nv[1]));
+      for (int d = 0; d < dim; d++) vc[d] = vc[d] + avoid[d];
+      double nv[3] = {0, 0, 0};
+      for (int d = 0; d < dim; d++) nv[d] = iv[d] + vc[d] * global_scale;
+      double ss = nv[0] * nv[0] + nv[1] * nv[1];
+      if (dim == 3) ss = ss + nv[2] * nv[2];
+      double scale = (double) sqrtf((float) ss);
       if (scale > 1) {
-        nv[0] = nv[0] / scale;
-        nv[1] = nv[1] / scale;
+        for (int d = 0; d < dim; d++) nv[d] = nv[d] / scale;
       }
-      double np[2] = {ip[0] + nv[0] * time_scale, ip[1] + nv[1] * time_scale};
-      /* boundPosition, examples/boids2d.abl:43-50 */
-      for (int d = 0; d < 2; d++) {
-        double v = np[d];
-        np[d] = v < min_pos ? max_pos : (v > max_pos ? min_pos : v);
+      /* boundPosition (examples/boids2d.abl:43-50, boids.abl:43-52) */
+      for (int d = 0; d < dim; d++) {
+        double v = ip[d] + nv[d] * time_scale;
+        pos_out[dim * i + d] = v < min_pos ? max_pos : (v > max_pos ? min_pos : v);
+        vel_out[dim * i + d] = nv[d];
       }
-      pos_out[2 * i] = np[0];
-      pos_out[2 * i + 1] = np[1];
-      vel_out[2 * i] = nv[0];
-      vel_out[2 * i + 1] = nv[1];
     }
     free(buf);
   }
   if (mode == 1) grid_free(&g);
   return 0;
+}
+
+ORACLE_API int oracle_boids2d_step(long n, const double *pos_in, const double *vel_in,
+                                   double *pos_out, double *vel_out, const double *p,
+                                   int mode, int nthreads, long first, long count) {
+  return boids_step(2, n, pos_in, vel_in, pos_out, vel_out, p, mode, nthreads, first, count);
+}
+
+ORACLE_API int oracle_boids3d_step(long n, const double *pos_in, const double *vel_in,
+                                   double *pos_out, double *vel_out, const double *p,
+                                   int mode, int nthreads, long first, long count) {
+  return boids_step(3, n, pos_in, vel_in, pos_out, vel_out, p, mode, nthreads, first, count);
 }
 
 /* ------------------------------------------------------- game of life */

@@ -39,6 +39,8 @@ def lib():
         L.oracle_init_game_of_life.argtypes = [_i, _d, _p, _p]
         L.oracle_circle_step.argtypes = [_i, _l, _p, _p, _d, _d, _d, _d, _p, _p, _i, _i, _l, _l]
         L.oracle_boids2d_step.argtypes = [_l, _p, _p, _p, _p, _p, _i, _i, _l, _l]
+        L.oracle_init_boids3d.argtypes = [_l, _d, _d, _p, _p]
+        L.oracle_boids3d_step.argtypes = [_l, _p, _p, _p, _p, _p, _i, _i, _l, _l]
         L.oracle_game_of_life_step.argtypes = [_l, _p, _p, _p, _p, _d, _d, _i, _i, _l, _l]
         _LIB = L
     return _LIB
@@ -112,6 +114,28 @@ def boids2d_step(state, c, mode=1, nthreads=0, first=0, count=None):
     return {"pos": po, "velocity": vo}
 
 
+def init_boids3d(n, min_pos, max_pos):
+    """examples/boids.abl's main(): positions and velocities from the reference stream."""
+    rng_reset()
+    pos = np.zeros((n, 3), np.float64)
+    vel = np.zeros((n, 3), np.float64)
+    lib().oracle_init_boids3d(n, min_pos, max_pos, _ptr(pos), _ptr(vel))
+    return {"pos": pos, "velocity": vel}
+
+
+def boids3d_step(state, c, mode=1, nthreads=0, first=0, count=None):
+    """One timestep of examples/boids.abl (boids in 3D); constants as BOIDS2D_KEYS."""
+    pos = np.ascontiguousarray(state["pos"])
+    vel = np.ascontiguousarray(state["velocity"])
+    n = pos.shape[0]
+    po, vo = pos.copy(), vel.copy()
+    p = np.array([c[k] for k in BOIDS2D_KEYS] + [0.0], np.float64)
+    first, count = _range(n, first, count)
+    lib().oracle_boids3d_step(n, _ptr(pos), _ptr(vel), _ptr(po), _ptr(vo), _ptr(p), mode,
+                              nthreads, first, count)
+    return {"pos": po, "velocity": vo}
+
+
 def game_of_life_step(state, c, mode=1, nthreads=0, first=0, count=None):
     pos = np.ascontiguousarray(state["pos"])
     alive = np.ascontiguousarray(state["alive"], dtype=np.uint8)
@@ -124,7 +148,7 @@ def game_of_life_step(state, c, mode=1, nthreads=0, first=0, count=None):
 
 
 STEP = {"circle": circle_step, "circle3d": circle_step, "boids2d": boids2d_step,
-        "game_of_life": game_of_life_step}
+        "game_of_life": game_of_life_step, "boids": boids3d_step}
 
 
 # ------------------------------------------------------------ predator_prey

@@ -27,10 +27,15 @@ def consts(meta):
                     min_pos=0.0, max_pos=float("%g" % math.sqrt(n / dens)))
     if ex == "game_of_life":
         return dict(radius=1.5, size=int(math.sqrt(int(p["num_agents"]))))
+    if ex == "boids":
+        # examples/boids.abl at its defaults: 5000 agents, agent_density 1000
+        return dict(interaction_radius=0.05, separation_radius=0.005, time_scale=0.0005,
+                    global_scale=0.15, steer_scale=0.65, collision_scale=0.75, match_scale=1.25,
+                    min_pos=0.0, max_pos=float("%g" % (5000 / 1000) ** (1 / 3)))
     raise KeyError(ex)
 
 
-CASES = ["circle_4000", "circle3d_4000", "boids2d_4096", "game_of_life_64"]
+CASES = ["circle_4000", "circle3d_4000", "boids2d_4096", "game_of_life_64", "boids3d_5000"]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -42,6 +47,8 @@ def test_reference_init_restated(case):
         s = O.init_circle(2 if ex == "circle" else 3, meta["agents"], c["W"])
     elif ex == "boids2d":
         s = O.init_boids2d(meta["agents"], c["min_pos"], c["max_pos"])
+    elif ex == "boids":
+        s = O.init_boids3d(meta["agents"], c["min_pos"], c["max_pos"])
     else:
         s = O.init_game_of_life(c["size"], float(meta["params"]["alive_fraction"]))
     for k in state:
