@@ -84,6 +84,24 @@ def test_boids2d_1m_matches_oracle():
     sim.close()
 
 
+def test_boids3d_1m_matches_oracle():
+    """The 3D bench workload (1,048,576 boids, ~9 per interaction cell)
+    against the oracle's restatement of examples/boids.abl."""
+    model, g = o.globals_for_config("boids3d_1m")
+    state = workloads.boids3d(g.get("num_agents"), g.get("max_pos"), seed=0)
+    sim = o.Simulation(model, g)
+    sim.upload("Boid", state)
+    c = boids_consts(g)
+    ref = state
+    for t in range(2):
+        sim.step()
+        ref = O.boids3d_step(ref, c, mode=1)
+        got = sim.download("Boid")
+        for k in ("pos", "velocity"):
+            assert np.array_equal(got[k], ref[k]), (t, k)
+    sim.close()
+
+
 def test_game_of_life_4096_matches_oracle():
     model, g = o.globals_for_config("game_of_life_4096")
     state = workloads.game_of_life(g.get("size"), 0.5, seed=0)
