@@ -467,6 +467,124 @@ ORACLE_API int oracle_game_of_life_step(long n, const double *pos_in, const uint
   return 0;
 }
 
+/* ---------------------------------------------------------- sugarscape */
+/* examples/sugarscape.abl:67-160, the four step functions as printed by the
+ * reference.  Members of `out` a step does not write keep what the double
+ * buffer held (agents_X_dbuf, src/backend/CPrinter.cpp:189-233: the dbuf
+ * starts as a copy of the population and the two are swapped after every
+ * step function), so `out` is passed in holding the double buffer and only
+ * the members the printed code assigns are changed.  States: 0 unoccupied,
+ * 1 occupied, 2 movement requested, 3 movement unresolved; the near radius is
+ * the global `radius` and the sugar growback rate 1 (sugarscape.abl:28-39). */
+typedef struct {
+  double *pos, *target_pos;
+  int *agent_id, *state, *sugar_level, *metabolism, *env_sugar_level, *max_env_sugar_level;
+} sg_cols;
+
+static inline int sg_same(const double *a, const double *b) { return a[0] == b[0] && a[1] == b[1]; }
+
+ORACLE_API int oracle_sugarscape_step(int k, long n, const sg_cols *in, sg_cols *out,
+                                      double radius, double grid_width, int mode, int nthreads) {
+  enum { UNOCCUPIED = 0, OCCUPIED = 1, REQUESTED = 2, UNRESOLVED = 3 };
+  grid_t g;
+  double emin[2] = {0, 0}, emax[2] = {grid_width, grid_width};
+  if (k > 0 && mode == 1) grid_build(&g, 2, n, in->pos, emin, emax, radius);
+#pragma omp parallel num_threads(threads_or_default(nthreads))
+  {
+    long *buf = NULL, cap = 0;
+#pragma omp for schedule(dynamic, 64)
+    for (long i = 0; i < n; i++) {
+      const double *ip = in->pos + 2 * i;
+      if (k == 0) {
+        /* metabolise_and_growback, sugarscape.abl:67-92 */
+        int new_env = in->env_sugar_level[i];
+        if (in->state[i] == OCCUPIED) {
+          int new_sugar = in->sugar_level[i] + in->env_sugar_level[i] - in->metabolism[i];
+          new_env = 0;
+          if (new_sugar <= 0) {
+            out->state[i] = UNOCCUPIED;
+            out->agent_id[i] = -1;
+            out->sugar_level[i] = 0;
+            out->metabolism[i] = 0;
+          } else {
+            out->state[i] = UNRESOLVED;
+            out->sugar_level[i] = new_sugar;
+          }
+        }
+        new_env += 1;
+        if (new_env > in->max_env_sugar_level[i]) new_env = in->max_env_sugar_level[i];
+        out->env_sugar_level[i] = new_env;
+      } else if (k == 1) {
+        /* movement_request, sugarscape.abl:94-113: the first unoccupied
+         * neighbour (ascending index) with the most sugar */
+        if (in->state[i] != UNRESOLVED) continue;
+        int best = -1;
+        double best_pos[2] = {0, 0};
+        FOR_EACH_CANDIDATE(j, i, n, mode, &g, buf, cap, {
+          const double *jp = in->pos + 2 * j;
+          if (dist2(jp, ip) > radius) continue;
+          if (sg_same(jp, ip)) continue;
+          if (in->state[j] == UNOCCUPIED && in->env_sugar_level[j] > best) {
+            best = in->env_sugar_level[j];
+            best_pos[0] = jp[0];
+            best_pos[1] = jp[1];
+          }
+        });
+        if (best > in->env_sugar_level[i]) {
+          out->state[i] = REQUESTED;
+          out->target_pos[2 * i] = best_pos[0];
+          out->target_pos[2 * i + 1] = best_pos[1];
+        } else {
+          out->state[i] = OCCUPIED;
+        }
+      } else if (k == 2) {
+        /* movement_response, sugarscape.abl:115-142: the first requester
+         * (ascending index) whose target is this cell */
+        if (in->state[i] != UNOCCUPIED) continue;
+        int best_priority = -1, best_id = -1, best_sugar = -1, best_metab = -1;
+        FOR_EACH_CANDIDATE(j, i, n, mode, &g, buf, cap, {
+          const double *jp = in->pos + 2 * j;
+          if (dist2(jp, ip) > radius) continue;
+          if (in->state[j] == REQUESTED && sg_same(in->target_pos + 2 * j, ip)) {
+            const int priority = 0;
+            if (priority > best_priority) {
+              best_priority = priority;
+              best_id = in->agent_id[j];
+              best_sugar = in->sugar_level[j];
+              best_metab = in->metabolism[j];
+            }
+          }
+        });
+        if (best_id >= 0) {
+          out->state[i] = OCCUPIED;
+          out->agent_id[i] = best_id;
+          out->sugar_level[i] = best_sugar;
+          out->metabolism[i] = best_metab;
+        }
+      } else {
+        /* movement_transaction, sugarscape.abl:144-160 */
+        if (in->state[i] != REQUESTED) continue;
+        int moved = 0;
+        FOR_EACH_CANDIDATE(j, i, n, mode, &g, buf, cap, {
+          const double *jp = in->pos + 2 * j;
+          if (dist2(jp, ip) > radius) continue;
+          if (in->state[j] == OCCUPIED && in->agent_id[j] == in->agent_id[i]) {
+            moved = 1;
+            out->state[i] = UNOCCUPIED;
+            out->agent_id[i] = -1;
+            out->sugar_level[i] = 0;
+            out->metabolism[i] = 0;
+          }
+        });
+        if (!moved) out->state[i] = OCCUPIED;
+      }
+    }
+    free(buf);
+  }
+  if (k > 0 && mode == 1) grid_free(&g);
+  return 0;
+}
+
 /* ------------------------------------------------------- predator_prey */
 /* examples/predator_prey.abl:26-309.  The reference `c` backend refuses this
  * model (runtime add/remove, src/backend/CBackend.cpp:30-32), so its

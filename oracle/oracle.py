@@ -40,6 +40,7 @@ def lib():
         L.oracle_circle_step.argtypes = [_i, _l, _p, _p, _d, _d, _d, _d, _p, _p, _i, _i, _l, _l]
         L.oracle_boids2d_step.argtypes = [_l, _p, _p, _p, _p, _p, _i, _i, _l, _l]
         L.oracle_init_boids3d.argtypes = [_l, _d, _d, _p, _p]
+        L.oracle_sugarscape_step.argtypes = [_i, _l, _p, _p, _d, _d, _i, _i]
         L.oracle_boids3d_step.argtypes = [_l, _p, _p, _p, _p, _p, _i, _i, _l, _l]
         L.oracle_game_of_life_step.argtypes = [_l, _p, _p, _p, _p, _d, _d, _i, _i, _l, _l]
         _LIB = L
@@ -145,6 +146,40 @@ def game_of_life_step(state, c, mode=1, nthreads=0, first=0, count=None):
     lib().oracle_game_of_life_step(n, _ptr(pos), _ptr(alive), _ptr(po), _ptr(ao), c["radius"],
                                    float(c["size"]), mode, nthreads, first, count)
     return {"pos": po, "alive": ao}
+
+
+SUGARSCAPE_MEMBERS = ("pos", "target_pos", "agent_id", "state", "sugar_level", "metabolism",
+                      "env_sugar_level", "max_env_sugar_level")
+
+
+class _SgCols(ctypes.Structure):
+    _fields_ = [(m, ctypes.c_void_p) for m in SUGARSCAPE_MEMBERS]
+
+
+def _sg_cols(state):
+    return _SgCols(*[state[m].ctypes.data for m in SUGARSCAPE_MEMBERS])
+
+
+class Sugarscape:
+    """examples/sugarscape.abl's simulate loop with the reference's double
+    buffer (src/backend/CPrinter.cpp:189-233): the buffer a step function
+    writes starts as a copy of the population and keeps, in the members the
+    step does not assign, what it held two swaps before."""
+
+    def __init__(self, state, radius=1.5, grid_width=100.0, mode=1, nthreads=0):
+        self.cur = {m: np.array(state[m], copy=True, order="C") for m in SUGARSCAPE_MEMBERS}
+        self.dbuf = {m: v.copy() for m, v in self.cur.items()}
+        self.radius, self.grid_width = float(radius), float(grid_width)
+        self.mode, self.nthreads = mode, nthreads
+
+    def step(self):
+        n = len(self.cur["state"])
+        for k in range(4):
+            a, b = _sg_cols(self.cur), _sg_cols(self.dbuf)
+            lib().oracle_sugarscape_step(k, n, ctypes.byref(a), ctypes.byref(b), self.radius,
+                                         self.grid_width, self.mode, self.nthreads)
+            self.cur, self.dbuf = self.dbuf, self.cur
+        return self.cur
 
 
 STEP = {"circle": circle_step, "circle3d": circle_step, "boids2d": boids2d_step,

@@ -74,3 +74,16 @@ def test_brute_force_oracle_matches_reference(case):
     for t in range(1, 4):
         state = step(state, c, mode=0)
         assert state_hash(meta, state) == meta["sha256"][t], f"step {t}"
+
+
+@pytest.mark.parametrize("mode", [1, 0])
+def test_sugarscape_oracle_matches_reference(mode):
+    """sugarscape 100 x 100: the oracle's four step functions with the
+    reference's double buffer reproduce every golden hash (binned), or the
+    first three timesteps (brute force)."""
+    meta, state = load_case("sugarscape_10000")
+    sim = O.Sugarscape(state, radius=1.5, grid_width=100.0, mode=mode)
+    assert state_hash(meta, sim.cur) == meta["sha256"][0]
+    T = meta["timesteps"] if mode == 1 else 3
+    for t in range(1, T + 1):
+        assert state_hash(meta, sim.step()) == meta["sha256"][t], f"step {t}"
