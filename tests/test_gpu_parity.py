@@ -102,6 +102,24 @@ def test_boids3d_1m_matches_oracle():
     sim.close()
 
 
+def test_sugarscape_1m_matches_oracle():
+    """The sugarscape bench workload (1024 x 1024 grid agents, kept
+    neighbour lists) against the oracle's restatement with the reference's
+    double buffer."""
+    model, g = o.globals_for_config("sugarscape_1m")
+    state = workloads.sugarscape(g.get("grid_width"), g.get("occupiedFrac"), seed=0)
+    sim = o.Simulation(model, g)
+    sim.upload("Agent", state)
+    ref = O.Sugarscape(state, radius=g.get("radius"), grid_width=float(g.get("grid_width")))
+    for t in range(3):
+        sim.step()
+        want = ref.step()
+        got = sim.download("Agent")
+        for k in want:
+            assert np.array_equal(got[k], want[k]), (t, k)
+    sim.close()
+
+
 def test_game_of_life_4096_matches_oracle():
     model, g = o.globals_for_config("game_of_life_4096")
     state = workloads.game_of_life(g.get("size"), 0.5, seed=0)
