@@ -19,6 +19,10 @@
  *                    (builtins at src/main.cpp:65-130, lowered for FlameGPU
  *                    at src/backend/FlameGPUBackend.cpp:204-225)
  *   abl_last_exec_time -> getLastExecTime() (src/main.cpp:66)
+ *   abl_save_state / abl_load_state -> save() (asset/c/libabl.c:46-124),
+ *                    binary and lossless, plus the resume the reference lacks
+ *   abl_set_serial_random -> the one xorshift128+ stream random() draws
+ *                    from (asset/c/libabl.c:8-39), continued in steps
  *
  * Conventions: every call returns 0 or a negative ABL_E_* code (text via
  * abl_strerror); host buffers belong to the caller, device buffers to the
