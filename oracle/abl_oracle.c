@@ -467,6 +467,85 @@ ORACLE_API int oracle_game_of_life_step(long n, const double *pos_in, const uint
   return 0;
 }
 
+/* ---------------------------------------------------- boids2d_flockers */
+/* examples/boids2d_flockers.abl:39-86 as printed by the reference, run as
+ * the reference program runs on one OpenMP thread: agents in index order,
+ * each step's random(float2(-1.0), float2(1.0)) drawing from the one
+ * xorshift stream (y first, as gcc on x86-64 evaluates
+ * float2_create(random_float(..), random_float(..))).  Parameters:
+ * p[0..8] = interaction_radius, steer_scale, collision_scale, match_scale,
+ * randomness_scale, momentum_scale, time_scale, max_pos, (unused).
+ * wraparound is asset/lib.abl's. */
+ORACLE_API int oracle_flockers_step(long n, const double *pos_in, const double *vel_in,
+                                    double *pos_out, double *vel_out, const double *p, int mode) {
+  const double interaction_radius = p[0], steer_scale = p[1], collision_scale = p[2],
+               match_scale = p[3], randomness_scale = p[4], momentum_scale = p[5],
+               time_scale = p[6], max_pos = p[7];
+  grid_t g;
+  double emin[2] = {0, 0}, emax[2] = {max_pos, max_pos};
+  if (mode == 1) grid_build(&g, 2, n, pos_in, emin, emax, interaction_radius);
+  long *buf = NULL, cap = 0;
+  for (long i = 0; i < n; i++) {
+    const double *ip = pos_in + 2 * i;
+    const double *iv = vel_in + 2 * i;
+    double gv[2] = {0, 0}, gc[2] = {0, 0}, av[2] = {0, 0};
+    int interaction_count = 0;
+    FOR_EACH_CANDIDATE(j, i, n, mode, &g, buf, cap, {
+      const double *jp = pos_in + 2 * j;
+      const double *jv = vel_in + 2 * j;
+      if (dist2(jp, ip) > interaction_radius) continue;
+      if (jp[0] == ip[0] && jp[1] == ip[1]) continue;
+      interaction_count += 1;
+      gc[0] = gc[0] + jp[0];
+      gc[1] = gc[1] + jp[1];
+      gv[0] = gv[0] + jv[0];
+      gv[1] = gv[1] + jv[1];
+      const double sep[2] = {ip[0] - jp[0], ip[1] - jp[1]};
+      const double lensquared = sep[0] * sep[0] + sep[1] * sep[1];
+      const double den = lensquared * lensquared + 1;
+      av[0] = av[0] + sep[0] / den;
+      av[1] = av[1] + sep[1] / den;
+    });
+    double vc[2] = {0, 0};
+    if (interaction_count > 0) {
+      gc[0] = gc[0] / interaction_count;
+      gc[1] = gc[1] / interaction_count;
+      vc[0] = vc[0] + (gc[0] - ip[0]) * steer_scale;
+      vc[1] = vc[1] + (gc[1] - ip[1]) * steer_scale;
+      gv[0] = gv[0] / interaction_count;
+      gv[1] = gv[1] / interaction_count;
+      vc[0] = vc[0] + gv[0] * match_scale;
+      vc[1] = vc[1] + gv[1] * match_scale;
+      av[0] = av[0] / interaction_count;
+      av[1] = av[1] / interaction_count;
+      vc[0] = vc[0] + av[0] * collision_scale;
+      vc[1] = vc[1] + av[1] * collision_scale;
+    }
+    double rd[2];
+    const double lo[2] = {-1.0, -1.0}, hi[2] = {1.0, 1.0};
+    draw_vec(rd, 2, lo, hi);
+    const double rl = (double) sqrtf((float) (rd[0] * rd[0] + rd[1] * rd[1]));
+    rd[0] = rd[0] / rl;
+    rd[1] = rd[1] / rl;
+    vc[0] = vc[0] + rd[0] * randomness_scale;
+    vc[1] = vc[1] + rd[1] * randomness_scale;
+    double nv[2] = {iv[0] * momentum_scale + vc[0], iv[1] * momentum_scale + vc[1]};
+    const double scale = (double) sqrtf((float) (nv[0] * nv[0] + nv[1] * nv[1]));
+    if (scale > 0) {
+      nv[0] = nv[0] / scale;
+      nv[1] = nv[1] / scale;
+    }
+    for (int d = 0; d < 2; d++) {
+      const double v = ip[d] + nv[d] * time_scale;
+      pos_out[2 * i + d] = (v < 0) ? (max_pos + v) : ((v >= max_pos) ? (v - max_pos) : v);
+      vel_out[2 * i + d] = nv[d];
+    }
+  }
+  free(buf);
+  if (mode == 1) grid_free(&g);
+  return 0;
+}
+
 /* ---------------------------------------------------------- sugarscape */
 /* examples/sugarscape.abl:67-160, the four step functions as printed by the
  * reference.  Members of `out` a step does not write keep what the double

@@ -39,6 +39,8 @@ CASES = {
                                        "num_timesteps": "100"}, {"use_float": "true"}),
     "boids3d_5000": ("boids", {"num_timesteps": "100"}, {}),
     "sugarscape_10000": ("sugarscape", {"num_timesteps": "100"}, {}),
+    # random() inside the step: recorded on one OpenMP thread (SERIAL_RANDOM)
+    "boids2d_flockers_1000": ("boids2d_flockers", {"num_timesteps": "50"}, {}),
 }
 
 # model -> (example, -C config): whole reference programs at default parameters
@@ -59,7 +61,7 @@ PROGRAMS = {
 
 # Programs whose reference run uses one thread and whose cuda build continues
 # the host stream in steps (-DABL_SERIAL_RANDOM).
-SERIAL_RANDOM = {"boids2d_flockers"}
+SERIAL_RANDOM = {"boids2d_flockers", "boids2d_flockers_1000"}
 
 
 def model_path(example):

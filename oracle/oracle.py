@@ -41,6 +41,7 @@ def lib():
         L.oracle_boids2d_step.argtypes = [_l, _p, _p, _p, _p, _p, _i, _i, _l, _l]
         L.oracle_init_boids3d.argtypes = [_l, _d, _d, _p, _p]
         L.oracle_sugarscape_step.argtypes = [_i, _l, _p, _p, _d, _d, _i, _i]
+        L.oracle_flockers_step.argtypes = [_l, _p, _p, _p, _p, _p, _i]
         L.oracle_boids3d_step.argtypes = [_l, _p, _p, _p, _p, _p, _i, _i, _l, _l]
         L.oracle_game_of_life_step.argtypes = [_l, _p, _p, _p, _p, _d, _d, _i, _i, _l, _l]
         _LIB = L
@@ -146,6 +147,23 @@ def game_of_life_step(state, c, mode=1, nthreads=0, first=0, count=None):
     lib().oracle_game_of_life_step(n, _ptr(pos), _ptr(alive), _ptr(po), _ptr(ao), c["radius"],
                                    float(c["size"]), mode, nthreads, first, count)
     return {"pos": po, "alive": ao}
+
+
+FLOCKERS_KEYS = ("interaction_radius", "steer_scale", "collision_scale", "match_scale",
+                 "randomness_scale", "momentum_scale", "time_scale", "max_pos")
+
+
+def flockers_step(state, c, mode=1):
+    """One timestep of examples/boids2d_flockers.abl as the reference runs it
+    on one thread: random() continues the oracle's xorshift stream (reset by
+    the init_* functions), agent by agent."""
+    pos = np.ascontiguousarray(state["pos"])
+    vel = np.ascontiguousarray(state["velocity"])
+    n = pos.shape[0]
+    po, vo = pos.copy(), vel.copy()
+    p = np.array([c[k] for k in FLOCKERS_KEYS] + [0.0], np.float64)
+    lib().oracle_flockers_step(n, _ptr(pos), _ptr(vel), _ptr(po), _ptr(vo), _ptr(p), mode)
+    return {"pos": po, "velocity": vo}
 
 
 SUGARSCAPE_MEMBERS = ("pos", "target_pos", "agent_id", "state", "sugar_level", "metabolism",

@@ -38,6 +38,7 @@ LAYOUTS = {
     "boids2d": [("pos", "<f8", (2,)), ("velocity", "<f8", (2,))],
     "game_of_life": [("pos", "<f8", (2,)), ("alive", "u1", ())],
     "boids": [("pos", "<f8", (3,)), ("velocity", "<f8", (3,))],
+    "boids2d_flockers": [("pos", "<f8", (2,)), ("velocity", "<f8", (2,))],
     "sugarscape": [("pos", "<f8", (2,)), ("target_pos", "<f8", (2,)), ("agent_id", "<i4", ()),
                    ("state", "<i4", ()), ("sugar_level", "<i4", ()), ("metabolism", "<i4", ()),
                    ("env_sugar_level", "<i4", ()), ("max_env_sugar_level", "<i4", ())],
@@ -69,7 +70,8 @@ def main():
         exe = build_ref.build_case(name)
         d = os.path.dirname(exe)
         dump = os.path.join(d, "dump.bin")
-        env = dict(os.environ, ABL_DUMP=dump, OMP_NUM_THREADS=str(os.cpu_count()))
+        threads = 1 if name in build_ref.SERIAL_RANDOM else os.cpu_count()
+        env = dict(os.environ, ABL_DUMP=dump, OMP_NUM_THREADS=str(threads))
         subprocess.check_call([exe], cwd=d, env=env)
         use_float = config.get("use_float") == "true"
         lay = layout(example, use_float)
@@ -87,7 +89,7 @@ def main():
             "timesteps": len(states) - 1,
             "sha256": hashes,
             "source": "reference c backend (OpenABL -b c) + asset/c/libabl.c, gcc -O2 -std=c99 "
-                      "-fopenmp on x86-64",
+                      "-fopenmp on x86-64" + (", OMP_NUM_THREADS=1" if threads == 1 else ""),
         }
         with open(os.path.join(HERE, name + ".json"), "w") as f:
             json.dump(meta, f, indent=1)

@@ -87,3 +87,22 @@ def test_sugarscape_oracle_matches_reference(mode):
     T = meta["timesteps"] if mode == 1 else 3
     for t in range(1, T + 1):
         assert state_hash(meta, sim.step()) == meta["sha256"][t], f"step {t}"
+
+
+@pytest.mark.parametrize("mode", [1, 0])
+def test_flockers_oracle_matches_single_thread_reference(mode):
+    """boids2d_flockers (random() inside the step), recorded from the
+    reference program on one thread: the oracle's init draws main()'s agents
+    from the xorshift stream, and its steps continue that stream agent by
+    agent; every timestep's state hashes like the reference's."""
+    meta, state = load_case("boids2d_flockers_1000")
+    c = dict(interaction_radius=10.0, steer_scale=0.1, collision_scale=400.0, match_scale=1.0,
+             randomness_scale=0.05, momentum_scale=1.0, time_scale=0.7,
+             max_pos=float("%g" % math.sqrt(1000 / 0.004)))
+    s = O.init_boids2d(meta["agents"], 0.0, c["max_pos"])
+    for k in state:
+        assert np.array_equal(s[k], state[k]), k
+    T = meta["timesteps"] if mode == 1 else 3
+    for t in range(1, T + 1):
+        s = O.flockers_step(s, c, mode=mode)
+        assert state_hash(meta, s) == meta["sha256"][t], f"step {t}"
