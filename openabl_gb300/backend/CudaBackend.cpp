@@ -7,6 +7,10 @@
 //   cuda.model=NAME        identifier of the model inside the runtime (default "model")
 //   cuda.device_init=true  main()'s add() loops run as kernels (CudaPrinter::findDeviceInit)
 //   cuda.seed=N            key of the counter-based random() stream in steps (default 0)
+//   cuda.near_mode=M       how ordered near loops gather neighbours: auto, runs, rows,
+//                          lists or block (abl_set_near_mode; results are identical)
+//   cuda.near_cache=B      keep neighbour lists of agents that never move (default true)
+//   cuda.balance=B         hand a block's agents to threads by neighbour count (default true)
 #include "CudaBackend.hpp"
 
 #include <cctype>
@@ -86,6 +90,18 @@ void CudaBackend::generate(AST::Script &script, const BackendContext &ctx) {
 
   CudaPrinter printer(script, useFloat, model, ctx.config.getBool("cuda.device_init", false),
                       ctx.config.getInt("cuda.seed", 0));
+  auto mode = ctx.config.config.find("cuda.near_mode");
+  if (mode != ctx.config.config.end()) {
+    static const char *const kModes[] = {"auto", "runs", "rows", "lists", "block"};
+    for (int k = 0; k < 5; k++)
+      if (mode->second == kModes[k]) printer.nearMode = k;
+    if (printer.nearMode < 0)
+      throw BackendError("cuda.near_mode must be auto, runs, rows, lists or block");
+  }
+  if (ctx.config.config.count("cuda.near_cache"))
+    printer.nearCache = ctx.config.getBool("cuda.near_cache", true) ? 1 : 0;
+  if (ctx.config.config.count("cuda.balance"))
+    printer.balance = ctx.config.getBool("cuda.balance", true) ? 1 : 0;
   printer.print(script);
   writeToFile(ctx.outputDir + "/" + model + ".cu", printer.extractStr());
   writeToFile(ctx.outputDir + "/" + model + ".globals.json", globalsManifest(script, model));

@@ -1257,6 +1257,13 @@ void CudaPrinter::printHostSimulate() {
     *this << "abl_check(abl_set_seed(ctx, " << std::to_string((unsigned long) seed)
           << "ull), \"abl_set_seed\");" << nl;
   }
+  if (nearMode >= 0)
+    *this << "abl_check(abl_set_near_mode(ctx, " << nearMode << "), \"abl_set_near_mode\");" << nl;
+  if (nearCache >= 0)
+    *this << "abl_check(abl_set_near_cache(ctx, " << nearCache << "), \"abl_set_near_cache\");"
+          << nl;
+  if (balance >= 0)
+    *this << "abl_check(abl_set_balance(ctx, " << balance << "), \"abl_set_balance\");" << nl;
   *this << "abl_check(abl_set_globals(ctx, &abl_G, sizeof abl_G), \"abl_set_globals\");";
   for (size_t ti = 0; ti < script.agents.size() && !devInit.empty(); ti++) {
     const AST::AgentDeclaration &a = *script.agents[ti];

@@ -52,6 +52,13 @@ private:
   bool deviceInit;
   long seed;  // -C cuda.seed: key of random() in steps (abl_set_seed)
 
+public:
+  // Runtime settings the generated main() applies before simulating
+  // (-C cuda.near_mode, cuda.near_cache, cuda.balance); -1: the default.
+  int nearMode = -1, nearCache = -1, balance = -1;
+
+private:
+
   // Device initialisation: main()'s add() loops run as kernels.
   struct DevInit {
     const AST::ForStatement *loop = nullptr;

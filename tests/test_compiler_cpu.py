@@ -186,3 +186,21 @@ def test_step_descriptors(model, step, changed, cacheable):
     if changed is not None:
         assert d["out_changed"] == changed
     assert d["near_cacheable"] == cacheable
+
+
+def test_runtime_settings_options(compiler, tmp_path):
+    """-C cuda.near_mode / cuda.near_cache / cuda.balance become calls in the
+    generated main(); an unknown mode is refused with exit 2."""
+    base = [compiler, "-A", os.path.join(REF, "asset"), "-i",
+            os.path.join(REF, "examples", "boids2d.abl"), "-b", "cuda", "-C", "cuda.model=b"]
+    r = subprocess.run(base + ["-o", str(tmp_path / "a"), "-C", "cuda.near_mode=lists",
+                               "-C", "cuda.near_cache=false", "-C", "cuda.balance=false"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    src = (tmp_path / "a" / "b.cu").read_text()
+    assert 'abl_check(abl_set_near_mode(ctx, 3), "abl_set_near_mode");' in src
+    assert 'abl_check(abl_set_near_cache(ctx, 0), "abl_set_near_cache");' in src
+    assert 'abl_check(abl_set_balance(ctx, 0), "abl_set_balance");' in src
+    r = subprocess.run(base + ["-o", str(tmp_path / "b"), "-C", "cuda.near_mode=fastest"],
+                       capture_output=True, text=True)
+    assert r.returncode == 2
