@@ -66,3 +66,26 @@ def test_served_job_globals_match_compiler_folding():
         n = int(c["globals"]["num_agents"])
         _, g, _ = workloads.served_job(c["model"].replace("_float", ""), n, "fp64", 0)
         assert g.get(key) == float(c["globals"][key]), name
+
+
+def test_every_error_code_has_its_own_text(lib):
+    """abl_strerror (no GPU needed) names every ABL_E_* code the header
+    defines, each differently."""
+    src = open(os.path.join(REPO, "include", "openabl_cuda.h")).read()
+    codes = {n: int(v) for n, v in re.findall(r"#define (ABL_E_\w+) (-\d+)", src)}
+    assert "ABL_E_IO" in codes and len(codes) >= 10
+    lib.abl_strerror.restype = ctypes.c_char_p
+    lib.abl_strerror.argtypes = [ctypes.c_int]
+    texts = {n: lib.abl_strerror(v).decode() for n, v in codes.items()}
+    unknown = lib.abl_strerror(-999).decode()
+    for n, t in texts.items():
+        assert t and t != unknown, n
+    assert len(set(texts.values())) == len(texts)
+
+
+@pytest.mark.parametrize("name", ["kinds", "boids2d_flockers", "ants", "keratinocyte",
+                                  "boids3d", "sugarscape"])
+def test_more_models_are_compiled_in(lib, name):
+    import openabl_gb300 as o
+    m = o.Model(name)
+    assert m.agent_types
