@@ -467,6 +467,103 @@ ORACLE_API int oracle_game_of_life_step(long n, const double *pos_in, const uint
   return 0;
 }
 
+/* ----------------------------------------------------- boids2d (FP32) */
+/* examples/boids2d.abl:43-108 as the reference builds it with
+ * LIBABL_USE_FLOAT (-C use_float=true): abl_float is float, so agents,
+ * globals and every float2 operation of libabl.h are single precision;
+ * length/dist are sqrtf of the float sum of squares.  Parameters as for
+ * oracle_boids2d_step, rounded to float as the printed `float` globals are.
+ * Positions are widened to double for the candidate grid only. */
+static inline float dist2f(const float *a, const float *b) {
+  const float dx = a[0] - b[0], dy = a[1] - b[1];
+  return sqrtf(dx * dx + dy * dy);
+}
+
+ORACLE_API int oracle_boids2d_step_f32(long n, const float *pos_in, const float *vel_in,
+                                       float *pos_out, float *vel_out, const float *p,
+                                       int mode, int nthreads) {
+  const float interaction_radius = p[0], separation_radius = p[1], time_scale = p[2],
+              global_scale = p[3], steer_scale = p[4], collision_scale = p[5],
+              match_scale = p[6], min_pos = p[7], max_pos = p[8];
+  grid_t g;
+  double *posd = NULL;
+  if (mode == 1) {
+    posd = (double *) malloc(sizeof(double) * 2 * (n > 0 ? n : 1));
+    for (long k = 0; k < 2 * n; k++) posd[k] = pos_in[k];
+    double emin[2] = {min_pos, min_pos}, emax[2] = {max_pos, max_pos};
+    grid_build(&g, 2, n, posd, emin, emax, interaction_radius);
+  }
+#pragma omp parallel num_threads(threads_or_default(nthreads))
+  {
+    long *buf = NULL, cap = 0;
+#pragma omp for schedule(dynamic, 64)
+    for (long i = 0; i < n; i++) {
+      const float *ip = pos_in + 2 * i;
+      const float *iv = vel_in + 2 * i;
+      float gv[2] = {0, 0}, gc[2] = {0, 0}, cc[2] = {0, 0};
+      int interaction_count = 0, collision_count = 0;
+      FOR_EACH_CANDIDATE(j, i, n, mode, &g, buf, cap, {
+        const float *jp = pos_in + 2 * j;
+        const float *jv = vel_in + 2 * j;
+        if (dist2f(jp, ip) > interaction_radius) continue;
+        gc[0] = gc[0] + jp[0];
+        gc[1] = gc[1] + jp[1];
+        gv[0] = gv[0] + jv[0];
+        gv[1] = gv[1] + jv[1];
+        interaction_count += 1;
+        const float separation = dist2f(ip, jp);
+        if (separation < separation_radius) {
+          cc[0] = cc[0] + jp[0];
+          cc[1] = cc[1] + jp[1];
+          collision_count += 1;
+        }
+      });
+      float vc[2] = {0, 0}, steer[2] = {0, 0}, match[2] = {0, 0}, avoid[2] = {0, 0};
+      if (interaction_count > 0) {
+        gc[0] = gc[0] / (float) interaction_count;
+        gc[1] = gc[1] / (float) interaction_count;
+        steer[0] = (gc[0] - ip[0]) * steer_scale;
+        steer[1] = (gc[1] - ip[1]) * steer_scale;
+      }
+      vc[0] = vc[0] + steer[0];
+      vc[1] = vc[1] + steer[1];
+      if (interaction_count > 0) {
+        gv[0] = gv[0] / (float) interaction_count;
+        gv[1] = gv[1] / (float) interaction_count;
+        match[0] = gv[0] * match_scale;
+        match[1] = gv[1] * match_scale;
+      }
+      vc[0] = vc[0] + match[0];
+      vc[1] = vc[1] + match[1];
+      if (collision_count > 0) {
+        cc[0] = cc[0] / (float) collision_count;
+        cc[1] = cc[1] / (float) collision_count;
+        avoid[0] = (ip[0] - cc[0]) * collision_scale;
+        avoid[1] = (ip[1] - cc[1]) * collision_scale;
+      }
+      vc[0] = vc[0] + avoid[0];
+      vc[1] = vc[1] + avoid[1];
+      float nv[2] = {iv[0] + vc[0] * global_scale, iv[1] + vc[1] * global_scale};
+      const float scale = sqrtf(nv[0] * nv[0] + nv[1] * nv[1]);
+      if (scale > 1) {
+        nv[0] = nv[0] / scale;
+        nv[1] = nv[1] / scale;
+      }
+      for (int d = 0; d < 2; d++) {
+        const float v = ip[d] + nv[d] * time_scale;
+        pos_out[2 * i + d] = (v < min_pos) ? max_pos : ((v > max_pos) ? min_pos : v);
+        vel_out[2 * i + d] = nv[d];
+      }
+    }
+    free(buf);
+  }
+  if (mode == 1) {
+    grid_free(&g);
+    free(posd);
+  }
+  return 0;
+}
+
 /* ---------------------------------------------------- boids2d_flockers */
 /* examples/boids2d_flockers.abl:39-86 as printed by the reference, run as
  * the reference program runs on one OpenMP thread: agents in index order,

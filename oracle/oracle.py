@@ -42,6 +42,7 @@ def lib():
         L.oracle_init_boids3d.argtypes = [_l, _d, _d, _p, _p]
         L.oracle_sugarscape_step.argtypes = [_i, _l, _p, _p, _d, _d, _i, _i]
         L.oracle_flockers_step.argtypes = [_l, _p, _p, _p, _p, _p, _i]
+        L.oracle_boids2d_step_f32.argtypes = [_l, _p, _p, _p, _p, _p, _i, _i]
         L.oracle_boids3d_step.argtypes = [_l, _p, _p, _p, _p, _p, _i, _i, _l, _l]
         L.oracle_game_of_life_step.argtypes = [_l, _p, _p, _p, _p, _d, _d, _i, _i, _l, _l]
         _LIB = L
@@ -147,6 +148,19 @@ def game_of_life_step(state, c, mode=1, nthreads=0, first=0, count=None):
     lib().oracle_game_of_life_step(n, _ptr(pos), _ptr(alive), _ptr(po), _ptr(ao), c["radius"],
                                    float(c["size"]), mode, nthreads, first, count)
     return {"pos": po, "alive": ao}
+
+
+def boids2d_step_f32(state, c, mode=1, nthreads=0):
+    """One timestep of examples/boids2d.abl as built with LIBABL_USE_FLOAT:
+    float32 state, constants rounded to float like the printed globals."""
+    pos = np.ascontiguousarray(state["pos"], dtype=np.float32)
+    vel = np.ascontiguousarray(state["velocity"], dtype=np.float32)
+    n = pos.shape[0]
+    po, vo = pos.copy(), vel.copy()
+    p = np.array([c[k] for k in BOIDS2D_KEYS] + [0.0], np.float32)
+    lib().oracle_boids2d_step_f32(n, _ptr(pos), _ptr(vel), _ptr(po), _ptr(vo), _ptr(p), mode,
+                                  nthreads)
+    return {"pos": po, "velocity": vo}
 
 
 FLOCKERS_KEYS = ("interaction_radius", "steer_scale", "collision_scale", "match_scale",

@@ -106,3 +106,17 @@ def test_flockers_oracle_matches_single_thread_reference(mode):
     for t in range(1, T + 1):
         s = O.flockers_step(s, c, mode=mode)
         assert state_hash(meta, s) == meta["sha256"][t], f"step {t}"
+
+
+@pytest.mark.parametrize("mode", [1, 0])
+def test_boids2d_fp32_oracle_matches_reference(mode):
+    """boids2d built with LIBABL_USE_FLOAT (-C use_float=true): the oracle's
+    single-precision restatement reproduces the reference's FP32 program every
+    timestep (binned), or the first three (brute force)."""
+    meta, state = load_case("boids2d_4096_float")
+    c = consts(dict(meta, example="boids2d"))
+    s = state
+    T = meta["timesteps"] if mode == 1 else 3
+    for t in range(1, T + 1):
+        s = O.boids2d_step_f32(s, c, mode=mode)
+        assert state_hash(meta, s) == meta["sha256"][t], f"step {t}"
