@@ -274,7 +274,11 @@ int abl_server_destroy(abl_server *s);
  * array of ABL_NOALLOC_SCRATCH_BYTES, which every GPU that loads this library
  * holds until the process exits.  Limits: at most ABL_NOALLOC_MAX_AGENTS
  * agents and ABL_NOALLOC_MAX_CELLS grid cells, and everything must fit the
- * array; larger problems return ABL_E_SCRATCH without touching the GPU.  The
+ * array; larger problems return ABL_E_SCRATCH without touching the GPU.  In
+ * 3D the neighbourhood lists take about 300 bytes per agent, so there the
+ * array runs out near 90,000 agents.  Models whose step calls random(),
+ * removeCurrent() or add(), and models with a sequential step, return
+ * ABL_E_UNSUPPORTED before any GPU work.  The
  * first call on a device, with that device current, looks up the array's
  * address (cudaGetSymbolAddress) and sets up host bookkeeping; make it
  * before any stream capture.  All calls share the array: calls that overlap

@@ -2562,9 +2562,16 @@ int abl_load_state(abl_ctx *ctx, const char *path) {
   if (std::strcmp(h.model, ctx->model->name) != 0 || h.types != (int32_t) ctx->types.size()
       || h.globals_size != ctx->globals.size())
     return ABL_E_IO;
+  // The whole file is read and checked into host buffers first; the context
+  // is changed only once every check has passed, so a truncated or
+  // mismatched file leaves it as it was.
   std::vector<unsigned char> globals(h.globals_size);
   if (std::fread(globals.data(), 1, globals.size(), fc.f) != globals.size()) return ABL_E_IO;
-  ABL_TRY(abl_set_globals(ctx, globals.data(), globals.size()));
+  struct TypeImage {
+    int64_t n = 0;
+    std::vector<std::vector<unsigned char>> cur, dbuf;
+  };
+  std::vector<TypeImage> img(ctx->types.size());
   for (int ti = 0; ti < (int) ctx->types.size(); ti++) {
     const abl_agent_desc &d = ctx->model->agents[ti];
     int64_t n = 0;
@@ -2572,26 +2579,35 @@ int abl_load_state(abl_ctx *ctx, const char *path) {
     if (std::fread(&n, sizeof n, 1, fc.f) != 1 || std::fread(&members, sizeof members, 1, fc.f) != 1
         || members != d.num_members || n < 0 || n > INT32_MAX)
       return ABL_E_IO;
-    std::vector<std::vector<unsigned char>> cur(members), dbuf(members);
-    std::vector<const void *> cols(members);
+    TypeImage &T = img[ti];
+    T.n = n;
+    T.cur.resize(members);
+    T.dbuf.resize(members);
     for (int k = 0; k < members; k++) {
       uint64_t b = 0;
       if (std::fread(&b, sizeof b, 1, fc.f) != 1 || b != member_bytes(d.members[k]))
         return ABL_E_IO;
       const size_t bytes = b * (size_t) n;
-      cur[k].resize(std::max<size_t>(bytes, 1));
-      dbuf[k].resize(std::max<size_t>(bytes, 1));
-      if (bytes > 0 && (std::fread(cur[k].data(), 1, bytes, fc.f) != bytes
-                        || std::fread(dbuf[k].data(), 1, bytes, fc.f) != bytes))
+      T.cur[k].resize(std::max<size_t>(bytes, 1));
+      T.dbuf[k].resize(std::max<size_t>(bytes, 1));
+      if (bytes > 0 && (std::fread(T.cur[k].data(), 1, bytes, fc.f) != bytes
+                        || std::fread(T.dbuf[k].data(), 1, bytes, fc.f) != bytes))
         return ABL_E_IO;
-      cols[k] = cur[k].data();
     }
-    ABL_TRY(abl_upload(ctx, ti, cols.data(), (size_t) n));
+  }
+  if (std::fgetc(fc.f) != EOF) return ABL_E_IO;  // trailing bytes: not this model's file
+  ABL_TRY(abl_set_globals(ctx, globals.data(), globals.size()));
+  for (int ti = 0; ti < (int) ctx->types.size(); ti++) {
+    const abl_agent_desc &d = ctx->model->agents[ti];
+    TypeImage &T = img[ti];
+    std::vector<const void *> cols(d.num_members);
+    for (int k = 0; k < d.num_members; k++) cols[k] = T.cur[k].data();
+    ABL_TRY(abl_upload(ctx, ti, cols.data(), (size_t) T.n));
     TypeState &t = ctx->types[ti];
-    for (int k = 0; k < members; k++) {
-      const size_t bytes = member_bytes(d.members[k]) * (size_t) n;
+    for (int k = 0; k < d.num_members; k++) {
+      const size_t bytes = member_bytes(d.members[k]) * (size_t) T.n;
       if (bytes == 0) continue;
-      ABL_CUDA_TRY(cudaMemcpyAsync(t.cols[1 - t.cur][k], dbuf[k].data(), bytes,
+      ABL_CUDA_TRY(cudaMemcpyAsync(t.cols[1 - t.cur][k], T.dbuf[k].data(), bytes,
                                    cudaMemcpyHostToDevice, ctx->stream));
     }
     ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -2888,6 +2904,15 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
   if (!model || !globals || !in_cols || !out_cols) return ABL_E_INVALID;
   if (globals_size != model->globals_size) return ABL_E_INVALID;
   if (model->num_agent_types != 1 || model->num_steps != 1) return ABL_E_UNSUPPORTED;
+  // A sequential step needs the context's events and reductions; removal and
+  // addition resize the population (an allocation); random() is keyed by a
+  // timestep and seed that this entry point does not take.  All are refused
+  // before any GPU work.
+  if (model->seq_step) return ABL_E_UNSUPPORTED;
+  {
+    const abl_step_desc &s0 = model->steps[0];
+    if (s0.uses_remove || s0.add_type >= 0 || s0.uses_rng) return ABL_E_UNSUPPORTED;
+  }
   if ((long) n > kNoAllocMaxAgents) return ABL_E_SCRATCH;
   const abl_agent_desc &ad = model->agents[0];
   if (ad.num_members > ABL_MAX_MEMBERS) return ABL_E_UNSUPPORTED;

@@ -19,7 +19,9 @@ import tempfile
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
 REPO = os.path.dirname(PKG)
-REF = os.environ.get("OPENABL_REF", "/root/reference")
+# The OpenABL source tree: $OPENABL_REF, else a `reference` directory beside
+# this repository.
+REF = os.environ.get("OPENABL_REF") or os.path.join(os.path.dirname(REPO), "reference")
 COMPILER = os.path.join(REPO, "_build", "compiler", "openabl")
 
 # model name -> (example file, -C config)

@@ -21,9 +21,11 @@ import os
 import subprocess
 import sys
 
-REF = os.environ.get("OPENABL_REF", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
+# The OpenABL source tree: $OPENABL_REF, else a `reference` directory beside
+# this repository.
+REF = os.environ.get("OPENABL_REF") or os.path.join(os.path.dirname(REPO), "reference")
 OUT = os.path.join(HERE, "_ref")
 COMPILER = os.path.join(REPO, "_build", "compiler", "openabl")
 

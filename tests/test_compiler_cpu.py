@@ -25,7 +25,9 @@ import sys
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("OPENABL_REF", "/root/reference")
+# The OpenABL source tree: $OPENABL_REF, else a `reference` directory beside
+# this repository.
+REF = os.environ.get("OPENABL_REF") or os.path.join(os.path.dirname(REPO), "reference")
 COMPILER = os.path.join(REPO, "_build", "compiler", "openabl")
 GEN = os.path.join(REPO, "openabl_gb300", "generated")
 

@@ -100,3 +100,34 @@ def test_state_of_another_model_is_refused(tmp_path):
         b.load_state(tmp_path / "missing.bin")
     assert e.value.code == -10
     b.close()
+
+
+def test_truncated_state_leaves_the_context_unchanged(tmp_path):
+    """A file cut short is refused before anything is applied: the context
+    keeps its own globals, agents and timestep."""
+    model, g = o.globals_for_config("game_of_life_64")
+    a = o.Simulation(model, g)
+    a.upload("Cell", workloads.game_of_life(64, 0.5, seed=1))
+    a.run(2)
+    a.save_state(tmp_path / "full.bin")
+    a.close()
+    data = (tmp_path / "full.bin").read_bytes()
+    (tmp_path / "cut.bin").write_bytes(data[: len(data) - 100])
+    (tmp_path / "long.bin").write_bytes(data + b"\0")
+
+    b = o.Simulation(model, g)
+    b.upload("Cell", workloads.game_of_life(64, 0.5, seed=7))
+    b.run(3)
+    before = b.download("Cell")
+    for bad in ("cut.bin", "long.bin"):
+        with pytest.raises(o.AblError) as e:
+            b.load_state(tmp_path / bad)
+        assert e.value.code == -10
+        assert_same(b.download("Cell"), before)
+    b.run(1)
+    c = o.Simulation(model, g)
+    c.upload("Cell", workloads.game_of_life(64, 0.5, seed=7))
+    c.run(4)
+    assert_same(b.download("Cell"), c.download("Cell"))
+    b.close()
+    c.close()

@@ -21,7 +21,8 @@ from golden_io import load_case
 
 pytestmark = pytest.mark.gpu
 
-CASES = [("boids2d_4096", "Boid"), ("game_of_life_64", "Cell"), ("circle_4000", "Point")]
+CASES = [("boids2d_4096", "Boid"), ("game_of_life_64", "Cell"), ("circle_4000", "Point"),
+         ("circle3d_4000", "Point")]
 
 
 def _entry():
@@ -87,3 +88,29 @@ def test_noalloc_rejects_problems_beyond_its_scratch():
     rc = step(model.ptr, ctypes.addressof(g.buf), model.globals_size, cols, cols, n, None)
     assert rc == -9
     assert b"scratch" in o.library().abl_strerror(rc)
+
+
+def test_noalloc_rejects_3d_problems_whose_lists_do_not_fit():
+    """In 3D the neighbourhood lists take about 300 bytes per agent, so the
+    fixed array runs out well below the agent limit (near 90,000 agents)."""
+    torch = pytest.importorskip("torch")
+    model, g = o.globals_for_config("circle3d_4000")
+    step = _entry()
+    dummy = torch.zeros(16, dtype=torch.float64, device="cuda")
+    cols = (ctypes.c_void_p * 1)(dummy.data_ptr())
+    rc = step(model.ptr, ctypes.addressof(g.buf), model.globals_size, cols, cols, 120000, None)
+    assert rc == -9
+
+
+def test_noalloc_refuses_models_it_cannot_step_without_allocating():
+    """random() in a step (its stream is keyed by a timestep this entry point
+    does not take) and several agent types are refused before any GPU work."""
+    torch = pytest.importorskip("torch")
+    step = _entry()
+    dummy = torch.zeros(16, dtype=torch.float64, device="cuda")
+    cols = (ctypes.c_void_p * 16)(*([dummy.data_ptr()] * 16))
+    for name in ("boids2d_flockers", "predator_prey"):
+        model = o.Model(name)
+        g = model.default_globals()
+        rc = step(model.ptr, ctypes.addressof(g.buf), model.globals_size, cols, cols, 4, None)
+        assert rc == -6, name
