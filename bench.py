@@ -30,7 +30,10 @@ sys.path.insert(0, REPO)
 CONFIG = "boids2d_1m"
 METRIC = "agent-steps/s (1M boids2d fp64)"
 BYTES_PER_AGENT_STEP = 80        # SoA pos+vel read + written, binning key/id written + read
-FP64_FLOP_PER_AGENT_STEP = 560   # ~72 candidates x 5 + ~25 in-radius x 8 FP64 ops
+# FP64 instructions per agent executed by update_boid on this workload (ncu
+# smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on.sum / agents, one
+# launch).  The FP32 band decides most radius tests without FP64.
+UPDATE_BOID_FP64_INSTR = {"dadd": 122, "dmul": 18, "dfma": 8}
 # DRAM bytes of one update_boid launch on this workload (ncu capture, L2 cold
 # as in the timed steps, which flush L2 first).
 UPDATE_BOID_DRAM_BYTES = 240.00e6
@@ -82,8 +85,9 @@ def job_rate(world, agents, steps, seconds):
 
 
 def cpu_reference_sample(state, consts, target_seconds, n_total):
-    """Brute-force reference step (every agent scans all agents) on a bounded
-    sample of agents, all host threads.  Returns (agent-steps/s, sample, cores)."""
+    """Brute-force reference step (every agent scans all agents: the `c`
+    backend's near loop, CPrinter.cpp:148-173) on a bounded sample of agents,
+    all host threads.  Returns (agent-steps/s, sample, cores, seconds)."""
     from oracle import oracle as O
     cores = os.cpu_count() or 1
     count = 512
@@ -95,6 +99,30 @@ def cpu_reference_sample(state, consts, target_seconds, n_total):
     O.boids2d_step(state, consts, mode=0, nthreads=cores, first=0, count=count)
     dt = time.perf_counter() - t0
     return count / dt, count, cores, dt
+
+
+def cpu_whole_steps(step, state, agents, target_seconds, max_steps=1000):
+    """Whole timesteps of a CPU oracle step function `step(state) -> state`
+    (all host threads), repeated until `target_seconds` have passed.
+    Returns (agent-steps/s, timesteps, seconds)."""
+    t0 = time.perf_counter()
+    k = 0
+    while k < max_steps:
+        state = step(state)
+        k += 1
+        if time.perf_counter() - t0 >= target_seconds:
+            break
+    dt = time.perf_counter() - t0
+    return agents * k / dt, k, dt
+
+
+def binned_cpu_baseline(kind_label, step, state, agents, target_seconds):
+    """`cpu_baseline` object for a CPU oracle timed on whole timesteps."""
+    rate, k, dt = cpu_whole_steps(step, state, agents, target_seconds)
+    return {"value": rate, "unit": "agent-steps/s", "cores": os.cpu_count() or 1,
+            "kind": "port",
+            "sample": f"{kind_label}: {k} whole timesteps of all {agents} agents from the "
+                      f"initial state, {dt:.1f} s, all host threads"}
 
 
 class ClockSampler:
@@ -275,6 +303,12 @@ def measure_other_workloads(args, o, W, np):
     out["circle_4000"] = {"value": 4000 * 100 / sim.last_exec_time(), "unit": "agent-steps/s",
                           "ms_per_step": sim.last_exec_time() * 10.0}
     sim.close()
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    cc = {"r": g.get("r"), "k_rep": g.get("k_rep"), "k_att": g.get("k_att"), "W": g.get("W")}
+    out["circle_4000"]["cpu_baseline"] = binned_cpu_baseline(
+        "brute-force near loop (the reference c backend's algorithm, oracle/abl_oracle.c "
+        "mode 0)", lambda s_: O.circle_step(s_, cc, mode=0, nthreads=cores), st, 4000, 3.0)
     # game of life 4096^2, 50% live, 100 timesteps
     model, g = o.globals_for_config("game_of_life_4096")
     st = W.game_of_life(g.get("size"), 0.5, seed=0)
@@ -302,9 +336,12 @@ def measure_other_workloads(args, o, W, np):
         "bound": "hbm", "kernel": "step_move", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
         "frac": gbs / hbm_peak, "kernel_ms": kernel_s * 1e3, "bytes_per_agent": GOL_BYTES_PER_CELL,
         "traffic": GOL_DRAM_BYTES_4096,
-        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
-                          "(profiles/step_move_game_of_life_4096.md)"}
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch"}
     sim.close()
+    gc = {"radius": g.get("radius"), "size": g.get("size")}
+    out["game_of_life_4096"]["cpu_baseline"] = binned_cpu_baseline(
+        "binned CPU oracle (oracle/abl_oracle.c mode 1)",
+        lambda s_: O.game_of_life_step(s_, gc, mode=1, nthreads=cores), st, n, 5.0)
     # boids (3D), 1,048,576 agents (~9 per interaction cell), and sugarscape
     # on a 1024 x 1024 grid, 100 timesteps each
     for name, cfg, agent, make in (
@@ -323,6 +360,15 @@ def measure_other_workloads(args, o, W, np):
         out[name] = {"value": n * 100 / sim.last_exec_time(), "unit": "agent-steps/s",
                      "ms_per_step": sim.last_exec_time() * 10.0, "agents": n}
         sim.close()
+        if name == "boids3d_1m":
+            bc = {k: g.get(k) for k in O.BOIDS2D_KEYS}
+            stepf = (lambda bc_: lambda s_: O.boids3d_step(s_, bc_, mode=1, nthreads=cores))(bc)
+        else:
+            sg = O.Sugarscape(st, radius=g.get("radius"), grid_width=float(g.get("grid_width")),
+                              nthreads=cores)
+            stepf = (lambda sg_: lambda s_: sg_.step())(sg)
+        out[name]["cpu_baseline"] = binned_cpu_baseline(
+            "binned CPU oracle (oracle/abl_oracle.c mode 1)", stepf, st, n, 5.0)
     # predator_prey, 500 timesteps, FP64 and FP32
     from pp_setup import case
     cfg, st, consts = case("predator_prey_1m")
@@ -352,10 +398,89 @@ def measure_other_workloads(args, o, W, np):
         "metric": "relative difference of the per-timestep counts (prey, predators, available "
                   "grass) between the FP32 and FP64 runs",
         "max_at_step_100": float(rel[:100].max()), "max_over_500": float(rel.max())}
+    out["predator_prey_fp32_vs_fp64"].update(pp_agent_error(o, np, cfg, st))
+    # CPU baselines: the oracle's restatement (the reference `c` backend
+    # refuses this model), binned, all host threads, whole timesteps
+    for name, cls in (("predator_prey_1m", O.PredatorPrey),
+                      ("predator_prey_float_1m", O.PredatorPreyF32)):
+        st_ = st
+        if cls is O.PredatorPreyF32:
+            st_ = {t: {k: (v.astype(np.float32) if v.dtype.kind == "f" else v)
+                       for k, v in d.items()} for t, d in st.items()}
+        ref = cls(st_, consts, seed=1)
+        t0 = time.perf_counter()
+        k, agent_steps = 0, 0
+        while True:
+            agent_steps += sum(ref._fn("oracle_pp_count")(ref.h, i) for i in range(3))
+            ref.run(1, mode=1, nthreads=cores)
+            k += 1
+            if time.perf_counter() - t0 >= 5.0:
+                break
+        dt = time.perf_counter() - t0
+        ref.close()
+        out[name]["cpu_baseline"] = {
+            "value": agent_steps / dt, "unit": "agent-steps/s", "cores": cores, "kind": "port",
+            "sample": f"binned CPU restatement (oracle/abl_oracle.c predator_prey): {k} whole "
+                      f"timesteps from the initial state, {dt:.1f} s, all host threads"}
     return out
 
 
+def pp_agent_error(o, np, cfg, st, steps=100):
+    """Per-agent error of the FP32 predator_prey run against the FP64 run
+    while the two runs have the same populations.  Births and deaths are
+    decided by comparisons, so once one comparison flips, the populations
+    differ and agents are no longer matched by index."""
+    sims = []
+    for name in ("predator_prey", "predator_prey_float"):
+        model = o.Model(name)
+        g = model.default_globals().update(cfg["globals"])
+        sim = o.Simulation(model, g)
+        sim.set_seed(1)
+        fd = np.float32 if model.float_bytes == 4 else np.float64
+        for t, cols in st.items():
+            sim.upload(t, {k: (v.astype(fd) if v.dtype.kind == "f" else v)
+                           for k, v in cols.items()})
+        sims.append(sim)
+    L = float(cfg["globals"]["env_size"])
+    last_matched, errs = 0, {}
+    for t in range(1, steps + 1):
+        for sim in sims:
+            sim.step()
+        a = {ty: sims[0].download(ty) for ty in ("Predator", "Prey")}
+        b = {ty: sims[1].download(ty) for ty in ("Predator", "Prey")}
+        if any(len(a[ty]["pos"]) != len(b[ty]["pos"]) for ty in a):
+            break
+        d = np.concatenate([np.abs(b[ty]["pos"].astype(np.float64) - a[ty]["pos"]).max(axis=1)
+                            for ty in a]) / L
+        last_matched = t
+        if t in (1, 10, 100) or t == steps:
+            errs[f"step_{t}"] = {"pos_rel_err_max": float(d.max()),
+                                 "pos_rel_err_median": float(np.median(d)),
+                                 "pos_rel_err_p99": float(np.quantile(d, 0.99)),
+                                 "frac_le_1e-5": float((d <= 1e-5).mean())}
+    for sim in sims:
+        sim.close()
+    return {"agent_error_metric": "per animal max |pos32 - pos64| / env_size while the "
+                                  "populations agree",
+            "populations_agree_through_step": last_matched, "agent_error": errs}
+
+
+def headline_config(n, world):
+    """`config` of the headline line, the same for both arms."""
+    return {"workload": "boids2d 1,048,576 agents FP64, agent_density 3200.0, "
+                        "per-step bit-exact", "agents": n, "cell": "0.05 (+2^-10)",
+            "l2": "flushed (256 MB write) before every timed timestep (GPU arm)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def run_reference(args):
+    """The reference's own algorithm for the path -- the `c` backend's
+    brute-force near loop (src/backend/CPrinter.cpp:148-173), restated in
+    oracle/abl_oracle.c and pinned bit for bit to the reference programs --
+    on all host cores.  One whole timestep of 1,048,576 agents is ~10^12
+    distance tests, so each step here is a bounded sample: a block of agents
+    each scanning all N agents; `ms_per_step` is that sample's wall time and
+    `value` the agent-steps per second it achieved."""
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
@@ -366,26 +491,30 @@ def run_reference(args):
     state = W.boids2d(n, float(g["max_pos"]), seed=0)
     from oracle import oracle as O
     consts = {k: float(g[k]) for k in O.BOIDS2D_KEYS}
-    per_step = max(1.0, 60.0 / max(1, args.steps + args.warmup))
+    per_step = min(10.0, max(1.0, 120.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
-        cpu_reference_sample(state, consts, min(per_step, 2.0), n)
-    rates = []
-    sample = 0
+        cpu_reference_sample(state, consts, min(per_step, 1.0), n)
+    secs, samples = [], []
     cores = os.cpu_count()
     for _ in range(args.steps):
-        r, sample, cores, _ = cpu_reference_sample(state, consts, per_step, n)
-        rates.append(r)
-    value = statistics.mean(rates)
+        r, sample, cores, dt = cpu_reference_sample(state, consts, per_step, n)
+        secs.append(dt)
+        samples.append(sample)
+    value = sum(samples) / sum(secs)
+    mean_sample = int(statistics.mean(samples))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "agent-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * n / value, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, uniform positions)",
-        "config": {"workload": "boids2d 1,048,576 agents FP64, agent_density 3200.0",
-                   "agents": n, "l2": "n/a (host)"},
+        "ms_per_step": 1000.0 * sum(secs) / len(secs), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded: uniform positions, unit-circle headings, speed U[0.5,1])",
+        "config": headline_config(n, 1),
+        "step_definition": f"one bounded sample: ~{mean_sample} of {n} agents, each scanning "
+                           f"all agents (a whole timestep would take {n / value:.0f} s)",
         "cpu_baseline": {"value": value, "unit": "agent-steps/s", "cores": cores, "kind": "port",
                          "sample": f"brute-force near loop (reference c backend algorithm, "
-                                   f"oracle/abl_oracle.c) for {sample} of {n} agents per step"},
+                                   f"oracle/abl_oracle.c), ~{mean_sample} of {n} agents per "
+                                   f"step, extrapolated to agent-steps/s"},
         "e2e": {"value": value, "unit": "agent-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -442,6 +571,21 @@ def run_ours(args):
     total = slowest_rank_seconds(sum(times), world)
     value = job_rate(world, n, args.steps, total)
 
+    # Boids flock over time, so later timesteps have more neighbours: the
+    # average over the configuration's whole run (timesteps 1..100) too.
+    ts = times
+    if args.steps < 100:
+        sim.upload("Boid", state)
+        ts = []
+        for _ in range(100):
+            flush.zero_()
+            torch.cuda.synchronize()
+            sim.step()
+            ts.append(sim.last_exec_time())
+    run100 = {"value": n * len(ts[:100]) / sum(ts[:100]), "unit": "agent-steps/s",
+              "ms_per_step": 1000.0 * sum(ts[:100]) / len(ts[:100]),
+              "timesteps": f"1..{len(ts[:100])}, L2 flushed before each"}
+
     # graph replay of the same timesteps, back to back (no flush)
     sim.upload("Boid", state)
     sim.run(args.steps)
@@ -462,8 +606,10 @@ def run_ours(args):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     achieved_gbs = BYTES_PER_AGENT_STEP * n / kernel_s / 1e9
     dfma, dadd, dmul = o.runtime.fp64_rates()
-    fp64_peak_tflops = 2 * dfma / 1e12
-    achieved_fp64 = FP64_FLOP_PER_AGENT_STEP * n / kernel_s / 1e12
+    # FP64 floor of the kernel: its executed FP64 instructions, each class at
+    # its own measured issue rate (DADD, DMUL, DFMA share the FP64 pipe).
+    rate = {"dadd": dadd, "dmul": dmul, "dfma": dfma}
+    fp64_floor_s = n * sum(c / rate[k] for k, c in UPDATE_BOID_FP64_INSTR.items())
 
     # end to end through the C ABI: pinned host state in, step, state out
     pin = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in state.items()}
@@ -490,14 +636,21 @@ def run_ours(args):
         forms["serving"] = measure_serving(args, o, W, np)
         forms["other_workloads"] = measure_other_workloads(args, o, W, np)
 
-    cpu = None
+    cpu = cpu_bf = None
     if rank == 0:
         from oracle import oracle as O
         consts = {k: g.get(k) for k in O.BOIDS2D_KEYS}
-        rate, sample, cores, dt = cpu_reference_sample(state, consts, args.cpu_seconds, n)
-        cpu = {"value": rate, "unit": "agent-steps/s", "cores": cores, "kind": "port",
-               "sample": f"brute-force near loop (reference c backend algorithm restated in "
-                         f"oracle/abl_oracle.c) for {sample} of {n} agents, {dt:.1f} s"}
+        cores = os.cpu_count() or 1
+        cpu = binned_cpu_baseline(
+            "binned CPU oracle (oracle/abl_oracle.c mode 1: the reference c backend's "
+            "arithmetic and neighbour order, uniform-grid candidates)",
+            lambda st: O.boids2d_step(st, consts, mode=1, nthreads=cores), state, n,
+            args.cpu_seconds)
+        rate_bf, sample, cores, dt = cpu_reference_sample(state, consts, args.cpu_seconds, n)
+        cpu_bf = {"value": rate_bf, "unit": "agent-steps/s", "cores": cores, "kind": "port",
+                  "sample": f"brute-force near loop (the reference c backend's algorithm, "
+                            f"CPrinter.cpp:148-173, restated in oracle/abl_oracle.c): "
+                            f"extrapolated from {sample} of {n} agents, {dt:.1f} s"}
     sim.close()
     if rank != 0:
         return 0
@@ -506,28 +659,29 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded: uniform positions, unit-circle headings, speed U[0.5,1])",
-        "config": {"workload": "boids2d 1,048,576 agents FP64, agent_density 3200.0, "
-                               "per-step bit-exact", "agents": n, "cell": "0.05 (+2^-10)",
-                   "l2": "flushed (256 MB write) before every timed timestep",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": headline_config(n, world),
         "graph_replay_value": graph_rate,
+        "timesteps_1_100": run100,
         "e2e": {"value": e2e_value, "unit": "agent-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": h2d},
         "roofline": {"bound": "hbm", "kernel": "update_boid", "achieved": achieved_gbs,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
                      "traffic": UPDATE_BOID_DRAM_BYTES,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one "
-                                       "launch (profiles/update_boid_boids2d_1m.md)",
+                                       "launch, L2 cold",
                      "bytes_per_agent": BYTES_PER_AGENT_STEP,
                      "kernel_ms": kernel_s * 1e3, "peak_source": "measured (MEASURED_PEAKS.json)"},
-        "fp64": {"achieved_tflops": achieved_fp64, "peak_tflops": fp64_peak_tflops,
-                 "frac": achieved_fp64 / fp64_peak_tflops,
-                 "flop_per_agent": FP64_FLOP_PER_AGENT_STEP,
-                 "peak_source": "measured DFMA rate (abl_diag_fp64_rates)",
-                 "dadd_per_s": dadd, "dmul_per_s": dmul},
+        "fp64": {"instr_per_agent": UPDATE_BOID_FP64_INSTR,
+                 "instr_source": "ncu executed DADD/DMUL/DFMA of one launch / agents",
+                 "rates_per_s": rate, "rates_source": "measured (abl_diag_fp64_rates)",
+                 "floor_ms": fp64_floor_s * 1e3, "kernel_ms": kernel_s * 1e3,
+                 "frac": fp64_floor_s / kernel_s},
         "gpu_launches": launches,
         "clocks": clock_info,
         "cpu_baseline": cpu,
+        "cpu_baseline_brute_force": cpu_bf,
+        "speedup_vs_cpu_baseline": value / cpu["value"] if cpu else None,
+        "e2e_speedup_vs_cpu_baseline": e2e_value / cpu["value"] if cpu else None,
     }
     line.update(forms)
     print(json.dumps(line))

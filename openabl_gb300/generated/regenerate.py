@@ -59,6 +59,10 @@ CONFIGS = {
                                              "num_timesteps": "100"}),
     "boids2d_float_1m": ("boids2d_float", {"num_agents": "1048576", "agent_density": "3200.0",
                                            "num_timesteps": "100"}),
+    "circle_float_4000": ("circle_float", {"num_agents": "4000", "rho": "0.1",
+                                           "num_timesteps": "100"}),
+    "circle3d_float_4000": ("circle3d_float", {"num_agents": "4000", "rho": "0.01",
+                                               "num_timesteps": "50"}),
     "game_of_life_64": ("game_of_life", {"num_agents": "4096", "alive_fraction": "0.5",
                                          "num_timesteps": "100"}),
     "game_of_life_4096": ("game_of_life", {"num_agents": "16777216", "alive_fraction": "0.5",
@@ -69,6 +73,14 @@ CONFIGS = {
                                            "predator_fraction": "0.1", "num_timesteps": "500"}),
     "predator_prey_small": ("predator_prey", {"num_agents": "20000", "prey_fraction": "0.4",
                                               "predator_fraction": "0.1", "num_timesteps": "50"}),
+    "predator_prey_float_1m": ("predator_prey_float", {"num_agents": "2000000",
+                                                       "prey_fraction": "0.4",
+                                                       "predator_fraction": "0.1",
+                                                       "num_timesteps": "500"}),
+    "predator_prey_float_small": ("predator_prey_float", {"num_agents": "20000",
+                                                          "prey_fraction": "0.4",
+                                                          "predator_fraction": "0.1",
+                                                          "num_timesteps": "50"}),
     # examples/boids.abl (3D) at its defaults: 5,000 agents, agent_density 1000.
     "boids3d_5000": ("boids3d", {"num_timesteps": "100"}),
     # 1,048,576 agents at 16 per unit volume: ~9 agents per interaction cell.

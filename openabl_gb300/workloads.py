@@ -8,15 +8,34 @@ path and into the CPU oracle.
 import numpy as np
 
 
+def unit_vectors(rng, n, dim):
+    """n directions uniform on the circle (dim 2) or sphere (dim 3): points
+    drawn uniformly in the cube [-1, 1)^dim, kept when inside the unit ball
+    (and not within 1e-6 of the centre), divided by their length.  Only
+    correctly rounded operations (+, *, /, sqrt) are used, so every host
+    builds the same bits from the same seed (sin/cos/log differ by an ulp
+    between math libraries)."""
+    out = np.empty((0, dim))
+    while len(out) < n:
+        m = int((n - len(out)) * (1.3 if dim == 2 else 2.0)) + 64
+        c = rng.uniform(-1.0, 1.0, size=(m, dim))
+        r2 = c[:, 0] * c[:, 0] + c[:, 1] * c[:, 1]
+        if dim == 3:
+            r2 = r2 + c[:, 2] * c[:, 2]
+        keep = (r2 <= 1.0) & (r2 > 1e-12)
+        out = np.concatenate([out, c[keep] / np.sqrt(r2[keep])[:, None]])
+    return np.ascontiguousarray(out[:n])
+
+
 def boids2d(n, max_pos, seed=0, vmax=1.0):
     """Positions uniform in [0, max_pos)^2; velocity directions uniform on the
     circle with speed uniform in [0.5, 1] * vmax (the speed cap of
     examples/boids2d.abl:98-101 is 1)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     pos = rng.uniform(0.0, max_pos, size=(n, 2))
-    theta = rng.uniform(0.0, 2.0 * np.pi, size=n)
+    d = unit_vectors(rng, n, 2)
     speed = rng.uniform(0.5, 1.0, size=n) * vmax
-    vel = np.stack([np.cos(theta) * speed, np.sin(theta) * speed], axis=1)
+    vel = d * speed[:, None]
     return {"pos": np.ascontiguousarray(pos), "velocity": np.ascontiguousarray(vel)}
 
 
@@ -39,15 +58,17 @@ def game_of_life(size, alive_fraction=0.5, seed=0):
 
 def predator_prey(n_pred, n_prey, n_grass, env_size, gain_pred=35, gain_prey=60, seed=0):
     """Uniform positions in [0, env_size)^2 for all three types; animals get a
-    heading (sin phi, cos phi) with phi uniform in [0, 2 pi) and zero steer, as
-    examples/predator_prey.abl:87-90 and :316-333 initialise them, and life
-    GAIN_FROM_FOOD + an integer uniform in [0, 10]; grass starts available."""
+    heading uniform on the circle (examples/predator_prey.abl:87-90 draws it
+    as (sin phi, cos phi); here it is drawn without sin/cos so that every
+    host builds the same bits) and zero steer, as :316-333 initialise them,
+    and life GAIN_FROM_FOOD + an integer uniform in [0, 10]; grass starts
+    available."""
     rng = np.random.Generator(np.random.PCG64(seed))
 
     def animals(n, gain):
-        phi = rng.uniform(0.0, 2.0 * np.pi, size=n)
-        return {"pos": rng.uniform(0.0, env_size, size=(n, 2)),
-                "dir": np.stack([np.sin(phi), np.cos(phi)], axis=1),
+        pos = rng.uniform(0.0, env_size, size=(n, 2))
+        return {"pos": pos,
+                "dir": unit_vectors(rng, n, 2),
                 "steer": np.zeros((n, 2)),
                 "life": (gain + rng.integers(0, 11, size=n)).astype(np.int32)}
 
@@ -171,8 +192,7 @@ def boids3d(n, max_pos, seed=0, vmax=1.0):
     [0.5, 1] * vmax."""
     rng = np.random.Generator(np.random.PCG64(seed))
     pos = rng.uniform(0.0, max_pos, size=(n, 3))
-    d = rng.normal(size=(n, 3))
-    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d = unit_vectors(rng, n, 3)
     vel = d * (rng.uniform(0.5, 1.0, size=n) * vmax)[:, None]
     return {"pos": np.ascontiguousarray(pos), "velocity": np.ascontiguousarray(vel)}
 

@@ -774,7 +774,8 @@ ORACLE_API int oracle_sugarscape_step(int k, long n, const sg_cols *in, sg_cols 
  *    SC'11) with key (seed low, seed high) and counter (agent index, step
  *    function index in simulate order, timestep, draw number); a draw's 64
  *    bits (words 0 and 1) give u = (bits >> 11) * 2^-53 and
- *    random(lo, hi) = lo + u * (hi - lo);
+ *    random(lo, hi) = lo + u * (hi - lo), evaluated in abl_float (the one
+ *    draw of the model, random(1.0), is therefore (abl_float) u);
  *  - the sequential step gather_stats runs after the parallel steps of every
  *    timestep (src/AnalysisVisitor.cpp:695-704).
  * Arithmetic follows the printed step bodies (float2 ops component-wise,
@@ -807,200 +808,15 @@ static void philox_next4(pp_rng *R, uint32_t out[4]) {
   out[3] = x3;
 }
 
-static double pp_uniform(pp_rng *R, double lo, double hi) {
+/* A draw's 53-bit uniform in [0, 1). */
+static double pp_unit(pp_rng *R) {
   uint32_t x[4];
   philox_next4(R, x);
   uint64_t b = (((uint64_t) x[0] << 32) | x[1]) >> 11;
-  double u = (double) b * (1.0 / 9007199254740992.0);
-  return lo + u * (hi - lo);
+  return (double) b * (1.0 / 9007199254740992.0);
 }
 
 enum { PP_PRED = 0, PP_PREY = 1, PP_GRASS = 2 };
-
-typedef struct {
-  long n, cap;
-  double *pos, *dir, *steer; /* cap x 2 (dir/steer: animals only) */
-  int *life;                 /* animals */
-  int *dead_cycles;          /* grass */
-  uint8_t *avail;            /* grass */
-} pp_pop;
-
-typedef struct {
-  pp_pop t[3];
-  /* printed constants */
-  double PRED_PREY_INTERACTION_RADIUS, PREY_GROUP_COHESION_RADIUS,
-      SAME_SPECIES_AVOIDANCE_RADIUS, GRASS_EAT_DISTANCE, PRED_KILL_DISTANCE, DELTA_TIME,
-      PRED_SPEED_ADVANTAGE, SPACE_MULT, REPRODUCE_PREY_PROB, REPRODUCE_PREDATOR_PROB, env_size;
-  int GAIN_FROM_FOOD_PREDATOR, GAIN_FROM_FOOD_PREY, GRASS_REGROW_CYCLES;
-  uint64_t seed;
-  long timestep;
-} pp_sim;
-
-static void pp_alloc(pp_pop *p, long cap, int grass) {
-  p->cap = cap;
-  p->pos = calloc(2 * cap, sizeof(double));
-  if (grass) {
-    p->dead_cycles = calloc(cap, sizeof(int));
-    p->avail = calloc(cap, 1);
-  } else {
-    p->dir = calloc(2 * cap, sizeof(double));
-    p->steer = calloc(2 * cap, sizeof(double));
-    p->life = calloc(cap, sizeof(int));
-  }
-}
-
-static void pp_free(pp_pop *p) {
-  free(p->pos);
-  free(p->dir);
-  free(p->steer);
-  free(p->life);
-  free(p->dead_cycles);
-  free(p->avail);
-  memset(p, 0, sizeof *p);
-}
-
-static void pp_copy_agent(const pp_pop *src, long i, pp_pop *dst, long j, int grass) {
-  dst->pos[2 * j] = src->pos[2 * i];
-  dst->pos[2 * j + 1] = src->pos[2 * i + 1];
-  if (grass) {
-    dst->dead_cycles[j] = src->dead_cycles[i];
-    dst->avail[j] = src->avail[i];
-  } else {
-    dst->dir[2 * j] = src->dir[2 * i];
-    dst->dir[2 * j + 1] = src->dir[2 * i + 1];
-    dst->steer[2 * j] = src->steer[2 * i];
-    dst->steer[2 * j + 1] = src->steer[2 * i + 1];
-    dst->life[j] = src->life[i];
-  }
-}
-
-/* pp_params: 11 doubles (radii..env_size in the order of pp_sim) + 3 ints. */
-ORACLE_API void *oracle_pp_create(const double *dparams, const int *iparams, uint64_t seed,
-                                  const long *n, const double *const *pos,
-                                  const double *const *dir, const double *const *steer,
-                                  const int *const *life, const int *dead_cycles,
-                                  const uint8_t *avail) {
-  pp_sim *S = calloc(1, sizeof *S);
-  double *d = &S->PRED_PREY_INTERACTION_RADIUS;
-  for (int k = 0; k < 11; k++) d[k] = dparams[k];
-  S->GAIN_FROM_FOOD_PREDATOR = iparams[0];
-  S->GAIN_FROM_FOOD_PREY = iparams[1];
-  S->GRASS_REGROW_CYCLES = iparams[2];
-  S->seed = seed;
-  for (int ti = 0; ti < 3; ti++) {
-    long cap = 2 * n[ti] + 1024;
-    pp_alloc(&S->t[ti], cap, ti == PP_GRASS);
-    S->t[ti].n = n[ti];
-    memcpy(S->t[ti].pos, pos[ti], sizeof(double) * 2 * n[ti]);
-    if (ti == PP_GRASS) {
-      memcpy(S->t[ti].dead_cycles, dead_cycles, sizeof(int) * n[ti]);
-      memcpy(S->t[ti].avail, avail, n[ti]);
-    } else {
-      memcpy(S->t[ti].dir, dir[ti], sizeof(double) * 2 * n[ti]);
-      memcpy(S->t[ti].steer, steer[ti], sizeof(double) * 2 * n[ti]);
-      memcpy(S->t[ti].life, life[ti], sizeof(int) * n[ti]);
-    }
-  }
-  return S;
-}
-
-ORACLE_API void oracle_pp_destroy(void *h) {
-  pp_sim *S = h;
-  for (int ti = 0; ti < 3; ti++) pp_free(&S->t[ti]);
-  free(S);
-}
-
-ORACLE_API long oracle_pp_count(void *h, int type) { return ((pp_sim *) h)->t[type].n; }
-
-ORACLE_API void oracle_pp_get(void *h, int type, double *pos, double *dir, double *steer,
-                              int *life, int *dead_cycles, uint8_t *avail) {
-  pp_pop *p = &((pp_sim *) h)->t[type];
-  memcpy(pos, p->pos, sizeof(double) * 2 * p->n);
-  if (type == PP_GRASS) {
-    memcpy(dead_cycles, p->dead_cycles, sizeof(int) * p->n);
-    memcpy(avail, p->avail, p->n);
-  } else {
-    memcpy(dir, p->dir, sizeof(double) * 2 * p->n);
-    memcpy(steer, p->steer, sizeof(double) * 2 * p->n);
-    memcpy(life, p->life, sizeof(int) * p->n);
-  }
-}
-
-static inline double len_sub(const double *a, const double *b) {
-  /* length_float2(float2_sub(a, b)) */
-  double dx = a[0] - b[0], dy = a[1] - b[1];
-  return (double) sqrtf((float) (dx * dx + dy * dy));
-}
-
-static inline double clampd(double v, double lo, double hi) {
-  return (v < lo) ? lo : ((v > hi) ? hi : v);
-}
-
-/* Candidates of a near loop: all agents of `nb` (mode 0) or the sorted grid
- * candidates (mode 1), the in-radius test applied by the caller. */
-typedef struct {
-  int mode;
-  grid_t g;
-  const pp_pop *nb;
-  double env;
-} pp_near;
-
-static void pp_near_init(pp_near *N, const pp_pop *nb, double radius, double env, int mode) {
-  N->mode = mode;
-  N->nb = nb;
-  N->env = env;
-  if (mode == 1) {
-    double emin[2] = {0, 0}, emax[2] = {env, env};
-    grid_build(&N->g, 2, nb->n, nb->pos, emin, emax, radius);
-  }
-}
-
-static void pp_near_free(pp_near *N) {
-  if (N->mode == 1) grid_free(&N->g);
-}
-
-/* Candidate list of query position q (ascending neighbour index). */
-static long pp_candidates(const pp_near *N, const double *q, long **buf, long *cap) {
-  if (N->mode == 0) {
-    if (N->nb->n > *cap) {
-      *cap = N->nb->n + 64;
-      *buf = realloc(*buf, *cap * sizeof(long));
-    }
-    for (long j = 0; j < N->nb->n; j++) (*buf)[j] = j;
-    return N->nb->n;
-  }
-  const grid_t *g = &N->g;
-  long kx = (long) floor((q[0] - g->lo[0]) * g->inv_cell);
-  long ky = (long) floor((q[1] - g->lo[1]) * g->inv_cell);
-  kx = clampl(kx, 0, g->dims[0] - 1);
-  ky = clampl(ky, 0, g->dims[1] - 1);
-  long cnt = 0;
-  for (long y = ky - 1; y <= ky + 1; y++) {
-    if (y < 0 || y >= g->dims[1]) continue;
-    for (long x = kx - 1; x <= kx + 1; x++) {
-      if (x < 0 || x >= g->dims[0]) continue;
-      long cc = y * g->dims[0] + x;
-      long s = g->cell_start[cc], e = g->cell_start[cc + 1];
-      if (cnt + (e - s) > *cap) {
-        *cap = 2 * (cnt + (e - s)) + 64;
-        *buf = realloc(*buf, *cap * sizeof(long));
-      }
-      for (long j = s; j < e; j++) (*buf)[cnt++] = g->order[j];
-    }
-  }
-  qsort(*buf, cnt, sizeof(long), cmp_long);
-  return cnt;
-}
-
-#define PP_NEAR_LOOP(N, q, radius, j, ...)                                        \
-  do {                                                                            \
-    long cnt_ = pp_candidates((N), (q), &buf, &bcap);                             \
-    for (long q_ = 0; q_ < cnt_; q_++) {                                          \
-      long j = buf[q_];                                                           \
-      if (len_sub((N)->nb->pos + 2 * j, (q)) > (radius)) continue;                \
-      __VA_ARGS__                                                                 \
-    }                                                                             \
-  } while (0)
 
 enum {
   S_PRED_FOLLOW_PREY, S_PREY_AVOID_PRED, S_PREY_FLOCK, S_PRED_AVOID, S_PREY_MOVE, S_PRED_MOVE,
@@ -1012,267 +828,14 @@ static const int pp_step_type[S_COUNT] = {PP_PRED, PP_PREY, PP_PREY, PP_PRED, PP
                                          PP_PREY, PP_PRED, PP_GRASS, PP_PREY, PP_PRED, PP_PREY,
                                          PP_GRASS};
 
-/* One step function over all agents of its type; `out` starts as `in`. */
-static void pp_step(pp_sim *S, int k, int mode, int nthreads) {
-  int ti = pp_step_type[k];
-  pp_pop *in = &S->t[ti];
-  long n = in->n;
-  int grass = ti == PP_GRASS;
-  pp_pop out;
-  memset(&out, 0, sizeof out);
-  pp_alloc(&out, in->cap, grass);
-  out.n = n;
-  for (long i = 0; i < n; i++) pp_copy_agent(in, i, &out, i, grass);
-  uint8_t *removed = calloc(n ? n : 1, 1), *child = calloc(n ? n : 1, 1);
-  pp_pop kids;
-  memset(&kids, 0, sizeof kids);
-  pp_alloc(&kids, n ? n : 1, grass);
-
-  int near_type = -1;
-  double radius = 0;
-  switch (k) {
-    case S_PRED_FOLLOW_PREY: near_type = PP_PREY; radius = S->PRED_PREY_INTERACTION_RADIUS; break;
-    case S_PREY_AVOID_PRED: near_type = PP_PRED; radius = S->PRED_PREY_INTERACTION_RADIUS; break;
-    case S_PREY_FLOCK: near_type = PP_PREY; radius = S->PREY_GROUP_COHESION_RADIUS; break;
-    case S_PRED_AVOID: near_type = PP_PRED; radius = S->SAME_SPECIES_AVOIDANCE_RADIUS; break;
-    case S_PREY_EAT_OR_STARVE: near_type = PP_GRASS; radius = S->GRASS_EAT_DISTANCE; break;
-    case S_PRED_EAT_OR_STARVE: near_type = PP_PREY; radius = S->PRED_KILL_DISTANCE; break;
-    case S_GRASS_EATEN: near_type = PP_PREY; radius = S->GRASS_EAT_DISTANCE; break;
-    case S_PREY_EATEN: near_type = PP_PRED; radius = S->PRED_KILL_DISTANCE; break;
-    default: break;
-  }
-  pp_near N;
-  memset(&N, 0, sizeof N);
-  if (near_type >= 0) pp_near_init(&N, &S->t[near_type], radius, S->env_size, mode);
-  const pp_pop *nb = near_type >= 0 ? &S->t[near_type] : NULL;
-
-#pragma omp parallel num_threads(threads_or_default(nthreads))
-  {
-    long *buf = NULL, bcap = 0;
-#pragma omp for schedule(dynamic, 256)
-    for (long i = 0; i < n; i++) {
-      const double *ip = in->pos + 2 * i;
-      switch (k) {
-        case S_PRED_FOLLOW_PREY: {
-          double steer[2] = {0, 0}, cpp[2] = {0, 0};
-          double cpd = S->PRED_PREY_INTERACTION_RADIUS;
-          int see = 0;
-          PP_NEAR_LOOP(&N, ip, radius, j, {
-            const double *jp = nb->pos + 2 * j;
-            double sep = len_sub(ip, jp);
-            if (sep < cpd) {
-              cpp[0] = jp[0];
-              cpp[1] = jp[1];
-              cpd = sep;
-              see = 1;
-            }
-          });
-          if (see) {
-            steer[0] = cpp[0] - ip[0];
-            steer[1] = cpp[1] - ip[1];
-          }
-          out.steer[2 * i] = steer[0];
-          out.steer[2 * i + 1] = steer[1];
-          break;
-        }
-        case S_PREY_AVOID_PRED:
-        case S_PRED_AVOID: {
-          double R = k == S_PREY_AVOID_PRED ? S->PRED_PREY_INTERACTION_RADIUS
-                                            : S->SAME_SPECIES_AVOIDANCE_RADIUS;
-          double av[2] = {0, 0};
-          PP_NEAR_LOOP(&N, ip, radius, j, {
-            const double *jp = nb->pos + 2 * j;
-            double sep = len_sub(ip, jp);
-            int cond = k == S_PREY_AVOID_PRED
-                           ? sep < R
-                           : ((sep < R) && (jp[0] != ip[0] || jp[1] != ip[1]));
-            if (cond && sep > 0.0) {
-              double s = R / sep;
-              av[0] = av[0] + (ip[0] - jp[0]) * s;
-              av[1] = av[1] + (ip[1] - jp[1]) * s;
-            }
-          });
-          if (k == S_PREY_AVOID_PRED) {
-            out.steer[2 * i] = av[0];
-            out.steer[2 * i + 1] = av[1];
-          } else {
-            out.steer[2 * i] = in->steer[2 * i] + av[0];
-            out.steer[2 * i + 1] = in->steer[2 * i + 1] + av[1];
-          }
-          break;
-        }
-        case S_PREY_FLOCK: {
-          double gc[2] = {0, 0}, gv[2] = {0, 0}, av[2] = {0, 0};
-          int cnt = 0;
-          double R = S->SAME_SPECIES_AVOIDANCE_RADIUS;
-          PP_NEAR_LOOP(&N, ip, radius, j, {
-            const double *jp = nb->pos + 2 * j;
-            double sep = len_sub(ip, jp);
-            gc[0] = gc[0] + jp[0];
-            gc[1] = gc[1] + jp[1];
-            cnt += 1;
-            if ((sep < R) && (jp[0] != ip[0] || jp[1] != ip[1])) {
-              if (sep > 0.0) {
-                double s = R / sep;
-                av[0] = av[0] + (ip[0] - jp[0]) * s;
-                av[1] = av[1] + (ip[1] - jp[1]) * s;
-              }
-            }
-          });
-          if (cnt > 0) {
-            gc[0] = gc[0] / cnt;
-            gc[1] = gc[1] / cnt;
-            gv[0] = gc[0] - ip[0];
-            gv[1] = gc[1] - ip[1];
-          }
-          out.steer[2 * i] = (in->steer[2 * i] + gv[0]) + av[0];
-          out.steer[2 * i + 1] = (in->steer[2 * i + 1] + gv[1]) + av[1];
-          break;
-        }
-        case S_PREY_MOVE:
-        case S_PRED_MOVE: {
-          double p[2] = {ip[0], ip[1]};
-          double v[2] = {in->dir[2 * i] + in->steer[2 * i], in->dir[2 * i + 1] + in->steer[2 * i + 1]};
-          double cs = (double) sqrtf((float) (v[0] * v[0] + v[1] * v[1]));
-          if (cs > 1.0) {
-            double l = (double) sqrtf((float) (v[0] * v[0] + v[1] * v[1]));
-            v[0] = v[0] / l;
-            v[1] = v[1] / l;
-          }
-          for (int d = 0; d < 2; d++) {
-            double step = k == S_PREY_MOVE
-                              ? (v[d] * S->DELTA_TIME) * S->SPACE_MULT
-                              : ((v[d] * S->DELTA_TIME) * S->PRED_SPEED_ADVANTAGE) * S->SPACE_MULT;
-            p[d] = p[d] + step;
-            p[d] = clampd(p[d], 0.0, S->env_size);  /* boundPosition -> clamp(pos, float2(env_size)) */
-          }
-          out.pos[2 * i] = p[0];
-          out.pos[2 * i + 1] = p[1];
-          out.dir[2 * i] = v[0];
-          out.dir[2 * i + 1] = v[1];
-          out.life[i] = in->life[i] - 1;
-          break;
-        }
-        case S_PREY_EAT_OR_STARVE:
-        case S_PRED_EAT_OR_STARVE: {
-          int life = in->life[i];
-          PP_NEAR_LOOP(&N, ip, radius, j, {
-            if (k == S_PREY_EAT_OR_STARVE) {
-              if (nb->avail[j]) life += S->GAIN_FROM_FOOD_PREY;
-            } else {
-              life += S->GAIN_FROM_FOOD_PREDATOR;
-            }
-          });
-          out.life[i] = life;
-          if (life < 1) removed[i] = 1;
-          break;
-        }
-        case S_GRASS_EATEN:
-        case S_PREY_EATEN: {
-          double closest = k == S_GRASS_EATEN ? S->GRASS_EAT_DISTANCE : S->PRED_KILL_DISTANCE;
-          int eaten = 0;
-          PP_NEAR_LOOP(&N, ip, radius, j, {
-            const double *jp = nb->pos + 2 * j;
-            if (k == S_GRASS_EATEN) {
-              double distance = len_sub(ip, jp);
-              if ((distance < closest) && in->avail[i]) {
-                closest = distance;
-                eaten = 1;
-              }
-            } else {
-              double distance = len_sub(jp, ip);
-              if (distance < closest) {
-                closest = distance;
-                eaten = 1;
-              }
-            }
-          });
-          if (k == S_GRASS_EATEN) {
-            if (eaten) {
-              out.dead_cycles[i] = 0;
-              out.avail[i] = 0;
-            }
-          } else if (eaten) {
-            removed[i] = 1;
-          }
-          break;
-        }
-        case S_PRED_REPRODUCTION:
-        case S_PREY_REPRODUCTION: {
-          pp_rng R;
-          R.k0 = (uint32_t) S->seed;
-          R.k1 = (uint32_t) (S->seed >> 32);
-          R.c0 = (uint32_t) i;
-          R.c1 = (uint32_t) k;
-          R.c2 = (uint32_t) S->timestep;
-          R.draw = 0;
-          double prob = k == S_PREY_REPRODUCTION ? S->REPRODUCE_PREY_PROB
-                                                 : S->REPRODUCE_PREDATOR_PROB;
-          if (pp_uniform(&R, 0.0, 1.0) < prob) {
-            child[i] = 1;
-            kids.pos[2 * i] = ip[0];
-            kids.pos[2 * i + 1] = ip[1];
-            kids.dir[2 * i] = in->dir[2 * i] * -1.0;
-            kids.dir[2 * i + 1] = in->dir[2 * i + 1] * -1.0;
-            kids.steer[2 * i] = in->steer[2 * i] * -1.0;
-            kids.steer[2 * i + 1] = in->steer[2 * i + 1] * -1.0;
-            kids.life[i] = in->life[i] / 2;
-            out.life[i] = in->life[i] / 2;
-          }
-          break;
-        }
-        case S_GRASS_GROWTH: {
-          if (in->dead_cycles[i] == S->GRASS_REGROW_CYCLES) {
-            out.dead_cycles[i] = 0;
-            out.avail[i] = 1;
-          }
-          if (!in->avail[i]) out.dead_cycles[i] = in->dead_cycles[i] + 1;
-          break;
-        }
-      }
-    }
-    free(buf);
-  }
-  if (near_type >= 0) pp_near_free(&N);
-
-  /* Survivors (stable) then children in parent order. */
-  long survivors = 0, kids_n = 0;
-  for (long i = 0; i < n; i++) {
-    survivors += !removed[i];
-    kids_n += child[i];
-  }
-  long need = survivors + kids_n;
-  pp_pop res;
-  memset(&res, 0, sizeof res);
-  long cap = in->cap > need ? in->cap : 2 * need + 1024;
-  pp_alloc(&res, cap, grass);
-  long j = 0;
-  for (long i = 0; i < n; i++)
-    if (!removed[i]) pp_copy_agent(&out, i, &res, j++, grass);
-  for (long i = 0; i < n; i++)
-    if (child[i]) pp_copy_agent(&kids, i, &res, j++, grass);
-  res.n = need;
-  pp_free(in);
-  *in = res;
-  pp_free(&out);
-  pp_free(&kids);
-  free(removed);
-  free(child);
-}
-
-/* Runs `timesteps` timesteps; stats (3 ints per timestep: count(Prey),
- * count(Predator), sum(Grass.avail)) are written to `stats` if not NULL. */
-ORACLE_API void oracle_pp_run(void *h, int timesteps, int mode, int nthreads, int *stats) {
-  pp_sim *S = h;
-  for (int t = 0; t < timesteps; t++) {
-    for (int k = 0; k < S_COUNT; k++) pp_step(S, k, mode, nthreads);
-    S->timestep++;
-    if (stats) {
-      long g = 0;
-      for (long i = 0; i < S->t[PP_GRASS].n; i++) g += S->t[PP_GRASS].avail[i];
-      stats[3 * t] = (int) S->t[PP_PREY].n;
-      stats[3 * t + 1] = (int) S->t[PP_PRED].n;
-      stats[3 * t + 2] = (int) g;
-    }
-  }
-}
+/* The FP64 build (oracle_pp_*) and the use_float build (oracle_pp_*_f32). */
+#define PP_REAL double
+#define PP_FN(x) x
+#include "abl_oracle_pp.h"
+#undef PP_REAL
+#undef PP_FN
+#define PP_REAL float
+#define PP_FN(x) x##_f32
+#include "abl_oracle_pp.h"
+#undef PP_REAL
+#undef PP_FN

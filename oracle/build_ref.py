@@ -39,6 +39,10 @@ CASES = {
                                          "num_timesteps": "100"}, {}),
     "boids2d_4096_float": ("boids2d", {"num_agents": "4096", "agent_density": "3200.0",
                                        "num_timesteps": "100"}, {"use_float": "true"}),
+    "circle_4000_float": ("circle", {"num_agents": "4000", "rho": "0.1", "num_timesteps": "100"},
+                          {"use_float": "true"}),
+    "circle3d_4000_float": ("circle3d", {"num_agents": "4000", "rho": "0.01",
+                                         "num_timesteps": "50"}, {"use_float": "true"}),
     "boids3d_5000": ("boids", {"num_timesteps": "100"}, {}),
     "sugarscape_10000": ("sugarscape", {"num_timesteps": "100"}, {}),
     # random() inside the step: recorded on one OpenMP thread (SERIAL_RANDOM)
@@ -52,6 +56,8 @@ PROGRAMS = {
     "boids2d": ("boids2d", {}),
     "game_of_life": ("game_of_life", {}),
     "boids2d_float": ("boids2d", {"use_float": "true"}),
+    "circle_float": ("circle", {"use_float": "true"}),
+    "circle3d_float": ("circle3d", {"use_float": "true"}),
     "boids3d": ("boids", {}),
     # a model of this repository's tests (constant arrays, a member written
     # on one branch only)

@@ -26,8 +26,9 @@ def lib():
     global _LIB
     if _LIB is None:
         path = os.path.join(HERE, "liboracle.so")
+        srcs = [os.path.join(HERE, f) for f in ("abl_oracle.c", "abl_oracle_pp.h")]
         if not os.path.exists(path) or (os.path.getmtime(path)
-                                        < os.path.getmtime(os.path.join(HERE, "abl_oracle.c"))):
+                                        < max(os.path.getmtime(f) for f in srcs)):
             build()
         L = ctypes.CDLL(path)
         L.oracle_random_float.restype = _d
@@ -230,59 +231,76 @@ PP_IPARAMS = ("GAIN_FROM_FOOD_PREDATOR", "GAIN_FROM_FOOD_PREY", "GRASS_REGROW_CY
 
 class PredatorPrey:
     """The predator_prey restatement (abl_oracle.c) over a population dict
-    {type name: {member: array}} and the printed constants `c`."""
+    {type name: {member: array}} and the printed constants `c`; FP64 build."""
+
+    SUFFIX = ""
+    REAL = np.float64
+
+    def _fn(self, name):
+        return getattr(lib(), name + self.SUFFIX)
 
     def __init__(self, state, c, seed=0):
-        L = lib()
-        L.oracle_pp_create.restype = ctypes.c_void_p
-        L.oracle_pp_create.argtypes = [_p, _p, ctypes.c_uint64, _p, _p, _p, _p, _p, _p, _p]
-        L.oracle_pp_destroy.argtypes = [_p]
-        L.oracle_pp_count.restype = _l
-        L.oracle_pp_count.argtypes = [_p, _i]
-        L.oracle_pp_get.argtypes = [_p, _i, _p, _p, _p, _p, _p, _p]
-        L.oracle_pp_run.argtypes = [_p, _i, _i, _i, _p]
+        create = self._fn("oracle_pp_create")
+        create.restype = ctypes.c_void_p
+        create.argtypes = [_p, _p, ctypes.c_uint64, _p, _p, _p, _p, _p, _p, _p]
+        self._fn("oracle_pp_destroy").argtypes = [_p]
+        self._fn("oracle_pp_count").restype = _l
+        self._fn("oracle_pp_count").argtypes = [_p, _i]
+        self._fn("oracle_pp_get").argtypes = [_p, _i, _p, _p, _p, _p, _p, _p]
+        self._fn("oracle_pp_run").argtypes = [_p, _i, _i, _i, _p]
         self._keep = []
         dp = np.array([float(c[k]) for k in PP_DPARAMS], np.float64)
         ip = np.array([int(c[k]) for k in PP_IPARAMS], np.int32)
         n = np.array([len(state[t]["pos"]) for t in PP_TYPES], np.int64)
+        R = self.REAL
 
         def arr(a, dt):
             a = np.ascontiguousarray(a, dtype=dt)
             self._keep.append(a)
             return a.ctypes.data
 
-        pos = (ctypes.c_void_p * 3)(*[arr(state[t]["pos"], np.float64) for t in PP_TYPES])
-        dirs = (ctypes.c_void_p * 2)(*[arr(state[t]["dir"], np.float64) for t in PP_TYPES[:2]])
-        steer = (ctypes.c_void_p * 2)(*[arr(state[t]["steer"], np.float64) for t in PP_TYPES[:2]])
+        pos = (ctypes.c_void_p * 3)(*[arr(state[t]["pos"], R) for t in PP_TYPES])
+        dirs = (ctypes.c_void_p * 2)(*[arr(state[t]["dir"], R) for t in PP_TYPES[:2]])
+        steer = (ctypes.c_void_p * 2)(*[arr(state[t]["steer"], R) for t in PP_TYPES[:2]])
         life = (ctypes.c_void_p * 2)(*[arr(state[t]["life"], np.int32) for t in PP_TYPES[:2]])
-        self.h = L.oracle_pp_create(_ptr(dp), _ptr(ip), seed, _ptr(n), pos, dirs, steer, life,
-                                    arr(state["Grass"]["dead_cycles"], np.int32),
-                                    arr(state["Grass"]["avail"], np.uint8))
+        self.h = create(_ptr(dp), _ptr(ip), seed, _ptr(n), pos, dirs, steer, life,
+                        arr(state["Grass"]["dead_cycles"], np.int32),
+                        arr(state["Grass"]["avail"], np.uint8))
 
     def run(self, timesteps, mode=1, nthreads=0):
         stats = np.zeros((timesteps, 3), np.int32)
-        lib().oracle_pp_run(self.h, timesteps, mode, nthreads, _ptr(stats))
+        self._fn("oracle_pp_run")(self.h, timesteps, mode, nthreads, _ptr(stats))
         return stats
 
     def get(self):
         out = {}
+        R = self.REAL
         for k, t in enumerate(PP_TYPES):
-            n = lib().oracle_pp_count(self.h, k)
-            pos = np.zeros((n, 2))
+            n = self._fn("oracle_pp_count")(self.h, k)
+            pos = np.zeros((n, 2), R)
             if t == "Grass":
                 dc = np.zeros(n, np.int32)
                 av = np.zeros(n, np.uint8)
-                lib().oracle_pp_get(self.h, k, _ptr(pos), None, None, None, _ptr(dc), _ptr(av))
+                self._fn("oracle_pp_get")(self.h, k, _ptr(pos), None, None, None, _ptr(dc),
+                                          _ptr(av))
                 out[t] = {"pos": pos, "dead_cycles": dc, "avail": av}
             else:
-                d, s = np.zeros((n, 2)), np.zeros((n, 2))
+                d, s = np.zeros((n, 2), R), np.zeros((n, 2), R)
                 life = np.zeros(n, np.int32)
-                lib().oracle_pp_get(self.h, k, _ptr(pos), _ptr(d), _ptr(s), _ptr(life), None,
-                                    None)
+                self._fn("oracle_pp_get")(self.h, k, _ptr(pos), _ptr(d), _ptr(s), _ptr(life),
+                                          None, None)
                 out[t] = {"pos": pos, "dir": d, "steer": s, "life": life}
         return out
 
     def close(self):
         if self.h:
-            lib().oracle_pp_destroy(self.h)
+            self._fn("oracle_pp_destroy")(self.h)
             self.h = None
+
+
+class PredatorPreyF32(PredatorPrey):
+    """The same restatement as the use_float build computes it: every member,
+    printed constant and intermediate in float (abl_oracle_pp.h)."""
+
+    SUFFIX = "_f32"
+    REAL = np.float32

@@ -14,5 +14,8 @@ def case(config, seed=0):
     state = workloads.predator_prey(n_pred, n_prey, n_grass, float(g["env_size"]),
                                     int(g["GAIN_FROM_FOOD_PREDATOR"]),
                                     int(g["GAIN_FROM_FOOD_PREY"]), seed=seed)
+    if cfg["model"].endswith("_float"):
+        state = {t: {k: (v.astype("float32") if v.dtype.kind == "f" else v)
+                     for k, v in d.items()} for t, d in state.items()}
     consts = {k: g[k] for k in O.PP_DPARAMS + O.PP_IPARAMS}
     return cfg, state, consts

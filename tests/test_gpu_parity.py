@@ -51,16 +51,28 @@ def test_graph_replay_matches_reference(case, agent):
     sim.close()
 
 
-def test_use_float_matches_reference_every_timestep():
+FLOAT_GOLDEN = [("boids2d_4096_float", "boids2d_float_4096", "Boid"),
+                ("circle_4000_float", "circle_float_4000", "Point"),
+                ("circle3d_4000_float", "circle3d_float_4000", "Point")]
+
+
+@pytest.mark.parametrize("case,config,agent", FLOAT_GOLDEN)
+def test_use_float_matches_reference_every_timestep(case, config, agent):
     """-C use_float=true: the reference `c` program built with
     LIBABL_USE_FLOAT (float agents, double literals) against the generated
-    FP32 model, bit-exact after every timestep."""
-    meta, state = load_case("boids2d_4096_float")
-    sim = make_sim("boids2d_float_4096")
-    sim.upload("Boid", state)
+    FP32 model, bit-exact after every timestep, one timestep at a time and
+    through graph replay."""
+    meta, state = load_case(case)
+    sim = make_sim(config)
+    sim.upload(agent, state)
     for t in range(1, meta["timesteps"] + 1):
         sim.step()
-        assert state_hash(meta, sim.download("Boid")) == meta["sha256"][t], f"timestep {t}"
+        assert state_hash(meta, sim.download(agent)) == meta["sha256"][t], f"timestep {t}"
+    sim.close()
+    sim = make_sim(config)
+    sim.upload(agent, state)
+    sim.run(meta["timesteps"])
+    assert state_hash(meta, sim.download(agent)) == meta["sha256"][meta["timesteps"]]
     sim.close()
 
 

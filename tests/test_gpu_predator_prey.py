@@ -49,6 +49,25 @@ def test_every_timestep_matches_oracle():
     ref.close()
 
 
+def test_float_build_every_timestep_matches_oracle():
+    """-C use_float=true: the FP32 model against the oracle's float
+    restatement (every member and intermediate in float), bit-exact after
+    every timestep, with the sequential step's statistics."""
+    cfg, state, consts = case("predator_prey_float_small")
+    sim = sim_for("predator_prey_float_small", state, seed=11)
+    ref = O.PredatorPreyF32(state, consts, seed=11)
+    stats = []
+    for t in range(30):
+        sim.step()
+        stats.append(ref.run(1, mode=1)[0])
+        assert_same(sim, ref, t)
+    rows = [r.split(",") for r in sim.log_text().strip().splitlines()]
+    for r, s in zip(rows, stats):
+        assert [int(r[0]), int(r[1]), int(r[2])] == s.tolist()
+    sim.close()
+    ref.close()
+
+
 def test_reductions():
     cfg, state, consts = case("predator_prey_small")
     sim = sim_for("predator_prey_small", state, seed=1)
