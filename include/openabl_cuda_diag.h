@@ -16,6 +16,10 @@ extern "C" {
  * (per lane) on the current device; any pointer may be NULL. */
 int abl_diag_fp64_rates(double *dfma_per_s, double *dadd_per_s, double *dmul_per_s);
 
+/* Measured rate of FP64 additions issued as fma(x, 1.0, y) -- the same
+ * correctly rounded sum as x + y -- in instructions per second (per lane). */
+int abl_diag_fp64_add_as_fma_rate(double *per_s);
+
 /* Checks the step kernels' division of a double by an int count (a two-term
  * reciprocal table, abl::div_int in the runtime) against IEEE division on
  * the device: per_n operands for every n from -3 to 1027 (both ends outside

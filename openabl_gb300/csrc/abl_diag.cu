@@ -29,7 +29,7 @@ __global__ void k_fp64_chain(double *out, int iters, double a, double b) {
 }
 
 template <int OP>
-int time_op(double *ops_per_s) {
+int time_op(double *ops_per_s, double a = 1.0000001) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -39,9 +39,9 @@ int time_op(double *ops_per_s) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  k_fp64_chain<OP><<<blocks, threads>>>(out, 64, 1.0000001, 1e-9);  // warm-up
+  k_fp64_chain<OP><<<blocks, threads>>>(out, 64, a, 1e-9);  // warm-up
   cudaEventRecord(e0);
-  k_fp64_chain<OP><<<blocks, threads>>>(out, iters, 1.0000001, 1e-9);
+  k_fp64_chain<OP><<<blocks, threads>>>(out, iters, a, 1e-9);
   cudaEventRecord(e1);
   cudaError_t err = cudaEventSynchronize(e1);
   float ms = 0;
@@ -108,6 +108,14 @@ extern "C" int abl_diag_check_int_division(unsigned long long seed, long per_n,
   *mismatches = h[0];
   *checked = h[1];
   return 0;
+}
+
+// An addition x + b issued as fma(x, 1.0, b): the same correctly rounded
+// sum, on the fused-multiply-add path.  The 1.0 is a kernel argument, so the
+// compiler cannot turn the fma back into an add.
+extern "C" int abl_diag_fp64_add_as_fma_rate(double *per_s) {
+  if (!per_s) return ABL_DIAG_E_ARG;
+  return time_op<0>(per_s, 1.0);
 }
 
 extern "C" int abl_diag_fp64_rates(double *dfma_per_s, double *dadd_per_s, double *dmul_per_s) {

@@ -113,14 +113,42 @@ static void write_member_json(FILE *f, const char *agent, const type_info *m, in
   }
 }
 
-void abl_save(void *agents, const agent_info *info, const char *path, save_type type,
-              int float_bytes) {
-  (void) type;  // JSON, as the reference runtime writes for the C backend
-  FILE *f = std::fopen(path, "w");
-  if (!f) {
-    std::fprintf(stderr, "save(): Count not open \"%s\" for writing\n", path);
+// FLAME / FLAMEGPU XML (asset/c/libabl.c:126-213): one <xagent> per agent
+// with its type name and one element per member; vectors are split into
+// <m_x>, <m_y>[, <m_z>]; for FLAMEGPU the position member is always written
+// as <x>, <y>, <z> (z = 0.0 in 2D).  Booleans are written as integers.  The
+// reference reads a bool member through an int pointer, i.e. together with
+// the three bytes after it in the agent record; here the member's own value
+// (0 or 1) is written, which is what the reference writes when those bytes
+// are zero.
+static void write_member_xml(FILE *f, const char *agent, const type_info *m, int fb,
+                             bool for_gpu) {
+  const char *p = agent + m->offset;
+  const char *nm = m->name;
+  if (for_gpu && m->is_pos && (m->type == TYPE_FLOAT2 || m->type == TYPE_FLOAT3)) {
+    std::fprintf(f, "<x>%f</x>\n<y>%f</y>\n", read_float(p, fb), read_float(p + fb, fb));
+    if (m->type == TYPE_FLOAT3) std::fprintf(f, "<z>%f</z>\n", read_float(p + 2 * fb, fb));
+    else std::fputs("<z>0.0</z>\n", f);
     return;
   }
+  switch (m->type) {
+    case TYPE_BOOL: std::fprintf(f, "<%s>%d</%s>\n", nm, *(const bool *) p ? 1 : 0, nm); break;
+    case TYPE_INT: std::fprintf(f, "<%s>%d</%s>\n", nm, *(const int *) p, nm); break;
+    case TYPE_FLOAT: std::fprintf(f, "<%s>%f</%s>\n", nm, read_float(p, fb), nm); break;
+    case TYPE_FLOAT2:
+    case TYPE_FLOAT3: {
+      const int comps = m->type == TYPE_FLOAT2 ? 2 : 3;
+      const char axis[3] = {'x', 'y', 'z'};
+      for (int c = 0; c < comps; c++)
+        std::fprintf(f, "<%s_%c>%f</%s_%c>\n", nm, axis[c], read_float(p + c * fb, fb), nm,
+                     axis[c]);
+      break;
+    }
+    default: break;
+  }
+}
+
+static void save_json(FILE *f, void *agents, const agent_info *info, int float_bytes) {
   std::fputs("{", f);
   for (const agent_info *a = info; a->name; a++) {
     if (a != info) std::fputs(",", f);
@@ -141,7 +169,39 @@ void abl_save(void *agents, const agent_info *info, const char *path, save_type 
     std::fputs("]", f);
   }
   std::fputs("}", f);
-  std::fclose(f);
+}
+
+static void save_xml(FILE *f, void *agents, const agent_info *info, int float_bytes,
+                     bool for_gpu) {
+  std::fputs("<states>\n<itno>0</itno>\n", f);
+  for (const agent_info *a = info; a->name; a++) {
+    const dyn_array *arr = (const dyn_array *) ((const char *) agents + a->offset);
+    const size_t rec = record_size(a->info);
+    for (size_t i = 0; i < arr->len; i++) {
+      const char *agent = (const char *) arr->values + rec * i;
+      std::fprintf(f, "<xagent>\n<name>%s</name>\n", a->name);
+      for (const type_info *m = a->info; m->type != TYPE_END; m++)
+        write_member_xml(f, agent, m, float_bytes, for_gpu);
+      std::fputs("</xagent>\n", f);
+    }
+  }
+  std::fputs("</states>\n", f);
+}
+
+int abl_save(void *agents, const agent_info *info, const char *path, save_type type,
+             int float_bytes) {
+  if (type != SAVE_JSON && type != SAVE_FLAME_XML && type != SAVE_FLAMEGPU_XML) {
+    std::fprintf(stderr, "save(): unknown output format %d\n", (int) type);
+    return -1;
+  }
+  FILE *f = std::fopen(path, "w");
+  if (!f) {
+    std::fprintf(stderr, "save(): Count not open \"%s\" for writing\n", path);
+    return -1;
+  }
+  if (type == SAVE_JSON) save_json(f, agents, info, float_bytes);
+  else save_xml(f, agents, info, float_bytes, type == SAVE_FLAMEGPU_XML);
+  return std::fclose(f) == 0 ? 0 : -1;
 }
 
 }  // extern "C"

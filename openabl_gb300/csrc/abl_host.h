@@ -76,9 +76,13 @@ typedef enum {
   SAVE_FLAMEGPU_XML,
 } save_type;
 
-/* `float_bytes` is sizeof(abl_float) of the generated program. */
-void abl_save(void *agents, const agent_info *info, const char *path, save_type type,
-              int float_bytes);
+/* Writes every agent to `path` as JSON (SAVE_JSON, the format the `c`
+ * backend's programs write) or FLAME / FLAMEGPU XML, as the reference
+ * runtime's save() (asset/c/libabl.c:46-231).  `float_bytes` is
+ * sizeof(abl_float) of the generated program.  Returns 0, or -1 (with a
+ * message on stderr) when the file cannot be written or `type` is unknown. */
+int abl_save(void *agents, const agent_info *info, const char *path, save_type type,
+             int float_bytes);
 
 #ifdef __cplusplus
 }

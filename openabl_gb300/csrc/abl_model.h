@@ -154,6 +154,14 @@ typedef struct {
 /* Host function run after every timestep: the `sequential step`. */
 typedef int (*abl_seq_step_fn)(abl_ctx *ctx, const void *globals);
 
+/* Called by the sequential step's builtins (count, sum, getLastExecTime)
+ * when their runtime call fails: the first such code is what the timestep
+ * returns once the sequential step has finished. */
+#ifdef __cplusplus
+extern "C"
+#endif
+void abl_seq_record_error(abl_ctx *ctx, int code);
+
 struct abl_model_desc {
   const char *name;
   int num_agent_types;

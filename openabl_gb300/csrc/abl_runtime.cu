@@ -914,6 +914,7 @@ struct abl_ctx {
   long timestep = 0;
   cudaEvent_t ts0 = nullptr, ts1 = nullptr;
   double last_timestep = 0.0;
+  int seq_error = 0;  // first error of a builtin called by the sequential step
   std::string log;
   int *d_pair = nullptr;   // two ints read back after compaction scans
   double *d_red = nullptr; // reduction results
@@ -2037,7 +2038,9 @@ int step_once(abl_ctx *ctx) {
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, ctx->ts0, ctx->ts1);
     ctx->last_timestep = ms / 1000.0;
+    ctx->seq_error = 0;
     ABL_TRY(m->seq_step(ctx, ctx->globals.data()));
+    if (ctx->seq_error) return ctx->seq_error;
   }
   return ABL_OK;
 }
@@ -2676,6 +2679,10 @@ int abl_reduce(abl_ctx *ctx, int kind, int type_id, int member, void *out) {
     return ABL_OK;
   }
   return ABL_E_INVALID;
+}
+
+void abl_seq_record_error(abl_ctx *ctx, int code) {
+  if (ctx && code != ABL_OK && ctx->seq_error == ABL_OK) ctx->seq_error = code;
 }
 
 int abl_set_seed(abl_ctx *ctx, uint64_t seed) {

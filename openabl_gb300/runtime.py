@@ -86,6 +86,16 @@ def fp64_rates():
     return a.value, b.value, c.value
 
 
+def fp64_add_as_fma_rate():
+    """Measured rate of FP64 additions issued as fma(x, 1.0, y), per lane, per s."""
+    L = _load()
+    d = ctypes.c_double
+    L.abl_diag_fp64_add_as_fma_rate.argtypes = [ctypes.POINTER(d)]
+    a = d()
+    _check(L.abl_diag_fp64_add_as_fma_rate(ctypes.byref(a)), "abl_diag_fp64_add_as_fma_rate")
+    return a.value
+
+
 def check_int_division(seed=1, per_n=200000):
     """Device check of the step kernels' division by an int count against
     IEEE division: returns (quotients compared, quotients that differ)."""
