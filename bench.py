@@ -235,7 +235,29 @@ def measure_precision(args, o, W, np, steps=100):
     d = np.abs(r32["pos"].astype(np.float64) - r64["pos"])
     dpi = np.minimum(d, np.abs(L - d)).max(axis=1) / L
     dv = np.abs(r32["velocity"].astype(np.float64) - r64["velocity"]).max(axis=1)
+    # The mixed form (-C cuda.precision=mixed): FP64 state and arithmetic,
+    # near-loop sums of neighbour members in FP32.
+    mm, gm = o.globals_for_config("boids2d_mixed_1m")
+    c = o.Simulation(mm, gm)
+    c.upload("Boid", st)
+    c.run(steps)
+    tmx = c.last_exec_time()
+    rmx = c.download("Boid")
+    c.close()
+    dm = np.abs(rmx["pos"] - r64["pos"])
+    dmi = np.minimum(dm, np.abs(L - dm)).max(axis=1) / L
+    dmv = np.abs(rmx["velocity"] - r64["velocity"]).max(axis=1)
+    mixed = {"value": n * steps / tmx, "unit": "agent-steps/s",
+             "speedup_vs_fp64": t64 / tmx,
+             "pos_rel_err_min_image_max": float(dmi.max()),
+             "pos_rel_err_min_image_median": float(np.median(dmi)),
+             "pos_rel_err_min_image_p99": float(np.quantile(dmi, 0.99)),
+             "frac_agents_min_image_err_le_1e-5": float((dmi <= 1e-5).mean()),
+             "vel_abs_err_max": float(dmv.max()), "vel_abs_err_median": float(np.median(dmv)),
+             "form": "FP64 state, integration and radius tests; near-loop sums of neighbour "
+                     "positions (as offsets from the agent) and velocities in FP32"}
     return {"workload": f"boids2d {n} agents, {steps} timesteps, FP32 (use_float) vs FP64",
+            "mixed": mixed,
             "fp32_value": n * steps / t32, "fp64_value": n * steps / t64, "unit": "agent-steps/s",
             "pos_rel_err_max": float(dp.max()), "pos_rel_err_median": float(np.median(dp)),
             "pos_rel_err_p99": float(np.quantile(dp, 0.99)),

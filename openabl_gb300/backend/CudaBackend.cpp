@@ -11,6 +11,9 @@
 //                          lists or block (abl_set_near_mode; results are identical)
 //   cuda.near_cache=B      keep neighbour lists of agents that never move (default true)
 //   cuda.balance=B         hand a block's agents to threads by neighbour count (default true)
+//   cuda.precision=P       double (default): the reference's arithmetic, bit for bit;
+//                          mixed: near-loop sums of neighbour members in FP32, the
+//                          rest FP64 (CudaPrinter::findMixedAccs)
 #include "CudaBackend.hpp"
 
 #include <cctype>
@@ -102,6 +105,15 @@ void CudaBackend::generate(AST::Script &script, const BackendContext &ctx) {
     printer.nearCache = ctx.config.getBool("cuda.near_cache", true) ? 1 : 0;
   if (ctx.config.config.count("cuda.balance"))
     printer.balance = ctx.config.getBool("cuda.balance", true) ? 1 : 0;
+  auto prec = ctx.config.config.find("cuda.precision");
+  if (prec != ctx.config.config.end()) {
+    if (prec->second == "mixed") {
+      if (useFloat) throw BackendError("cuda.precision=mixed needs the FP64 build (use_float=false)");
+      printer.mixed = true;
+    } else if (prec->second != "double") {
+      throw BackendError("cuda.precision must be double or mixed");
+    }
+  }
   printer.print(script);
   writeToFile(ctx.outputDir + "/" + model + ".cu", printer.extractStr());
   writeToFile(ctx.outputDir + "/" + model + ".globals.json", globalsManifest(script, model));

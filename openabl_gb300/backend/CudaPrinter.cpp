@@ -51,6 +51,7 @@ struct Collector : public AST::Visitor {
   std::vector<const AST::VarExpression *> varExprs;
   std::vector<const AST::VarDeclarationStatement *> decls;
   std::vector<const AST::ForStatement *> fors;
+  std::vector<const AST::MemberAccessExpression *> members;
   int breaks = 0, returns = 0, continues = 0, whiles = 0;
 
   void enter(AST::CallExpression &e) override { calls.push_back(&e); }
@@ -62,6 +63,7 @@ struct Collector : public AST::Visitor {
   void enter(AST::AssignOpStatement &s) override { assignOps.push_back(&s); }
   void enter(AST::VarExpression &e) override { varExprs.push_back(&e); }
   void enter(AST::VarDeclarationStatement &s) override { decls.push_back(&s); }
+  void enter(AST::MemberAccessExpression &e) override { members.push_back(&e); }
   void enter(AST::BreakStatement &) override { breaks++; }
   void enter(AST::ReturnStatement &) override { returns++; }
   void enter(AST::ContinueStatement &) override { continues++; }
@@ -576,6 +578,61 @@ void CudaPrinter::print(const AST::BreakStatement &stmt) {
   CPrinter::print(stmt);
 }
 
+// Mixed precision (-C cuda.precision=mixed): the accumulations of a near
+// body that run in FP32.  A statement `acc += nx.m` qualifies when acc is a
+// float, float2 or float3 variable declared outside the loop, mentioned
+// nowhere else in the body, and m a member of the loop's agent of the same
+// type.  Only the sum changes precision: which neighbours are visited, the
+// order, the radius test and every other expression stay the reference's
+// FP64 ones.
+std::vector<CudaPrinter::MixedAcc> CudaPrinter::findMixedAccs(
+    const AST::ForStatement &loop, const AST::AgentDeclaration &nearAgent) {
+  std::vector<MixedAcc> out;
+  if (!mixed) return out;
+  Collector c = collect(*loop.stmt);
+  std::set<VarId> inner;
+  for (auto *d : c.decls) inner.insert(d->var->id);
+  for (auto *f : c.fors) inner.insert(f->var->id);
+  std::map<VarId, int> uses;
+  for (auto *v : c.varExprs) uses[v->var->id]++;
+  for (auto *a : c.assignOps) {
+    if (a->op != AST::BinaryOp::ADD) continue;
+    auto *lv = dynamic_cast<const AST::VarExpression *>(&*a->left);
+    auto *rm = dynamic_cast<const AST::MemberAccessExpression *>(&*a->right);
+    if (!lv || !rm || inner.count(lv->var->id) || isGlobal(*lv->var)) continue;
+    auto *rv = dynamic_cast<const AST::VarExpression *>(&*rm->expr);
+    if (!rv || rv->var->id != loop.var->id || uses[lv->var->id] != 1) continue;
+    for (size_t k = 0; k < nearAgent.members->size(); k++) {
+      const AST::AgentMember &m = *(*nearAgent.members)[k];
+      if (m.name != rm->member) continue;
+      Type t = m.type->resolved;
+      if (!(t == Type::FLOAT || t.isVec()) || !(a->left->type == t)) break;
+      MixedAcc acc;
+      acc.stmt = a;
+      acc.member = (int) k;
+      acc.isPos = m.isPosition;
+      acc.comps = t.isVec() ? t.getVecLen() : 1;
+      out.push_back(acc);
+      break;
+    }
+  }
+  return out;
+}
+
+void CudaPrinter::print(const AST::AssignOpStatement &stmt) {
+  auto it = mixedAccs.find(&stmt);
+  if (it == mixedAccs.end()) {
+    CPrinter::print(stmt);
+    return;
+  }
+  const MixedAcc &m = it->second;
+  if (m.isPos) {
+    *this << m.acc << ".add_offset(abl_NB, " << nearSlot << ", " << mixedAnchor << ");";
+  } else {
+    *this << m.acc << ".add_member(abl_NB, " << m.member << ", " << nearSlot << ");";
+  }
+}
+
 // The near loop (reference: CPrinter.cpp:148-173).  Candidates come from the
 // runtime's grid; the reference's own radius test decides the rare
 // candidates that the float prefilter cannot.
@@ -634,6 +691,24 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   } else {
     *this << "abl::near_cursor<" << dim << "> " << c << "(abl_NB, " << q << ");";
   }
+  std::vector<MixedAcc> maccs = fnKind == FnKind::STEP ? findMixedAccs(stmt, *agentDecl)
+                                                       : std::vector<MixedAcc>();
+  auto savedMixed = mixedAccs;
+  std::string savedAnchor = mixedAnchor;
+  mixedAccs.clear();
+  if (!maccs.empty()) {
+    mixedAnchor = "abl_ma" + sid;
+    *this << nl << "const abl::mixed_anchor<" << dim << "> " << mixedAnchor << "((double) "
+          << agentExpr << "->" << posMember->name << ".x, (double) " << agentExpr << "->"
+          << posMember->name << ".y, " << (is3 ? "(double) " : "0.0");
+    if (is3) *this << agentExpr << "->" << posMember->name << ".z";
+    *this << ");";
+    for (size_t j = 0; j < maccs.size(); j++) {
+      maccs[j].acc = "abl_fa" + sid + "_" + std::to_string(j);
+      mixedAccs[maccs[j].stmt] = maccs[j];
+      *this << nl << "abl::facc<" << maccs[j].comps << "> " << maccs[j].acc << ";";
+    }
+  }
   *this << nl
         << "auto " << ex << " = [&](int abl_s) -> bool {" << indent << nl
         << "const " << cType(posMember->type->resolved) << " abl_p = " << posCol << "[abl_s];"
@@ -645,11 +720,24 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   // loaded while the body runs on the current one.
   const AST::FunctionDeclaration *cur = steps.empty() ? nullptr : steps.back().decl;
   std::string pslot = "abl_pslot" + sid, pnx = "abl_pnx" + sid;
+  // Members the FP32 sums read from float copies need no FP64 load unless
+  // the body reads them elsewhere too.
+  std::map<std::string, int> fp64Reads;
+  {
+    Collector bc = collect(*stmt.stmt);
+    for (auto *ma : bc.members) {
+      auto *v = dynamic_cast<const AST::VarExpression *>(&*ma->expr);
+      if (v && v->var->id == stmt.var->id) fp64Reads[ma->member]++;
+    }
+    for (const MixedAcc &m : maccs)
+      fp64Reads[(*agentDecl->members)[m.member]->name]--;
+  }
   auto loadMembers = [&](const std::string &var, const std::string &at) {
     for (size_t k = 0; k < agentDecl->members->size(); k++) {
       const AST::AgentMember &m = *(*agentDecl->members)[k];
       bool used = cur && cur->accessedMembers.count(m.name);
       if (!used) continue;
+      if (!maccs.empty() && fp64Reads[m.name] <= 0) continue;
       *this << nl << var << "." << m.name << " = ((const " << cType(m.type->resolved)
             << " *) abl_NB.cols[" << (int) k << "])[" << at << "];";
     }
@@ -704,7 +792,25 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   deferredPass = false;
   deferredMasks = savedMasks;
   nearLoopDepth = -1;
-  *this << outdent << nl << "}" << outdent << nl << "}";
+  *this << outdent << nl << "}";
+  // Mixed precision: the FP32 sums back into their FP64 variables.
+  for (const MixedAcc &m : maccs) {
+    const AST::VarExpression &v = *dynamic_cast<const AST::VarExpression *>(&*m.stmt->left);
+    std::string fn = m.isPos ? "offset_total(" + mixedAnchor + ", " : "total(";
+    *this << nl << v << " = ";
+    if (m.comps == 1) {
+      *this << v << " + " << m.acc << "." << fn << "0);";
+    } else {
+      const char *vt = m.comps == 2 ? "float2" : "float3";
+      *this << vt << "_add(" << v << ", " << vt << "_create(";
+      for (int d = 0; d < m.comps; d++)
+        *this << (d ? ", " : "") << m.acc << "." << fn << d << ")";
+      *this << "));";
+    }
+  }
+  mixedAccs = savedMixed;
+  mixedAnchor = savedAnchor;
+  *this << outdent << nl << "}";
   if (nearNeedsEnd) *this << nl << nearEndLabel << ": ;";
   nearEndLabel = savedLabel;
   nearNeedsEnd = savedNeeds;
@@ -813,6 +919,28 @@ void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
     for (size_t k = 0; k < nearAgent->members->size(); k++) {
       const AST::AgentMember &m = *(*nearAgent->members)[k];
       if (decl.accessedMembers.count(m.name) || m.isPosition) info.nearMembers |= 1u << k;
+    }
+    // Mixed precision: members read only by FP32 sums come from float
+    // copies and need no FP64 copy (the position's is kept for the radius
+    // test).
+    std::vector<MixedAcc> maccs = findMixedAccs(*loop, *nearAgent);
+    if (!maccs.empty()) {
+      std::map<int, int> reads;
+      for (auto *ma : collect(*loop->stmt).members) {
+        auto *v = dynamic_cast<const AST::VarExpression *>(&*ma->expr);
+        if (!v || v->var->id != loop->var->id) continue;
+        for (size_t k = 0; k < nearAgent->members->size(); k++)
+          if ((*nearAgent->members)[k]->name == ma->member) reads[(int) k]++;
+      }
+      for (const MixedAcc &m : maccs) {
+        reads[m.member]--;
+        if (m.isPos) info.nearPosLo = true;
+        else info.nearMembersF32 |= 1u << m.member;
+      }
+      for (auto &kv : reads) {
+        if (kv.second <= 0 && !(*nearAgent->members)[kv.first]->isPosition)
+          info.nearMembers &= ~(1u << kv.first);
+      }
     }
     // The radius must not depend on the agent: it sizes the grid search.  A
     // step-local variable holding a value of globals (`float radius = 125;`
@@ -1439,9 +1567,13 @@ void CudaPrinter::printDescriptor() {
           << (s.ordered ? 1 : 0) << ", " << (s.nearLoop ? "abl_radius_" + n : "nullptr") << ", "
           << s.nearMembers << "u, " << s.outAlways << "u, abl_launch_" << n << ", "
           << (s.usesRemove ? 1 : 0) << ", " << s.addType << ", " << (copyOut() ? 1 : 0) << ", "
-          << (s.addType < 0 && !s.usesRemove ? "abl_launch_ens_" + n : std::string("nullptr"))
+          << (s.addType < 0 && !s.usesRemove && !s.nearMembersF32 && !s.nearPosLo
+                  ? "abl_launch_ens_" + n : std::string("nullptr"))
           << ", " << (s.usesRng ? 1 : 0) << ", " << (s.presorted ? 1 : 0) << ", " << s.outChanged
-          << "u, " << (s.nearCacheable ? 1 : 0) << "},";
+          << "u, " << (s.nearCacheable ? 1 : 0);
+    if (s.nearMembersF32 || s.nearPosLo)
+      *this << ", " << s.nearMembersF32 << "u, " << (s.nearPosLo ? 1 : 0);
+    *this << "},";
   }
   if (steps.empty()) *this << nl << "{nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0, 0},";
   *this << outdent << nl << "};" << nl;

@@ -42,6 +42,7 @@ struct CudaPrinter : public CPrinter {
   void print(const AST::BreakStatement &) override;
   void print(const AST::SimulateStatement &) override;
   void print(const AST::VarDeclarationStatement &) override;
+  void print(const AST::AssignOpStatement &) override;
   void print(const AST::FunctionDeclaration &) override;
   void print(const AST::Script &) override;
 
@@ -56,6 +57,9 @@ public:
   // Runtime settings the generated main() applies before simulating
   // (-C cuda.near_mode, cuda.near_cache, cuda.balance); -1: the default.
   int nearMode = -1, nearCache = -1, balance = -1;
+  // -C cuda.precision=mixed: near-loop sums of neighbour members in FP32,
+  // everything else in FP64 (an FP64 build only).
+  bool mixed = false;
 
 private:
 
@@ -85,6 +89,19 @@ private:
   std::map<const AST::IfStatement *, std::string> deferredMasks;
   // Printing the second pass: declarations are printed with their exact value.
   bool deferredPass = false;
+  // Mixed precision: the current near body's accumulations `acc += nx.m`
+  // that run in FP32, by statement, with the name of their FP32 accumulator.
+  struct MixedAcc {
+    const AST::AssignOpStatement *stmt = nullptr;
+    std::string acc;     // the FP32 accumulator (abl::facc)
+    int member = -1;     // index of the neighbour member
+    bool isPos = false;  // summed as offsets from the querying position
+    int comps = 1;
+  };
+  std::map<const AST::AssignOpStatement *, MixedAcc> mixedAccs;
+  std::string mixedAnchor;
+  std::vector<MixedAcc> findMixedAccs(const AST::ForStatement &loop,
+                                      const AST::AgentDeclaration &nearAgent);
 
   // Kind of function being printed (decides how builtins are lowered).
   enum class FnKind { HOST, STEP, USER, SEQ } fnKind = FnKind::HOST;
@@ -109,6 +126,10 @@ private:
     bool usesRemove = false;
     int addType = -1;
     bool usesRng = false;
+    // Mixed precision: neighbour members summed from float copies, and
+    // whether position offsets are summed (the position's low part).
+    unsigned nearMembersF32 = 0;
+    bool nearPosLo = false;
     // The step's only near loop is ordered and iterates around the step's own
     // agent: the kernel gathers and sorts neighbour lists per block.
     bool presorted = false;

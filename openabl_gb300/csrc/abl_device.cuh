@@ -61,6 +61,16 @@
 
 namespace abl {
 
+// FP64 additions on this GPU issue faster as fused multiply-adds than as
+// adds (measured: abl_diag_fp64_add_as_fma_rate against abl_diag_fp64_rates).
+// fma(a, 1, b) rounds a * 1 + b = a + b once, so it is the same correctly
+// rounded sum (signed zeros included); a - b is fma(b, -1, a).  The 1.0 lives
+// in constant memory so that the compiler cannot fold the fma back into an
+// add.
+static __constant__ double fp64_one = 1.0;
+__device__ __forceinline__ double dadd(double a, double b) { return __fma_rn(a, fp64_one, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __fma_rn(b, -fp64_one, a); }
+
 // Cell coordinate of x along one axis; out-of-range positions are clamped
 // into the border cells (monotone, so neighbours within one cell width stay
 // within one cell index).
@@ -1129,5 +1139,67 @@ template <int DIM, typename Exact, typename R>
 __device__ inline bool operator==(R r, const lazy_dist<DIM, Exact> &a) { return a == r; }
 template <int DIM, typename Exact, typename R>
 __device__ inline bool operator!=(R r, const lazy_dist<DIM, Exact> &a) { return a != r; }
+
+// ------------------------------------------------ mixed precision (-C cuda.precision=mixed)
+//
+// A near-loop accumulation `acc += nx.m` of a floating-point member runs in
+// FP32 in the mixed form; everything else (the radius test, the body's other
+// arithmetic, the step's integration) stays FP64.
+//  - m the position: the sum of offsets from the querying position p,
+//    (nx.pos - p), each formed from the neighbour's position split in two
+//    floats (hi = (float) pos, lo = (float) (pos - hi), slot-ordered copies
+//    made by the binning) minus p split the same way; after the loop
+//    acc += n * p + sum.  The offsets are short (within the radius), so
+//    their FP32 sum keeps ~2^-24 of the radius, not of the coordinates.
+//  - another member: the FP32 sum of its float copy; after the loop
+//    acc += sum.
+
+template <int DIM>
+struct mixed_anchor {
+  double p[3];
+  float hi[3], lo[3];
+  __device__ mixed_anchor(double x, double y, double z) {
+    const double q[3] = {x, y, z};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      p[d] = d < DIM ? q[d] : 0.0;
+      hi[d] = (float) p[d];
+      lo[d] = (float) (p[d] - (double) hi[d]);
+    }
+  }
+};
+
+template <int DIM>
+struct facc {
+  float v[DIM];
+  int n;
+  __device__ facc() : n(0) {
+#pragma unroll
+    for (int d = 0; d < DIM; d++) v[d] = 0.0f;
+  }
+  // += (position of slot s) - anchor
+  __device__ __forceinline__ void add_offset(const abl_near_view &V, int s,
+                                             const mixed_anchor<DIM> &a) {
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      const float hi = __fsub_rn(__ldg(&V.posf[DIM * s + d]), a.hi[d]);
+      const float lo = __fsub_rn(__ldg(&V.poslo[DIM * s + d]), a.lo[d]);
+      v[d] = __fadd_rn(v[d], __fadd_rn(hi, lo));
+    }
+    n++;
+  }
+  // += float copy of member column `k` at slot s (DIM components)
+  __device__ __forceinline__ void add_member(const abl_near_view &V, int k, int s) {
+    const float *c = (const float *) V.fcols[k];
+#pragma unroll
+    for (int d = 0; d < DIM; d++) v[d] = __fadd_rn(v[d], __ldg(&c[DIM * s + d]));
+    n++;
+  }
+  // The accumulated value in FP64: n * anchor + offsets, or the plain sum.
+  __device__ __forceinline__ double offset_total(const mixed_anchor<DIM> &a, int d) const {
+    return a.p[d] * (double) n + (double) v[d];
+  }
+  __device__ __forceinline__ double total(int d) const { return (double) v[d]; }
+};
 
 }  // namespace abl

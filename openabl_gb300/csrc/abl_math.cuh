@@ -30,11 +30,25 @@ __host__ __device__ static inline float2 float2_create(abl_float x, abl_float y)
   return r;
 }
 __host__ __device__ static inline float2 float2_fill(abl_float x) { return float2_create(x, x); }
+// Sums and differences of components; FP64 ones on the device go through
+// abl::dadd / abl::dsub (the same correctly rounded results).
+__host__ __device__ static inline abl_float abl_add(abl_float a, abl_float b) {
+#ifdef __CUDA_ARCH__
+  if (sizeof(abl_float) == sizeof(double)) return (abl_float) abl::dadd((double) a, (double) b);
+#endif
+  return a + b;
+}
+__host__ __device__ static inline abl_float abl_sub(abl_float a, abl_float b) {
+#ifdef __CUDA_ARCH__
+  if (sizeof(abl_float) == sizeof(double)) return (abl_float) abl::dsub((double) a, (double) b);
+#endif
+  return a - b;
+}
 __host__ __device__ static inline float2 float2_add(float2 a, float2 b) {
-  return float2_create(a.x + b.x, a.y + b.y);
+  return float2_create(abl_add(a.x, b.x), abl_add(a.y, b.y));
 }
 __host__ __device__ static inline float2 float2_sub(float2 a, float2 b) {
-  return float2_create(a.x - b.x, a.y - b.y);
+  return float2_create(abl_sub(a.x, b.x), abl_sub(a.y, b.y));
 }
 __host__ __device__ static inline float2 float2_mul_scalar(float2 a, abl_float s) {
   return float2_create(a.x * s, a.y * s);
@@ -69,10 +83,10 @@ __host__ __device__ static inline float3 float3_create(abl_float x, abl_float y,
 }
 __host__ __device__ static inline float3 float3_fill(abl_float x) { return float3_create(x, x, x); }
 __host__ __device__ static inline float3 float3_add(float3 a, float3 b) {
-  return float3_create(a.x + b.x, a.y + b.y, a.z + b.z);
+  return float3_create(abl_add(a.x, b.x), abl_add(a.y, b.y), abl_add(a.z, b.z));
 }
 __host__ __device__ static inline float3 float3_sub(float3 a, float3 b) {
-  return float3_create(a.x - b.x, a.y - b.y, a.z - b.z);
+  return float3_create(abl_sub(a.x, b.x), abl_sub(a.y, b.y), abl_sub(a.z, b.z));
 }
 __host__ __device__ static inline float3 float3_mul_scalar(float3 a, abl_float s) {
   return float3_create(a.x * s, a.y * s, a.z * s);

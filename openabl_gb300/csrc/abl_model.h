@@ -77,6 +77,10 @@ typedef struct {
                                from the query agent's index */
   int ncache_narrow;
   int cell_f32;             /* query cells may be computed in FP32 (as the binning does) */
+  /* mixed precision: slot-ordered float copies of the members a loop sums in
+     FP32, and the low part of the position, (float) (pos - (double) posf) */
+  const void *fcols[ABL_MAX_MEMBERS];
+  const float *poslo;
 } abl_near_view;
 
 /* Everything a generated step launcher needs. */
@@ -149,6 +153,9 @@ typedef struct {
   uint32_t out_changed;         /* bitmask of members the body may set to anything but the
                                    agent's own `in` value (`out.m = in.m` does not count) */
   int near_cacheable;           /* one near loop, centred on the step's own agent */
+  uint32_t near_members_f32;    /* mixed precision: neighbour members summed from float copies */
+  int near_pos_lo;              /* mixed precision: the loop sums position offsets (needs the
+                                   position's low part) */
 } abl_step_desc;
 
 /* Host function run after every timestep: the `sequential step`. */

@@ -805,6 +805,12 @@ struct TypeState {
   int *order = nullptr;
   float *posf = nullptr;
   void *gcols[ABL_MAX_MEMBERS] = {};
+  // Mixed precision: members summed in FP32 get slot-ordered float copies,
+  // and position offsets need the position's low part.
+  uint32_t gather_f32_mask = 0;
+  bool gather_pos_lo = false;
+  void *fcols[ABL_MAX_MEMBERS] = {};
+  float *poslo = nullptr;
   int *nb_cnt = nullptr, *nb_off = nullptr, *nb_list = nullptr;
   SepLevels sep;
   ScanPlan cell_scan, nb_scan;
@@ -1062,6 +1068,8 @@ void free_bins(abl_ctx *ctx, TypeState &t) {
   t.sep = SepLevels();
   t.posf = nullptr;
   for (auto &g : t.gcols) g = nullptr;
+  for (auto &f : t.fcols) f = nullptr;
+  t.poslo = nullptr;
 }
 
 // Sizes one grid per (neighbour type, cell size) -- the cells of a near
@@ -1119,6 +1127,8 @@ int prepare(abl_ctx *ctx) {
     g.ordered = g.ordered || depth == 2;
     g.rows = g.rows || depth == 1;
     g.gather_mask |= sd.near_members;
+    g.gather_f32_mask |= sd.near_members_f32;
+    g.gather_pos_lo = g.gather_pos_lo || sd.near_pos_lo;
     ctx->step_grid[k] = gi;
   }
   for (size_t gi = 0; gi < ctx->grids.size(); gi++) {
@@ -1173,7 +1183,13 @@ int prepare(abl_ctx *ctx) {
         ABL_TRY(dev_alloc(ctx, &p, member_bytes(g.d->members[k]) * n, own));
         g.gcols[k] = p;
       }
+      if (g.gather_f32_mask & (1u << k)) {
+        void *p = nullptr;
+        ABL_TRY(dev_alloc(ctx, &p, sizeof(float) * g.d->members[k].components * n, own));
+        g.fcols[k] = p;
+      }
     }
+    if (g.gather_pos_lo) ABL_TRY(dev_alloc_t(ctx, &g.poslo, n * dim, own));
     if (g.ordered || g.rows) {
       long span = 2 * g.R + 1, level = n;
       const int inter = g.ordered ? dim - 1 : 1;  // levels kept as (id, slot) lists
@@ -1443,6 +1459,53 @@ void build_lists(abl_ctx *ctx, const G &geo, int dim, int levels, int Rmax, long
 
 // Slot-ordered copies of the gathered members (and, with_pos, the float
 // positions); without with_pos the position member itself is skipped too.
+// Mixed precision: float copies of members summed in FP32, and the
+// position's low part (float) (pos - (double) posf), in slot order.
+struct GatherF32Args {
+  int nmem;
+  const double *src[ABL_MAX_MEMBERS];
+  float *dst[ABL_MAX_MEMBERS];
+  int comps[ABL_MAX_MEMBERS];
+};
+
+template <int DIM>
+__global__ void k_gather_f32(long n, const int *order, const double *pos, const float *posf,
+                             float *poslo, const __grid_constant__ GatherF32Args g) {
+  long s = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  long i = order[s];
+  if (poslo) {
+#pragma unroll
+    for (int d = 0; d < DIM; d++)
+      poslo[DIM * s + d] = (float) (pos[DIM * i + d] - (double) posf[DIM * s + d]);
+  }
+  for (int k = 0; k < g.nmem; k++) {
+    const int c = g.comps[k];
+    for (int j = 0; j < c; j++) g.dst[k][c * s + j] = (float) g.src[k][c * i + j];
+  }
+}
+
+void launch_gather_f32(abl_ctx *ctx, TypeState &t, int dim, bool with_pos) {
+  GatherF32Args g;
+  std::memset(&g, 0, sizeof g);
+  for (int k = 0; k < t.d->num_members; k++) {
+    if (!(t.gather_f32_mask & (1u << k))) continue;
+    if (!with_pos && k == t.d->position_member) continue;
+    g.src[g.nmem] = (const double *) t.cols[t.cur][k];
+    g.dst[g.nmem] = (float *) t.fcols[k];
+    g.comps[g.nmem] = t.d->members[k].components;
+    g.nmem++;
+  }
+  float *poslo = with_pos && t.gather_pos_lo ? t.poslo : nullptr;
+  if (!poslo && g.nmem == 0) return;
+  const double *pos = (const double *) t.cols[t.cur][t.d->position_member];
+  const int B = 256;
+  long nb = blocks_for(t.n, B);
+  if (dim == 2) k_gather_f32<2><<<nb, B, 0, ctx->stream>>>(t.n, t.order, pos, t.posf, poslo, g);
+  else k_gather_f32<3><<<nb, B, 0, ctx->stream>>>(t.n, t.order, pos, t.posf, poslo, g);
+  ctx->launches++;
+}
+
 template <typename Real>
 void launch_gather(abl_ctx *ctx, TypeState &t, int dim, bool with_pos) {
   cudaStream_t s = ctx->stream;
@@ -1465,7 +1528,10 @@ void launch_gather(abl_ctx *ctx, TypeState &t, int dim, bool with_pos) {
   for (int k = 0; k < g.nmem; k++) g.all16 = g.all16 && g.bytes[k] == 16;
   // The position taken from its gathered copy only for double 2D positions.
   if (!(dim == 2 && sizeof(Real) == 8)) g.pos16 = -1;
-  if (!with_pos && g.nmem == 0) return;
+  if (!with_pos && g.nmem == 0) {
+    if (sizeof(Real) == 8 && t.gather_f32_mask) launch_gather_f32(ctx, t, dim, false);
+    return;
+  }
   float *posf = with_pos ? t.posf : nullptr;
   if (dim == 2) {
     k_gather<Real, 2><<<nb, B, 0, s>>>(t.n, t.order, pos, posf, g);
@@ -1473,6 +1539,8 @@ void launch_gather(abl_ctx *ctx, TypeState &t, int dim, bool with_pos) {
     k_gather<Real, 3><<<nb, B, 0, s>>>(t.n, t.order, pos, posf, g);
   }
   ctx->launches++;
+  if (sizeof(Real) == 8 && (t.gather_f32_mask || t.gather_pos_lo))
+    launch_gather_f32(ctx, t, dim, with_pos);
 }
 
 // Whether a grid may compute cell coordinates in FP32 (k_bin_assign).  The
@@ -1764,8 +1832,11 @@ void launch_nc_lists(abl_ctx *ctx, const TypeState &g, double radius, int *count
 
 // Whether step k keeps its neighbour lists.
 bool near_cache_wanted(const abl_ctx *ctx, const abl_step_desc &sd) {
+  // Kept lists index neighbours by agent; the float copies of the mixed
+  // form are slot-ordered, so such loops search the grid.
   return ctx->near_cache && sd.near_cacheable && sd.agent_type == sd.near_type
-      && positions_static(ctx->model, sd.agent_type);
+      && positions_static(ctx->model, sd.agent_type) && !sd.near_members_f32
+      && !sd.near_pos_lo;
 }
 
 void nc_release(abl_ctx *ctx, StepState &st, void *p) {
@@ -1952,7 +2023,11 @@ int step_once(abl_ctx *ctx) {
       V.posf = nt.posf;
       V.nb_off = nt.nb_off;
       V.nb_list = nt.nb_list;
-      for (int j = 0; j < nt.d->num_members; j++) V.cols[j] = nt.gcols[j];
+      for (int j = 0; j < nt.d->num_members; j++) {
+        V.cols[j] = nt.gcols[j];
+        V.fcols[j] = nt.fcols[j];
+      }
+      V.poslo = nt.poslo;
       V.balance = ctx->balance;
       V.cap = V.ordered ? ctx->list_cap : ctx->runs_cap;
       V.cell_of = sd.agent_type == sd.near_type ? nt.cell_of : nullptr;
@@ -2919,6 +2994,7 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
   {
     const abl_step_desc &s0 = model->steps[0];
     if (s0.uses_remove || s0.add_type >= 0 || s0.uses_rng) return ABL_E_UNSUPPORTED;
+    if (s0.near_members_f32 || s0.near_pos_lo) return ABL_E_UNSUPPORTED;  // mixed form
   }
   if ((long) n > kNoAllocMaxAgents) return ABL_E_SCRATCH;
   const abl_agent_desc &ad = model->agents[0];

@@ -1,0 +1,445 @@
+// Generated by OpenABL -b cuda (model "boids2d_mixed").
+#include "abl_gen.cuh"
+
+namespace abl_model_boids2d_mixed {
+
+typedef double abl_float;
+#include "abl_math.cuh"
+
+typedef struct {
+    float2 pos;
+    float2 velocity;
+} Boid;
+static const type_info Boid_info[] = {
+    { TYPE_FLOAT2, offsetof(Boid, pos), "pos", true },
+    { TYPE_FLOAT2, offsetof(Boid, velocity), "velocity", false },
+    { TYPE_END, sizeof(Boid), NULL }
+};
+
+struct agent_struct {
+    dyn_array agents_Boid;
+    dyn_array agents_Boid_dbuf;
+};
+static struct agent_struct agents;
+static const agent_info agents_info[] = {
+    { Boid_info, offsetof(struct agent_struct, agents_Boid), "Boid" },
+    { NULL, 0, NULL }
+};
+
+struct abl_globals {
+    double PI;
+    double interaction_radius;
+    double separation_radius;
+    double agent_density;
+    double time_scale;
+    double global_scale;
+    double steer_scale;
+    double collision_scale;
+    double match_scale;
+    int num_agents;
+    int num_timesteps;
+    double min_pos;
+    double max_pos;
+};
+static const abl_globals abl_globals_default = {
+    3.14159,
+    0.05,
+    0.005,
+    500.0,
+    0.0005,
+    0.15,
+    0.65,
+    0.75,
+    1.25,
+    5000,
+    100,
+    0.0,
+    3.16228,
+};
+static abl_globals abl_G = abl_globals_default;
+static abl::rng abl_R;  // unused on the host: main() draws from the host stream
+struct abl_cols_Boid {
+    float2 *pos;
+    float2 *velocity;
+};
+
+__host__ __device__ static inline float2 random_1(const abl_globals &abl_G, abl::rng &abl_R, float2 min, float2 max) {
+    return ([&]() { const auto abl_e1_1 = abl_random(abl_R, min.y, max.y); const auto abl_e1_0 = abl_random(abl_R, min.x, max.x); return float2_create(abl_e1_0, abl_e1_1); }());
+}
+__host__ __device__ static inline float3 random_2(const abl_globals &abl_G, abl::rng &abl_R, float3 min, float3 max) {
+    return ([&]() { const auto abl_e2_2 = abl_random(abl_R, min.z, max.z); const auto abl_e2_1 = abl_random(abl_R, min.y, max.y); const auto abl_e2_0 = abl_random(abl_R, min.x, max.x); return float3_create(abl_e2_0, abl_e2_1, abl_e2_2); }());
+}
+__host__ __device__ static inline double random_3(const abl_globals &abl_G, abl::rng &abl_R, double max) {
+    return abl_random(abl_R, 0, max);
+}
+__host__ __device__ static inline float2 random_4(const abl_globals &abl_G, abl::rng &abl_R, float2 max) {
+    return random_1(abl_G, abl_R, float2_fill(0), max);
+}
+__host__ __device__ static inline float3 random_5(const abl_globals &abl_G, abl::rng &abl_R, float3 max) {
+    return random_2(abl_G, abl_R, float3_fill(0), max);
+}
+__host__ __device__ static inline int randomInt_1(const abl_globals &abl_G, abl::rng &abl_R, int max) {
+    return abl_random_int(abl_R, 0, max);
+}
+__host__ __device__ static inline double clamp(const abl_globals &abl_G, abl::rng &abl_R, double pos, double min, double max) {
+    return ((pos < min) ? min : ((pos > max) ? max : pos));
+}
+__host__ __device__ static inline float2 clamp_1(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 min, float2 max) {
+    return float2_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)));
+}
+__host__ __device__ static inline float3 clamp_2(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 min, float3 max) {
+    return float3_create(((pos.x < min.x) ? min.x : ((pos.x > max.x) ? max.x : pos.x)), ((pos.y < min.y) ? min.y : ((pos.y > max.y) ? max.y : pos.y)), ((pos.z < min.z) ? min.z : ((pos.z > max.z) ? max.z : pos.z)));
+}
+__host__ __device__ static inline double clamp_3(const abl_globals &abl_G, abl::rng &abl_R, double pos, double max) {
+    return clamp(abl_G, abl_R, pos, 0, max);
+}
+__host__ __device__ static inline float2 clamp_4(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return clamp_1(abl_G, abl_R, pos, float2_fill(0), max);
+}
+__host__ __device__ static inline float3 clamp_5(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 max) {
+    return clamp_2(abl_G, abl_R, pos, float3_fill(0), max);
+}
+__host__ __device__ static inline double wraparound(const abl_globals &abl_G, abl::rng &abl_R, double pos, double max) {
+    return ((pos < 0) ? (max + pos) : ((pos >= max) ? (pos - max) : pos));
+}
+__host__ __device__ static inline float2 wraparound_1(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return float2_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)));
+}
+__host__ __device__ static inline float3 wraparound_2(const abl_globals &abl_G, abl::rng &abl_R, float3 pos, float3 max) {
+    return float3_create(((pos.x < 0) ? (max.x + pos.x) : ((pos.x >= max.x) ? (pos.x - max.x) : pos.x)), ((pos.y < 0) ? (max.y + pos.y) : ((pos.y >= max.y) ? (pos.y - max.y) : pos.y)), ((pos.z < 0) ? (max.z + pos.z) : ((pos.z >= max.z) ? (pos.z - max.z) : pos.z)));
+}
+__host__ __device__ static inline bool is_inside(const abl_globals &abl_G, abl::rng &abl_R, float2 pos, float2 max) {
+    return ((((pos.x >= 0) && (pos.y >= 0)) && (pos.x <= max.x)) && (pos.y <= max.y));
+}
+__host__ __device__ static inline float2 boundPosition(const abl_globals &abl_G, abl::rng &abl_R, float2 pos) {
+    return float2_create(((pos.x < abl_G.min_pos) ? abl_G.max_pos : ((pos.x > abl_G.max_pos) ? abl_G.min_pos : pos.x)), ((pos.y < abl_G.min_pos) ? abl_G.max_pos : ((pos.y > abl_G.max_pos) ? abl_G.min_pos : pos.y)));
+}
+__device__ static void update_boid(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Boid* in, Boid* out) {
+    abl::rng &abl_R = abl_K.R;
+    (void) abl_R; (void) abl_NB;
+    float2 global_velocity = float2_create(0, 0);
+    float2 global_center = float2_create(0, 0);
+    float2 collision_center = float2_create(0, 0);
+    int interaction_count = 0;
+    int collision_count = 0;
+    {
+        const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
+        abl::near_list_cursor<2> abl_c1(abl_NB, abl_q1, abl_K);
+        const abl::mixed_anchor<2> abl_ma1((double) in->pos.x, (double) in->pos.y, 0.0);
+        abl::facc<2> abl_fa1_0;
+        abl::facc<2> abl_fa1_1;
+        abl::facc<2> abl_fa1_2;
+        auto abl_exact1 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, in->pos) > abl_G.interaction_radius);
+        };
+        while (abl_c1.fill(abl_q1, abl_exact1)) {
+            int abl_pslot1 = abl_c1.slot(0);
+            Boid abl_pnx1;
+            abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
+            unsigned long long abl_dm1_0 = 0ull;
+            for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
+                const int abl_slot1 = abl_pslot1;
+                Boid abl_nx1 = abl_pnx1;
+                if (abl_k + 1 < abl_c1.cnt) {
+                    abl_pslot1 = abl_c1.slot(abl_k + 1);
+                    abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
+                }
+                Boid* nx = &abl_nx1;
+                {
+                    abl_fa1_0.add_offset(abl_NB, abl_slot1, abl_ma1);
+                    abl_fa1_1.add_member(abl_NB, 1, abl_slot1);
+                    interaction_count += 1;
+                    const auto separation = abl::make_lazy_dist(abl_q1, abl_NB, abl_slot1, [&]() -> abl_float { return dist_float2(in->pos, nx->pos); });
+                    if ((separation < abl_G.separation_radius)) abl_dm1_0 |= 1ull << abl_k;
+                }
+            }
+            for (unsigned long long abl_m = abl_dm1_0; abl_m; abl_m &= abl_m - 1ull) {
+                const int abl_slot1 = abl_c1.slot(__ffsll((long long) abl_m) - 1);
+                Boid abl_nx1;
+                abl_nx1.pos = ((const float2 *) abl_NB.cols[0])[abl_slot1];
+                Boid* nx = &abl_nx1;
+                {
+                    abl_fa1_2.add_offset(abl_NB, abl_slot1, abl_ma1);
+                    collision_count += 1;
+                }
+            }
+        }
+        global_center = float2_add(global_center, float2_create(abl_fa1_0.offset_total(abl_ma1, 0), abl_fa1_0.offset_total(abl_ma1, 1)));
+        global_velocity = float2_add(global_velocity, float2_create(abl_fa1_1.total(0), abl_fa1_1.total(1)));
+        collision_center = float2_add(collision_center, float2_create(abl_fa1_2.offset_total(abl_ma1, 0), abl_fa1_2.offset_total(abl_ma1, 1)));
+    }
+    float2 velocity_change = float2_create(0, 0);
+    float2 steer_velocity = float2_create(0, 0);
+    if ((interaction_count > 0)) {
+        global_center = float2_div_scalar(global_center, interaction_count);
+        steer_velocity = float2_mul_scalar(float2_sub(global_center, in->pos), abl_G.steer_scale);
+    }
+    velocity_change = float2_add(velocity_change, steer_velocity);
+    float2 match_velocity = float2_create(0, 0);
+    if ((interaction_count > 0)) {
+        global_velocity = float2_div_scalar(global_velocity, interaction_count);
+        match_velocity = float2_mul_scalar(global_velocity, abl_G.match_scale);
+    }
+    velocity_change = float2_add(velocity_change, match_velocity);
+    float2 avoid_velocity = float2_create(0, 0);
+    if ((collision_count > 0)) {
+        collision_center = float2_div_scalar(collision_center, collision_count);
+        avoid_velocity = float2_mul_scalar(float2_sub(in->pos, collision_center), abl_G.collision_scale);
+    }
+    velocity_change = float2_add(velocity_change, avoid_velocity);
+    float2 new_velocity = float2_add(in->velocity, float2_mul_scalar(velocity_change, abl_G.global_scale));
+    double new_velocity_scale = length_float2(new_velocity);
+    if ((new_velocity_scale > 1)) {
+        new_velocity = float2_div_scalar(new_velocity, new_velocity_scale);
+    }
+    float2 new_pos = float2_add(in->pos, float2_mul_scalar(new_velocity, abl_G.time_scale));
+    new_pos = boundPosition(abl_G, abl_R, new_pos);
+    out->pos = new_pos;
+    out->velocity = new_velocity;
+}
+
+struct abl_kargs_update_boid {
+    abl_globals G;
+    long n;
+    const int *visit;
+    abl_cols_Boid in, out;
+    abl_near_view NB;
+    uint8_t *removed;
+    uint8_t *child_flag;
+    void *child_cols[ABL_MAX_MEMBERS];
+    uint64_t seed;
+    long timestep;
+    int step_index;
+    uint32_t skip_store;
+    unsigned long long *serial_rng;
+};
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_update_boid(const __grid_constant__ abl_kargs_update_boid A) {
+    int abl_j;
+    {
+        const abl_globals &abl_G = A.G;
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
+        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.interaction_radius);
+        };
+        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seed, (uint32_t) abl_i, (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.xs = A.serial_rng;
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = A.child_cols;
+    abl_K.near_col = abl_j;
+    Boid abl_in, abl_out;
+    abl_in.pos = A.in.pos[abl_i];
+    abl_in.velocity = A.in.velocity[abl_i];
+    update_boid(A.G, A.NB, abl_K, &abl_in, &abl_out);
+    A.out.pos[abl_i] = abl_out.pos;
+    A.out.velocity[abl_i] = abl_out.velocity;
+}
+static int abl_launch_update_boid(const abl_step_launch *L, cudaStream_t abl_stream) {
+    abl_kargs_update_boid A;
+    A.G = *(const abl_globals *) L->globals;
+    A.n = L->n;
+    A.visit = L->visit_order;
+    A.in.pos = (float2 *) L->in_cols[0];
+    A.out.pos = (float2 *) L->out_cols[0];
+    A.in.velocity = (float2 *) L->in_cols[1];
+    A.out.velocity = (float2 *) L->out_cols[1];
+    A.NB = L->near;
+    A.removed = L->removed;
+    A.child_flag = L->child_flag;
+    for (int k = 0; k < ABL_MAX_MEMBERS; k++) A.child_cols[k] = L->child_cols[k];
+    A.seed = L->seed;
+    A.timestep = L->timestep;
+    A.step_index = L->step_index;
+    A.skip_store = L->skip_store;
+    A.serial_rng = L->serial_rng;
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (A.n + abl_block - 1) / abl_block;
+    abl_kernel_update_boid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_update_boid(const __grid_constant__ abl_ens_launch A) {
+    int abl_j;
+    {
+        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const bool abl_has = abl_t1 < A.n;
+        const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
+        const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
+        const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
+        const abl_near_view &abl_V1 = A.views[abl_r1];
+        const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
+        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
+        auto abl_x0 = [&](int abl_s) -> bool {
+            const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
+            return !(dist_float2(abl_p, abl_p1) > abl_G.interaction_radius);
+        };
+        abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
+    }
+    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    if (abl_t >= A.n) return;
+    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
+    const int abl_r = A.replica[abl_i];
+    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
+    abl::step_ctx abl_K;
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.self = abl_i;
+    abl_K.removed = 0;
+    abl_K.added = 0;
+    abl_K.child_cols = nullptr;
+    abl_K.near_col = abl_j;
+    Boid abl_in, abl_out;
+    abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
+    abl_in.velocity = ((const float2 *) A.in_cols[1])[abl_i];
+    update_boid(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
+    ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
+    ((float2 *) A.out_cols[1])[abl_i] = abl_out.velocity;
+}
+static int abl_launch_ens_update_boid(const abl_ens_launch *L, cudaStream_t abl_stream) {
+    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
+    const long abl_grid = (L->n + abl_block - 1) / abl_block;
+    abl_kernel_ens_update_boid<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
+    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
+}
+static double abl_radius_update_boid(const void *abl_gp) {
+    const abl_globals &abl_G = *(const abl_globals *) abl_gp;
+    abl::rng abl_R;
+    (void) abl_G; (void) abl_R;
+    return (double) (abl_G.interaction_radius);
+}
+
+
+static const abl_member_desc abl_members_Boid[] = {
+    {"pos", ABL_T_FLOAT2, 2, 8, 1},
+    {"velocity", ABL_T_FLOAT2, 2, 8, 0},
+};
+static const abl_agent_desc abl_agents[] = {
+    {"Boid", 2, abl_members_Boid, 0, 2},
+};
+static const abl_global_desc abl_global_table[] = {
+    {"PI", ABL_T_FLOAT, offsetof(abl_globals, PI)},
+    {"interaction_radius", ABL_T_FLOAT, offsetof(abl_globals, interaction_radius)},
+    {"separation_radius", ABL_T_FLOAT, offsetof(abl_globals, separation_radius)},
+    {"agent_density", ABL_T_FLOAT, offsetof(abl_globals, agent_density)},
+    {"time_scale", ABL_T_FLOAT, offsetof(abl_globals, time_scale)},
+    {"global_scale", ABL_T_FLOAT, offsetof(abl_globals, global_scale)},
+    {"steer_scale", ABL_T_FLOAT, offsetof(abl_globals, steer_scale)},
+    {"collision_scale", ABL_T_FLOAT, offsetof(abl_globals, collision_scale)},
+    {"match_scale", ABL_T_FLOAT, offsetof(abl_globals, match_scale)},
+    {"num_agents", ABL_T_INT, offsetof(abl_globals, num_agents)},
+    {"num_timesteps", ABL_T_INT, offsetof(abl_globals, num_timesteps)},
+    {"min_pos", ABL_T_FLOAT, offsetof(abl_globals, min_pos)},
+    {"max_pos", ABL_T_FLOAT, offsetof(abl_globals, max_pos)},
+    {nullptr, 0, 0}
+};
+static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max) {
+    const abl_globals &abl_G = *(const abl_globals *) abl_gp;
+    abl::rng abl_R;
+    (void) abl_G; (void) abl_R;
+    float2 abl_lo = float2_fill(abl_G.min_pos);
+    float2 abl_hi = float2_fill(abl_G.max_pos);
+    abl_min[0] = abl_lo.x; abl_min[1] = abl_lo.y; abl_min[2] = 0;
+    abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
+}
+static const abl_step_desc abl_steps[] = {
+    {"update_boid", 0, 0, 1, abl_radius_update_boid, 1u, 3u, abl_launch_update_boid, 0, -1, 0, nullptr, 0, 1, 3u, 1, 2u, 1},
+};
+static const abl_step_desc abl_steps_ordered[] = {
+    abl_steps[0],
+    {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
+};
+extern const abl_model_desc abl_desc = {
+    "boids2d_mixed", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 13, abl_global_table, 2, abl_env_bounds, nullptr, 0, nullptr
+};
+static void abl_check(int r, const char *what) {
+    if (r != ABL_OK) {
+        std::fprintf(stderr, "%s failed: %s\n", what, abl_strerror(r));
+        std::exit(1);
+    }
+}
+static void abl_simulate(int abl_timesteps) {
+    abl_ctx *ctx = nullptr;
+    abl_check(abl_create(&abl_desc, 0, &ctx), "abl_create");
+    abl_check(abl_set_globals(ctx, &abl_G, sizeof abl_G), "abl_set_globals");
+    {
+        size_t n = agents.agents_Boid.len;
+        const Boid *aos = (const Boid *) agents.agents_Boid.values;
+        float2 *c0 = (float2 *) std::malloc(sizeof(float2) * (n ? n : 1));
+        for (size_t i = 0; i < n; i++) c0[i] = aos[i].pos;
+        float2 *c1 = (float2 *) std::malloc(sizeof(float2) * (n ? n : 1));
+        for (size_t i = 0; i < n; i++) c1[i] = aos[i].velocity;
+        const void *cols[] = {c0, c1};
+        abl_check(abl_upload(ctx, 0, cols, n), "abl_upload");
+        std::free(c0);
+        std::free(c1);
+    }
+    #ifdef ABL_SERIAL_RANDOM
+    uint64_t abl_xs[2];
+    abl_host_rng_get(abl_xs);
+    abl_check(abl_set_serial_random(ctx, abl_xs), "abl_set_serial_random");
+    #endif
+    abl_check(abl_run(ctx, abl_timesteps), "abl_run");
+    #ifdef ABL_SERIAL_RANDOM
+    abl_check(abl_get_serial_random(ctx, abl_xs), "abl_get_serial_random");
+    abl_host_rng_set(abl_xs);
+    #endif
+    {
+        size_t n = 0;
+        abl_check(abl_count(ctx, 0, &n), "abl_count");
+        float2 *c0 = (float2 *) std::malloc(sizeof(float2) * (n ? n : 1));
+        float2 *c1 = (float2 *) std::malloc(sizeof(float2) * (n ? n : 1));
+        void *cols[] = {c0, c1};
+        size_t cap = n;
+        abl_check(abl_download(ctx, 0, cols, &cap), "abl_download");
+        dyn_array_clean(&agents.agents_Boid);
+        agents.agents_Boid = dyn_array_create_fixed(sizeof(Boid), n);
+        Boid *aos = (Boid *) agents.agents_Boid.values;
+        for (size_t i = 0; i < n; i++) {
+            aos[i].pos = c0[i];
+            aos[i].velocity = c1[i];
+        }
+        std::free(c0);
+        std::free(c1);
+    }
+    size_t abl_log_len = 0;
+    abl_log_text(ctx, nullptr, 0, &abl_log_len);
+    if (abl_log_len > 0) {
+        char *abl_log = (char *) std::malloc(abl_log_len + 1);
+        abl_log_text(ctx, abl_log, abl_log_len + 1, nullptr);
+        FILE *abl_f = std::fopen("log.csv", "w");
+        if (abl_f) { std::fputs(abl_log, abl_f); std::fclose(abl_f); }
+        std::free(abl_log);
+    }
+    abl_destroy(ctx);
+}
+static int abl_main() {
+    for (int i = 0, _var0 = abl_G.num_agents; i < _var0; ++i) {
+        *DYN_ARRAY_PLACE(&agents.agents_Boid, Boid) = ([&]() { Boid abl_a; abl_a.pos = random_1(abl_G, abl_R, float2_fill(abl_G.min_pos), float2_fill(abl_G.max_pos)); abl_a.velocity = random_1(abl_G, abl_R, float2_fill((-1)), float2_fill(1)); return abl_a; }());
+    }
+    abl_simulate(abl_G.num_timesteps);
+    save(&agents, agents_info, "boids.out", SAVE_JSON);
+    return 0;
+}
+
+}  // namespace abl_model_boids2d_mixed
+
+extern "C" const abl_model_desc *abl_model_desc_boids2d_mixed(void) {
+    return &abl_model_boids2d_mixed::abl_desc;
+}
+
+#ifdef ABL_STANDALONE_MAIN
+extern "C" const abl_model_desc *const abl_builtin_models[] = {
+    &abl_model_boids2d_mixed::abl_desc, nullptr};
+int main() { return abl_model_boids2d_mixed::abl_main(); }
+#endif

@@ -36,6 +36,9 @@ MODELS = {
     "circle3d_float": ("circle3d.abl", {"use_float": "true"}),
     "predator_prey_float": ("predator_prey.abl", {"use_float": "true"}),
     "boids3d": ("boids.abl", {}),
+    # near-loop sums in FP32, everything else FP64 (-C cuda.precision=mixed)
+    "boids2d_mixed": ("boids2d.abl", {"cuda.precision": "mixed"}),
+    "boids3d_mixed": ("boids.abl", {"cuda.precision": "mixed"}),
     "sugarscape": ("sugarscape.abl", {}),
     # main()'s add() loop as a kernel (-C cuda.device_init=true)
     "boids2d_devinit": ("boids2d.abl", {"cuda.device_init": "true"}),
@@ -58,6 +61,10 @@ CONFIGS = {
     "boids2d_float_4096": ("boids2d_float", {"num_agents": "4096", "agent_density": "3200.0",
                                              "num_timesteps": "100"}),
     "boids2d_float_1m": ("boids2d_float", {"num_agents": "1048576", "agent_density": "3200.0",
+                                           "num_timesteps": "100"}),
+    "boids2d_mixed_4096": ("boids2d_mixed", {"num_agents": "4096", "agent_density": "3200.0",
+                                             "num_timesteps": "100"}),
+    "boids2d_mixed_1m": ("boids2d_mixed", {"num_agents": "1048576", "agent_density": "3200.0",
                                            "num_timesteps": "100"}),
     "circle_float_4000": ("circle_float", {"num_agents": "4000", "rho": "0.1",
                                            "num_timesteps": "100"}),
@@ -83,6 +90,7 @@ CONFIGS = {
                                                           "num_timesteps": "50"}),
     # examples/boids.abl (3D) at its defaults: 5,000 agents, agent_density 1000.
     "boids3d_5000": ("boids3d", {"num_timesteps": "100"}),
+    "boids3d_mixed_5000": ("boids3d_mixed", {"num_timesteps": "100"}),
     # 1,048,576 agents at 16 per unit volume: ~9 agents per interaction cell.
     "boids3d_1m": ("boids3d", {"num_agents": "1048576", "agent_density": "16",
                                "interaction_radius": "0.8", "separation_radius": "0.08",

@@ -12,6 +12,8 @@ const abl_model_desc *abl_model_desc_circle_float(void);
 const abl_model_desc *abl_model_desc_circle3d_float(void);
 const abl_model_desc *abl_model_desc_predator_prey_float(void);
 const abl_model_desc *abl_model_desc_boids3d(void);
+const abl_model_desc *abl_model_desc_boids2d_mixed(void);
+const abl_model_desc *abl_model_desc_boids3d_mixed(void);
 const abl_model_desc *abl_model_desc_sugarscape(void);
 const abl_model_desc *abl_model_desc_boids2d_devinit(void);
 const abl_model_desc *abl_model_desc_kinds(void);
@@ -30,6 +32,8 @@ const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_circle3d_float(),
     abl_model_desc_predator_prey_float(),
     abl_model_desc_boids3d(),
+    abl_model_desc_boids2d_mixed(),
+    abl_model_desc_boids3d_mixed(),
     abl_model_desc_sugarscape(),
     abl_model_desc_boids2d_devinit(),
     abl_model_desc_kinds(),
