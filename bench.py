@@ -448,10 +448,17 @@ def measure_other_workloads(args, o, W, np):
 
 
 def pp_agent_error(o, np, cfg, st, steps=100):
-    """Per-agent error of the FP32 predator_prey run against the FP64 run
-    while the two runs have the same populations.  Births and deaths are
-    decided by comparisons, so once one comparison flips, the populations
-    differ and agents are no longer matched by index."""
+    """Per-animal error of the FP32 predator_prey run against the FP64 run.
+
+    Births and deaths are decided by comparisons, so after the first flipped
+    comparison the two populations differ and agents can no longer be
+    matched by index.  Each FP32 animal is therefore matched to the nearest
+    FP64 animal of its type (scipy cKDTree; animals are ~1/40 of the domain
+    apart, far more than the FP32 error); the error is that distance over
+    env_size.  Animals born or killed in one run only find a farther partner,
+    so the distribution's tail includes them: the median and p99 describe
+    the arithmetic, the maximum the population differences."""
+    from scipy.spatial import cKDTree
     sims = []
     for name in ("predator_prey", "predator_prey_float"):
         model = o.Model(name)
@@ -464,27 +471,29 @@ def pp_agent_error(o, np, cfg, st, steps=100):
                            for k, v in cols.items()})
         sims.append(sim)
     L = float(cfg["globals"]["env_size"])
-    last_matched, errs = 0, {}
+    errs = {}
     for t in range(1, steps + 1):
         for sim in sims:
             sim.step()
-        a = {ty: sims[0].download(ty) for ty in ("Predator", "Prey")}
-        b = {ty: sims[1].download(ty) for ty in ("Predator", "Prey")}
-        if any(len(a[ty]["pos"]) != len(b[ty]["pos"]) for ty in a):
-            break
-        d = np.concatenate([np.abs(b[ty]["pos"].astype(np.float64) - a[ty]["pos"]).max(axis=1)
-                            for ty in a]) / L
-        last_matched = t
-        if t in (1, 10, 100) or t == steps:
-            errs[f"step_{t}"] = {"pos_rel_err_max": float(d.max()),
-                                 "pos_rel_err_median": float(np.median(d)),
-                                 "pos_rel_err_p99": float(np.quantile(d, 0.99)),
-                                 "frac_le_1e-5": float((d <= 1e-5).mean())}
+        if t not in (1, 10, 100) and t != steps:
+            continue
+        d, counts = [], {}
+        for ty in ("Predator", "Prey"):
+            a = sims[0].download(ty)["pos"]
+            b = sims[1].download(ty)["pos"].astype(np.float64)
+            counts[ty] = [len(a), len(b)]
+            if len(a) and len(b):
+                d.append(cKDTree(a).query(b, k=1)[0] / L)
+        d = np.concatenate(d) if d else np.zeros(1)
+        errs[f"step_{t}"] = {"pos_rel_err_median": float(np.median(d)),
+                             "pos_rel_err_p99": float(np.quantile(d, 0.99)),
+                             "pos_rel_err_max": float(d.max()),
+                             "frac_le_1e-5": float((d <= 1e-5).mean()),
+                             "animals_fp64_fp32": counts}
     for sim in sims:
         sim.close()
-    return {"agent_error_metric": "per animal max |pos32 - pos64| / env_size while the "
-                                  "populations agree",
-            "populations_agree_through_step": last_matched, "agent_error": errs}
+    return {"agent_error_metric": "per FP32 animal: distance to the nearest FP64 animal of "
+                                  "its type / env_size", "agent_error": errs}
 
 
 def headline_config(n, world):

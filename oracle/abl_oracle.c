@@ -839,3 +839,35 @@ static const int pp_step_type[S_COUNT] = {PP_PRED, PP_PREY, PP_PREY, PP_PRED, PP
 #include "abl_oracle_pp.h"
 #undef PP_REAL
 #undef PP_FN
+
+/* ------------------------------------------------- device-side main() init */
+/* examples/boids2d.abl:110-118 as `-b cuda -C cuda.device_init=true` runs it:
+ * the loop `for (int i : 0..num_agents) add(Boid{pos: random(float2(min_pos),
+ * float2(max_pos)), velocity: random(float2(-1), float2(1))})` becomes one
+ * thread per iteration, drawing from the counter-based stream instead of the
+ * reference's sequential xorshift stream.  The stated semantics:
+ *  - iteration t of add() loop number L draws from Philox4x32-10 with key
+ *    (0x5eed, 0) and counter (t, 0xffffff00 + L, 0, draw number);
+ *  - random(float2 lo, float2 hi) draws y before x (the evaluation order the
+ *    generator fixes for calls whose arguments draw, last argument first);
+ *  - random(lo, hi) = lo + u * (hi - lo) with u the draw's 53-bit uniform. */
+ORACLE_API void oracle_devinit_boids2d(long n, double min_pos, double max_pos, double *pos,
+                                       double *vel) {
+  for (long t = 0; t < n; t++) {
+    pp_rng R;
+    R.k0 = 0x5eedu;
+    R.k1 = 0;
+    R.c0 = (uint32_t) t;
+    R.c1 = 0xffffff00u;
+    R.c2 = 0;
+    R.draw = 0;
+    double py = min_pos + pp_unit(&R) * (max_pos - min_pos);
+    double px = min_pos + pp_unit(&R) * (max_pos - min_pos);
+    double vy = -1.0 + pp_unit(&R) * (1.0 - -1.0);
+    double vx = -1.0 + pp_unit(&R) * (1.0 - -1.0);
+    pos[2 * t] = px;
+    pos[2 * t + 1] = py;
+    vel[2 * t] = vx;
+    vel[2 * t + 1] = vy;
+  }
+}

@@ -65,11 +65,13 @@ PROGRAMS = {
     # random() inside the step: run on one OpenMP thread, so its draws come
     # from the xorshift stream in agent order (SERIAL_RANDOM)
     "boids2d_flockers": ("boids2d_flockers", {}),
+    # random() and randomInt() inside ant_act (serial, as boids2d_flockers)
+    "ants": ("ants", {}),
 }
 
 # Programs whose reference run uses one thread and whose cuda build continues
 # the host stream in steps (-DABL_SERIAL_RANDOM).
-SERIAL_RANDOM = {"boids2d_flockers", "boids2d_flockers_1000"}
+SERIAL_RANDOM = {"boids2d_flockers", "boids2d_flockers_1000", "ants"}
 
 
 def model_path(example):

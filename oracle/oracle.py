@@ -41,6 +41,7 @@ def lib():
         L.oracle_circle_step.argtypes = [_i, _l, _p, _p, _d, _d, _d, _d, _p, _p, _i, _i, _l, _l]
         L.oracle_boids2d_step.argtypes = [_l, _p, _p, _p, _p, _p, _i, _i, _l, _l]
         L.oracle_init_boids3d.argtypes = [_l, _d, _d, _p, _p]
+        L.oracle_devinit_boids2d.argtypes = [_l, _d, _d, _p, _p]
         L.oracle_sugarscape_step.argtypes = [_i, _l, _p, _p, _d, _d, _i, _i]
         L.oracle_flockers_step.argtypes = [_l, _p, _p, _p, _p, _p, _i]
         L.oracle_boids2d_step_f32.argtypes = [_l, _p, _p, _p, _p, _p, _i, _i]
@@ -116,6 +117,15 @@ def boids2d_step(state, c, mode=1, nthreads=0, first=0, count=None):
     lib().oracle_boids2d_step(n, _ptr(pos), _ptr(vel), _ptr(po), _ptr(vo), _ptr(p), mode,
                               nthreads, first, count)
     return {"pos": po, "velocity": vo}
+
+
+def devinit_boids2d(n, min_pos, max_pos):
+    """boids2d's main() loop as the device initialisation kernel draws it
+    (-C cuda.device_init=true; counter-based stream, see abl_oracle.c)."""
+    pos = np.zeros((n, 2), np.float64)
+    vel = np.zeros((n, 2), np.float64)
+    lib().oracle_devinit_boids2d(n, min_pos, max_pos, _ptr(pos), _ptr(vel))
+    return {"pos": pos, "velocity": vel}
 
 
 def init_boids3d(n, min_pos, max_pos):

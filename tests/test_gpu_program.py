@@ -63,13 +63,17 @@ def test_generated_program_writes_the_reference_output(model, runtime_objects, t
 
 
 @pytest.mark.gpu
-def test_device_initialised_program_runs_deterministically(runtime_objects, tmp_path):
+def test_device_initialised_program_matches_the_oracle(runtime_objects, tmp_path):
     """`-C cuda.device_init=true`: boids2d's main() loop `for (int i :
     0..num_agents) add(Boid{...})` runs as a kernel drawing from the
     counter-based stream (so results differ from the reference's host init
-    by design).  The program writes the example's 5000 boids, every position
-    inside the domain after 100 timesteps and finite, and two runs write the
-    same file."""
+    by design).  The oracle restates those draws (oracle_devinit_boids2d) and
+    the 100 timesteps that follow; the file the program writes must equal,
+    byte for byte, the oracle's state written in save()'s JSON layout
+    (asset/c/libabl.c:46-124).  Two runs of the program write the same file."""
+    import numpy as np
+    import openabl_gb300 as o
+    from oracle import oracle as O
     obj = str(tmp_path / "devinit.o")
     exe = str(tmp_path / "main")
     subprocess.check_call(NVCC + ["-c", os.path.join(GEN, "boids2d_devinit.cu"), "-o", obj])
@@ -81,12 +85,16 @@ def test_device_initialised_program_runs_deterministically(runtime_objects, tmp_
         subprocess.run([exe], cwd=run_dir, check=True, stdout=subprocess.DEVNULL, timeout=300)
         outs.append((run_dir / "boids.out").read_bytes())
     assert outs[0] == outs[1]
-    boids = json.loads(outs[0])["Boid"]
-    assert len(boids) == 5000
-    max_pos = 3.16228  # sqrt(num_agents / agent_density) at the example's defaults
-    for b in boids:
-        assert all(0.0 <= c <= max_pos for c in b["pos"])
-        assert all(abs(v) <= 1.0 + 1e-6 for v in b["velocity"])
+    g = o.Model("boids2d").default_globals()
+    n = g.get("num_agents")
+    state = O.devinit_boids2d(n, g.get("min_pos"), g.get("max_pos"))
+    c = {k: g.get(k) for k in O.BOIDS2D_KEYS}
+    for _ in range(g.get("num_timesteps")):
+        state = O.boids2d_step(state, c, mode=1)
+    want = '{"Boid":[' + ",\n".join(
+        '{"pos":[%f,%f],"velocity":[%f,%f]}' % (p[0], p[1], v[0], v[1])
+        for p, v in zip(state["pos"], state["velocity"])) + "]}"
+    assert outs[0].decode() == want
 
 
 # Models that call random() inside step functions.  The reference draws those
@@ -97,6 +105,8 @@ def test_device_initialised_program_runs_deterministically(runtime_objects, tmp_
 # must match (keratinocyte's log.csv without its timing column), and they
 # must hold the populations the models keep.
 UNPINNED = {"ants": "ants.out", "boids2d_flockers": "boids.out", "keratinocyte": "log.csv"}
+# (ants and boids2d_flockers are also pinned in their sequential mode, above,
+# against the reference programs run on one thread)
 
 
 def run_program(exe, run_dir):
