@@ -81,7 +81,11 @@ Collector collect(N &node) {
 // neighbours are visited.  Order-free bodies only accumulate integers into
 // variables declared outside the loop with +=, -=, |=, &=, ^= and never read
 // those variables otherwise; everything else is treated as order-dependent.
-bool nearBodyIsOrdered(const AST::ForStatement &loop) {
+// `orderFree` lists further accumulations whose order does not matter (the
+// mixed form's FP32 sums, which are not bit-exact to the reference in any
+// order).
+bool nearBodyIsOrdered(const AST::ForStatement &loop,
+                       const std::set<const AST::AssignOpStatement *> *orderFree = nullptr) {
   Collector c = collect(*loop.stmt);
   if (c.breaks || c.returns) return true;
   std::set<VarId> inner;
@@ -101,6 +105,10 @@ bool nearBodyIsOrdered(const AST::ForStatement &loop) {
     const AST::VarExpression *root = targetRoot(*a->left);
     if (!root) return true;
     if (inner.count(root->var->id)) continue;
+    if (orderFree && orderFree->count(a)) {
+      accTargets[root->var->id]++;
+      continue;
+    }
     auto *plain = dynamic_cast<const AST::VarExpression *>(&*a->left);
     if (!plain) return true;
     Type t = a->left->type;
@@ -619,6 +627,20 @@ std::vector<CudaPrinter::MixedAcc> CudaPrinter::findMixedAccs(
   return out;
 }
 
+// A member of the near loop's neighbour that is not loaded ahead (mixed
+// form, read only by lazy distances) is read from its column at the current
+// slot.
+void CudaPrinter::print(const AST::MemberAccessExpression &expr) {
+  auto *v = dynamic_cast<const AST::VarExpression *>(&*expr.expr);
+  auto it = columnOnly.find(expr.member);
+  if (v && it != columnOnly.end() && v->var->id == nearVar) {
+    *this << "((const " << cType(expr.type) << " *) abl_NB.cols[" << it->second << "])["
+          << nearSlot << "]";
+    return;
+  }
+  CPrinter::print(expr);
+}
+
 void CudaPrinter::print(const AST::AssignOpStatement &stmt) {
   auto it = mixedAccs.find(&stmt);
   if (it == mixedAccs.end()) {
@@ -722,15 +744,37 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   std::string pslot = "abl_pslot" + sid, pnx = "abl_pnx" + sid;
   // Members the FP32 sums read from float copies need no FP64 load unless
   // the body reads them elsewhere too.
+  // The same for members read only inside lazy distances, whose reference
+  // expression runs for the few candidates the FP32 band leaves undecided:
+  // those members are read from their column where used (`columnOnly`).
   std::map<std::string, int> fp64Reads;
-  {
+  std::vector<DeferredIf> deferred;
+  if (fnKind == FnKind::STEP) deferred = findDeferredIfs(script, stepDecl, stmt);
+  auto savedColumnOnly = columnOnly;
+  const VarId savedNearVar = nearVar;
+  columnOnly.clear();
+  if (!maccs.empty()) {
+    std::vector<const AST::Statement *> bodies;
+    for (const DeferredIf &d : deferred) bodies.push_back(&*d.ifs->ifStmt);
+    std::set<const AST::MemberAccessExpression *> inLazy;
+    for (const AST::VarDeclarationStatement *d : findLazyDistances(script, stmt, bodies))
+      for (auto *ma : collect(*const_cast<AST::Expression *>(&*d->initializer)).members)
+        inLazy.insert(ma);
+    std::map<std::string, int> lazyReads;
     Collector bc = collect(*stmt.stmt);
     for (auto *ma : bc.members) {
       auto *v = dynamic_cast<const AST::VarExpression *>(&*ma->expr);
-      if (v && v->var->id == stmt.var->id) fp64Reads[ma->member]++;
+      if (!v || v->var->id != stmt.var->id) continue;
+      if (inLazy.count(ma)) lazyReads[ma->member]++;
+      else fp64Reads[ma->member]++;
     }
     for (const MixedAcc &m : maccs)
       fp64Reads[(*agentDecl->members)[m.member]->name]--;
+    for (size_t k = 0; k < agentDecl->members->size(); k++) {
+      const std::string &nm = (*agentDecl->members)[k]->name;
+      if (fp64Reads[nm] <= 0 && lazyReads[nm] > 0) columnOnly[nm] = (int) k;
+    }
+    nearVar = stmt.var->id;
   }
   auto loadMembers = [&](const std::string &var, const std::string &at) {
     for (size_t k = 0; k < agentDecl->members->size(); k++) {
@@ -745,8 +789,6 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   *this << nl << "int " << pslot << " = " << c << ".slot(0);" << nl << agentDecl->name << " "
         << pnx << ";";
   loadMembers(pnx, pslot);
-  std::vector<DeferredIf> deferred;
-  if (fnKind == FnKind::STEP) deferred = findDeferredIfs(script, stepDecl, stmt);
   std::map<const AST::IfStatement *, std::string> savedMasks = deferredMasks;
   deferredMasks.clear();
   for (size_t j = 0; j < deferred.size(); j++) {
@@ -810,6 +852,8 @@ void CudaPrinter::print(const AST::ForStatement &stmt) {
   }
   mixedAccs = savedMixed;
   mixedAnchor = savedAnchor;
+  columnOnly = savedColumnOnly;
+  nearVar = savedNearVar;
   *this << outdent << nl << "}";
   if (nearNeedsEnd) *this << nl << nearEndLabel << ": ;";
   nearEndLabel = savedLabel;
@@ -915,7 +959,12 @@ void CudaPrinter::printStepFunction(const AST::FunctionDeclaration &decl) {
     info.nearLoop = loop;
     const AST::AgentDeclaration *nearAgent = loop->type->resolved.getAgentDecl();
     info.nearType = agentIndex(nearAgent);
-    info.ordered = nearBodyIsOrdered(*loop);
+    // Mixed precision: the FP32 sums do not depend on the visiting order
+    // (they are not the reference's bits in any order), so a body whose only
+    // order-dependent statements they were runs without sorting neighbours.
+    std::set<const AST::AssignOpStatement *> fp32Sums;
+    for (const MixedAcc &m : findMixedAccs(*loop, *nearAgent)) fp32Sums.insert(m.stmt);
+    info.ordered = nearBodyIsOrdered(*loop, &fp32Sums);
     for (size_t k = 0; k < nearAgent->members->size(); k++) {
       const AST::AgentMember &m = *(*nearAgent->members)[k];
       if (decl.accessedMembers.count(m.name) || m.isPosition) info.nearMembers |= 1u << k;

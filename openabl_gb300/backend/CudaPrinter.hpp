@@ -43,6 +43,7 @@ struct CudaPrinter : public CPrinter {
   void print(const AST::SimulateStatement &) override;
   void print(const AST::VarDeclarationStatement &) override;
   void print(const AST::AssignOpStatement &) override;
+  void print(const AST::MemberAccessExpression &) override;
   void print(const AST::FunctionDeclaration &) override;
   void print(const AST::Script &) override;
 
@@ -100,6 +101,10 @@ private:
   };
   std::map<const AST::AssignOpStatement *, MixedAcc> mixedAccs;
   std::string mixedAnchor;
+  // Neighbour members read from their column where used instead of loaded
+  // ahead (member -> column), for the loop variable `nearVar`.
+  std::map<std::string, int> columnOnly;
+  VarId nearVar;
   std::vector<MixedAcc> findMixedAccs(const AST::ForStatement &loop,
                                       const AST::AgentDeclaration &nearAgent);
 

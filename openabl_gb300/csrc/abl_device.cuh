@@ -1210,21 +1210,36 @@ struct facc {
     for (int d = 0; d < DIM; d++) v[d] = 0.0f;
   }
   // += (position of slot s) - anchor
+  // DIM floats of a slot-ordered array (one 8-byte load for two)
+  __device__ __forceinline__ static void load(const float *a, int s, float *out) {
+    if (DIM == 2) {
+      const ::float2 t = __ldg(reinterpret_cast<const ::float2 *>(a) + s);
+      out[0] = t.x;
+      out[DIM - 1] = t.y;
+    } else {
+#pragma unroll
+      for (int d = 0; d < DIM; d++) out[d] = __ldg(&a[DIM * s + d]);
+    }
+  }
   __device__ __forceinline__ void add_offset(const abl_near_view &V, int s,
                                              const mixed_anchor<DIM> &a) {
+    float ph[DIM], pl[DIM];
+    load(V.posf, s, ph);
+    load(V.poslo, s, pl);
 #pragma unroll
     for (int d = 0; d < DIM; d++) {
-      const float hi = __fsub_rn(__ldg(&V.posf[DIM * s + d]), a.hi[d]);
-      const float lo = __fsub_rn(__ldg(&V.poslo[DIM * s + d]), a.lo[d]);
+      const float hi = __fsub_rn(ph[d], a.hi[d]);
+      const float lo = __fsub_rn(pl[d], a.lo[d]);
       v[d] = __fadd_rn(v[d], __fadd_rn(hi, lo));
     }
     n++;
   }
   // += float copy of member column `k` at slot s (DIM components)
   __device__ __forceinline__ void add_member(const abl_near_view &V, int k, int s) {
-    const float *c = (const float *) V.fcols[k];
+    float m[DIM];
+    load((const float *) V.fcols[k], s, m);
 #pragma unroll
-    for (int d = 0; d < DIM; d++) v[d] = __fadd_rn(v[d], __ldg(&c[DIM * s + d]));
+    for (int d = 0; d < DIM; d++) v[d] = __fadd_rn(v[d], m[d]);
     n++;
   }
   // The accumulated value in FP64: n * anchor + offsets, or the plain sum.

@@ -124,7 +124,7 @@ __device__ static void update_boid(const abl_globals &abl_G, const abl_near_view
     int collision_count = 0;
     {
         const abl::near_query<2> abl_q1(abl_NB, (double) in->pos.x, (double) in->pos.y, 0.0, abl_K.self);
-        abl::near_list_cursor<2> abl_c1(abl_NB, abl_q1, abl_K);
+        abl::near_cursor<2> abl_c1(abl_NB, abl_q1);
         const abl::mixed_anchor<2> abl_ma1((double) in->pos.x, (double) in->pos.y, 0.0);
         abl::facc<2> abl_fa1_0;
         abl::facc<2> abl_fa1_1;
@@ -136,28 +136,25 @@ __device__ static void update_boid(const abl_globals &abl_G, const abl_near_view
         while (abl_c1.fill(abl_q1, abl_exact1)) {
             int abl_pslot1 = abl_c1.slot(0);
             Boid abl_pnx1;
-            abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
             unsigned long long abl_dm1_0 = 0ull;
             for (int abl_k = 0; abl_k < abl_c1.cnt; ++abl_k) {
                 const int abl_slot1 = abl_pslot1;
                 Boid abl_nx1 = abl_pnx1;
                 if (abl_k + 1 < abl_c1.cnt) {
                     abl_pslot1 = abl_c1.slot(abl_k + 1);
-                    abl_pnx1.pos = ((const float2 *) abl_NB.cols[0])[abl_pslot1];
                 }
                 Boid* nx = &abl_nx1;
                 {
                     abl_fa1_0.add_offset(abl_NB, abl_slot1, abl_ma1);
                     abl_fa1_1.add_member(abl_NB, 1, abl_slot1);
                     interaction_count += 1;
-                    const auto separation = abl::make_lazy_dist(abl_q1, abl_NB, abl_slot1, [&]() -> abl_float { return dist_float2(in->pos, nx->pos); });
+                    const auto separation = abl::make_lazy_dist(abl_q1, abl_NB, abl_slot1, [&]() -> abl_float { return dist_float2(in->pos, ((const float2 *) abl_NB.cols[0])[abl_slot1]); });
                     if ((separation < abl_G.separation_radius)) abl_dm1_0 |= 1ull << abl_k;
                 }
             }
             for (unsigned long long abl_m = abl_dm1_0; abl_m; abl_m &= abl_m - 1ull) {
                 const int abl_slot1 = abl_c1.slot(__ffsll((long long) abl_m) - 1);
                 Boid abl_nx1;
-                abl_nx1.pos = ((const float2 *) abl_NB.cols[0])[abl_slot1];
                 Boid* nx = &abl_nx1;
                 {
                     abl_fa1_2.add_offset(abl_NB, abl_slot1, abl_ma1);
@@ -215,21 +212,7 @@ struct abl_kargs_update_boid {
     unsigned long long *serial_rng;
 };
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_update_boid(const __grid_constant__ abl_kargs_update_boid A) {
-    int abl_j;
-    {
-        const abl_globals &abl_G = A.G;
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
-        const bool abl_has = abl_t1 < A.n;
-        const long abl_i1 = abl_has ? (A.visit ? (long) A.visit[abl_t1] : abl_t1) : 0;
-        const float2 abl_p1 = abl_has ? A.in.pos[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(A.NB, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
-        auto abl_x0 = [&](int abl_s) -> bool {
-            const float2 abl_p = ((const float2 *) A.NB.cols[0])[abl_s];
-            return !(dist_float2(abl_p, abl_p1) > abl_G.interaction_radius);
-        };
-        abl_j = abl::presort_block<2>(A.NB, abl_has, abl_q0, abl_x0);
-    }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit ? (long) A.visit[abl_t] : abl_t;
     abl::step_ctx abl_K;
@@ -239,7 +222,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = A.child_cols;
-    abl_K.near_col = abl_j;
+    abl_K.near_col = -1;
     Boid abl_in, abl_out;
     abl_in.pos = A.in.pos[abl_i];
     abl_in.velocity = A.in.velocity[abl_i];
@@ -271,23 +254,7 @@ static int abl_launch_update_boid(const abl_step_launch *L, cudaStream_t abl_str
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
 __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_update_boid(const __grid_constant__ abl_ens_launch A) {
-    int abl_j;
-    {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
-        const bool abl_has = abl_t1 < A.n;
-        const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
-        const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
-        const abl_globals &abl_G = ((const abl_globals *) A.globals)[abl_r1];
-        const abl_near_view &abl_V1 = A.views[abl_r1];
-        const float2 abl_p1 = abl_has ? ((const float2 *) A.in_cols[0])[abl_i1] : float2{};
-        const abl::near_query<2> abl_q0(abl_V1, (double) abl_p1.x, (double) abl_p1.y, 0.0, abl_has ? abl_i1 : -1);
-        auto abl_x0 = [&](int abl_s) -> bool {
-            const float2 abl_p = ((const float2 *) abl_V1.cols[0])[abl_s];
-            return !(dist_float2(abl_p, abl_p1) > abl_G.interaction_radius);
-        };
-        abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
-    }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
@@ -298,7 +265,7 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     abl_K.removed = 0;
     abl_K.added = 0;
     abl_K.child_cols = nullptr;
-    abl_K.near_col = abl_j;
+    abl_K.near_col = -1;
     Boid abl_in, abl_out;
     abl_in.pos = ((const float2 *) A.in_cols[0])[abl_i];
     abl_in.velocity = ((const float2 *) A.in_cols[1])[abl_i];
@@ -353,7 +320,7 @@ static void abl_env_bounds(const void *abl_gp, double *abl_min, double *abl_max)
     abl_max[0] = abl_hi.x; abl_max[1] = abl_hi.y; abl_max[2] = 0;
 }
 static const abl_step_desc abl_steps[] = {
-    {"update_boid", 0, 0, 1, abl_radius_update_boid, 1u, 3u, abl_launch_update_boid, 0, -1, 0, nullptr, 0, 1, 3u, 1, 2u, 1},
+    {"update_boid", 0, 0, 0, abl_radius_update_boid, 1u, 3u, abl_launch_update_boid, 0, -1, 0, nullptr, 0, 0, 3u, 1, 2u, 1},
 };
 static const abl_step_desc abl_steps_ordered[] = {
     abl_steps[0],
