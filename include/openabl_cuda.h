@@ -157,17 +157,13 @@ int abl_set_balance(abl_ctx *ctx, int enable);
  * LISTS reads whole precomputed neighbourhood lists, BLOCK (2D, loops around
  * the step's own agents) has each thread block merge the row lists once per
  * cell in shared memory (falling back to ROWS for a block whose lists do not
- * fit), STEPLISTS (2D, loops around the step's own agents) builds every
- * agent's ordered in-radius list in a kernel of its own before the step
- * (agents with more neighbours than the lists hold fall back to ROWS).
- * Results are identical in every mode; this is a tuning and testing
+ * fit).  Results are identical in every mode; this is a tuning and testing
  * control. */
 #define ABL_NEAR_AUTO 0
 #define ABL_NEAR_RUNS 1
 #define ABL_NEAR_ROWS 2
 #define ABL_NEAR_LISTS 3
 #define ABL_NEAR_BLOCK 4
-#define ABL_NEAR_STEPLISTS 5
 int abl_set_near_mode(abl_ctx *ctx, int mode);
 /* A near loop around the step's own agent, over a type whose positions no
  * step function changes (nor adds or removes agents of), keeps each agent's

@@ -961,28 +961,6 @@ __device__ int presort_block(const abl_near_view &V, bool has, const near_query<
       S.total[t] = key;
       S.resume[t] = from + n;
     }
-  } else if (V.slist) {
-    // Step lists (built before the step, one per slot; threads visit agents
-    // in slot order).  An agent with more neighbours than a list holds
-    // gathers them from the row lists itself.
-    if (has) {
-      const long s = (long) blockIdx.x * blockDim.x + t;
-      const int c = __ldg(&V.slist_cnt[s]);
-      if (c <= V.slist_cap) {
-        const int n = c < S.cap ? c : S.cap;
-        for (int j = 0; j < n; j++)
-          S.slots[j * ABL_STEP_BLOCK + t] = __ldg(&V.slist[(long) j * V.slist_stride + s]);
-        key = c;
-        S.resume[t] = n;
-        S.bstart[t] = -2;
-      } else {
-        int stored = 0, last = -1;
-        key = gather_rows(S, V, q, exact, t, -1, stored, last);
-        S.resume[t] = last;
-        S.bstart[t] = -1;
-      }
-      S.total[t] = key;
-    }
   } else if (S.block_cap > 0 && gather_block(S, V, has, q, exact, key)) {
     // gathered from the block lists
   } else if (has) {
@@ -1051,16 +1029,6 @@ struct near_list_cursor {
         S.resume[col] = from + n;
         stored = n;
         tot = end - from;
-      } else if (V.slist && S.bstart[col] == -2) {
-        // Step list: entries from `from` on (the list holds all of them).
-        const long s = (long) blockIdx.x * blockDim.x + col;
-        const int from = first ? 0 : S.resume[col];
-        tot = __ldg(&V.slist_cnt[s]) - from;
-        const int n = tot < S.cap ? tot : S.cap;
-        for (int j = 0; j < n; j++)
-          S.slots[j * ABL_STEP_BLOCK + col] = __ldg(&V.slist[(long) (from + j) * V.slist_stride + s]);
-        S.resume[col] = from + n;
-        stored = n;
       } else if (S.block_cap > 0 && S.bstart[col] >= 0) {
         const int from = first ? S.bstart[col] : S.resume[col];
         int next = 0;

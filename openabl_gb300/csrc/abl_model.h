@@ -81,14 +81,6 @@ typedef struct {
      FP32, and the low part of the position, (float) (pos - (double) posf) */
   const void *fcols[ABL_MAX_MEMBERS];
   const float *poslo;
-  /* step lists (ABL_NEAR_STEPLISTS): per slot of the step's agents (threads
-     visit agents in slot order) the number of in-radius neighbours, and the
-     first slist_cap of their slots in ascending id, column-major:
-     entry k of slot s at slist[k * slist_stride + s]; NULL: none */
-  const int *slist;
-  const int *slist_cnt;
-  long slist_stride;
-  int slist_cap;
 } abl_near_view;
 
 /* Everything a generated step launcher needs. */

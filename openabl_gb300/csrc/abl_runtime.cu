@@ -832,7 +832,6 @@ int list_depth(const abl_step_desc &sd, const abl_agent_desc &d, int mode) {
     case ABL_NEAR_RUNS: return 0;
     case ABL_NEAR_ROWS: return d.dim == 2 ? 1 : 0;
     case ABL_NEAR_BLOCK: return d.dim == 2 ? 1 : 0;
-    case ABL_NEAR_STEPLISTS: return d.dim == 2 ? 1 : 0;
     case ABL_NEAR_LISTS: return 2;
     default: break;
   }
@@ -845,12 +844,6 @@ int list_depth(const abl_step_desc &sd, const abl_agent_desc &d, int mode) {
 bool block_lists_wanted(const abl_step_desc &sd, int depth, int mode) {
   return depth == 1 && sd.agent_type == sd.near_type
       && (mode == ABL_NEAR_AUTO || mode == ABL_NEAR_BLOCK);
-}
-
-// Step lists (k_step_lists) serve the same loops when asked for.
-bool step_lists_wanted(const abl_step_desc &sd, int depth, int mode) {
-  return depth == 1 && sd.agent_type == sd.near_type && sd.presorted
-      && mode == ABL_NEAR_STEPLISTS;
 }
 
 size_t member_bytes(const abl_member_desc &m) {
@@ -886,12 +879,6 @@ struct StepState {
   ScanPlan nc_scan;
   long nc_n = 0, nc_wide_cap = 0, nc_short_cap = 0;
   std::vector<void *> nc_allocs;
-  // Step lists (ABL_NEAR_STEPLISTS): per slot the neighbour count and up to
-  // sl_cap neighbour slots, column-major (stride sl_stride), rebuilt every
-  // timestep; sized with the step's buffers in prepare().
-  int *sl_cnt = nullptr, *sl_list = nullptr;
-  long sl_stride = 0;
-  int sl_cap = 0;
 };
 
 struct abl_ctx {
@@ -948,8 +935,6 @@ struct abl_ctx {
   int near_mode = ABL_NEAR_AUTO;
   // Entries of a thread block's shared-memory neighbourhood lists (ABL_NEAR_BLOCK).
   int block_cap = 2048;
-  // Neighbour slots a step list holds per agent (ABL_NEAR_STEPLISTS).
-  int step_list_cap = 48;
   bool near_cache = true;
   long bin_serial = 0;
   // Step kernels skip stores of members that never change (both buffers
@@ -1232,18 +1217,6 @@ int prepare(abl_ctx *ctx) {
   ctx->step_allocs.clear();
   for (StepState &st : ctx->step_state) nc_free_all(ctx, st);
   ctx->step_state.assign(m->num_steps, StepState());
-  for (int k = 0; k < m->num_steps; k++) {
-    const abl_step_desc &sd = m->steps[k];
-    if (sd.near_type < 0) continue;
-    const int depth = list_depth(sd, *ctx->types[sd.near_type].d, ctx->near_mode);
-    if (!step_lists_wanted(sd, depth, ctx->near_mode)) continue;
-    StepState &st = ctx->step_state[k];
-    const TypeState &pt = ctx->types[sd.agent_type];
-    st.sl_stride = std::max<long>(std::max(pt.cap, pt.n), 1);
-    st.sl_cap = ctx->step_list_cap;
-    ABL_TRY(dev_alloc_t(ctx, &st.sl_cnt, st.sl_stride, &ctx->step_allocs));
-    ABL_TRY(dev_alloc_t(ctx, &st.sl_list, st.sl_stride * st.sl_cap, &ctx->step_allocs));
-  }
   for (int k = 0; k < m->num_steps; k++) {
     const abl_step_desc &sd = m->steps[k];
     if (!sd.uses_remove && sd.add_type < 0) continue;
@@ -1857,109 +1830,6 @@ void launch_nc_lists(abl_ctx *ctx, const TypeState &g, double radius, int *count
   ctx->launches++;
 }
 
-// ------------------------------------------------------------- step lists
-//
-// ABL_NEAR_STEPLISTS: before a 2D ordered near step around its own agents,
-// one thread per slot builds the agent's in-radius neighbour list in
-// ascending id, so the step kernel reads it instead of gathering.  The
-// candidates are the row lists of the cells above, at and below the agent's
-// cell (each in ascending id; entries (id, slot, float x, float y)); each is
-// tested once -- the FP32 distance of the float copies outside the radius's
-// error band decides, inside it the reference test does, as in the step
-// kernels -- into one bit mask per row, and the masks are merged by id.
-// cnt[s] = the number of neighbours; the first `cap` slots go to
-// list[k * stride + s].  Rows longer than 64 entries give cnt = INT_MAX: the
-// step kernel then gathers that agent's neighbours itself.
-template <typename Real>
-__global__ void k_step_lists(long n, const int *order, const int *cell_of, const Real *pos,
-                             const float *posf, const int *row_off, const int4 *rows, int nx,
-                             int ny, const float *amax, double radius, int cap, long stride,
-                             int *cnt, int *list) {
-  const long s = (long) blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const int i = order[s];
-  const int cell = cell_of[i];
-  const int cy = cell / nx, cx = cell - cy * nx;
-  const abl::band bd = abl::make_band(radius, *amax, 2);
-  const float p0 = posf[2 * s], p1 = posf[2 * s + 1];
-  int b[3], m[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const int y = cy + k - 1;
-    b[k] = m[k] = 0;
-    if (y >= 0 && y < ny) {
-      b[k] = row_off[y * nx + cx];
-      m[k] = row_off[y * nx + cx + 1] - b[k];
-    }
-  }
-  if (m[0] > 64 || m[1] > 64 || m[2] > 64) {
-    cnt[s] = 0x7fffffff;
-    return;
-  }
-  unsigned long long mask[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    unsigned long long mk = 0ull;
-    for (int j = 0; j < m[k]; j += 4) {
-      int4 e[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++) e[u] = j + u < m[k] ? rows[b[k] + j + u] : make_int4(-1, 0, 0, 0);
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        if (e[u].x < 0) continue;
-        const float dx = __int_as_float(e[u].z) - p0, dy = __int_as_float(e[u].w) - p1;
-        const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-        if (d2 > bd.hi) continue;
-        if (!(d2 < bd.lo) && !nc_within<Real, 2>(pos, i, e[u].x, radius)) continue;
-        mk |= 1ull << (j + u);
-      }
-    }
-    mask[k] = mk;
-  }
-  const int total = __popcll(mask[0]) + __popcll(mask[1]) + __popcll(mask[2]);
-  cnt[s] = total;
-  const int *ent = reinterpret_cast<const int *>(rows);
-  const int kNone = 0x7fffffff;
-  int h[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) h[k] = mask[k] ? ent[4 * (b[k] + __ffsll(mask[k]) - 1)] : kNone;
-  const int want = total < cap ? total : cap;
-  for (int c = 0; c < want; c++) {
-    const bool a01 = h[0] < h[1];
-    const int m01 = a01 ? h[0] : h[1];
-    const int k = h[2] < m01 ? 2 : (a01 ? 0 : 1);
-    unsigned long long mk = k == 0 ? mask[0] : (k == 1 ? mask[1] : mask[2]);
-    const int bk = k == 0 ? b[0] : (k == 1 ? b[1] : b[2]);
-    list[(long) c * stride + s] = ent[4 * (bk + __ffsll(mk) - 1) + 1];
-    mk &= mk - 1ull;
-    const int nh = mk ? ent[4 * (bk + __ffsll(mk) - 1)] : kNone;
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      if (j == k) {
-        mask[j] = mk;
-        h[j] = nh;
-      }
-    }
-  }
-}
-
-void launch_step_lists(abl_ctx *ctx, const TypeState &g, StepState &st, double radius) {
-  const int B = 128;
-  const long nb = blocks_for(g.n, B);
-  const int *rowoff = g.sep.off[0];
-  const int4 *rows = g.sep.elem[0];
-  if (pos_is_double(g)) {
-    k_step_lists<double><<<nb, B, 0, ctx->stream>>>(
-        g.n, g.order, g.cell_of, (const double *) g.cols[g.cur][g.d->position_member], g.posf,
-        rowoff, rows, g.nx, g.ny, g.amax, radius, st.sl_cap, st.sl_stride, st.sl_cnt, st.sl_list);
-  } else {
-    k_step_lists<float><<<nb, B, 0, ctx->stream>>>(
-        g.n, g.order, g.cell_of, (const float *) g.cols[g.cur][g.d->position_member], g.posf,
-        rowoff, rows, g.nx, g.ny, g.amax, radius, st.sl_cap, st.sl_stride, st.sl_cnt, st.sl_list);
-  }
-  ctx->launches++;
-}
-
 // Whether step k keeps its neighbour lists.
 bool near_cache_wanted(const abl_ctx *ctx, const abl_step_desc &sd) {
   // Kept lists index neighbours by agent; the float copies of the mixed
@@ -2166,18 +2036,6 @@ int step_once(abl_ctx *ctx) {
       // Threads visit the binned agents in slot order, so a block's agents
       // fill consecutive cells: block lists pay off.
       V.block_cap = block_lists_wanted(sd, depth, ctx->near_mode) ? ctx->block_cap : 0;
-      V.slist = nullptr;
-      V.slist_cnt = nullptr;
-      if (!cached && step_lists_wanted(sd, depth, ctx->near_mode) && nt.n > 0) {
-        StepState &sst = ctx->step_state[k];
-        Phase ph("step lists");
-        launch_step_lists(ctx, nt, sst, V.radius);
-        V.slist = sst.sl_list;
-        V.slist_cnt = sst.sl_cnt;
-        V.slist_stride = sst.sl_stride;
-        V.slist_cap = sst.sl_cap;
-        V.block_cap = 0;
-      }
       if (cached) {
         // Kept lists: agents in index order, neighbours read by index from
         // the step's own columns, no block lists.
@@ -2966,7 +2824,7 @@ int abl_set_profiling(abl_ctx *ctx, int enable) {
 }
 
 int abl_set_near_mode(abl_ctx *ctx, int mode) {
-  if (!ctx || mode < ABL_NEAR_AUTO || mode > ABL_NEAR_STEPLISTS) return ABL_E_INVALID;
+  if (!ctx || mode < ABL_NEAR_AUTO || mode > ABL_NEAR_BLOCK) return ABL_E_INVALID;
   ctx->near_mode = mode;
   ctx->prepared = false;
   drop_graph(ctx);

@@ -368,7 +368,7 @@ class Simulation:
         L.abl_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _check(L.abl_set_profiling(self.ctx, 1 if enable else 0), "abl_set_profiling")
 
-    NEAR_AUTO, NEAR_RUNS, NEAR_ROWS, NEAR_LISTS, NEAR_BLOCK, NEAR_STEPLISTS = 0, 1, 2, 3, 4, 5
+    NEAR_AUTO, NEAR_RUNS, NEAR_ROWS, NEAR_LISTS, NEAR_BLOCK = 0, 1, 2, 3, 4
 
     def set_near_mode(self, mode):
         """How ordered near loops gather neighbours (results are identical in every mode)."""

@@ -21,7 +21,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 MODES = [o.Simulation.NEAR_RUNS, o.Simulation.NEAR_ROWS, o.Simulation.NEAR_LISTS,
-         o.Simulation.NEAR_BLOCK, o.Simulation.NEAR_STEPLISTS]
+         o.Simulation.NEAR_BLOCK]
 CASES = [("circle_4000", "circle_4000", "Point"), ("circle3d_4000", "circle3d_4000", "Point"),
          ("boids2d_4096", "boids2d_4096", "Boid"),
          ("boids2d_4096_float", "boids2d_float_4096", "Boid"),
@@ -71,7 +71,7 @@ def test_clustered_boids_match_oracle(mode):
 
 @pytest.mark.parametrize("balance", [0, 1])
 @pytest.mark.parametrize("mode", [o.Simulation.NEAR_AUTO, o.Simulation.NEAR_BLOCK,
-                                  o.Simulation.NEAR_ROWS, o.Simulation.NEAR_STEPLISTS])
+                                  o.Simulation.NEAR_ROWS])
 def test_mixed_density_boids_match_oracle(mode, balance):
     """Uneven density in one domain: a sparse background (~8 agents per
     cell), a dense band (~60 per cell: most agents have more neighbours than
