@@ -981,15 +981,31 @@ __device__ int presort_block(const abl_near_view &V, bool has, const near_query<
   }
   S.fresh[t] = 1;
   if (!V.balance) return t;
-  S.key[t] = key;
-  __syncthreads();
-  int rank = 0;
+  // Counting sort of the block's agents by neighbour count, in 64 buckets
+  // (counts above 62 share the last; threads without an agent go last too).
+  // Agents of one bucket take their places in whatever order the atomics
+  // give: which thread runs an agent changes no result.
+  int *hist = S.key;  // 64 counters, then bucket starts (blockDim.x >= 64)
   const int nb = blockDim.x;
-  for (int j = 0; j < nb; j++) {
-    const int kj = S.key[j];
-    rank += (kj < key) || (kj == key && j < t);
+  for (int i = t; i < 64; i += nb) hist[i] = 0;
+  __syncthreads();
+  const int b = key < 63 ? key : 63;
+  const int local = atomicAdd(&hist[b], 1);
+  __syncthreads();
+  if (t < 32) {
+    const int a = hist[2 * t], c = hist[2 * t + 1];
+    int x = a + c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (t >= o) x += y;
+    }
+    const int start = x - a - c;
+    hist[2 * t] = start;
+    hist[2 * t + 1] = start + a;
   }
-  S.perm[rank] = t;
+  __syncthreads();
+  S.perm[hist[b] + local] = t;
   __syncthreads();
   return S.perm[t];
 }
