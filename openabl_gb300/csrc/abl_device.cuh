@@ -55,6 +55,11 @@
 // boids2d body fits without spilling, and the extra resident warps hide the
 // latency of the neighbour gathering (measured: 1M boids2d step kernel
 // 0.74 -> 0.67 ms against no cap; eight blocks gain nothing more and spill).
+// Neighbours held per agent in a presorted kernel's shared-memory column
+// (agents with more take further chunks).
+#ifndef ABL_LIST_CAP
+#define ABL_LIST_CAP 32
+#endif
 #ifndef ABL_STEP_MIN_BLOCKS
 #define ABL_STEP_MIN_BLOCKS 6
 #endif

@@ -930,7 +930,7 @@ struct abl_ctx {
   // count; neighbours held per agent in shared memory with and without
   // neighbourhood lists (4 and 8 bytes each).
   int balance = 1;
-  int list_cap = 32;
+  int list_cap = ABL_LIST_CAP;
   int runs_cap = 40;
   int near_mode = ABL_NEAR_AUTO;
   // Entries of a thread block's shared-memory neighbourhood lists (ABL_NEAR_BLOCK).
