@@ -215,8 +215,20 @@ int abl_ensemble_download(abl_ensemble *e, int type_id, size_t *counts, void *co
  * cell size as a multiple (>= 1) of the granularity, and whether threads visit
  * agents in cell order (1) or index order (0).  Results do not depend on it. */
 int abl_ensemble_set_tuning(abl_ensemble *e, int block, double cell_factor, int visit_sorted);
-/* Times every configuration for `trial_timesteps` timesteps, restores the
- * state after each trial and keeps the fastest. */
+/* Cells-per-block tiling of ordered 2D near loops when threads visit agents
+ * in cell order: each thread block merges the neighbourhood lists of the run
+ * of cells its agents fill once, in shared memory, holding up to `entries`
+ * list entries (0: no block tiling, every agent merges its own rows; else a
+ * multiple of 256 up to 4096).  A block whose cells need more falls back to
+ * per-agent merging.  Results do not depend on it. */
+int abl_ensemble_set_tiling(abl_ensemble *e, int entries);
+/* The configuration in use (any pointer may be NULL). */
+int abl_ensemble_get_tuning(abl_ensemble *e, int *block, double *cell_factor, int *visit_sorted,
+                            int *tiling_entries);
+/* Times every configuration -- block size, cell size factor, visiting order
+ * and tiling -- for `trial_timesteps` timesteps, restores the state after
+ * each trial and keeps the fastest (abl_ensemble_get_tuning reports the
+ * tiling it chose). */
 int abl_ensemble_autotune(abl_ensemble *e, int trial_timesteps, int *block, double *cell_factor,
                           int *visit_sorted);
 int abl_ensemble_last_exec_time(abl_ensemble *e, double *seconds);

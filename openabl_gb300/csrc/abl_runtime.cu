@@ -3749,9 +3749,27 @@ int abl_ensemble_set_tuning(abl_ensemble *e, int block, double cell_factor, int 
   return ABL_OK;
 }
 
-// Tries every combination of block size, cell size factor and visiting order
-// for `trial_timesteps` timesteps (after one warm-up timestep) and keeps the
-// fastest.  The state and timestep counter are restored after each trial, so
+int abl_ensemble_set_tiling(abl_ensemble *e, int entries) {
+  if (!e || entries < 0 || entries > 4096 || entries % 256) return ABL_E_INVALID;
+  if (entries != e->base.block_cap) e->prepared = false;  // views carry it
+  e->base.block_cap = entries;
+  ens_drop_graphs(e);
+  return ABL_OK;
+}
+
+int abl_ensemble_get_tuning(abl_ensemble *e, int *block, double *cell_factor, int *visit_sorted,
+                            int *tiling_entries) {
+  if (!e) return ABL_E_INVALID;
+  if (block) *block = e->block;
+  if (cell_factor) *cell_factor = e->cell_factor;
+  if (visit_sorted) *visit_sorted = e->visit_sorted;
+  if (tiling_entries) *tiling_entries = e->base.block_cap;
+  return ABL_OK;
+}
+
+// Tries every combination of block size, cell size factor, visiting order and
+// (with cell-order visits) block tiling for `trial_timesteps` timesteps
+// (after one warm-up timestep) and keeps the fastest.  The state and timestep counter are restored after each trial, so
 // tuning does not advance the simulation; every candidate computes identical
 // results.
 int abl_ensemble_autotune(abl_ensemble *e, int trial_timesteps, int *block, double *cell_factor,
@@ -3791,29 +3809,36 @@ int abl_ensemble_autotune(abl_ensemble *e, int trial_timesteps, int *block, doub
   const int blocks[] = {64, 128};
   const double factors[] = {1.0, 1.5, 2.0};
   const int visits[] = {1, 0};
+  const int tilings[] = {2048, 1024, 4096, 0};
   double best = 1e30;
-  int bb = e->block, bv = e->visit_sorted;
+  int bb = e->block, bv = e->visit_sorted, bt = e->base.block_cap;
   double bf = e->cell_factor;
   for (int b : blocks) {
     for (double f : factors) {
       for (int v : visits) {
-        ABL_TRY(abl_ensemble_set_tuning(e, b, f, v));
-        ABL_TRY(ens_ready(e));
-        ABL_TRY(restore());
-        e->timestep = ts0;
-        ABL_TRY(abl_ensemble_run(e, 1));
-        ABL_TRY(abl_ensemble_run(e, trial_timesteps));
-        double t = ctx->last_exec;
-        if (t < best) {
-          best = t;
-          bb = b;
-          bf = f;
-          bv = v;
+        for (int tl : tilings) {
+          if (!v && tl != tilings[0]) continue;  // tiling needs cell-order visits
+          ABL_TRY(abl_ensemble_set_tuning(e, b, f, v));
+          ABL_TRY(abl_ensemble_set_tiling(e, tl));
+          ABL_TRY(ens_ready(e));
+          ABL_TRY(restore());
+          e->timestep = ts0;
+          ABL_TRY(abl_ensemble_run(e, 1));
+          ABL_TRY(abl_ensemble_run(e, trial_timesteps));
+          double t = ctx->last_exec;
+          if (t < best) {
+            best = t;
+            bb = b;
+            bf = f;
+            bv = v;
+            bt = tl;
+          }
         }
       }
     }
   }
   ABL_TRY(abl_ensemble_set_tuning(e, bb, bf, bv));
+  ABL_TRY(abl_ensemble_set_tiling(e, bt));
   ABL_TRY(ens_ready(e));
   ABL_TRY(restore());
   ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));

@@ -421,6 +421,11 @@ class Ensemble:
         L.abl_ensemble_run.argtypes = [vp, ctypes.c_int]
         L.abl_ensemble_download.argtypes = [vp, ctypes.c_int, vp, ctypes.POINTER(vp)]
         L.abl_ensemble_set_tuning.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        L.abl_ensemble_set_tiling.argtypes = [vp, ctypes.c_int]
+        L.abl_ensemble_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(ctypes.c_int)]
         L.abl_ensemble_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_int)]
@@ -479,12 +484,25 @@ class Ensemble:
         _check(_load().abl_ensemble_set_tuning(self.e, block, cell_factor, visit_sorted),
                "abl_ensemble_set_tuning")
 
+    def set_tiling(self, entries):
+        """Block tiling of ordered 2D near loops: shared-memory list entries per
+        block (0: none); results do not depend on it."""
+        _check(_load().abl_ensemble_set_tiling(self.e, int(entries)), "abl_ensemble_set_tiling")
+
+    def tuning(self):
+        b, f, v, t = ctypes.c_int(), ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
+        _check(_load().abl_ensemble_get_tuning(self.e, ctypes.byref(b), ctypes.byref(f),
+                                               ctypes.byref(v), ctypes.byref(t)),
+               "abl_ensemble_get_tuning")
+        return {"block": b.value, "cell_factor": f.value, "visit_sorted": v.value,
+                "tiling_entries": t.value}
+
     def autotune(self, trial_timesteps=3):
         b, f, v = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
         _check(_load().abl_ensemble_autotune(self.e, trial_timesteps, ctypes.byref(b),
                                              ctypes.byref(f), ctypes.byref(v)),
                "abl_ensemble_autotune")
-        return {"block": b.value, "cell_factor": f.value, "visit_sorted": v.value}
+        return self.tuning()
 
     def last_exec_time(self):
         s = ctypes.c_double()

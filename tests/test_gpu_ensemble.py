@@ -50,3 +50,31 @@ def test_autotune_keeps_results():
             assert np.array_equal(ra[k], rb[k])
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("tiling", [0, 256, 1024, 4096])
+def test_block_tiling_keeps_results(tiling):
+    """The cells-per-block tiling knob (abl_ensemble_set_tiling) changes how
+    ordered near loops gather neighbours, never what they compute: every
+    setting gives the replicas the bits of separate contexts.  256 entries
+    are too few for most blocks, which then fall back to per-agent merging."""
+    model, base = o.globals_for_config("boids2d_4096")
+    gl, states, seeds = workloads.boids2d_ensemble(model, base, replicas=6, n_min=500,
+                                                   n_max=6000, seed=8)
+    ens = o.Ensemble(model, gl, seeds=seeds)
+    ens.set_tiling(tiling)
+    assert ens.tuning()["tiling_entries"] == tiling
+    ens.upload("Boid", states)
+    ens.run(6)
+    got = ens.download("Boid")
+    for r in range(len(gl)):
+        sim = o.Simulation(model, gl[r])
+        sim.upload("Boid", states[r])
+        sim.run(6)
+        want = sim.download("Boid")
+        sim.close()
+        for k in want:
+            assert np.array_equal(got[r][k], want[k]), (tiling, r, k)
+    with pytest.raises(o.AblError):
+        ens.set_tiling(100)
+    ens.close()
