@@ -188,7 +188,24 @@ def measure_ensemble(args, o, W, np):
     ens.run(T)
     ens_s = ens.last_exec_time()
     launches = ens.last_launch_count()
+    final = ens.download("Boid")
     ens.close()
+    # The same run as one persistent cooperative launch (its own autotune).
+    pe = o.Ensemble(model, gl, seeds=seeds)
+    pe.set_persistent(True)
+    pe.upload("Boid", states)
+    p_tuning = pe.autotune(3)
+    pe.run(3)
+    pe.upload("Boid", states)
+    pe.run(T)
+    pers_s = pe.last_exec_time()
+    pers = {"value": total * T / pers_s, "seconds": pers_s,
+            "gpu_launches": pe.last_launch_count(), "blocks": pe.persistent_blocks(),
+            "tuning": p_tuning,
+            "equal_to_per_phase_run": all(np.array_equal(a[k], b[k])
+                                          for a, b in zip(pe.download("Boid"), final)
+                                          for k in a)}
+    pe.close()
     base_s = 0.0
     base_launches = 0
     for g, st in zip(gl, states):
@@ -204,6 +221,7 @@ def measure_ensemble(args, o, W, np):
                         f"1e3-2e5 (total {total}), weights +-20%, {T} timesteps",
             "value": total * T / ens_s, "unit": "agent-steps/s", "seconds": ens_s,
             "gpu_launches": launches, "tuning": tuning,
+            "persistent": pers,
             "baseline_value": total * T / base_s, "baseline_seconds": base_s,
             "baseline_gpu_launches": base_launches,
             "baseline": "same replicas one after another, each in its own context",

@@ -233,6 +233,18 @@ int abl_ensemble_autotune(abl_ensemble *e, int trial_timesteps, int *block, doub
                           int *visit_sorted);
 int abl_ensemble_last_exec_time(abl_ensemble *e, double *seconds);
 int abl_ensemble_last_launch_count(abl_ensemble *e, long *launches);
+/* Persistent runs (enable = 1): abl_ensemble_run executes all its timesteps
+ * -- every binning phase and step function of every replica -- in ONE
+ * cooperative kernel launch of as many blocks as the device holds at once,
+ * the phases separated by grid-wide barriers.  Each barrier wait gives up
+ * after a time limit (4 s by default), and the run then returns
+ * ABL_E_TIMEOUT.  Results equal those of the per-phase launches bit for bit.
+ * ABL_E_UNSUPPORTED for models without an ensemble form.  The replicas'
+ * timestep pattern must repeat with period two after the first (every model
+ * whose steps all run each timestep does). */
+int abl_ensemble_set_persistent(abl_ensemble *e, int enable);
+/* Blocks of the last persistent launch (0 before the first). */
+int abl_ensemble_persistent_blocks(abl_ensemble *e, int *blocks);
 int abl_ensemble_destroy(abl_ensemble *e);
 
 /* ---- serving: continuous batching of simulation jobs ----

@@ -28,6 +28,15 @@ int abl_diag_fp64_add_as_fma_rate(double *per_s);
 int abl_diag_check_int_division(unsigned long long seed, long per_n,
                                 unsigned long long *checked, unsigned long long *mismatches);
 
+/* Failure injection for the persistent ensemble kernel's grid barriers
+ * (abl_ensemble_set_persistent): every wait gives up after limit_seconds,
+ * and each barrier waits for extra_arrivals arrivals beyond the launch's
+ * blocks.  With extra_arrivals = 1 no barrier can complete, so the next run
+ * returns ABL_E_TIMEOUT (-4) once the first wait has run out, with no kernel
+ * left running.  (0.0, 0) restores the defaults.  The ensemble handle is an
+ * abl_ensemble* of openabl_cuda.h. */
+int abl_diag_ensemble_barrier(void *ensemble, double limit_seconds, int extra_arrivals);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,7 +33,7 @@ namespace OpenABL {
 
 static const char *kRuntimeFiles[] = {
   "abl_runtime.cu", "abl_host.cpp", "abl_host.h", "abl_model.h", "abl_device.cuh",
-  "abl_math.cuh", "abl_gen.cuh",
+  "abl_math.cuh", "abl_gen.cuh", "abl_bin.cuh", "abl_persist.cuh",
 };
 
 static std::string runtimeDir(const BackendContext &ctx) {
@@ -124,13 +124,20 @@ void CudaBackend::generate(AST::Script &script, const BackendContext &ctx) {
     if (!fileExists(src)) throw std::runtime_error("cuda runtime file missing: " + src);
     copyFile(src, ctx.outputDir + "/" + f);
   }
-  std::string header = fileExists(rt + "/openabl_cuda.h")
-      ? rt + "/openabl_cuda.h" : std::string(ABL_CUDA_INCLUDE_DIR) + "/openabl_cuda.h";
-  copyFile(header, ctx.outputDir + "/openabl_cuda.h");
+  for (const char *h : {"openabl_cuda.h", "openabl_cuda_diag.h"}) {
+    std::string header = fileExists(rt + "/" + h) ? rt + "/" + h
+                                                  : std::string(ABL_CUDA_INCLUDE_DIR) + "/" + h;
+    copyFile(header, ctx.outputDir + "/" + h);
+  }
+  // The model file is compiled twice: once for its per-phase kernels, host
+  // code and main(), once with ABL_PERSIST for its persistent ensemble
+  // kernel (plain loads instead of read-only ones, abl_device.cuh).
+  const std::string nvcc = "nvcc -gencode arch=compute_103a,code=sm_103a -O3 -fmad=false "
+                           "-Xcompiler -ffp-contract=off -std=c++17 -diag-suppress 177 -I. ";
   writeToFile(ctx.outputDir + "/build.sh",
-              "nvcc -gencode arch=compute_103a,code=sm_103a -O3 -fmad=false -Xcompiler -ffp-contract=off "
-              "-std=c++17 -diag-suppress 177 "
-              "-DABL_STANDALONE_MAIN -I. " + model + ".cu abl_runtime.cu abl_host.cpp -o main\n");
+              nvcc + "-DABL_PERSIST -x cu -c " + model + ".cu -o " + model + ".persist.o && \\\n" +
+              nvcc + "-DABL_STANDALONE_MAIN " + model + ".cu abl_runtime.cu abl_host.cpp " +
+              model + ".persist.o -o main\n");
   writeToFile(ctx.outputDir + "/run.sh", "./main\n");
   makeFileExecutable(ctx.outputDir + "/build.sh");
   makeFileExecutable(ctx.outputDir + "/run.sh");

@@ -1138,6 +1138,10 @@ void CudaPrinter::printKernel(const StepInfo &info) {
   const std::string &T = agent.name;
   const std::string &name = decl.name;
   bool copy = copyOut();
+  // The per-phase kernels and their launchers are compiled once, without
+  // ABL_PERSIST; the persistent ensemble kernel's compilation (ABL_PERSIST)
+  // needs only the step bodies.
+  *this << nl << "#ifndef ABL_PERSIST";
   *this << nl << "struct abl_kargs_" << name << " {" << indent << nl
         << "abl_globals G;" << nl << "long n;" << nl << "const int *visit;" << nl
         << "abl_cols_" << T << " in, out;" << nl << "abl_near_view NB;" << nl
@@ -1222,17 +1226,20 @@ void CudaPrinter::printKernel(const StepInfo &info) {
         << "const long abl_grid = (A.n + abl_block - 1) / abl_block;" << nl
         << "abl_kernel_" << name << "<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);" << nl
         << "return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;" << outdent << nl
-        << "}" << nl;
-  if (info.addType < 0 && !info.usesRemove) {
+        << "}" << nl << "#endif" << nl;
+  if (ensembleStep(info)) {
     // Ensemble variant: every agent reads its replica's globals and grid.
     // Random numbers are keyed by the replica's seed and the agent's index
     // within its replica, so each replica draws what it would draw alone.
-    *this << "__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_" << name
-          << "(const __grid_constant__ abl_ens_launch A) {" << indent << nl;
+    // The body runs the agents of virtual block abl_vb at timestep abl_ts:
+    // the per-phase kernel passes its block index, the persistent kernel
+    // strides over the blocks of every step function of every timestep.
+    *this << "__device__ __forceinline__ void abl_ens_body_" << name
+          << "(const abl_ens_launch &A, long abl_vb, long abl_ts) {" << indent << nl;
     if (info.presorted) {
       int posIdx = memberIndex(&agent, agent.getPositionMember());
       *this << "int abl_j;" << nl << "{" << indent << nl
-            << "const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl
+            << "const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;" << nl
             << "const bool abl_has = abl_t1 < A.n;" << nl
             << "const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] "
                ": abl_t1) : 0;" << nl
@@ -1243,9 +1250,9 @@ void CudaPrinter::printKernel(const StepInfo &info) {
                         "((const " + cType(agent.getPositionMember()->type->resolved)
                             + " *) A.in_cols[" + std::to_string(posIdx) + "])[abl_i1]");
       *this << outdent << nl << "}" << nl
-            << "const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;" << nl;
+            << "const long abl_t = abl_vb * blockDim.x + abl_j;" << nl;
     } else {
-      *this << "const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;" << nl;
+      *this << "const long abl_t = abl_vb * blockDim.x + threadIdx.x;" << nl;
     }
     *this << "if (abl_t >= A.n) return;" << nl
           << "const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;" << nl
@@ -1253,7 +1260,7 @@ void CudaPrinter::printKernel(const StepInfo &info) {
           << "const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];" << nl
           << "abl::step_ctx abl_K;" << nl
           << "abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), "
-             "(uint32_t) A.step_index, (uint64_t) A.timestep);"
+             "(uint32_t) A.step_index, (uint64_t) abl_ts);"
           << nl << "abl_K.self = abl_i;" << nl << "abl_K.removed = 0;" << nl
           << "abl_K.added = 0;" << nl << "abl_K.child_cols = nullptr;" << nl
           << "abl_K.near_col = " << (info.presorted ? "abl_j" : "-1") << ";" << nl
@@ -1284,25 +1291,66 @@ void CudaPrinter::printKernel(const StepInfo &info) {
               << m.name << ";";
       }
     }
-    *this << outdent << nl << "}" << nl
-          << "static int abl_launch_ens_" << name
+    *this << outdent << nl << "}" << nl << "#ifndef ABL_PERSIST" << nl
+          << "__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_"
+          << name << "(const __grid_constant__ abl_ens_launch A) {" << indent << nl
+          << "abl_ens_body_" << name << "(A, blockIdx.x, A.timestep);" << outdent << nl << "}"
+          << nl << "static int abl_launch_ens_" << name
           << "(const abl_ens_launch *L, cudaStream_t abl_stream) {" << indent << nl
           << "const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : "
              "ABL_STEP_BLOCK;" << nl
           << "const long abl_grid = (L->n + abl_block - 1) / abl_block;" << nl
           << "abl_kernel_ens_" << name << "<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);" << nl
           << "return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;" << outdent << nl
-          << "}" << nl;
+          << "}" << nl << "#endif" << nl;
   }
   if (info.nearLoop) {
-    *this << "static double abl_radius_" << name << "(const void *abl_gp) {" << indent << nl
+    *this << "#ifndef ABL_PERSIST" << nl
+          << "static double abl_radius_" << name << "(const void *abl_gp) {" << indent << nl
           << "const abl_globals &abl_G = *(const abl_globals *) abl_gp;" << nl
           << "abl::rng abl_R;" << nl << "(void) abl_G; (void) abl_R;" << nl
           << "return (double) (";
     printNearRadius(info);
     *this << ");" << outdent << nl
-          << "}" << nl;
+          << "}" << nl << "#endif" << nl;
   }
+}
+
+// Steps with an ensemble variant: no runtime population changes, and no
+// mixed-precision sums (the ensemble builds no float copies).
+bool CudaPrinter::ensembleStep(const StepInfo &s) const {
+  return s.addType < 0 && !s.usesRemove && !s.nearMembersF32 && !s.nearPosLo;
+}
+
+// The model supports ensembles when every step function in simulate order
+// has an ensemble variant and there is no sequential step.
+bool CudaPrinter::ensembleModel() const {
+  if (seqStep || !script.simStmt) return false;
+  for (AST::FunctionDeclaration *f : script.simStmt->stepFuncDecls) {
+    for (const StepInfo &s : steps) {
+      if (s.decl == f && !ensembleStep(s)) return false;
+    }
+  }
+  return !script.simStmt->stepFuncDecls.empty();
+}
+
+// The persistent ensemble kernel (compiled with ABL_PERSIST, into its own
+// object): every binning and step function of every timestep in one
+// cooperative launch (abl_persist.cuh).  step_index is the step's place in
+// simulate order, as the runtime numbers the model's steps.
+void CudaPrinter::printPersistentKernel() {
+  *this << "__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) "
+           "abl_kernel_ens_persist(const abl::persist_prog *abl_P, int *abl_err) {"
+        << indent << nl
+        << "abl::persist_run(abl_P, abl_err, [&](const abl_ens_launch &abl_L, long abl_vb, "
+           "long abl_ts) {" << indent << nl << "switch (abl_L.step_index) {" << indent;
+  const auto &order = script.simStmt->stepFuncDecls;
+  for (size_t k = 0; k < order.size(); k++) {
+    *this << nl << "case " << (int) k << ": abl_ens_body_" << order[k]->name
+          << "(abl_L, abl_vb, abl_ts); break;";
+  }
+  *this << nl << "default: break;" << outdent << nl << "}" << outdent << nl << "});"
+        << outdent << nl << "}" << nl;
 }
 
 void CudaPrinter::printGlobals() {
@@ -1616,8 +1664,7 @@ void CudaPrinter::printDescriptor() {
           << (s.ordered ? 1 : 0) << ", " << (s.nearLoop ? "abl_radius_" + n : "nullptr") << ", "
           << s.nearMembers << "u, " << s.outAlways << "u, abl_launch_" << n << ", "
           << (s.usesRemove ? 1 : 0) << ", " << s.addType << ", " << (copyOut() ? 1 : 0) << ", "
-          << (s.addType < 0 && !s.usesRemove && !s.nearMembersF32 && !s.nearPosLo
-                  ? "abl_launch_ens_" + n : std::string("nullptr"))
+          << (ensembleStep(s) ? "abl_launch_ens_" + n : std::string("nullptr"))
           << ", " << (s.usesRng ? 1 : 0) << ", " << (s.presorted ? 1 : 0) << ", " << s.outChanged
           << "u, " << (s.nearCacheable ? 1 : 0);
     if (s.nearMembersF32 || s.nearPosLo)
@@ -1646,8 +1693,9 @@ void CudaPrinter::printDescriptor() {
         << scalarConsts << ", abl_global_table, " << envDim
         << ", abl_env_bounds, " << (granE ? "abl_granularity" : "nullptr") << ", "
         << (useFloat ? 1 : 0) << ", "
-        << (seqStep ? "abl_seq_" + seqStep->name : std::string("nullptr")) << outdent << nl
-        << "};" << nl;
+        << (seqStep ? "abl_seq_" + seqStep->name : std::string("nullptr")) << ", "
+        << (ensembleModel() ? "abl_persist_launch_" + modelName : std::string("nullptr"))
+        << outdent << nl << "};" << nl;
 }
 
 void CudaPrinter::print(const AST::Script &) {
@@ -1703,18 +1751,36 @@ void CudaPrinter::print(const AST::Script &) {
   }
   *this << nl;
   if (deviceInit && mainDecl) findDeviceInit(*mainDecl);
+  const bool persist = ensembleModel();
+  *this << "#ifndef ABL_PERSIST" << nl;
   printDeviceInit();
+  if (persist) {
+    *this << "extern \"C\" int abl_persist_launch_" << modelName
+          << "(const void *, int *, int, size_t, int *, cudaStream_t);" << nl;
+  }
   printDescriptor();
   if (mainDecl) {
     printHostSimulate();
     *this << *mainDecl << nl;
   }
-  *this << nl << "}  // namespace abl_model_" << modelName << nl << nl
+  *this << "#else" << nl;
+  if (persist) printPersistentKernel();
+  *this << "#endif" << nl;
+  *this << nl << "}  // namespace abl_model_" << modelName << nl << nl;
+  if (persist) {
+    *this << "#ifdef ABL_PERSIST" << nl << "extern \"C\" int abl_persist_launch_" << modelName
+          << "(const void *abl_prog, int *abl_err, int abl_block, size_t abl_smem, int *abl_grid, "
+             "cudaStream_t abl_stream) {" << indent << nl
+          << "return abl::persist_launch((const void *) abl_model_" << modelName
+          << "::abl_kernel_ens_persist, abl_prog, abl_err, abl_block, abl_smem, abl_grid, "
+             "abl_stream);" << outdent << nl << "}" << nl << "#endif" << nl;
+  }
+  *this << "#ifndef ABL_PERSIST" << nl
         << "extern \"C\" const abl_model_desc *abl_model_desc_" << modelName << "(void) {"
         << indent << nl << "return &abl_model_" << modelName << "::abl_desc;" << outdent << nl
-        << "}" << nl;
+        << "}" << nl << "#endif" << nl;
   if (mainDecl) {
-    *this << nl << "#ifdef ABL_STANDALONE_MAIN" << nl
+    *this << nl << "#if defined(ABL_STANDALONE_MAIN) && !defined(ABL_PERSIST)" << nl
           << "extern \"C\" const abl_model_desc *const abl_builtin_models[] = {" << nl
           << "    &abl_model_" << modelName << "::abl_desc, nullptr};" << nl
           << "int main() { return abl_model_" << modelName << "::abl_main(); }" << nl

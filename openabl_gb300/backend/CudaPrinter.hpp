@@ -150,6 +150,9 @@ private:
   void printNearRadius(const StepInfo &info);
   void printPresortPhase(const StepInfo &info, const std::string &view, const std::string &pos);
   void printDescriptor();
+  bool ensembleStep(const StepInfo &s) const;
+  bool ensembleModel() const;
+  void printPersistentKernel();
   void printHostSimulate();
   void printUserFunction(const AST::FunctionDeclaration &decl);
   void printSeqStep(const AST::FunctionDeclaration &decl);

@@ -35,11 +35,19 @@ def nvcc():
 
 
 def sources():
+    """(source, defines) pairs.  A model with a persistent ensemble kernel is
+    compiled a second time with ABL_PERSIST, which builds only that kernel
+    (with plain instead of read-only loads) into an object of its own."""
     srcs = [os.path.join(CSRC, "abl_runtime.cu"), os.path.join(CSRC, "abl_host.cpp"),
             os.path.join(CSRC, "abl_diag.cu"), os.path.join(CSRC, "abl_serve.cpp"),
             os.path.join(GEN, "registry.cpp")]
-    srcs += sorted(os.path.join(GEN, f) for f in os.listdir(GEN) if f.endswith(".cu"))
-    return srcs
+    models = sorted(os.path.join(GEN, f) for f in os.listdir(GEN) if f.endswith(".cu"))
+    out = [(s, ()) for s in srcs + models]
+    for m in models:
+        with open(m) as f:
+            if "#ifdef ABL_PERSIST\nextern \"C\" int abl_persist_launch_" in f.read():
+                out.append((m, ("-DABL_PERSIST",)))
+    return out
 
 
 def _deps_mtime():
@@ -48,13 +56,15 @@ def _deps_mtime():
     return max(os.path.getmtime(f) for f in files)
 
 
-def _compile(src):
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(item):
+    src, defines = item
+    tag = ".persist" if defines else ""
+    obj = os.path.join(BUILD, os.path.basename(src) + tag + ".o")
     if (os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src)
             and os.path.getmtime(obj) >= _deps_mtime()):
         return obj
     lang = ["-x", "cu"] if src.endswith((".cu", "registry.cpp")) else ["-Xcompiler", "-pthread"]
-    cmd = [nvcc()] + NVCC_FLAGS + lang + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + NVCC_FLAGS + list(defines) + lang + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
@@ -64,7 +74,7 @@ def _compile(src):
 def build(verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     srcs = sources()
-    with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+    with concurrent.futures.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, srcs))
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
         return LIB

@@ -42,6 +42,17 @@
 
 #include "abl_model.h"
 
+// Loads of data that no kernel writes while the reading kernel runs go
+// through the read-only (non-coherent) data path.  The persistent ensemble
+// kernel rewrites its grids between phases of one launch, where that path
+// could return lines cached before the rewrite, so its translation units are
+// compiled with ABL_PERSIST and use plain (coherent) loads.
+#ifdef ABL_PERSIST
+#define ABL_LDG(p) (*(p))
+#else
+#define ABL_LDG(p) __ldg(p)
+#endif
+
 #ifndef ABL_NEAR_CHUNK
 #define ABL_NEAR_CHUNK 32
 #endif
@@ -145,8 +156,8 @@ __device__ inline band make_band(double radius, float amax, int dim) {
 // Entry k of the kept neighbour lists (abl_near_view::ncache_list) of agent
 // `self`: the neighbour's agent index.
 __device__ __forceinline__ int kept_entry(const abl_near_view &V, long self, int k) {
-  return V.ncache_narrow ? (int) self + (int) __ldg(&((const short *) V.ncache_list)[k])
-                         : __ldg(&((const int *) V.ncache_list)[k]);
+  return V.ncache_narrow ? (int) self + (int) ABL_LDG(&((const short *) V.ncache_list)[k])
+                         : ABL_LDG(&((const int *) V.ncache_list)[k]);
 }
 
 // Query side of a near loop: the agent's cell and float position.
@@ -171,7 +182,7 @@ struct near_query {
     if (self >= 0 && V.ncache_off) {
       c[0] = c[1] = c[2] = 0;  // kept lists: no cell search
     } else if (self >= 0 && V.cell_of) {
-      const int l = (int) (__ldg(&V.cell_of[self]) - V.cell_base);
+      const int l = (int) (ABL_LDG(&V.cell_of[self]) - V.cell_base);
       const int nxy = V.nx * V.ny;
       c[2] = l / nxy;
       c[1] = (l - c[2] * nxy) / V.nx;
@@ -219,8 +230,8 @@ struct near_cursor {
     buf = chunk + threadIdx.x;
     if (V.ncache_off && q.self >= 0) {
       // The agent's neighbour list kept across timesteps.
-      cur = __ldg(&V.ncache_off[q.self]);
-      end = __ldg(&V.ncache_off[q.self + 1]);
+      cur = ABL_LDG(&V.ncache_off[q.self]);
+      end = ABL_LDG(&V.ncache_off[q.self + 1]);
       rz = ry = 0;
       x0 = x1 = 0;
     } else if (V.ordered) {
@@ -269,12 +280,12 @@ struct near_cursor {
     }
     for (;;) {
       while (cur < end && cnt < ABL_NEAR_CHUNK) {
-        int s = V.ordered ? __ldg(&V.nb_list[cur]) : cur;
+        int s = V.ordered ? ABL_LDG(&V.nb_list[cur]) : cur;
         cur++;
         float d2 = 0.0f;
 #pragma unroll
         for (int d = 0; d < DIM; d++) {
-          float dd = __ldg(&V.posf[DIM * s + d]) - q.pf[d];
+          float dd = ABL_LDG(&V.posf[DIM * s + d]) - q.pf[d];
           d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
         }
         bool take;
@@ -343,7 +354,7 @@ static __device__ constexpr recip_table recip = make_recip_table();
 __device__ __forceinline__ double div_int(double a, int n) {
   const unsigned e = ((unsigned) __double2hiint(a) >> 20) & 0x7ffu;
   if ((unsigned) (n - 1) < (unsigned) (kRecipN - 1) && e >= 200u && e < 0x7ffu) {
-    const double2 y = __ldg(reinterpret_cast<const double2 *>(recip.v) + n);
+    const double2 y = ABL_LDG(reinterpret_cast<const double2 *>(recip.v) + n);
     return __fma_rn(a, y.x, __dmul_rn(a, y.y));
   }
   return __ddiv_rn(a, (double) n);
@@ -556,16 +567,16 @@ __device__ int gather_sorted(const presort_shared &S, const abl_near_view &V,
   for (int z = zlo; z <= zhi; z++) {
     for (int y = ylo; y <= yhi; y++) {
       const int base = (z * V.ny + y) * V.nx;
-      const int s1 = __ldg(&V.cell_start[base + x1 + 1]);
-      for (int s = __ldg(&V.cell_start[base + x0]); s < s1; s++) {
+      const int s1 = ABL_LDG(&V.cell_start[base + x1 + 1]);
+      for (int s = ABL_LDG(&V.cell_start[base + x0]); s < s1; s++) {
         float d2 = 0.0f;
 #pragma unroll
         for (int d = 0; d < DIM; d++) {
-          float dd = __ldg(&V.posf[DIM * s + d]) - q.pf[d];
+          float dd = ABL_LDG(&V.posf[DIM * s + d]) - q.pf[d];
           d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
         }
         if (d2 > q.bd.hi) continue;
-        const int id = __ldg(&V.order[s]);
+        const int id = ABL_LDG(&V.order[s]);
         if (id <= lower) continue;
         if (!(d2 < q.bd.lo) && !exact(s)) continue;
         total++;
@@ -616,7 +627,7 @@ __device__ __forceinline__ int filter_candidates(const presort_shared &S, const 
     float d2 = 0.0f;
 #pragma unroll
     for (int d = 0; d < DIM; d++) {
-      const float dd = __ldg(&V.posf[DIM * s + d]) - q.pf[d];
+      const float dd = ABL_LDG(&V.posf[DIM * s + d]) - q.pf[d];
       d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
     }
     return d2;
@@ -649,10 +660,10 @@ __device__ int gather_list(const presort_shared &S, const abl_near_view &V,
                            const near_query<DIM> &q, Exact &exact, int col, int from,
                            int &stored, int &next) {
   const int cell = (q.c[2] * V.ny + q.c[1]) * V.nx + q.c[0];
-  const int end = __ldg(&V.nb_off[cell + 1]);
+  const int end = ABL_LDG(&V.nb_off[cell + 1]);
   const int *list = V.nb_list;
   return filter_candidates(S, V, q, exact, col, from, end,
-                           [list](int k) { return __ldg(&list[k]); }, stored, next);
+                           [list](int k) { return ABL_LDG(&list[k]); }, stored, next);
 }
 
 // Rows mode (2D): the in-radius neighbours with id > lower, taken in
@@ -676,10 +687,10 @@ __device__ int gather_rows(const presort_shared &S, const abl_near_view &V,
     pos[k] = end[k] = 0;
     if (y >= 0 && y < V.ny) {
       const int u = y * V.nx + q.c[0];
-      pos[k] = __ldg(&V.row_off[u]);
-      end[k] = __ldg(&V.row_off[u + 1]);
+      pos[k] = ABL_LDG(&V.row_off[u]);
+      end[k] = ABL_LDG(&V.row_off[u + 1]);
     }
-    h[k] = pos[k] < end[k] ? __ldg(&V.rows[pos[k]]) : make_int4(kNone, 0, 0, 0);
+    h[k] = pos[k] < end[k] ? ABL_LDG(&V.rows[pos[k]]) : make_int4(kNone, 0, 0, 0);
   }
   int n = 0, total = 0;
   last = lower;
@@ -693,7 +704,7 @@ __device__ int gather_rows(const presort_shared &S, const abl_near_view &V,
     for (int j = 0; j < 3; j++) {
       if (j == k) {
         const int e = ++pos[j];
-        h[j] = e < end[j] ? __ldg(&V.rows[e]) : make_int4(kNone, 0, 0, 0);
+        h[j] = e < end[j] ? ABL_LDG(&V.rows[e]) : make_int4(kNone, 0, 0, 0);
       }
     }
     if (v.x <= lower) continue;
@@ -837,8 +848,8 @@ __device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bo
       int b = 0, n = 0;
       if (y >= 0 && y < V.ny) {
         const int u = y * V.nx + q.c[0];
-        b = __ldg(&V.row_off[u]);
-        n = __ldg(&V.row_off[u + 1]) - b;
+        b = ABL_LDG(&V.row_off[u]);
+        n = ABL_LDG(&V.row_off[u + 1]) - b;
       }
       lrow[3 * t + k] = b;
       llen[3 * t + k] = n;
@@ -861,8 +872,8 @@ __device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bo
       hi = hi > ncells - 1 ? ncells - 1 : hi;
       int e0 = 0, n = 0;
       if (lo <= hi) {
-        e0 = __ldg(&V.row_off[lo]);
-        n = __ldg(&V.row_off[hi + 1]) - e0;
+        e0 = ABL_LDG(&V.row_off[lo]);
+        n = ABL_LDG(&V.row_off[hi + 1]) - e0;
       }
       scr[168 + k] = e0;
       scr[171 + k] = n;
@@ -886,7 +897,7 @@ __device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bo
 #pragma unroll
         for (int u = 0; u < kBatch; u++) {
           const int i = i0 + u * nb + t;
-          if (i < n) v[u] = __ldg(&ids[4 * (e0 + i)]);
+          if (i < n) v[u] = ABL_LDG(&ids[4 * (e0 + i)]);
         }
 #pragma unroll
         for (int u = 0; u < kBatch; u++) {
@@ -913,7 +924,7 @@ __device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bo
     // Staged position of list m of this leader: its row list lies in range m.
     auto spos = [&](int m) { return scr[174 + m] + (lrow[3 * lt + m] - scr[168 + m]); };
     const int id = sid[spos(l) + i];
-    const int slot = __ldg(reinterpret_cast<const int *>(V.rows) + 4 * (lrow[3 * lt + l] + i) + 1);
+    const int slot = ABL_LDG(reinterpret_cast<const int *>(V.rows) + 4 * (lrow[3 * lt + l] + i) + 1);
     int p = lbase[lo] + i;
 #pragma unroll
     for (int m = 0; m < 3; m++) {
@@ -942,7 +953,7 @@ __device__ bool gather_block(const presort_shared &S, const abl_near_view &V, bo
 
 template <int DIM>
 __device__ __forceinline__ int list_begin(const abl_near_view &V, const near_query<DIM> &q) {
-  return __ldg(&V.nb_off[(q.c[2] * V.ny + q.c[1]) * V.nx + q.c[0]]);
+  return ABL_LDG(&V.nb_off[(q.c[2] * V.ny + q.c[1]) * V.nx + q.c[0]]);
 }
 
 // Phase one of a presorted step kernel; every thread of the block calls it.
@@ -959,7 +970,7 @@ __device__ int presort_block(const abl_near_view &V, bool has, const near_query<
   if (V.ncache_off) {
     // The agent's neighbour list kept across timesteps (ascending id).
     if (has) {
-      const int from = __ldg(&V.ncache_off[q.self]), end = __ldg(&V.ncache_off[q.self + 1]);
+      const int from = ABL_LDG(&V.ncache_off[q.self]), end = ABL_LDG(&V.ncache_off[q.self + 1]);
       const int n = end - from < S.cap ? end - from : S.cap;
       for (int j = 0; j < n; j++) S.slots[j * ABL_STEP_BLOCK + t] = kept_entry(V, q.self, from + j);
       key = end - from;
@@ -1043,8 +1054,8 @@ struct near_list_cursor {
       // A second pass over the neighbours, or the ones past the stored ones.
       int stored = 0, tot = 0;
       if (V.ncache_off) {
-        const int from = first ? __ldg(&V.ncache_off[q.self]) : S.resume[col];
-        const int end = __ldg(&V.ncache_off[q.self + 1]);
+        const int from = first ? ABL_LDG(&V.ncache_off[q.self]) : S.resume[col];
+        const int end = ABL_LDG(&V.ncache_off[q.self + 1]);
         const int n = end - from < S.cap ? end - from : S.cap;
         for (int j = 0; j < n; j++) S.slots[j * ABL_STEP_BLOCK + col] = kept_entry(V, q.self, from + j);
         S.resume[col] = from + n;
@@ -1096,7 +1107,7 @@ struct lazy_dist {
     float d2 = 0.0f;
 #pragma unroll
     for (int d = 0; d < DIM; d++) {
-      float dd = __ldg(&V.posf[DIM * slot + d]) - q.pf[d];
+      float dd = ABL_LDG(&V.posf[DIM * slot + d]) - q.pf[d];
       d2 = __fadd_rn(d2, __fmul_rn(dd, dd));
     }
     d2f = d2;
@@ -1202,12 +1213,12 @@ struct facc {
   // DIM floats of a slot-ordered array (one 8-byte load for two)
   __device__ __forceinline__ static void load(const float *a, int s, float *out) {
     if (DIM == 2) {
-      const ::float2 t = __ldg(reinterpret_cast<const ::float2 *>(a) + s);
+      const ::float2 t = ABL_LDG(reinterpret_cast<const ::float2 *>(a) + s);
       out[0] = t.x;
       out[DIM - 1] = t.y;
     } else {
 #pragma unroll
-      for (int d = 0; d < DIM; d++) out[d] = __ldg(&a[DIM * s + d]);
+      for (int d = 0; d < DIM; d++) out[d] = ABL_LDG(&a[DIM * s + d]);
     }
   }
   __device__ __forceinline__ void add_offset(const abl_near_view &V, int s,

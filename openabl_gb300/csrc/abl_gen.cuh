@@ -10,6 +10,9 @@
 #include <cstring>
 
 #include "abl_device.cuh"
+#ifdef ABL_PERSIST
+#include "abl_persist.cuh"
+#endif
 #include "abl_host.h"
 #include "abl_model.h"
 #include "openabl_cuda.h"

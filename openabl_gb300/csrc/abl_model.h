@@ -132,6 +132,15 @@ typedef struct {
 } abl_ens_launch;
 
 typedef int (*abl_ens_launch_fn)(const abl_ens_launch *launch, cudaStream_t stream);
+
+/* Persistent ensemble kernel: runs the program `prog` (device memory, an
+ * abl::persist_prog of abl_persist.cuh) in one cooperative launch of as many
+ * blocks of `block` threads as are co-resident on the device with `smem`
+ * bytes of dynamic shared memory each; *grid receives that block count.
+ * With prog == NULL it only computes *grid.  `error` is the device error
+ * word for non-finite positions. */
+typedef int (*abl_persist_launch_fn)(const void *prog, int *error, int block, size_t smem,
+                                     int *grid, cudaStream_t stream);
 typedef double (*abl_globals_fn)(const void *globals);
 typedef void (*abl_env_fn)(const void *globals, double *min3, double *max3);
 
@@ -184,6 +193,7 @@ struct abl_model_desc {
   abl_globals_fn granularity;    /* cell size before the safety margin */
   int uses_float;                /* built with use_float */
   abl_seq_step_fn seq_step;      /* NULL when the simulation has none */
+  abl_persist_launch_fn launch_ens_persist; /* NULL when the model has no ensemble form */
 };
 
 #endif /* ABL_MODEL_H */

@@ -29,16 +29,22 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
 
+#include "abl_bin.cuh"
 #include "abl_device.cuh"
 #include "abl_model.h"
+#include "abl_persist.cuh"
+#include "openabl_cuda_diag.h"
 
 namespace {
+
+using namespace ablbin;
 
 constexpr int kScanBlock = 1024;
 
@@ -195,31 +201,6 @@ struct ScanPlan {
 
 // ------------------------------------------------------------ binning
 
-// Folds m (this thread's largest |coordinate|) into *amax: a block-wide
-// maximum first, then one atomic per block, skipped when it cannot raise the
-// current value.  A per-warp atomic on the one address serialised up to
-// 500 K atomics per binning of 16M agents at the L2.
-__device__ __forceinline__ void fold_amax(float m, float *amax) {
-  __shared__ float warp_max[32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  if (lane == 0) warp_max[w] = m;
-  __syncthreads();
-  if (w == 0) {
-    m = lane < nw ? warp_max[lane] : 0.0f;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane == 0 && m > 0.0f && m > __ldcg(amax)) abl::atomic_max_nonneg(amax, m);
-  }
-}
-
-__device__ __forceinline__ bool finite_bits(double x) {
-  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
-}
-__device__ __forceinline__ bool finite_bits(float x) {
-  return ((__float_as_int(x) >> 23) & 0xff) != 0xff;
-}
 
 // F32: cell coordinates from the float-rounded position in FP32 (this GPU's
 // FP64 pipe is narrow; the conversions to float are needed for amax anyway).
@@ -258,47 +239,14 @@ __global__ void k_bin_scatter(long n, const int *cell_of, const int *local_rank,
                               const int *cell_start, int *order) {
   long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  order[cell_start[cell_of[i]] + local_rank[i]] = (int) i;
+  bin_scatter_item(i, cell_of, local_rank, cell_start, order);
 }
 
-// Sorts every cell's run of slots by agent id (one thread per cell,
-// insertion sort: runs are short).  Together with the counting-sort scatter
-// this gives the slot order sorted by (cell, agent id), deterministic.
+// One thread per cell: its run of slots sorted by agent id.
 __global__ void k_cell_sort(long ncells, const int *cell_start, int *order) {
   long c = (long) blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
-  int s = cell_start[c], e = cell_start[c + 1];
-  constexpr int K = 16;
-  if (e - s <= K) {
-    // Short runs (nearly all): loaded together into registers, sorted by an
-    // odd-even transposition network, stored back.
-    const int len = e - s;
-    int v[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) v[k] = k < len ? order[s + k] : 0x7fffffff;
-#pragma unroll
-    for (int p = 0; p < K; p++) {
-#pragma unroll
-      for (int k = p & 1; k + 1 < K; k += 2) {
-        const int a = min(v[k], v[k + 1]), b = max(v[k], v[k + 1]);
-        v[k] = a;
-        v[k + 1] = b;
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < K; k++)
-      if (k < len) order[s + k] = v[k];
-    return;
-  }
-  for (int i = s + 1; i < e; i++) {
-    int v = order[i];
-    int j = i - 1;
-    while (j >= s && order[j] > v) {
-      order[j + 1] = order[j];
-      j--;
-    }
-    order[j + 1] = v;
-  }
+  cell_sort_item(c, cell_start, order);
 }
 
 // Largest |coordinate| of a type that is not binned (query side only).
@@ -377,225 +325,19 @@ __global__ void k_count_eq(const void *col, long n, const __grid_constant__ EqAr
   if ((threadIdx.x & 31) == 0 && m) atomicAdd(out, (unsigned long long) __popc(m));
 }
 
-// Slot-ordered copies: float positions and the requested member columns.
-struct GatherArgs {
-  int nmem;
-  const void *src[ABL_MAX_MEMBERS];
-  void *dst[ABL_MAX_MEMBERS];
-  int bytes[ABL_MAX_MEMBERS];
-  // Up to four members of 16 bytes each (float2 of doubles, e.g. boids2d's
-  // pos and velocity): all loads issued before the stores.  pos16 is the
-  // position's place among them (-1: not gathered, or 3D).
-  int all16;
-  int pos16;
-};
-
 template <typename Real, int DIM>
 __global__ void k_gather(long n, const int *order, const Real *pos, float *posf,
                          const __grid_constant__ GatherArgs g) {
   long s = (long) blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  long i = order[s];
-  if (g.all16) {
-    uint4 v[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++)
-      if (k < g.nmem) v[k] = __ldg((const uint4 *) g.src[k] + i);
-    if (posf && g.pos16 >= 0 && DIM == 2) {
-      uint4 p = v[0];
-#pragma unroll
-      for (int k = 1; k < 4; k++)
-        if (k == g.pos16) p = v[k];
-      posf[2 * s] = (float) __hiloint2double((int) p.y, (int) p.x);
-      posf[2 * s + 1] = (float) __hiloint2double((int) p.w, (int) p.z);
-    } else if (posf) {
-#pragma unroll
-      for (int d = 0; d < DIM; d++) posf[DIM * s + d] = (float) pos[DIM * i + d];
-    }
-#pragma unroll
-    for (int k = 0; k < 4; k++)
-      if (k < g.nmem) ((uint4 *) g.dst[k])[s] = v[k];
-    return;
-  }
-  if (posf) {
-#pragma unroll
-    for (int d = 0; d < DIM; d++) posf[DIM * s + d] = (float) pos[DIM * i + d];
-  }
-  for (int k = 0; k < g.nmem; k++) {
-    int b = g.bytes[k];
-    if ((b & 7) == 0) {
-      const uint64_t *src = (const uint64_t *) g.src[k] + (b / 8) * i;
-      uint64_t *dst = (uint64_t *) g.dst[k] + (b / 8) * s;
-      for (int w = 0; w < b / 8; w++) dst[w] = src[w];
-    } else if ((b & 3) == 0) {
-      const uint32_t *src = (const uint32_t *) g.src[k] + (b / 4) * i;
-      uint32_t *dst = (uint32_t *) g.dst[k] + (b / 4) * s;
-      for (int w = 0; w < b / 4; w++) dst[w] = src[w];
-    } else {
-      const uint8_t *src = (const uint8_t *) g.src[k] + b * i;
-      uint8_t *dst = (uint8_t *) g.dst[k] + b * s;
-      for (int w = 0; w < b; w++) dst[w] = src[w];
-    }
-  }
-}
-
-// Per cell: number of candidates in the surrounding (2R+1)^DIM cells.
-// ------------------------------------------------- neighbourhood lists
-//
-// Ordered near loops read, per cell, the slots of every agent in the
-// surrounding (2R+1)^dim cells in ascending agent id.  The lists are built
-// one axis at a time: level 0 is the cells' own runs (id-sorted by
-// k_cell_sort); level a+1 merges, for every cell c, the level-a lists of the
-// cells c - R .. c + R along axis a.  An element's place in a merged list is
-// its index in its own source list plus, for every other source list, the
-// number of smaller ids there (a binary search), so every element is written
-// once per target list with no sorting pass.
-
-// Cell geometry of a single grid.
-struct GridGeom {
-  int nx, ny, nz, R;
-  __device__ void locate(long, long &base, int &gx, int &gy, int &gz, int &r) const {
-    base = 0;
-    gx = nx;
-    gy = ny;
-    gz = nz;
-    r = R;
-  }
-};
-
-// Coordinates of a cell within its grid (32-bit: grids have < 2^30 cells).
-struct CellPos {
-  int x[3], n[3];
-  int stride[3];
-  int R;
-};
-
-template <typename G>
-__device__ inline CellPos cell_pos(const G &geo, long c) {
-  long base;
-  int nx, ny, nz, R;
-  geo.locate(c, base, nx, ny, nz, R);
-  CellPos p;
-  const int l = (int) (c - base);
-  const int nxy = nx * ny;
-  p.x[2] = l / nxy;
-  const int r = l - p.x[2] * nxy;
-  p.x[1] = r / nx;
-  p.x[0] = r - p.x[1] * nx;
-  p.n[0] = nx;
-  p.n[1] = ny;
-  p.n[2] = nz;
-  p.stride[0] = 1;
-  p.stride[1] = nx;
-  p.stride[2] = nxy;
-  p.R = R;
-  return p;
-}
-
-// Neighbour of cell c (at p) at offset d along AXIS, or -1 outside the grid.
-template <int AXIS>
-__device__ inline long axis_neighbour(const CellPos &p, long c, int d) {
-  const int k = p.x[AXIS] + d;
-  if (k < 0 || k >= p.n[AXIS]) return -1;
-  return c + (long) d * p.stride[AXIS];
+  gather_item<Real, DIM>(s, order, pos, posf, g);
 }
 
 template <typename G, int AXIS>
 __global__ void k_sep_count(long ncells, G geo, const int *src_off, int *dst_cnt) {
   const long c = (long) blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
-  const CellPos p = cell_pos(geo, c);
-  int cnt = 0;
-  for (int d = -p.R; d <= p.R; d++) {
-    const long u = axis_neighbour<AXIS>(p, c, d);
-    if (u >= 0) cnt += src_off[u + 1] - src_off[u];
-  }
-  dst_cnt[c] = cnt;
-}
-
-// Source lists of one level.  Level 0: the binned slots themselves (list of
-// cell u = slots off[u] .. off[u+1]); later levels store one element per
-// entry: (id, slot, float x, float y), the float position of the slot being
-// what the radius prefilter reads.
-struct SepSrc {
-  const int *off;     // ncells + 1
-  const int *order;   // level 0: slot -> id
-  const float *posf;  // level 0: slot -> float position (dim per slot)
-  int dim;
-  const int4 *elem;   // later levels
-};
-
-constexpr int kSepMaxSrc = 7;    // source lists per target: 2R + 1 for R <= 3
-constexpr int kSepWarps = 8;     // target cells (warps) per block of the warp merge kernels
-constexpr int kSepThreads = 128; // target cells (threads) per block of k_sep_merge
-
-template <bool LEVEL0>
-__device__ __forceinline__ int4 sep_elem_t(const SepSrc &S, int e) {
-  if (!LEVEL0) return __ldg(&S.elem[e]);
-  return make_int4(__ldg(&S.order[e]), e, __float_as_int(__ldg(&S.posf[S.dim * e])),
-                   __float_as_int(__ldg(&S.posf[S.dim * e + 1])));
-}
-
-__device__ __forceinline__ int4 sep_elem(const SepSrc &S, int e) {
-  return S.elem ? sep_elem_t<false>(S, e) : sep_elem_t<true>(S, e);
-}
-
-__device__ inline int lower_bound_src(const SepSrc &S, int b, int len, int id) {
-  int lo = 0, hi = len;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (sep_elem(S, b + mid).x < id) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// Source lists of target cell t along AXIS: begin and length per offset
-// -R .. R (length 0 outside the grid).  Returns the total length.
-template <int AXIS>
-__device__ inline int sep_sources(const CellPos &P, long t, const SepSrc &S, int *b, int *n) {
-  int total = 0;
-#pragma unroll
-  for (int k = 0; k < kSepMaxSrc; k++) {
-    b[k] = 0;
-    n[k] = 0;
-    const int d = k - P.R;
-    if (d > P.R) continue;
-    const long u = axis_neighbour<AXIS>(P, t, d);
-    if (u < 0) continue;
-    b[k] = S.off[u];
-    n[k] = S.off[u + 1] - b[k];
-    total += n[k];
-  }
-  return total;
-}
-
-// A three-way merge of the id-sorted source lists pos[k] .. end[k], by one
-// thread.  Writes elements (dst_elem) or, for the last level, slots only
-// (dst_slot).
-template <bool LEVEL0>
-__device__ void seq_merge3(const SepSrc &S, int *pos, const int *end, int total, long out0,
-                           int4 *dst_elem, int *dst_slot) {
-  const int kNone = 0x7fffffff;
-  int4 h[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++)
-    h[k] = pos[k] < end[k] ? sep_elem_t<LEVEL0>(S, pos[k]) : make_int4(kNone, 0, 0, 0);
-  for (int q = 0; q < total; q++) {
-    const bool a01 = h[0].x < h[1].x;
-    const int m01 = a01 ? h[0].x : h[1].x;
-    const int k = h[2].x < m01 ? 2 : (a01 ? 0 : 1);
-    const int4 v = k == 0 ? h[0] : (k == 1 ? h[1] : h[2]);
-    if (dst_elem) dst_elem[out0 + q] = v;
-    else dst_slot[out0 + q] = v.y;
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      if (j == k) {
-        const int e = ++pos[j];
-        h[j] = e < end[j] ? sep_elem_t<LEVEL0>(S, e) : make_int4(kNone, 0, 0, 0);
-      }
-    }
-  }
+  sep_count_item<G, AXIS>(c, geo, src_off, dst_cnt);
 }
 
 // One thread per target cell with R = 1 (short lists: level 0).
@@ -604,18 +346,7 @@ __global__ void __launch_bounds__(kSepThreads)
 k_sep_merge(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_elem, int *dst_slot) {
   const long t = (long) blockIdx.x * kSepThreads + threadIdx.x;
   if (t >= ncells) return;
-  const CellPos P = cell_pos(geo, t);
-  const long out0 = dst_off[t];
-  const int total = (int) (dst_off[t + 1] - out0);
-  if (P.R != 1 || total == 0) return;
-  int pos[3], end[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const long u = axis_neighbour<AXIS>(P, t, k - 1);
-    pos[k] = u >= 0 ? S.off[u] : 0;
-    end[k] = u >= 0 ? S.off[u + 1] : 0;
-  }
-  seq_merge3<LEVEL0>(S, pos, end, total, out0, dst_elem, dst_slot);
+  sep_merge_item<G, AXIS, LEVEL0>(t, geo, S, dst_off, dst_elem, dst_slot);
 }
 
 // Level 0 of a single grid (R = 1), one thread per source slot: the three
@@ -665,15 +396,8 @@ __global__ void k_sep_rows_by_slot(long n, G geo, const int *cell_start, const i
   }
 }
 
-constexpr int kSepStage = 512;  // source ids a warp of k_sep_merge_warp stages
-
-// One warp per target cell with R = 1.  The ids of the three source lists
-// are staged in shared memory with coalesced loads; an element's place is
-// its index in its own list plus the number of smaller ids in the other two
-// (binary searches in shared memory; the lists hold different agents).  So
-// the loads are independent instead of a chain of one per merged element.
-// Cells whose sources exceed the staging area are merged by one lane.
-// Cells of grids with R > 1 are left to k_sep_merge_large.
+// One warp per target cell with R = 1, the source ids staged in shared
+// memory.
 template <typename G, int AXIS, bool LEVEL0>
 __global__ void __launch_bounds__(32 * kSepWarps)
 k_sep_merge_warp(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_elem,
@@ -681,65 +405,11 @@ k_sep_merge_warp(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_ele
   __shared__ int ids[kSepWarps][kSepStage];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long t = (long) blockIdx.x * kSepWarps + w;
-  if (t >= ncells) return;  // uniform over the warp, as is every exit below
-  const CellPos P = cell_pos(geo, t);
-  const long out0 = dst_off[t];
-  const int total = (int) (dst_off[t + 1] - out0);
-  if (P.R != 1 || total == 0) return;
-  int b[3], n[3], st[3];
-  int staged = 0;
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const long u = axis_neighbour<AXIS>(P, t, k - 1);
-    b[k] = u >= 0 ? S.off[u] : 0;
-    n[k] = u >= 0 ? S.off[u + 1] - b[k] : 0;
-    st[k] = staged;
-    staged += n[k];
-  }
-  if (staged > kSepStage) {
-    if (lane == 0) {
-      int pos[3] = {b[0], b[1], b[2]}, end[3] = {b[0] + n[0], b[1] + n[1], b[2] + n[2]};
-      seq_merge3<LEVEL0>(S, pos, end, total, out0, dst_elem, dst_slot);
-    }
-    return;
-  }
-  int *my = ids[w];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    for (int j = lane; j < n[k]; j += 32)
-      my[st[k] + j] = LEVEL0 ? __ldg(&S.order[b[k] + j]) : __ldg(&S.elem[b[k] + j].x);
-  }
-  __syncwarp();
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    for (int j = lane; j < n[k]; j += 32) {
-      const int4 v = sep_elem_t<LEVEL0>(S, b[k] + j);
-      int rank = j;
-#pragma unroll
-      for (int k2 = 0; k2 < 3; k2++) {
-        if (k2 == k) continue;
-        int lo = 0, len = n[k2];
-        const int *a = my + st[k2];
-        while (len > 0) {
-          const int half = len >> 1;
-          if (a[lo + half] < v.x) {
-            lo += half + 1;
-            len -= half + 1;
-          } else {
-            len = half;
-          }
-        }
-        rank += lo;
-      }
-      if (dst_elem) dst_elem[out0 + rank] = v;
-      else dst_slot[out0 + rank] = v.y;
-    }
-  }
+  if (t >= ncells) return;  // uniform over the warp
+  sep_merge_warp_item<G, AXIS, LEVEL0>(t, lane, geo, S, dst_off, dst_elem, dst_slot, ids[w]);
 }
 
-// One warp per target cell of a grid with R > 1: an element's place is its
-// index in its own source list plus a binary search in every other source
-// list.
+// One warp per target cell of a grid with R > 1.
 template <typename G, int AXIS>
 __global__ void __launch_bounds__(32 * kSepWarps)
 k_sep_merge_large(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_elem,
@@ -747,25 +417,9 @@ k_sep_merge_large(long ncells, G geo, SepSrc S, const int *dst_off, int4 *dst_el
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long t = (long) blockIdx.x * kSepWarps + w;
   if (t >= ncells) return;
-  const CellPos P = cell_pos(geo, t);
-  if (P.R == 1) return;
-  int b[kSepMaxSrc], n[kSepMaxSrc];
-  sep_sources<AXIS>(P, t, S, b, n);
-  const long out = dst_off[t];
-#pragma unroll
-  for (int k = 0; k < kSepMaxSrc; k++) {
-    for (int j = lane; j < n[k]; j += 32) {
-      const int4 v = sep_elem(S, b[k] + j);
-      int rank = j;
-#pragma unroll
-      for (int k2 = 0; k2 < kSepMaxSrc; k2++) {
-        if (k2 != k && n[k2] > 0) rank += lower_bound_src(S, b[k2], n[k2], v.x);
-      }
-      if (dst_elem) dst_elem[out + rank] = v;
-      else dst_slot[out + rank] = v.y;
-    }
-  }
+  sep_merge_large_item<G, AXIS>(t, lane, geo, S, dst_off, dst_elem, dst_slot);
 }
+
 
 // Intermediate levels of the separable list build (dim - 1 of them).
 struct SepLevels {
@@ -3162,52 +2816,18 @@ extern "C" int abl_step_noalloc(const abl_model_desc *model, const void *globals
 
 namespace {
 
-struct EnsGrid {
-  int nx, ny, nz, R;
-  double lo[3];
-  double inv_cell;
-  long cell_base;
-};
-
 template <typename Real, int DIM>
 __global__ void k_ens_bin_assign(const Real *pos, long n, const int *replica_of,
                                  const EnsGrid *grids, int *cell_of, int *cell_count,
                                  int *local_rank, float *amax, int *error) {
   long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
   float m = 0.0f;
-  if (i < n) {
-    const EnsGrid g = grids[replica_of[i]];
-    const int dims[3] = {g.nx, g.ny, g.nz};
-    int c[3] = {0, 0, 0};
-    bool finite = true;
-#pragma unroll
-    for (int d = 0; d < DIM; d++) {
-      double x = (double) pos[DIM * i + d];
-      finite = finite && isfinite(x);
-      c[d] = abl::cell_coord(x, g.lo[d], g.inv_cell, dims[d]);
-      m = fmaxf(m, fabsf((float) x));
-    }
-    if (!finite) atomicExch(error, ABL_E_NONFINITE);
-    int cell = (int) (g.cell_base + ((long) c[2] * g.ny + c[1]) * g.nx + c[0]);
-    cell_of[i] = cell;
-    local_rank[i] = atomicAdd(&cell_count[cell], 1);
-  }
+  if (i < n)
+    m = ens_bin_assign_item<Real, DIM>(i, pos, replica_of, grids, cell_of, cell_count,
+                                       local_rank, error);
   fold_amax(m, amax);
 }
 
-// Cell geometry of a segmented grid: each replica's cells in its own block.
-struct EnsGeom {
-  const int *cell_replica;
-  const EnsGrid *grids;
-  __device__ void locate(long c, long &base, int &gx, int &gy, int &gz, int &r) const {
-    const EnsGrid &g = grids[cell_replica[c]];
-    base = g.cell_base;
-    gx = g.nx;
-    gy = g.ny;
-    gz = g.nz;
-    r = g.R;
-  }
-};
 
 struct EnsType {
   const abl_agent_desc *d = nullptr;
@@ -3228,6 +2848,7 @@ struct EnsType {
   int *cell_count = nullptr, *cell_start = nullptr, *local_rank = nullptr, *cell_of = nullptr;
   int *order = nullptr;
   float *posf = nullptr, *amax = nullptr;
+  float *amax_acc = nullptr;  // persistent runs: the assign phase's maximum
   void *gcols[ABL_MAX_MEMBERS] = {};
   int *nb_cnt = nullptr, *nb_off = nullptr, *nb_list = nullptr;
   SepLevels sep;
@@ -3255,6 +2876,13 @@ struct abl_ensemble {
   std::vector<size_t> smem;  // per step: dynamic shared memory of its kernel
   std::vector<abl_ctx::Graph> graphs;
   long timestep = 0;
+  // persistent runs (abl_ensemble_set_persistent)
+  bool persistent = false;
+  abl::persist_prog *d_prog = nullptr;
+  abl::persist_sync *d_sync = nullptr;
+  unsigned long long barrier_limit_ns = 4000000000ull;
+  unsigned int barrier_extra = 0;
+  int persist_grid = 0;
 };
 
 namespace {
@@ -3267,7 +2895,7 @@ void ens_free_bins(abl_ensemble *e, EnsType &t) {
   t.cell_count = t.cell_start = t.local_rank = t.cell_of = t.order = nullptr;
   t.nb_cnt = t.nb_off = t.nb_list = t.cell_replica = nullptr;
   t.sep = SepLevels();
-  t.posf = t.amax = nullptr;
+  t.posf = t.amax = t.amax_acc = nullptr;
   t.d_grids = nullptr;
   for (auto &g : t.gcols) g = nullptr;
 }
@@ -3303,6 +2931,7 @@ int ens_prepare(abl_ensemble *e) {
     }
     auto *own = &t.allocs;
     ABL_TRY(dev_alloc_t(ctx, &t.amax, 1, own));
+    ABL_TRY(dev_alloc_t(ctx, &t.amax_acc, 1, own));
     if (!t.is_near) continue;
     int dim = t.d->dim;
     t.grids.assign(e->replicas, EnsGrid());
@@ -3572,6 +3201,187 @@ int ens_capture(abl_ensemble *e, abl_ctx::Graph **out) {
   return ABL_OK;
 }
 
+// ---------------------------------------------------- persistent runs
+//
+// A persistent run records the ops of a timestep -- the binnings and step
+// functions ens_step_once would launch, with the buffers they would use --
+// into a program (abl_persist.cuh) and runs all timesteps in one cooperative
+// launch of the model's persistent kernel.  The double buffers flip every
+// timestep, so from the second timestep on the program repeats with period
+// two; the first may differ (types that are binned once and never stepped).
+
+// The binning of `t` from its current buffer, as ens_launch_bin does it.
+void ens_persist_bin(abl_ensemble *e, EnsType &t, abl::persist_bin &B) {
+  std::memset(&B, 0, sizeof B);
+  const int dim = t.d->dim;
+  B.dim = dim;
+  B.pos_double = t.d->members[t.d->position_member].scalar_bytes == 8;
+  B.n = t.n;
+  B.ncells = t.ncells;
+  B.pos = t.cols[t.cur][t.d->position_member];
+  B.replica_of = t.replica_of;
+  B.grids = t.d_grids;
+  B.cell_replica = t.cell_replica;
+  B.cell_of = t.cell_of;
+  B.cell_count = t.cell_count;
+  B.local_rank = t.local_rank;
+  B.order = t.order;
+  B.cell_start = t.cell_start;
+  B.posf = t.posf;
+  B.amax = t.amax;
+  B.amax_acc = t.amax_acc;
+  // Chunks of kScanBlock ints: the scan plan's first level has the room.
+  B.scan_incl = t.cell_scan.levels[0].incl;
+  B.scan_sums = t.cell_scan.levels[0].sums;
+  for (int k = 0; k < t.d->num_members; k++) {
+    if (!(t.gather_mask & (1u << k))) continue;
+    GatherArgs &g = B.gather;
+    g.src[g.nmem] = t.cols[t.cur][k];
+    g.dst[g.nmem] = t.gcols[k];
+    g.bytes[g.nmem] = (int) member_bytes(t.d->members[k]);
+    g.nmem++;
+  }
+  if (t.ordered || t.rows) {
+    B.levels = t.ordered ? dim : 1;
+    B.Rmax = 1;
+    for (auto &g : t.grids) B.Rmax = std::max(B.Rmax, g.R);
+    B.cnt = t.nb_cnt;
+    for (int a = 0; a < B.levels; a++) {
+      const bool last = a == dim - 1;
+      B.dst_off[a] = last ? t.nb_off : t.sep.off[a];
+      B.dst_elem[a] = last ? nullptr : t.sep.elem[a];
+      B.dst_slot[a] = last ? t.nb_list : nullptr;
+    }
+  }
+}
+
+// One timestep's ops into T (T == nullptr: only the bookkeeping -- buffer
+// flips, dirty flags, timestep -- that running it leaves behind).
+int ens_record(abl_ensemble *e, abl::persist_timestep *T) {
+  abl_ctx *ctx = &e->base;
+  const abl_model_desc *m = ctx->model;
+  int nops = 0;
+  auto next = [&]() -> abl::persist_op * {
+    if (!T) return nullptr;
+    if (nops >= abl::kPersistMaxOps) return nullptr;
+    return &T->ops[nops++];
+  };
+  for (int k = 0; k < m->num_steps; k++) {
+    const abl_step_desc &sd = m->steps[k];
+    EnsType &t = e->types[sd.agent_type];
+    if (sd.near_type >= 0) {
+      EnsType &nt = e->types[sd.near_type];
+      if (nt.dirty) {
+        if (T) {
+          abl::persist_op *op = next();
+          if (!op) return ABL_E_UNSUPPORTED;
+          op->kind = abl::kPersistBin;
+          ens_persist_bin(e, nt, op->bin);
+        }
+        nt.dirty = false;
+      }
+    }
+    if (T) {
+      abl::persist_op *op = next();
+      if (!op) return ABL_E_UNSUPPORTED;
+      op->kind = abl::kPersistStep;
+      abl_ens_launch &L = op->step;
+      std::memset(&L, 0, sizeof L);
+      L.n = t.n;
+      for (int j = 0; j < t.d->num_members; j++) {
+        L.in_cols[j] = t.cols[t.cur][j];
+        L.out_cols[j] = t.cols[1 - t.cur][j];
+      }
+      L.visit_order = (e->visit_sorted && sd.near_type == sd.agent_type) ? t.order : nullptr;
+      L.replica = t.replica_of;
+      L.globals = e->d_globals;
+      L.views = sd.near_type >= 0 ? e->d_views[k] : nullptr;
+      L.smem = e->smem[k];
+      L.agent_base = t.d_base;
+      L.seeds = e->d_seeds;
+      L.timestep = e->timestep;
+      L.step_index = k;
+      L.block = e->block;
+    }
+    t.cur = 1 - t.cur;
+    t.dirty = true;
+  }
+  if (T) T->nops = nops;
+  e->timestep++;
+  return ABL_OK;
+}
+
+// Puts the bookkeeping back to `key` (ens_graph_key) and timestep `ts`.
+void ens_restore(abl_ensemble *e, const std::vector<int> &key, long ts) {
+  for (size_t k = 0; k < e->types.size(); k++) {
+    e->types[k].cur = key[2 * k];
+    e->types[k].dirty = key[2 * k + 1] != 0;
+  }
+  e->timestep = ts;
+}
+
+std::vector<int> ens_graph_key(const abl_ensemble *e);
+
+int ens_run_persistent(abl_ensemble *e, int timesteps) {
+  abl_ctx *ctx = &e->base;
+  const abl_model_desc *m = ctx->model;
+  if (!m->launch_ens_persist) return ABL_E_UNSUPPORTED;
+  if (timesteps <= 0) return ABL_OK;
+  if (!e->d_prog) {
+    ABL_TRY(dev_alloc_t(ctx, &e->d_prog, 1));
+    ABL_TRY(dev_alloc_t(ctx, &e->d_sync, 1));
+  }
+  std::unique_ptr<abl::persist_prog> P(new abl::persist_prog());
+  const std::vector<int> k0 = ens_graph_key(e);
+  const long ts0 = e->timestep;
+  int r = ens_record(e, &P->ts[0]);
+  const std::vector<int> k1 = ens_graph_key(e);
+  if (r == ABL_OK) r = ens_record(e, &P->ts[1]);
+  if (r == ABL_OK && ens_graph_key(e) != k0) {
+    // The first timestep differs: ts[0] once, then ts[1], ts[2] in turn.
+    P->first_special = 1;
+    r = ens_record(e, &P->ts[2]);
+    if (r == ABL_OK && ens_graph_key(e) != k1) r = ABL_E_UNSUPPORTED;
+  }
+  ens_restore(e, k0, ts0);
+  if (r != ABL_OK) return r;
+  size_t smem = 0;
+  int levels = 0;
+  for (int k = 0; k < 3; k++) {
+    for (int o = 0; o < P->ts[k].nops; o++) {
+      const abl::persist_op &op = P->ts[k].ops[o];
+      if (op.kind == abl::kPersistStep) smem = std::max(smem, op.step.smem);
+      else levels = std::max(levels, op.bin.levels);
+    }
+  }
+  if (levels > 1)  // warp merges stage kSepStage ids per warp
+    smem = std::max(smem, (size_t) (e->block / 32) * kSepStage * sizeof(int));
+  P->timesteps = timesteps;
+  P->base_timestep = ts0;
+  P->sync = e->d_sync;
+  P->limit_ns = e->barrier_limit_ns;
+  P->extra_arrivals = e->barrier_extra;
+  P->scan_chunk = kScanBlock;
+  ABL_CUDA_TRY(cudaMemcpyAsync(e->d_prog, P.get(), sizeof(abl::persist_prog),
+                               cudaMemcpyHostToDevice, ctx->stream));
+  ABL_CUDA_TRY(cudaMemsetAsync(e->d_sync, 0, sizeof(abl::persist_sync), ctx->stream));
+  ABL_TRY(m->launch_ens_persist(e->d_prog, ctx->error, e->block, smem, &e->persist_grid,
+                                ctx->stream));
+  ctx->launches++;
+  // The host copy of the program must outlive the asynchronous copy.
+  ABL_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  for (int it = 0; it < timesteps; it++) ens_record(e, nullptr);
+  return ABL_OK;
+}
+
+// The barrier's error word after a persistent run (0 or ABL_E_TIMEOUT).
+int ens_persist_error(abl_ensemble *e) {
+  if (!e->d_sync) return ABL_OK;
+  int h = 0;
+  ABL_CUDA_TRY(cudaMemcpy(&h, &e->d_sync->error, sizeof(int), cudaMemcpyDeviceToHost));
+  return h;
+}
+
 // Graph replay bakes the timestep into kernel arguments, and random() keys
 // on it: models that draw in step functions run eagerly.
 bool uses_rng(const abl_model_desc *m) {
@@ -3697,7 +3507,11 @@ int abl_ensemble_run(abl_ensemble *e, int timesteps) {
   long l0 = ctx->launches;
   ABL_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
   int done = 0;
-  if (timesteps > 0) {
+  if (e->persistent && timesteps > 0) {
+    ABL_TRY(ens_run_persistent(e, timesteps));
+    done = timesteps;
+  }
+  if (done < timesteps) {
     ABL_TRY(ens_step_once(e));
     done = 1;
   }
@@ -3713,6 +3527,7 @@ int abl_ensemble_run(abl_ensemble *e, int timesteps) {
   for (; done < timesteps; done++) ABL_TRY(ens_step_once(e));
   ABL_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
   int r = check_error(ctx);
+  if (r == ABL_OK && e->persistent) r = ens_persist_error(e);
   float ms = 0.0f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   ctx->last_exec = ms / 1000.0;
@@ -3754,6 +3569,30 @@ int abl_ensemble_set_tiling(abl_ensemble *e, int entries) {
   if (entries != e->base.block_cap) e->prepared = false;  // views carry it
   e->base.block_cap = entries;
   ens_drop_graphs(e);
+  return ABL_OK;
+}
+
+int abl_ensemble_set_persistent(abl_ensemble *e, int enable) {
+  if (!e) return ABL_E_INVALID;
+  if (enable && !e->base.model->launch_ens_persist) return ABL_E_UNSUPPORTED;
+  e->persistent = enable != 0;
+  return ABL_OK;
+}
+
+int abl_ensemble_persistent_blocks(abl_ensemble *e, int *blocks) {
+  if (!e || !blocks) return ABL_E_INVALID;
+  *blocks = e->persist_grid;
+  return ABL_OK;
+}
+
+int abl_diag_ensemble_barrier(void *ensemble, double limit_seconds, int extra_arrivals) {
+  abl_ensemble *e = (abl_ensemble *) ensemble;
+  if (!e || limit_seconds < 0.0 || limit_seconds > 60.0 || extra_arrivals < 0 ||
+      extra_arrivals > 1)
+    return ABL_E_INVALID;
+  e->barrier_limit_ns = limit_seconds > 0.0 ? (unsigned long long) (limit_seconds * 1e9)
+                                            : 4000000000ull;
+  e->barrier_extra = (unsigned int) extra_arrivals;
   return ABL_OK;
 }
 

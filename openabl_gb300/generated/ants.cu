@@ -233,6 +233,7 @@ __device__ static void ant_deposit(const abl_globals &abl_G, const abl_near_view
     out->reward = 0;
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_ant_deposit {
     abl_globals G;
     long n;
@@ -319,10 +320,11 @@ static int abl_launch_ant_deposit(const abl_step_launch *L, cudaStream_t abl_str
     abl_kernel_ant_deposit<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_ant_deposit(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_ant_deposit(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -336,13 +338,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -362,18 +364,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((double *) A.out_cols[3])[abl_i] = abl_out.max_home;
     ((double *) A.out_cols[4])[abl_i] = abl_out.max_food;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_ant_deposit(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_ant_deposit(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_ant_deposit(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_ant_deposit<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_ant_deposit(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.pheromone_radius);
 }
+#endif
 
 __device__ static void pheromone_deposit(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Pheromone* in, Pheromone* out) {
     abl::rng &abl_R = abl_K.R;
@@ -417,6 +426,7 @@ __device__ static void pheromone_deposit(const abl_globals &abl_G, const abl_nea
     out->home = (home * abl_G.evaporationConstant);
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_pheromone_deposit {
     abl_globals G;
     long n;
@@ -491,10 +501,11 @@ static int abl_launch_pheromone_deposit(const abl_step_launch *L, cudaStream_t a
     abl_kernel_pheromone_deposit<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pheromone_deposit(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_pheromone_deposit(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -508,13 +519,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -528,18 +539,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((double *) A.out_cols[1])[abl_i] = abl_out.food;
     ((double *) A.out_cols[2])[abl_i] = abl_out.home;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pheromone_deposit(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_pheromone_deposit(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_pheromone_deposit(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_pheromone_deposit<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_pheromone_deposit(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (0.9);
 }
+#endif
 
 __device__ static void ant_act(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Ant* in, Ant* out) {
     abl::rng &abl_R = abl_K.R;
@@ -617,6 +635,7 @@ __device__ static void ant_act(const abl_globals &abl_G, const abl_near_view &ab
     out->pos = new_pos;
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_ant_act {
     abl_globals G;
     long n;
@@ -706,10 +725,11 @@ static int abl_launch_ant_act(const abl_step_launch *L, cudaStream_t abl_stream)
     abl_kernel_ant_act<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_ant_act(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_ant_act(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -723,13 +743,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -752,20 +772,29 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((double *) A.out_cols[4])[abl_i] = abl_out.max_food;
     ((bool *) A.out_cols[5])[abl_i] = abl_out.hasFood;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_ant_act(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_ant_act(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_ant_act(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_ant_act<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_ant_act(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.pheromone_radius);
 }
+#endif
 
 
+#ifndef ABL_PERSIST
+extern "C" int abl_persist_launch_ants(const void *, int *, int, size_t, int *, cudaStream_t);
 static const abl_member_desc abl_members_Ant[] = {
     {"pos", ABL_T_FLOAT2, 2, 8, 1},
     {"last_pos", ABL_T_FLOAT2, 2, 8, 0},
@@ -824,7 +853,7 @@ static const abl_step_desc abl_steps_ordered[] = {
     {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
 };
 extern const abl_model_desc abl_desc = {
-    "ants", 2, abl_agents, 3, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 17, abl_global_table, 2, abl_env_bounds, nullptr, 0, nullptr
+    "ants", 2, abl_agents, 3, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 17, abl_global_table, 2, abl_env_bounds, nullptr, 0, nullptr, abl_persist_launch_ants
 };
 static void abl_check(int r, const char *what) {
     if (r != ABL_OK) {
@@ -961,14 +990,33 @@ static int abl_main() {
     save(&agents, agents_info, "ants.out", SAVE_JSON);
     return 0;
 }
+#else
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_persist(const abl::persist_prog *abl_P, int *abl_err) {
+    abl::persist_run(abl_P, abl_err, [&](const abl_ens_launch &abl_L, long abl_vb, long abl_ts) {
+        switch (abl_L.step_index) {
+            case 0: abl_ens_body_ant_deposit(abl_L, abl_vb, abl_ts); break;
+            case 1: abl_ens_body_pheromone_deposit(abl_L, abl_vb, abl_ts); break;
+            case 2: abl_ens_body_ant_act(abl_L, abl_vb, abl_ts); break;
+            default: break;
+        }
+    });
+}
+#endif
 
 }  // namespace abl_model_ants
 
+#ifdef ABL_PERSIST
+extern "C" int abl_persist_launch_ants(const void *abl_prog, int *abl_err, int abl_block, size_t abl_smem, int *abl_grid, cudaStream_t abl_stream) {
+    return abl::persist_launch((const void *) abl_model_ants::abl_kernel_ens_persist, abl_prog, abl_err, abl_block, abl_smem, abl_grid, abl_stream);
+}
+#endif
+#ifndef ABL_PERSIST
 extern "C" const abl_model_desc *abl_model_desc_ants(void) {
     return &abl_model_ants::abl_desc;
 }
+#endif
 
-#ifdef ABL_STANDALONE_MAIN
+#if defined(ABL_STANDALONE_MAIN) && !defined(ABL_PERSIST)
 extern "C" const abl_model_desc *const abl_builtin_models[] = {
     &abl_model_ants::abl_desc, nullptr};
 int main() { return abl_model_ants::abl_main(); }

@@ -196,6 +196,7 @@ __device__ static void update_boid(const abl_globals &abl_G, const abl_near_view
     out->velocity = new_velocity;
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_update_boid {
     abl_globals G;
     long n;
@@ -253,40 +254,18 @@ static int abl_launch_update_boid(const abl_step_launch *L, cudaStream_t abl_str
     abl_kernel_update_boid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_update_boid(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
-    if (abl_t >= A.n) return;
-    const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
-    const int abl_r = A.replica[abl_i];
-    const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
-    abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
-    abl_K.self = abl_i;
-    abl_K.removed = 0;
-    abl_K.added = 0;
-    abl_K.child_cols = nullptr;
-    abl_K.near_col = -1;
-    Boid abl_in, abl_out;
-    abl_in.pos = ((const float3 *) A.in_cols[0])[abl_i];
-    abl_in.velocity = ((const float3 *) A.in_cols[1])[abl_i];
-    update_boid(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
-    ((float3 *) A.out_cols[0])[abl_i] = abl_out.pos;
-    ((float3 *) A.out_cols[1])[abl_i] = abl_out.velocity;
-}
-static int abl_launch_ens_update_boid(const abl_ens_launch *L, cudaStream_t abl_stream) {
-    const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
-    const long abl_grid = (L->n + abl_block - 1) / abl_block;
-    abl_kernel_ens_update_boid<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
-    return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
-}
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_update_boid(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.interaction_radius);
 }
+#endif
 
 
+#ifndef ABL_PERSIST
 static const abl_member_desc abl_members_Boid[] = {
     {"pos", ABL_T_FLOAT3, 3, 8, 1},
     {"velocity", ABL_T_FLOAT3, 3, 8, 0},
@@ -327,7 +306,7 @@ static const abl_step_desc abl_steps_ordered[] = {
     {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
 };
 extern const abl_model_desc abl_desc = {
-    "boids3d_mixed", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 13, abl_global_table, 3, abl_env_bounds, nullptr, 0, nullptr
+    "boids3d_mixed", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 13, abl_global_table, 3, abl_env_bounds, nullptr, 0, nullptr, nullptr
 };
 static void abl_check(int r, const char *what) {
     if (r != ABL_OK) {
@@ -398,14 +377,18 @@ static int abl_main() {
     save(&agents, agents_info, "boids.out", SAVE_JSON);
     return 0;
 }
+#else
+#endif
 
 }  // namespace abl_model_boids3d_mixed
 
+#ifndef ABL_PERSIST
 extern "C" const abl_model_desc *abl_model_desc_boids3d_mixed(void) {
     return &abl_model_boids3d_mixed::abl_desc;
 }
+#endif
 
-#ifdef ABL_STANDALONE_MAIN
+#if defined(ABL_STANDALONE_MAIN) && !defined(ABL_PERSIST)
 extern "C" const abl_model_desc *const abl_builtin_models[] = {
     &abl_model_boids3d_mixed::abl_desc, nullptr};
 int main() { return abl_model_boids3d_mixed::abl_main(); }

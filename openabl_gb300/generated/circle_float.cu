@@ -139,6 +139,7 @@ __device__ static void move_point(const abl_globals &abl_G, const abl_near_view 
     out->pos = clamp_1(abl_G, abl_R, new_pos, float2_fill(1), float2_fill((abl_G.W - 1.0)));
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_move_point {
     abl_globals G;
     long n;
@@ -206,10 +207,11 @@ static int abl_launch_move_point(const abl_step_launch *L, cudaStream_t abl_stre
     abl_kernel_move_point<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_move_point(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_move_point(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -223,13 +225,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -240,20 +242,29 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     move_point(abl_Gr, A.views[abl_r], abl_K, &abl_in, &abl_out);
     ((float2 *) A.out_cols[0])[abl_i] = abl_out.pos;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_move_point(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_move_point(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_move_point(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_move_point<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_move_point(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) ((2.0 * abl_G.r));
 }
+#endif
 
 
+#ifndef ABL_PERSIST
+extern "C" int abl_persist_launch_circle_float(const void *, int *, int, size_t, int *, cudaStream_t);
 static const abl_member_desc abl_members_Point[] = {
     {"pos", ABL_T_FLOAT2, 2, 4, 1},
 };
@@ -288,7 +299,7 @@ static const abl_step_desc abl_steps_ordered[] = {
     {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
 };
 extern const abl_model_desc abl_desc = {
-    "circle_float", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 8, abl_global_table, 2, abl_env_bounds, nullptr, 1, nullptr
+    "circle_float", 1, abl_agents, 1, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 8, abl_global_table, 2, abl_env_bounds, nullptr, 1, nullptr, abl_persist_launch_circle_float
 };
 static void abl_check(int r, const char *what) {
     if (r != ABL_OK) {
@@ -353,14 +364,31 @@ static int abl_main() {
     save(&agents, agents_info, "points.json", SAVE_JSON);
     return 0;
 }
+#else
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_persist(const abl::persist_prog *abl_P, int *abl_err) {
+    abl::persist_run(abl_P, abl_err, [&](const abl_ens_launch &abl_L, long abl_vb, long abl_ts) {
+        switch (abl_L.step_index) {
+            case 0: abl_ens_body_move_point(abl_L, abl_vb, abl_ts); break;
+            default: break;
+        }
+    });
+}
+#endif
 
 }  // namespace abl_model_circle_float
 
+#ifdef ABL_PERSIST
+extern "C" int abl_persist_launch_circle_float(const void *abl_prog, int *abl_err, int abl_block, size_t abl_smem, int *abl_grid, cudaStream_t abl_stream) {
+    return abl::persist_launch((const void *) abl_model_circle_float::abl_kernel_ens_persist, abl_prog, abl_err, abl_block, abl_smem, abl_grid, abl_stream);
+}
+#endif
+#ifndef ABL_PERSIST
 extern "C" const abl_model_desc *abl_model_desc_circle_float(void) {
     return &abl_model_circle_float::abl_desc;
 }
+#endif
 
-#ifdef ABL_STANDALONE_MAIN
+#if defined(ABL_STANDALONE_MAIN) && !defined(ABL_PERSIST)
 extern "C" const abl_model_desc *const abl_builtin_models[] = {
     &abl_model_circle_float::abl_desc, nullptr};
 int main() { return abl_model_circle_float::abl_main(); }

@@ -273,6 +273,7 @@ __device__ static void cycle(const abl_globals &abl_G, const abl_near_view &abl_
     }
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_cycle {
     abl_globals G;
     long n;
@@ -376,6 +377,7 @@ static int abl_launch_cycle(const abl_step_launch *L, cudaStream_t abl_stream) {
     abl_kernel_cycle<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
 
 __device__ static void differentiate(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Keratinocyte* in, Keratinocyte* out) {
     abl::rng &abl_R = abl_K.R;
@@ -457,6 +459,7 @@ __device__ static void differentiate(const abl_globals &abl_G, const abl_near_vi
     }
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_differentiate {
     abl_globals G;
     long n;
@@ -573,10 +576,11 @@ static int abl_launch_differentiate(const abl_step_launch *L, cudaStream_t abl_s
     abl_kernel_differentiate<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_differentiate(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_differentiate(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -590,13 +594,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<3>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -644,18 +648,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((double *) A.out_cols[11])[abl_i] = abl_out.dir;
     ((double *) A.out_cols[12])[abl_i] = abl_out.movement;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_differentiate(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_differentiate(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_differentiate(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_differentiate<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_differentiate(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (((double) (125.0)));
 }
+#endif
 
 __device__ static void death_signal(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Keratinocyte* in, Keratinocyte* out) {
     abl::rng &abl_R = abl_K.R;
@@ -699,6 +710,7 @@ __device__ static void death_signal(const abl_globals &abl_G, const abl_near_vie
     }
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_death_signal {
     abl_globals G;
     long n;
@@ -801,14 +813,15 @@ static int abl_launch_death_signal(const abl_step_launch *L, cudaStream_t abl_st
     abl_kernel_death_signal<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_death_signal(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+#endif
+__device__ __forceinline__ void abl_ens_body_death_signal(const abl_ens_launch &A, long abl_vb, long abl_ts) {
+    const long abl_t = abl_vb * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -856,18 +869,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((double *) A.out_cols[11])[abl_i] = abl_out.dir;
     ((double *) A.out_cols[12])[abl_i] = abl_out.movement;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_death_signal(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_death_signal(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_death_signal(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_death_signal<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_death_signal(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) ((abl_G.K_WIDTH + abl_G.FORCE_IRADIUS));
 }
+#endif
 
 __device__ static void migrate(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Keratinocyte* in, Keratinocyte* out) {
     abl::rng &abl_R = abl_K.R;
@@ -947,6 +967,7 @@ __device__ static void migrate(const abl_globals &abl_G, const abl_near_view &ab
     out->dir = dir1;
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_migrate {
     abl_globals G;
     long n;
@@ -1063,10 +1084,11 @@ static int abl_launch_migrate(const abl_step_launch *L, cudaStream_t abl_stream)
     abl_kernel_migrate<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_migrate(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_migrate(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -1080,13 +1102,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<3>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1134,18 +1156,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((double *) A.out_cols[11])[abl_i] = abl_out.dir;
     ((double *) A.out_cols[12])[abl_i] = abl_out.movement;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_migrate(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_migrate(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_migrate(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_migrate<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_migrate(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.K_WIDTH);
 }
+#endif
 
 __device__ static void resolve_forces(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Keratinocyte* in, Keratinocyte* out) {
     abl::rng &abl_R = abl_K.R;
@@ -1225,6 +1254,7 @@ __device__ static void resolve_forces(const abl_globals &abl_G, const abl_near_v
     out->pos = new_pos;
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_resolve_forces {
     abl_globals G;
     long n;
@@ -1341,10 +1371,11 @@ static int abl_launch_resolve_forces(const abl_step_launch *L, cudaStream_t abl_
     abl_kernel_resolve_forces<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_resolve_forces(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_resolve_forces(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -1358,13 +1389,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<3>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1412,18 +1443,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((double *) A.out_cols[11])[abl_i] = abl_out.dir;
     ((double *) A.out_cols[12])[abl_i] = abl_out.movement;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_resolve_forces(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_resolve_forces(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_resolve_forces(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_resolve_forces<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_resolve_forces(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) ((abl_G.K_WIDTH + abl_G.FORCE_IRADIUS));
 }
+#endif
 
 static int abl_seq_gather_stats(abl_ctx *abl_C, const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
@@ -1440,6 +1478,7 @@ static int abl_seq_gather_stats(abl_ctx *abl_C, const void *abl_gp) {
     return ABL_OK;
 }
 
+#ifndef ABL_PERSIST
 static const abl_member_desc abl_members_Keratinocyte[] = {
     {"type", ABL_T_INT, 1, 4, 0},
     {"pos", ABL_T_FLOAT3, 3, 8, 1},
@@ -1504,7 +1543,7 @@ static const abl_step_desc abl_steps_ordered[] = {
     {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
 };
 extern const abl_model_desc abl_desc = {
-    "keratinocyte", 1, abl_agents, 5, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 18, abl_global_table, 3, abl_env_bounds, nullptr, 0, abl_seq_gather_stats
+    "keratinocyte", 1, abl_agents, 5, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 18, abl_global_table, 3, abl_env_bounds, nullptr, 0, abl_seq_gather_stats, nullptr
 };
 static void abl_check(int r, const char *what) {
     if (r != ABL_OK) {
@@ -1640,14 +1679,18 @@ static int abl_main() {
     abl_simulate(abl_G.num_timesteps);
     return 0;
 }
+#else
+#endif
 
 }  // namespace abl_model_keratinocyte
 
+#ifndef ABL_PERSIST
 extern "C" const abl_model_desc *abl_model_desc_keratinocyte(void) {
     return &abl_model_keratinocyte::abl_desc;
 }
+#endif
 
-#ifdef ABL_STANDALONE_MAIN
+#if defined(ABL_STANDALONE_MAIN) && !defined(ABL_PERSIST)
 extern "C" const abl_model_desc *const abl_builtin_models[] = {
     &abl_model_keratinocyte::abl_desc, nullptr};
 int main() { return abl_model_keratinocyte::abl_main(); }

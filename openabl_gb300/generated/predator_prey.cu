@@ -247,6 +247,7 @@ __device__ static void prey_avoid_pred(const abl_globals &abl_G, const abl_near_
     out->steer = avoid_velocity;
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_prey_avoid_pred {
     abl_globals G;
     long n;
@@ -327,10 +328,11 @@ static int abl_launch_prey_avoid_pred(const abl_step_launch *L, cudaStream_t abl
     abl_kernel_prey_avoid_pred<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_prey_avoid_pred(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_prey_avoid_pred(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -344,13 +346,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -371,18 +373,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
     ((int *) A.out_cols[3])[abl_i] = abl_out.life;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_prey_avoid_pred(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_prey_avoid_pred(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_prey_avoid_pred(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_prey_avoid_pred<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_prey_avoid_pred(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.PRED_PREY_INTERACTION_RADIUS);
 }
+#endif
 
 __device__ static void prey_flock(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Prey* in, Prey* out) {
     abl::rng &abl_R = abl_K.R;
@@ -439,6 +448,7 @@ __device__ static void prey_flock(const abl_globals &abl_G, const abl_near_view 
     out->steer = float2_add(float2_add(in->steer, group_velocity), avoid_velocity);
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_prey_flock {
     abl_globals G;
     long n;
@@ -519,10 +529,11 @@ static int abl_launch_prey_flock(const abl_step_launch *L, cudaStream_t abl_stre
     abl_kernel_prey_flock<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_prey_flock(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_prey_flock(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -536,13 +547,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -563,18 +574,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
     ((int *) A.out_cols[3])[abl_i] = abl_out.life;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_prey_flock(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_prey_flock(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_prey_flock(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_prey_flock<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_prey_flock(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.PREY_GROUP_COHESION_RADIUS);
 }
+#endif
 
 __device__ static void prey_move(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Prey* in, Prey* out) {
     abl::rng &abl_R = abl_K.R;
@@ -592,6 +610,7 @@ __device__ static void prey_move(const abl_globals &abl_G, const abl_near_view &
     out->life = (in->life - 1);
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_prey_move {
     abl_globals G;
     long n;
@@ -658,14 +677,15 @@ static int abl_launch_prey_move(const abl_step_launch *L, cudaStream_t abl_strea
     abl_kernel_prey_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_prey_move(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+#endif
+__device__ __forceinline__ void abl_ens_body_prey_move(const abl_ens_launch &A, long abl_vb, long abl_ts) {
+    const long abl_t = abl_vb * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -686,12 +706,17 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
     ((int *) A.out_cols[3])[abl_i] = abl_out.life;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_prey_move(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_prey_move(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_prey_move(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_prey_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
 
 __device__ static void prey_eaten(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Prey* in, Prey* out) {
     abl::rng &abl_R = abl_K.R;
@@ -730,6 +755,7 @@ __device__ static void prey_eaten(const abl_globals &abl_G, const abl_near_view 
     if (eaten) abl_K.remove();
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_prey_eaten {
     abl_globals G;
     long n;
@@ -811,12 +837,15 @@ static int abl_launch_prey_eaten(const abl_step_launch *L, cudaStream_t abl_stre
     abl_kernel_prey_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_prey_eaten(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.PRED_KILL_DISTANCE);
 }
+#endif
 
 __device__ static void prey_eat_or_starve(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Prey* in, Prey* out) {
     abl::rng &abl_R = abl_K.R;
@@ -851,6 +880,7 @@ __device__ static void prey_eat_or_starve(const abl_globals &abl_G, const abl_ne
     if ((life < 1)) abl_K.remove();
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_prey_eat_or_starve {
     abl_globals G;
     long n;
@@ -918,12 +948,15 @@ static int abl_launch_prey_eat_or_starve(const abl_step_launch *L, cudaStream_t 
     abl_kernel_prey_eat_or_starve<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_prey_eat_or_starve(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.GRASS_EAT_DISTANCE);
 }
+#endif
 
 __device__ static void prey_reproduction(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Prey* in, Prey* out) {
     abl::rng &abl_R = abl_K.R;
@@ -934,6 +967,7 @@ __device__ static void prey_reproduction(const abl_globals &abl_G, const abl_nea
     }
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_prey_reproduction {
     abl_globals G;
     long n;
@@ -1001,6 +1035,7 @@ static int abl_launch_prey_reproduction(const abl_step_launch *L, cudaStream_t a
     abl_kernel_prey_reproduction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
 
 __device__ static void pred_follow_prey(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Predator* in, Predator* out) {
     abl::rng &abl_R = abl_K.R;
@@ -1046,6 +1081,7 @@ __device__ static void pred_follow_prey(const abl_globals &abl_G, const abl_near
     out->steer = agent_steer;
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_pred_follow_prey {
     abl_globals G;
     long n;
@@ -1126,10 +1162,11 @@ static int abl_launch_pred_follow_prey(const abl_step_launch *L, cudaStream_t ab
     abl_kernel_pred_follow_prey<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pred_follow_prey(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_pred_follow_prey(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -1143,13 +1180,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1170,18 +1207,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
     ((int *) A.out_cols[3])[abl_i] = abl_out.life;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pred_follow_prey(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_pred_follow_prey(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_pred_follow_prey(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_pred_follow_prey<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_pred_follow_prey(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.PRED_PREY_INTERACTION_RADIUS);
 }
+#endif
 
 __device__ static void pred_avoid(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Predator* in, Predator* out) {
     abl::rng &abl_R = abl_K.R;
@@ -1227,6 +1271,7 @@ __device__ static void pred_avoid(const abl_globals &abl_G, const abl_near_view 
     out->steer = float2_add(in->steer, avoid_velocity);
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_pred_avoid {
     abl_globals G;
     long n;
@@ -1307,10 +1352,11 @@ static int abl_launch_pred_avoid(const abl_step_launch *L, cudaStream_t abl_stre
     abl_kernel_pred_avoid<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pred_avoid(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_pred_avoid(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -1324,13 +1370,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1351,18 +1397,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
     ((int *) A.out_cols[3])[abl_i] = abl_out.life;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pred_avoid(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_pred_avoid(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_pred_avoid(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_pred_avoid<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_pred_avoid(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.SAME_SPECIES_AVOIDANCE_RADIUS);
 }
+#endif
 
 __device__ static void pred_move(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Predator* in, Predator* out) {
     abl::rng &abl_R = abl_K.R;
@@ -1382,6 +1435,7 @@ __device__ static void pred_move(const abl_globals &abl_G, const abl_near_view &
     out->life = (in->life - 1);
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_pred_move {
     abl_globals G;
     long n;
@@ -1448,14 +1502,15 @@ static int abl_launch_pred_move(const abl_step_launch *L, cudaStream_t abl_strea
     abl_kernel_pred_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pred_move(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+#endif
+__device__ __forceinline__ void abl_ens_body_pred_move(const abl_ens_launch &A, long abl_vb, long abl_ts) {
+    const long abl_t = abl_vb * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1476,12 +1531,17 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((float2 *) A.out_cols[2])[abl_i] = abl_out.steer;
     ((int *) A.out_cols[3])[abl_i] = abl_out.life;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_pred_move(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_pred_move(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_pred_move(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_pred_move<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
 
 __device__ static void pred_eat_or_starve(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Predator* in, Predator* out) {
     abl::rng &abl_R = abl_K.R;
@@ -1514,6 +1574,7 @@ __device__ static void pred_eat_or_starve(const abl_globals &abl_G, const abl_ne
     if ((pred_life < 1)) abl_K.remove();
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_pred_eat_or_starve {
     abl_globals G;
     long n;
@@ -1581,12 +1642,15 @@ static int abl_launch_pred_eat_or_starve(const abl_step_launch *L, cudaStream_t 
     abl_kernel_pred_eat_or_starve<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_pred_eat_or_starve(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.PRED_KILL_DISTANCE);
 }
+#endif
 
 __device__ static void pred_reproduction(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Predator* in, Predator* out) {
     abl::rng &abl_R = abl_K.R;
@@ -1597,6 +1661,7 @@ __device__ static void pred_reproduction(const abl_globals &abl_G, const abl_nea
     }
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_pred_reproduction {
     abl_globals G;
     long n;
@@ -1664,6 +1729,7 @@ static int abl_launch_pred_reproduction(const abl_step_launch *L, cudaStream_t a
     abl_kernel_pred_reproduction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
 
 __device__ static void grass_eaten(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Grass* in, Grass* out) {
     abl::rng &abl_R = abl_K.R;
@@ -1705,6 +1771,7 @@ __device__ static void grass_eaten(const abl_globals &abl_G, const abl_near_view
     }
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_grass_eaten {
     abl_globals G;
     long n;
@@ -1781,10 +1848,11 @@ static int abl_launch_grass_eaten(const abl_step_launch *L, cudaStream_t abl_str
     abl_kernel_grass_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_grass_eaten(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_grass_eaten(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -1798,13 +1866,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1822,18 +1890,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((int *) A.out_cols[1])[abl_i] = abl_out.dead_cycles;
     ((bool *) A.out_cols[2])[abl_i] = abl_out.avail;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_grass_eaten(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_grass_eaten(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_grass_eaten(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_grass_eaten<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_grass_eaten(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.GRASS_EAT_DISTANCE);
 }
+#endif
 
 __device__ static void grass_growth(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Grass* in, Grass* out) {
     abl::rng &abl_R = abl_K.R;
@@ -1846,6 +1921,7 @@ __device__ static void grass_growth(const abl_globals &abl_G, const abl_near_vie
     if ((!in->avail)) out->dead_cycles = (in->dead_cycles + 1);
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_grass_growth {
     abl_globals G;
     long n;
@@ -1908,14 +1984,15 @@ static int abl_launch_grass_growth(const abl_step_launch *L, cudaStream_t abl_st
     abl_kernel_grass_growth<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_grass_growth(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+#endif
+__device__ __forceinline__ void abl_ens_body_grass_growth(const abl_ens_launch &A, long abl_vb, long abl_ts) {
+    const long abl_t = abl_vb * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -1933,12 +2010,17 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((int *) A.out_cols[1])[abl_i] = abl_out.dead_cycles;
     ((bool *) A.out_cols[2])[abl_i] = abl_out.avail;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_grass_growth(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_grass_growth(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_grass_growth(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_grass_growth<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
 
 static int abl_seq_gather_stats(abl_ctx *abl_C, const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
@@ -1953,6 +2035,7 @@ static int abl_seq_gather_stats(abl_ctx *abl_C, const void *abl_gp) {
     return ABL_OK;
 }
 
+#ifndef ABL_PERSIST
 static const abl_member_desc abl_members_Predator[] = {
     {"pos", ABL_T_FLOAT2, 2, 8, 1},
     {"dir", ABL_T_FLOAT2, 2, 8, 0},
@@ -2039,7 +2122,7 @@ static const abl_step_desc abl_steps_ordered[] = {
     {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
 };
 extern const abl_model_desc abl_desc = {
-    "predator_prey", 3, abl_agents, 13, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 20, abl_global_table, 2, abl_env_bounds, nullptr, 0, abl_seq_gather_stats
+    "predator_prey", 3, abl_agents, 13, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 20, abl_global_table, 2, abl_env_bounds, nullptr, 0, abl_seq_gather_stats, nullptr
 };
 static void abl_check(int r, const char *what) {
     if (r != ABL_OK) {
@@ -2209,14 +2292,18 @@ static int abl_main() {
     save(&agents, agents_info, "agents.json", SAVE_JSON);
     return 0;
 }
+#else
+#endif
 
 }  // namespace abl_model_predator_prey
 
+#ifndef ABL_PERSIST
 extern "C" const abl_model_desc *abl_model_desc_predator_prey(void) {
     return &abl_model_predator_prey::abl_desc;
 }
+#endif
 
-#ifdef ABL_STANDALONE_MAIN
+#if defined(ABL_STANDALONE_MAIN) && !defined(ABL_PERSIST)
 extern "C" const abl_model_desc *const abl_builtin_models[] = {
     &abl_model_predator_prey::abl_desc, nullptr};
 int main() { return abl_model_predator_prey::abl_main(); }

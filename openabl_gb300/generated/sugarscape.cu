@@ -161,6 +161,7 @@ __device__ static void metabolise_and_growback(const abl_globals &abl_G, const a
     out->env_sugar_level = new_env_sugar_level;
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_metabolise_and_growback {
     abl_globals G;
     long n;
@@ -243,14 +244,15 @@ static int abl_launch_metabolise_and_growback(const abl_step_launch *L, cudaStre
     abl_kernel_metabolise_and_growback<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_metabolise_and_growback(const __grid_constant__ abl_ens_launch A) {
-    const long abl_t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+#endif
+__device__ __forceinline__ void abl_ens_body_metabolise_and_growback(const abl_ens_launch &A, long abl_vb, long abl_ts) {
+    const long abl_t = abl_vb * blockDim.x + threadIdx.x;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -276,12 +278,17 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((int *) A.out_cols[5])[abl_i] = abl_out.metabolism;
     ((int *) A.out_cols[6])[abl_i] = abl_out.env_sugar_level;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_metabolise_and_growback(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_metabolise_and_growback(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_metabolise_and_growback(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_metabolise_and_growback<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
 
 __device__ static void movement_request(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Agent* in, Agent* out) {
     abl::rng &abl_R = abl_K.R;
@@ -331,6 +338,7 @@ __device__ static void movement_request(const abl_globals &abl_G, const abl_near
     }
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_movement_request {
     abl_globals G;
     long n;
@@ -422,10 +430,11 @@ static int abl_launch_movement_request(const abl_step_launch *L, cudaStream_t ab
     abl_kernel_movement_request<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_movement_request(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_movement_request(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -439,13 +448,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -466,18 +475,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((float2 *) A.out_cols[1])[abl_i] = abl_out.target_pos;
     ((int *) A.out_cols[3])[abl_i] = abl_out.state;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_movement_request(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_movement_request(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_movement_request(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_movement_request<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_movement_request(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.radius);
 }
+#endif
 
 __device__ static void movement_response(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Agent* in, Agent* out) {
     abl::rng &abl_R = abl_K.R;
@@ -537,6 +553,7 @@ __device__ static void movement_response(const abl_globals &abl_G, const abl_nea
     }
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_movement_response {
     abl_globals G;
     long n;
@@ -632,10 +649,11 @@ static int abl_launch_movement_response(const abl_step_launch *L, cudaStream_t a
     abl_kernel_movement_response<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_movement_response(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_movement_response(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -649,13 +667,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -680,18 +698,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((int *) A.out_cols[4])[abl_i] = abl_out.sugar_level;
     ((int *) A.out_cols[5])[abl_i] = abl_out.metabolism;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_movement_response(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_movement_response(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_movement_response(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_movement_response<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_movement_response(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.radius);
 }
+#endif
 
 __device__ static void movement_transaction(const abl_globals &abl_G, const abl_near_view &abl_NB, abl::step_ctx &abl_K, Agent* in, Agent* out) {
     abl::rng &abl_R = abl_K.R;
@@ -737,6 +762,7 @@ __device__ static void movement_transaction(const abl_globals &abl_G, const abl_
     }
 }
 
+#ifndef ABL_PERSIST
 struct abl_kargs_movement_transaction {
     abl_globals G;
     long n;
@@ -832,10 +858,11 @@ static int abl_launch_movement_transaction(const abl_step_launch *L, cudaStream_
     abl_kernel_movement_transaction<<<abl_grid, abl_block, L->smem, abl_stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_movement_transaction(const __grid_constant__ abl_ens_launch A) {
+#endif
+__device__ __forceinline__ void abl_ens_body_movement_transaction(const abl_ens_launch &A, long abl_vb, long abl_ts) {
     int abl_j;
     {
-        const long abl_t1 = (long) blockIdx.x * blockDim.x + threadIdx.x;
+        const long abl_t1 = abl_vb * blockDim.x + threadIdx.x;
         const bool abl_has = abl_t1 < A.n;
         const long abl_i1 = abl_has ? (A.visit_order ? (long) A.visit_order[abl_t1] : abl_t1) : 0;
         const int abl_r1 = abl_has ? A.replica[abl_i1] : 0;
@@ -849,13 +876,13 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
         };
         abl_j = abl::presort_block<2>(abl_V1, abl_has, abl_q0, abl_x0);
     }
-    const long abl_t = (long) blockIdx.x * blockDim.x + abl_j;
+    const long abl_t = abl_vb * blockDim.x + abl_j;
     if (abl_t >= A.n) return;
     const long abl_i = A.visit_order ? (long) A.visit_order[abl_t] : abl_t;
     const int abl_r = A.replica[abl_i];
     const abl_globals &abl_Gr = ((const abl_globals *) A.globals)[abl_r];
     abl::step_ctx abl_K;
-    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) A.timestep);
+    abl_K.R.init(A.seeds[abl_r], (uint32_t) (abl_i - A.agent_base[abl_r]), (uint32_t) A.step_index, (uint64_t) abl_ts);
     abl_K.self = abl_i;
     abl_K.removed = 0;
     abl_K.added = 0;
@@ -880,18 +907,25 @@ __global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kerne
     ((int *) A.out_cols[4])[abl_i] = abl_out.sugar_level;
     ((int *) A.out_cols[5])[abl_i] = abl_out.metabolism;
 }
+#ifndef ABL_PERSIST
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_movement_transaction(const __grid_constant__ abl_ens_launch A) {
+    abl_ens_body_movement_transaction(A, blockIdx.x, A.timestep);
+}
 static int abl_launch_ens_movement_transaction(const abl_ens_launch *L, cudaStream_t abl_stream) {
     const int abl_block = L->block > 0 && L->block <= ABL_STEP_BLOCK ? L->block : ABL_STEP_BLOCK;
     const long abl_grid = (L->n + abl_block - 1) / abl_block;
     abl_kernel_ens_movement_transaction<<<abl_grid, abl_block, L->smem, abl_stream>>>(*L);
     return cudaGetLastError() == cudaSuccess ? ABL_OK : ABL_E_CUDA;
 }
+#endif
+#ifndef ABL_PERSIST
 static double abl_radius_movement_transaction(const void *abl_gp) {
     const abl_globals &abl_G = *(const abl_globals *) abl_gp;
     abl::rng abl_R;
     (void) abl_G; (void) abl_R;
     return (double) (abl_G.radius);
 }
+#endif
 
 __host__ __device__ static inline int calc_max_env_sugar_level(const abl_globals &abl_G, abl::rng &abl_R, int x, int y) {
     int gmax = abl_G.global_max_env_sugar_level;
@@ -904,6 +938,8 @@ __host__ __device__ static inline int calc_max_env_sugar_level(const abl_globals
     return max;
 }
 
+#ifndef ABL_PERSIST
+extern "C" int abl_persist_launch_sugarscape(const void *, int *, int, size_t, int *, cudaStream_t);
 static const abl_member_desc abl_members_Agent[] = {
     {"pos", ABL_T_FLOAT2, 2, 8, 1},
     {"target_pos", ABL_T_FLOAT2, 2, 8, 0},
@@ -960,7 +996,7 @@ static const abl_step_desc abl_steps_ordered[] = {
     {nullptr, 0, -1, 0, nullptr, 0u, 0u, nullptr, 0, -1, 0, nullptr, 0}
 };
 extern const abl_model_desc abl_desc = {
-    "sugarscape", 1, abl_agents, 4, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 17, abl_global_table, 2, abl_env_bounds, nullptr, 0, nullptr
+    "sugarscape", 1, abl_agents, 4, abl_steps_ordered, sizeof(abl_globals), &abl_globals_default, 17, abl_global_table, 2, abl_env_bounds, nullptr, 0, nullptr, abl_persist_launch_sugarscape
 };
 static void abl_check(int r, const char *what) {
     if (r != ABL_OK) {
@@ -1072,14 +1108,34 @@ static int abl_main() {
     abl_simulate(abl_G.num_timesteps);
     return 0;
 }
+#else
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_persist(const abl::persist_prog *abl_P, int *abl_err) {
+    abl::persist_run(abl_P, abl_err, [&](const abl_ens_launch &abl_L, long abl_vb, long abl_ts) {
+        switch (abl_L.step_index) {
+            case 0: abl_ens_body_metabolise_and_growback(abl_L, abl_vb, abl_ts); break;
+            case 1: abl_ens_body_movement_request(abl_L, abl_vb, abl_ts); break;
+            case 2: abl_ens_body_movement_response(abl_L, abl_vb, abl_ts); break;
+            case 3: abl_ens_body_movement_transaction(abl_L, abl_vb, abl_ts); break;
+            default: break;
+        }
+    });
+}
+#endif
 
 }  // namespace abl_model_sugarscape
 
+#ifdef ABL_PERSIST
+extern "C" int abl_persist_launch_sugarscape(const void *abl_prog, int *abl_err, int abl_block, size_t abl_smem, int *abl_grid, cudaStream_t abl_stream) {
+    return abl::persist_launch((const void *) abl_model_sugarscape::abl_kernel_ens_persist, abl_prog, abl_err, abl_block, abl_smem, abl_grid, abl_stream);
+}
+#endif
+#ifndef ABL_PERSIST
 extern "C" const abl_model_desc *abl_model_desc_sugarscape(void) {
     return &abl_model_sugarscape::abl_desc;
 }
+#endif
 
-#ifdef ABL_STANDALONE_MAIN
+#if defined(ABL_STANDALONE_MAIN) && !defined(ABL_PERSIST)
 extern "C" const abl_model_desc *const abl_builtin_models[] = {
     &abl_model_sugarscape::abl_desc, nullptr};
 int main() { return abl_model_sugarscape::abl_main(); }

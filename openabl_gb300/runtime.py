@@ -431,6 +431,9 @@ class Ensemble:
                                             ctypes.POINTER(ctypes.c_int)]
         L.abl_ensemble_last_exec_time.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
         L.abl_ensemble_last_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_long)]
+        L.abl_ensemble_set_persistent.argtypes = [vp, ctypes.c_int]
+        L.abl_ensemble_persistent_blocks.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+        L.abl_diag_ensemble_barrier.argtypes = [vp, ctypes.c_double, ctypes.c_int]
         L.abl_ensemble_destroy.argtypes = [vp]
         self.model = model if isinstance(model, Model) else Model(model)
         self.replicas = len(globals_list)
@@ -513,6 +516,25 @@ class Ensemble:
         c = ctypes.c_long()
         _check(_load().abl_ensemble_last_launch_count(self.e, ctypes.byref(c)), "launches")
         return c.value
+
+    def set_persistent(self, enable=True):
+        """Every timestep of a run in one cooperative launch (grid barriers
+        between the phases); results do not depend on it."""
+        _check(_load().abl_ensemble_set_persistent(self.e, int(bool(enable))),
+               "abl_ensemble_set_persistent")
+
+    def persistent_blocks(self):
+        c = ctypes.c_int()
+        _check(_load().abl_ensemble_persistent_blocks(self.e, ctypes.byref(c)),
+               "abl_ensemble_persistent_blocks")
+        return c.value
+
+    def inject_barrier_failure(self, limit_seconds, extra_arrivals):
+        """Failure injection (abl_diag_ensemble_barrier): barrier waits give up
+        after limit_seconds; with extra_arrivals=1 no barrier completes."""
+        _check(_load().abl_diag_ensemble_barrier(self.e, float(limit_seconds),
+                                                 int(extra_arrivals)),
+               "abl_diag_ensemble_barrier")
 
     def close(self):
         if self.e:

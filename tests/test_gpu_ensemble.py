@@ -78,3 +78,133 @@ def test_block_tiling_keeps_results(tiling):
     with pytest.raises(o.AblError):
         ens.set_tiling(100)
     ens.close()
+
+
+def _prefix_replicas(config, sizes):
+    """Replicas cut from a golden case's initial state: the first n agents,
+    for each n in sizes, all with the case's globals."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from golden_io import load_case
+    meta, st = load_case(config)
+    model, g = o.globals_for_config(config)
+    tname = model.agent_types[0][0]
+    states = [{k: np.ascontiguousarray(v[:n]) for k, v in st.items()} for n in sizes]
+    return model, [g] * len(sizes), tname, states
+
+
+@pytest.mark.parametrize("config,sizes", [
+    ("circle_4000", [4000, 1500, 700, 2500]),          # 2D ordered: row lists
+    ("circle3d_4000", [4000, 900, 2600]),              # 3D ordered: three list levels
+    ("game_of_life_64", [4096, 2048, 1000]),           # order-free loop: no lists
+    ("boids3d_5000", [5000, 1200, 3100]),
+    ("sugarscape_10000", [10000, 4000]),               # members kept from two swaps before
+])
+def test_persistent_run_equals_separate_contexts(config, sizes):
+    """One cooperative launch for all timesteps of every replica gives each
+    replica the bits of its own context, over an odd number of timesteps (the
+    program alternates two buffer sets) and in two runs in a row."""
+    model, gl, tname, states = _prefix_replicas(config, sizes)
+    ens = o.Ensemble(model, gl, seeds=list(range(len(gl))))
+    ens.set_persistent(True)
+    ens.upload(tname, states)
+    ens.run(5)
+    assert ens.last_launch_count() == 1
+    assert ens.persistent_blocks() >= 152
+    ens.run(2)
+    got = ens.download(tname)
+    for r in range(len(gl)):
+        sim = o.Simulation(model, gl[r])
+        sim.set_seed(r)
+        sim.upload(tname, states[r])
+        sim.run(7)
+        want = sim.download(tname)
+        sim.close()
+        for k in want:
+            assert np.array_equal(got[r][k], want[k]), (config, r, k)
+    ens.close()
+
+
+@pytest.mark.parametrize("model_name,config", [("boids2d", "boids2d_4096"),
+                                                ("boids2d_float", "boids2d_float_4096")])
+def test_persistent_boids_equal_per_phase_launches(model_name, config):
+    """The boids ensemble of uneven replicas: persistent run == per-phase
+    graph replay, replica by replica, after an autotune on the persistent
+    path; a 200-timestep run is one launch."""
+    model, base = o.globals_for_config(config)
+    gl, states, seeds = workloads.boids2d_ensemble(model, base, replicas=10, n_min=300,
+                                                   n_max=6000, seed=11)
+    fd = np.float32 if model.float_bytes == 4 else np.float64
+    states = [{k: v.astype(fd) for k, v in s.items()} for s in states]
+    a = o.Ensemble(model, gl, seeds=seeds)
+    a.set_persistent(True)
+    a.upload("Boid", states)
+    a.autotune(2)
+    a.upload("Boid", states)
+    a.run(200)
+    assert a.last_launch_count() == 1
+    b = o.Ensemble(model, gl, seeds=seeds)
+    b.upload("Boid", states)
+    b.run(200)
+    for r, (ra, rb) in enumerate(zip(a.download("Boid"), b.download("Boid"))):
+        for k in ra:
+            assert np.array_equal(ra[k], rb[k]), (r, k)
+    a.close()
+    b.close()
+
+
+def test_persistent_random_steps_equal_per_phase_launches():
+    """random() in a step is keyed by the timestep, which the persistent
+    kernel counts itself: boids2d_flockers gives the bits of the (eager)
+    per-phase path."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from golden_io import load_case
+    meta, st = load_case("boids2d_flockers_1000")
+    model = o.Model("boids2d_flockers")
+    g = model.default_globals()
+    tname = model.agent_types[0][0]
+    states = [{k: np.ascontiguousarray(v[:n]) for k, v in st.items()} for n in (1000, 500, 300)]
+    gl = [g] * 3
+    a = o.Ensemble(model, gl, seeds=[5, 6, 7])
+    a.set_persistent(True)
+    a.upload(tname, states)
+    a.run(9)
+    b = o.Ensemble(model, gl, seeds=[5, 6, 7])
+    b.upload(tname, states)
+    b.run(9)
+    for ra, rb in zip(a.download(tname), b.download(tname)):
+        for k in ra:
+            assert np.array_equal(ra[k], rb[k]), k
+    a.close()
+    b.close()
+
+
+def test_persistent_barrier_wait_runs_out_and_context_stays_usable():
+    """A barrier that waits for one arrival more than the grid has (a flag
+    that nothing sets) gives up after its limit: the run returns
+    ABL_E_TIMEOUT, no kernel is left running, and the same ensemble then
+    computes the right bits."""
+    model, base = o.globals_for_config("boids2d_4096")
+    gl, states, seeds = workloads.boids2d_ensemble(model, base, replicas=4, n_min=500,
+                                                   n_max=3000, seed=2)
+    ens = o.Ensemble(model, gl, seeds=seeds)
+    ens.set_persistent(True)
+    ens.upload("Boid", states)
+    ens.inject_barrier_failure(0.2, 1)
+    with pytest.raises(o.AblError) as err:
+        ens.run(3)
+    assert err.value.code == -4
+    ens.inject_barrier_failure(0.0, 0)
+    ens.upload("Boid", states)
+    ens.run(3)
+    got = ens.download("Boid")
+    for r in range(len(gl)):
+        sim = o.Simulation(model, gl[r])
+        sim.upload("Boid", states[r])
+        sim.run(3)
+        want = sim.download("Boid")
+        sim.close()
+        for k in want:
+            assert np.array_equal(got[r][k], want[k]), (r, k)
+    ens.close()

@@ -31,6 +31,22 @@ NVCC = [shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc", "-gencode",
         "-diag-suppress", "177", "-DABL_STANDALONE_MAIN", "-I", CSRC, "-I", INC]
 
 
+def build_program(model, runtime_objects, tmp_path, defines=()):
+    """The two compilations of build.sh: the model file for its kernels, host
+    code and main(), and (models with an ensemble form) again with
+    ABL_PERSIST for the persistent ensemble kernel; then the link."""
+    src = os.path.join(GEN, model + ".cu")
+    objs = [str(tmp_path / (model + ".o"))]
+    subprocess.check_call(NVCC + list(defines) + ["-c", src, "-o", objs[0]])
+    with open(src) as f:
+        if "#ifdef ABL_PERSIST" in f.read():
+            objs.append(str(tmp_path / (model + ".persist.o")))
+            subprocess.check_call(NVCC + ["-DABL_PERSIST", "-c", src, "-o", objs[1]])
+    exe = str(tmp_path / "main")
+    subprocess.check_call(NVCC[:3] + objs + runtime_objects + ["-o", exe])
+    return exe
+
+
 @pytest.fixture(scope="module")
 def runtime_objects(tmp_path_factory):
     d = tmp_path_factory.mktemp("abl_program_runtime")
@@ -46,13 +62,10 @@ def runtime_objects(tmp_path_factory):
 @pytest.mark.parametrize("model", sorted(PROGRAMS))
 def test_generated_program_writes_the_reference_output(model, runtime_objects, tmp_path):
     want = PROGRAMS[model]
-    obj = str(tmp_path / (model + ".o"))
-    exe = str(tmp_path / "main")
     # Programs drawing random numbers in steps were recorded on one thread;
     # -DABL_SERIAL_RANDOM continues the host stream in the same order.
     serial = ["-DABL_SERIAL_RANDOM"] if want.get("serial_random") else []
-    subprocess.check_call(NVCC + serial + ["-c", os.path.join(GEN, model + ".cu"), "-o", obj])
-    subprocess.check_call(NVCC[:3] + [obj] + runtime_objects + ["-o", exe])
+    exe = build_program(model, runtime_objects, tmp_path, serial)
     run_dir = tmp_path / "run"
     run_dir.mkdir()
     subprocess.run([exe], cwd=run_dir, check=True, stdout=subprocess.DEVNULL, timeout=300)
@@ -74,10 +87,7 @@ def test_device_initialised_program_matches_the_oracle(runtime_objects, tmp_path
     import numpy as np
     import openabl_gb300 as o
     from oracle import oracle as O
-    obj = str(tmp_path / "devinit.o")
-    exe = str(tmp_path / "main")
-    subprocess.check_call(NVCC + ["-c", os.path.join(GEN, "boids2d_devinit.cu"), "-o", obj])
-    subprocess.check_call(NVCC[:3] + [obj] + runtime_objects + ["-o", exe])
+    exe = build_program("boids2d_devinit", runtime_objects, tmp_path)
     outs = []
     for k in range(2):
         run_dir = tmp_path / f"run{k}"
@@ -118,10 +128,7 @@ def run_program(exe, run_dir):
 @pytest.mark.gpu
 @pytest.mark.parametrize("model", sorted(UNPINNED))
 def test_programs_with_random_steps_repeat_exactly(model, runtime_objects, tmp_path):
-    obj = str(tmp_path / (model + ".o"))
-    exe = str(tmp_path / "main")
-    subprocess.check_call(NVCC + ["-c", os.path.join(GEN, model + ".cu"), "-o", obj])
-    subprocess.check_call(NVCC[:3] + [obj] + runtime_objects + ["-o", exe])
+    exe = build_program(model, runtime_objects, tmp_path)
     out = UNPINNED[model]
     texts = []
     for r in ("a", "b"):
