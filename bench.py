@@ -202,6 +202,9 @@ def measure_ensemble(args, o, W, np):
     pers = {"value": total * T / pers_s, "seconds": pers_s,
             "gpu_launches": pe.last_launch_count(), "blocks": pe.persistent_blocks(),
             "tuning": p_tuning,
+            # per phase of the first timesteps: assign, cell scan (2), scatter,
+            # sort, gather, list merge, step; block 0's clock at each barrier
+            "phase_ms_first": [round(x * 1e3, 4) for x in pe.phase_times(24)],
             "equal_to_per_phase_run": all(np.array_equal(a[k], b[k])
                                           for a, b in zip(pe.download("Boid"), final)
                                           for k in a)}

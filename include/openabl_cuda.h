@@ -245,6 +245,11 @@ int abl_ensemble_last_launch_count(abl_ensemble *e, long *launches);
 int abl_ensemble_set_persistent(abl_ensemble *e, int enable);
 /* Blocks of the last persistent launch (0 before the first). */
 int abl_ensemble_persistent_blocks(abl_ensemble *e, int *blocks);
+/* Durations of the first phases of the last persistent run, in order (the
+ * time between the ends of consecutive phases as block 0 saw them: the
+ * binning phases of the first timestep, its step functions, then the next
+ * timestep's): up to `cap` of them, *count set to how many. */
+int abl_ensemble_phase_times(abl_ensemble *e, double *seconds, int cap, int *count);
 int abl_ensemble_destroy(abl_ensemble *e);
 
 /* ---- serving: continuous batching of simulation jobs ----

@@ -1339,11 +1339,22 @@ bool CudaPrinter::ensembleModel() const {
 // cooperative launch (abl_persist.cuh).  step_index is the step's place in
 // simulate order, as the runtime numbers the model's steps.
 void CudaPrinter::printPersistentKernel() {
-  *this << "__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) "
+  // The binning phases are compiled for the dimension of the positions the
+  // near loops bin (0: types of both dimensions, chosen per binning).
+  int dim = -1;
+  for (const StepInfo &s : steps) {
+    if (!s.nearLoop) continue;
+    AST::AgentDeclaration *a = s.nearLoop->type->resolved.getAgentDecl();
+    int d = a->getPositionMember()->type->resolved == Type::VEC3 ? 3 : 2;
+    dim = dim < 0 || dim == d ? d : 0;
+  }
+  if (dim < 0) dim = 2;
+  *this << "__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_PERSIST_MIN_BLOCKS) "
            "abl_kernel_ens_persist(const abl::persist_prog *abl_P, int *abl_err) {"
         << indent << nl
-        << "abl::persist_run(abl_P, abl_err, [&](const abl_ens_launch &abl_L, long abl_vb, "
-           "long abl_ts) {" << indent << nl << "switch (abl_L.step_index) {" << indent;
+        << "abl::persist_run<abl_float, " << dim << ">(abl_P, abl_err, [&](const abl_ens_launch "
+           "&abl_L, long abl_vb, long abl_ts) {" << indent << nl
+        << "switch (abl_L.step_index) {" << indent;
   const auto &order = script.simStmt->stepFuncDecls;
   for (size_t k = 0; k < order.size(); k++) {
     *this << nl << "case " << (int) k << ": abl_ens_body_" << order[k]->name

@@ -57,32 +57,39 @@ __device__ __forceinline__ bool finite_bits(float x) {
 // ------------------------------------------------------------ binning
 
 // Grid of one replica of an ensemble: its cells are cell_base .. cell_base +
-// nx*ny*nz - 1 of the segmented grid.
+// nx*ny*nz - 1 of the segmented grid.  f32: the grid's rounding-error bound
+// allows cell coordinates in FP32 (flo, finv: lo and 1 / cell size in
+// float), as the runtime decides for single grids.
 struct EnsGrid {
   int nx, ny, nz, R;
+  int f32;
+  float flo[3], finv;
   double lo[3];
   double inv_cell;
   long cell_base;
 };
 
-// Assign of ensemble agent i: cell in its replica's grid (FP64 cell
-// coordinates); returns the agent's largest |coordinate| (0 for i >= n).
+// Assign of ensemble agent i: cell in its replica's grid; returns the
+// agent's largest |coordinate| (0 for i >= n).
 template <typename Real, int DIM>
 __device__ __forceinline__ float ens_bin_assign_item(long i, const Real *pos,
                                                      const int *replica_of, const EnsGrid *grids,
                                                      int *cell_of, int *cell_count,
                                                      int *local_rank, int *error) {
   float m = 0.0f;
-  const EnsGrid g = grids[replica_of[i]];
+  const EnsGrid &g = grids[replica_of[i]];
   const int dims[3] = {g.nx, g.ny, g.nz};
   int c[3] = {0, 0, 0};
   bool finite = true;
+  const bool f32 = g.f32 != 0;
 #pragma unroll
   for (int d = 0; d < DIM; d++) {
-    double x = (double) pos[DIM * i + d];
-    finite = finite && isfinite(x);
-    c[d] = abl::cell_coord(x, g.lo[d], g.inv_cell, dims[d]);
-    m = fmaxf(m, fabsf((float) x));
+    const Real xr = pos[DIM * i + d];
+    finite = finite && finite_bits(xr);
+    const float xf = (float) xr;
+    c[d] = f32 ? abl::cell_coord_f32(xf, g.flo[d], g.finv, dims[d])
+               : abl::cell_coord((double) xr, g.lo[d], g.inv_cell, dims[d]);
+    m = fmaxf(m, fabsf(xf));
   }
   if (!finite) atomicExch(error, ABL_E_NONFINITE);
   int cell = (int) (g.cell_base + ((long) c[2] * g.ny + c[1]) * g.nx + c[0]);

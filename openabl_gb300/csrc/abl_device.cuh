@@ -46,8 +46,10 @@
 // through the read-only (non-coherent) data path.  The persistent ensemble
 // kernel rewrites its grids between phases of one launch, where that path
 // could return lines cached before the rewrite, so its translation units are
-// compiled with ABL_PERSIST and use plain (coherent) loads.
-#ifdef ABL_PERSIST
+// compiled with ABL_PERSIST and use plain (coherent) loads.  ABL_PLAIN_LOADS
+// selects plain loads for every kernel (a build option for comparing the
+// two paths).
+#if defined(ABL_PERSIST) || defined(ABL_PLAIN_LOADS)
 #define ABL_LDG(p) (*(p))
 #else
 #define ABL_LDG(p) __ldg(p)

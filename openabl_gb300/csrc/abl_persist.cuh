@@ -30,9 +30,26 @@
 
 #include "abl_bin.cuh"
 
+// Resident blocks per SM the persistent kernel's register allocation must
+// allow (its step phase is the step kernel's body).
+// Five blocks of 128 threads leave 96 registers a thread: the kernel holds
+// its walk through the run beside the step body (measured on the 256-replica
+// FP32 boids2d ensemble: 1.93 s with six blocks and spills, 1.77 s with five).
+#ifndef ABL_PERSIST_MIN_BLOCKS
+#define ABL_PERSIST_MIN_BLOCKS 5
+#endif
+
 namespace abl {
 
 enum { kPersistBin = 0, kPersistStep = 1 };
+// Items a thread of the persistent kernel takes at a time in the gathering
+// phases, loads first: the binning phases run at the step phase's
+// occupancy, so each thread keeps more loads in flight than in the
+// per-phase kernels.
+#ifndef ABL_PERSIST_ILP
+#define ABL_PERSIST_ILP 4
+#endif
+constexpr int kPersistILP = ABL_PERSIST_ILP;
 constexpr int kPersistMaxOps = 8;     // ops (binnings + step functions) per timestep
 constexpr int kPersistMaxLevels = 3;  // list levels (3D ordered lists)
 
@@ -74,6 +91,9 @@ struct persist_sync {
   unsigned int gen;    // barrier generation
   int error;           // ABL_E_TIMEOUT once a wait gave up
   int pad;
+  // Virtual blocks of the step phases handed out so far (one counter for
+  // the whole run; each phase's share starts where the last one's ended).
+  unsigned long long work;
 };
 
 // A run: timesteps [0, timesteps) use ts[0] for the first one when
@@ -87,7 +107,11 @@ struct persist_prog {
   persist_sync *sync;
   unsigned long long limit_ns;  // longest wait at one barrier
   unsigned int extra_arrivals;  // arrivals a barrier waits for beyond the grid's blocks
-  int scan_chunk;               // ints per scan chunk: 8 per thread
+  int scan_chunk;               // ints per scan chunk
+  // Phase timestamps (globaltimer ns, NULL: none): block 0 records when
+  // each barrier completed, the first `stamp_cap` of them.
+  unsigned long long *stamps;
+  int stamp_cap;
 };
 
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
@@ -243,6 +267,34 @@ __device__ __forceinline__ long grid_thread() {
 }
 __device__ __forceinline__ long grid_threads() { return (long) gridDim.x * blockDim.x; }
 
+static_assert(sizeof(abl_ens_launch) % 8 == 0 && alignof(abl_ens_launch) == 8 &&
+                  sizeof(persist_bin) % 8 == 0 && alignof(persist_bin) == 8,
+              "op arguments are copied as 8-byte words");
+
+// Block-wide copy of `bytes` (a multiple of 8) from global to shared memory.
+__device__ __forceinline__ void copy_words(void *dst, const void *src, size_t bytes) {
+  for (int w = threadIdx.x; w < (int) (bytes / 8); w += blockDim.x)
+    ((unsigned long long *) dst)[w] = ((const unsigned long long *) src)[w];
+}
+
+// State of one block's walk through the run: the barrier's arrivals and
+// limit, and (block 0, thread 0) the phase timestamps.
+struct persist_walk {
+  const persist_prog &P;
+  unsigned int expected;
+  int *error;
+  int *stage;
+  int nstamps;
+
+  // Grid barrier; block 0 then records when the phase ended.
+  __device__ bool sync() {
+    if (!grid_barrier(P.sync, expected, P.limit_ns)) return false;
+    if (P.stamps && blockIdx.x == 0 && threadIdx.x == 0 && nstamps < P.stamp_cap)
+      P.stamps[nstamps++] = global_ns();
+    return true;
+  }
+};
+
 template <typename Real, int DIM>
 __device__ float persist_assign(const persist_bin &B, int *error) {
   float m = 0.0f;
@@ -254,11 +306,116 @@ __device__ float persist_assign(const persist_bin &B, int *error) {
   return m;
 }
 
+// Slot-ordered copies (as gather_item), kPersistILP slots at a time.
 template <typename Real, int DIM>
 __device__ void persist_gather(const persist_bin &B) {
+  constexpr int U = kPersistILP;
   const Real *pos = (const Real *) B.pos;
-  for (long s = grid_thread(); s < B.n; s += grid_threads())
-    ablbin::gather_item<Real, DIM>(s, B.order, pos, B.posf, B.gather);
+  const ablbin::GatherArgs &g = B.gather;
+  const long T = grid_threads();
+  for (long s0 = grid_thread(); s0 < B.n; s0 += U * T) {
+    long idx[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) idx[u] = s0 + u * T < B.n ? B.order[s0 + u * T] : -1;
+    if (B.posf) {
+      Real p[U][DIM];
+#pragma unroll
+      for (int u = 0; u < U; u++)
+#pragma unroll
+        for (int d = 0; d < DIM; d++) p[u][d] = idx[u] >= 0 ? pos[DIM * idx[u] + d] : Real(0);
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (idx[u] >= 0)
+#pragma unroll
+          for (int d = 0; d < DIM; d++) B.posf[DIM * (s0 + u * T) + d] = (float) p[u][d];
+    }
+    for (int k = 0; k < g.nmem; k++) {
+      const int b = g.bytes[k];
+      if ((b & 7) == 0) {
+        for (int w = 0; w < b / 8; w++) {
+          uint64_t v[U];
+#pragma unroll
+          for (int u = 0; u < U; u++)
+            if (idx[u] >= 0) v[u] = ((const uint64_t *) g.src[k])[(b / 8) * idx[u] + w];
+#pragma unroll
+          for (int u = 0; u < U; u++)
+            if (idx[u] >= 0) ((uint64_t *) g.dst[k])[(b / 8) * (s0 + u * T) + w] = v[u];
+        }
+      } else if ((b & 3) == 0) {
+        for (int w = 0; w < b / 4; w++) {
+          uint32_t v[U];
+#pragma unroll
+          for (int u = 0; u < U; u++)
+            if (idx[u] >= 0) v[u] = ((const uint32_t *) g.src[k])[(b / 4) * idx[u] + w];
+#pragma unroll
+          for (int u = 0; u < U; u++)
+            if (idx[u] >= 0) ((uint32_t *) g.dst[k])[(b / 4) * (s0 + u * T) + w] = v[u];
+        }
+      } else {
+        for (int w = 0; w < b; w++) {
+          uint8_t v[U];
+#pragma unroll
+          for (int u = 0; u < U; u++)
+            if (idx[u] >= 0) v[u] = ((const uint8_t *) g.src[k])[b * idx[u] + w];
+#pragma unroll
+          for (int u = 0; u < U; u++)
+            if (idx[u] >= 0) ((uint8_t *) g.dst[k])[b * (s0 + u * T) + w] = v[u];
+        }
+      }
+    }
+  }
+}
+
+// Counting-sort placement (as bin_scatter_item), kPersistILP agents at a
+// time; the cell counts, consumed by the scan, are reset for the next
+// binning in the same pass.
+__device__ inline void persist_scatter(const persist_bin &B) {
+  constexpr int U = kPersistILP;
+  const long T = grid_threads();
+  for (long i0 = grid_thread(); i0 < B.n; i0 += U * T) {
+    int cell[U], rank[U], start[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const long i = i0 + u * T;
+      cell[u] = i < B.n ? B.cell_of[i] : 0;
+      rank[u] = i < B.n ? B.local_rank[i] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) start[u] = i0 + u * T < B.n ? B.cell_start[cell[u]] : 0;
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (i0 + u * T < B.n) B.order[start[u] + rank[u]] = (int) (i0 + u * T);
+  }
+  for (long c = grid_thread(); c < B.ncells; c += T) B.cell_count[c] = 0;
+}
+
+// DIM 2 or 3 with Real the position's scalar: the model's one kind of
+// binned position, fixed when the kernel is generated.  DIM 0: chosen per
+// binning from the program.
+template <typename Real, int DIM>
+__device__ __forceinline__ float assign_any(const persist_bin &B, int *error) {
+  if constexpr (DIM != 0) {
+    return persist_assign<Real, DIM>(B, error);
+  } else {
+    if (B.pos_double) return B.dim == 2 ? persist_assign<double, 2>(B, error)
+                                        : persist_assign<double, 3>(B, error);
+    return B.dim == 2 ? persist_assign<float, 2>(B, error) : persist_assign<float, 3>(B, error);
+  }
+}
+
+template <typename Real, int DIM>
+__device__ __forceinline__ void gather_any(const persist_bin &B) {
+  if constexpr (DIM != 0) {
+    persist_gather<Real, DIM>(B);
+  } else {
+    if (B.pos_double) {
+      if (B.dim == 2) persist_gather<double, 2>(B);
+      else persist_gather<double, 3>(B);
+    } else {
+      if (B.dim == 2) persist_gather<float, 2>(B);
+      else persist_gather<float, 3>(B);
+    }
+  }
 }
 
 template <int AXIS>
@@ -275,7 +432,7 @@ __device__ void persist_merge(const persist_bin &B, const ablbin::EnsGeom &geo,
                               const ablbin::SepSrc &S, int *stage) {
   const int lane = threadIdx.x & 31;
   const long warp = grid_thread() >> 5, warps = grid_threads() >> 5;
-  if (AXIS == 0) {
+  if constexpr (AXIS == 0) {
     for (long t = grid_thread(); t < B.ncells; t += grid_threads())
       ablbin::sep_merge_item<ablbin::EnsGeom, 0, true>(t, geo, S, B.dst_off[0], B.dst_elem[0],
                                                       B.dst_slot[0]);
@@ -293,82 +450,67 @@ __device__ void persist_merge(const persist_bin &B, const ablbin::EnsGeom &geo,
   }
 }
 
-template <int AXIS>
-__device__ void persist_count_level(const persist_bin &B, const ablbin::EnsGeom &geo, int a) {
-  persist_count<AXIS>(B, geo, B.dst_off[a - 1]);
-}
-
+// Counts of list level a (sources: the cells' runs at level 0, else level
+// a - 1's lists).  Axes beyond the positions' dimension never occur.
+template <int DIM>
 __device__ inline void persist_count_dispatch(const persist_bin &B, const ablbin::EnsGeom &geo,
                                               int a) {
   if (a == 0) persist_count<0>(B, geo, B.cell_start);
-  else if (a == 1) persist_count_level<1>(B, geo, 1);
-  else persist_count_level<2>(B, geo, 2);
+  else if (a == 1) persist_count<1>(B, geo, B.dst_off[0]);
+  else if (DIM != 2) persist_count<2>(B, geo, B.dst_off[1]);
 }
 
+template <int DIM>
 __device__ inline void persist_merge_dispatch(const persist_bin &B, const ablbin::EnsGeom &geo,
                                               int a, int *stage) {
-  ablbin::SepSrc S;
   if (a == 0) {
-    S = ablbin::SepSrc{B.cell_start, B.order, B.posf, B.dim, nullptr};
-    persist_merge<0>(B, geo, S, stage);
-  } else {
-    S = ablbin::SepSrc{B.dst_off[a - 1], nullptr, nullptr, B.dim, B.dst_elem[a - 1]};
-    if (a == 1) persist_merge<1>(B, geo, S, stage);
-    else persist_merge<2>(B, geo, S, stage);
+    persist_merge<0>(B, geo, ablbin::SepSrc{B.cell_start, B.order, B.posf, B.dim, nullptr},
+                     stage);
+    return;
   }
+  const ablbin::SepSrc S{B.dst_off[a - 1], nullptr, nullptr, B.dim, B.dst_elem[a - 1]};
+  if (a == 1) persist_merge<1>(B, geo, S, stage);
+  else if (DIM != 2) persist_merge<2>(B, geo, S, stage);
 }
 
 // The binning of one type: returns false when a barrier gave up.
-__device__ inline bool persist_binning(const persist_prog &P, const persist_bin &B,
-                                       unsigned int expected, int *error, int *stage) {
-  persist_sync *sy = P.sync;
-  const unsigned long long lim = P.limit_ns;
-  const int chunk = P.scan_chunk;
+template <typename Real, int DIM>
+__device__ inline bool persist_binning(persist_walk &W, const persist_bin &B) {
+  const int chunk = W.P.scan_chunk;
   // assign
-  float m;
-  if (B.pos_double) m = B.dim == 2 ? persist_assign<double, 2>(B, error)
-                                   : persist_assign<double, 3>(B, error);
-  else m = B.dim == 2 ? persist_assign<float, 2>(B, error) : persist_assign<float, 3>(B, error);
+  const float m = assign_any<Real, DIM>(B, W.error);
   ablbin::fold_amax(m, B.amax_acc);
-  if (!grid_barrier(sy, expected, lim)) return false;
+  if (!W.sync()) return false;
   scan_phase_a(B.cell_count, B.ncells, chunk, B.scan_incl, B.scan_sums);
-  if (!grid_barrier(sy, expected, lim)) return false;
+  if (!W.sync()) return false;
   scan_phase_c(B.scan_incl, B.scan_sums, B.ncells, chunk, B.cell_start);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *B.amax = *B.amax_acc;
     *B.amax_acc = 0.0f;
   }
-  if (!grid_barrier(sy, expected, lim)) return false;
+  if (!W.sync()) return false;
   // scatter; the counts of list level 0 need only the cell starts; the cell
   // counts are consumed, so they are reset for the next binning here
   const ablbin::EnsGeom geo{B.cell_replica, B.grids};
-  for (long i = grid_thread(); i < B.n; i += grid_threads())
-    ablbin::bin_scatter_item(i, B.cell_of, B.local_rank, B.cell_start, B.order);
-  for (long c = grid_thread(); c < B.ncells; c += grid_threads()) B.cell_count[c] = 0;
-  if (B.levels > 0) persist_count_dispatch(B, geo, 0);
-  if (!grid_barrier(sy, expected, lim)) return false;
+  persist_scatter(B);
+  if (B.levels > 0) persist_count_dispatch<DIM>(B, geo, 0);
+  if (!W.sync()) return false;
   for (long c = grid_thread(); c < B.ncells; c += grid_threads())
     ablbin::cell_sort_item(c, B.cell_start, B.order);
   if (B.levels > 0) scan_phase_a(B.cnt, B.ncells, chunk, B.scan_incl, B.scan_sums);
-  if (!grid_barrier(sy, expected, lim)) return false;
-  if (B.pos_double) {
-    if (B.dim == 2) persist_gather<double, 2>(B);
-    else persist_gather<double, 3>(B);
-  } else {
-    if (B.dim == 2) persist_gather<float, 2>(B);
-    else persist_gather<float, 3>(B);
-  }
+  if (!W.sync()) return false;
+  gather_any<Real, DIM>(B);
   if (B.levels > 0) scan_phase_c(B.scan_incl, B.scan_sums, B.ncells, chunk, B.dst_off[0]);
-  if (!grid_barrier(sy, expected, lim)) return false;
+  if (!W.sync()) return false;
   for (int a = 0; a < B.levels; a++) {
-    persist_merge_dispatch(B, geo, a, stage);
-    if (a + 1 < B.levels) persist_count_dispatch(B, geo, a + 1);
-    if (!grid_barrier(sy, expected, lim)) return false;
+    persist_merge_dispatch<DIM>(B, geo, a, W.stage);
+    if (a + 1 < B.levels) persist_count_dispatch<DIM>(B, geo, a + 1);
+    if (!W.sync()) return false;
     if (a + 1 < B.levels) {
       scan_phase_a(B.cnt, B.ncells, chunk, B.scan_incl, B.scan_sums);
-      if (!grid_barrier(sy, expected, lim)) return false;
+      if (!W.sync()) return false;
       scan_phase_c(B.scan_incl, B.scan_sums, B.ncells, chunk, B.dst_off[a + 1]);
-      if (!grid_barrier(sy, expected, lim)) return false;
+      if (!W.sync()) return false;
     }
   }
   return true;
@@ -377,13 +519,24 @@ __device__ inline bool persist_binning(const persist_prog &P, const persist_bin 
 // The whole run.  `body(L, vb, ts)` runs the step function L.step_index
 // for virtual block vb (the agents vb * blockDim.x ...) at timestep ts; it
 // is the generated ensemble step body.  `error` is the context's error word
-// (non-finite positions).
-template <typename Body>
+// (non-finite positions).  Real and DIM: see assign_any.
+template <typename Real, int DIM, typename Body>
 __device__ void persist_run(const persist_prog *Pp, int *error, Body &&body) {
   const persist_prog &P = *Pp;
   extern __shared__ int abl_presort_dyn[];
-  int *stage = abl_presort_dyn;  // list staging shares the step's dynamic shared memory
-  const unsigned int expected = gridDim.x + P.extra_arrivals;
+  // The step's launch block and the binning's arguments, copied to shared
+  // memory for each op: read at shared-memory latency.
+  __shared__ abl_ens_launch Ls;
+  __shared__ persist_bin Bs;
+  // List staging shares the step's dynamic shared memory.
+  persist_walk W{P, gridDim.x + P.extra_arrivals, error, abl_presort_dyn, 0};
+  // Step phases hand out virtual blocks dynamically, as the hardware hands
+  // out the blocks of a kernel: agents' neighbour counts vary, so a fixed
+  // share per block would finish unevenly.  Every block takes one block
+  // index past the end of each phase, so each phase's share starts
+  // nvb + gridDim.x after the last one's.
+  __shared__ long vb_next;
+  unsigned long long work_base = 0;
   // Cell counts and coordinate maxima start at zero.
   for (int k = 0; k < 3; k++) {
     const persist_timestep &T = P.ts[k];
@@ -394,7 +547,7 @@ __device__ void persist_run(const persist_prog *Pp, int *error, Body &&body) {
       if (grid_thread() == 0) *op.bin.amax_acc = 0.0f;
     }
   }
-  if (!grid_barrier(P.sync, expected, P.limit_ns)) return;
+  if (!W.sync()) return;
   for (long it = 0; it < P.timesteps; it++) {
     const int k = P.first_special ? (it == 0 ? 0 : 1 + (int) ((it - 1) & 1)) : (int) (it & 1);
     const persist_timestep &T = P.ts[k];
@@ -402,16 +555,24 @@ __device__ void persist_run(const persist_prog *Pp, int *error, Body &&body) {
     for (int o = 0; o < T.nops; o++) {
       const persist_op &op = T.ops[o];
       if (op.kind == kPersistBin) {
-        if (!persist_binning(P, op.bin, expected, error, stage)) return;
+        copy_words(&Bs, &op.bin, sizeof(persist_bin));
+        __syncthreads();
+        if (!persist_binning<Real, DIM>(W, Bs)) return;
         continue;
       }
-      const abl_ens_launch &L = op.step;
-      const long nvb = (L.n + blockDim.x - 1) / blockDim.x;
-      for (long vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
-        body(L, vb, ts);
+      copy_words(&Ls, &op.step, sizeof(abl_ens_launch));
+      __syncthreads();
+      const long nvb = (Ls.n + blockDim.x - 1) / blockDim.x;
+      for (;;) {
+        if (threadIdx.x == 0) vb_next = (long) (atomicAdd(&P.sync->work, 1ull) - work_base);
+        __syncthreads();
+        const long vb = vb_next;
+        if (vb >= nvb) break;  // uniform over the block
+        body(Ls, vb, ts);
         __syncthreads();  // shared memory is reused by the next virtual block
       }
-      if (!grid_barrier(P.sync, expected, P.limit_ns)) return;
+      work_base += (unsigned long long) nvb + gridDim.x;
+      if (!W.sync()) return;
     }
   }
 }

@@ -614,13 +614,69 @@ struct Phase {
   ~Phase() { nvtxRangePop(); }
 };
 
+// Device memory comes from the device's stream-ordered pool (cudaMallocAsync
+// on the context's stream).  cudaMalloc and cudaFree synchronise the whole
+// device, so contexts created and destroyed while others run (the job
+// server) would stall every running simulation; pool allocations and frees
+// wait only for the context's own stream.  The pool keeps freed memory for
+// reuse instead of returning it at each synchronisation.
+void keep_pool_memory() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  });
+}
+
+// Pinned words that check_error reads the device error word into, one per
+// context, from one pinned block allocated once: pinned allocations, like
+// device ones, synchronise the device.
+constexpr int kErrorSlots = 4096;
+std::mutex error_slot_mu;
+int *error_slots = nullptr;
+std::vector<int> free_error_slots;
+
+cudaError_t take_error_slot(int **slot) {
+  std::lock_guard<std::mutex> lock(error_slot_mu);
+  if (!error_slots) {
+    cudaError_t e = cudaHostAlloc((void **) &error_slots, sizeof(int) * kErrorSlots,
+                                  cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      error_slots = nullptr;
+      return e;
+    }
+    for (int k = kErrorSlots - 1; k >= 0; k--) free_error_slots.push_back(k);
+  }
+  if (free_error_slots.empty()) {
+    *slot = nullptr;  // check_error then reads the word with a plain copy
+    return cudaSuccess;
+  }
+  *slot = error_slots + free_error_slots.back();
+  free_error_slots.pop_back();
+  return cudaSuccess;
+}
+
+void release_error_slot(int *slot) {
+  if (!slot) return;
+  std::lock_guard<std::mutex> lock(error_slot_mu);
+  free_error_slots.push_back((int) (slot - error_slots));
+}
+
 int dev_alloc(abl_ctx *ctx, void **p, size_t bytes, std::vector<void *> *owner = nullptr) {
   if (bytes == 0) bytes = 16;
   bytes = (bytes + 255) & ~(size_t) 255;
   if (ctx->budget && ctx->used + bytes > ctx->budget) return ABL_E_BUDGET;
-  cudaError_t e = cudaMalloc(p, bytes);
+  keep_pool_memory();
+  // The block is in use on any stream once the context's stream has reached
+  // the allocation (host copies address it right away).
+  cudaError_t e = cudaMallocAsync(p, bytes, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
-    std::fprintf(stderr, "openabl-cuda: cudaMalloc(%zu) failed: %s\n", bytes,
+    std::fprintf(stderr, "openabl-cuda: cudaMallocAsync(%zu) failed: %s\n", bytes,
                  cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? ABL_E_BUDGET : ABL_E_CUDA;
   }
@@ -634,7 +690,7 @@ int dev_alloc(abl_ctx *ctx, void **p, size_t bytes, std::vector<void *> *owner =
 void dev_free(abl_ctx *ctx, void *p) {
   for (size_t k = 0; k < ctx->allocations.size(); k++) {
     if (ctx->allocations[k] == p) {
-      cudaFree(p);
+      cudaFreeAsync(p, ctx->stream);
       ctx->used -= ctx->sizes[k];
       ctx->allocations.erase(ctx->allocations.begin() + k);
       ctx->sizes.erase(ctx->sizes.begin() + k);
@@ -1988,7 +2044,7 @@ int abl_create(const abl_model_desc *model, size_t hbm_budget, abl_ctx **out) {
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ts0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ts1);
-  if (e == cudaSuccess) e = cudaHostAlloc(&ctx->error_host, sizeof(int), cudaHostAllocDefault);
+  if (e == cudaSuccess) e = take_error_slot(&ctx->error_host);
   if (e != cudaSuccess) {
     std::fprintf(stderr, "openabl-cuda: context setup failed: %s\n", cudaGetErrorString(e));
     delete ctx;
@@ -2533,8 +2589,9 @@ int abl_destroy(abl_ctx *ctx) {
   if (!ctx) return ABL_E_INVALID;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   drop_graph(ctx);
-  for (void *p : ctx->allocations) cudaFree(p);
-  if (ctx->error_host) cudaFreeHost(ctx->error_host);
+  for (void *p : ctx->allocations) cudaFreeAsync(p, ctx->stream);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  release_error_slot(ctx->error_host);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->ts0) cudaEventDestroy(ctx->ts0);
@@ -2880,6 +2937,7 @@ struct abl_ensemble {
   bool persistent = false;
   abl::persist_prog *d_prog = nullptr;
   abl::persist_sync *d_sync = nullptr;
+  unsigned long long *d_stamps = nullptr;  // phase end times of the last run's first phases
   unsigned long long barrier_limit_ns = 4000000000ull;
   unsigned int barrier_extra = 0;
   int persist_grid = 0;
@@ -2966,6 +3024,17 @@ int ens_prepare(abl_ensemble *e) {
       g.nx = dims[0];
       g.ny = dims[1];
       g.nz = dims[2];
+      // FP32 cell coordinates where the rounding-error bound of
+      // bin_in_fp32 allows them (the radius prefilter decides the same
+      // neighbours either way; only the FP64 pipe's load changes).
+      g.f32 = 1;
+      for (int d = 0; d < dim; d++) {
+        const double bound = (2.0 * std::fabs(g.lo[d]) * g.inv_cell + 4.0 * dims[d]) *
+                             5.9604644775390625e-8;
+        if (!(bound <= 2.4e-4)) g.f32 = 0;
+      }
+      for (int d = 0; d < 3; d++) g.flo[d] = (float) g.lo[d];
+      g.finv = (float) g.inv_cell;
       g.cell_base = cells;
       cells += (long) g.nx * g.ny * g.nz;
       if (cells > (1L << 30)) return ABL_E_UNSUPPORTED;
@@ -3039,6 +3108,7 @@ int ens_prepare(abl_ensemble *e) {
       V.nz = g.nz;
       for (int d = 0; d < 3; d++) V.lo[d] = g.lo[d];
       V.inv_cell = g.inv_cell;
+      V.cell_f32 = g.f32;
       V.radius = sd.radius(e->globals.data() + (size_t) r * m->globals_size);
       V.n = nt.counts.empty() ? 0 : nt.counts[r];
       V.cell_start = nt.cell_start + g.cell_base;
@@ -3210,6 +3280,9 @@ int ens_capture(abl_ensemble *e, abl_ctx::Graph **out) {
 // timestep, so from the second timestep on the program repeats with period
 // two; the first may differ (types that are binned once and never stepped).
 
+// Phase end times a persistent run records (block 0, after each barrier).
+constexpr int kPersistStamps = 64;
+
 // The binning of `t` from its current buffer, as ens_launch_bin does it.
 void ens_persist_bin(abl_ensemble *e, EnsType &t, abl::persist_bin &B) {
   std::memset(&B, 0, sizeof B);
@@ -3330,6 +3403,7 @@ int ens_run_persistent(abl_ensemble *e, int timesteps) {
   if (!e->d_prog) {
     ABL_TRY(dev_alloc_t(ctx, &e->d_prog, 1));
     ABL_TRY(dev_alloc_t(ctx, &e->d_sync, 1));
+    ABL_TRY(dev_alloc_t(ctx, &e->d_stamps, kPersistStamps));
   }
   std::unique_ptr<abl::persist_prog> P(new abl::persist_prog());
   const std::vector<int> k0 = ens_graph_key(e);
@@ -3362,6 +3436,10 @@ int ens_run_persistent(abl_ensemble *e, int timesteps) {
   P->limit_ns = e->barrier_limit_ns;
   P->extra_arrivals = e->barrier_extra;
   P->scan_chunk = kScanBlock;
+  P->stamps = e->d_stamps;
+  P->stamp_cap = kPersistStamps;
+  ABL_CUDA_TRY(cudaMemsetAsync(e->d_stamps, 0, sizeof(unsigned long long) * kPersistStamps,
+                               ctx->stream));
   ABL_CUDA_TRY(cudaMemcpyAsync(e->d_prog, P.get(), sizeof(abl::persist_prog),
                                cudaMemcpyHostToDevice, ctx->stream));
   ABL_CUDA_TRY(cudaMemsetAsync(e->d_sync, 0, sizeof(abl::persist_sync), ctx->stream));
@@ -3585,6 +3663,19 @@ int abl_ensemble_persistent_blocks(abl_ensemble *e, int *blocks) {
   return ABL_OK;
 }
 
+int abl_ensemble_phase_times(abl_ensemble *e, double *seconds, int cap, int *count) {
+  if (!e || !count || cap < 0 || (cap > 0 && !seconds)) return ABL_E_INVALID;
+  *count = 0;
+  if (!e->d_stamps) return ABL_OK;
+  unsigned long long st[kPersistStamps];
+  ABL_CUDA_TRY(cudaMemcpy(st, e->d_stamps, sizeof st, cudaMemcpyDeviceToHost));
+  int n = 0;
+  while (n < kPersistStamps && st[n] != 0) n++;
+  for (int k = 0; k + 1 < n && k < cap; k++) seconds[k] = (double) (st[k + 1] - st[k]) * 1e-9;
+  *count = std::max(0, std::min(n - 1, cap));
+  return ABL_OK;
+}
+
 int abl_diag_ensemble_barrier(void *ensemble, double limit_seconds, int extra_arrivals) {
   abl_ensemble *e = (abl_ensemble *) ensemble;
   if (!e || limit_seconds < 0.0 || limit_seconds > 60.0 || extra_arrivals < 0 ||
@@ -3707,7 +3798,8 @@ int abl_ensemble_destroy(abl_ensemble *e) {
   abl_ctx *ctx = &e->base;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ens_drop_graphs(e);
-  for (void *p : ctx->allocations) cudaFree(p);
+  for (void *p : ctx->allocations) cudaFreeAsync(p, ctx->stream);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->allocations.clear();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);

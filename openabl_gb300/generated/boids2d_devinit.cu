@@ -458,8 +458,8 @@ static int abl_main() {
     return 0;
 }
 #else
-__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_STEP_MIN_BLOCKS) abl_kernel_ens_persist(const abl::persist_prog *abl_P, int *abl_err) {
-    abl::persist_run(abl_P, abl_err, [&](const abl_ens_launch &abl_L, long abl_vb, long abl_ts) {
+__global__ void __launch_bounds__(ABL_STEP_BLOCK, ABL_PERSIST_MIN_BLOCKS) abl_kernel_ens_persist(const abl::persist_prog *abl_P, int *abl_err) {
+    abl::persist_run<abl_float, 2>(abl_P, abl_err, [&](const abl_ens_launch &abl_L, long abl_vb, long abl_ts) {
         switch (abl_L.step_index) {
             case 0: abl_ens_body_update_boid(abl_L, abl_vb, abl_ts); break;
             default: break;

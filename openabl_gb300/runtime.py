@@ -433,6 +433,8 @@ class Ensemble:
         L.abl_ensemble_last_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_long)]
         L.abl_ensemble_set_persistent.argtypes = [vp, ctypes.c_int]
         L.abl_ensemble_persistent_blocks.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+        L.abl_ensemble_phase_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                               ctypes.POINTER(ctypes.c_int)]
         L.abl_diag_ensemble_barrier.argtypes = [vp, ctypes.c_double, ctypes.c_int]
         L.abl_ensemble_destroy.argtypes = [vp]
         self.model = model if isinstance(model, Model) else Model(model)
@@ -528,6 +530,14 @@ class Ensemble:
         _check(_load().abl_ensemble_persistent_blocks(self.e, ctypes.byref(c)),
                "abl_ensemble_persistent_blocks")
         return c.value
+
+    def phase_times(self, cap=64):
+        """Durations (s) of the first phases of the last persistent run."""
+        buf = (ctypes.c_double * cap)()
+        n = ctypes.c_int()
+        _check(_load().abl_ensemble_phase_times(self.e, buf, cap, ctypes.byref(n)),
+               "abl_ensemble_phase_times")
+        return list(buf[:n.value])
 
     def inject_barrier_failure(self, limit_seconds, extra_arrivals):
         """Failure injection (abl_diag_ensemble_barrier): barrier waits give up
