@@ -55,6 +55,11 @@ def parse():
                     help="skip the ensemble and precision measurements")
     ap.add_argument("--ensemble-replicas", type=int, default=256)
     ap.add_argument("--ensemble-steps", type=int, default=200)
+    ap.add_argument("--ensemble-only", action="store_true",
+                    help="print only the ensemble measurement, graph replay and persistent, "
+                         "without the replica-by-replica baseline (for profiling)")
+    ap.add_argument("--ensemble-no-autotune", action="store_true",
+                    help="run the ensemble with its default launch configuration")
     ap.add_argument("--serve-jobs", type=int, default=48)
     ap.add_argument("--serve-slots", type=int, default=8)
     return ap.parse_args()
@@ -180,9 +185,10 @@ def measure_ensemble(args, o, W, np):
     states = [{k: v.astype(np.float32) for k, v in s.items()} for s in states]
     total = sum(len(s["pos"]) for s in states)
     T = args.ensemble_steps
+    tune = (lambda e: e.tuning()) if args.ensemble_no_autotune else (lambda e: e.autotune(3))
     ens = o.Ensemble(model, gl, seeds=seeds)
     ens.upload("Boid", states)
-    tuning = ens.autotune(3)
+    tuning = tune(ens)
     ens.run(3)
     ens.upload("Boid", states)
     ens.run(T)
@@ -194,7 +200,7 @@ def measure_ensemble(args, o, W, np):
     pe = o.Ensemble(model, gl, seeds=seeds)
     pe.set_persistent(True)
     pe.upload("Boid", states)
-    p_tuning = pe.autotune(3)
+    p_tuning = tune(pe)
     pe.run(3)
     pe.upload("Boid", states)
     pe.run(T)
@@ -211,6 +217,11 @@ def measure_ensemble(args, o, W, np):
     pe.close()
     base_s = 0.0
     base_launches = 0
+    if getattr(args, "ensemble_only", False):
+        # profiling runs: the ensemble's two ways only, not the replicas one
+        # by one (which would add T x 15 launches per replica)
+        return {"value": total * T / ens_s, "seconds": ens_s, "gpu_launches": launches,
+                "tuning": tuning, "persistent": pers}
     for g, st in zip(gl, states):
         sim = o.Simulation(model, g)
         sim.upload("Boid", st)
@@ -312,6 +323,15 @@ def measure_serving(args, o, W, np):
     srv.close()
     lat = np.array([i["done"] - i["submit"] for i in infos])
     wait = np.array([i["admit"] - i["submit"] for i in infos])
+    # Where the time goes, per model: the jobs' device time in timesteps and
+    # their time in a slot (admission to completion), summed.
+    per_model = {}
+    for (jid, n, steps, m, prec), i in zip(ids, infos):
+        d = per_model.setdefault(m, {"jobs": 0, "agent_steps": 0, "device_s": 0.0, "slot_s": 0.0})
+        d["jobs"] += 1
+        d["agent_steps"] += n * steps
+        d["device_s"] += i["exec_s"]
+        d["slot_s"] += i["done"] - i["admit"]
     first = min(i["submit"] for i in infos)
     last = max(i["done"] for i in infos)
     work = sum(n * steps for _, n, steps, _, _ in ids)
@@ -340,7 +360,8 @@ def measure_serving(args, o, W, np):
             "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p99_s": float(np.percentile(lat, 99)),
             "queue_wait_p50_s": float(np.percentile(wait, 50)),
-            "makespan_s": last - first, "jobs": len(ids), "failed": failed}
+            "makespan_s": last - first, "jobs": len(ids), "failed": failed,
+            "per_model": per_model}
 
 
 def measure_other_workloads(args, o, W, np):
@@ -597,6 +618,10 @@ def run_ours(args):
     import torch
     import openabl_gb300 as o
     import openabl_gb300.workloads as W
+
+    if args.ensemble_only:
+        print(json.dumps({"ensemble": measure_ensemble(args, o, W, np)}))
+        return 0
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
