@@ -258,8 +258,9 @@ int abl_ensemble_destroy(abl_ensemble *e);
  * process.  A server runs submitted simulation jobs concurrently: a job is
  * admitted as soon as one of `slots` workers is free and its estimated
  * device memory fits in what is left of `hbm_budget` (0: 90% of free
- * memory); each running job has its own context and stream, so the work of
- * all running jobs overlaps on the device, and queued jobs start as soon as
+ * memory); each running job has its own context and stream (small jobs of
+ * one model share an ensemble, abl_server_set_batching), so the work of all
+ * running jobs overlaps on the device, and queued jobs start as soon as
  * running ones release their slot and memory.  State stays on the device for
  * the whole job; results are kept in host memory until released. */
 typedef struct abl_server abl_server;
@@ -283,6 +284,14 @@ int abl_server_job_info(abl_server *s, long job_id, int *status, double *times);
 int abl_server_result(abl_server *s, long job_id, int type_id, void *const *cols, size_t *n);
 int abl_server_release(abl_server *s, long job_id);
 int abl_server_stats(abl_server *s, int *queued, int *running, size_t *bytes_in_use);
+/* Batching of small jobs (default: up to 64 jobs of at most 65,536 agents
+ * each): a worker that admits such a job of a model with an ensemble form
+ * also admits the queued small jobs of the same model whose memory fits, and
+ * runs them as the replicas of one ensemble in its slot (one launch per
+ * phase for all of them), each job completing when its own timestep count
+ * is reached.
+ * Results are those of each job run alone.  max_jobs = 1 turns it off. */
+int abl_server_set_batching(abl_server *s, int max_jobs, long max_agents);
 /* Runs the queued jobs to completion, then stops the workers. */
 int abl_server_destroy(abl_server *s);
 

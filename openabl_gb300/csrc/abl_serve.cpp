@@ -10,10 +10,20 @@
 // state stays resident on the device for the whole run; the final population
 // is copied back to host memory owned by the server until released.
 //
+// Small jobs are batched: when a worker admits a job of at most
+// `batch_agents` agents whose model has an ensemble form, it also admits
+// the queued jobs of the same model that are small too (up to
+// `batch_jobs`, each as its memory fits), and runs them as the replicas of
+// one ensemble in one slot: each phase of a timestep is one launch for all
+// of them instead of one per job.  The ensemble runs to each job's
+// timestep count in turn; a job's result is read back and the job
+// completes when its count is reached.
+//
 // Each job keeps its submit, admission and completion times (steady clock)
 // and the device time of its timesteps, so callers can report latency
 // percentiles next to aggregate throughput.  A job computes exactly what the
-// same job computes alone: contexts share nothing but the device.
+// same job computes alone: contexts share nothing but the device, and an
+// ensemble replica's results equal its own context's bit for bit.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -58,6 +68,8 @@ struct abl_server {
   int device = 0;
   size_t budget = 0, in_use = 0;
   int slots = 0, running = 0;
+  int batch_jobs = 64;       // replicas of one batch (1: no batching)
+  long batch_agents = 65536; // largest job (agents of all types) that is batched
   bool stop = false;
   long next_id = 1;
   std::mutex mu;
@@ -128,6 +140,112 @@ void run_job(abl_server *S, const std::shared_ptr<Job> &job) {
   S->done_cv.notify_all();
 }
 
+// Every step function has an ensemble form and there is no sequential step.
+bool batchable(const abl_model_desc *m) {
+  if (m->seq_step || m->num_steps == 0) return false;
+  for (int k = 0; k < m->num_steps; k++)
+    if (!m->steps[k].launch_ens) return false;
+  return true;
+}
+
+long job_agents(const Job &j) {
+  long n = 0;
+  for (size_t c : j.counts) n += (long) c;
+  return n;
+}
+
+// Runs `jobs` (one model, all admitted) as the replicas of one ensemble.
+void run_batch(abl_server *S, const std::vector<std::shared_ptr<Job>> &jobs) {
+  const abl_model_desc *m = jobs[0]->model;
+  const int R = (int) jobs.size();
+  size_t reserve = 0;
+  std::vector<unsigned char> globals;
+  std::vector<uint64_t> seeds;
+  for (auto &j : jobs) {
+    reserve += j->reserve;
+    globals.insert(globals.end(), j->globals.begin(), j->globals.end());
+    seeds.push_back(j->seed);
+  }
+  // Per-phase launches (graph replay), not the persistent kernel: a
+  // persistent launch holds every SM for its whole run, so the kernels of
+  // the other running jobs could not interleave with it.
+  abl_ensemble *e = nullptr;
+  int r = abl_ensemble_create(m, R, globals.data(), seeds.data(), reserve, &e);
+  for (int t = 0; r == ABL_OK && t < m->num_agent_types; t++) {
+    std::vector<size_t> counts(R);
+    std::vector<std::vector<unsigned char>> cat(m->agents[t].num_members);
+    for (int q = 0; q < R; q++) {
+      counts[q] = jobs[q]->counts[t];
+      for (int k = 0; k < m->agents[t].num_members; k++) {
+        const auto &c = jobs[q]->cols[t][k];
+        cat[k].insert(cat[k].end(), c.begin(), c.end());
+      }
+    }
+    std::vector<const void *> cols;
+    for (auto &c : cat) cols.push_back(c.data());
+    r = abl_ensemble_upload(e, t, counts.data(), cols.data());
+  }
+  // Segments: up to each distinct timestep count in turn.
+  std::vector<int> order(R);
+  for (int q = 0; q < R; q++) order[q] = q;
+  std::sort(order.begin(), order.end(),
+            [&](int a, int b) { return jobs[a]->timesteps < jobs[b]->timesteps; });
+  int done = 0;
+  double exec = 0;
+  size_t pos = 0;
+  while (pos < order.size()) {
+    const int target = jobs[order[pos]]->timesteps;
+    if (r == ABL_OK && target > done) {
+      r = abl_ensemble_run(e, target - done);
+      double seg = 0;
+      if (r == ABL_OK) abl_ensemble_last_exec_time(e, &seg);
+      exec += seg;
+      done = target;
+    }
+    // Read back every replica, keep those finishing here.
+    for (int t = 0; r == ABL_OK && t < m->num_agent_types; t++) {
+      std::vector<size_t> counts(R);
+      r = abl_ensemble_download(e, t, counts.data(), nullptr);
+      if (r != ABL_OK) break;
+      size_t total = 0;
+      for (size_t c : counts) total += c;
+      std::vector<std::vector<unsigned char>> cat(m->agents[t].num_members);
+      std::vector<void *> cols;
+      for (int k = 0; k < m->agents[t].num_members; k++) {
+        cat[k].resize(std::max<size_t>(1, total * member_size(m->agents[t].members[k])));
+        cols.push_back(cat[k].data());
+      }
+      r = abl_ensemble_download(e, t, nullptr, cols.data());
+      size_t base = 0;
+      for (int q = 0; r == ABL_OK && q < R; q++) {
+        if (jobs[q]->timesteps == target) {
+          jobs[q]->counts[t] = counts[q];
+          for (int k = 0; k < m->agents[t].num_members; k++) {
+            const size_t b = member_size(m->agents[t].members[k]);
+            auto &dst = jobs[q]->cols[t][k];
+            dst.assign(cat[k].begin() + base * b, cat[k].begin() + (base + counts[q]) * b);
+          }
+        }
+        base += counts[q];
+      }
+    }
+    std::lock_guard<std::mutex> lock(S->mu);
+    for (; pos < order.size() && jobs[order[pos]]->timesteps == target; pos++) {
+      Job &j = *jobs[order[pos]];
+      j.exec_s = exec;
+      j.t_done = now_s();
+      j.status = r == ABL_OK ? 2 : r;
+    }
+    S->done_cv.notify_all();
+  }
+  if (e) abl_ensemble_destroy(e);
+  std::lock_guard<std::mutex> lock(S->mu);
+  S->in_use -= reserve;
+  S->running--;
+  S->cv.notify_all();
+  S->done_cv.notify_all();
+}
+
 void worker(abl_server *S) {
   cudaSetDevice(S->device);
   for (;;) {
@@ -148,6 +266,30 @@ void worker(abl_server *S) {
       S->running++;
       job->status = 1;
       job->t_admit = now_s();
+      if (S->batch_jobs > 1 && job_agents(*job) <= S->batch_agents && batchable(job->model)) {
+        // Admit the small queued jobs of the same model with it, in queue
+        // order, as long as their memory fits.
+        std::vector<std::shared_ptr<Job>> batch{job};
+        for (auto it = S->queue.begin();
+             it != S->queue.end() && (int) batch.size() < S->batch_jobs;) {
+          Job &q = **it;
+          if (q.model == job->model && job_agents(q) <= S->batch_agents &&
+              S->in_use + q.reserve <= S->budget) {
+            S->in_use += q.reserve;
+            q.status = 1;
+            q.t_admit = job->t_admit;
+            batch.push_back(*it);
+            it = S->queue.erase(it);
+          } else {
+            ++it;
+          }
+        }
+        if (batch.size() > 1) {
+          lock.unlock();
+          run_batch(S, batch);
+          continue;
+        }
+      }
     }
     run_job(S, job);
   }
@@ -263,6 +405,14 @@ int abl_server_release(abl_server *S, long job_id) {
   if (it == S->jobs.end()) return ABL_E_INVALID;
   if (it->second->status == 0 || it->second->status == 1) return ABL_E_INVALID;
   S->jobs.erase(it);
+  return ABL_OK;
+}
+
+int abl_server_set_batching(abl_server *S, int max_jobs, long max_agents) {
+  if (!S || max_jobs < 1 || max_agents < 0) return ABL_E_INVALID;
+  std::lock_guard<std::mutex> lock(S->mu);
+  S->batch_jobs = max_jobs;
+  S->batch_agents = max_agents;
   return ABL_OK;
 }
 

@@ -582,9 +582,16 @@ class Server:
                                        ctypes.POINTER(ctypes.c_int),
                                        ctypes.POINTER(ctypes.c_size_t)]
         L.abl_server_destroy.argtypes = [vp]
+        L.abl_server_set_batching.argtypes = [vp, ctypes.c_int, ctypes.c_long]
         self.s = ctypes.c_void_p()
         _check(L.abl_server_create(slots, hbm_budget, ctypes.byref(self.s)), "abl_server_create")
         self.models = {}
+
+    def set_batching(self, max_jobs=64, max_agents=65536):
+        """Small jobs of one model run as the replicas of one ensemble
+        (max_jobs=1: off)."""
+        _check(_load().abl_server_set_batching(self.s, int(max_jobs), int(max_agents)),
+               "abl_server_set_batching")
 
     def submit(self, model, globals_, state, timesteps, seed=0):
         """`state`: {type name: {member: array}}; returns the job id."""
