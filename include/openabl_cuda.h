@@ -238,7 +238,10 @@ int abl_ensemble_last_launch_count(abl_ensemble *e, long *launches);
  * cooperative kernel launch of as many blocks as the device holds at once,
  * the phases separated by grid-wide barriers.  Each barrier wait gives up
  * after a time limit (4 s by default), and the run then returns
- * ABL_E_TIMEOUT.  Results equal those of the per-phase launches bit for bit.
+ * ABL_E_TIMEOUT; the replicas' state is then undefined until the next
+ * abl_ensemble_upload.  Results equal those of the per-phase launches bit
+ * for bit.  The launch holds every SM until the run ends, so work on other
+ * streams waits for it.
  * ABL_E_UNSUPPORTED for models without an ensemble form.  The replicas'
  * timestep pattern must repeat with period two after the first (every model
  * whose steps all run each timestep does). */

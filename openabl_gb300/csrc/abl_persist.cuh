@@ -50,7 +50,7 @@ enum { kPersistBin = 0, kPersistStep = 1 };
 #define ABL_PERSIST_ILP 4
 #endif
 constexpr int kPersistILP = ABL_PERSIST_ILP;
-constexpr int kPersistMaxOps = 8;     // ops (binnings + step functions) per timestep
+constexpr int kPersistMaxOps = 16;    // ops (binnings + step functions) per timestep
 constexpr int kPersistMaxLevels = 3;  // list levels (3D ordered lists)
 
 // Binning of one agent type over all replicas.

@@ -103,7 +103,9 @@ size_t estimate_bytes(const abl_model_desc *m, const std::vector<size_t> &counts
   return total;
 }
 
-void run_job(abl_server *S, const std::shared_ptr<Job> &job) {
+// Runs one job in a context of its own: its results replace its columns,
+// *exec receives the device time of its timesteps.  Returns the status.
+int run_alone(Job *job, double *exec) {
   abl_ctx *ctx = nullptr;
   int r = abl_create(job->model, job->reserve, &ctx);
   if (r == ABL_OK) r = abl_set_globals(ctx, job->globals.data(), job->globals.size());
@@ -114,8 +116,8 @@ void run_job(abl_server *S, const std::shared_ptr<Job> &job) {
     r = abl_upload(ctx, t, cols.data(), job->counts[t]);
   }
   if (r == ABL_OK) r = abl_run(ctx, job->timesteps);
-  double exec = 0;
-  if (r == ABL_OK) abl_last_exec_time(ctx, &exec);
+  *exec = 0;
+  if (r == ABL_OK) abl_last_exec_time(ctx, exec);
   for (int t = 0; r == ABL_OK && t < job->model->num_agent_types; t++) {
     size_t n = 0;
     r = abl_count(ctx, t, &n);
@@ -130,6 +132,12 @@ void run_job(abl_server *S, const std::shared_ptr<Job> &job) {
     job->counts[t] = n;
   }
   if (ctx) abl_destroy(ctx);
+  return r;
+}
+
+void run_job(abl_server *S, const std::shared_ptr<Job> &job) {
+  double exec = 0;
+  const int r = run_alone(job.get(), &exec);
   std::lock_guard<std::mutex> lock(S->mu);
   job->exec_s = exec;
   job->t_done = now_s();
@@ -184,6 +192,26 @@ void run_batch(abl_server *S, const std::vector<std::shared_ptr<Job>> &jobs) {
     std::vector<const void *> cols;
     for (auto &c : cat) cols.push_back(c.data());
     r = abl_ensemble_upload(e, t, counts.data(), cols.data());
+  }
+  if (r != ABL_OK) {
+    // The ensemble could not be set up (e.g. its memory): the jobs run one
+    // after another in this slot instead, each alone.
+    if (e) abl_ensemble_destroy(e);
+    for (auto &j : jobs) {
+      double exec = 0;
+      const int rj = run_alone(j.get(), &exec);
+      std::lock_guard<std::mutex> lock(S->mu);
+      j->exec_s = exec;
+      j->t_done = now_s();
+      j->status = rj == ABL_OK ? 2 : rj;
+      S->done_cv.notify_all();
+    }
+    std::lock_guard<std::mutex> lock(S->mu);
+    S->in_use -= reserve;
+    S->running--;
+    S->cv.notify_all();
+    S->done_cv.notify_all();
+    return;
   }
   // Segments: up to each distinct timestep count in turn.
   std::vector<int> order(R);
