@@ -45,9 +45,11 @@ enum { kPersistBin = 0, kPersistStep = 1 };
 // Items a thread of the persistent kernel takes at a time in the gathering
 // phases, loads first: the binning phases run at the step phase's
 // occupancy, so each thread keeps more loads in flight than in the
-// per-phase kernels.
+// per-phase kernels.  (Two: four spill more registers in the step phase;
+// 200 timesteps of the 256-replica FP32 boids2d ensemble took 1.65 s with
+// two, 1.67 s with four.)
 #ifndef ABL_PERSIST_ILP
-#define ABL_PERSIST_ILP 4
+#define ABL_PERSIST_ILP 2
 #endif
 constexpr int kPersistILP = ABL_PERSIST_ILP;
 constexpr int kPersistMaxOps = 16;    // ops (binnings + step functions) per timestep
@@ -277,20 +279,31 @@ __device__ __forceinline__ void copy_words(void *dst, const void *src, size_t by
     ((unsigned long long *) dst)[w] = ((const unsigned long long *) src)[w];
 }
 
-// State of one block's walk through the run: the barrier's arrivals and
-// limit, and (block 0, thread 0) the phase timestamps.
+// State of one block's walk through the run.  Its position (timestep, op,
+// virtual block, the phase timestamps taken) lives in shared memory and is
+// written by thread 0 between barriers, so that across a step body nothing
+// is live but kernel parameters and shared memory, and the body keeps the
+// registers to itself.
+struct persist_cursor {
+  long it;                       // timestep of the run
+  long ts;                       // its number (random() keys on it)
+  long nvb, vb;                  // step phase: virtual blocks, the one to run
+  unsigned long long work_base;  // the counter's value where this phase's share starts
+  int o;                         // op of the timestep
+  int nstamps;                   // phase timestamps taken (block 0)
+};
+
 struct persist_walk {
-  const persist_prog &P;
-  unsigned int expected;
+  const persist_prog *P;
   int *error;
   int *stage;
-  int nstamps;
+  persist_cursor *C;
 
   // Grid barrier; block 0 then records when the phase ended.
   __device__ bool sync() {
-    if (!grid_barrier(P.sync, expected, P.limit_ns)) return false;
-    if (P.stamps && blockIdx.x == 0 && threadIdx.x == 0 && nstamps < P.stamp_cap)
-      P.stamps[nstamps++] = global_ns();
+    if (!grid_barrier(P->sync, gridDim.x + P->extra_arrivals, P->limit_ns)) return false;
+    if (P->stamps && blockIdx.x == 0 && threadIdx.x == 0 && C->nstamps < P->stamp_cap)
+      P->stamps[C->nstamps++] = global_ns();
     return true;
   }
 };
@@ -476,7 +489,7 @@ __device__ inline void persist_merge_dispatch(const persist_bin &B, const ablbin
 // The binning of one type: returns false when a barrier gave up.
 template <typename Real, int DIM>
 __device__ inline bool persist_binning(persist_walk &W, const persist_bin &B) {
-  const int chunk = W.P.scan_chunk;
+  const int chunk = W.P->scan_chunk;
   // assign
   const float m = assign_any<Real, DIM>(B, W.error);
   ablbin::fold_amax(m, B.amax_acc);
@@ -522,24 +535,23 @@ __device__ inline bool persist_binning(persist_walk &W, const persist_bin &B) {
 // (non-finite positions).  Real and DIM: see assign_any.
 template <typename Real, int DIM, typename Body>
 __device__ void persist_run(const persist_prog *Pp, int *error, Body &&body) {
-  const persist_prog &P = *Pp;
   extern __shared__ int abl_presort_dyn[];
   // The step's launch block and the binning's arguments, copied to shared
   // memory for each op: read at shared-memory latency.
   __shared__ abl_ens_launch Ls;
   __shared__ persist_bin Bs;
+  __shared__ persist_cursor C;
   // List staging shares the step's dynamic shared memory.
-  persist_walk W{P, gridDim.x + P.extra_arrivals, error, abl_presort_dyn, 0};
-  // Step phases hand out virtual blocks dynamically, as the hardware hands
-  // out the blocks of a kernel: agents' neighbour counts vary, so a fixed
-  // share per block would finish unevenly.  Every block takes one block
-  // index past the end of each phase, so each phase's share starts
-  // nvb + gridDim.x after the last one's.
-  __shared__ long vb_next;
-  unsigned long long work_base = 0;
+  persist_walk W{Pp, error, abl_presort_dyn, &C};
+  if (threadIdx.x == 0) {
+    C.it = 0;
+    C.o = 0;
+    C.work_base = 0;
+    C.nstamps = 0;
+  }
   // Cell counts and coordinate maxima start at zero.
   for (int k = 0; k < 3; k++) {
-    const persist_timestep &T = P.ts[k];
+    const persist_timestep &T = Pp->ts[k];
     for (int o = 0; o < T.nops; o++) {
       const persist_op &op = T.ops[o];
       if (op.kind != kPersistBin) continue;
@@ -548,32 +560,45 @@ __device__ void persist_run(const persist_prog *Pp, int *error, Body &&body) {
     }
   }
   if (!W.sync()) return;
-  for (long it = 0; it < P.timesteps; it++) {
-    const int k = P.first_special ? (it == 0 ? 0 : 1 + (int) ((it - 1) & 1)) : (int) (it & 1);
-    const persist_timestep &T = P.ts[k];
-    const long ts = P.base_timestep + it;
-    for (int o = 0; o < T.nops; o++) {
-      const persist_op &op = T.ops[o];
-      if (op.kind == kPersistBin) {
-        copy_words(&Bs, &op.bin, sizeof(persist_bin));
-        __syncthreads();
-        if (!persist_binning<Real, DIM>(W, Bs)) return;
-        continue;
-      }
-      copy_words(&Ls, &op.step, sizeof(abl_ens_launch));
+  for (;;) {
+    const long it = C.it;
+    if (it >= Pp->timesteps) break;
+    const int k = Pp->first_special ? (it == 0 ? 0 : 1 + (int) ((it - 1) & 1)) : (int) (it & 1);
+    const persist_timestep &T = Pp->ts[k];
+    const persist_op &op = T.ops[C.o];
+    if (op.kind == kPersistBin) {
+      copy_words(&Bs, &op.bin, sizeof(persist_bin));
       __syncthreads();
-      const long nvb = (Ls.n + blockDim.x - 1) / blockDim.x;
-      for (;;) {
-        if (threadIdx.x == 0) vb_next = (long) (atomicAdd(&P.sync->work, 1ull) - work_base);
-        __syncthreads();
-        const long vb = vb_next;
-        if (vb >= nvb) break;  // uniform over the block
-        body(Ls, vb, ts);
-        __syncthreads();  // shared memory is reused by the next virtual block
+      if (!persist_binning<Real, DIM>(W, Bs)) return;
+    } else {
+      // Step phases hand out virtual blocks dynamically, as the hardware
+      // hands out a kernel's blocks (agents' neighbour counts vary, so fixed
+      // shares would finish unevenly).  A block claims its next virtual
+      // block while it runs the current one.  Every block makes one claim
+      // past the end, so the next phase's share starts nvb + gridDim.x on.
+      copy_words(&Ls, &op.step, sizeof(abl_ens_launch));
+      if (threadIdx.x == 0) {
+        C.ts = Pp->base_timestep + it;
+        C.nvb = (op.step.n + blockDim.x - 1) / blockDim.x;
+        C.vb = (long) (atomicAdd(&Pp->sync->work, 1ull) - C.work_base);
       }
-      work_base += (unsigned long long) nvb + gridDim.x;
+      __syncthreads();
+      while (C.vb < C.nvb) {  // uniform over the block
+        unsigned long long next = 0;
+        if (threadIdx.x == 0) next = atomicAdd(&Pp->sync->work, 1ull);
+        body(Ls, C.vb, C.ts);
+        __syncthreads();  // shared memory is reused by the next virtual block
+        if (threadIdx.x == 0) C.vb = (long) (next - C.work_base);
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) C.work_base += (unsigned long long) C.nvb + gridDim.x;
       if (!W.sync()) return;
     }
+    if (threadIdx.x == 0 && ++C.o >= T.nops) {
+      C.o = 0;
+      C.it++;
+    }
+    __syncthreads();
   }
 }
 

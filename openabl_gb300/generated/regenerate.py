@@ -44,6 +44,8 @@ MODELS = {
     "boids2d_devinit": ("boids2d.abl", {"cuda.device_init": "true"}),
     # a model of this repository's tests: constant arrays
     "kinds": ("tests/models/kinds.abl", {}),
+    # a model of this repository's tests: a neighbour type no step changes
+    "grazers": ("tests/models/grazers.abl", {}),
     # random() inside steps: runs are reproducible, the reference's are not
     "ants": ("ants.abl", {}),
     "boids2d_flockers": ("boids2d_flockers.abl", {}),

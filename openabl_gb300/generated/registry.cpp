@@ -17,6 +17,7 @@ const abl_model_desc *abl_model_desc_boids3d_mixed(void);
 const abl_model_desc *abl_model_desc_sugarscape(void);
 const abl_model_desc *abl_model_desc_boids2d_devinit(void);
 const abl_model_desc *abl_model_desc_kinds(void);
+const abl_model_desc *abl_model_desc_grazers(void);
 const abl_model_desc *abl_model_desc_ants(void);
 const abl_model_desc *abl_model_desc_boids2d_flockers(void);
 const abl_model_desc *abl_model_desc_keratinocyte(void);
@@ -37,6 +38,7 @@ const abl_model_desc *const abl_builtin_models[] = {
     abl_model_desc_sugarscape(),
     abl_model_desc_boids2d_devinit(),
     abl_model_desc_kinds(),
+    abl_model_desc_grazers(),
     abl_model_desc_ants(),
     abl_model_desc_boids2d_flockers(),
     abl_model_desc_keratinocyte(),

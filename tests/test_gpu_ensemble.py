@@ -208,3 +208,47 @@ def test_persistent_barrier_wait_runs_out_and_context_stays_usable():
         for k in want:
             assert np.array_equal(got[r][k], want[k]), (r, k)
     ens.close()
+
+
+def _grazer_replicas(sizes, seed=6):
+    model = o.Model("grazers")
+    g = model.default_globals()
+    W = float(g.get("W"))
+    rng = np.random.Generator(np.random.PCG64(seed))
+    states = []
+    for n in sizes:
+        ang = rng.uniform(0, 2 * np.pi, n)
+        states.append({
+            "Grazer": {"pos": rng.uniform(0, W, (n, 2)), "dir": np.stack([np.cos(ang), np.sin(ang)], 1),
+                       "fed": np.zeros(n)},
+            "Patch": {"pos": rng.uniform(0, W, (2 * n, 2)), "grass": rng.uniform(0, 1, 2 * n)}})
+    return model, [g] * len(sizes), states
+
+
+@pytest.mark.parametrize("persistent", [False, True])
+def test_unstepped_neighbour_type(persistent):
+    """A neighbour type that no step changes is binned in the first timestep
+    only, so the first timestep's program differs from the later ones (the
+    persistent kernel runs ts[0] once, then ts[1], ts[2] in turn); every
+    replica gets the bits of its own context."""
+    model, gl, states = _grazer_replicas([1500, 600, 2400])
+    ens = o.Ensemble(model, gl, seeds=[1, 2, 3])
+    ens.set_persistent(persistent)
+    for tname in ("Grazer", "Patch"):
+        ens.upload(tname, [s[tname] for s in states])
+    ens.run(7)
+    if persistent:
+        assert ens.last_launch_count() == 1
+    got = {t: ens.download(t) for t in ("Grazer", "Patch")}
+    ens.close()
+    for r, st in enumerate(states):
+        sim = o.Simulation(model, gl[r])
+        sim.set_seed(r + 1)
+        for tname in ("Grazer", "Patch"):
+            sim.upload(tname, st[tname])
+        sim.run(7)
+        for tname in ("Grazer", "Patch"):
+            want = sim.download(tname)
+            for k in want:
+                assert np.array_equal(got[tname][r][k], want[k]), (persistent, r, tname, k)
+        sim.close()
