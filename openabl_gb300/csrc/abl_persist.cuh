@@ -32,9 +32,9 @@
 
 // Resident blocks per SM the persistent kernel's register allocation must
 // allow (its step phase is the step kernel's body).
-// Five blocks of 128 threads leave 96 registers a thread: the kernel holds
-// its walk through the run beside the step body (measured on the 256-replica
-// FP32 boids2d ensemble: 1.93 s with six blocks and spills, 1.77 s with five).
+// Five blocks of 128 threads leave 96 registers a thread; with six (80) the
+// step body spills (measured on 200 timesteps of the 256-replica FP32
+// boids2d ensemble: 1.67 s with five blocks, 1.82 s with six).
 #ifndef ABL_PERSIST_MIN_BLOCKS
 #define ABL_PERSIST_MIN_BLOCKS 5
 #endif
