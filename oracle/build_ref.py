@@ -62,6 +62,9 @@ PROGRAMS = {
     # a model of this repository's tests (constant arrays, a member written
     # on one branch only)
     "kinds": ("tests/models/kinds", {}),
+    # a model of this repository's tests: a near loop over another agent
+    # type whose agents no step changes
+    "grazers": ("tests/models/grazers", {}),
     # random() inside the step: run on one OpenMP thread, so its draws come
     # from the xorshift stream in agent order (SERIAL_RANDOM)
     "boids2d_flockers": ("boids2d_flockers", {}),
