@@ -136,9 +136,10 @@ typedef int (*abl_ens_launch_fn)(const abl_ens_launch *launch, cudaStream_t stre
 /* Persistent ensemble kernel: runs the program `prog` (device memory, an
  * abl::persist_prog of abl_persist.cuh) in one cooperative launch of as many
  * blocks of `block` threads as are co-resident on the device with `smem`
- * bytes of dynamic shared memory each; *grid receives that block count.
- * With prog == NULL it only computes *grid.  `error` is the device error
- * word for non-finite positions. */
+ * bytes of dynamic shared memory each, or *grid blocks when that is
+ * positive and fewer; *grid receives the block count.  With prog == NULL it
+ * only computes *grid.  `error` is the device error word for non-finite
+ * positions. */
 typedef int (*abl_persist_launch_fn)(const void *prog, int *error, int block, size_t smem,
                                      int *grid, cudaStream_t stream);
 typedef double (*abl_globals_fn)(const void *globals);

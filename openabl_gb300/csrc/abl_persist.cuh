@@ -603,9 +603,10 @@ __device__ void persist_run(const persist_prog *Pp, int *error, Body &&body) {
 }
 
 // Host side of abl_persist_launch_fn for a model's persistent kernel: the
-// grid is every block that can be resident at once (a cooperative launch
-// refuses more), so a grid barrier never waits on a block that has not
-// started.
+// grid is at most every block that can be resident at once (a cooperative
+// launch refuses more), so a grid barrier never waits on a block that has
+// not started; *grid > 0 on entry caps it (small ensembles: fewer blocks to
+// synchronise at every barrier).
 inline int persist_launch(const void *kernel, const void *prog, int *err, int block, size_t smem,
                           int *grid, cudaStream_t stream) {
   if (smem > 48 * 1024 &&
@@ -620,7 +621,8 @@ inline int persist_launch(const void *kernel, const void *prog, int *err, int bl
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess)
     return ABL_E_CUDA;
   if (!coop || per_sm < 1) return ABL_E_UNSUPPORTED;
-  const int g = per_sm * sms;
+  int g = per_sm * sms;
+  if (grid && *grid > 0 && *grid < g) g = *grid;
   if (grid) *grid = g;
   if (!prog) return ABL_OK;
   void *args[2] = {(void *) &prog, (void *) &err};

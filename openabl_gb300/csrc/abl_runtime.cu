@@ -3443,6 +3443,15 @@ int ens_run_persistent(abl_ensemble *e, int timesteps) {
   ABL_CUDA_TRY(cudaMemcpyAsync(e->d_prog, P.get(), sizeof(abl::persist_prog),
                                cudaMemcpyHostToDevice, ctx->stream));
   ABL_CUDA_TRY(cudaMemsetAsync(e->d_sync, 0, sizeof(abl::persist_sync), ctx->stream));
+  // Enough blocks for the largest step phase's virtual blocks, at least one
+  // per SM (the binning phases stride over agents and cells).
+  long most = 0;
+  for (const EnsType &t : e->types) most = std::max(most, t.n);
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e->persist_grid = (int) std::min<long>(1L << 30, std::max<long>(std::max(sms, 1),
+                                                                   blocks_for(most, e->block)));
   ABL_TRY(m->launch_ens_persist(e->d_prog, ctx->error, e->block, smem, &e->persist_grid,
                                 ctx->stream));
   ctx->launches++;
