@@ -1264,13 +1264,20 @@ void launch_gather(abl_ctx *ctx, TypeState &t, int dim, bool with_pos) {
 // n the cells along the axis.  Points outside clamp into border cells, which
 // keeps them in order.  FP32 is used when that bound is below 2.4e-4, half
 // the allowance; queries that compute their cell in FP64 stay consistent.
-bool bin_in_fp32(const TypeState &t, int dim) {
-  const int dims[3] = {t.nx, t.ny, t.nz};
+// Whether a grid (origin lo, 1 / cell size, cells per axis) may compute cell
+// coordinates in FP32: the bound on the FP32 rounding error, (2|lo|/w +
+// 4n) 2^-24 cell widths, stays within half the cells' 2^-10 margin.
+bool fp32_cells_ok(const double *lo, double inv_cell, const int *dims, int dim) {
   for (int d = 0; d < dim; d++) {
-    const double bound = (2.0 * std::fabs(t.lo[d]) * t.inv_cell + 4.0 * dims[d]) * 5.9604644775390625e-8;
+    const double bound = (2.0 * std::fabs(lo[d]) * inv_cell + 4.0 * dims[d]) * 5.9604644775390625e-8;
     if (!(bound <= 2.4e-4)) return false;
   }
   return true;
+}
+
+bool bin_in_fp32(const TypeState &t, int dim) {
+  const int dims[3] = {t.nx, t.ny, t.nz};
+  return fp32_cells_ok(t.lo, t.inv_cell, dims, dim);
 }
 
 template <typename Real>
@@ -3024,15 +3031,10 @@ int ens_prepare(abl_ensemble *e) {
       g.nx = dims[0];
       g.ny = dims[1];
       g.nz = dims[2];
-      // FP32 cell coordinates where the rounding-error bound of
-      // bin_in_fp32 allows them (the radius prefilter decides the same
-      // neighbours either way; only the FP64 pipe's load changes).
-      g.f32 = 1;
-      for (int d = 0; d < dim; d++) {
-        const double bound = (2.0 * std::fabs(g.lo[d]) * g.inv_cell + 4.0 * dims[d]) *
-                             5.9604644775390625e-8;
-        if (!(bound <= 2.4e-4)) g.f32 = 0;
-      }
+      // FP32 cell coordinates where the rounding-error bound allows them
+      // (the radius prefilter decides the same neighbours either way; only
+      // the FP64 pipe's load changes).
+      g.f32 = fp32_cells_ok(g.lo, g.inv_cell, dims, dim) ? 1 : 0;
       for (int d = 0; d < 3; d++) g.flo[d] = (float) g.lo[d];
       g.finv = (float) g.inv_cell;
       g.cell_base = cells;
