@@ -178,7 +178,8 @@ def measure_ensemble(args, o, W, np):
     [1e3, 2e5] and steer/match/collision weights within +-20% of the file's,
     one seed each, run as one ensemble (segmented grid, graph replay,
     autotuned launch configuration) against the same replicas run one after
-    another through the plain single-model path."""
+    another through the plain single-model path; and the same ensemble run
+    as one persistent cooperative launch for all its timesteps."""
     model, base = o.globals_for_config("boids2d_float_4096")
     gl, states, seeds = W.boids2d_ensemble(model, base, replicas=args.ensemble_replicas,
                                            n_min=1000, n_max=200000, seed=0)

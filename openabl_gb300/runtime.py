@@ -410,7 +410,9 @@ class Ensemble:
     """Replicas of one model run together (abl_ensemble_* in the C ABI).
 
     `globals_list` holds one Globals block per replica (its parameter point);
-    states are uploaded and downloaded as one list of per-replica dicts."""
+    states are uploaded and downloaded as one list of per-replica dicts.  A
+    run is one launch per phase for all replicas (graph replay), or with
+    set_persistent() one cooperative launch for all its timesteps."""
 
     def __init__(self, model, globals_list, seeds=None, hbm_budget=0):
         L = _load()
